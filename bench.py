@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark: reinitialize_2nd_order node-iterations/s on one GB300, mixed precision vs FP64.
+
+Workload (the 3D flower configuration): octree on [-1,1]^3, levels 5-10, refined where
+|phi_exact| <= 1.2*diag(cell) (refine_levelset_cf with lip = 2.4) around r = 0.5 + 0.1 sin(5 theta)
+sin(4 phi); phi0 = (r - r_s)(0.2 + |x - (0.1,-0.2,0.15)|^2); reinitialize_2nd_order, 50 iterations.
+A step is one 50-iteration reinitialisation of the whole grid; a node-iteration is one node through
+one RK2 pseudo-time iteration. Synthetic data (no dataset); the working set (tables + fields, >1 GB)
+is far larger than L2, so no L2 flush is needed between steps.
+
+Prints one JSON line (rank 0). `--impl reference` times the CPU restatement of the reference loops
+(oracle/, the reference itself needs p4est/PETSc/MPI) on all host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ITERS = 50
+LEVELS = (5, 10)
+LIP = 2.4
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--levels", type=int, nargs=2, default=list(LEVELS))
+    p.add_argument("--iters", type=int, default=ITERS)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--fp64-steps", type=int, default=2)
+    return p.parse_args()
+
+
+def build_grid(levels):
+    import casl_p4est_gb300 as G
+    from casl_p4est_gb300 import shapes
+    f = G.my_p4est_brick_new([1, 1, 1], [-1, -1, -1], [1, 1, 1])
+    f.refine_levelset(shapes.flower([0, 0, 0], 0.5, 0.1, 5, 4), levels[0], levels[1], lip=LIP)
+    f.build_nodes()
+    phi0 = f.sample(shapes.flower([0, 0, 0], 0.5, 0.1, 5, 4, scale=(0.2, (0.1, -0.2, 0.15))))
+    return f, phi0
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_node(kernel):
+    """DRAM bytes per node of one launch, from the committed ncu summary (profiles/), if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_flower3d.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_node:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reinit_sample(f, phi0, iters, nthreads):
+    """The oracle (CPU restatement of reinitialize_2nd_order) on the same grid: `iters` iterations."""
+    import casl_p4est_gb300 as G
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    rec = G.my_p4est_node_neighbors_t(f).get_neighbors()
+    og = O.OracleGrid.from_records(3, rec, f.wall_mask(), [2.0, 2.0, 2.0])
+    phi = phi0.copy()
+    t = time.perf_counter()
+    og.reinitialize(phi, 2, 2, iterations=iters, nthreads=nthreads)
+    return time.perf_counter() - t, og, rec
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    f, phi0 = build_grid(args.levels)
+    N = f.num_nodes
+    cores = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import casl_p4est_gb300 as G
+    rec = G.my_p4est_node_neighbors_t(f).get_neighbors()
+    og = O.OracleGrid.from_records(3, rec, f.wall_mask(), [2.0, 2.0, 2.0])
+    sample_iters = 1
+    phi = phi0.copy()
+    for _ in range(args.warmup):
+        og.reinitialize(phi, 2, 2, iterations=sample_iters, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        phi = phi0.copy()
+        t = time.perf_counter()
+        og.reinitialize(phi, 2, 2, iterations=sample_iters, nthreads=cores)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = N * sample_iters * args.steps / total
+    out = {
+        "impl": "reference", "metric": "reinit node-iters/s (reinitialize_2nd_order, 3D flower octree L5-10)", "value": value,
+        "unit": "node-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"3D flower octree levels {args.levels[0]}-{args.levels[1]}, {N} nodes, reinitialize_2nd_order",
+                   "nodes": N, "sample": f"{sample_iters} iteration(s) of the full grid per step"},
+        "cpu_baseline": {"value": value, "unit": "node-iters/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample_iters} reinit iteration(s) x {N} nodes per step, {cores} threads, CPU restatement of "
+                                   "reinitialize_one_iteration/compute_derivatives (the reference needs p4est/PETSc/MPI)"},
+        "e2e": {"value": value, "unit": "node-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import casl_p4est_gb300 as G
+    from casl_p4est_gb300 import _lib as L
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    t0 = time.perf_counter()
+    f, phi0 = build_grid(args.levels)
+    N = f.num_nodes
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    ngbd.init_neighbors()
+    ls = G.my_p4est_level_set_t(ngbd, precision="mixed")
+    stream = torch.cuda.current_stream()
+    ls.set_stream(stream.cuda_stream)
+    setup_s = time.perf_counter() - t0
+    _, dmin, _ = f.dxyz_min(args.levels[1])
+
+    phi0_d = torch.from_numpy(phi0).cuda()
+    phi_d = torch.empty_like(phi0_d)
+
+    def step(prec):
+        phi_d.copy_(phi0_d)
+        ls.reinitialize_2nd_order(phi_d, args.iters, precision=prec)
+
+    # accuracy of mixed vs FP64 (untimed): band L-infinity and near-interface error
+    step("fp64")
+    ref64 = phi_d.cpu().numpy().copy()
+    step("mixed")
+    mixed = phi_d.cpu().numpy().copy()
+    band = np.abs(ref64) < 3 * dmin
+    band_err = float(np.max(np.abs(mixed[band] - ref64[band])))
+    near = np.abs(ref64) < dmin
+    iface_err = float(np.max(np.abs(mixed[near] - ref64[near])))
+
+    # warm-up and timed region (mixed)
+    for _ in range(args.warmup):
+        step("mixed")
+    lib = L.load()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.lsg_level_set_launch_count(ls.handle)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step("mixed")
+    ev1.record(stream)
+    barrier()
+    launches = lib.lsg_level_set_launch_count(ls.handle) - launches0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_t = torch.tensor([ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    node_iters = N * args.iters * args.steps * world
+    value = node_iters / (ms / 1e3)
+
+    # FP64 GPU path, same workload (fewer steps: it is compute-bound on GB300's FP64 units)
+    step("fp64")
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.fp64_steps):
+        step("fp64")
+    e1.record(stream)
+    barrier()
+    ms64 = e0.elapsed_time(e1)
+    value64 = N * args.iters * args.fp64_steps * world / (ms64 / 1e3)
+
+    # per-kernel timing pass (events around each launch) for the roofline
+    import ctypes as C
+    kms = np.zeros(10)
+    kcnt = np.zeros(10, np.int64)
+    lib.lsg_level_set_kernel_times(ls.handle, kms.ctypes.data_as(L._DP), kcnt.ctypes.data_as(C.POINTER(C.c_int64)), 10, 1)
+    lib.lsg_level_set_enable_kernel_timing(ls.handle, 1)
+    step("mixed")
+    lib.lsg_level_set_kernel_times(ls.handle, kms.ctypes.data_as(L._DP), kcnt.ctypes.data_as(C.POINTER(C.c_int64)), 10, 1)
+    lib.lsg_level_set_enable_kernel_timing(ls.handle, 0)
+    kinds = L.KERNEL_KINDS
+    per_kernel = {kinds[k]: {"ms_total": float(kms[k]), "launches": int(kcnt[k]),
+                             "ms_per_launch": float(kms[k] / kcnt[k]) if kcnt[k] else None} for k in range(10) if kcnt[k]}
+    # algorithmic bytes per node and launch, mixed 3D (w_f = w_d = 4 bytes): table 2D*(4+w_d) = 48 B per
+    # table-reading sweep; dd sweep reads 1 and writes D values; stage sweep reads phi_0, phi_k and D
+    # second derivatives and writes 1; the RK average (3 values) is fused into every second stage.
+    table = 6 * (4 + 4)
+    alg = {"dd32": table + (1 + 3) * 4, "stage32": table + (3 + 3) * 4 + 3 * 4 / 2}
+    peak, peak_kind = measured_peak()
+    dom = max(("dd32", "stage32"), key=lambda k: per_kernel.get(k, {}).get("ms_total", 0))
+    dom_ms = per_kernel[dom]["ms_per_launch"]
+    achieved = alg[dom] * N / (dom_ms / 1e3) / 1e9
+    tpn = profile_traffic_per_node(dom)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tpn * N if tpn is not None else None), "kernel": dom, "peak_source": peak_kind,
+                "alg_bytes_per_node": alg[dom]}
+    iter_bytes = 2 * (alg["dd32"] + table + (3 + 3) * 4) + 3 * 4  # 284 B per node-iteration
+    roofline["per_iteration"] = {"alg_bytes_per_node_iter": iter_bytes, "achieved_GBps": iter_bytes * value / world / 1e9,
+                                 "frac": iter_bytes * value / world / 1e9 / peak}
+
+    # end to end through the public host API: pinned host phi, H2D + reinit + D2H per step
+    host = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(2):
+        host[:] = phi0
+        ls.reinitialize_2nd_order(host, args.iters, precision="mixed")
+    barrier()
+    te = 0.0
+    for _ in range(args.steps):
+        host[:] = phi0
+        t = time.perf_counter()
+        ls.reinitialize_2nd_order(host, args.iters, precision="mixed")
+        te += time.perf_counter() - t
+    te_t = torch.tensor([te], device="cuda")
+    if dist is not None:
+        dist.all_reduce(te_t, op=dist.ReduceOp.MAX)
+    e2e = {"value": N * args.iters * args.steps * world / float(te_t.item()), "unit": "node-iters/s",
+           "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8}
+
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        secs, _, _ = cpu_reinit_sample(f, phi0, 1, cores)
+        cpu = {"value": N / secs, "unit": "node-iters/s", "cores": cores, "kind": "port",
+               "sample": f"1 reinitialize_2nd_order iteration of the same {N}-node grid on {cores} host threads (oracle/, CPU "
+                         "restatement of the reference loops)"}
+
+    if rank == 0:
+        out = {
+            "metric": "reinit node-iters/s on 1 GB300: mixed vs FP64 at stated band Linf error; HBM %",
+            "value": value, "unit": "node-iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"3D flower octree [-1,1]^3 levels {args.levels[0]}-{args.levels[1]} (lip 2.4), "
+                                   f"{N} nodes, reinitialize_2nd_order {args.iters} iterations, mixed FP32/FP64",
+                       "nodes": N, "iterations": args.iters, "precision": "mixed",
+                       "l2": "working set > L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "single GPU"},
+            "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
+            "speedup_mixed_vs_fp64": value / value64,
+            "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
+            "dx_min": dmin,
+            "roofline": roofline, "kernels": per_kernel,
+            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
+        }
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

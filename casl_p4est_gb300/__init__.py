@@ -1,0 +1,15 @@
+"""casl_p4est_gb300: the level-set hot path of parCASL (UCSB-CASL/casl_p4est) on GB300.
+
+Reinitialisation (reinitialize_2nd_order and its siblings), normal-direction advection and
+semi-Lagrangian node interpolation on quadtree/octree grids, as CUDA kernels for sm_103a behind a
+C ABI (include/lsgpu.h). The Python classes mirror the reference's C++ class API.
+"""
+from . import shapes
+from ._lib import LSG_FP64, LSG_MIXED, LsgError, LsgInvalidArgument, load
+from .forest import Forest, my_p4est_brick_new, my_p4est_node_neighbors_t, qnnn_dtype
+from .level_set import DBL_MAX, my_p4est_level_set_t
+
+__all__ = [
+    "shapes", "load", "LsgError", "LsgInvalidArgument", "LSG_FP64", "LSG_MIXED", "Forest", "my_p4est_brick_new",
+    "my_p4est_node_neighbors_t", "qnnn_dtype", "my_p4est_level_set_t", "DBL_MAX",
+]

@@ -1,0 +1,118 @@
+"""ctypes binding of liblsgpu.so (the C ABI declared in include/lsgpu.h).
+
+The library is loaded from the package's ``_lib`` directory; nothing here falls back to Python
+arithmetic: if the library is missing, importing the bindings raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liblsgpu.so")
+
+LSG_OK, LSG_EINVAL, LSG_ENOMEM, LSG_EDEVICE, LSG_ETIMEOUT, LSG_ENAN, LSG_ESTATE = range(7)
+LSG_FP64, LSG_MIXED = 0, 1
+
+_P = C.c_void_p
+_I = C.c_int
+_I64 = C.c_int64
+_D = C.c_double
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+_I32P = C.POINTER(C.c_int32)
+_U8P = C.POINTER(C.c_uint8)
+
+# name: (restype, argtypes)
+SIGNATURES = {
+    "lsg_last_error": (C.c_char_p, []),
+    "lsg_version": (_I, []),
+    "lsg_forest_create": (_I, [_I, _IP, _DP, _DP, _IP, C.POINTER(_P)]),
+    "lsg_forest_destroy": (_I, [_P]),
+    "lsg_forest_dim": (_I, [_P]),
+    "lsg_forest_num_leaves": (_I64, [_P]),
+    "lsg_forest_leaves": (_I, [_P, _I32P, _I32P, _I32P]),
+    "lsg_forest_refine": (_I, [_P, _U8P, _I64]),
+    "lsg_forest_coarsen": (_I, [_P, _U8P, _I64]),
+    "lsg_forest_tag_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _U8P]),
+    "lsg_forest_refine_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _I]),
+    "lsg_forest_build_nodes": (_I, [_P]),
+    "lsg_forest_num_nodes": (_I64, [_P]),
+    "lsg_forest_node_xyz": (_I, [_P, _DP]),
+    "lsg_forest_nodes": (_I, [_P, _I32P, _I32P]),
+    "lsg_forest_local_nodes": (_I, [_P, _I32P]),
+    "lsg_forest_sample_shape": (_I, [_P, _I, _DP, _I, _DP]),
+    "lsg_qnnn_record_bytes": (C.c_size_t, [_I]),
+    "lsg_forest_export_qnnn": (_I, [_P, _I64, _I64, _P, C.c_size_t]),
+    "lsg_forest_wall_mask": (_I, [_P, _U8P]),
+    "lsg_forest_dxyz_min": (_I, [_P, _DP]),
+    "lsg_level_set_create": (_I, [_P, C.POINTER(_P)]),
+    "lsg_level_set_destroy": (_I, [_P]),
+    "lsg_level_set_set_stream": (_I, [_P, _P]),
+    "lsg_level_set_stream": (_P, [_P]),
+    "lsg_level_set_num_nodes": (_I64, [_P]),
+    "lsg_level_set_zero_distance_threshold": (_D, [_P]),
+    "lsg_reinitialize": (_I, [_P, _DP, _I, _I, _D, _D, _I, _I]),
+    "lsg_reinitialize_device": (_I, [_P, _P, _I, _I, _D, _D, _I, _I]),
+    "lsg_reinit_2nd": (_I, [_P, _DP, _I, _D, _I]),
+    "lsg_advect_in_normal_direction": (_I, [_P, _DP, _DP, _DP, _D, _DP, _I]),
+    "lsg_advect_in_normal_direction_device": (_I, [_P, _P, _P, _P, _D, _P, _I]),
+    "lsg_advect_cfl_dt": (_I, [_P, _DP, _DP]),
+    "lsg_second_derivatives": (_I, [_P, _DP, _DP]),
+    "lsg_second_derivatives_device": (_I, [_P, _P, _P]),
+    "lsg_perturb_level_set_function": (_I, [_P, _DP, _D]),
+    "lsg_level_set_enable_kernel_timing": (_I, [_P, _I]),
+    "lsg_level_set_kernel_times": (_I, [_P, _DP, C.POINTER(_I64), _I, _I]),
+    "lsg_level_set_launch_count": (_I64, [_P]),
+}
+
+KERNEL_KINDS = ["dd64", "prep64", "stage64", "advect64", "dd32", "prep_mixed", "stage32", "advect32", "convert", "copy"]
+
+
+class LsgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[lsgpu status {code}] {msg}")
+        self.code = code
+
+
+class LsgInvalidArgument(LsgError, ValueError):
+    pass
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m casl_p4est_gb300.build`")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> None:
+    if code == LSG_OK:
+        return
+    msg = load().lsg_last_error().decode(errors="replace")
+    if code == LSG_EINVAL:
+        raise LsgInvalidArgument(code, msg)
+    raise LsgError(code, msg)
+
+
+def dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+def i32ptr(a):
+    return a.ctypes.data_as(_I32P)
+
+
+def u8ptr(a):
+    return a.ctypes.data_as(_U8P)

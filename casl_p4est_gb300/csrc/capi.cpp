@@ -1,0 +1,538 @@
+// extern "C" boundary (include/lsgpu.h): argument checks, dimension dispatch and error capture.
+#include <float.h>
+#include <string.h>
+
+#include <exception>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lsgpu.h"
+#include "level_set.hpp"
+#include "shapes.h"
+
+using namespace lsg;
+
+struct lsg_forest {
+  int dim = 2;
+  Forest<2>* f2 = nullptr;
+  Forest<3>* f3 = nullptr;
+  ~lsg_forest() {
+    delete f2;
+    delete f3;
+  }
+};
+
+struct lsg_level_set {
+  int dim = 2;
+  LevelSet<2>* l2 = nullptr;
+  LevelSet<3>* l3 = nullptr;
+  ~lsg_level_set() {
+    delete l2;
+    delete l3;
+  }
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct InvalidArg : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+struct StateError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+template <typename Fn>
+int guard(Fn&& fn) {
+  try {
+    fn();
+    return LSG_OK;
+  } catch (const CudaError& e) {
+    g_last_error = e.what();
+    return LSG_EDEVICE;
+  } catch (const StateError& e) {
+    g_last_error = e.what();
+    return LSG_ESTATE;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "allocation failed";
+    return LSG_ENOMEM;
+  } catch (const std::invalid_argument& e) {
+    g_last_error = e.what();
+    return LSG_EINVAL;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return LSG_EDEVICE;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return LSG_EDEVICE;
+  }
+}
+
+void need(bool cond, const char* msg) {
+  if (!cond) throw InvalidArg(msg);
+}
+
+template <typename Fn>
+void with_forest(const lsg_forest* f, Fn&& fn) {
+  need(f != nullptr, "null forest");
+  if (f->dim == 2)
+    fn(*f->f2);
+  else
+    fn(*f->f3);
+}
+
+template <typename Fn>
+void with_ls(lsg_level_set* ls, Fn&& fn) {
+  need(ls != nullptr, "null level set");
+  if (ls->dim == 2)
+    fn(*ls->l2);
+  else
+    fn(*ls->l3);
+}
+
+template <int D>
+void need_nodes(const Forest<D>& F) {
+  if (!F.nodes_built) throw StateError("the forest's nodes are not built (call lsg_forest_build_nodes)");
+}
+
+// refine_levelset_cf (src/my_p4est_refine_coarsen.cpp:18-90) with refine_only_inside = false.
+template <int D>
+void tag_levelset(const Forest<D>& F, int min_lvl, int max_lvl, double lip, double band_rel, int shape, const double* params,
+                  uint8_t* tags) {
+  using DD = Dim<D>;
+  const size_t nl = F.leaves.size();
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (long long ii = 0; ii < (long long)nl; ++ii) {
+    const Quad& qd = F.leaves[(size_t)ii];
+    uint8_t tag = 0;
+    if (qd.level < min_lvl) {
+      tag = 1;
+    } else if (qd.level >= max_lvl) {
+      tag = 0;
+    } else {
+      const int t = qd.tree;
+      double tmin[3], tmax[3];
+      for (int a = 0; a < 3; ++a) {
+        tmin[a] = F.brick.tmin[3 * t + a];
+        tmax[a] = F.brick.tmax[3 * t + a];
+      }
+      const double dmin = (double)quadrant_len(DD::MAXLEVEL, qd.level) / (double)DD::ROOT_LEN;
+      double dxyz[3];
+      for (int a = 0; a < D; ++a) dxyz[a] = (tmax[a] - tmin[a]) * dmin;
+      double smallest = max2(tmax[0] - tmin[0], tmax[1] - tmin[1]) * ((double)quadrant_len(DD::MAXLEVEL, max_lvl)) / ((double)DD::ROOT_LEN);
+      if (D == 3)
+        smallest = max2(smallest, (tmax[2] - tmin[2]) * ((double)quadrant_len(DD::MAXLEVEL, max_lvl)) / ((double)DD::ROOT_LEN));
+      const double dd = (D == 3) ? sqrt(dxyz[0] * dxyz[0] + dxyz[1] * dxyz[1] + dxyz[2] * dxyz[2])
+                                 : sqrt(dxyz[0] * dxyz[0] + dxyz[1] * dxyz[1]);
+      double xq[3];
+      for (int a = 0; a < D; ++a) xq[a] = (tmax[a] - tmin[a]) * (double)qd.x[a] / (double)DD::ROOT_LEN + tmin[a];
+      const double band = band_rel * smallest;
+      double fv[8];
+      for (int c = 0; c < DD::CHILDREN && !tag; ++c) {
+        double p[3];
+        for (int a = 0; a < D; ++a) p[a] = xq[a] + ((c >> a) & 1) * dxyz[a];
+        fv[c] = shape_eval<D>(shape, params, p);
+        if (fabs(fv[c]) - band <= 0.5 * lip * dd) tag = 1;
+      }
+      if (!tag) {
+        if (D == 3) {
+          if (fv[0] * fv[1] < 0 || fv[0] * fv[2] < 0 || fv[1] * fv[3] < 0 || fv[2] * fv[3] < 0 || fv[3] * fv[4] < 0 ||
+              fv[4] * fv[5] < 0 || fv[5] * fv[6] < 0 || fv[6] * fv[7] < 0)
+            tag = 1;
+        } else {
+          if (fv[0] * fv[1] < 0 || fv[0] * fv[2] < 0 || fv[1] * fv[3] < 0 || fv[2] * fv[3] < 0) tag = 1;
+        }
+      }
+    }
+    tags[ii] = tag;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lsg_last_error(void) { return g_last_error.c_str(); }
+int lsg_version(void) { return 1; }
+
+int lsg_forest_create(int dim, const int n_xyz[3], const double xyz_min[3], const double xyz_max[3], const int periodic[3],
+                      lsg_forest** out) {
+  return guard([&] {
+    need(out != nullptr, "null output pointer");
+    need(dim == 2 || dim == 3, "dim must be 2 or 3");
+    need(n_xyz && xyz_min && xyz_max, "null brick description");
+    lsg_forest* f = new lsg_forest();
+    f->dim = dim;
+    try {
+      if (dim == 2) {
+        f->f2 = new Forest<2>();
+        f->f2->init(n_xyz, xyz_min, xyz_max, periodic);
+      } else {
+        f->f3 = new Forest<3>();
+        f->f3->init(n_xyz, xyz_min, xyz_max, periodic);
+      }
+    } catch (...) {
+      delete f;
+      throw;
+    }
+    *out = f;
+  });
+}
+
+int lsg_forest_destroy(lsg_forest* f) {
+  return guard([&] { delete f; });
+}
+
+int lsg_forest_dim(const lsg_forest* f) { return f ? f->dim : 0; }
+
+int64_t lsg_forest_num_leaves(const lsg_forest* f) {
+  int64_t n = -1;
+  guard([&] { with_forest(f, [&](auto& F) { n = (int64_t)F.num_leaves(); }); });
+  return n;
+}
+
+int lsg_forest_leaves(const lsg_forest* f, int32_t* tree, int32_t* level, int32_t* xyz) {
+  return guard([&] {
+    with_forest(f, [&](auto& F) {
+      for (size_t i = 0; i < F.leaves.size(); ++i) {
+        const Quad& q = F.leaves[i];
+        if (tree) tree[i] = q.tree;
+        if (level) level[i] = q.level;
+        if (xyz)
+          for (int a = 0; a < 3; ++a) xyz[3 * i + a] = q.x[a];
+      }
+    });
+  });
+}
+
+int lsg_forest_refine(lsg_forest* f, const uint8_t* tags, int64_t n) {
+  return guard([&] {
+    with_forest(f, [&](auto& F) {
+      need(tags != nullptr && n == (int64_t)F.num_leaves(), "refine: one tag per leaf required");
+      F.refine(tags);
+    });
+  });
+}
+
+int lsg_forest_coarsen(lsg_forest* f, const uint8_t* tags, int64_t n) {
+  return guard([&] {
+    with_forest(f, [&](auto& F) {
+      need(tags != nullptr && n == (int64_t)F.num_leaves(), "coarsen: one tag per leaf required");
+      F.coarsen(tags);
+    });
+  });
+}
+
+int lsg_forest_tag_levelset(const lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, int shape,
+                            const double* params, int nparams, uint8_t* tags) {
+  return guard([&] {
+    need(params != nullptr && nparams > 0 && tags != nullptr, "tag_levelset: null arguments");
+    need(min_lvl >= 0 && min_lvl <= max_lvl, "tag_levelset: need 0 <= min_lvl <= max_lvl");
+    with_forest(f, [&](auto& F) {
+      using FT = std::decay_t<decltype(F)>;
+      need(max_lvl <= FT::DD::QMAXLEVEL, "tag_levelset: max_lvl above the maximum quadrant level");
+      tag_levelset(F, min_lvl, max_lvl, lip, band, shape, params, tags);
+    });
+  });
+}
+
+int lsg_forest_refine_levelset(lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, int shape,
+                               const double* params, int nparams, int passes) {
+  return guard([&] {
+    need(params != nullptr && nparams > 0, "refine_levelset: null params");
+    need(min_lvl >= 0 && min_lvl <= max_lvl, "refine_levelset: need 0 <= min_lvl <= max_lvl");
+    with_forest(f, [&](auto& F) {
+      using FT = std::decay_t<decltype(F)>;
+      need(max_lvl <= FT::DD::QMAXLEVEL, "refine_levelset: max_lvl above the maximum quadrant level");
+      for (int p = 0; p < passes; ++p) {
+        std::vector<uint8_t> tags(F.num_leaves());
+        tag_levelset(F, min_lvl, max_lvl, lip, band, shape, params, tags.data());
+        bool any = false;
+        for (uint8_t t : tags) any = any || t;
+        if (!any) break;
+        F.refine(tags.data());
+      }
+    });
+  });
+}
+
+int lsg_forest_build_nodes(lsg_forest* f) {
+  return guard([&] { with_forest(f, [&](auto& F) { const_cast<std::decay_t<decltype(F)>&>(F).build_nodes(); }); });
+}
+
+int64_t lsg_forest_num_nodes(const lsg_forest* f) {
+  int64_t n = -1;
+  guard([&] {
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      n = (int64_t)F.num_nodes();
+    });
+  });
+  return n;
+}
+
+int lsg_forest_node_xyz(const lsg_forest* f, double* xyz) {
+  return guard([&] {
+    need(xyz != nullptr, "null output");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      using FT = std::decay_t<decltype(F)>;
+      constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
+#pragma omp parallel for schedule(static)
+      for (long long n = 0; n < (long long)F.num_nodes(); ++n) F.node_xyz((int32_t)n, xyz + (size_t)D * n);
+    });
+  });
+}
+
+int lsg_forest_nodes(const lsg_forest* f, int32_t* tree, int32_t* xyz) {
+  return guard([&] {
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      using FT = std::decay_t<decltype(F)>;
+      constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
+      for (size_t n = 0; n < F.num_nodes(); ++n) {
+        if (tree) tree[n] = F.node_tree[n];
+        if (xyz)
+          for (int a = 0; a < 3; ++a) xyz[3 * n + a] = a < D ? F.node_x[D * n + a] : 0;
+      }
+    });
+  });
+}
+
+int lsg_forest_local_nodes(const lsg_forest* f, int32_t* out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      memcpy(out, F.local_nodes.data(), F.local_nodes.size() * sizeof(int32_t));
+    });
+  });
+}
+
+int lsg_forest_sample_shape(const lsg_forest* f, int shape, const double* params, int nparams, double* out) {
+  return guard([&] {
+    need(params != nullptr && nparams > 0 && out != nullptr, "sample_shape: null arguments");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      using FT = std::decay_t<decltype(F)>;
+      constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
+#pragma omp parallel for schedule(static)
+      for (long long n = 0; n < (long long)F.num_nodes(); ++n) {
+        double x[3] = {0, 0, 0};
+        F.node_xyz((int32_t)n, x);
+        out[n] = shape_eval<D>(shape, params, x);
+      }
+    });
+  });
+}
+
+size_t lsg_qnnn_record_bytes(int dim) { return dim == 2 ? sizeof(Qnnn<2>) : (dim == 3 ? sizeof(Qnnn<3>) : 0); }
+
+int lsg_forest_export_qnnn(const lsg_forest* f, int64_t first, int64_t count, void* out, size_t record_bytes) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      using FT = std::decay_t<decltype(F)>;
+      constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
+      need(record_bytes == sizeof(Qnnn<D>), "export_qnnn: record size mismatch");
+      need(first >= 0 && count >= 0 && first + count <= (int64_t)F.num_nodes(), "export_qnnn: range outside the nodes");
+      Qnnn<D>* rec = static_cast<Qnnn<D>*>(out);
+      int failed = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : failed)
+      for (long long i = 0; i < (long long)count; ++i) {
+        memset(&rec[i], 0, sizeof(Qnnn<D>));
+        if (construct_neighbors<D>(F, (int32_t)(first + i), rec[i])) ++failed;
+      }
+      if (failed) throw std::runtime_error("export_qnnn: incomplete stencil");
+    });
+  });
+}
+
+int lsg_forest_wall_mask(const lsg_forest* f, uint8_t* out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      using FT = std::decay_t<decltype(F)>;
+      constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
+      for (size_t n = 0; n < F.num_nodes(); ++n) out[n] = (uint8_t)wall_mask<D>(F, (int32_t)n);
+    });
+  });
+}
+
+int lsg_forest_dxyz_min(const lsg_forest* f, double* dxyz) {
+  return guard([&] {
+    need(dxyz != nullptr, "null output");
+    with_forest(f, [&](auto& F) { F.dxyz_min(dxyz); });
+  });
+}
+
+int lsg_level_set_create(const lsg_forest* f, lsg_level_set** out) {
+  return guard([&] {
+    need(out != nullptr, "null output pointer");
+    need(f != nullptr, "null forest");
+    lsg_level_set* ls = new lsg_level_set();
+    ls->dim = f->dim;
+    try {
+      if (f->dim == 2) {
+        need_nodes(*f->f2);
+        ls->l2 = new LevelSet<2>(*f->f2);
+      } else {
+        need_nodes(*f->f3);
+        ls->l3 = new LevelSet<3>(*f->f3);
+      }
+    } catch (...) {
+      delete ls;
+      throw;
+    }
+    *out = ls;
+  });
+}
+
+int lsg_level_set_destroy(lsg_level_set* ls) {
+  return guard([&] { delete ls; });
+}
+
+int lsg_level_set_set_stream(lsg_level_set* ls, void* cuda_stream) {
+  return guard([&] { with_ls(ls, [&](auto& L) { L.set_stream((cudaStream_t)cuda_stream); }); });
+}
+
+void* lsg_level_set_stream(const lsg_level_set* ls) {
+  if (!ls) return nullptr;
+  return ls->dim == 2 ? (void*)ls->l2->stream : (void*)ls->l3->stream;
+}
+
+int64_t lsg_level_set_num_nodes(const lsg_level_set* ls) {
+  if (!ls) return -1;
+  return ls->dim == 2 ? ls->l2->N : ls->l3->N;
+}
+
+double lsg_level_set_zero_distance_threshold(const lsg_level_set* ls) {
+  if (!ls) return 0.0;
+  return ls->dim == 2 ? ls->l2->zdt : ls->l3->zdt;
+}
+
+int lsg_reinitialize(lsg_level_set* ls, double* phi, int order_space, int order_pseudotime, double limit_high, double limit_low,
+                     int iterations, int precision) {
+  return guard([&] {
+    need(phi != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) { L.reinitialize_host(phi, order_space, order_pseudotime, limit_high, limit_low, iterations, precision); });
+  });
+}
+
+int lsg_reinitialize_device(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime, double limit_high,
+                            double limit_low, int iterations, int precision) {
+  return guard([&] {
+    need(phi_dev != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) { L.reinitialize(phi_dev, order_space, order_pseudotime, limit_high, limit_low, iterations, precision); });
+  });
+}
+
+int lsg_reinit_2nd(lsg_level_set* ls, double* phi, int iterations, double limit, int precision) {
+  return lsg_reinitialize(ls, phi, 2, 2, limit, -limit, iterations, precision);
+}
+
+int lsg_advect_in_normal_direction_device(lsg_level_set* ls, const double* vn_dev, const double* vn_np1_dev, double* phi_dev,
+                                          double dt, double* phi_dd_dev, int precision) {
+  return guard([&] {
+    need(vn_dev != nullptr && phi_dev != nullptr, "null vn or phi");
+    with_ls(ls, [&](auto& L) { L.advect_normal(vn_dev, vn_np1_dev, phi_dev, dt, phi_dd_dev, precision); });
+  });
+}
+
+int lsg_advect_in_normal_direction(lsg_level_set* ls, const double* vn, const double* vn_np1, double* phi, double dt,
+                                   double* phi_dd, int precision) {
+  return guard([&] {
+    need(vn != nullptr && phi != nullptr, "null vn or phi");
+    with_ls(ls, [&](auto& L) {
+      using LT = std::decay_t<decltype(L)>;
+      constexpr int D = LT::H == 2 ? 2 : 3;
+      const int64_t N = L.N;
+      L.ws_phi.alloc(N);
+      L.ws_vn.alloc(N);
+      if (vn_np1) L.ws_vn1.alloc(N);
+      if (phi_dd) L.ws_dd.alloc((size_t)D * N);
+      cudaStream_t s = L.stream;
+      cuda_check(cudaMemcpyAsync(L.ws_phi.p, phi, N * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+      cuda_check(cudaMemcpyAsync(L.ws_vn.p, vn, N * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+      if (vn_np1) cuda_check(cudaMemcpyAsync(L.ws_vn1.p, vn_np1, N * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+      if (phi_dd) cuda_check(cudaMemcpyAsync(L.ws_dd.p, phi_dd, (size_t)D * N * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+      L.advect_normal(L.ws_vn.p, vn_np1 ? L.ws_vn1.p : nullptr, L.ws_phi.p, dt, phi_dd ? L.ws_dd.p : nullptr, precision);
+      cuda_check(cudaMemcpyAsync(phi, L.ws_phi.p, N * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+      if (phi_dd) cuda_check(cudaMemcpyAsync(phi_dd, L.ws_dd.p, (size_t)D * N * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+      cuda_check(cudaStreamSynchronize(s), "advect sync");
+    });
+  });
+}
+
+int lsg_advect_cfl_dt(lsg_level_set* ls, const double* vn, double* dt_out) {
+  return guard([&] {
+    need(vn != nullptr && dt_out != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      L.ws_vn.alloc(L.N);
+      cuda_check(cudaMemcpyAsync(L.ws_vn.p, vn, L.N * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      *dt_out = L.cfl_dt(L.ws_vn.p);
+    });
+  });
+}
+
+int lsg_second_derivatives_device(lsg_level_set* ls, const double* f_dev, double* f_dd_dev) {
+  return guard([&] {
+    need(f_dev != nullptr && f_dd_dev != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.second_derivatives(f_dev, f_dd_dev); });
+  });
+}
+
+int lsg_second_derivatives(lsg_level_set* ls, const double* f, double* f_dd) {
+  return guard([&] {
+    need(f != nullptr && f_dd != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      using LT = std::decay_t<decltype(L)>;
+      constexpr int D = LT::H == 2 ? 2 : 3;
+      L.ws_phi.alloc(L.N);
+      L.ws_dd.alloc((size_t)D * L.N);
+      cuda_check(cudaMemcpyAsync(L.ws_phi.p, f, L.N * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      L.second_derivatives(L.ws_phi.p, L.ws_dd.p);
+      cuda_check(cudaMemcpyAsync(f_dd, L.ws_dd.p, (size_t)D * L.N * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H");
+      cuda_check(cudaStreamSynchronize(L.stream), "dd sync");
+    });
+  });
+}
+
+int lsg_perturb_level_set_function(lsg_level_set* ls, double* phi, double epsilon) {
+  return guard([&] {
+    need(phi != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) {
+      for (int64_t n = 0; n < L.N; ++n)
+        if (fabs(phi[n]) < epsilon) phi[n] = (phi[n] > 0) ? epsilon : -epsilon;
+    });
+  });
+}
+
+int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on) {
+  return guard([&] { with_ls(ls, [&](auto& L) { L.timer.enabled = on != 0; }); });
+}
+
+int lsg_level_set_kernel_times(lsg_level_set* ls, double* ms, int64_t* counts, int nkinds, int reset) {
+  return guard([&] {
+    need(ms != nullptr && counts != nullptr, "null output");
+    with_ls(ls, [&](auto& L) {
+      L.timer.collect();
+      for (int k = 0; k < nkinds && k < K_NUM_KINDS; ++k) {
+        ms[k] = L.timer.ms[k];
+        counts[k] = L.timer.count[k];
+      }
+      if (reset) L.timer.reset();
+    });
+  });
+}
+
+int64_t lsg_level_set_launch_count(const lsg_level_set* ls) {
+  if (!ls) return -1;
+  return ls->dim == 2 ? ls->l2->timer.launches : ls->l3->timer.launches;
+}
+
+}  // extern "C"

@@ -1,0 +1,304 @@
+// Host forest implementation (see forest.hpp for what it stands in for).
+#include "forest.hpp"
+
+#include <algorithm>
+#include <cstring>
+#ifdef _OPENMP
+#include <omp.h>
+#include <parallel/algorithm>
+#endif
+
+namespace lsg {
+
+void sort_u64(std::vector<uint64_t>& v) {
+#ifdef _OPENMP
+  if (v.size() > (size_t)1 << 16) {
+    __gnu_parallel::sort(v.begin(), v.end());
+    return;
+  }
+#endif
+  std::sort(v.begin(), v.end());
+}
+
+// Trees of a brick are numbered along a Morton curve of their (i,j,k) position, as
+// p4est_connectivity_new_brick does; vertex coordinates follow my_p4est_brick_new
+// (src/my_p4est_tools.c:138-168): xyz_min + (i+ii)*dx with dx = (xyz_max - xyz_min)/n.
+void Brick::init(int dim_, const int* n_, const double* xyz_min_, const double* xyz_max_, const int* periodic_) {
+  dim = dim_;
+  for (int a = 0; a < 3; ++a) {
+    n[a] = (a < dim) ? n_[a] : 1;
+    xyz_min[a] = (a < dim) ? xyz_min_[a] : 0.0;
+    xyz_max[a] = (a < dim) ? xyz_max_[a] : 0.0;
+    periodic[a] = (a < dim && periodic_) ? periodic_[a] : 0;
+    if (n[a] < 1) throw std::invalid_argument("brick: number of trees per axis must be >= 1");
+    if (a < dim && !(xyz_max[a] > xyz_min[a])) throw std::invalid_argument("brick: xyz_max must exceed xyz_min");
+  }
+  num_trees = n[0] * n[1] * n[2];
+  std::vector<std::pair<uint64_t, int>> order;
+  order.reserve(num_trees);
+  for (int k = 0; k < n[2]; ++k)
+    for (int j = 0; j < n[1]; ++j)
+      for (int i = 0; i < n[0]; ++i) {
+        uint64_t key = spread3((uint64_t)i) | (spread3((uint64_t)j) << 1) | (spread3((uint64_t)k) << 2);
+        order.push_back({key, (n[0] * n[1] * k + n[0] * j + i)});
+      }
+  std::sort(order.begin(), order.end());
+  ijk_to_tree.assign(num_trees, -1);
+  tree_ijk.assign(3 * (size_t)num_trees, 0);
+  tmin.assign(3 * (size_t)num_trees, 0.0);
+  tmax.assign(3 * (size_t)num_trees, 0.0);
+  double dxyz[3];
+  for (int a = 0; a < 3; ++a) dxyz[a] = (xyz_max[a] - xyz_min[a]) / (double)n[a];
+  for (int t = 0; t < num_trees; ++t) {
+    int lin = order[t].second;
+    int ijk[3] = {lin % n[0], (lin / n[0]) % n[1], lin / (n[0] * n[1])};
+    ijk_to_tree[lin] = t;
+    for (int a = 0; a < 3; ++a) {
+      tree_ijk[3 * t + a] = ijk[a];
+      if (a < dim) {
+        tmin[3 * t + a] = xyz_min[a] + (ijk[a] + 0) * dxyz[a];
+        tmax[3 * t + a] = xyz_min[a] + (ijk[a] + 1) * dxyz[a];
+      }
+    }
+  }
+}
+
+template <int D>
+void Forest<D>::init(const int* n, const double* xyz_min, const double* xyz_max, const int* periodic) {
+  brick.init(D, n, xyz_min, xyz_max, periodic);
+  for (int a = 0; a < D; ++a)
+    if (brick.periodic[a]) throw std::invalid_argument("periodic bricks are not supported by this build of the host forest");
+  if (brick.num_trees > max_trees_for_keys<D>()) throw std::invalid_argument("too many trees for 64-bit node keys");
+  leaves.clear();
+  leaf_key.clear();
+  for (int t = 0; t < brick.num_trees; ++t) {
+    Quad q;
+    q.x[0] = q.x[1] = q.x[2] = 0;
+    q.tree = t;
+    q.level = 0;
+    leaves.push_back(q);
+    leaf_key.push_back(((uint64_t)t) << tree_shift<D>());
+  }
+  nodes_built = false;
+}
+
+template <int D>
+void Forest<D>::refine(const uint8_t* tags) {
+  const size_t nl = leaves.size();
+  std::vector<size_t> offset(nl + 1, 0);
+  for (size_t i = 0; i < nl; ++i) {
+    if (tags[i] && leaves[i].level >= DD::QMAXLEVEL) throw std::invalid_argument("refine: quadrant already at the maximum level");
+    offset[i + 1] = offset[i] + (tags[i] ? DD::CHILDREN : 1);
+  }
+  std::vector<Quad> out(offset[nl]);
+  std::vector<uint64_t> keys(offset[nl]);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii) {
+    const size_t i = (size_t)ii;
+    const Quad& q = leaves[i];
+    size_t o = offset[i];
+    if (!tags[i]) {
+      out[o] = q;
+      keys[o] = leaf_key[i];
+      continue;
+    }
+    const int32_t h = quadrant_len(DD::MAXLEVEL, q.level + 1);
+    for (int c = 0; c < DD::CHILDREN; ++c) {
+      Quad ch = q;
+      ch.level = q.level + 1;
+      for (int a = 0; a < D; ++a) ch.x[a] = q.x[a] + (((c >> a) & 1) ? h : 0);
+      out[o + c] = ch;
+      keys[o + c] = (((uint64_t)ch.tree) << tree_shift<D>()) | morton<D>(ch.x);
+    }
+  }
+  leaves.swap(out);
+  leaf_key.swap(keys);
+  nodes_built = false;
+}
+
+template <int D>
+void Forest<D>::coarsen(const uint8_t* tags) {
+  const size_t nl = leaves.size();
+  std::vector<Quad> out;
+  std::vector<uint64_t> keys;
+  out.reserve(nl);
+  keys.reserve(nl);
+  size_t i = 0;
+  while (i < nl) {
+    const Quad& q = leaves[i];
+    bool family = false;
+    if (q.level > 0 && i + DD::CHILDREN <= nl) {
+      const int32_t hp = quadrant_len(DD::MAXLEVEL, q.level - 1);
+      bool first_child = true;
+      for (int a = 0; a < D; ++a) first_child = first_child && (q.x[a] % hp == 0);
+      if (first_child) {
+        family = true;
+        const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
+        for (int c = 0; c < DD::CHILDREN && family; ++c) {
+          const Quad& s = leaves[i + c];
+          if (s.level != q.level || s.tree != q.tree || !tags[i + c]) family = false;
+          for (int a = 0; a < D && family; ++a)
+            if (s.x[a] != q.x[a] + (((c >> a) & 1) ? h : 0)) family = false;
+        }
+      }
+    }
+    if (family) {
+      Quad p = q;
+      p.level = q.level - 1;
+      out.push_back(p);
+      keys.push_back(leaf_key[i]);
+      i += DD::CHILDREN;
+    } else {
+      out.push_back(q);
+      keys.push_back(leaf_key[i]);
+      ++i;
+    }
+  }
+  leaves.swap(out);
+  leaf_key.swap(keys);
+  nodes_built = false;
+}
+
+template <int D>
+bool Forest<D>::global_to_tree(const int64_t* G, int32_t& tree, int32_t* x) const {
+  int ijk[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    const int64_t L = (int64_t)brick.n[a] * DD::ROOT_LEN;
+    if (G[a] < 0 || G[a] >= L) return false;
+    ijk[a] = (int)(G[a] / DD::ROOT_LEN);
+    x[a] = (int32_t)(G[a] - (int64_t)ijk[a] * DD::ROOT_LEN);
+  }
+  tree = brick.tree_at(ijk);
+  return true;
+}
+
+template <int D>
+int32_t Forest<D>::find_leaf(int32_t tree, const int32_t* x) const {
+  const uint64_t key = (((uint64_t)tree) << tree_shift<D>()) | morton<D>(x);
+  auto it = std::upper_bound(leaf_key.begin(), leaf_key.end(), key);
+  if (it == leaf_key.begin()) return -1;
+  const int32_t idx = (int32_t)((it - leaf_key.begin()) - 1);
+  const Quad& q = leaves[idx];
+  if (q.tree != tree) return -1;
+  const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
+  for (int a = 0; a < D; ++a)
+    if (x[a] < q.x[a] || x[a] >= q.x[a] + h) return -1;
+  return idx;
+}
+
+// Every leaf corner becomes a node (src/my_p4est_nodes.h:55-63). A corner shared by several trees
+// is owned by the lowest tree id that touches it and is clamped inside that tree
+// (p4est_node_canonicalize, src/my_p4est_nodes.c); nodes are sorted by (owner tree, Morton index)
+// (src/my_p4est_nodes.c:606-627).
+template <int D>
+void Forest<D>::build_nodes() {
+  const size_t nl = leaves.size();
+  std::vector<uint64_t> corner_key(nl * DD::CHILDREN);
+  auto canon = [&](const Quad& q, int c) -> uint64_t {
+    int64_t G[3] = {0, 0, 0};
+    const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
+    for (int a = 0; a < D; ++a)
+      G[a] = (int64_t)brick.tree_ijk[3 * q.tree + a] * DD::ROOT_LEN + q.x[a] + (((c >> a) & 1) ? h : 0);
+    // candidate trees along each axis
+    int cand[3][2];
+    int ncand[3] = {1, 1, 1};
+    for (int a = 0; a < 3; ++a) cand[a][0] = cand[a][1] = 0;
+    for (int a = 0; a < D; ++a) {
+      const int64_t L = (int64_t)brick.n[a] * DD::ROOT_LEN;
+      int64_t t = G[a] / DD::ROOT_LEN;
+      if (G[a] == L) {
+        cand[a][0] = (int)(t - 1);
+      } else if (G[a] % DD::ROOT_LEN == 0 && G[a] > 0) {
+        cand[a][0] = (int)(t - 1);
+        cand[a][1] = (int)t;
+        ncand[a] = 2;
+      } else {
+        cand[a][0] = (int)t;
+      }
+    }
+    int32_t owner = -1;
+    int owner_ijk[3] = {0, 0, 0};
+    for (int k = 0; k < ncand[2]; ++k)
+      for (int j = 0; j < ncand[1]; ++j)
+        for (int i = 0; i < ncand[0]; ++i) {
+          int ijk[3] = {cand[0][i], cand[1][j], cand[2][k]};
+          int32_t t = brick.tree_at(ijk);
+          if (owner < 0 || t < owner) {
+            owner = t;
+            owner_ijk[0] = ijk[0];
+            owner_ijk[1] = ijk[1];
+            owner_ijk[2] = ijk[2];
+          }
+        }
+    int32_t xl[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) {
+      int64_t v = G[a] - (int64_t)owner_ijk[a] * DD::ROOT_LEN;
+      if (v == DD::ROOT_LEN) v = DD::ROOT_LEN - 1;  // p4est_node_clamp_inside
+      xl[a] = (int32_t)v;
+    }
+    return (((uint64_t)owner) << tree_shift<D>()) | morton<D>(xl);
+  };
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii)
+    for (int c = 0; c < DD::CHILDREN; ++c) corner_key[(size_t)ii * DD::CHILDREN + c] = canon(leaves[(size_t)ii], c);
+  node_key = corner_key;
+  sort_u64(node_key);
+  node_key.erase(std::unique(node_key.begin(), node_key.end()), node_key.end());
+  const size_t nn = node_key.size();
+  if (nn >= (size_t)INT32_MAX) throw std::runtime_error("too many nodes for 32-bit node indices");
+  node_tree.resize(nn);
+  node_x.resize(nn * D);
+  const uint64_t mask = (((uint64_t)1) << tree_shift<D>()) - 1;
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nn; ++ii) {
+    const uint64_t key = node_key[(size_t)ii];
+    node_tree[(size_t)ii] = (int32_t)(key >> tree_shift<D>());
+    const uint64_t m = key & mask;
+    for (int a = 0; a < D; ++a) {
+      uint64_t v = 0;
+      for (int b = 0; b < DD::MAXLEVEL; ++b) v |= ((m >> (D * b + a)) & 1ull) << b;
+      node_x[(size_t)ii * D + a] = (int32_t)v;
+    }
+  }
+  local_nodes.resize(nl * DD::CHILDREN);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)(nl * DD::CHILDREN); ++ii) {
+    auto it = std::lower_bound(node_key.begin(), node_key.end(), corner_key[(size_t)ii]);
+    local_nodes[(size_t)ii] = (int32_t)(it - node_key.begin());
+  }
+  nodes_built = true;
+}
+
+template <int D>
+void Forest<D>::node_xyz(int32_t n, double* xyz) const {
+  const int32_t t = node_tree[n];
+  for (int a = 0; a < D; ++a) {
+    const int32_t v = node_x[(size_t)D * n + a];
+    const double r = (v == DD::ROOT_LEN - 1) ? 1.0 : (double)v / (double)DD::ROOT_LEN;
+    xyz[a] = (brick.tmax[3 * t + a] - brick.tmin[3 * t + a]) * r + brick.tmin[3 * t + a];
+  }
+}
+
+template <int D>
+int Forest<D>::max_level() const {
+  int l = 0;
+  for (const Quad& q : leaves) l = std::max(l, (int)q.level);
+  return l;
+}
+template <int D>
+int Forest<D>::min_level() const {
+  int l = DD::MAXLEVEL;
+  for (const Quad& q : leaves) l = std::min(l, (int)q.level);
+  return l;
+}
+
+template <int D>
+void Forest<D>::dxyz_min(double* dxyz) const {
+  const int l = max_level();
+  for (int a = 0; a < D; ++a) dxyz[a] = (brick.tmax[a] - brick.tmin[a]) / (double)(1 << l);
+}
+
+template struct Forest<2>;
+template struct Forest<3>;
+
+}  // namespace lsg

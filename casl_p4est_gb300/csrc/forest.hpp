@@ -1,0 +1,95 @@
+// Host forest: the minimal stand-in for the p4est objects that parCASL's level-set path reads.
+//
+// parCASL builds its grids with p4est (brick connectivity, refinement passes, ghost layer, node
+// numbering). p4est is an external library, so this file provides the pieces the hot path needs,
+// for a single process:
+//   - brick connectivity and tree geometry          src/my_p4est_tools.c:37-170 (my_p4est_brick_new)
+//   - one refinement pass over all leaves            p4est_refine(non-recursive), as called by
+//                                                    examples/reinitialization/main_2d.cpp:169-173
+//   - node numbering where every leaf corner is an independent node, owned by the lowest tree
+//     that touches it, clamped inside that tree, sorted by (tree, Morton)
+//                                                    src/my_p4est_nodes.h:55-63, src/my_p4est_nodes.c:606-627
+//   - local_nodes: corner node of each leaf          p4est_nodes_t::local_nodes
+//   - point location of the leaf containing a logical point
+//                                                    src/my_p4est_hierarchy.cpp:569-600
+// Leaves are kept in tree-major Morton order (p4est's linear order), so locating the leaf that
+// contains a point is a binary search over sorted keys instead of a walk down a cell tree.
+#pragma once
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lsg_common.h"
+
+namespace lsg {
+
+struct Brick {
+  int dim = 2;
+  int n[3] = {1, 1, 1};
+  double xyz_min[3] = {0, 0, 0};
+  double xyz_max[3] = {1, 1, 1};
+  int periodic[3] = {0, 0, 0};
+  int num_trees = 1;
+  std::vector<int32_t> ijk_to_tree;  // n0*n1*k + n0*j + i -> tree id
+  std::vector<int32_t> tree_ijk;     // 3 per tree
+  std::vector<double> tmin, tmax;    // 3 per tree: vertex coordinates of the tree's corners 0 and last
+
+  void init(int dim, const int* n, const double* xyz_min, const double* xyz_max, const int* periodic);
+  int32_t tree_at(const int* ijk) const { return ijk_to_tree[(size_t)n[0] * n[1] * ijk[2] + (size_t)n[0] * ijk[1] + ijk[0]]; }
+};
+
+struct Quad {
+  int32_t x[3];
+  int32_t tree;
+  int32_t level;
+};
+
+template <int D>
+struct Forest {
+  using DD = Dim<D>;
+  Brick brick;
+  std::vector<Quad> leaves;          // tree-major Morton order
+  std::vector<uint64_t> leaf_key;    // (tree << D*MAXLEVEL) | morton(x)
+  // node numbering (valid once build_nodes() ran)
+  std::vector<int32_t> node_tree;    // owner tree
+  std::vector<int32_t> node_x;       // D per node, clamped logical coordinates in the owner tree
+  std::vector<uint64_t> node_key;
+  std::vector<int32_t> local_nodes;  // CHILDREN per leaf, corner c = xbit + 2 ybit + 4 zbit
+  bool nodes_built = false;
+
+  void init(const int* n, const double* xyz_min, const double* xyz_max, const int* periodic);
+  // One refinement pass: every leaf with tags[i] != 0 is replaced by its CHILDREN children.
+  void refine(const uint8_t* tags);
+  // Coarsening pass: each complete family of CHILDREN sibling leaves with all tags set is merged.
+  void coarsen(const uint8_t* tags);
+  void build_nodes();
+
+  size_t num_leaves() const { return leaves.size(); }
+  size_t num_nodes() const { return node_tree.size(); }
+
+  // Leaf containing the logical point x (0 <= x < ROOT_LEN) of tree `tree`; -1 if none.
+  int32_t find_leaf(int32_t tree, const int32_t* x) const;
+  // Map global logical coordinates (tree_ijk*ROOT_LEN + local) to (tree, local); false if outside.
+  bool global_to_tree(const int64_t* G, int32_t& tree, int32_t* x) const;
+  // Node coordinates, as node_x_fr_n / node_xyz_fr_n (src/my_p4est_utils.h:1346-1405).
+  void node_xyz(int32_t n, double* xyz) const;
+  // Unclamped logical coordinates of a node (p4est_node_unclamp).
+  void node_unclamped(int32_t n, int32_t* x) const {
+    for (int a = 0; a < D; ++a) {
+      int32_t v = node_x[(size_t)D * n + a];
+      x[a] = (v == DD::ROOT_LEN - 1) ? DD::ROOT_LEN : v;
+    }
+  }
+  // Finest leaf level present (for dx_min reporting).
+  int max_level() const;
+  int min_level() const;
+  // Smallest cell size along each axis (get_dxyz_min, src/my_p4est_utils.cpp).
+  void dxyz_min(double* dxyz) const;
+};
+
+// Parallel sort of 64-bit keys (OpenMP when available).
+void sort_u64(std::vector<uint64_t>& v);
+
+}  // namespace lsg

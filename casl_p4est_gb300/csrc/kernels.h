@@ -1,0 +1,77 @@
+// Device table views and kernel launchers shared by the host drivers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lsg_common.h"
+
+namespace lsg {
+
+// Status word written once per reinitialisation call by the preparation kernel.
+enum : uint16_t {
+  ST_ANCHORED = 1,   // |phi_0| < zero_distance_threshold -> 0
+  ST_OUTSIDE = 2,    // phi_0 outside (limit_low, limit_high) -> phi_0
+  ST_NEAR = 4,       // a neighbour of phi_0 has the opposite sign: subcell distances in s_near
+  ST_POSITIVE = 8,   // phi_0 > 0
+  ST_CUT_SHIFT = 8,  // bit (8 + dir): the neighbour in direction dir is across the interface
+};
+
+template <int D>
+struct DTab64 {
+  int64_t N;
+  const int32_t* nbr;   // NS x N
+  const double* w;      // NS x N
+  const double* nrm;    // 2D x N
+  const double* d;      // 2D x N
+  const double* q;      // 2D(D-1) x N
+  const int32_t* cidx;  // N
+  const double* crec;   // 6 x R
+  const uint8_t* wall;  // N
+};
+
+// Mixed-precision tables (layout described in tables32.cpp).
+template <int D>
+struct DTab32 {
+  int64_t N;
+  const uint32_t* meta;  // N
+  const int32_t* nbr;    // NS x N (shared with the FP64 tables)
+  const float* wf;       // NS x N
+  const float* d;        // 2D x N
+  const float* q;        // 2D(D-1) x N
+  const int32_t* cidx;   // N (shared with the FP64 tables)
+  const float* corr;     // D*D x R
+};
+
+template <int D>
+void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s);
+template <int D>
+void launch_reinit_prep64(const DTab64<D>& T, const double* phi0, const double* dd0, double zdt, double lim_lo, double lim_hi,
+                          int order_space, uint16_t* status, double* s_near, cudaStream_t s);
+// out = stage(phin); if avg_with != nullptr: out = 0.5*(avg_with + stage(phin)) (may alias avg_with).
+template <int D>
+void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* status, const double* s_near, const double* phi0,
+                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s);
+template <int D>
+void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double* ddq, const double* ddm, const double* vn, double dt,
+                           double* out, const double* avg_with, cudaStream_t s);
+void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
+void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
+
+// Mixed precision.
+template <int D>
+void launch_dd32(const DTab32<D>& T, const float* f, float* dd, cudaStream_t s);
+template <int D>
+void launch_reinit_prep_mixed(const DTab64<D>& T, const uint32_t* meta32, const double* phi0, double zdt, double lim_lo,
+                              double lim_hi, int order_space, uint16_t* status, float* s_near, cudaStream_t s);
+template <int D>
+void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
+                           const float* dd, float* out, const float* avg_with, cudaStream_t s);
+template <int D>
+void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
+                           float* out, const float* avg_with, cudaStream_t s);
+void launch_f64_to_f32(const double* src, float* dst, int64_t n, cudaStream_t s);
+void launch_f32_to_f64(const float* src, double* dst, int64_t n, cudaStream_t s);
+// dst = src except at nodes whose status marks them outside the reinitialisation limits
+void launch_f32_to_f64_status(const float* src, const uint16_t* status, double* dst, int64_t n, cudaStream_t s);
+
+}  // namespace lsg

@@ -1,0 +1,327 @@
+// FP64 level-set kernels that evaluate every floating-point expression in the reference's order.
+// This translation unit is compiled with -fmad=false so that no multiply-add is contracted, which
+// makes each result the IEEE double the reference's C++ produces for the same inputs.
+//
+// One thread per node. Restated reference routines:
+//   laplace + correct_naive_second_derivatives  src/my_p4est_quad_neighbor_nodes_of_node.h:615-635,
+//                                               src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298
+//   ngbd_with_quadratic_interpolation          .h:1514-1545
+//   reinitialize_one_iteration                 src/my_p4est_level_set.cpp:59-288
+//   interface_Location[_With_Second_Order_Derivative]  src/casl_math.cpp:55-97
+//   advect_in_normal_direction_one_iteration   src/my_p4est_level_set.cpp:559-654
+//   CFL of the CF overload                     src/my_p4est_level_set.cpp:745-783
+#include "kernels.h"
+#include "stencil64.cuh"
+#include "tables.hpp"
+
+namespace lsg {
+
+namespace {
+
+using namespace st64;
+constexpr int TPB = 256;
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_dd64(DTab64<D> T, const double* __restrict__ f, double* __restrict__ dd) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= T.N) return;
+  double Dv[D];
+  laplace64<D>(T, n, f, Dv);
+#pragma unroll
+  for (int a = 0; a < D; ++a) dd[(int64_t)a * T.N + n] = Dv[a];
+}
+
+// Everything reinitialize_one_iteration derives from phi_0 alone: anchoring, range limits, sign,
+// and the subcell distances of the interface-adjacent nodes (src/my_p4est_level_set.cpp:84-211).
+template <int D>
+__global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0,
+                                                       double zdt, double lim_lo, double lim_hi, int order_space,
+                                                       uint16_t* __restrict__ status, double* __restrict__ s_near) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const double p0 = phi0[n];
+  if (fabs(p0) < zdt) {
+    status[n] = ST_ANCHORED;
+    return;
+  }
+  if (!(lim_lo < p0 && p0 < lim_hi)) {
+    status[n] = ST_OUTSIDE;
+    return;
+  }
+  double Dv[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) Dv[a] = dd0[(int64_t)a * N + n];
+  double fn[2 * D];
+  bool near = false;
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    fn[dir] = quad_nb64<D>(T, dir, n, phi0, Dv);
+    near = near || (p0 * fn[dir] < 0.0);
+  }
+  uint16_t st = (p0 > 0.0) ? ST_POSITIVE : 0;
+  if (near) {
+    st |= ST_NEAR;
+    double s[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.d[(int64_t)dir * N + n];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      if (!(p0 * fn[dir] < 0.0)) continue;
+      st |= (uint16_t)(1u << (ST_CUT_SHIFT + dir));
+      const int axis = dir >> 1;
+      if (dir & 1) {
+        if (order_space > 1)
+          s[dir] = interface_location_2nd(0.0, s[dir], p0, fn[dir], Dv[axis], lin64<D>(T, dir, n, dd0 + (int64_t)axis * N));
+        else
+          s[dir] = interface_location(0.0, s[dir], p0, fn[dir]);
+      } else {
+        if (order_space > 1)
+          s[dir] = -interface_location_2nd(-s[dir], 0.0, fn[dir], p0, lin64<D>(T, dir, n, dd0 + (int64_t)axis * N), Dv[axis]);
+        else
+          s[dir] = -interface_location(-s[dir], 0.0, fn[dir], p0);
+      }
+    }
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) s_near[(int64_t)dir * N + n] = max2(s[dir], zdt);
+  }
+  status[n] = st;
+}
+
+template <int D, int ORDER_SPACE, bool AVG>
+__global__ void __launch_bounds__(TPB) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
+                                                        const double* __restrict__ phi0, const double* __restrict__ phin,
+                                                        const double* __restrict__ dd, double* out, const double* avg_with) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const uint16_t st = status[n];
+  double r;
+  if (st & ST_ANCHORED) {
+    r = 0.0;
+  } else if (st & ST_OUTSIDE) {
+    r = phi0[n];
+  } else {
+    const double p0 = phi0[n];
+    const double f0 = phin[n];
+    double Dv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) Dv[a] = dd[(int64_t)a * N + n];
+    double fnb[2 * D], s[2 * D], xx0[D], xxnb[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dv);
+    if (st & ST_NEAR) {
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        s[dir] = s_near[(int64_t)dir * N + n];
+        if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0;
+      }
+    } else {
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.d[(int64_t)dir * N + n];
+    }
+    if (ORDER_SPACE > 1) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        xx0[a] = Dv[a];
+        xxnb[2 * a] = lin64<D>(T, 2 * a, n, dd + (int64_t)a * N);
+        xxnb[2 * a + 1] = lin64<D>(T, 2 * a + 1, n, dd + (int64_t)a * N);
+      }
+    }
+    const uint8_t wl = T.wall[n];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      if (wl & (1u << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        fnb[2 * a] = fnb[2 * a + 1];
+        if (ORDER_SPACE > 1) xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
+      }
+      if (wl & (1u << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        fnb[2 * a + 1] = fnb[2 * a];
+        if (ORDER_SPACE > 1) xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
+      }
+    }
+    double gp[D], gm[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      gp[a] = (fnb[2 * a + 1] - f0) / s[2 * a + 1];
+      gm[a] = (f0 - fnb[2 * a]) / s[2 * a];
+    }
+    if (ORDER_SPACE > 1) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const double xm = minmod(xxnb[2 * a], xx0[a]);
+        gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
+        const double xp = minmod(xxnb[2 * a + 1], xx0[a]);
+        gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
+      }
+    }
+    const double sgn = (p0 > 0.0 ? 1.0 : -1.0);
+    double dt = min2(s[0], s[1]);
+    dt = min3(dt, s[2], s[3]);
+    if (D == 3) dt = min3(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
+    dt /= (double)D;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      if (sgn * gp[a] > 0.0) gp[a] = 0.0;
+      if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+    }
+    double h = max2(gp[0] * gp[0], gm[0] * gm[0]) + max2(gp[1] * gp[1], gm[1] * gm[1]);
+    if (D == 3) h = h + max2(gp[2 % D] * gp[2 % D], gm[2 % D] * gm[2 % D]);
+    r = f0 - dt * sgn * (sqrt(h) - 1.);
+    if (p0 * r < 0.0) r *= -1.0;
+  }
+  if (AVG) r = .5 * (avg_with[n] + r);
+  out[n] = r;
+}
+
+template <int D, bool AVG>
+__global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
+                                                        const double* __restrict__ ddm, const double* __restrict__ vn, double dt,
+                                                        double* out, const double* avg_with) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const double f0 = phin[n];
+  double Dq[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) Dq[a] = ddq[(int64_t)a * N + n];
+  double fnb[2 * D], s[2 * D], xx0[D], xxnb[2 * D];
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dq);
+    s[dir] = T.d[(int64_t)dir * N + n];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    xx0[a] = ddm[(int64_t)a * N + n];
+    xxnb[2 * a] = lin64<D>(T, 2 * a, n, ddm + (int64_t)a * N);
+    xxnb[2 * a + 1] = lin64<D>(T, 2 * a + 1, n, ddm + (int64_t)a * N);
+  }
+  const uint8_t wl = T.wall[n];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    if (wl & (1u << (2 * a))) {
+      s[2 * a] = s[2 * a + 1];
+      fnb[2 * a] = fnb[2 * a + 1];
+      xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
+    }
+    if (wl & (1u << (2 * a + 1))) {
+      s[2 * a + 1] = s[2 * a];
+      fnb[2 * a + 1] = fnb[2 * a];
+      xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
+    }
+  }
+  double gp[D], gm[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    gp[a] = (fnb[2 * a + 1] - f0) / s[2 * a + 1];
+    gm[a] = (f0 - fnb[2 * a]) / s[2 * a];
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double xm = minmod(xxnb[2 * a], xx0[a]);
+    gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
+    const double xp = minmod(xxnb[2 * a + 1], xx0[a]);
+    gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
+  }
+  const double v = vn[n];
+  const double sgn = (v > 0.0 ? +1.0 : -1.0);
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    if (sgn * gp[a] > 0.0) gp[a] = 0.0;
+    if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+  }
+  double h = (gp[0] * gp[0] + gm[0] * gm[0]) + (gp[1] * gp[1] + gm[1] * gm[1]);
+  if (D == 3) h = h + (gp[2 % D] * gp[2 % D] + gm[2 % D] * gm[2 % D]);
+  double r = f0 - dt * v * (sqrt(h));
+  if (AVG) r = 0.5 * (avg_with[n] + r);
+  out[n] = r;
+}
+
+__global__ void k_copy64(const double* __restrict__ a, double* __restrict__ b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+// dt = min over nodes of 0.8*|s_min/vn| (min is exact in any order). Values are non-negative, so
+// their IEEE bit patterns order like unsigned integers and an atomicMin on the bits is exact.
+__global__ void k_min_cfl(const double* __restrict__ smin, const double* __restrict__ vn, int64_t n, unsigned long long* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 1.7976931348623157e308;
+  if (i < n) v = 0.8 * fabs(smin[i] / vn[i]);
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) atomicMin(out, (unsigned long long)__double_as_longlong(v));
+}
+
+inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+}  // namespace
+
+template <int D>
+void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s) {
+  if (T.N == 0) return;
+  k_dd64<D><<<nblocks(T.N), TPB, 0, s>>>(T, f, dd);
+}
+
+template <int D>
+void launch_reinit_prep64(const DTab64<D>& T, const double* phi0, const double* dd0, double zdt, double lim_lo, double lim_hi,
+                          int order_space, uint16_t* status, double* s_near, cudaStream_t s) {
+  if (T.N == 0) return;
+  k_reinit_prep64<D><<<nblocks(T.N), TPB, 0, s>>>(T, phi0, dd0, zdt, lim_lo, lim_hi, order_space, status, s_near);
+}
+
+template <int D>
+void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* status, const double* s_near, const double* phi0,
+                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s) {
+  if (T.N == 0) return;
+  const unsigned g = nblocks(T.N);
+  if (order_space > 1) {
+    if (avg_with)
+      k_reinit_stage64<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+    else
+      k_reinit_stage64<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+  } else {
+    if (avg_with)
+      k_reinit_stage64<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+    else
+      k_reinit_stage64<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+  }
+}
+
+template <int D>
+void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double* ddq, const double* ddm, const double* vn, double dt,
+                           double* out, const double* avg_with, cudaStream_t s) {
+  if (T.N == 0) return;
+  if (avg_with)
+    k_advect_stage64<D, true><<<nblocks(T.N), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with);
+  else
+    k_advect_stage64<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with);
+}
+
+void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s) {
+  if (n == 0) return;
+  k_copy64<<<nblocks(n), TPB, 0, s>>>(src, dst, n);
+}
+
+void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s) {
+  const double init = 1.7976931348623157e308;
+  cudaMemcpyAsync(dt_out_dev, &init, sizeof(double), cudaMemcpyHostToDevice, s);
+  if (n == 0) return;
+  k_min_cfl<<<nblocks(n), TPB, 0, s>>>(smin, vn, n, (unsigned long long*)dt_out_dev);
+}
+
+#define LSG_INST(D)                                                                                                          \
+  template void launch_dd64<D>(const DTab64<D>&, const double*, double*, cudaStream_t);                                      \
+  template void launch_reinit_prep64<D>(const DTab64<D>&, const double*, const double*, double, double, double, int, uint16_t*, \
+                                        double*, cudaStream_t);                                                              \
+  template void launch_reinit_stage64<D>(const DTab64<D>&, int, const uint16_t*, const double*, const double*, const double*, \
+                                         const double*, double*, const double*, cudaStream_t);                               \
+  template void launch_advect_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, double,  \
+                                         double*, const double*, cudaStream_t);
+LSG_INST(2)
+LSG_INST(3)
+#undef LSG_INST
+
+}  // namespace lsg

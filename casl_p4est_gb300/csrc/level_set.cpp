@@ -1,0 +1,304 @@
+// Host drivers of the device level-set operator (see level_set.hpp).
+#include "level_set.hpp"
+
+#include <float.h>
+
+#include <cstring>
+#include <stdexcept>
+
+namespace lsg {
+
+// src/my_p4est_utils.h:322-330
+double largest_dbl_smaller_than_dbl_max() {
+  double p = 1.0;
+  while (DBL_MAX - p == DBL_MAX) p *= 2.0;
+  return DBL_MAX - p;
+}
+
+KernelTimer::~KernelTimer() {
+  for (auto& e : pool) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+}
+
+void KernelTimer::begin(int kind, cudaStream_t s) {
+  ++launches;
+  if (!enabled) return;
+  if (used == pool.size()) {
+    cudaEvent_t a, b;
+    cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+    pool.push_back({a, b});
+  }
+  auto ev = pool[used++];
+  cuda_check(cudaEventRecord(ev.first, s), "cudaEventRecord");
+  pending.push_back({kind, ev});
+}
+
+void KernelTimer::end(cudaStream_t s) {
+  if (!enabled) return;
+  cuda_check(cudaEventRecord(pending.back().second.second, s), "cudaEventRecord");
+}
+
+void KernelTimer::collect() {
+  for (auto& p : pending) {
+    cuda_check(cudaEventSynchronize(p.second.second), "cudaEventSynchronize");
+    float t = 0;
+    cuda_check(cudaEventElapsedTime(&t, p.second.first, p.second.second), "cudaEventElapsedTime");
+    ms[p.first] += t;
+    count[p.first] += 1;
+  }
+  pending.clear();
+  used = 0;
+}
+
+void KernelTimer::reset() {
+  collect();
+  for (int k = 0; k < K_NUM_KINDS; ++k) {
+    ms[k] = 0;
+    count[k] = 0;
+  }
+  launches = 0;
+}
+
+#define LSG_LAUNCH(kind, expr) \
+  do {                         \
+    timer.begin(kind, stream); \
+    expr;                      \
+    timer.end(stream);         \
+  } while (0)
+
+template <int D>
+LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
+  if (!forest.nodes_built) throw std::invalid_argument("level set: the forest's nodes are not built");
+  N = (int64_t)forest.num_nodes();
+  double tdim[3];
+  for (int a = 0; a < D; ++a) tdim[a] = (forest.brick.xyz_max[a] - forest.brick.xyz_min[a]) / forest.brick.n[a];
+  zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
+  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  own_stream = true;
+  Tables64<D> T;
+  build_tables64<D>(forest, T);
+  num_corrections = (int64_t)(T.crec.size() / 6);
+  nbr.upload(T.nbr, stream);
+  w.upload(T.w, stream);
+  nrm.upload(T.nrm, stream);
+  d.upload(T.d, stream);
+  q.upload(T.q, stream);
+  cidx.upload(T.cidx, stream);
+  crec.upload(T.crec, stream);
+  wall.upload(T.wall, stream);
+  smin.upload(T.smin, stream);
+  if (with_mixed) {
+    Tables32<D> M;
+    build_tables32<D>(T, M);
+    upload_mixed(M);
+  }
+  cuda_check(cudaStreamSynchronize(stream), "table upload");
+  T64.N = N;
+  T64.nbr = nbr.p;
+  T64.w = w.p;
+  T64.nrm = nrm.p;
+  T64.d = d.p;
+  T64.q = q.p;
+  T64.cidx = cidx.p;
+  T64.crec = crec.p;
+  T64.wall = wall.p;
+}
+
+template <int D>
+LevelSet<D>::~LevelSet() {
+  if (stream) cudaStreamSynchronize(stream);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+template <int D>
+void LevelSet<D>::set_stream(cudaStream_t s) {
+  cuda_check(cudaStreamSynchronize(stream), "stream sync");
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  own_stream = false;
+  stream = s;
+}
+
+template <int D>
+void LevelSet<D>::second_derivatives(const double* f, double* dd) {
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, f, dd, stream));
+  cuda_check(cudaGetLastError(), "second derivatives");
+}
+
+template <int D>
+void LevelSet<D>::reinitialize(double* phi, int os, int ot, double limit_high, double limit_low, int iterations, int precision) {
+  if (os < 1 || os > 2 || ot < 1 || ot > 2)
+    throw std::invalid_argument(
+        "reinitialize_within_range_of_phi_0: valid orders of orders of accuracy for space and pseudotime are 1 and 2 only!");
+  if (!(limit_high > limit_low)) throw std::invalid_argument("reinitialize: limit_high must exceed limit_low");
+  if (iterations < 0) throw std::invalid_argument("reinitialize: negative number of iterations");
+  // phi_0 limits widened as in reinitialize_one_iteration (src/my_p4est_level_set.cpp:75-76)
+  const double big = largest_dbl_smaller_than_dbl_max();
+  const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
+  const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
+  if (precision == PREC_FP64)
+    reinit_fp64(phi, os, ot, hi, lo, iterations);
+  else if (precision == PREC_MIXED)
+    reinit_mixed(phi, os, ot, hi, lo, iterations);
+  else
+    throw std::invalid_argument("reinitialize: unknown precision mode");
+}
+
+// reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557) on one device:
+// the ghost updates of a single process are no-ops and the layer/local split merges into one launch.
+template <int D>
+void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo, int iters) {
+  phi0.alloc(N);
+  phi1.alloc(N);
+  dd0.alloc((size_t)D * N);
+  ddc.alloc((size_t)D * N);
+  snear.alloc((size_t)2 * D * N);
+  status.alloc(N);
+  cuda_check(cudaMemcpyAsync(phi0.p, phi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_0");
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi0.p, dd0.p, stream));
+  LSG_LAUNCH(K_PREP64, launch_reinit_prep64<D>(T64, phi0.p, dd0.p, zdt, lo, hi, os, status.p, snear.p, stream));
+  for (int it = 0; it < iters; ++it) {
+    LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, ddc.p, stream));
+    LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0.p, phi, ddc.p, phi1.p, nullptr, stream));
+    if (ot > 1) {
+      LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi1.p, ddc.p, stream));
+      LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0.p, phi1.p, ddc.p, phi, phi, stream));
+    } else {
+      cuda_check(cudaMemcpyAsync(phi, phi1.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_np1");
+    }
+  }
+  cuda_check(cudaGetLastError(), "reinitialize (fp64)");
+}
+
+template <int D>
+void LevelSet<D>::build_mixed() {
+  if (mixed_ready) return;
+  // The FP32 tables derive from the FP64 ones; rebuild those on the host.
+  Tables64<D> T;
+  build_tables64<D>(*F, T);
+  Tables32<D> M;
+  build_tables32<D>(T, M);
+  upload_mixed(M);
+}
+
+template <int D>
+void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
+  meta.upload(M.meta, stream);
+  wf.upload(M.wf, stream);
+  df.upload(M.d, stream);
+  qf.upload(M.q, stream);
+  corr32.upload(M.corr, stream);
+  cuda_check(cudaStreamSynchronize(stream), "mixed table upload");
+  T32.N = N;
+  T32.meta = meta.p;
+  T32.nbr = nbr.p;
+  T32.wf = wf.p;
+  T32.d = df.p;
+  T32.q = qf.p;
+  T32.cidx = cidx.p;
+  T32.corr = corr32.p;
+  mixed_ready = true;
+}
+
+
+// Mixed precision: phi_n and all per-iteration work in FP32; the phi_0-only subcell step in FP64.
+template <int D>
+void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters) {
+  build_mixed();
+  f_phi.alloc(N);
+  f_phi1.alloc(N);
+  f_dd.alloc((size_t)D * N);
+  f_snear.alloc((size_t)2 * D * N);
+  status.alloc(N);
+  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T64, meta.p, phi, zdt, lo, hi, os, status.p, f_snear.p, stream));
+  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi, f_phi.p, N, stream));
+  for (int it = 0; it < iters; ++it) {
+    LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));
+    LSG_LAUNCH(K_STAGE32, launch_reinit_stage32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
+    if (ot > 1) {
+      LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi1.p, f_dd.p, stream));
+      LSG_LAUNCH(K_STAGE32, launch_reinit_stage32<D>(T32, os, status.p, f_snear.p, f_phi1.p, f_dd.p, f_phi.p, f_phi.p, stream));
+    } else {
+      std::swap(f_phi.p, f_phi1.p);
+    }
+  }
+  LSG_LAUNCH(K_CONVERT, launch_f32_to_f64_status(f_phi.p, status.p, phi, N, stream));
+  cuda_check(cudaGetLastError(), "reinitialize (mixed)");
+}
+
+// advect_in_normal_direction (src/my_p4est_level_set.cpp:656-725).
+template <int D>
+void LevelSet<D>::advect_normal(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd, int precision) {
+  if (precision == PREC_MIXED) {
+    advect_mixed(vn, vn_np1, phi, dt, phi_dd);
+    return;
+  }
+  if (precision != PREC_FP64) throw std::invalid_argument("advect_in_normal_direction: unknown precision mode");
+  phi0.alloc(N);
+  phi1.alloc(N);
+  ddc.alloc((size_t)D * N);
+  // stage 1: the quadratic neighbours use laplace(phi) (computed inline by the reference); the
+  // minmod terms use the given second derivatives, or the same laplace(phi) when none are given.
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, ddc.p, stream));
+  const double* ddm = phi_dd ? phi_dd : ddc.p;
+  cuda_check(cudaMemcpyAsync(phi0.p, phi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_n");
+  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T64, phi0.p, ddc.p, ddm, vn, dt, phi, nullptr, stream));
+  // stage 2 with the derivatives of the intermediate phi (written to the caller's arrays if given)
+  double* dd2 = phi_dd ? phi_dd : ddc.p;
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, dd2, stream));
+  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T64, phi, dd2, dd2, vn_np1 ? vn_np1 : vn, dt, phi1.p, phi0.p, stream));
+  cuda_check(cudaMemcpyAsync(phi, phi1.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi");
+  cuda_check(cudaGetLastError(), "advect_in_normal_direction");
+}
+
+template <int D>
+void LevelSet<D>::advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd) {
+  build_mixed();
+  f_phi.alloc(N);
+  f_phi0.alloc(N);
+  f_phi1.alloc(N);
+  f_dd.alloc((size_t)D * N);
+  f_vn.alloc(vn_np1 ? 2 * (size_t)N : (size_t)N);
+  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi, f_phi0.p, N, stream));
+  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(vn, f_vn.p, N, stream));
+  if (vn_np1) LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(vn_np1, f_vn.p + N, N, stream));
+  LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi0.p, f_dd.p, stream));
+  const float* ddm = f_dd.p;
+  if (phi_dd) {
+    f_ddm.alloc((size_t)D * N);
+    LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi_dd, f_ddm.p, (int64_t)D * N, stream));
+    ddm = f_ddm.p;
+  }
+  LSG_LAUNCH(K_ADVECT32, launch_advect_stage32<D>(T32, f_phi0.p, f_dd.p, ddm, f_vn.p, (float)dt, f_phi.p, nullptr, stream));
+  LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));
+  if (phi_dd) LSG_LAUNCH(K_CONVERT, launch_f32_to_f64(f_dd.p, phi_dd, (int64_t)D * N, stream));
+  LSG_LAUNCH(K_ADVECT32, launch_advect_stage32<D>(T32, f_phi.p, f_dd.p, f_dd.p, vn_np1 ? f_vn.p + N : f_vn.p, (float)dt, f_phi1.p, f_phi0.p, stream));
+  LSG_LAUNCH(K_CONVERT, launch_f32_to_f64(f_phi1.p, phi, N, stream));
+  cuda_check(cudaGetLastError(), "advect_in_normal_direction (mixed)");
+}
+
+template <int D>
+double LevelSet<D>::cfl_dt(const double* vn) {
+  dt_dev.alloc(1);
+  LSG_LAUNCH(K_CONVERT, launch_min_cfl(smin.p, vn, N, dt_dev.p, stream));
+  double dt = 0;
+  cuda_check(cudaMemcpyAsync(&dt, dt_dev.p, sizeof(double), cudaMemcpyDeviceToHost, stream), "cfl dt");
+  cuda_check(cudaStreamSynchronize(stream), "cfl dt sync");
+  return dt;
+}
+
+template <int D>
+void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision) {
+  ws_phi.alloc(N);
+  cuda_check(cudaMemcpyAsync(ws_phi.p, phi, N * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D phi");
+  reinitialize(ws_phi.p, os, ot, hi, lo, iters, precision);
+  cuda_check(cudaMemcpyAsync(phi, ws_phi.p, N * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H phi");
+  cuda_check(cudaStreamSynchronize(stream), "reinitialize sync");
+}
+
+template struct LevelSet<2>;
+template struct LevelSet<3>;
+
+}  // namespace lsg

@@ -1,0 +1,98 @@
+// Device-resident level-set operator: the GPU counterpart of my_p4est_level_set_t
+// (src/my_p4est_level_set.h:203-848) restricted to reinitialisation and normal-direction advection.
+//
+// One object per grid. Construction flattens the node neighbours into device tables (once per grid,
+// as the reference's init_neighbors caches one record per node); the work vectors the reference
+// creates and destroys inside every call (src/my_p4est_level_set.cpp:323-344, 527-544) are allocated
+// on first use and kept.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <utility>
+#include <vector>
+
+#include "devbuf.hpp"
+#include "kernels.h"
+#include "tables.hpp"
+
+namespace lsg {
+
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// Kernel classes for the optional per-launch timing (CUDA events around each launch).
+enum KernelKind {
+  K_DD64 = 0, K_PREP64, K_STAGE64, K_ADVECT64, K_DD32, K_PREP_MIXED, K_STAGE32, K_ADVECT32, K_CONVERT, K_COPY, K_NUM_KINDS
+};
+
+struct KernelTimer {
+  bool enabled = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+  size_t used = 0;
+  double ms[K_NUM_KINDS] = {0};
+  int64_t count[K_NUM_KINDS] = {0};
+  int64_t launches = 0;  // all launches of this object's kernels, timed or not
+  ~KernelTimer();
+  void begin(int kind, cudaStream_t s);
+  void end(cudaStream_t s);
+  void collect();  // synchronises the recorded events and accumulates their durations
+  void reset();
+};
+
+template <int D>
+struct LevelSet {
+  static constexpr int H = Dim<D>::HALF;
+  static constexpr int NS = 2 * D * H;
+  const Forest<D>* F = nullptr;
+  int64_t N = 0;
+  double zdt = 0;  // zero_distance_threshold = EPS * min(tree dimensions) (src/my_p4est_level_set.h:388)
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  KernelTimer timer;
+  int64_t num_corrections = 0;
+
+  // FP64 tables
+  DevBuf<int32_t> nbr, cidx;
+  DevBuf<double> w, nrm, d, q, crec, smin;
+  DevBuf<uint8_t> wall;
+  DTab64<D> T64{};
+  // mixed tables (built on first mixed call)
+  bool mixed_ready = false;
+  DevBuf<uint32_t> meta;
+  DevBuf<float> wf, df, qf, corr32;
+  DTab32<D> T32{};
+  // work vectors
+  DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
+  DevBuf<uint16_t> status;
+  DevBuf<float> f_phi0, f_phi, f_phi1, f_dd, f_ddm, f_snear, f_vn;
+
+  explicit LevelSet(const Forest<D>& forest, bool with_mixed = true);
+  ~LevelSet();
+  void set_stream(cudaStream_t s);
+
+  // phi: device pointer, N doubles, updated in place (reinitialize_within_range_of_phi_0).
+  void reinitialize(double* phi, int order_space, int order_pseudotime, double limit_high, double limit_low, int iterations,
+                    int precision);
+  // advect_in_normal_direction(vn[, vn_np1], phi, dt, phi_xx...): device pointers; phi_dd may be null
+  // (D*N doubles, overwritten with the derivatives of the intermediate stage as the reference does).
+  void advect_normal(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd, int precision);
+  // compute_derivatives: dd = D*N doubles.
+  void second_derivatives(const double* f, double* dd);
+  // dt of the CF overload: min over nodes of 0.8*|s_min/vn| (src/my_p4est_level_set.cpp:752-776).
+  double cfl_dt(const double* vn);
+
+  // host-buffer conveniences (copies inside)
+  void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision);
+
+ private:
+  void build_mixed();
+  void upload_mixed(const Tables32<D>& M);
+  void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
+  void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
+  void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
+};
+
+double largest_dbl_smaller_than_dbl_max();
+
+}  // namespace lsg

@@ -1,0 +1,181 @@
+// FP64 stencil helpers shared by the FP64 kernels and the FP64 subcell step of the mixed path.
+// Each function restates one reference routine with the reference's expression order; the FP64
+// translation unit is compiled with -fmad=false, which makes its results bit-identical to the
+// reference's double arithmetic.
+//   lin64            interpolate_linearly          src/my_p4est_quad_neighbor_nodes_of_node.h:290-306
+//   correct64        correct_naive_second_derivatives  src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298
+//   laplace64        laplace                       .h:615-635 (central_second_derivative .h:214-220)
+//   quad_nb64        ngbd_with_quadratic_interpolation .h:1514-1545
+//   interface_location[_2nd]                       src/casl_math.cpp:55-97
+#pragma once
+#include "kernels.h"
+#include "tables.hpp"
+
+namespace lsg {
+namespace st64 {
+
+__device__ __forceinline__ bool is_zero(double v) { return fabs(v) < EPS; }  // check_if_zero, .h:186
+
+template <int D>
+__device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t N = T.N;
+  const int64_t base = (int64_t)(dir * H) * N + n;
+  double acc = f[T.nbr[base]] * T.w[base];
+#pragma unroll
+  for (int k = 1; k < H; ++k) {
+    const int32_t ik = T.nbr[base + k * N];
+    if (ik >= 0) acc = acc + f[ik] * T.w[base + k * N];
+  }
+  return acc / T.nrm[(int64_t)dir * N + n];
+}
+
+// correct_naive_second_derivatives (src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298), all branches.
+template <int D>
+__device__ void correct64(const double* __restrict__ m, double* Dv) {
+  if (D == 2) {
+    const double m12 = m[CM12], m21 = m[CM21];
+    if (is_zero(m12)) {
+      if (!is_zero(m21)) Dv[1] = Dv[1] - m21 * Dv[0];
+    } else if (is_zero(m21)) {
+      Dv[0] = Dv[0] - m12 * Dv[1];
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const double nx = Dv[0], ny = Dv[1];
+      Dv[0] = nx * idet - ny * (m12 * idet);
+      Dv[1] = ny * idet - nx * (m21 * idet);
+    }
+    return;
+  }
+  const double m12 = m[CM12], m13 = m[CM13], m21 = m[CM21], m23 = m[CM23], m31 = m[CM31], m32 = m[CM32];
+  double& Dxx = Dv[0];
+  double& Dyy = Dv[1];
+  double& Dzz = Dv[2 % D];
+  if (is_zero(m12) && is_zero(m13)) {
+    if (is_zero(m23)) {
+      const bool m21nz = !is_zero(m21), m31nz = !is_zero(m31), m32nz = !is_zero(m32);
+      if (m21nz) Dyy = Dyy - m21 * Dxx;
+      if (m31nz) Dzz = Dzz - m31 * Dxx;
+      if (m32nz) Dzz = Dzz - m32 * Dyy;
+    } else if (is_zero(m32)) {
+      const bool m21nz = !is_zero(m21), m31nz = !is_zero(m31);
+      if (m31nz) Dzz = Dzz - m31 * Dxx;
+      Dyy = Dyy - m23 * Dzz;
+      if (m21nz) Dyy = Dyy - m21 * Dxx;
+    } else {
+      const double idet = 1.0 / (1.0 - m23 * m32);
+      const bool m21z = is_zero(m21), m31z = is_zero(m31);
+      const double nDyy = Dyy, nDzz = Dzz;
+      Dyy = ((m21z ? nDyy : (nDyy - m21 * Dxx)) - m23 * (m31z ? nDzz : (nDzz - m31 * Dxx))) * idet;
+      Dzz = ((m31z ? nDzz : (nDzz - m31 * Dxx)) - m32 * (m21z ? nDyy : (nDyy - m21 * Dxx))) * idet;
+    }
+  } else if (is_zero(m21) && is_zero(m23)) {
+    if (is_zero(m13)) {
+      const bool m12nz = !is_zero(m12), m31nz = !is_zero(m31), m32nz = !is_zero(m32);
+      if (m12nz) Dxx = Dxx - m12 * Dyy;
+      if (m31nz) Dzz = Dzz - m31 * Dxx;
+      if (m32nz) Dzz = Dzz - m32 * Dyy;
+    } else if (is_zero(m31)) {
+      const bool m12nz = !is_zero(m12), m32nz = !is_zero(m32);
+      if (m32nz) Dzz = Dzz - m32 * Dyy;
+      Dxx = Dxx - m13 * Dzz;
+      if (m12nz) Dxx = Dxx - m12 * Dyy;
+    } else {
+      const double idet = 1.0 / (1.0 - m13 * m31);
+      const bool m12z = is_zero(m12), m32z = is_zero(m32);
+      const double nDxx = Dxx, nDzz = Dzz;
+      Dxx = ((m12z ? nDxx : (nDxx - m12 * Dyy)) - m13 * (m32z ? nDzz : (nDzz - m32 * Dyy))) * idet;
+      Dzz = ((m32z ? nDzz : (nDzz - m32 * Dyy)) - m31 * (m12z ? nDxx : (nDxx - m12 * Dyy))) * idet;
+    }
+  } else if (is_zero(m31) && is_zero(m32)) {
+    if (is_zero(m12)) {
+      const bool m13nz = !is_zero(m13), m21nz = !is_zero(m21), m23nz = !is_zero(m23);
+      if (m13nz) Dxx = Dxx - m13 * Dzz;
+      if (m21nz) Dyy = Dyy - m21 * Dxx;
+      if (m23nz) Dyy = Dyy - m23 * Dzz;
+    } else if (is_zero(m21)) {
+      const bool m13nz = !is_zero(m13), m23nz = !is_zero(m23);
+      if (m23nz) Dyy = Dyy - m23 * Dzz;
+      Dxx = Dxx - m12 * Dyy;
+      if (m13nz) Dxx = Dxx - m13 * Dzz;
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const bool m13z = is_zero(m13), m23z = is_zero(m23);
+      const double nDxx = Dxx, nDyy = Dyy;
+      Dxx = ((m13z ? nDxx : (nDxx - m13 * Dzz)) - m12 * (m23z ? nDyy : (nDyy - m23 * Dzz))) * idet;
+      Dyy = ((m23z ? nDyy : (nDyy - m23 * Dzz)) - m21 * (m13z ? nDxx : (nDxx - m13 * Dzz))) * idet;
+    }
+  } else {
+    const double idet = 1.0 / (1.0 + m12 * m23 * m31 + m13 * m21 * m32 - m12 * m21 - m13 * m31 - m23 * m32);
+    const double nDxx = Dxx, nDyy = Dyy, nDzz = Dzz;
+    Dxx = (nDxx * (idet * (1.0 - m23 * m32)) + nDyy * (idet * (m32 * m13 - m12)) + nDzz * (idet * (m12 * m23 - m13)));
+    Dyy = (nDxx * (idet * (m31 * m23 - m21)) + nDyy * (idet * (1.0 - m31 * m13)) + nDzz * (idet * (m21 * m13 - m23)));
+    Dzz = (nDxx * (idet * (m21 * m32 - m31)) + nDyy * (idet * (m31 * m12 - m32)) + nDzz * (idet * (1.0 - m21 * m12)));
+  }
+}
+
+// laplace(): virtual neighbours by linear interpolation, naive central second derivatives
+// ((fp-f0)/dp + (fm-f0)/dm)*2/(dp+dm), then the cross-term correction.
+template <int D>
+__device__ __forceinline__ void laplace64(const DTab64<D>& T, int64_t n, const double* __restrict__ f, double* Dv) {
+  const int64_t N = T.N;
+  const double f0 = f[n];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double fm = lin64<D>(T, 2 * a, n, f);
+    const double fp = lin64<D>(T, 2 * a + 1, n, f);
+    const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
+    Dv[a] = ((fp - f0) / dp + (fm - f0) / dm) * 2. / (dp + dm);
+  }
+  const int32_t ci = T.cidx[n];
+  if (ci >= 0) correct64<D>(T.crec + (int64_t)6 * ci, Dv);
+}
+
+// Tangential axes of the neighbour direction along `axis` (x: y,z; y: x,z; z: x,y).
+__device__ __forceinline__ int tan_axis(int axis, int j) {
+  return j == 0 ? (axis == 0 ? 1 : 0) : (axis == 2 ? 1 : 2);
+}
+
+// ngbd_with_quadratic_interpolation: f_dir -= (0.5 d_m0 d_p0 f_t1t1 [+ 0.5 d_0m d_0p f_t2t2]).
+template <int D>
+__device__ __forceinline__ double quad_nb64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f, const double* Dv) {
+  const int64_t N = T.N;
+  double v = lin64<D>(T, dir, n, f);
+  const int axis = dir >> 1;
+  if (D == 2) {
+    const double q0 = T.q[(int64_t)dir * N + n];
+    if (q0 != 0.0) v = v - q0 * Dv[tan_axis(axis, 0)];
+  } else {
+    const double q0 = T.q[(int64_t)(2 * dir) * N + n], q1 = T.q[(int64_t)(2 * dir + 1) * N + n];
+    if (q0 != 0.0 || q1 != 0.0) v = v - (q0 * Dv[tan_axis(axis, 0)] + q1 * Dv[tan_axis(axis, 1 % (D - 1))]);
+  }
+  return v;
+}
+
+__device__ __forceinline__ double interface_location(double a, double b, double fa, double fb) {
+  return 0.5 * (a + b + (a - b) * (fa + fb) / (fb - fa));
+}
+
+__device__ inline double interface_location_2nd(double a, double b, double fa, double fb, double fxxa, double fxxb) {
+  if (fabs(fa) < EPS) return a + EPS;
+  if (fabs(fb) < EPS) return b - EPS;
+  const double fxx = minmod(fxxa, fxxb);
+  const double h = b - a;
+  const double c2 = 0.5 * fxx;
+  const double c1 = (fb - fa) / h;
+  const double c0 = 0.5 * (fb + fa) - h * h / 8 * fxx;
+  double x;
+  if (fabs(c2) < EPS)
+    x = -c0 / c1;
+  else {
+    if (fb < 0)
+      x = (-2 * c0) / (c1 - sqrt(c1 * c1 - 4 * c2 * c0));
+    else
+      x = (-2 * c0) / (c1 + sqrt(c1 * c1 - 4 * c2 * c0));
+  }
+  return x + 0.5 * (a + b);
+}
+
+
+}  // namespace st64
+}  // namespace lsg

@@ -1,0 +1,88 @@
+// Flattened node-neighbour tables (host side of the flattener).
+//
+// The flattener turns the per-node quad_neighbor_nodes_of_node_t records into structure-of-arrays
+// tables, indexed [slot * N + node] so that consecutive threads read consecutive words:
+//
+//   slot = dir * HALF + k   one of the HALF face nodes of direction dir
+//
+// FP64 tables keep every quantity the reference derives from the stencil geometry with exactly the
+// reference's floating-point expressions, precomputed once per grid:
+//   w      get_linear_interpolation_weights (src/my_p4est_quad_neighbor_nodes_of_node.h:222-245):
+//          w_mm = d_p0*d_0p, w_pm = d_m0*d_0p, w_mp = d_p0*d_0m, w_pp = d_m0*d_0m (2D: d_p0, d_m0)
+//   nrm    the matching normalisation (d_m0+d_p0)*(d_0m+d_0p) (2D: d_m0+d_p0)
+//   q      the third-order neighbour correction factors 0.5*d_m0*d_p0 and 0.5*d_0m*d_0p
+//          (ngbd_with_quadratic_interpolation, .h:1514-1545)
+//   m      the second-derivative cross-term coefficients m12..m32
+//          (correct_naive_second_derivatives, src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-56)
+// Face nodes whose weight is exactly zero are dropped and the remaining ones are stored in the order
+// the reference sums them (pp, pm, mp, mm in 3D; pm, mm in 2D), so the device sum is the reference
+// sum without its +-0 terms. A slot holding -1 is unused.
+//
+// Mixed-precision tables hold the same stencil with all divisions folded into FP32 coefficients.
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+#include "neighbors.hpp"
+
+namespace lsg {
+
+// Correction record: the six cross-term coefficients (2D uses m12, m21) of one node whose stencil
+// has at least one coefficient with |m| >= EPS.
+enum { CM12 = 0, CM13 = 1, CM21 = 2, CM23 = 3, CM31 = 4, CM32 = 5 };
+
+template <int D>
+struct Tables64 {
+  static constexpr int H = Dim<D>::HALF;
+  static constexpr int NS = 2 * D * H;  // face-node slots per node
+  int64_t N = 0;
+  std::vector<int32_t> nbr;   // NS * N
+  std::vector<double> w;      // NS * N
+  std::vector<double> nrm;    // 2D * N
+  std::vector<double> d;      // 2D * N
+  std::vector<double> q;      // 2D*(D-1) * N, [dir*(D-1) + j]
+  std::vector<int32_t> cidx;  // N (-1: no cross-term correction)
+  std::vector<double> crec;   // 6 * R
+  std::vector<uint8_t> wall;  // N, bit dir set on a domain wall
+  std::vector<double> smin;   // N, min |d| over directions (CFL of advect_in_normal_direction)
+};
+
+template <int D>
+void build_tables64(const Forest<D>& F, Tables64<D>& T);
+
+template <int D>
+struct Tables32 {
+  int64_t N = 0;
+  std::vector<uint32_t> meta;  // N
+  std::vector<float> wf;       // NS * N
+  std::vector<float> d;        // 2D * N
+  std::vector<float> q;        // 2D*(D-1) * N
+  std::vector<float> corr;     // D*D * R, row-major: corrected = corr * naive
+};
+
+template <int D>
+void build_tables32(const Tables64<D>& T, Tables32<D>& M);
+
+// Cross-term coefficients of one record, exactly as correct_naive_second_derivatives computes them.
+template <int D>
+inline void cross_terms(const Qnnn<D>& q, double* m) {
+  for (int i = 0; i < 6; ++i) m[i] = 0.0;
+  // m_ab: correction of the naive second derivative along axis a by the one along axis b, built from
+  // the offsets of the two neighbours along a, in the tangential axis b.
+  auto mab = [&](int a, int j) -> double {
+    const int dm = 2 * a, dp = 2 * a + 1;
+    return q.dt[dm][2 * j] * q.dt[dm][2 * j + 1] / q.d[dm] / (q.d[dp] + q.d[dm]) +
+           q.dt[dp][2 * j] * q.dt[dp][2 * j + 1] / q.d[dp] / (q.d[dp] + q.d[dm]);
+  };
+  m[CM12] = mab(0, 0);
+  m[CM21] = mab(1, 0);
+  if (D == 3) {
+    m[CM13] = mab(0, 1);
+    m[CM23] = mab(1, 1);
+    m[CM31] = mab(2, 0);
+    m[CM32] = mab(2, 1);
+  }
+}
+
+}  // namespace lsg

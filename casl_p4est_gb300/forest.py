@@ -1,0 +1,172 @@
+"""Host grid: the p4est objects parCASL's level-set path reads, built natively (see csrc/forest.hpp).
+
+Python names mirror the parCASL calls a driver makes (examples/reinitialization/main_2d.cpp:157-188):
+
+    forest = my_p4est_brick_new(n_xyz, xyz_min, xyz_max, periodic)     # + my_p4est_new (one root per tree)
+    for _ in range(lmax): forest.refine_levelset(shape, lmin, lmax, lip) # my_p4est_refine(refine_levelset_cf)
+    forest.build_nodes()                                               # my_p4est_nodes_new
+    ngbd = my_p4est_node_neighbors_t(forest); ngbd.init_neighbors()
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Forest:
+    """p4est_t + p4est_nodes_t for one process (brick of trees, non-periodic)."""
+
+    def __init__(self, dim, n_xyz, xyz_min, xyz_max, periodic=None):
+        lib = L.load()
+        self.dim = int(dim)
+        n = (C.c_int * 3)(*(list(n_xyz) + [1] * (3 - len(n_xyz))))
+        lo = (C.c_double * 3)(*(list(xyz_min) + [0.0] * (3 - len(xyz_min))))
+        hi = (C.c_double * 3)(*(list(xyz_max) + [1.0] * (3 - len(xyz_max))))
+        per = (C.c_int * 3)(*((list(periodic) if periodic is not None else [0, 0, 0]) + [0] * 3)[:3])
+        h = C.c_void_p()
+        L.check(lib.lsg_forest_create(self.dim, n, lo, hi, per, C.byref(h)))
+        self._h = h
+        self.n_xyz = tuple(n[:3])
+        self.xyz_min = tuple(lo[:3])
+        self.xyz_max = tuple(hi[:3])
+        self.max_lvl_requested = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                L.load().lsg_forest_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- leaves -------------------------------------------------------------------------------
+    @property
+    def num_leaves(self) -> int:
+        return int(L.load().lsg_forest_num_leaves(self._h))
+
+    def leaves(self):
+        n = self.num_leaves
+        tree = np.empty(n, np.int32)
+        level = np.empty(n, np.int32)
+        xyz = np.empty((n, 3), np.int32)
+        L.check(L.load().lsg_forest_leaves(self._h, L.i32ptr(tree), L.i32ptr(level), L.i32ptr(xyz)))
+        return tree, level, xyz
+
+    def refine(self, tags):
+        tags = np.ascontiguousarray(tags, dtype=np.uint8)
+        L.check(L.load().lsg_forest_refine(self._h, L.u8ptr(tags), tags.size))
+
+    def coarsen(self, tags):
+        tags = np.ascontiguousarray(tags, dtype=np.uint8)
+        L.check(L.load().lsg_forest_coarsen(self._h, L.u8ptr(tags), tags.size))
+
+    def tag_levelset(self, shape, min_lvl, max_lvl, lip=1.2, band=0.0):
+        kind, params = shape
+        params = np.ascontiguousarray(params, np.float64)
+        tags = np.empty(self.num_leaves, np.uint8)
+        L.check(L.load().lsg_forest_tag_levelset(self._h, min_lvl, max_lvl, lip, band, kind, L.dptr(params), params.size,
+                                                 L.u8ptr(tags)))
+        return tags
+
+    def refine_levelset(self, shape, min_lvl, max_lvl, lip=1.2, band=0.0, passes=None):
+        """Repeated my_p4est_refine(refine_levelset_cf) passes (default: max_lvl passes, as the examples)."""
+        kind, params = shape
+        params = np.ascontiguousarray(params, np.float64)
+        passes = max_lvl if passes is None else passes
+        self.max_lvl_requested = max(self.max_lvl_requested, max_lvl)
+        L.check(L.load().lsg_forest_refine_levelset(self._h, min_lvl, max_lvl, lip, band, kind, L.dptr(params), params.size,
+                                                    passes))
+
+    # ---- nodes --------------------------------------------------------------------------------
+    def build_nodes(self):
+        L.check(L.load().lsg_forest_build_nodes(self._h))
+        return self
+
+    @property
+    def num_nodes(self) -> int:
+        n = int(L.load().lsg_forest_num_nodes(self._h))
+        if n < 0:
+            L.check(L.LSG_ESTATE)
+        return n
+
+    def node_xyz(self) -> np.ndarray:
+        out = np.empty((self.num_nodes, self.dim), np.float64)
+        L.check(L.load().lsg_forest_node_xyz(self._h, L.dptr(out)))
+        return out
+
+    def nodes(self):
+        n = self.num_nodes
+        tree = np.empty(n, np.int32)
+        xyz = np.empty((n, 3), np.int32)
+        L.check(L.load().lsg_forest_nodes(self._h, L.i32ptr(tree), L.i32ptr(xyz)))
+        return tree, xyz
+
+    def local_nodes(self) -> np.ndarray:
+        out = np.empty((self.num_leaves, 1 << self.dim), np.int32)
+        L.check(L.load().lsg_forest_local_nodes(self._h, L.i32ptr(out)))
+        return out
+
+    def sample(self, shape) -> np.ndarray:
+        """sample_cf_on_nodes for an analytic shape."""
+        kind, params = shape
+        params = np.ascontiguousarray(params, np.float64)
+        out = np.empty(self.num_nodes, np.float64)
+        L.check(L.load().lsg_forest_sample_shape(self._h, kind, L.dptr(params), params.size, L.dptr(out)))
+        return out
+
+    def wall_mask(self) -> np.ndarray:
+        out = np.empty(self.num_nodes, np.uint8)
+        L.check(L.load().lsg_forest_wall_mask(self._h, L.u8ptr(out)))
+        return out
+
+    def dxyz_min(self, max_lvl=None):
+        """get_dxyz_min (src/my_p4est_utils.cpp:1148-1173) for the splitting criterion's max level."""
+        lvl = self.max_lvl_requested if max_lvl is None else max_lvl
+        dx = [(self.xyz_max[a] - self.xyz_min[a]) / self.n_xyz[a] / (1 << lvl) for a in range(self.dim)]
+        return np.array(dx), min(dx), float(np.sqrt(sum(v * v for v in dx)))
+
+
+def qnnn_dtype(dim: int) -> np.dtype:
+    """numpy layout of one quad_neighbor_nodes_of_node_t record as exported by the library."""
+    h = 1 << (dim - 1)
+    dt = np.dtype([("node_000", np.int32), ("nb", np.int32, (2 * dim, h)), ("d", np.float64, (2 * dim,)),
+                   ("dt", np.float64, (2 * dim, 2 * (dim - 1))), ("inverse_d_max", np.float64)], align=True)
+    assert dt.itemsize == L.load().lsg_qnnn_record_bytes(dim), "record layout mismatch"
+    return dt
+
+
+def my_p4est_brick_new(n_xyz, xyz_min, xyz_max, periodic=None) -> Forest:
+    return Forest(len(n_xyz), n_xyz, xyz_min, xyz_max, periodic)
+
+
+class my_p4est_node_neighbors_t:
+    """Node neighbourhood of a forest (quad_neighbor_nodes_of_node_t per node)."""
+
+    def __init__(self, forest: Forest):
+        if forest.num_nodes <= 0:
+            raise ValueError("forest has no nodes")
+        self.forest = forest
+        self.dim = forest.dim
+        self._initialized = False
+
+    def init_neighbors(self):
+        self._initialized = True
+
+    def neighbors_are_initialized(self) -> bool:
+        return self._initialized
+
+    def get_neighbors(self, first=0, count=None) -> np.ndarray:
+        n = self.forest.num_nodes
+        count = n - first if count is None else count
+        dt = qnnn_dtype(self.dim)
+        out = np.zeros(count, dtype=dt)
+        L.check(L.load().lsg_forest_export_qnnn(self.forest.handle, first, count, out.ctypes.data_as(C.c_void_p), dt.itemsize))
+        return out

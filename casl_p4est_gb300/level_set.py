@@ -1,0 +1,170 @@
+"""my_p4est_level_set_t on the GPU (src/my_p4est_level_set.h:203-848, reinit + normal advection).
+
+Same method names, argument meaning and error behaviour as the reference class. A "Vec" is a numpy
+float64 array in node order (host; copied to the device inside each call) or a CUDA tensor with a
+``data_ptr()`` (device-resident; used in place). ``precision`` selects the FP64 path (evaluates the
+reference's expressions in the same order) or the mixed FP32/FP64 path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+
+import numpy as np
+
+from . import _lib as L
+from .forest import my_p4est_node_neighbors_t
+
+DBL_MAX = sys.float_info.max
+PRECISIONS = {"fp64": L.LSG_FP64, "mixed": L.LSG_MIXED}
+
+
+def _is_device(v) -> bool:
+    return hasattr(v, "data_ptr") and getattr(getattr(v, "device", None), "type", "cpu") == "cuda"
+
+
+def _host_f64(v, n, name):
+    if not isinstance(v, np.ndarray) or v.dtype != np.float64 or not v.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous float64 numpy array (or a CUDA tensor)")
+    if v.size != n:
+        raise ValueError(f"{name} has {v.size} entries, the grid has {n} nodes")
+    return v
+
+
+class my_p4est_level_set_t:
+    def __init__(self, ngbd: my_p4est_node_neighbors_t, precision: str = "fp64"):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {list(PRECISIONS)}")
+        self.ngbd = ngbd
+        self.precision = precision
+        self._h = None
+        self._build(ngbd)
+
+    def _build(self, ngbd):
+        h = C.c_void_p()
+        L.check(L.load().lsg_level_set_create(ngbd.forest.handle, C.byref(h)))
+        self._h = h
+        self.num_nodes = int(L.load().lsg_level_set_num_nodes(h))
+        self.zero_distance_threshold = float(L.load().lsg_level_set_zero_distance_threshold(h))
+
+    def update(self, ngbd: my_p4est_node_neighbors_t):
+        """my_p4est_level_set_t::update (src/my_p4est_level_set.h:416-422): rebuild the device tables."""
+        self._free()
+        self.ngbd = ngbd
+        self._build(ngbd)
+
+    def _free(self):
+        if self._h is not None and self._h.value:
+            L.load().lsg_level_set_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self._free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None):
+        L.check(L.load().lsg_level_set_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    @property
+    def stream(self) -> int:
+        return int(L.load().lsg_level_set_stream(self._h) or 0)
+
+    def _prec(self, precision):
+        return PRECISIONS[precision or self.precision]
+
+    # ---- reinitialisation -------------------------------------------------------------------
+    def reinitialize_within_range_of_phi_0(self, phi, order_space, order_pseudotime, phi_0_limit_high, phi_0_limit_low,
+                                           number_of_iterations, precision=None):
+        if order_space not in (1, 2) or order_pseudotime not in (1, 2):
+            raise ValueError("my_p4est_level_set_t::reinitialize_within_range_of_phi_0: valid orders of orders of accuracy "
+                             "for space and pseudotime are 1 and 2 only!")
+        p = self._prec(precision)
+        if _is_device(phi):
+            L.check(L.load().lsg_reinitialize_device(self._h, C.c_void_p(phi.data_ptr()), order_space, order_pseudotime,
+                                                     float(phi_0_limit_high), float(phi_0_limit_low), int(number_of_iterations), p))
+        else:
+            _host_f64(phi, self.num_nodes, "phi")
+            L.check(L.load().lsg_reinitialize(self._h, L.dptr(phi), order_space, order_pseudotime, float(phi_0_limit_high),
+                                              float(phi_0_limit_low), int(number_of_iterations), p))
+
+    def reinitialize_1st_order(self, phi, number_of_iterations=50, limit_absolute_value_phi_0=DBL_MAX, precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 1, 1, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
+                                                number_of_iterations, precision)
+
+    def reinitialize_1st_order_above_threshold(self, phi, threshold, number_of_iterations=50, upper_limit_phi_0=DBL_MAX,
+                                               precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 1, 1, upper_limit_phi_0, threshold, number_of_iterations, precision)
+
+    def reinitialize_2nd_order(self, phi, number_of_iterations=50, limit_absolute_value_phi_0=DBL_MAX, precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 2, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
+                                                number_of_iterations, precision)
+
+    def reinitialize_2nd_order_above_threshold(self, phi, threshold, number_of_iterations=50, upper_limit_phi_0=DBL_MAX,
+                                               precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 2, 2, upper_limit_phi_0, threshold, number_of_iterations, precision)
+
+    def reinitialize_2nd_order_time_1st_order_space(self, phi, number_of_iterations=50, limit_absolute_value_phi_0=DBL_MAX,
+                                                    precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 1, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
+                                                number_of_iterations, precision)
+
+    def reinitialize_1st_order_time_2nd_order_space(self, phi, number_of_iterations=50, limit_absolute_value_phi_0=DBL_MAX,
+                                                    precision=None):
+        self.reinitialize_within_range_of_phi_0(phi, 2, 1, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
+                                                number_of_iterations, precision)
+
+    # ---- normal-direction advection ----------------------------------------------------------
+    def advect_in_normal_direction(self, vn, phi, dt=None, phi_xx=None, vn_np1=None, precision=None):
+        """Forms of the reference (src/my_p4est_level_set.h:632-659):
+        - advect_in_normal_direction(vn_cf, phi[, phi_xx]) with vn a callable of node coordinates:
+          dt from CFL 0.8, returned;
+        - advect_in_normal_direction(vn, phi, dt[, phi_xx]) with node-sampled vn: returns dt;
+        - advect_in_normal_direction(vn, phi, dt, vn_np1=...) two-velocity form.
+        phi_xx, if given, is a (dim, N) float64 array overwritten with the derivatives of the
+        intermediate stage, as the reference does."""
+        p = self._prec(precision)
+        lib = L.load()
+        if callable(vn):
+            xyz = self.ngbd.forest.node_xyz()
+            vn_arr = np.ascontiguousarray(vn(xyz), dtype=np.float64)
+            dtv = C.c_double()
+            L.check(lib.lsg_advect_cfl_dt(self._h, L.dptr(vn_arr), C.byref(dtv)))
+            self.advect_in_normal_direction(vn_arr, phi, dtv.value, phi_xx=phi_xx, precision=precision)
+            return dtv.value
+        if dt is None:
+            raise ValueError("advect_in_normal_direction: dt is required with a node-sampled velocity")
+        if _is_device(phi):
+            L.check(lib.lsg_advect_in_normal_direction_device(
+                self._h, C.c_void_p(vn.data_ptr()), C.c_void_p(vn_np1.data_ptr() if vn_np1 is not None else 0),
+                C.c_void_p(phi.data_ptr()), float(dt), C.c_void_p(phi_xx.data_ptr() if phi_xx is not None else 0), p))
+            return dt
+        n = self.num_nodes
+        _host_f64(phi, n, "phi")
+        _host_f64(vn, n, "vn")
+        if vn_np1 is not None:
+            _host_f64(vn_np1, n, "vn_np1")
+        if phi_xx is not None:
+            if not (isinstance(phi_xx, np.ndarray) and phi_xx.dtype == np.float64 and phi_xx.flags.c_contiguous
+                    and phi_xx.size == self.ngbd.dim * n):
+                raise TypeError("phi_xx must be a C-contiguous float64 array of shape (dim, N)")
+        L.check(lib.lsg_advect_in_normal_direction(self._h, L.dptr(vn), L.dptr(vn_np1) if vn_np1 is not None else None,
+                                                   L.dptr(phi), float(dt), L.dptr(phi_xx) if phi_xx is not None else None, p))
+        return dt
+
+    def compute_derivatives(self, phi) -> np.ndarray:
+        """second_derivatives_central of phi: returns (dim, N)."""
+        n = self.num_nodes
+        _host_f64(phi, n, "phi")
+        out = np.empty((self.ngbd.dim, n), np.float64)
+        L.check(L.load().lsg_second_derivatives(self._h, L.dptr(phi), L.dptr(out)))
+        return out
+
+    def perturb_level_set_function(self, phi, epsilon):
+        _host_f64(phi, self.num_nodes, "phi")
+        L.check(L.load().lsg_perturb_level_set_function(self._h, L.dptr(phi), float(epsilon)))

@@ -1,0 +1,981 @@
+// ORACLE — test infrastructure only. CPU restatement of parCASL's level-set hot path, used by the
+// tests, by smoke() and by the benchmark's CPU baseline as the checker of the CUDA path. Nothing in
+// the product links, loads or calls this file.
+//
+// Plain IEEE double arithmetic compiled with -ffp-contract=off, following the reference line by line:
+//   node numbering          src/my_p4est_nodes.h:55-63, src/my_p4est_nodes.c:606-627 (every leaf corner
+//                           is a node, owned by the lowest tree, clamped, sorted by (tree, Morton))
+//   cell tree / point location  src/my_p4est_hierarchy.h:142-152, src/my_p4est_hierarchy.cpp:264-600
+//   construct_neighbors     src/my_p4est_node_neighbors.cpp:114-1201
+//   walls                   src/my_p4est_utils.cpp:1815-1905
+//   linear interpolation, laplace, second-derivative correction, quadratic neighbours
+//                           src/my_p4est_quad_neighbor_nodes_of_node.h:214-245, 290-306, 513-524,
+//                           615-635, 1514-1545; .cpp:44-298
+//   interface location      src/casl_math.cpp:55-97, MINMOD src/casl_math.h:80-88
+//   reinitialisation        src/my_p4est_level_set.cpp:59-557
+//   normal advection        src/my_p4est_level_set.cpp:559-815
+//   node interpolation      src/my_p4est_utils.cpp:367-576, src/my_p4est_interpolation_nodes.cpp:107-288,
+//                           src/my_p4est_hierarchy.cpp:264-567, src/my_p4est_utils.h:2177-2187
+//   semi-Lagrangian step    src/my_p4est_semi_lagrangian.cpp:148-223
+// Parity is pinned by analytic known answers and convergence orders (the reference has no value-level
+// golden vectors for this path and cannot be built here: p4est/PETSc/MPI are absent).
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#define ORA_EPS 1e-13
+
+namespace {
+
+std::string g_err;
+
+inline double MINMOD(double a, double b) {
+  if (a * b <= 0) return 0;
+  if ((fabs(a)) < (fabs(b))) return a;
+  return b;
+}
+template <typename T>
+inline const T& MIN(const T& a, const T& b) { return a < b ? a : b; }
+template <typename T>
+inline const T& MIN(const T& a, const T& b, const T& c) { return a < b ? MIN(a, c) : MIN(b, c); }
+template <typename T>
+inline const T& MAX(const T& a, const T& b) { return b < a ? a : b; }
+template <typename T>
+inline const T& MAX(const T& a, const T& b, const T& c) { return b < a ? MAX(a, c) : MAX(b, c); }
+
+// ---------------------------------------------------------------------------------------------
+// record layout identical to the product export (include/lsgpu.h, lsg_forest_export_qnnn)
+template <int D>
+struct Qnnn {
+  int32_t node_000;
+  int32_t nb[2 * D][1 << (D - 1)];
+  double d[2 * D];
+  double dt[2 * D][2 * (D - 1)];
+  double inverse_d_max;
+};
+
+struct Leaf {
+  int32_t tree, level, x[3];
+};
+
+struct Cell {  // HierarchyCell: child = -1 for a leaf
+  int32_t child;
+  int32_t quad;
+  int32_t imin[3];
+  int32_t level;
+};
+
+template <int D>
+struct Grid {
+  static constexpr int MAXLEVEL = (D == 2 ? 30 : 19);
+  static constexpr int64_t ROOT_LEN = int64_t(1) << MAXLEVEL;
+  static constexpr int CH = 1 << D;
+  int n[3];
+  double xyz_min[3], xyz_max[3];
+  std::vector<int> tree_ijk;                 // 3 per tree
+  std::vector<int> ijk_to_tree;
+  std::vector<double> tv_min, tv_max;         // 3 per tree
+  std::vector<Leaf> leaves;
+  std::vector<std::vector<Cell>> cells;       // per tree
+  // nodes
+  std::vector<int32_t> node_tree;
+  std::vector<int64_t> node_x;                // D per node, clamped
+  std::vector<int32_t> local_nodes;
+  std::vector<Qnnn<D>> qnnn;
+  std::vector<uint8_t> wall;
+  double tree_dim[3];
+
+  int32_t tree_at(int i, int j, int k) const { return ijk_to_tree[(size_t)n[0] * n[1] * k + (size_t)n[0] * j + i]; }
+};
+
+uint64_t interleave(const int64_t* x, int D) {
+  uint64_t key = 0;
+  const int bits = (D == 2 ? 30 : 19);
+  for (int b = 0; b < bits; ++b)
+    for (int a = 0; a < D; ++a) key |= (uint64_t)((x[a] >> b) & 1) << (D * b + a);
+  return key;
+}
+
+template <int D>
+void setup_brick(Grid<D>& g, const int* n, const double* lo, const double* hi) {
+  for (int a = 0; a < 3; ++a) {
+    g.n[a] = a < D ? n[a] : 1;
+    g.xyz_min[a] = a < D ? lo[a] : 0;
+    g.xyz_max[a] = a < D ? hi[a] : 0;
+  }
+  const int nt = g.n[0] * g.n[1] * g.n[2];
+  // trees along a Morton curve of their brick position
+  std::vector<std::pair<uint64_t, int>> order;
+  for (int k = 0; k < g.n[2]; ++k)
+    for (int j = 0; j < g.n[1]; ++j)
+      for (int i = 0; i < g.n[0]; ++i) {
+        int64_t c[3] = {i, j, k};
+        uint64_t key = 0;
+        for (int b = 0; b < 20; ++b)
+          for (int a = 0; a < 3; ++a) key |= (uint64_t)((c[a] >> b) & 1) << (3 * b + a);
+        order.push_back({key, g.n[0] * g.n[1] * k + g.n[0] * j + i});
+      }
+  std::sort(order.begin(), order.end());
+  g.tree_ijk.assign(3 * nt, 0);
+  g.ijk_to_tree.assign(nt, 0);
+  g.tv_min.assign(3 * nt, 0);
+  g.tv_max.assign(3 * nt, 0);
+  double dxyz[3];
+  for (int a = 0; a < 3; ++a) dxyz[a] = (g.xyz_max[a] - g.xyz_min[a]) / (double)g.n[a];
+  for (int t = 0; t < nt; ++t) {
+    const int lin = order[t].second;
+    const int ijk[3] = {lin % g.n[0], (lin / g.n[0]) % g.n[1], lin / (g.n[0] * g.n[1])};
+    g.ijk_to_tree[lin] = t;
+    for (int a = 0; a < 3; ++a) {
+      g.tree_ijk[3 * t + a] = ijk[a];
+      if (a < D) {
+        g.tv_min[3 * t + a] = g.xyz_min[a] + (ijk[a] + 0) * dxyz[a];
+        g.tv_max[3 * t + a] = g.xyz_min[a] + (ijk[a] + 1) * dxyz[a];
+      }
+    }
+  }
+  for (int a = 0; a < D; ++a) g.tree_dim[a] = (g.xyz_max[a] - g.xyz_min[a]) / g.n[a];
+}
+
+// ---- hierarchy: explicit cell tree per tree (HierarchyCell) ----------------------------------
+template <int D>
+void build_hierarchy(Grid<D>& g) {
+  const int nt = g.n[0] * g.n[1] * g.n[2];
+  g.cells.assign(nt, std::vector<Cell>());
+  for (int t = 0; t < nt; ++t) {
+    Cell root;
+    root.child = -1;
+    root.quad = -1;
+    root.imin[0] = root.imin[1] = root.imin[2] = 0;
+    root.level = 0;
+    g.cells[t].push_back(root);
+  }
+  for (size_t q = 0; q < g.leaves.size(); ++q) {
+    const Leaf& L = g.leaves[q];
+    std::vector<Cell>& C = g.cells[L.tree];
+    int ind = 0;
+    while (C[ind].level < L.level) {
+      if (C[ind].child < 0) {
+        const int first = (int)C.size();
+        const int64_t h = Grid<D>::ROOT_LEN >> (C[ind].level + 1);
+        for (int c = 0; c < Grid<D>::CH; ++c) {
+          Cell ch;
+          ch.child = -1;
+          ch.quad = -1;
+          ch.level = C[ind].level + 1;
+          for (int a = 0; a < 3; ++a) ch.imin[a] = C[ind].imin[a] + (a < D && ((c >> a) & 1) ? (int32_t)h : 0);
+          C.push_back(ch);
+        }
+        C[ind].child = first;
+      }
+      const int64_t half = Grid<D>::ROOT_LEN >> (C[ind].level + 1);
+      int c = 0;
+      for (int a = 0; a < D; ++a) c |= (L.x[a] >= C[ind].imin[a] + half ? 1 : 0) << a;
+      ind = C[ind].child + c;
+    }
+    C[ind].quad = (int32_t)q;
+  }
+}
+
+// descend with logical (possibly non-integer) coordinates; returns the leaf quad index
+template <int D>
+int32_t descend(const Grid<D>& g, int tree, const double* s) {
+  const std::vector<Cell>& C = g.cells[tree];
+  int ind = 0;
+  while (C[ind].child >= 0) {
+    const int64_t half = Grid<D>::ROOT_LEN >> (C[ind].level + 1);
+    int c = 0;
+    for (int a = 0; a < D; ++a) c |= (s[a] >= (double)(C[ind].imin[a] + half) ? 1 : 0) << a;
+    ind = C[ind].child + c;
+  }
+  return C[ind].quad;
+}
+
+// ---- nodes -----------------------------------------------------------------------------------
+template <int D>
+void build_nodes(Grid<D>& g) {
+  typedef std::pair<int32_t, uint64_t> Key;
+  std::map<Key, int32_t> idx;
+  std::vector<Key> corner_keys(g.leaves.size() * Grid<D>::CH);
+  std::vector<std::pair<int32_t, std::vector<int64_t>>> node_data;
+  for (size_t q = 0; q < g.leaves.size(); ++q) {
+    const Leaf& L = g.leaves[q];
+    const int64_t h = Grid<D>::ROOT_LEN >> L.level;
+    for (int c = 0; c < Grid<D>::CH; ++c) {
+      int64_t G[3] = {0, 0, 0};
+      for (int a = 0; a < D; ++a) G[a] = (int64_t)g.tree_ijk[3 * L.tree + a] * Grid<D>::ROOT_LEN + L.x[a] + (((c >> a) & 1) ? h : 0);
+      // owner: lowest tree id among trees containing the point
+      int32_t owner = -1;
+      int oijk[3] = {0, 0, 0};
+      int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+      for (int a = 0; a < D; ++a) {
+        const int64_t Lx = (int64_t)g.n[a] * Grid<D>::ROOT_LEN;
+        int64_t t = G[a] / Grid<D>::ROOT_LEN;
+        if (G[a] == Lx) lo[a] = hi[a] = (int)t - 1;
+        else if (G[a] % Grid<D>::ROOT_LEN == 0 && G[a] > 0) {
+          lo[a] = (int)t - 1;
+          hi[a] = (int)t;
+        } else lo[a] = hi[a] = (int)t;
+      }
+      for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+          for (int i = lo[0]; i <= hi[0]; ++i) {
+            const int32_t t = g.tree_at(i, j, k);
+            if (owner < 0 || t < owner) {
+              owner = t;
+              oijk[0] = i;
+              oijk[1] = j;
+              oijk[2] = k;
+            }
+          }
+      std::vector<int64_t> xl(D);
+      for (int a = 0; a < D; ++a) {
+        int64_t v = G[a] - (int64_t)oijk[a] * Grid<D>::ROOT_LEN;
+        if (v == Grid<D>::ROOT_LEN) v = Grid<D>::ROOT_LEN - 1;
+        xl[a] = v;
+      }
+      const Key key(owner, interleave(xl.data(), D));
+      corner_keys[q * Grid<D>::CH + c] = key;
+      if (!idx.count(key)) {
+        idx[key] = 0;
+        node_data.push_back({owner, xl});
+      }
+    }
+  }
+  // (tree, Morton) order
+  int32_t k = 0;
+  for (auto& kv : idx) kv.second = k++;
+  g.node_tree.assign(idx.size(), 0);
+  g.node_x.assign(idx.size() * D, 0);
+  for (auto& nd : node_data) {
+    const Key key(nd.first, interleave(nd.second.data(), D));
+    const int32_t i = idx[key];
+    g.node_tree[i] = nd.first;
+    for (int a = 0; a < D; ++a) g.node_x[(size_t)i * D + a] = nd.second[a];
+  }
+  g.local_nodes.assign(g.leaves.size() * Grid<D>::CH, 0);
+  for (size_t i = 0; i < corner_keys.size(); ++i) g.local_nodes[i] = idx[corner_keys[i]];
+}
+
+// ---- construct_neighbors ----------------------------------------------------------------------
+template <int D>
+void unclamped(const Grid<D>& g, int32_t n, int64_t* x) {
+  for (int a = 0; a < D; ++a) {
+    int64_t v = g.node_x[(size_t)n * D + a];
+    x[a] = (v == Grid<D>::ROOT_LEN - 1) ? Grid<D>::ROOT_LEN : v;
+  }
+}
+
+// find_neighbor_cell_of_node: perturbed node, is_node_in_domain, descend the owning tree
+template <int D>
+int32_t find_neighbor_cell_of_node(const Grid<D>& g, int32_t n, const int* c) {
+  int64_t x[3] = {0, 0, 0};
+  unclamped(g, n, x);
+  const int t = g.node_tree[n];
+  int ijk[3] = {0, 0, 0};
+  double s[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    int64_t G = (int64_t)g.tree_ijk[3 * t + a] * Grid<D>::ROOT_LEN + x[a] + c[a];
+    if (G < 0 || G >= (int64_t)g.n[a] * Grid<D>::ROOT_LEN) return -1;
+    ijk[a] = (int)(G / Grid<D>::ROOT_LEN);
+    s[a] = (double)(G - (int64_t)ijk[a] * Grid<D>::ROOT_LEN);
+  }
+  return descend(g, g.tree_at(ijk[0], ijk[1], D == 3 ? ijk[2] : 0), s);
+}
+
+template <int D>
+void neighbor_offsets(const Grid<D>& g, const Leaf& Q, int axis, const double* c, double* out) {
+  int tan[2];
+  int j = 0;
+  for (int a = 0; a < D; ++a)
+    if (a != axis) tan[j++] = a;
+  const double qh = (double)(Grid<D>::ROOT_LEN >> Q.level) / (double)Grid<D>::ROOT_LEN;
+  for (int jj = 0; jj < D - 1; ++jj) {
+    const int t = tan[jj];
+    const double tmin = g.tv_min[3 * Q.tree + t], tmax = g.tv_max[3 * Q.tree + t];
+    const double thr = (tmax - tmin) * ((double)1) / ((double)Grid<D>::ROOT_LEN);
+    const double q = (tmax - tmin) * (Q.x[t] / (double)Grid<D>::ROOT_LEN) + tmin;
+    double m0 = ((fabs(c[t] - q) > thr) ? (c[t] - q) : 0.0);
+    double p0 = ((fabs((tmax - tmin) * qh - m0) > thr) ? ((tmax - tmin) * qh - m0) : 0.0);
+    out[2 * jj] = m0;
+    out[2 * jj + 1] = p0;
+  }
+}
+
+template <int D>
+int corner_of(int axis, int abit, int k) {
+  int tan[2];
+  int j = 0;
+  for (int a = 0; a < D; ++a)
+    if (a != axis) tan[j++] = a;
+  int c = abit << axis;
+  c |= (k & 1) << tan[0];
+  if (D == 3) c |= ((k >> 1) & 1) << tan[1];
+  return c;
+}
+
+template <int D>
+bool construct_neighbors(const Grid<D>& g, int32_t n, Qnnn<D>& q) {
+  const int CH = Grid<D>::CH;
+  memset(&q, 0, sizeof(q));
+  int64_t xu[3] = {0, 0, 0};
+  unclamped(g, n, xu);
+  const int t = g.node_tree[n];
+  double c[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a)
+    c[a] = (g.tv_max[3 * t + a] - g.tv_min[3 * t + a]) * (xu[a] / (double)Grid<D>::ROOT_LEN) + g.tv_min[3 * t + a];
+  int32_t cell[8];
+  for (int v = 0; v < CH; ++v) {
+    int dir[3];
+    for (int a = 0; a < D; ++a) dir[a] = ((v >> a) & 1) ? 1 : -1;
+    cell[v] = find_neighbor_cell_of_node(g, n, dir);
+  }
+  auto level = [&](int32_t quad) { return quad < 0 ? -1 : g.leaves[quad].level; };
+  q.node_000 = n;
+  bool is_wall[6] = {false, false, false, false, false, false};
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int axis = dir / 2, side = dir % 2;
+    int32_t best = -1;
+    for (int v = 0; v < CH; ++v)
+      if (((v >> axis) & 1) == side && level(best) < level(cell[v])) best = cell[v];
+    if (best < 0) {
+      is_wall[dir] = true;
+      continue;
+    }
+    const Leaf& Q = g.leaves[best];
+    q.d[dir] = (g.tv_max[3 * Q.tree + axis] - g.tv_min[3 * Q.tree + axis]) * ((double)(Grid<D>::ROOT_LEN >> Q.level) / (double)Grid<D>::ROOT_LEN);
+    for (int k = 0; k < (1 << (D - 1)); ++k) q.nb[dir][k] = g.local_nodes[(size_t)CH * best + corner_of<D>(axis, side, k)];
+    neighbor_offsets(g, Q, axis, c, q.dt[dir]);
+  }
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    if (!is_wall[dir]) continue;
+    const int axis = dir / 2, side = dir % 2, other = 1 - side;
+    int32_t qmin = -1;
+    int cv[3] = {-1, -1, -1};
+    for (int v = 0; v < CH; ++v)
+      if (((v >> axis) & 1) == other && level(qmin) < level(cell[v])) {
+        qmin = cell[v];
+        for (int a = 0; a < D; ++a) cv[a] = ((v >> a) & 1) ? 1 : -1;
+      }
+    if (qmin < 0) return true;
+    int corner = 0;
+    for (int a = 0; a < D; ++a) corner |= (a == axis ? other : (cv[a] != 1)) << a;
+    const int32_t ntmp = g.local_nodes[(size_t)CH * qmin + corner];
+    const int32_t qtmp = find_neighbor_cell_of_node(g, ntmp, cv);
+    if (qtmp < 0) return true;
+    const Leaf& Q = g.leaves[qtmp];
+    q.d[dir] = -q.d[2 * axis + other] -
+               (g.tv_max[3 * Q.tree + axis] - g.tv_min[3 * Q.tree + axis]) * ((double)(Grid<D>::ROOT_LEN >> Q.level) / (double)Grid<D>::ROOT_LEN);
+    for (int k = 0; k < (1 << (D - 1)); ++k) q.nb[dir][k] = g.local_nodes[(size_t)CH * qtmp + corner_of<D>(axis, other, k)];
+    neighbor_offsets(g, Q, axis, c, q.dt[dir]);
+  }
+  double m = MAX(q.d[0], q.d[1]);
+  m = MAX(m, q.d[2], q.d[3]);
+  if (D == 3) m = MAX(m, q.d[4], q.d[5]);
+  m = MAX(m, q.dt[0][0], q.dt[0][1]);
+  m = MAX(m, q.dt[1][0], q.dt[1][1]);
+  m = MAX(m, q.dt[2][0], q.dt[2][1]);
+  m = MAX(m, q.dt[3][0], q.dt[3][1]);
+  if (D == 3) {
+    m = MAX(m, q.dt[0][2], q.dt[0][3]);
+    m = MAX(m, q.dt[1][2], q.dt[1][3]);
+    m = MAX(m, q.dt[2][2], q.dt[2][3]);
+    m = MAX(m, q.dt[3][2], q.dt[3][3]);
+    m = MAX(m, q.dt[4][0], q.dt[4][1]);
+    m = MAX(m, q.dt[4][2], q.dt[5][3]);  // d_00m_0m with d_00p_0p, as the reference
+    m = MAX(m, q.dt[5][0], q.dt[5][1]);
+    m = MAX(m, q.dt[5][2], q.dt[5][3]);
+  }
+  q.inverse_d_max = 1.0 / m;
+  return false;
+}
+
+template <int D>
+uint8_t wall_of(const Grid<D>& g, int32_t n) {
+  uint8_t w = 0;
+  const int t = g.node_tree[n];
+  for (int a = 0; a < D; ++a) {
+    const int64_t v = g.node_x[(size_t)n * D + a];
+    if (v == 0 && g.tree_ijk[3 * t + a] == 0) w |= 1 << (2 * a);
+    if ((v == Grid<D>::ROOT_LEN - 1 || v == Grid<D>::ROOT_LEN) && g.tree_ijk[3 * t + a] == g.n[a] - 1) w |= 1 << (2 * a + 1);
+  }
+  return w;
+}
+
+// ---- quad_neighbor_nodes_of_node_t arithmetic ---------------------------------------------------
+// interpolate_linearly over the face nodes of direction dir
+template <int D>
+double f_linear(const Qnnn<D>& q, int dir, const double* f) {
+  const double d_m0 = q.dt[dir][0], d_p0 = q.dt[dir][1];
+  if (D == 2) {
+    const double w_mm = d_p0, w_pm = d_m0, normalization = d_m0 + d_p0;
+    return (f[q.nb[dir][1]] * w_pm + f[q.nb[dir][0]] * w_mm) / normalization;
+  }
+  const double d_0m = q.dt[dir][2], d_0p = q.dt[dir][3];
+  const double w_mm = d_p0 * d_0p, w_pm = d_m0 * d_0p, w_mp = d_p0 * d_0m, w_pp = d_m0 * d_0m;
+  const double normalization = (d_m0 + d_p0) * (d_0m + d_0p);
+  return (f[q.nb[dir][3]] * w_pp + f[q.nb[dir][1]] * w_pm + f[q.nb[dir][2]] * w_mp + f[q.nb[dir][0]] * w_mm) / normalization;
+}
+
+inline double central_second_derivative(double fp, double f0, double fm, double dp, double dm) {
+  return ((fp - f0) / dp + (fm - f0) / dm) * 2. / (dp + dm);
+}
+inline bool check_if_zero(double v) { return fabs(v) < ORA_EPS; }
+
+template <int D>
+void correct_naive_second_derivatives(const Qnnn<D>& q, double* Dxx, double* Dyy, double* Dzz) {
+  const double d_m00 = q.d[0], d_p00 = q.d[1], d_0m0 = q.d[2], d_0p0 = q.d[3];
+  const double m12 = q.dt[0][0] * q.dt[0][1] / d_m00 / (d_p00 + d_m00) + q.dt[1][0] * q.dt[1][1] / d_p00 / (d_p00 + d_m00);
+  const double m21 = q.dt[2][0] * q.dt[2][1] / d_0m0 / (d_0p0 + d_0m0) + q.dt[3][0] * q.dt[3][1] / d_0p0 / (d_0p0 + d_0m0);
+  if (D == 2) {
+    if (check_if_zero(m12)) {
+      if (!check_if_zero(m21)) *Dyy -= m21 * *Dxx;
+    } else if (check_if_zero(m21)) {
+      *Dxx -= m12 * *Dyy;
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const double nDxx = *Dxx, nDyy = *Dyy;
+      *Dxx = nDxx * idet - nDyy * (m12 * idet);
+      *Dyy = nDyy * idet - nDxx * (m21 * idet);
+    }
+    return;
+  }
+  const double d_00m = q.d[D == 3 ? 4 : 0], d_00p = q.d[D == 3 ? 5 : 0];
+  const int i4 = D == 3 ? 4 : 0, i5 = D == 3 ? 5 : 0, j2 = D == 3 ? 2 : 0, j3 = D == 3 ? 3 : 0;
+  const double m13 = q.dt[0][j2] * q.dt[0][j3] / d_m00 / (d_p00 + d_m00) + q.dt[1][j2] * q.dt[1][j3] / d_p00 / (d_p00 + d_m00);
+  const double m23 = q.dt[2][j2] * q.dt[2][j3] / d_0m0 / (d_0p0 + d_0m0) + q.dt[3][j2] * q.dt[3][j3] / d_0p0 / (d_0p0 + d_0m0);
+  const double m31 = q.dt[i4][0] * q.dt[i4][1] / d_00m / (d_00p + d_00m) + q.dt[i5][0] * q.dt[i5][1] / d_00p / (d_00p + d_00m);
+  const double m32 = q.dt[i4][j2] * q.dt[i4][j3] / d_00m / (d_00p + d_00m) + q.dt[i5][j2] * q.dt[i5][j3] / d_00p / (d_00p + d_00m);
+  double &xx = *Dxx, &yy = *Dyy, &zz = *Dzz;
+  if (check_if_zero(m12) && check_if_zero(m13)) {
+    if (check_if_zero(m23)) {
+      const bool a = !check_if_zero(m21), b = !check_if_zero(m31), c = !check_if_zero(m32);
+      if (a) yy -= m21 * xx;
+      if (b) zz -= m31 * xx;
+      if (c) zz -= m32 * yy;
+    } else if (check_if_zero(m32)) {
+      const bool a = !check_if_zero(m21), b = !check_if_zero(m31);
+      if (b) zz -= m31 * xx;
+      yy -= m23 * zz;
+      if (a) yy -= m21 * xx;
+    } else {
+      const double idet = 1.0 / (1.0 - m23 * m32);
+      const bool a = check_if_zero(m21), b = check_if_zero(m31);
+      const double ny = yy, nz = zz;
+      yy = ((a ? ny : (ny - m21 * xx)) - m23 * (b ? nz : (nz - m31 * xx))) * idet;
+      zz = ((b ? nz : (nz - m31 * xx)) - m32 * (a ? ny : (ny - m21 * xx))) * idet;
+    }
+  } else if (check_if_zero(m21) && check_if_zero(m23)) {
+    if (check_if_zero(m13)) {
+      const bool a = !check_if_zero(m12), b = !check_if_zero(m31), c = !check_if_zero(m32);
+      if (a) xx -= m12 * yy;
+      if (b) zz -= m31 * xx;
+      if (c) zz -= m32 * yy;
+    } else if (check_if_zero(m31)) {
+      const bool a = !check_if_zero(m12), c = !check_if_zero(m32);
+      if (c) zz -= m32 * yy;
+      xx -= m13 * zz;
+      if (a) xx -= m12 * yy;
+    } else {
+      const double idet = 1.0 / (1.0 - m13 * m31);
+      const bool a = check_if_zero(m12), c = check_if_zero(m32);
+      const double nx = xx, nz = zz;
+      xx = ((a ? nx : (nx - m12 * yy)) - m13 * (c ? nz : (nz - m32 * yy))) * idet;
+      zz = ((c ? nz : (nz - m32 * yy)) - m31 * (a ? nx : (nx - m12 * yy))) * idet;
+    }
+  } else if (check_if_zero(m31) && check_if_zero(m32)) {
+    if (check_if_zero(m12)) {
+      const bool a = !check_if_zero(m13), b = !check_if_zero(m21), c = !check_if_zero(m23);
+      if (a) xx -= m13 * zz;
+      if (b) yy -= m21 * xx;
+      if (c) yy -= m23 * zz;
+    } else if (check_if_zero(m21)) {
+      const bool a = !check_if_zero(m13), c = !check_if_zero(m23);
+      if (c) yy -= m23 * zz;
+      xx -= m12 * yy;
+      if (a) xx -= m13 * zz;
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const bool a = check_if_zero(m13), c = check_if_zero(m23);
+      const double nx = xx, ny = yy;
+      xx = ((a ? nx : (nx - m13 * zz)) - m12 * (c ? ny : (ny - m23 * zz))) * idet;
+      yy = ((c ? ny : (ny - m23 * zz)) - m21 * (a ? nx : (nx - m13 * zz))) * idet;
+    }
+  } else {
+    const double idet = 1.0 / (1.0 + m12 * m23 * m31 + m13 * m21 * m32 - m12 * m21 - m13 * m31 - m23 * m32);
+    const double nx = xx, ny = yy, nz = zz;
+    xx = (nx * (idet * (1.0 - m23 * m32)) + ny * (idet * (m32 * m13 - m12)) + nz * (idet * (m12 * m23 - m13)));
+    yy = (nx * (idet * (m31 * m23 - m21)) + ny * (idet * (1.0 - m31 * m13)) + nz * (idet * (m21 * m13 - m23)));
+    zz = (nx * (idet * (m21 * m32 - m31)) + ny * (idet * (m31 * m12 - m32)) + nz * (idet * (1.0 - m21 * m12)));
+  }
+}
+
+// laplace: neighbour values f_nb[2D] and corrected second derivatives fdd[D]
+template <int D>
+void laplace(const Qnnn<D>& q, const double* f, double* f_000, double* f_nb, double* fdd) {
+  *f_000 = f[q.node_000];
+  f_nb[1] = f_linear(q, 1, f);
+  f_nb[0] = f_linear(q, 0, f);
+  f_nb[3] = f_linear(q, 3, f);
+  f_nb[2] = f_linear(q, 2, f);
+  if (D == 3) {
+    f_nb[D == 3 ? 5 : 0] = f_linear(q, D == 3 ? 5 : 0, f);
+    f_nb[D == 3 ? 4 : 0] = f_linear(q, D == 3 ? 4 : 0, f);
+  }
+  for (int a = 0; a < D; ++a) fdd[a] = central_second_derivative(f_nb[2 * a + 1], *f_000, f_nb[2 * a], q.d[2 * a + 1], q.d[2 * a]);
+  double dummy = 0;
+  correct_naive_second_derivatives(q, &fdd[0], &fdd[1], D == 3 ? &fdd[D == 3 ? 2 : 0] : &dummy);
+}
+
+// ngbd_with_quadratic_interpolation
+template <int D>
+void ngbd_quadratic(const Qnnn<D>& q, const double* f, double* f_000, double* f_nb) {
+  double fdd[3] = {0, 0, 0};
+  laplace(q, f, f_000, f_nb, fdd);
+  const double fxx = fdd[0], fyy = fdd[1], fzz = fdd[2];
+  if (D == 2) {
+    f_nb[0] -= (0.5 * q.dt[0][0] * q.dt[0][1] * fyy);
+    f_nb[1] -= (0.5 * q.dt[1][0] * q.dt[1][1] * fyy);
+    f_nb[2] -= (0.5 * q.dt[2][0] * q.dt[2][1] * fxx);
+    f_nb[3] -= (0.5 * q.dt[3][0] * q.dt[3][1] * fxx);
+  } else {
+    const int j2 = D == 3 ? 2 : 0, j3 = D == 3 ? 3 : 0, i4 = D == 3 ? 4 : 0, i5 = D == 3 ? 5 : 0;
+    f_nb[0] -= (0.5 * q.dt[0][0] * q.dt[0][1] * fyy + 0.5 * q.dt[0][j2] * q.dt[0][j3] * fzz);
+    f_nb[1] -= (0.5 * q.dt[1][0] * q.dt[1][1] * fyy + 0.5 * q.dt[1][j2] * q.dt[1][j3] * fzz);
+    f_nb[2] -= (0.5 * q.dt[2][0] * q.dt[2][1] * fxx + 0.5 * q.dt[2][j2] * q.dt[2][j3] * fzz);
+    f_nb[3] -= (0.5 * q.dt[3][0] * q.dt[3][1] * fxx + 0.5 * q.dt[3][j2] * q.dt[3][j3] * fzz);
+    f_nb[i4] -= (0.5 * q.dt[i4][0] * q.dt[i4][1] * fxx + 0.5 * q.dt[i4][j2] * q.dt[i4][j3] * fyy);
+    f_nb[i5] -= (0.5 * q.dt[i5][0] * q.dt[i5][1] * fxx + 0.5 * q.dt[i5][j2] * q.dt[i5][j3] * fyy);
+  }
+}
+
+double interface_Location(double a, double b, double fa, double fb) { return 0.5 * (a + b + (a - b) * (fa + fb) / (fb - fa)); }
+
+double interface_Location_With_Second_Order_Derivative(double a, double b, double fa, double fb, double fxxa, double fxxb) {
+  if (fabs(fa) < ORA_EPS) return a + ORA_EPS;
+  if (fabs(fb) < ORA_EPS) return b - ORA_EPS;
+  double fxx = MINMOD(fxxa, fxxb);
+  double h = b - a;
+  double c2 = 0.5 * fxx;
+  double c1 = (fb - fa) / h;
+  double c0 = 0.5 * (fb + fa) - h * h / 8 * fxx;
+  double x;
+  if (fabs(c2) < ORA_EPS)
+    x = -c0 / c1;
+  else {
+    if (fb < 0)
+      x = (-2 * c0) / (c1 - sqrt(c1 * c1 - 4 * c2 * c0));
+    else
+      x = (-2 * c0) / (c1 + sqrt(c1 * c1 - 4 * c2 * c0));
+  }
+  return x + 0.5 * (a + b);
+}
+
+struct Ctx {
+  int dim;
+  int64_t N;
+  void* qnnn;        // Qnnn<D>* (owned or borrowed)
+  const uint8_t* wall;
+  double zero_distance_threshold;
+  void* grid;        // Grid<D>* when built from leaves
+  std::vector<uint8_t> wall_store;
+  std::vector<char> qnnn_store;
+};
+
+// reinitialize_one_iteration (src/my_p4est_level_set.cpp:59-288)
+template <int D>
+void reinitialize_one_iteration(const Ctx& cx, double* phi_np1, const double* phi_0, const double* phi_n, double limit_high_,
+                                double limit_low_, const double* phi_0_dd, const double* phi_n_dd, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const bool second_order = phi_0_dd != nullptr && phi_n_dd != nullptr;
+  const double zdt = cx.zero_distance_threshold;
+  double big = 1.0;
+  while (DBL_MAX - big == DBL_MAX) big *= 2.0;
+  big = DBL_MAX - big;
+  const double low = (limit_low_ < -big ? -DBL_MAX : limit_low_ - MAX(zdt, ORA_EPS * fabs(limit_low_)));
+  const double high = (limit_high_ > big ? DBL_MAX : limit_high_ + MAX(zdt, ORA_EPS * fabs(limit_high_)));
+  const int64_t N = cx.N;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long k = 0; k < (long long)N; ++k) {
+    const int64_t n = k;
+    if (fabs(phi_0[n]) < zdt) {
+      phi_np1[n] = 0.0;
+      continue;
+    }
+    if (!(low < phi_0[n] && phi_0[n] < high)) {
+      phi_np1[n] = phi_0[n];
+      continue;
+    }
+    const Qnnn<D>& q = Q[n];
+    double p0_000, p0_nb[6], pn_000, pn_nb[6];
+    ngbd_quadratic(q, phi_0, &p0_000, p0_nb);
+    ngbd_quadratic(q, phi_n, &pn_000, pn_nb);
+    double s[6];
+    for (int dir = 0; dir < 2 * D; ++dir) s[dir] = q.d[dir];
+    double xx_000[3] = {NAN, NAN, NAN}, xx_nb[6] = {NAN, NAN, NAN, NAN, NAN, NAN};
+    if (second_order) {
+      for (int a = 0; a < D; ++a) {
+        xx_000[a] = phi_n_dd[(size_t)a * N + n];
+        xx_nb[2 * a] = f_linear(q, 2 * a, phi_n_dd + (size_t)a * N);
+        xx_nb[2 * a + 1] = f_linear(q, 2 * a + 1, phi_n_dd + (size_t)a * N);
+      }
+    }
+    bool near = false;
+    for (int dir = 0; dir < 2 * D; ++dir) near = near || (p0_000 * p0_nb[dir] < 0.0);
+    if (near) {
+      double x0_000[3] = {NAN, NAN, NAN}, x0_nb[6] = {NAN, NAN, NAN, NAN, NAN, NAN};
+      if (second_order)
+        for (int a = 0; a < D; ++a) {
+          x0_000[a] = phi_0_dd[(size_t)a * N + n];
+          x0_nb[2 * a] = f_linear(q, 2 * a, phi_0_dd + (size_t)a * N);
+          x0_nb[2 * a + 1] = f_linear(q, 2 * a + 1, phi_0_dd + (size_t)a * N);
+        }
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        if (!(p0_000 * p0_nb[dir] < 0.0)) continue;
+        const int a = dir / 2;
+        if (dir % 2 == 0) {
+          if (second_order)
+            s[dir] = -interface_Location_With_Second_Order_Derivative(-s[dir], 0.0, p0_nb[dir], p0_000, x0_nb[dir], x0_000[a]);
+          else
+            s[dir] = -interface_Location(-s[dir], 0.0, p0_nb[dir], p0_000);
+        } else {
+          if (second_order)
+            s[dir] = interface_Location_With_Second_Order_Derivative(0.0, s[dir], p0_000, p0_nb[dir], x0_000[a], x0_nb[dir]);
+          else
+            s[dir] = interface_Location(0.0, s[dir], p0_000, p0_nb[dir]);
+        }
+        pn_nb[dir] = 0.0;
+      }
+      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = MAX(s[dir], zdt);
+    }
+    const uint8_t w = cx.wall[n];
+    for (int a = 0; a < D; ++a) {
+      if (w & (1 << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        pn_nb[2 * a] = pn_nb[2 * a + 1];
+        if (second_order) xx_000[a] = xx_nb[2 * a] = xx_nb[2 * a + 1] = 0.0;
+      }
+      if (w & (1 << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        pn_nb[2 * a + 1] = pn_nb[2 * a];
+        if (second_order) xx_000[a] = xx_nb[2 * a] = xx_nb[2 * a + 1] = 0.0;
+      }
+    }
+    double gp[3], gm[3];
+    for (int a = 0; a < D; ++a) {
+      gp[a] = (pn_nb[2 * a + 1] - pn_000) / s[2 * a + 1];
+      gm[a] = (pn_000 - pn_nb[2 * a]) / s[2 * a];
+    }
+    if (second_order)
+      for (int a = 0; a < D; ++a) {
+        xx_nb[2 * a] = MINMOD(xx_nb[2 * a], xx_000[a]);
+        gm[a] += 0.5 * s[2 * a] * xx_nb[2 * a];
+        xx_nb[2 * a + 1] = MINMOD(xx_nb[2 * a + 1], xx_000[a]);
+        gp[a] -= 0.5 * s[2 * a + 1] * xx_nb[2 * a + 1];
+      }
+    const double sgn = (p0_000 > 0.0 ? 1.0 : -1.0);
+    double dt = MIN(s[0], s[1]);
+    dt = MIN(dt, s[2], s[3]);
+    if (D == 3) dt = MIN(dt, s[4], s[5]);
+    dt /= (double)D;
+    for (int a = 0; a < D; ++a) {
+      if (sgn * gp[a] > 0.0) gp[a] = 0.0;
+      if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+    }
+    double sum = MAX(gp[0] * gp[0], gm[0] * gm[0]) + MAX(gp[1] * gp[1], gm[1] * gm[1]);
+    if (D == 3) sum = sum + MAX(gp[2] * gp[2], gm[2] * gm[2]);
+    phi_np1[n] = pn_000 - dt * sgn * (sqrt(sum) - 1.);
+    if (phi_0[n] * phi_np1[n] < 0.0) phi_np1[n] *= -1.0;
+  }
+}
+
+template <int D>
+void compute_derivatives(const Ctx& cx, const double* f, double* fdd, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long n = 0; n < (long long)N; ++n) {
+    double f0, fnb[6], dd[3] = {0, 0, 0};
+    laplace(Q[n], f, &f0, fnb, dd);
+    for (int a = 0; a < D; ++a) fdd[(size_t)a * N + n] = dd[a];
+  }
+}
+
+// reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557)
+template <int D>
+void reinitialize(const Ctx& cx, double* phi, int order_space, int order_pseudotime, double hi, double lo, int iters, int nthreads) {
+  const int64_t N = cx.N;
+  std::vector<double> phi_np1(N), phi_np2(order_pseudotime > 1 ? N : 0), phi_0(phi, phi + N);
+  std::vector<double> dd0, ddc;
+  if (order_space > 1) {
+    dd0.resize((size_t)D * N);
+    ddc.resize((size_t)D * N);
+    compute_derivatives<D>(cx, phi, dd0.data(), nthreads);
+  }
+  for (int i = 0; i < iters; ++i) {
+    if (order_space > 1) compute_derivatives<D>(cx, phi, ddc.data(), nthreads);
+    reinitialize_one_iteration<D>(cx, phi_np1.data(), phi_0.data(), phi, hi, lo, order_space > 1 ? dd0.data() : nullptr,
+                                  order_space > 1 ? ddc.data() : nullptr, nthreads);
+    if (order_pseudotime > 1) {
+      if (order_space > 1) compute_derivatives<D>(cx, phi_np1.data(), ddc.data(), nthreads);
+      reinitialize_one_iteration<D>(cx, phi_np2.data(), phi_0.data(), phi_np1.data(), hi, lo, order_space > 1 ? dd0.data() : nullptr,
+                                    order_space > 1 ? ddc.data() : nullptr, nthreads);
+      for (int64_t n = 0; n < N; ++n) phi[n] = .5 * (phi[n] + phi_np2[n]);
+    } else {
+      memcpy(phi, phi_np1.data(), N * sizeof(double));
+    }
+  }
+}
+
+// advect_in_normal_direction_one_iteration (src/my_p4est_level_set.cpp:559-654)
+template <int D>
+void advect_one_iteration(const Ctx& cx, const double* vn, double dt, const double* dd, const double* phi_n, double* phi_np1,
+                          int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long k = 0; k < (long long)N; ++k) {
+    const int64_t n = k;
+    const Qnnn<D>& q = Q[n];
+    double pn_000, pn_nb[6];
+    ngbd_quadratic(q, phi_n, &pn_000, pn_nb);
+    double s[6];
+    for (int dir = 0; dir < 2 * D; ++dir) s[dir] = q.d[dir];
+    double xx_000[3], xx_nb[6];
+    for (int a = 0; a < D; ++a) {
+      xx_000[a] = dd[(size_t)a * N + n];
+      xx_nb[2 * a] = f_linear(q, 2 * a, dd + (size_t)a * N);
+      xx_nb[2 * a + 1] = f_linear(q, 2 * a + 1, dd + (size_t)a * N);
+    }
+    const uint8_t w = cx.wall[n];
+    for (int a = 0; a < D; ++a) {
+      if (w & (1 << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        pn_nb[2 * a] = pn_nb[2 * a + 1];
+        xx_000[a] = xx_nb[2 * a] = xx_nb[2 * a + 1] = 0.0;
+      }
+      if (w & (1 << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        pn_nb[2 * a + 1] = pn_nb[2 * a];
+        xx_000[a] = xx_nb[2 * a] = xx_nb[2 * a + 1] = 0.0;
+      }
+    }
+    double gp[3], gm[3];
+    for (int a = 0; a < D; ++a) {
+      gp[a] = (pn_nb[2 * a + 1] - pn_000) / s[2 * a + 1];
+      gm[a] = (pn_000 - pn_nb[2 * a]) / s[2 * a];
+    }
+    for (int a = 0; a < D; ++a) {
+      xx_nb[2 * a] = MINMOD(xx_nb[2 * a], xx_000[a]);
+      gm[a] += 0.5 * s[2 * a] * xx_nb[2 * a];
+      xx_nb[2 * a + 1] = MINMOD(xx_nb[2 * a + 1], xx_000[a]);
+      gp[a] -= 0.5 * s[2 * a + 1] * xx_nb[2 * a + 1];
+    }
+    const double sgn = (vn[n] > 0.0 ? +1.0 : -1.0);
+    for (int a = 0; a < D; ++a) {
+      if (sgn * gp[a] > 0.0) gp[a] = 0.0;
+      if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+    }
+    double sum = (gp[0] * gp[0] + gm[0] * gm[0]) + (gp[1] * gp[1] + gm[1] * gm[1]);
+    if (D == 3) sum = sum + (gp[2] * gp[2] + gm[2] * gm[2]);
+    phi_np1[n] = pn_000 - dt * vn[n] * (sqrt(sum));
+  }
+}
+
+// advect_in_normal_direction(phi, dt, phi_xx.., vn, vn_np1) (src/my_p4est_level_set.cpp:656-725)
+template <int D>
+void advect_normal(const Ctx& cx, const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd, int nthreads) {
+  const int64_t N = cx.N;
+  std::vector<double> local_dd;
+  double* dd = phi_dd;
+  if (!dd) {
+    local_dd.resize((size_t)D * N);
+    dd = local_dd.data();
+    compute_derivatives<D>(cx, phi, dd, nthreads);
+  }
+  std::vector<double> phi_n(phi, phi + N), phi_np2(N);
+  advect_one_iteration<D>(cx, vn, dt, dd, phi_n.data(), phi, nthreads);
+  compute_derivatives<D>(cx, phi, dd, nthreads);
+  advect_one_iteration<D>(cx, vn_np1 ? vn_np1 : vn, dt, dd, phi, phi_np2.data(), nthreads);
+  for (int64_t n = 0; n < N; ++n) phi[n] = 0.5 * (phi_n[n] + phi_np2[n]);
+}
+
+template <int D>
+Ctx* build_from_leaves(const int* n_xyz, const double* lo, const double* hi, int64_t nleaves, const int32_t* tree,
+                       const int32_t* level, const int32_t* xyz) {
+  Grid<D>* g = new Grid<D>();
+  setup_brick(*g, n_xyz, lo, hi);
+  g->leaves.resize(nleaves);
+  for (int64_t i = 0; i < nleaves; ++i) {
+    g->leaves[i].tree = tree[i];
+    g->leaves[i].level = level[i];
+    for (int a = 0; a < 3; ++a) g->leaves[i].x[a] = xyz[3 * i + a];
+  }
+  build_hierarchy(*g);
+  build_nodes(*g);
+  const int64_t N = (int64_t)g->node_tree.size();
+  g->qnnn.resize(N);
+  g->wall.resize(N);
+  int bad = 0;
+  for (int64_t i = 0; i < N; ++i) {
+    if (construct_neighbors(*g, (int32_t)i, g->qnnn[i])) ++bad;
+    g->wall[i] = wall_of(*g, (int32_t)i);
+  }
+  if (bad) {
+    delete g;
+    throw std::runtime_error("oracle: incomplete node neighbourhood");
+  }
+  Ctx* cx = new Ctx();
+  cx->dim = D;
+  cx->N = N;
+  cx->qnnn = g->qnnn.data();
+  cx->wall = g->wall.data();
+  cx->grid = g;
+  double m = g->tree_dim[0];
+  for (int a = 1; a < D; ++a) m = MIN(m, g->tree_dim[a]);
+  cx->zero_distance_threshold = ORA_EPS * (D == 3 ? MIN(g->tree_dim[0], g->tree_dim[1], g->tree_dim[2]) : MIN(g->tree_dim[0], g->tree_dim[1]));
+  return cx;
+}
+
+template <typename Fn>
+int guard(Fn&& fn) {
+  try {
+    fn();
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ora_last_error(void) { return g_err.c_str(); }
+size_t ora_qnnn_record_bytes(int dim) { return dim == 2 ? sizeof(Qnnn<2>) : sizeof(Qnnn<3>); }
+
+int ora_grid_from_leaves(int dim, const int* n_xyz, const double* lo, const double* hi, int64_t nleaves, const int32_t* tree,
+                         const int32_t* level, const int32_t* xyz, void** out) {
+  return guard([&] {
+    *out = dim == 2 ? (void*)build_from_leaves<2>(n_xyz, lo, hi, nleaves, tree, level, xyz)
+                    : (void*)build_from_leaves<3>(n_xyz, lo, hi, nleaves, tree, level, xyz);
+  });
+}
+
+// Borrow neighbour records built elsewhere (same layout; kept alive by the caller) and copy the wall
+// mask; tree_dims gives the tree sizes for zero_distance_threshold.
+int ora_grid_from_qnnn(int dim, int64_t N, const void* qnnn, const uint8_t* wall, const double* tree_dims, void** out) {
+  return guard([&] {
+    Ctx* cx = new Ctx();
+    cx->dim = dim;
+    cx->N = N;
+    cx->qnnn = const_cast<void*>(qnnn);  // borrowed: the caller keeps the records alive
+    cx->wall_store.assign(wall, wall + N);
+    cx->wall = cx->wall_store.data();
+    cx->grid = nullptr;
+    cx->zero_distance_threshold =
+        ORA_EPS * (dim == 3 ? MIN(tree_dims[0], tree_dims[1], tree_dims[2]) : MIN(tree_dims[0], tree_dims[1]));
+    *out = cx;
+  });
+}
+
+void ora_grid_destroy(void* h) {
+  Ctx* cx = static_cast<Ctx*>(h);
+  if (!cx) return;
+  if (cx->grid) {
+    if (cx->dim == 2) delete static_cast<Grid<2>*>(cx->grid);
+    else delete static_cast<Grid<3>*>(cx->grid);
+  }
+  delete cx;
+}
+
+int64_t ora_grid_num_nodes(void* h) { return static_cast<Ctx*>(h)->N; }
+double ora_zero_distance_threshold(void* h) { return static_cast<Ctx*>(h)->zero_distance_threshold; }
+
+// owner tree and clamped logical coordinates (3 per node) of the oracle's own numbering
+int ora_grid_nodes(void* h, int32_t* tree, int64_t* xyz) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("grid built from records has no node coordinates");
+    const int D = cx->dim;
+    const std::vector<int32_t>& nt = D == 2 ? static_cast<Grid<2>*>(cx->grid)->node_tree : static_cast<Grid<3>*>(cx->grid)->node_tree;
+    const std::vector<int64_t>& nx = D == 2 ? static_cast<Grid<2>*>(cx->grid)->node_x : static_cast<Grid<3>*>(cx->grid)->node_x;
+    for (int64_t n = 0; n < cx->N; ++n) {
+      tree[n] = nt[n];
+      for (int a = 0; a < 3; ++a) xyz[3 * n + a] = a < D ? nx[(size_t)n * D + a] : 0;
+    }
+  });
+}
+
+int ora_grid_export_qnnn(void* h, void* out) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    memcpy(out, cx->qnnn, ora_qnnn_record_bytes(cx->dim) * cx->N);
+  });
+}
+
+int ora_grid_wall_mask(void* h, uint8_t* out) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    memcpy(out, cx->wall, cx->N);
+  });
+}
+
+int ora_compute_derivatives(void* h, const double* f, double* fdd, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) compute_derivatives<2>(*cx, f, fdd, nthreads);
+    else compute_derivatives<3>(*cx, f, fdd, nthreads);
+  });
+}
+
+int ora_reinitialize(void* h, double* phi, int order_space, int order_pseudotime, double limit_high, double limit_low, int iters,
+                     int nthreads) {
+  return guard([&] {
+    if (order_space < 1 || order_space > 2 || order_pseudotime < 1 || order_pseudotime > 2)
+      throw std::invalid_argument("valid orders of accuracy are 1 and 2 only");
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) reinitialize<2>(*cx, phi, order_space, order_pseudotime, limit_high, limit_low, iters, nthreads);
+    else reinitialize<3>(*cx, phi, order_space, order_pseudotime, limit_high, limit_low, iters, nthreads);
+  });
+}
+
+int ora_advect_in_normal_direction(void* h, const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd,
+                                   int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) advect_normal<2>(*cx, vn, vn_np1, phi, dt, phi_dd, nthreads);
+    else advect_normal<3>(*cx, vn, vn_np1, phi, dt, phi_dd, nthreads);
+  });
+}
+
+// CF overload's time step: dt = MIN over nodes of 0.8*fabs(s_min/vn) (src/my_p4est_level_set.cpp:752-776)
+int ora_advect_cfl_dt(void* h, const double* vn, double* dt_out) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    double dt = DBL_MAX;
+    for (int64_t n = 0; n < cx->N; ++n) {
+      double smin;
+      if (cx->dim == 2) {
+        const Qnnn<2>& q = static_cast<const Qnnn<2>*>(cx->qnnn)[n];
+        smin = MIN(MIN(fabs(q.d[1]), fabs(q.d[0])), MIN(fabs(q.d[3]), fabs(q.d[2])));
+      } else {
+        const Qnnn<3>& q = static_cast<const Qnnn<3>*>(cx->qnnn)[n];
+        smin = MIN(MIN(fabs(q.d[1]), fabs(q.d[0])), MIN(fabs(q.d[3]), fabs(q.d[2])), MIN(fabs(q.d[5]), fabs(q.d[4])));
+      }
+      dt = MIN(dt, 0.8 * fabs(smin / vn[n]));
+    }
+    *dt_out = dt;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+"""ORACLE — test infrastructure only (tests/, smoke() and the benchmark's CPU baseline).
+
+ctypes binding of oracle/_build/liboracle.so, the CPU restatement of parCASL's level-set loops
+(oracle.cpp). Used as the checker of the CUDA path; never imported by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_P, _I, _I64, _D = C.c_void_p, C.c_int, C.c_int64, C.c_double
+_DP = C.POINTER(C.c_double)
+SIG = {
+    "ora_last_error": (C.c_char_p, []),
+    "ora_qnnn_record_bytes": (C.c_size_t, [_I]),
+    "ora_grid_from_leaves": (_I, [_I, C.POINTER(_I), _DP, _DP, _I64, _P, _P, _P, C.POINTER(_P)]),
+    "ora_grid_from_qnnn": (_I, [_I, _I64, _P, _P, _DP, C.POINTER(_P)]),
+    "ora_grid_destroy": (None, [_P]),
+    "ora_grid_num_nodes": (_I64, [_P]),
+    "ora_zero_distance_threshold": (_D, [_P]),
+    "ora_grid_nodes": (_I, [_P, _P, _P]),
+    "ora_grid_export_qnnn": (_I, [_P, _P]),
+    "ora_grid_wall_mask": (_I, [_P, _P]),
+    "ora_compute_derivatives": (_I, [_P, _DP, _DP, _I]),
+    "ora_reinitialize": (_I, [_P, _DP, _I, _I, _D, _D, _I, _I]),
+    "ora_advect_in_normal_direction": (_I, [_P, _DP, _DP, _DP, _D, _DP, _I]),
+    "ora_advect_cfl_dt": (_I, [_P, _DP, _DP]),
+}
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = C.CDLL(LIB)
+        for k, (r, a) in SIG.items():
+            f = getattr(lib, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = lib
+    return _lib
+
+
+def _chk(code):
+    if code != 0:
+        raise RuntimeError("oracle: " + load().ora_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP) if a is not None else None
+
+
+class OracleGrid:
+    """CPU restatement of the grid-side objects and the level-set loops."""
+
+    def __init__(self, handle, dim):
+        self._h = handle
+        self.dim = dim
+        self.N = int(load().ora_grid_num_nodes(handle))
+        self.zero_distance_threshold = float(load().ora_zero_distance_threshold(handle))
+
+    @classmethod
+    def from_forest(cls, forest):
+        """Build nodes, cell tree and neighbours from the leaves of a product Forest (own numbering)."""
+        tree, level, xyz = forest.leaves()
+        n = (C.c_int * 3)(*forest.n_xyz)
+        lo = (C.c_double * 3)(*forest.xyz_min)
+        hi = (C.c_double * 3)(*forest.xyz_max)
+        h = C.c_void_p()
+        _chk(load().ora_grid_from_leaves(forest.dim, n, lo, hi, len(tree), tree.ctypes.data, level.ctypes.data, xyz.ctypes.data,
+                                         C.byref(h)))
+        return cls(h, forest.dim)
+
+    @classmethod
+    def from_records(cls, dim, qnnn_records, wall, tree_dims):
+        qn = np.ascontiguousarray(qnnn_records)
+        w = np.ascontiguousarray(wall, dtype=np.uint8)
+        td = np.ascontiguousarray(list(tree_dims) + [1.0] * (3 - len(tree_dims)), dtype=np.float64)
+        h = C.c_void_p()
+        _chk(load().ora_grid_from_qnnn(dim, len(qn), qn.ctypes.data, w.ctypes.data, _dp(td), C.byref(h)))
+        g = cls(h, dim)
+        g._records = qn  # the library borrows the records
+        return g
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None:
+            load().ora_grid_destroy(self._h)
+            self._h = None
+
+    def nodes(self):
+        tree = np.empty(self.N, np.int32)
+        xyz = np.empty((self.N, 3), np.int64)
+        _chk(load().ora_grid_nodes(self._h, tree.ctypes.data, xyz.ctypes.data))
+        return tree, xyz
+
+    def qnnn(self, dtype):
+        out = np.zeros(self.N, dtype=dtype)
+        _chk(load().ora_grid_export_qnnn(self._h, out.ctypes.data))
+        return out
+
+    def wall_mask(self):
+        out = np.empty(self.N, np.uint8)
+        _chk(load().ora_grid_wall_mask(self._h, out.ctypes.data))
+        return out
+
+    def compute_derivatives(self, f, nthreads=1):
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.empty((self.dim, self.N), np.float64)
+        _chk(load().ora_compute_derivatives(self._h, _dp(f), _dp(out), nthreads))
+        return out
+
+    def reinitialize(self, phi, order_space=2, order_pseudotime=2, limit_high=np.finfo(np.float64).max,
+                     limit_low=-np.finfo(np.float64).max, iterations=50, nthreads=1):
+        """In place on a float64 numpy array."""
+        assert phi.dtype == np.float64 and phi.flags.c_contiguous and phi.size == self.N
+        _chk(load().ora_reinitialize(self._h, _dp(phi), order_space, order_pseudotime, limit_high, limit_low, iterations, nthreads))
+
+    def advect_in_normal_direction(self, vn, phi, dt, vn_np1=None, phi_dd=None, nthreads=1):
+        _chk(load().ora_advect_in_normal_direction(self._h, _dp(vn), _dp(vn_np1), _dp(phi), dt, _dp(phi_dd), nthreads))
+
+    def advect_cfl_dt(self, vn):
+        out = C.c_double()
+        _chk(load().ora_advect_cfl_dt(self._h, _dp(np.ascontiguousarray(vn, np.float64)), C.byref(out)))
+        return out.value

@@ -1,0 +1,154 @@
+"""CUDA path against the CPU oracle, through the C ABI.
+
+FP64: the kernels evaluate the reference's expressions in the same order with no contracted
+multiply-adds, so the results must be bit-identical to the oracle (tolerance 0). The north-star
+tolerance for the FP64 GPU path is 1e-12*max|phi|; the tests hold it to exact equality.
+Mixed: FP32 stencil/RK with the FP64 subcell step; band L-infinity error against the FP64 path
+<= 1e-4 * dx_min (spec target), interface sign pattern identical.
+"""
+import numpy as np
+import pytest
+
+import casl_p4est_gb300 as G
+import oracle as O
+
+from grids import (band_error, brick_2d, brick_3d, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d)
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = {
+    "circle2d": (lambda: circle_2d(3, 8), phi0_circle_2d),
+    "brick2d": (lambda: brick_2d(1, 7), lambda f: f.sample(G.shapes.sphere_scaled([0.3, 0.1], 0.6, 0.2, [0.5, 0.5]))),
+    "flower3d": (lambda: flower_3d(3, 6), phi0_flower_3d),
+    "brick3d": (lambda: brick_3d(1, 5), lambda f: f.sample(G.shapes.sphere_scaled([0.7, 0.5, 0.9], 0.3, 0.1, [1, 0.5, 1]))),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(GRIDS))
+def case(request):
+    build, phi0 = GRIDS[request.param]
+    f = build()
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    ngbd.init_neighbors()
+    ls = G.my_p4est_level_set_t(ngbd)
+    og = O.OracleGrid.from_forest(f)
+    return request.param, f, ls, og, phi0(f)
+
+
+def test_second_derivatives_bitwise(case):
+    name, f, ls, og, phi = case
+    got = ls.compute_derivatives(phi)
+    ref = og.compute_derivatives(phi)
+    assert np.array_equal(got, ref), np.max(np.abs(got - ref))
+
+
+@pytest.mark.parametrize("orders", [(2, 2), (1, 1), (1, 2), (2, 1)])
+def test_reinit_fp64_bitwise(case, orders):
+    name, f, ls, og, phi0 = case
+    iters = 6
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.reinitialize_within_range_of_phi_0(a, orders[0], orders[1], G.DBL_MAX, -G.DBL_MAX, iters, precision="fp64")
+    og.reinitialize(b, orders[0], orders[1], iterations=iters)
+    assert np.array_equal(a, b), (name, orders, np.max(np.abs(a - b)))
+
+
+def test_reinit_fp64_limits_bitwise(case):
+    name, f, ls, og, phi0 = case
+    lim = 0.1 * float(np.max(np.abs(phi0)))
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.reinitialize_2nd_order(a, 5, lim, precision="fp64")
+    og.reinitialize(b, 2, 2, lim, -lim, iterations=5)
+    assert np.array_equal(a, b)
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.reinitialize_2nd_order_above_threshold(a, -0.5 * lim, 5, precision="fp64")
+    og.reinitialize(b, 2, 2, np.finfo(np.float64).max, -0.5 * lim, iterations=5)
+    assert np.array_equal(a, b)
+
+
+def test_advect_fp64_bitwise(case):
+    name, f, ls, og, phi0 = case
+    xyz = f.node_xyz()
+    vn = 1.0 + 0.5 * np.sin(3 * xyz[:, 0]) * np.cos(2 * xyz[:, 1])
+    dt_gpu = ls.advect_in_normal_direction(lambda x: 1.0 + 0.5 * np.sin(3 * x[:, 0]) * np.cos(2 * x[:, 1]), phi0.copy())
+    dt = og.advect_cfl_dt(vn)
+    assert dt_gpu == dt
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.advect_in_normal_direction(vn, a, dt, precision="fp64")
+    og.advect_in_normal_direction(vn, b, dt)
+    assert np.array_equal(a, b)
+    # two velocities + caller-supplied second derivatives (overwritten as the reference does)
+    vn1 = 0.5 * vn
+    dd_a = ls.compute_derivatives(phi0)
+    dd_b = dd_a.copy()
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.advect_in_normal_direction(vn, a, dt, phi_xx=dd_a, vn_np1=vn1, precision="fp64")
+    og.advect_in_normal_direction(vn, b, dt, vn_np1=vn1, phi_dd=dd_b)
+    assert np.array_equal(a, b)
+    assert np.array_equal(dd_a, dd_b)
+
+
+def test_mixed_band_error_vs_fp64(case):
+    name, f, ls, og, phi0 = case
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.reinitialize_2nd_order(a, 20, precision="fp64")
+    ls.reinitialize_2nd_order(b, 20, precision="mixed")
+    lvl = f.leaves()[1].max()
+    _, dmin, _ = f.dxyz_min(int(lvl))
+    err = band_error(b, a, 3 * dmin)
+    assert err <= 1e-4 * dmin, (name, err, dmin)
+    assert np.all(np.sign(a[np.abs(a) > 1e-9]) == np.sign(b[np.abs(a) > 1e-9]))
+
+
+def test_mixed_advect_close_to_fp64(case):
+    name, f, ls, og, phi0 = case
+    xyz = f.node_xyz()
+    vn = 1.0 + 0.5 * np.sin(3 * xyz[:, 0])
+    dt = og.advect_cfl_dt(vn)
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.advect_in_normal_direction(vn, a, dt, precision="fp64")
+    ls.advect_in_normal_direction(vn, b, dt, precision="mixed")
+    lvl = f.leaves()[1].max()
+    _, dmin, _ = f.dxyz_min(int(lvl))
+    assert band_error(b, a, 3 * dmin) <= 1e-4 * dmin
+
+
+def test_device_resident_matches_host(case):
+    torch = pytest.importorskip("torch")
+    name, f, ls, og, phi0 = case
+    a = phi0.copy()
+    ls.reinitialize_2nd_order(a, 4, precision="fp64")
+    t = torch.from_numpy(phi0.copy()).cuda()
+    torch.cuda.synchronize()
+    ls.reinitialize_2nd_order(t, 4, precision="fp64")
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), a)
+
+
+def test_deterministic(case):
+    name, f, ls, og, phi0 = case
+    a = phi0.copy()
+    b = phi0.copy()
+    ls.reinitialize_2nd_order(a, 5, precision="mixed")
+    ls.reinitialize_2nd_order(b, 5, precision="mixed")
+    assert np.array_equal(a, b)
+
+
+def test_errors_are_reported():
+    f = circle_2d(2, 5)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    phi = phi0_circle_2d(f)
+    with pytest.raises(ValueError):
+        ls.reinitialize_within_range_of_phi_0(phi, 3, 2, 1.0, -1.0, 5)
+    with pytest.raises(G.LsgInvalidArgument):
+        ls.reinitialize_within_range_of_phi_0(phi, 2, 2, -1.0, 1.0, 5)
+    with pytest.raises(ValueError):
+        ls.reinitialize_2nd_order(phi[:-1], 5)
+    with pytest.raises(G.LsgInvalidArgument):
+        ls.reinitialize_2nd_order(phi, -1)
