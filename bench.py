@@ -275,10 +275,14 @@ def main():
     lib.lsg_level_set_enable_kernel_timing(ls.handle, 1)
     step("mixed")
     lib.lsg_level_set_kernel_times(ls.handle, kms.ctypes.data_as(L._DP), kcnt.ctypes.data_as(C.POINTER(C.c_int64)), 10, 1)
-    lib.lsg_level_set_enable_kernel_timing(ls.handle, 0)
     kinds = L.KERNEL_KINDS
     per_kernel = {kinds[k]: {"ms_total": float(kms[k]), "launches": int(kcnt[k]),
                              "ms_per_launch": float(kms[k] / kcnt[k]) if kcnt[k] else None} for k in range(10) if kcnt[k]}
+    step("fp64")
+    lib.lsg_level_set_kernel_times(ls.handle, kms.ctypes.data_as(L._DP), kcnt.ctypes.data_as(C.POINTER(C.c_int64)), 10, 1)
+    lib.lsg_level_set_enable_kernel_timing(ls.handle, 0)
+    per_kernel_fp64 = {kinds[k]: {"ms_total": float(kms[k]), "launches": int(kcnt[k]),
+                                  "ms_per_launch": float(kms[k] / kcnt[k]) if kcnt[k] else None} for k in range(10) if kcnt[k]}
     # algorithmic bytes per node and launch, mixed 3D (w_f = w_d = 4 bytes): table 2D*(4+w_d) = 48 B per
     # table-reading sweep; dd sweep reads 1 and writes D values; stage sweep reads phi_0, phi_k and D
     # second derivatives and writes 1; the RK average (3 values) is fused into every second stage.
@@ -336,7 +340,7 @@ def main():
             "speedup_mixed_vs_fp64": value / value64,
             "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
             "dx_min": dmin,
-            "roofline": roofline, "kernels": per_kernel,
+            "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
             "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
         }
         print(json.dumps(out), flush=True)

@@ -29,16 +29,20 @@ struct DTab64 {
   const uint8_t* wall;  // N
 };
 
-// Mixed-precision tables (layout described in tables32.cpp).
+// Mixed-precision tables in device node order (layout described in tables32.cpp).
 template <int D>
 struct DTab32 {
-  int64_t N;
-  const uint32_t* meta;  // N
-  const int32_t* nbr;    // NS x N (shared with the FP64 tables)
-  const float* wf;       // NS x N
-  const float* d;        // 2D x N
-  const float* q;        // 2D(D-1) x N
-  const int32_t* cidx;   // N (shared with the FP64 tables)
+  int64_t N, nR, nI;
+  int base;              // base level of the regular nodes' level codes
+  float tsize[3];        // tree size per axis
+  const uint32_t* r_meta;
+  const int32_t* r_nbr;  // 2D x nR
+  const uint32_t* i_meta;
+  const int32_t* i_nbr;  // NS x nI
+  const float* i_wf;     // NS x nI
+  const float* i_d;      // 2D x nI
+  const float* i_q;      // 2D(D-1) x nI
+  const int32_t* i_cidx;
   const float* corr;     // D*D x R
 };
 
@@ -61,17 +65,20 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
 template <int D>
 void launch_dd32(const DTab32<D>& T, const float* f, float* dd, cudaStream_t s);
 template <int D>
-void launch_reinit_prep_mixed(const DTab64<D>& T, const uint32_t* meta32, const double* phi0, double zdt, double lim_lo,
-                              double lim_hi, int order_space, uint16_t* status, float* s_near, cudaStream_t s);
+void launch_reinit_prep_mixed(const DTab64<D>& T, const int32_t* iperm, const double* phi0, double zdt, double lim_lo, double lim_hi,
+                              int order_space, uint16_t* status, float* s_near, int32_t* near_list, unsigned* near_count,
+                              cudaStream_t s);
 template <int D>
 void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd, float* out, const float* avg_with, cudaStream_t s);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);
-void launch_f64_to_f32(const double* src, float* dst, int64_t n, cudaStream_t s);
-void launch_f32_to_f64(const float* src, double* dst, int64_t n, cudaStream_t s);
-// dst = src except at nodes whose status marks them outside the reinitialisation limits
-void launch_f32_to_f64_status(const float* src, const uint16_t* status, double* dst, int64_t n, cudaStream_t s);
+// node order (FP64) <-> device order (FP32): dst[b*dst_stride + i] = src[b*src_stride + perm[i]] and the
+// reverse scatter (skipping nodes whose status marks them outside the reinitialisation limits)
+void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64_t n, int64_t src_stride, int64_t dst_stride,
+                       int blocks, cudaStream_t s);
+void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* status, double* dst, int64_t n, int64_t src_stride,
+                        int64_t dst_stride, int blocks, cudaStream_t s);
 
 }  // namespace lsg

@@ -92,7 +92,9 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
   smin.upload(T.smin, stream);
   if (with_mixed) {
     Tables32<D> M;
-    build_tables32<D>(T, M);
+    double ts[3];
+    for (int a = 0; a < D; ++a) ts[a] = forest.brick.tmax[a] - forest.brick.tmin[a];
+    build_tables32<D>(T, ts, M);
     upload_mixed(M);
   }
   cuda_check(cudaStreamSynchronize(stream), "table upload");
@@ -179,31 +181,49 @@ void LevelSet<D>::build_mixed() {
   Tables64<D> T;
   build_tables64<D>(*F, T);
   Tables32<D> M;
-  build_tables32<D>(T, M);
+  double ts[3];
+  for (int a = 0; a < D; ++a) ts[a] = F->brick.tmax[a] - F->brick.tmin[a];
+  build_tables32<D>(T, ts, M);
   upload_mixed(M);
 }
 
 template <int D>
 void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
-  meta.upload(M.meta, stream);
-  wf.upload(M.wf, stream);
-  df.upload(M.d, stream);
-  qf.upload(M.q, stream);
+  r_meta.upload(M.r_meta, stream);
+  r_nbr.upload(M.r_nbr, stream);
+  i_meta.upload(M.i_meta, stream);
+  i_nbr.upload(M.i_nbr, stream);
+  i_wf.upload(M.i_wf, stream);
+  i_d.upload(M.i_d, stream);
+  i_q.upload(M.i_q, stream);
+  i_cidx.upload(M.i_cidx, stream);
   corr32.upload(M.corr, stream);
+  perm.upload(M.perm, stream);
+  iperm.upload(M.iperm, stream);
+  near_list.alloc((size_t)N);
+  near_count.alloc(1);
   cuda_check(cudaStreamSynchronize(stream), "mixed table upload");
+  nR = M.nR;
+  nI = M.nI;
   T32.N = N;
-  T32.meta = meta.p;
-  T32.nbr = nbr.p;
-  T32.wf = wf.p;
-  T32.d = df.p;
-  T32.q = qf.p;
-  T32.cidx = cidx.p;
+  T32.nR = M.nR;
+  T32.nI = M.nI;
+  T32.base = M.base_level;
+  for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)(F->brick.tmax[a] - F->brick.tmin[a]) : 1.0f;
+  T32.r_meta = r_meta.p;
+  T32.r_nbr = r_nbr.p;
+  T32.i_meta = i_meta.p;
+  T32.i_nbr = i_nbr.p;
+  T32.i_wf = i_wf.p;
+  T32.i_d = i_d.p;
+  T32.i_q = i_q.p;
+  T32.i_cidx = i_cidx.p;
   T32.corr = corr32.p;
   mixed_ready = true;
 }
 
-
-// Mixed precision: phi_n and all per-iteration work in FP32; the phi_0-only subcell step in FP64.
+// Mixed precision: phi_n and all per-iteration work in FP32 (device node order); the phi_0-only
+// subcell step in FP64.
 template <int D>
 void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters) {
   build_mixed();
@@ -212,8 +232,9 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   f_dd.alloc((size_t)D * N);
   f_snear.alloc((size_t)2 * D * N);
   status.alloc(N);
-  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T64, meta.p, phi, zdt, lo, hi, os, status.p, f_snear.p, stream));
-  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi, f_phi.p, N, stream));
+  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T64, iperm.p, phi, zdt, lo, hi, os, status.p, f_snear.p, near_list.p,
+                                                       near_count.p, stream));
+  LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
     LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));
     LSG_LAUNCH(K_STAGE32, launch_reinit_stage32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
@@ -224,7 +245,7 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
       std::swap(f_phi.p, f_phi1.p);
     }
   }
-  LSG_LAUNCH(K_CONVERT, launch_f32_to_f64_status(f_phi.p, status.p, phi, N, stream));
+  LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
 }
 
@@ -261,21 +282,22 @@ void LevelSet<D>::advect_mixed(const double* vn, const double* vn_np1, double* p
   f_phi1.alloc(N);
   f_dd.alloc((size_t)D * N);
   f_vn.alloc(vn_np1 ? 2 * (size_t)N : (size_t)N);
-  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi, f_phi0.p, N, stream));
-  LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(vn, f_vn.p, N, stream));
-  if (vn_np1) LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(vn_np1, f_vn.p + N, N, stream));
+  LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi0.p, N, 0, 0, 1, stream));
+  LSG_LAUNCH(K_CONVERT, launch_gather_f32(vn, perm.p, f_vn.p, N, 0, 0, 1, stream));
+  if (vn_np1) LSG_LAUNCH(K_CONVERT, launch_gather_f32(vn_np1, perm.p, f_vn.p + N, N, 0, 0, 1, stream));
   LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi0.p, f_dd.p, stream));
   const float* ddm = f_dd.p;
   if (phi_dd) {
     f_ddm.alloc((size_t)D * N);
-    LSG_LAUNCH(K_CONVERT, launch_f64_to_f32(phi_dd, f_ddm.p, (int64_t)D * N, stream));
+    LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi_dd, perm.p, f_ddm.p, N, N, N, D, stream));
     ddm = f_ddm.p;
   }
   LSG_LAUNCH(K_ADVECT32, launch_advect_stage32<D>(T32, f_phi0.p, f_dd.p, ddm, f_vn.p, (float)dt, f_phi.p, nullptr, stream));
   LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));
-  if (phi_dd) LSG_LAUNCH(K_CONVERT, launch_f32_to_f64(f_dd.p, phi_dd, (int64_t)D * N, stream));
-  LSG_LAUNCH(K_ADVECT32, launch_advect_stage32<D>(T32, f_phi.p, f_dd.p, f_dd.p, vn_np1 ? f_vn.p + N : f_vn.p, (float)dt, f_phi1.p, f_phi0.p, stream));
-  LSG_LAUNCH(K_CONVERT, launch_f32_to_f64(f_phi1.p, phi, N, stream));
+  if (phi_dd) LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_dd.p, perm.p, nullptr, phi_dd, N, N, N, D, stream));
+  LSG_LAUNCH(K_ADVECT32, launch_advect_stage32<D>(T32, f_phi.p, f_dd.p, f_dd.p, vn_np1 ? f_vn.p + N : f_vn.p, (float)dt, f_phi1.p,
+                                                  f_phi0.p, stream));
+  LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi1.p, perm.p, nullptr, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "advect_in_normal_direction (mixed)");
 }
 

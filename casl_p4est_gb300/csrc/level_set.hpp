@@ -59,9 +59,12 @@ struct LevelSet {
   DTab64<D> T64{};
   // mixed tables (built on first mixed call)
   bool mixed_ready = false;
-  DevBuf<uint32_t> meta;
-  DevBuf<float> wf, df, qf, corr32;
+  DevBuf<uint32_t> r_meta, i_meta;
+  DevBuf<int32_t> r_nbr, i_nbr, i_cidx, perm, iperm, near_list;
+  DevBuf<unsigned> near_count;
+  DevBuf<float> i_wf, i_d, i_q, corr32;
   DTab32<D> T32{};
+  int64_t nR = 0, nI = 0;
   // work vectors
   DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
   DevBuf<uint16_t> status;

@@ -53,16 +53,26 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T);
 
 template <int D>
 struct Tables32 {
-  int64_t N = 0;
-  std::vector<uint32_t> meta;  // N
-  std::vector<float> wf;       // NS * N
-  std::vector<float> d;        // 2D * N
-  std::vector<float> q;        // 2D*(D-1) * N
-  std::vector<float> corr;     // D*D * R, row-major: corrected = corr * naive
+  int64_t N = 0, nR = 0, nI = 0;
+  int base_level = 0;
+  float level_size[3 * 16] = {0};   // [axis*16 + code] cell size tree_size * 2^-(base_level + code)
+  std::vector<int32_t> perm;        // device index -> node
+  std::vector<int32_t> iperm;       // node -> device index
+  // regular group (device indices 0 .. nR-1)
+  std::vector<uint32_t> r_meta;     // nR: 4-bit level code per direction
+  std::vector<int32_t> r_nbr;       // 2D * nR, device indices
+  // irregular group (device indices nR .. N-1, stored at [i - nR])
+  std::vector<uint32_t> i_meta;     // nI: counts (2 bits/dir), bit 16 correction, bits 24.. walls
+  std::vector<int32_t> i_nbr;       // NS * nI, device indices
+  std::vector<float> i_wf;          // NS * nI
+  std::vector<float> i_d;           // 2D * nI
+  std::vector<float> i_q;           // 2D*(D-1) * nI
+  std::vector<int32_t> i_cidx;      // nI
+  std::vector<float> corr;          // D*D * R, row-major: corrected = corr * naive
 };
 
 template <int D>
-void build_tables32(const Tables64<D>& T, Tables32<D>& M);
+void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& M);
 
 // Cross-term coefficients of one record, exactly as correct_naive_second_derivatives computes them.
 template <int D>

@@ -1,15 +1,19 @@
-// Flattener, mixed-precision part: FP32 coefficient tables derived from the FP64 ones.
+// Flattener, mixed-precision part: FP32 tables in a device node order of their own.
 //
-// Per node, read unconditionally by the mixed kernels (3D: 52 bytes):
-//   meta   bits 2*dir..2*dir+1: number of face nodes of direction dir minus one
-//          bit 16: the node has a cross-term correction (index in cidx, matrix in corr)
-//          bits 24..29: wall mask
-//   nbr    slot 0 of every direction (shared with the FP64 tables)
-//   d      distance per direction
-// Read only for directions with more than one face node: the other nbr slots, the normalised
-// weights wf = w/nrm and the third-order factors q. The cross-term correction of
-// correct_naive_second_derivatives is linear in the naive second derivatives, so every branch of it
-// becomes one 3x3 (2x2) matrix, evaluated in FP64 on the unit vectors and stored in FP32.
+// Nodes are renumbered on the device into two groups so that every warp runs one code path and
+// reads only what it uses:
+//   regular    every direction has a single face node (weight exactly 1), no cross-term correction,
+//              no third-order correction, not on a wall, and every neighbour distance equals a cell
+//              size tree_size * 2^-level with level in [base_level, base_level + 15];
+//              per node: 6 (4 in 2D) neighbour indices and one 32-bit word of 4-bit level codes.
+//   irregular  everything else (hanging faces, walls, corrections), sorted by their pattern
+//              (face-node counts, correction flag, wall bits) and then by node index, so that warps
+//              see uniform patterns; per node the full stencil: counts word, face-node indices,
+//              normalised weights w/nrm, distances, third-order factors and an optional 3x3 (2x2)
+//              correction matrix (every branch of correct_naive_second_derivatives is linear in the
+//              naive second derivatives, so it is evaluated in FP64 on the unit vectors).
+// Regular nodes come first, each group keeps the node order (tree-major Morton) of the grid.
+#include <algorithm>
 #include <stdexcept>
 
 #include "tables.hpp"
@@ -93,35 +97,116 @@ static void apply_correction_host(const double* m, double* Dv) {
 }
 
 template <int D>
-void build_tables32(const Tables64<D>& T, Tables32<D>& M) {
+void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& M) {
   constexpr int H = Dim<D>::HALF;
   constexpr int NS = 2 * D * H;
   const int64_t N = T.N;
   M.N = N;
-  M.meta.assign((size_t)N, 0u);
-  M.wf.assign((size_t)NS * N, 0.0f);
-  M.d.assign((size_t)2 * D * N, 0.0f);
-  M.q.assign((size_t)2 * D * (D - 1) * N, 0.0f);
-  const size_t R = T.crec.size() / 6;
-  M.corr.assign((size_t)D * D * R, 0.0f);
+  // base level: the coarsest cell size present among all neighbour distances
+  int base = 64;
+  std::vector<int> lvl_code((size_t)2 * D * N, -1);
+#pragma omp parallel for schedule(static) reduction(min : base)
+  for (long long nn = 0; nn < (long long)N; ++nn) {
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const double dv = T.d[(size_t)dir * N + nn];
+      const double size = tree_size[dir >> 1];
+      if (!(dv > 0)) continue;
+      int l = 0;
+      double h = size;
+      while (h > dv && l < 63) {
+        h *= 0.5;
+        ++l;
+      }
+      if (h == dv) {
+        lvl_code[(size_t)dir * N + nn] = l;
+        base = std::min(base, l);
+      }
+    }
+  }
+  if (base == 64) base = 0;
+  M.base_level = base;
+  for (int a = 0; a < D; ++a)
+    for (int c = 0; c < 16; ++c) M.level_size[a * 16 + c] = (float)ldexp(tree_size[a], -(base + c));
+
+  std::vector<uint64_t> key((size_t)N);
+  std::vector<uint32_t> icount((size_t)N);
 #pragma omp parallel for schedule(static)
   for (long long nn = 0; nn < (long long)N; ++nn) {
     const size_t n = (size_t)nn;
-    uint32_t meta = 0;
+    uint32_t counts = 0;
+    bool regular = T.wall[n] == 0 && T.cidx[n] < 0;
     for (int dir = 0; dir < 2 * D; ++dir) {
       int cnt = 0;
       for (int k = 0; k < H; ++k)
         if (T.nbr[(size_t)(dir * H + k) * N + n] >= 0) cnt = k + 1;
-      meta |= (uint32_t)(cnt - 1) << (2 * dir);
-      const double nrm = T.nrm[(size_t)dir * N + n];
-      for (int k = 0; k < cnt; ++k) M.wf[(size_t)(dir * H + k) * N + n] = (float)(T.w[(size_t)(dir * H + k) * N + n] / nrm);
-      M.d[(size_t)dir * N + n] = (float)T.d[(size_t)dir * N + n];
-      for (int j = 0; j < D - 1; ++j) M.q[(size_t)(dir * (D - 1) + j) * N + n] = (float)T.q[(size_t)(dir * (D - 1) + j) * N + n];
+      counts |= (uint32_t)(cnt - 1) << (2 * dir);
+      if (cnt != 1) regular = false;
+      for (int j = 0; j < D - 1; ++j)
+        if (T.q[(size_t)(dir * (D - 1) + j) * N + n] != 0.0) regular = false;
+      const int lc = lvl_code[(size_t)dir * N + n];
+      if (lc < base || lc > base + 15) regular = false;
     }
+    icount[n] = counts;
+    const uint64_t pattern = (uint64_t)counts | ((uint64_t)(T.cidx[n] >= 0) << 16) | ((uint64_t)T.wall[n] << 17);
+    // regular nodes first in node order; irregular ones by (pattern, node)
+    key[n] = regular ? (uint64_t)n : ((uint64_t)1 << 63) | (pattern << 32) | (uint64_t)n;
+  }
+  std::vector<uint64_t> sorted = key;
+  std::sort(sorted.begin(), sorted.end());
+  M.perm.resize((size_t)N);
+  M.iperm.resize((size_t)N);
+  int64_t nR = 0;
+  for (int64_t i = 0; i < N; ++i) {
+    const int64_t n = (int64_t)(sorted[i] & 0xFFFFFFFFull);
+    M.perm[i] = (int32_t)n;
+    M.iperm[n] = (int32_t)i;
+    if (!(sorted[i] >> 63)) ++nR;
+  }
+  M.nR = nR;
+  const int64_t nI = N - nR;
+  M.nI = nI;
+  // regular group
+  M.r_meta.assign((size_t)nR, 0u);
+  M.r_nbr.assign((size_t)2 * D * nR, 0);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nR; ++ii) {
+    const size_t n = (size_t)M.perm[ii];
+    uint32_t codes = 0;
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      codes |= (uint32_t)(lvl_code[(size_t)dir * N + n] - base) << (4 * dir);
+      M.r_nbr[(size_t)dir * nR + ii] = M.iperm[T.nbr[(size_t)(dir * H) * N + n]];
+    }
+    M.r_meta[ii] = codes;
+  }
+  // irregular group
+  M.i_meta.assign((size_t)nI, 0u);
+  M.i_nbr.assign((size_t)NS * nI, 0);
+  M.i_wf.assign((size_t)NS * nI, 0.0f);
+  M.i_d.assign((size_t)2 * D * nI, 0.0f);
+  M.i_q.assign((size_t)2 * D * (D - 1) * nI, 0.0f);
+  M.i_cidx.assign((size_t)nI, -1);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nI; ++ii) {
+    const size_t n = (size_t)M.perm[nR + ii];
+    uint32_t meta = icount[n];
     if (T.cidx[n] >= 0) meta |= 1u << 16;
     meta |= (uint32_t)T.wall[n] << 24;
-    M.meta[n] = meta;
+    M.i_meta[ii] = meta;
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int cnt = (int)((icount[n] >> (2 * dir)) & 3) + 1;
+      const double nrm = T.nrm[(size_t)dir * N + n];
+      for (int k = 0; k < H; ++k) {
+        const int32_t nb = T.nbr[(size_t)(dir * H + k) * N + n];
+        M.i_nbr[(size_t)(dir * H + k) * nI + ii] = k < cnt ? M.iperm[nb] : M.iperm[T.nbr[(size_t)(dir * H) * N + n]];
+        M.i_wf[(size_t)(dir * H + k) * nI + ii] = k < cnt ? (float)(T.w[(size_t)(dir * H + k) * N + n] / nrm) : 0.0f;
+      }
+      M.i_d[(size_t)dir * nI + ii] = (float)T.d[(size_t)dir * N + n];
+      for (int j = 0; j < D - 1; ++j) M.i_q[(size_t)(dir * (D - 1) + j) * nI + ii] = (float)T.q[(size_t)(dir * (D - 1) + j) * N + n];
+    }
+    M.i_cidx[ii] = T.cidx[n];
   }
+  const size_t R = T.crec.size() / 6;
+  M.corr.assign((size_t)D * D * R, 0.0f);
   for (size_t r = 0; r < R; ++r) {
     for (int c = 0; c < D; ++c) {
       double e[3] = {0, 0, 0};
@@ -132,7 +217,7 @@ void build_tables32(const Tables64<D>& T, Tables32<D>& M) {
   }
 }
 
-template void build_tables32<2>(const Tables64<2>&, Tables32<2>&);
-template void build_tables32<3>(const Tables64<3>&, Tables32<3>&);
+template void build_tables32<2>(const Tables64<2>&, const double*, Tables32<2>&);
+template void build_tables32<3>(const Tables64<3>&, const double*, Tables32<3>&);
 
 }  // namespace lsg
