@@ -44,6 +44,12 @@ struct DTab32 {
   const float* i_q;      // 2D(D-1) x nI
   const int32_t* i_cidx;
   const float* corr;     // D*D x R
+  // FP64 coefficients of the irregular nodes (subcell step)
+  double tsize64[3];
+  const double* i_wf64;
+  const double* i_d64;
+  const double* i_q64;
+  const double* corr64;
 };
 
 template <int D>
@@ -64,10 +70,12 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
 // Mixed precision.
 template <int D>
 void launch_dd32(const DTab32<D>& T, const float* f, float* dd, cudaStream_t s);
+// FP64 subcell step of the mixed path, in device node order: phi0_dev and dd0_irr are work arrays
+// (N and D*nI doubles), status/s_near are written in device order.
 template <int D>
-void launch_reinit_prep_mixed(const DTab64<D>& T, const int32_t* iperm, const double* phi0, double zdt, double lim_lo, double lim_hi,
-                              int order_space, uint16_t* status, float* s_near, int32_t* near_list, unsigned* near_count,
-                              cudaStream_t s);
+void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const double* phi0, double zdt, double lim_lo, double lim_hi,
+                              int order_space, double* phi0_dev, double* dd0_irr, uint16_t* status, float* s_near, int32_t* near_list,
+                              unsigned* near_count, cudaStream_t s);
 template <int D>
 void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd, float* out, const float* avg_with, cudaStream_t s);

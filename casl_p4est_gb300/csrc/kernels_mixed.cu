@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
   } else {
     const float f0 = __ldg(phin + n);
     float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd + (int64_t)a * N + n);
+    // second derivatives at the node are recomputed from the gathered neighbours (same arithmetic
+    // as k_dd32) rather than re-read
     if (n < T.nR) {
       const Reg<D> R{__ldg(T.r_meta + n)};
 #pragma unroll
@@ -154,19 +154,27 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
         if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd + (int64_t)(dir >> 1) * N + nb);
         s[dir] = R.d(T, dir);
       }
+#pragma unroll
+      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
     } else {
       const int64_t i = n - T.nR;
       const uint32_t meta = __ldg(T.i_meta + i);
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
-        float v = lin_irr<D>(T, meta, dir, i, phin);
-        if (face_count(meta, dir) > 1) {
-#pragma unroll
-          for (int j = 0; j < D - 1; ++j) v = fmaf(-__ldg(T.i_q + (int64_t)(dir * (D - 1) + j) * T.nI + i), Dv[tan_axis32(dir >> 1, j)], v);
-        }
-        fnb[dir] = v;
+        fnb[dir] = lin_irr<D>(T, meta, dir, i, phin);
         if (ORDER_SPACE > 1) xxnb[dir] = lin_irr<D>(T, meta, dir, i, dd + (int64_t)(dir >> 1) * N);
         s[dir] = __ldg(T.i_d + (int64_t)dir * T.nI + i);
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
+      correct_irr<D>(T, meta, i, Dv);
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        if (face_count(meta, dir) > 1) {
+#pragma unroll
+          for (int j = 0; j < D - 1; ++j)
+            fnb[dir] = fmaf(-__ldg(T.i_q + (int64_t)(dir * (D - 1) + j) * T.nI + i), Dv[tan_axis32(dir >> 1, j)], fnb[dir]);
+        }
       }
       const uint32_t wl = meta >> 24;
 #pragma unroll
@@ -282,17 +290,119 @@ __global__ void __launch_bounds__(TPB) k_advect_stage32(DTab32<D> T, const float
   out[n] = r;
 }
 
-// ---- FP64 subcell step, in two passes -------------------------------------------------------------
-// pass 1 (every node, node order): anchoring, limits, sign, and the sign test against phi_0's
-// quadratic neighbours; interface-adjacent nodes are appended to a list.
+// ---- FP64 subcell step (device order) ------------------------------------------------------------
+// Accurate FP64 arithmetic without the reference's division order: reciprocals by Newton iteration,
+// normalised weights and correction matrices precomputed in FP64.
+__device__ __forceinline__ double rcp64(double x) {
+  const double ax = fabs(x);
+  if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
+  double r = (double)__frcp_rn((float)x);
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+__device__ __forceinline__ double level_size64(double tsize, int base, uint32_t code) {
+  return __longlong_as_double(__double_as_longlong(tsize) - ((long long)(base + (int)code) << 52));
+}
+
+__device__ __forceinline__ double central_dd64(double fp, double f0, double fm, double dp, double dm) {
+  return 2.0 * fma(fp - f0, dm, (fm - f0) * dp) * rcp64(dp * dm * (dp + dm));
+}
+
 template <int D>
-__global__ void __launch_bounds__(TPB) k_prep_classify(DTab64<D> T, const int32_t* __restrict__ iperm, const double* __restrict__ phi0,
+__device__ __forceinline__ double lin_irr64(const DTab32<D>& T, uint32_t meta, int dir, int64_t i, const double* __restrict__ f) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t nI = T.nI;
+  const int64_t base = (int64_t)(dir * H) * nI + i;
+  const int c = face_count(meta, dir);
+  if (c == 1) return f[T.i_nbr[base]];
+  double acc = 0.0;
+#pragma unroll
+  for (int k = 0; k < H; ++k)
+    if (k < c) acc = fma(T.i_wf64[base + k * nI], f[T.i_nbr[base + k * nI]], acc);
+  return acc;
+}
+
+// FP64 second derivatives of an irregular node (laplace + cross-term correction)
+template <int D>
+__device__ void laplace_irr64(const DTab32<D>& T, int64_t i, const double* __restrict__ f, double f0, double* Dv) {
+  const uint32_t meta = T.i_meta[i];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double fm = lin_irr64<D>(T, meta, 2 * a, i, f);
+    const double fp = lin_irr64<D>(T, meta, 2 * a + 1, i, f);
+    Dv[a] = central_dd64(fp, f0, fm, T.i_d64[(int64_t)(2 * a + 1) * T.nI + i], T.i_d64[(int64_t)(2 * a) * T.nI + i]);
+  }
+  if (meta & (1u << 16)) {
+    const double* M = T.corr64 + (int64_t)D * D * T.i_cidx[i];
+    double o[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      double acc = 0.0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc = fma(M[D * r + c], Dv[c], acc);
+      o[r] = acc;
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) Dv[r] = o[r];
+  }
+}
+
+// second derivative along `axis` of node j (device order)
+template <int D>
+__device__ __forceinline__ double dd_axis64(const DTab32<D>& T, int64_t j, int axis, const double* __restrict__ phi0,
+                                            const double* __restrict__ dd0_irr) {
+  if (j >= T.nR) return dd0_irr[(int64_t)axis * T.nI + (j - T.nR)];
+  const uint32_t codes = T.r_meta[j];
+  const double dm = level_size64(T.tsize64[axis], T.base, (codes >> (8 * axis)) & 15u);
+  const double dp = level_size64(T.tsize64[axis], T.base, (codes >> (8 * axis + 4)) & 15u);
+  const double fm = phi0[T.r_nbr[(int64_t)(2 * axis) * T.nR + j]];
+  const double fp = phi0[T.r_nbr[(int64_t)(2 * axis + 1) * T.nR + j]];
+  return central_dd64(fp, phi0[j], fm, dp, dm);
+}
+
+__global__ void k_gather64(const double* __restrict__ src, const int32_t* __restrict__ perm, double* __restrict__ dst, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[perm[i]];
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_dd0_irr(DTab32<D> T, const double* __restrict__ phi0, double* __restrict__ dd0_irr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= T.nI) return;
+  double Dv[D];
+  laplace_irr64<D>(T, i, phi0, phi0[T.nR + i], Dv);
+#pragma unroll
+  for (int a = 0; a < D; ++a) dd0_irr[(int64_t)a * T.nI + i] = Dv[a];
+}
+
+// phi_0's quadratic neighbour in direction dir (ngbd_with_quadratic_interpolation), FP64
+template <int D>
+__device__ __forceinline__ double quad_nb_m64(const DTab32<D>& T, int64_t n, int dir, const double* __restrict__ phi0,
+                                              const double* __restrict__ dd0_irr) {
+  if (n < T.nR) return phi0[T.r_nbr[(int64_t)dir * T.nR + n]];
+  const int64_t i = n - T.nR;
+  const uint32_t meta = T.i_meta[i];
+  double v = lin_irr64<D>(T, meta, dir, i, phi0);
+  if (face_count(meta, dir) > 1) {
+#pragma unroll
+    for (int j = 0; j < D - 1; ++j)
+      v = fma(-T.i_q64[(int64_t)(dir * (D - 1) + j) * T.nI + i], dd0_irr[(int64_t)tan_axis32(dir >> 1, j) * T.nI + i], v);
+  }
+  return v;
+}
+
+// pass 1 (every node): anchoring, limits, sign and the sign test against phi_0's quadratic
+// neighbours; interface-adjacent nodes are appended to a list.
+template <int D>
+__global__ void __launch_bounds__(TPB) k_prep_classify(DTab32<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0_irr,
                                                        double zdt, double lim_lo, double lim_hi, uint16_t* __restrict__ status,
                                                        int32_t* __restrict__ near_list, unsigned* __restrict__ near_count) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t N = T.N;
   bool near = false;
-  if (n < N) {
+  if (n < T.N) {
     const double p0 = phi0[n];
     uint16_t st;
     if (fabs(p0) < zdt) {
@@ -301,85 +411,85 @@ __global__ void __launch_bounds__(TPB) k_prep_classify(DTab64<D> T, const int32_
       st = ST_OUTSIDE;
     } else {
       st = (p0 > 0.0) ? ST_POSITIVE : 0;
-      bool hanging = false;
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) hanging = hanging || (T.nbr[(int64_t)(dir * Dim<D>::HALF + 1) * N + n] >= 0);
-      double Dv[D];
-      if (hanging) st64::laplace64<D>(T, n, phi0, Dv);
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        const double fn = hanging ? st64::quad_nb64<D>(T, dir, n, phi0, Dv) : phi0[T.nbr[(int64_t)(dir * Dim<D>::HALF) * N + n]];
-        near = near || (p0 * fn < 0.0);
-      }
+      for (int dir = 0; dir < 2 * D; ++dir) near = near || (p0 * quad_nb_m64<D>(T, n, dir, phi0, dd0_irr) < 0.0);
     }
-    status[iperm[n]] = st;
+    status[n] = st;
   }
   const unsigned mask = __ballot_sync(0xffffffffu, near);
   if (mask) {
     const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
     unsigned base = 0;
-    if (lane == __ffs(mask) - 1) base = atomicAdd(near_count, (unsigned)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (lane == leader) base = atomicAdd(near_count, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
     if (near) near_list[base + __popc(mask & ((1u << lane) - 1))] = (int32_t)n;
   }
 }
 
-// pass 2 (interface-adjacent nodes only): subcell distances in FP64 (src/my_p4est_level_set.cpp:133-211)
+// pass 2 (interface-adjacent nodes): subcell distances (src/my_p4est_level_set.cpp:133-211)
 template <int D>
-__device__ double lin_dd64(const DTab64<D>& T, int dir, int axis, int64_t n, const double* __restrict__ f) {
-  constexpr int H = Dim<D>::HALF;
-  const int64_t N = T.N;
-  const int64_t base = (int64_t)(dir * H) * N + n;
-  double acc = 0.0;
-#pragma unroll
-  for (int k = 0; k < H; ++k) {
-    const int32_t ik = T.nbr[base + k * N];
-    if (ik < 0) continue;
-    double Dj[D];
-    st64::laplace64<D>(T, ik, f, Dj);
-    acc = acc + Dj[axis] * T.w[base + k * N];
-  }
-  return acc / T.nrm[(int64_t)dir * N + n];
-}
-
-template <int D>
-__global__ void __launch_bounds__(TPB) k_prep_subcell(DTab64<D> T, const int32_t* __restrict__ iperm, const double* __restrict__ phi0,
+__global__ void __launch_bounds__(TPB) k_prep_subcell(DTab32<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0_irr,
                                                       double zdt, int order_space, const int32_t* __restrict__ near_list,
                                                       const unsigned* __restrict__ near_count, uint16_t* __restrict__ status,
                                                       float* __restrict__ s_near) {
+  constexpr int H = Dim<D>::HALF;
   const int64_t N = T.N;
   const unsigned cnt = *near_count;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const int64_t n = near_list[k];
     const double p0 = phi0[n];
-    double Dv[D];
-    st64::laplace64<D>(T, n, phi0, Dv);
-    double s[2 * D];
+    double s[2 * D], Dv[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) Dv[a] = dd_axis64<D>(T, n, a, phi0, dd0_irr);
+    if (n < T.nR) {
+      const uint32_t codes = T.r_meta[n];
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = level_size64(T.tsize64[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
+    } else {
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.i_d64[(int64_t)dir * T.nI + (n - T.nR)];
+    }
     uint16_t st = ((p0 > 0.0) ? ST_POSITIVE : 0) | ST_NEAR;
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.d[(int64_t)dir * N + n];
-#pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
-      const double fn = st64::quad_nb64<D>(T, dir, n, phi0, Dv);
+      const double fn = quad_nb_m64<D>(T, n, dir, phi0, dd0_irr);
       if (!(p0 * fn < 0.0)) continue;
       st |= (uint16_t)(1u << (ST_CUT_SHIFT + dir));
       const int axis = dir >> 1;
+      double xx_nb = 0.0;
+      if (order_space > 1) {
+        // f_<dir>_linear of phi_0's second derivative along axis
+        if (n < T.nR) {
+          xx_nb = dd_axis64<D>(T, T.r_nbr[(int64_t)dir * T.nR + n], axis, phi0, dd0_irr);
+        } else {
+          const int64_t i = n - T.nR;
+          const uint32_t meta = T.i_meta[i];
+          const int c = face_count(meta, dir);
+          const int64_t base = (int64_t)(dir * H) * T.nI + i;
+          if (c == 1) {
+            xx_nb = dd_axis64<D>(T, T.i_nbr[base], axis, phi0, dd0_irr);
+          } else {
+            for (int kk = 0; kk < c; ++kk)
+              xx_nb = fma(T.i_wf64[base + kk * T.nI], dd_axis64<D>(T, T.i_nbr[base + kk * T.nI], axis, phi0, dd0_irr), xx_nb);
+          }
+        }
+      }
       if (dir & 1) {
         if (order_space > 1)
-          s[dir] = st64::interface_location_2nd(0.0, s[dir], p0, fn, Dv[axis], lin_dd64<D>(T, dir, axis, n, phi0));
+          s[dir] = st64::interface_location_2nd(0.0, s[dir], p0, fn, Dv[axis], xx_nb);
         else
           s[dir] = st64::interface_location(0.0, s[dir], p0, fn);
       } else {
         if (order_space > 1)
-          s[dir] = -st64::interface_location_2nd(-s[dir], 0.0, fn, p0, lin_dd64<D>(T, dir, axis, n, phi0), Dv[axis]);
+          s[dir] = -st64::interface_location_2nd(-s[dir], 0.0, fn, p0, xx_nb, Dv[axis]);
         else
           s[dir] = -st64::interface_location(-s[dir], 0.0, fn, p0);
       }
     }
-    const int64_t dv = iperm[n];
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) s_near[(int64_t)dir * N + dv] = (float)max2(s[dir], zdt);
-    status[dv] = st;
+    for (int dir = 0; dir < 2 * D; ++dir) s_near[(int64_t)dir * N + n] = (float)max2(s[dir], zdt);
+    status[n] = st;
   }
 }
 
@@ -411,13 +521,15 @@ void launch_dd32(const DTab32<D>& T, const float* f, float* dd, cudaStream_t s) 
 }
 
 template <int D>
-void launch_reinit_prep_mixed(const DTab64<D>& T, const int32_t* iperm, const double* phi0, double zdt, double lim_lo, double lim_hi,
-                              int order_space, uint16_t* status, float* s_near, int32_t* near_list, unsigned* near_count,
-                              cudaStream_t s) {
+void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const double* phi0, double zdt, double lim_lo, double lim_hi,
+                              int order_space, double* phi0_dev, double* dd0_irr, uint16_t* status, float* s_near, int32_t* near_list,
+                              unsigned* near_count, cudaStream_t s) {
   if (T.N == 0) return;
   cudaMemsetAsync(near_count, 0, sizeof(unsigned), s);
-  k_prep_classify<D><<<nblocks(T.N), TPB, 0, s>>>(T, iperm, phi0, zdt, lim_lo, lim_hi, status, near_list, near_count);
-  k_prep_subcell<D><<<152 * 4, TPB, 0, s>>>(T, iperm, phi0, zdt, order_space, near_list, near_count, status, s_near);
+  k_gather64<<<nblocks(T.N), TPB, 0, s>>>(phi0, perm, phi0_dev, T.N);
+  if (T.nI) k_dd0_irr<D><<<nblocks(T.nI), TPB, 0, s>>>(T, phi0_dev, dd0_irr);
+  k_prep_classify<D><<<nblocks(T.N), TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, lim_lo, lim_hi, status, near_list, near_count);
+  k_prep_subcell<D><<<152 * 8, TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, order_space, near_list, near_count, status, s_near);
 }
 
 template <int D>
@@ -459,8 +571,8 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
 
 #define LSG_INST(D)                                                                                                             \
   template void launch_dd32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                           \
-  template void launch_reinit_prep_mixed<D>(const DTab64<D>&, const int32_t*, const double*, double, double, double, int,       \
-                                            uint16_t*, float*, int32_t*, unsigned*, cudaStream_t);                              \
+  template void launch_reinit_prep_mixed<D>(const DTab32<D>&, const int32_t*, const double*, double, double, double, int,       \
+                                            double*, double*, uint16_t*, float*, int32_t*, unsigned*, cudaStream_t);            \
   template void launch_reinit_stage32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
                                          float*, const float*, cudaStream_t);                                                   \
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \

@@ -198,6 +198,10 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   i_q.upload(M.i_q, stream);
   i_cidx.upload(M.i_cidx, stream);
   corr32.upload(M.corr, stream);
+  i_wf64.upload(M.i_wf64, stream);
+  i_d64.upload(M.i_d64, stream);
+  i_q64.upload(M.i_q64, stream);
+  corr64.upload(M.corr64, stream);
   perm.upload(M.perm, stream);
   iperm.upload(M.iperm, stream);
   near_list.alloc((size_t)N);
@@ -219,6 +223,11 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   T32.i_q = i_q.p;
   T32.i_cidx = i_cidx.p;
   T32.corr = corr32.p;
+  for (int a = 0; a < 3; ++a) T32.tsize64[a] = a < D ? F->brick.tmax[a] - F->brick.tmin[a] : 1.0;
+  T32.i_wf64 = i_wf64.p;
+  T32.i_d64 = i_d64.p;
+  T32.i_q64 = i_q64.p;
+  T32.corr64 = corr64.p;
   mixed_ready = true;
 }
 
@@ -232,8 +241,10 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   f_dd.alloc((size_t)D * N);
   f_snear.alloc((size_t)2 * D * N);
   status.alloc(N);
-  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T64, iperm.p, phi, zdt, lo, hi, os, status.p, f_snear.p, near_list.p,
-                                                       near_count.p, stream));
+  phi0.alloc(N);
+  dd0.alloc((size_t)D * (nI > 0 ? nI : 1));
+  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T32, perm.p, phi, zdt, lo, hi, os, phi0.p, dd0.p, status.p, f_snear.p,
+                                                       near_list.p, near_count.p, stream));
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
     LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));

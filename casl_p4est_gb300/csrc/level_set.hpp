@@ -63,6 +63,7 @@ struct LevelSet {
   DevBuf<int32_t> r_nbr, i_nbr, i_cidx, perm, iperm, near_list;
   DevBuf<unsigned> near_count;
   DevBuf<float> i_wf, i_d, i_q, corr32;
+  DevBuf<double> i_wf64, i_d64, i_q64, corr64;
   DTab32<D> T32{};
   int64_t nR = 0, nI = 0;
   // work vectors

@@ -69,6 +69,8 @@ struct Tables32 {
   std::vector<float> i_q;           // 2D*(D-1) * nI
   std::vector<int32_t> i_cidx;      // nI
   std::vector<float> corr;          // D*D * R, row-major: corrected = corr * naive
+  // FP64 copies of the irregular coefficients, for the FP64 subcell step of the mixed path
+  std::vector<double> i_wf64, i_d64, i_q64, corr64;
 };
 
 template <int D>

@@ -185,6 +185,9 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
   M.i_d.assign((size_t)2 * D * nI, 0.0f);
   M.i_q.assign((size_t)2 * D * (D - 1) * nI, 0.0f);
   M.i_cidx.assign((size_t)nI, -1);
+  M.i_wf64.assign((size_t)NS * nI, 0.0);
+  M.i_d64.assign((size_t)2 * D * nI, 0.0);
+  M.i_q64.assign((size_t)2 * D * (D - 1) * nI, 0.0);
 #pragma omp parallel for schedule(static)
   for (long long ii = 0; ii < (long long)nI; ++ii) {
     const size_t n = (size_t)M.perm[nR + ii];
@@ -198,21 +201,31 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
       for (int k = 0; k < H; ++k) {
         const int32_t nb = T.nbr[(size_t)(dir * H + k) * N + n];
         M.i_nbr[(size_t)(dir * H + k) * nI + ii] = k < cnt ? M.iperm[nb] : M.iperm[T.nbr[(size_t)(dir * H) * N + n]];
-        M.i_wf[(size_t)(dir * H + k) * nI + ii] = k < cnt ? (float)(T.w[(size_t)(dir * H + k) * N + n] / nrm) : 0.0f;
+        const double wn = k < cnt ? T.w[(size_t)(dir * H + k) * N + n] / nrm : 0.0;
+        M.i_wf[(size_t)(dir * H + k) * nI + ii] = (float)wn;
+        M.i_wf64[(size_t)(dir * H + k) * nI + ii] = wn;
       }
       M.i_d[(size_t)dir * nI + ii] = (float)T.d[(size_t)dir * N + n];
-      for (int j = 0; j < D - 1; ++j) M.i_q[(size_t)(dir * (D - 1) + j) * nI + ii] = (float)T.q[(size_t)(dir * (D - 1) + j) * N + n];
+      M.i_d64[(size_t)dir * nI + ii] = T.d[(size_t)dir * N + n];
+      for (int j = 0; j < D - 1; ++j) {
+        M.i_q[(size_t)(dir * (D - 1) + j) * nI + ii] = (float)T.q[(size_t)(dir * (D - 1) + j) * N + n];
+        M.i_q64[(size_t)(dir * (D - 1) + j) * nI + ii] = T.q[(size_t)(dir * (D - 1) + j) * N + n];
+      }
     }
     M.i_cidx[ii] = T.cidx[n];
   }
   const size_t R = T.crec.size() / 6;
   M.corr.assign((size_t)D * D * R, 0.0f);
+  M.corr64.assign((size_t)D * D * R, 0.0);
   for (size_t r = 0; r < R; ++r) {
     for (int c = 0; c < D; ++c) {
       double e[3] = {0, 0, 0};
       e[c] = 1.0;
       apply_correction_host<D>(&T.crec[6 * r], e);
-      for (int rr = 0; rr < D; ++rr) M.corr[(size_t)D * D * r + D * rr + c] = (float)e[rr];
+      for (int rr = 0; rr < D; ++rr) {
+        M.corr[(size_t)D * D * r + D * rr + c] = (float)e[rr];
+        M.corr64[(size_t)D * D * r + D * rr + c] = e[rr];
+      }
     }
   }
 }
