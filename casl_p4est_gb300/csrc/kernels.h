@@ -79,6 +79,13 @@ void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const dou
 template <int D>
 void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd, float* out, const float* avg_with, cudaStream_t s);
+// fused stage: second derivatives of regular face nodes recomputed from phi, of irregular nodes
+// read from dd_irr (D x nI, written by launch_dd_irr32 for the same phi)
+template <int D>
+void launch_dd_irr32(const DTab32<D>& T, const float* f, float* dd_irr, cudaStream_t s);
+template <int D>
+void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
+                           const float* dd_irr, float* out, const float* avg_with, cudaStream_t s);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);

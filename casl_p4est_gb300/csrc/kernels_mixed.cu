@@ -220,6 +220,149 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
   out[n] = r;
 }
 
+// ---- fused reinitialisation stage ----------------------------------------------------------------
+// One stage of reinitialize_one_iteration per node without a separate second-derivative sweep: the
+// second derivatives of the face nodes along their axis are recomputed from phi here (regular face
+// nodes: central difference of two gathered values), or read from dd_irr for irregular face nodes
+// (written by k_dd_irr32 just before). phi (4 bytes/node) is the only gathered array.
+template <int D>
+__global__ void __launch_bounds__(TPB) k_dd_irr32(DTab32<D> T, const float* __restrict__ f, float* __restrict__ dd_irr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= T.nI) return;
+  const uint32_t meta = __ldg(T.i_meta + i);
+  const float f0 = __ldg(f + T.nR + i);
+  float Dv[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const float fm = lin_irr<D>(T, meta, 2 * a, i, f);
+    const float fp = lin_irr<D>(T, meta, 2 * a + 1, i, f);
+    Dv[a] = central_dd(fp, f0, fm, __ldg(T.i_d + (int64_t)(2 * a + 1) * T.nI + i), __ldg(T.i_d + (int64_t)(2 * a) * T.nI + i));
+  }
+  correct_irr<D>(T, meta, i, Dv);
+#pragma unroll
+  for (int a = 0; a < D; ++a) dd_irr[(int64_t)a * T.nI + i] = Dv[a];
+}
+
+// second derivative along `axis` of node j; fj = f[j]
+template <int D>
+__device__ __forceinline__ float dd_axis32(const DTab32<D>& T, int32_t j, int axis, float fj, const float* __restrict__ f,
+                                           const float* __restrict__ dd_irr) {
+  if (j >= T.nR) return __ldg(dd_irr + (int64_t)axis * T.nI + (j - T.nR));
+  const uint32_t codes = __ldg(T.r_meta + j);
+  const float fm = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * axis) * T.nR + j));
+  const float fp = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * axis + 1) * T.nR + j));
+  return central_dd(fp, fj, fm, level_size(T.tsize[axis], T.base, (codes >> (8 * axis + 4)) & 15u),
+                    level_size(T.tsize[axis], T.base, (codes >> (8 * axis)) & 15u));
+}
+
+template <int D, int ORDER_SPACE, bool AVG>
+__global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint16_t* __restrict__ status,
+                                                        const float* __restrict__ s_near, const float* __restrict__ phin,
+                                                        const float* __restrict__ dd_irr, float* out, const float* avg_with) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const uint16_t st = status[n];
+  float r;
+  if (st & ST_ANCHORED) {
+    r = 0.0f;
+  } else if (st & ST_OUTSIDE) {
+    r = phin[n];
+  } else {
+    const float f0 = __ldg(phin + n);
+    float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
+    if (n < T.nR) {
+      const Reg<D> R{__ldg(T.r_meta + n)};
+      int32_t nb[2 * D];
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        nb[dir] = __ldg(T.r_nbr + (int64_t)dir * T.nR + n);
+        s[dir] = R.d(T, dir);
+      }
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = __ldg(phin + nb[dir]);
+#pragma unroll
+      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
+      if (ORDER_SPACE > 1) {
+#pragma unroll
+        for (int dir = 0; dir < 2 * D; ++dir) xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
+      }
+    } else {
+      const int64_t i = n - T.nR;
+      const uint32_t meta = __ldg(T.i_meta + i);
+#pragma unroll
+      for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd_irr + (int64_t)a * T.nI + i);
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        const int axis = dir >> 1;
+        const int c = face_count(meta, dir);
+        const int64_t base = (int64_t)(dir * H) * T.nI + i;
+        s[dir] = __ldg(T.i_d + (int64_t)dir * T.nI + i);
+        if (c == 1) {
+          const int32_t j = __ldg(T.i_nbr + base);
+          fnb[dir] = __ldg(phin + j);
+          if (ORDER_SPACE > 1) xxnb[dir] = dd_axis32<D>(T, j, axis, fnb[dir], phin, dd_irr);
+        } else {
+          float v = 0.0f, x = 0.0f;
+#pragma unroll
+          for (int k = 0; k < H; ++k) {
+            if (k < c) {
+              const int32_t j = __ldg(T.i_nbr + base + k * T.nI);
+              const float w = __ldg(T.i_wf + base + k * T.nI);
+              const float fj = __ldg(phin + j);
+              v = fmaf(w, fj, v);
+              if (ORDER_SPACE > 1) x = fmaf(w, dd_axis32<D>(T, j, axis, fj, phin, dd_irr), x);
+            }
+          }
+#pragma unroll
+          for (int jj = 0; jj < D - 1; ++jj) v = fmaf(-__ldg(T.i_q + (int64_t)(dir * (D - 1) + jj) * T.nI + i), Dv[tan_axis32(axis, jj)], v);
+          fnb[dir] = v;
+          xxnb[dir] = x;
+        }
+      }
+      const uint32_t wl = meta >> 24;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        if (wl & (1u << (2 * a))) {
+          s[2 * a] = s[2 * a + 1];
+          fnb[2 * a] = fnb[2 * a + 1];
+          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
+        }
+        if (wl & (1u << (2 * a + 1))) {
+          s[2 * a + 1] = s[2 * a];
+          fnb[2 * a + 1] = fnb[2 * a];
+          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
+        }
+      }
+    }
+    if (st & ST_NEAR) {
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        s[dir] = __ldg(s_near + (int64_t)dir * N + n);
+        if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
+      }
+      if (n >= T.nR) {
+        const uint32_t wl = __ldg(T.i_meta + (n - T.nR)) >> 24;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          if (wl & (1u << (2 * a))) {
+            s[2 * a] = s[2 * a + 1];
+            fnb[2 * a] = fnb[2 * a + 1];
+          }
+          if (wl & (1u << (2 * a + 1))) {
+            s[2 * a + 1] = s[2 * a];
+            fnb[2 * a + 1] = fnb[2 * a];
+          }
+        }
+      }
+    }
+    r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+  }
+  if (AVG) r = 0.5f * (avg_with[n] + r);
+  out[n] = r;
+}
+
 template <int D, bool AVG>
 __global__ void __launch_bounds__(TPB) k_advect_stage32(DTab32<D> T, const float* __restrict__ phin, const float* __restrict__ ddq,
                                                         const float* __restrict__ ddm, const float* __restrict__ vn, float dt,
@@ -551,6 +694,29 @@ void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* 
 }
 
 template <int D>
+void launch_dd_irr32(const DTab32<D>& T, const float* f, float* dd_irr, cudaStream_t s) {
+  if (T.nI) k_dd_irr32<D><<<nblocks(T.nI), TPB, 0, s>>>(T, f, dd_irr);
+}
+
+template <int D>
+void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
+                           const float* dd_irr, float* out, const float* avg_with, cudaStream_t s) {
+  if (T.N == 0) return;
+  const unsigned g = nblocks(T.N);
+  if (order_space > 1) {
+    if (avg_with)
+      k_reinit_fused32<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    else
+      k_reinit_fused32<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+  } else {
+    if (avg_with)
+      k_reinit_fused32<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    else
+      k_reinit_fused32<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+  }
+}
+
+template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s) {
   if (T.N == 0) return;
@@ -576,7 +742,10 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
   template void launch_reinit_stage32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
                                          float*, const float*, cudaStream_t);                                                   \
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \
-                                         const float*, cudaStream_t);
+                                         const float*, cudaStream_t);                                                           \
+  template void launch_dd_irr32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                       \
+  template void launch_reinit_fused32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
+                                         float*, const float*, cudaStream_t);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

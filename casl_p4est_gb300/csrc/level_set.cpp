@@ -245,13 +245,14 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   dd0.alloc((size_t)D * (nI > 0 ? nI : 1));
   LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T32, perm.p, phi, zdt, lo, hi, os, phi0.p, dd0.p, status.p, f_snear.p,
                                                        near_list.p, near_count.p, stream));
+  timer.launches += 3;  // the FP64 subcell step is four kernels
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
-    LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi.p, f_dd.p, stream));
-    LSG_LAUNCH(K_STAGE32, launch_reinit_stage32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
+    LSG_LAUNCH(K_DD32, launch_dd_irr32<D>(T32, f_phi.p, f_dd.p, stream));
+    LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
     if (ot > 1) {
-      LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi1.p, f_dd.p, stream));
-      LSG_LAUNCH(K_STAGE32, launch_reinit_stage32<D>(T32, os, status.p, f_snear.p, f_phi1.p, f_dd.p, f_phi.p, f_phi.p, stream));
+      LSG_LAUNCH(K_DD32, launch_dd_irr32<D>(T32, f_phi1.p, f_dd.p, stream));
+      LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi1.p, f_dd.p, f_phi.p, f_phi.p, stream));
     } else {
       std::swap(f_phi.p, f_phi1.p);
     }
