@@ -9,6 +9,8 @@
 // laplace/correct_naive_second_derivatives, ngbd_with_quadratic_interpolation,
 // reinitialize_one_iteration and advect_in_normal_direction_one_iteration, with geometric divisions
 // folded into FP32 coefficients.
+#include <algorithm>
+
 #include "kernels.h"
 #include "stencil64.cuh"
 #include "tables.hpp"
@@ -258,11 +260,12 @@ __device__ __forceinline__ float dd_axis32(const DTab32<D>& T, int32_t j, int ax
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                         const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                        const float* __restrict__ dd_irr, float* out, const float* avg_with) {
+                                                        const float* __restrict__ dd_irr, float* out, const float* avg_with,
+                                                        int64_t first, int64_t last) {
   constexpr int H = Dim<D>::HALF;
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
-  if (n >= N) return;
+  if (n >= last) return;
   const uint16_t st = status[n];
   float r;
   if (st & ST_ANCHORED) {
@@ -361,6 +364,68 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
   }
   if (AVG) r = 0.5f * (avg_with[n] + r);
   out[n] = r;
+}
+
+// Regular nodes, persistent and software-pipelined: while a node's gathers are in flight the
+// thread already loads the next node's status, level codes, face-node indices and value.
+template <int D, int ORDER_SPACE, bool AVG>
+__global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const uint16_t* __restrict__ status,
+                                                            const float* __restrict__ s_near, const float* __restrict__ phin,
+                                                            const float* __restrict__ dd_irr, float* out, const float* avg_with) {
+  const int64_t N = T.N, nR = T.nR;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint16_t p_st = 0;
+  uint32_t p_codes = 0;
+  int32_t p_nb[2 * D];
+  float p_f0 = 0.0f, p_avg = 0.0f;
+  auto prefetch = [&](int64_t m) {
+    p_st = status[m];
+    p_codes = __ldg(T.r_meta + m);
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) p_nb[dir] = __ldg(T.r_nbr + (int64_t)dir * nR + m);
+    p_f0 = __ldg(phin + m);
+    if (AVG) p_avg = avg_with[m];
+  };
+  if (n < nR) prefetch(n);
+  for (; n < nR; n += stride) {
+    const uint16_t st = p_st;
+    const Reg<D> R{p_codes};
+    int32_t nb[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) nb[dir] = p_nb[dir];
+    const float f0 = p_f0, avg = p_avg;
+    if (n + stride < nR) prefetch(n + stride);
+    float r;
+    if (st & ST_ANCHORED) {
+      r = 0.0f;
+    } else if (st & ST_OUTSIDE) {
+      r = f0;
+    } else {
+      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
+#pragma unroll
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        fnb[dir] = __ldg(phin + nb[dir]);
+        s[dir] = R.d(T, dir);
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
+      if (ORDER_SPACE > 1) {
+#pragma unroll
+        for (int dir = 0; dir < 2 * D; ++dir) xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
+      }
+      if (st & ST_NEAR) {
+#pragma unroll
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          s[dir] = __ldg(s_near + (int64_t)dir * N + n);
+          if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
+        }
+      }
+      r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+    }
+    if (AVG) r = 0.5f * (avg + r);
+    out[n] = r;
+  }
 }
 
 template <int D, bool AVG>
@@ -702,17 +767,33 @@ template <int D>
 void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd_irr, float* out, const float* avg_with, cudaStream_t s) {
   if (T.N == 0) return;
-  const unsigned g = nblocks(T.N);
+  static int reg_blocks = 0;
+  if (reg_blocks == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reinit_fused_reg32<D, 2, true>, TPB, 0);
+    reg_blocks = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const unsigned gi = nblocks(T.nI);
+  const int64_t lo = T.nR, hi = T.N;
+  const unsigned gr = (unsigned)std::min<int64_t>(reg_blocks, nblocks(T.nR));
   if (order_space > 1) {
-    if (avg_with)
-      k_reinit_fused32<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    else
-      k_reinit_fused32<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    if (avg_with) {
+      if (T.nI) k_reinit_fused32<D, 2, true><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
+      if (T.nR) k_reinit_fused_reg32<D, 2, true><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    } else {
+      if (T.nI) k_reinit_fused32<D, 2, false><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
+      if (T.nR) k_reinit_fused_reg32<D, 2, false><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    }
   } else {
-    if (avg_with)
-      k_reinit_fused32<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    else
-      k_reinit_fused32<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    if (avg_with) {
+      if (T.nI) k_reinit_fused32<D, 1, true><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
+      if (T.nR) k_reinit_fused_reg32<D, 1, true><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    } else {
+      if (T.nI) k_reinit_fused32<D, 1, false><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
+      if (T.nR) k_reinit_fused_reg32<D, 1, false><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
+    }
   }
 }
 
