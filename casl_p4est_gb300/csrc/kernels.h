@@ -37,6 +37,8 @@ struct DTab32 {
   float tsize[3];        // tree size per axis
   const uint32_t* r_meta;
   const int32_t* r_nbr;  // 2D x nR
+  const int32_t* r_nbr2; // 2D x nR, -1 when absent
+  const uint32_t* r_meta2;
   const uint32_t* i_meta;
   const int32_t* i_nbr;  // NS x nI
   const float* i_wf;     // NS x nI

@@ -367,33 +367,43 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
 }
 
 // Regular nodes, persistent and software-pipelined: while a node's gathers are in flight the
-// thread already loads the next node's status, level codes, face-node indices and value.
+// thread already loads the next node's status, level codes, face-node and second-neighbour indices
+// and value. A face node's second derivative along its axis is a central difference of
+// (second neighbour, face node, this node) when the second neighbour is recorded; otherwise it is
+// rebuilt from the face node's own table (dd_axis32).
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                             const float* __restrict__ s_near, const float* __restrict__ phin,
                                                             const float* __restrict__ dd_irr, float* out, const float* avg_with) {
-  const int64_t N = T.N, nR = T.nR;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nR = (int)T.nR;
+  const int stride = gridDim.x * blockDim.x;
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
   uint16_t p_st = 0;
-  uint32_t p_codes = 0;
-  int32_t p_nb[2 * D];
+  uint32_t p_codes = 0, p_far = 0;
+  int32_t p_nb[2 * D], p_nb2[2 * D];
   float p_f0 = 0.0f, p_avg = 0.0f;
-  auto prefetch = [&](int64_t m) {
+  auto prefetch = [&](int m) {
     p_st = status[m];
     p_codes = __ldg(T.r_meta + m);
+    p_far = __ldg(T.r_meta2 + m);
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) p_nb[dir] = __ldg(T.r_nbr + (int64_t)dir * nR + m);
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      p_nb[dir] = __ldg(T.r_nbr + dir * nR + m);
+      if (ORDER_SPACE > 1) p_nb2[dir] = __ldg(T.r_nbr2 + dir * nR + m);
+    }
     p_f0 = __ldg(phin + m);
     if (AVG) p_avg = avg_with[m];
   };
   if (n < nR) prefetch(n);
   for (; n < nR; n += stride) {
     const uint16_t st = p_st;
-    const Reg<D> R{p_codes};
-    int32_t nb[2 * D];
+    const uint32_t codes = p_codes, far = p_far;
+    int32_t nb[2 * D], nb2[2 * D];
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) nb[dir] = p_nb[dir];
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      nb[dir] = p_nb[dir];
+      nb2[dir] = p_nb2[dir];
+    }
     const float f0 = p_f0, avg = p_avg;
     if (n + stride < nR) prefetch(n + stride);
     float r;
@@ -402,22 +412,40 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     } else if (st & ST_OUTSIDE) {
       r = f0;
     } else {
-      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
+      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fn2[2 * D];
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
         fnb[dir] = __ldg(phin + nb[dir]);
-        s[dir] = R.d(T, dir);
+        if (ORDER_SPACE > 1 && (far >> 31)) fn2[dir] = __ldg(phin + nb2[dir]);
+        s[dir] = level_size(T.tsize[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
       }
 #pragma unroll
       for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
       if (ORDER_SPACE > 1) {
+        if (far >> 31) {
 #pragma unroll
-        for (int dir = 0; dir < 2 * D; ++dir) xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
+          for (int dir = 0; dir < 2 * D; ++dir) {
+            const float dfar = level_size(T.tsize[dir >> 1], T.base, (far >> (4 * dir)) & 15u);
+            // outer side of the face node: second neighbour; inner side: this node
+            xxnb[dir] = (dir & 1) ? central_dd(fn2[dir], fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], fn2[dir], s[dir], dfar);
+          }
+        } else {
+#pragma unroll
+          for (int dir = 0; dir < 2 * D; ++dir) {
+            if (nb2[dir] >= 0) {
+              const float dfar = level_size(T.tsize[dir >> 1], T.base, (far >> (4 * dir)) & 15u);
+              const float f2 = __ldg(phin + nb2[dir]);
+              xxnb[dir] = (dir & 1) ? central_dd(f2, fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], f2, s[dir], dfar);
+            } else {
+              xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
+            }
+          }
+        }
       }
       if (st & ST_NEAR) {
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) {
-          s[dir] = __ldg(s_near + (int64_t)dir * N + n);
+          s[dir] = __ldg(s_near + (int64_t)dir * T.N + n);
           if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
         }
       }

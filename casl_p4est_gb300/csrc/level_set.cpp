@@ -191,6 +191,8 @@ template <int D>
 void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   r_meta.upload(M.r_meta, stream);
   r_nbr.upload(M.r_nbr, stream);
+  r_nbr2.upload(M.r_nbr2, stream);
+  r_meta2.upload(M.r_meta2, stream);
   i_meta.upload(M.i_meta, stream);
   i_nbr.upload(M.i_nbr, stream);
   i_wf.upload(M.i_wf, stream);
@@ -216,6 +218,8 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)(F->brick.tmax[a] - F->brick.tmin[a]) : 1.0f;
   T32.r_meta = r_meta.p;
   T32.r_nbr = r_nbr.p;
+  T32.r_nbr2 = r_nbr2.p;
+  T32.r_meta2 = r_meta2.p;
   T32.i_meta = i_meta.p;
   T32.i_nbr = i_nbr.p;
   T32.i_wf = i_wf.p;

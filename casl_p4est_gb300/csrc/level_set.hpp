@@ -59,8 +59,8 @@ struct LevelSet {
   DTab64<D> T64{};
   // mixed tables (built on first mixed call)
   bool mixed_ready = false;
-  DevBuf<uint32_t> r_meta, i_meta;
-  DevBuf<int32_t> r_nbr, i_nbr, i_cidx, perm, iperm, near_list;
+  DevBuf<uint32_t> r_meta, i_meta, r_meta2;
+  DevBuf<int32_t> r_nbr, r_nbr2, i_nbr, i_cidx, perm, iperm, near_list;
   DevBuf<unsigned> near_count;
   DevBuf<float> i_wf, i_d, i_q, corr32;
   DevBuf<double> i_wf64, i_d64, i_q64, corr64;

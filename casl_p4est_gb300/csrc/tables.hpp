@@ -61,6 +61,11 @@ struct Tables32 {
   // regular group (device indices 0 .. nR-1)
   std::vector<uint32_t> r_meta;     // nR: 4-bit level code per direction
   std::vector<int32_t> r_nbr;       // 2D * nR, device indices
+  // second neighbour along each direction (the face node's own face node further out), valid when
+  // the face node is regular and its opposite face node is this node; -1 otherwise
+  std::vector<int32_t> r_nbr2;      // 2D * nR
+  std::vector<uint32_t> r_meta2;    // nR: 4-bit level code of the face node's outer distance per direction,
+                                    //     bit 31 set when every direction has a second neighbour
   // irregular group (device indices nR .. N-1, stored at [i - nR])
   std::vector<uint32_t> i_meta;     // nI: counts (2 bits/dir), bit 16 correction, bits 24.. walls
   std::vector<int32_t> i_nbr;       // NS * nI, device indices

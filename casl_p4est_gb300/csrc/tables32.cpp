@@ -178,6 +178,24 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     }
     M.r_meta[ii] = codes;
   }
+  M.r_nbr2.assign((size_t)2 * D * nR, -1);
+  M.r_meta2.assign((size_t)nR, 0u);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nR; ++ii) {
+    uint32_t far = 0;
+    bool all = true;
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int32_t j = M.r_nbr[(size_t)dir * nR + ii];
+      const int back = dir ^ 1;
+      if (j < nR && M.r_nbr[(size_t)back * nR + j] == (int32_t)ii) {
+        M.r_nbr2[(size_t)dir * nR + ii] = M.r_nbr[(size_t)dir * nR + j];
+        far |= ((M.r_meta[j] >> (4 * dir)) & 15u) << (4 * dir);
+      } else {
+        all = false;
+      }
+    }
+    M.r_meta2[ii] = far | (all ? (1u << 31) : 0u);
+  }
   // irregular group
   M.i_meta.assign((size_t)nI, 0u);
   M.i_nbr.assign((size_t)NS * nI, 0);
