@@ -46,6 +46,10 @@ struct DTab32 {
   const float* i_q;      // 2D(D-1) x nI
   const int32_t* i_cidx;
   const float* corr;     // D*D x R
+  const uint32_t* i_cls; // nI: geometry class of each irregular node
+  const float* cls32;    // class records (cls_words<D>() floats each)
+  const int32_t* x_list; // regular nodes of the extended second-derivative set
+  int64_t nX;
   // FP64 coefficients of the irregular nodes (subcell step)
   double tsize64[3];
   const double* i_wf64;
@@ -81,10 +85,10 @@ void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const dou
 template <int D>
 void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd, float* out, const float* avg_with, cudaStream_t s);
-// fused stage: second derivatives of regular face nodes recomputed from phi, of irregular nodes
-// read from dd_irr (D x nI, written by launch_dd_irr32 for the same phi)
+// fused stage: second derivatives of face nodes rebuilt from recorded second neighbours, or read from
+// ddx (D x N, written by launch_dd_x32 for the same phi on the extended set)
 template <int D>
-void launch_dd_irr32(const DTab32<D>& T, const float* f, float* dd_irr, cudaStream_t s);
+void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s);
 template <int D>
 void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd_irr, float* out, const float* avg_with, cudaStream_t s);

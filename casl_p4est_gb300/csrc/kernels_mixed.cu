@@ -226,35 +226,83 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
 // One stage of reinitialize_one_iteration per node without a separate second-derivative sweep: the
 // second derivatives of the face nodes along their axis are recomputed from phi here (regular face
 // nodes: central difference of two gathered values), or read from dd_irr for irregular face nodes
-// (written by k_dd_irr32 just before). phi (4 bytes/node) is the only gathered array.
+// (written by k_dd_x32 just before on the extended set).
+// class record accessors (layout in tables.hpp)
 template <int D>
-__global__ void __launch_bounds__(TPB) k_dd_irr32(DTab32<D> T, const float* __restrict__ f, float* __restrict__ dd_irr) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= T.nI) return;
-  const uint32_t meta = __ldg(T.i_meta + i);
-  const float f0 = __ldg(f + T.nR + i);
-  float Dv[D];
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    const float fm = lin_irr<D>(T, meta, 2 * a, i, f);
-    const float fp = lin_irr<D>(T, meta, 2 * a + 1, i, f);
-    Dv[a] = central_dd(fp, f0, fm, __ldg(T.i_d + (int64_t)(2 * a + 1) * T.nI + i), __ldg(T.i_d + (int64_t)(2 * a) * T.nI + i));
+struct Cls {
+  const float* c;
+  __device__ __forceinline__ uint32_t meta() const { return __float_as_uint(__ldg(c)); }
+  __device__ __forceinline__ float d(int dir) const { return __ldg(c + 1 + dir); }
+  __device__ __forceinline__ float wf(int dir, int k) const { return __ldg(c + 1 + 2 * D + dir * Dim<D>::HALF + k); }
+  __device__ __forceinline__ float q(int dir, int j) const { return __ldg(c + 1 + 2 * D + 2 * D * Dim<D>::HALF + dir * (D - 1) + j); }
+  __device__ __forceinline__ float corr(int r, int col) const {
+    return __ldg(c + 1 + 2 * D + 2 * D * Dim<D>::HALF + 2 * D * (D - 1) + r * D + col);
   }
-  correct_irr<D>(T, meta, i, Dv);
-#pragma unroll
-  for (int a = 0; a < D; ++a) dd_irr[(int64_t)a * T.nI + i] = Dv[a];
+};
+
+template <int D>
+__device__ __forceinline__ Cls<D> cls_of(const DTab32<D>& T, int64_t i) {
+  return Cls<D>{T.cls32 + (int64_t)__ldg(T.i_cls + i) * cls_words<D>()};
 }
 
-// second derivative along `axis` of node j; fj = f[j]
+// linear interpolation over the face nodes of an irregular node (class weights)
 template <int D>
-__device__ __forceinline__ float dd_axis32(const DTab32<D>& T, int32_t j, int axis, float fj, const float* __restrict__ f,
-                                           const float* __restrict__ dd_irr) {
-  if (j >= T.nR) return __ldg(dd_irr + (int64_t)axis * T.nI + (j - T.nR));
-  const uint32_t codes = __ldg(T.r_meta + j);
-  const float fm = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * axis) * T.nR + j));
-  const float fp = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * axis + 1) * T.nR + j));
-  return central_dd(fp, fj, fm, level_size(T.tsize[axis], T.base, (codes >> (8 * axis + 4)) & 15u),
-                    level_size(T.tsize[axis], T.base, (codes >> (8 * axis)) & 15u));
+__device__ __forceinline__ float lin_cls(const DTab32<D>& T, const Cls<D>& C, uint32_t meta, int dir, int64_t i, const float* __restrict__ f) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t base = (int64_t)(dir * H) * T.nI + i;
+  const int c = face_count(meta, dir);
+  if (c == 1) return __ldg(f + __ldg(T.i_nbr + base));
+  float acc = 0.0f;
+#pragma unroll
+  for (int k = 0; k < H; ++k)
+    if (k < c) acc = fmaf(C.wf(dir, k), __ldg(f + __ldg(T.i_nbr + base + k * T.nI)), acc);
+  return acc;
+}
+
+// second derivatives on the extended set: irregular nodes (laplace with the class coefficients and
+// the correction matrix) and the listed regular nodes (central differences)
+template <int D>
+__global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __restrict__ f, float* __restrict__ ddx) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  float Dv[D];
+  int64_t n;
+  if (t < T.nI) {
+    const int64_t i = t;
+    n = T.nR + i;
+    const Cls<D> C = cls_of<D>(T, i);
+    const uint32_t meta = C.meta();
+    const float f0 = __ldg(f + n);
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+      Dv[a] = central_dd(lin_cls<D>(T, C, meta, 2 * a + 1, i, f), f0, lin_cls<D>(T, C, meta, 2 * a, i, f), C.d(2 * a + 1), C.d(2 * a));
+    if (meta & (1u << 16)) {
+      float o[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc = fmaf(C.corr(r, c), Dv[c], acc);
+        o[r] = acc;
+      }
+#pragma unroll
+      for (int r = 0; r < D; ++r) Dv[r] = o[r];
+    }
+  } else if (t < T.nI + T.nX) {
+    n = __ldg(T.x_list + (t - T.nI));
+    const Reg<D> R{__ldg(T.r_meta + n)};
+    const float f0 = __ldg(f + n);
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const float fm = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a) * T.nR + n));
+      const float fp = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a + 1) * T.nR + n));
+      Dv[a] = central_dd(fp, f0, fm, R.d(T, 2 * a + 1), R.d(T, 2 * a));
+    }
+  } else {
+    return;
+  }
+#pragma unroll
+  for (int a = 0; a < D; ++a) ddx[(int64_t)a * N + n] = Dv[a];
 }
 
 template <int D, int ORDER_SPACE, bool AVG>
@@ -275,51 +323,36 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
   } else {
     const float f0 = __ldg(phin + n);
     float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
-    if (n < T.nR) {
-      const Reg<D> R{__ldg(T.r_meta + n)};
-      int32_t nb[2 * D];
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        nb[dir] = __ldg(T.r_nbr + (int64_t)dir * T.nR + n);
-        s[dir] = R.d(T, dir);
-      }
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = __ldg(phin + nb[dir]);
-#pragma unroll
-      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
-      if (ORDER_SPACE > 1) {
-#pragma unroll
-        for (int dir = 0; dir < 2 * D; ++dir) xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
-      }
-    } else {
+    {
+      // irregular nodes only (regular ones run in k_reinit_fused_reg32)
       const int64_t i = n - T.nR;
-      const uint32_t meta = __ldg(T.i_meta + i);
+      const Cls<D> C = cls_of<D>(T, i);
+      const uint32_t meta = C.meta();
 #pragma unroll
-      for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd_irr + (int64_t)a * T.nI + i);
+      for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd_irr + (int64_t)a * N + n);
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
         const int axis = dir >> 1;
         const int c = face_count(meta, dir);
         const int64_t base = (int64_t)(dir * H) * T.nI + i;
-        s[dir] = __ldg(T.i_d + (int64_t)dir * T.nI + i);
+        s[dir] = C.d(dir);
         if (c == 1) {
           const int32_t j = __ldg(T.i_nbr + base);
           fnb[dir] = __ldg(phin + j);
-          if (ORDER_SPACE > 1) xxnb[dir] = dd_axis32<D>(T, j, axis, fnb[dir], phin, dd_irr);
+          if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd_irr + (int64_t)axis * N + j);
         } else {
           float v = 0.0f, x = 0.0f;
 #pragma unroll
           for (int k = 0; k < H; ++k) {
             if (k < c) {
               const int32_t j = __ldg(T.i_nbr + base + k * T.nI);
-              const float w = __ldg(T.i_wf + base + k * T.nI);
-              const float fj = __ldg(phin + j);
-              v = fmaf(w, fj, v);
-              if (ORDER_SPACE > 1) x = fmaf(w, dd_axis32<D>(T, j, axis, fj, phin, dd_irr), x);
+              const float w = C.wf(dir, k);
+              v = fmaf(w, __ldg(phin + j), v);
+              if (ORDER_SPACE > 1) x = fmaf(w, __ldg(dd_irr + (int64_t)axis * N + j), x);
             }
           }
 #pragma unroll
-          for (int jj = 0; jj < D - 1; ++jj) v = fmaf(-__ldg(T.i_q + (int64_t)(dir * (D - 1) + jj) * T.nI + i), Dv[tan_axis32(axis, jj)], v);
+          for (int jj = 0; jj < D - 1; ++jj) v = fmaf(-C.q(dir, jj), Dv[tan_axis32(axis, jj)], v);
           fnb[dir] = v;
           xxnb[dir] = x;
         }
@@ -346,7 +379,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
       }
       if (n >= T.nR) {
-        const uint32_t wl = __ldg(T.i_meta + (n - T.nR)) >> 24;
+        const uint32_t wl = cls_of<D>(T, n - T.nR).meta() >> 24;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
           if (wl & (1u << (2 * a))) {
@@ -370,7 +403,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
 // thread already loads the next node's status, level codes, face-node and second-neighbour indices
 // and value. A face node's second derivative along its axis is a central difference of
 // (second neighbour, face node, this node) when the second neighbour is recorded; otherwise it is
-// rebuilt from the face node's own table (dd_axis32).
+// read from the extended second-derivative set (k_dd_x32).
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                             const float* __restrict__ s_near, const float* __restrict__ phin,
@@ -411,6 +444,30 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
       r = 0.0f;
     } else if (st & ST_OUTSIDE) {
       r = f0;
+    } else if (ORDER_SPACE > 1 && ((far >> 30) & 1u) && !(st & ST_NEAR)) {
+      // uniform stencil: equal spacing h_a along each axis for the node and its face nodes
+      const uint32_t code = codes & 15u;
+      const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
+      float hmin = 3.0e38f, hsum = 0.0f;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const float h = level_size(T.tsize[a], T.base, code);
+        const float ih = __frcp_rn(h);
+        const float ih2 = ih * ih;
+        const float fm = __ldg(phin + nb[2 * a]), fp = __ldg(phin + nb[2 * a + 1]);
+        const float fmm = __ldg(phin + nb2[2 * a]), fpp = __ldg(phin + nb2[2 * a + 1]);
+        const float xx0 = (fp + fm - 2.0f * f0) * ih2;
+        const float xm = (f0 + fmm - 2.0f * fm) * ih2;
+        const float xp = (fpp + f0 - 2.0f * fp) * ih2;
+        float gm = fmaf(0.5f * h, minmodf(xm, xx0), (f0 - fm) * ih);
+        float gp = fmaf(-0.5f * h, minmodf(xp, xx0), (fp - f0) * ih);
+        if (sgn * gp > 0.0f) gp = 0.0f;
+        if (sgn * gm < 0.0f) gm = 0.0f;
+        hsum += fmaxf(gp * gp, gm * gm);
+        hmin = fminf(hmin, h);
+      }
+      r = f0 - hmin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
+      if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
     } else {
       float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fn2[2 * D];
 #pragma unroll
@@ -437,7 +494,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
               const float f2 = __ldg(phin + nb2[dir]);
               xxnb[dir] = (dir & 1) ? central_dd(f2, fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], f2, s[dir], dfar);
             } else {
-              xxnb[dir] = dd_axis32<D>(T, nb[dir], dir >> 1, fnb[dir], phin, dd_irr);
+              xxnb[dir] = __ldg(dd_irr + (int64_t)(dir >> 1) * T.N + nb[dir]);
             }
           }
         }
@@ -787,8 +844,8 @@ void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* 
 }
 
 template <int D>
-void launch_dd_irr32(const DTab32<D>& T, const float* f, float* dd_irr, cudaStream_t s) {
-  if (T.nI) k_dd_irr32<D><<<nblocks(T.nI), TPB, 0, s>>>(T, f, dd_irr);
+void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s) {
+  if (T.nI + T.nX) k_dd_x32<D><<<nblocks(T.nI + T.nX), TPB, 0, s>>>(T, f, ddx);
 }
 
 template <int D>
@@ -852,7 +909,7 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
                                          float*, const float*, cudaStream_t);                                                   \
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \
                                          const float*, cudaStream_t);                                                           \
-  template void launch_dd_irr32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                       \
+  template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                       \
   template void launch_reinit_fused32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
                                          float*, const float*, cudaStream_t);
 LSG_INST(2)

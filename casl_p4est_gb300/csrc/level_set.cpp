@@ -192,6 +192,9 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   r_meta.upload(M.r_meta, stream);
   r_nbr.upload(M.r_nbr, stream);
   r_nbr2.upload(M.r_nbr2, stream);
+  i_cls.upload(M.i_cls, stream);
+  cls32.upload(M.cls32, stream);
+  x_list.upload(M.x_list, stream);
   r_meta2.upload(M.r_meta2, stream);
   i_meta.upload(M.i_meta, stream);
   i_nbr.upload(M.i_nbr, stream);
@@ -219,6 +222,10 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   T32.r_meta = r_meta.p;
   T32.r_nbr = r_nbr.p;
   T32.r_nbr2 = r_nbr2.p;
+  T32.i_cls = i_cls.p;
+  T32.cls32 = cls32.p;
+  T32.x_list = x_list.p;
+  T32.nX = (int64_t)M.x_list.size();
   T32.r_meta2 = r_meta2.p;
   T32.i_meta = i_meta.p;
   T32.i_nbr = i_nbr.p;
@@ -252,10 +259,10 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   timer.launches += 3;  // the FP64 subcell step is four kernels
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
-    LSG_LAUNCH(K_DD32, launch_dd_irr32<D>(T32, f_phi.p, f_dd.p, stream));
+    LSG_LAUNCH(K_DD32, launch_dd_x32<D>(T32, f_phi.p, f_dd.p, stream));
     LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
     if (ot > 1) {
-      LSG_LAUNCH(K_DD32, launch_dd_irr32<D>(T32, f_phi1.p, f_dd.p, stream));
+      LSG_LAUNCH(K_DD32, launch_dd_x32<D>(T32, f_phi1.p, f_dd.p, stream));
       LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi1.p, f_dd.p, f_phi.p, f_phi.p, stream));
     } else {
       std::swap(f_phi.p, f_phi1.p);

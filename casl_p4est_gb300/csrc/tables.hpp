@@ -66,9 +66,19 @@ struct Tables32 {
   std::vector<int32_t> r_nbr2;      // 2D * nR
   std::vector<uint32_t> r_meta2;    // nR: 4-bit level code of the face node's outer distance per direction,
                                     //     bit 31 set when every direction has a second neighbour
-  // irregular group (device indices nR .. N-1, stored at [i - nR])
+  // irregular group (device indices nR .. N-1, stored at [i - nR]), sorted by geometry class
   std::vector<uint32_t> i_meta;     // nI: counts (2 bits/dir), bit 16 correction, bits 24.. walls
+  std::vector<uint32_t> i_cls;      // nI: geometry class (index into cls32/cls64)
   std::vector<int32_t> i_nbr;       // NS * nI, device indices
+  // geometry classes of the irregular nodes: meta word, then per direction d, normalised weights,
+  // third-order factors, then the correction matrix (identity when none), as floats (cls32) and doubles
+  // (cls64); CLS_WORDS(D) entries per class
+  std::vector<float> cls32;
+  std::vector<double> cls64;
+  int64_t ncls = 0;
+  // nodes whose second derivatives are computed by the extended pass: the irregular nodes and every
+  // face node that the fused stage cannot rebuild from a second neighbour (regular ones listed here)
+  std::vector<int32_t> x_list;
   std::vector<float> i_wf;          // NS * nI
   std::vector<float> i_d;           // 2D * nI
   std::vector<float> i_q;           // 2D*(D-1) * nI
@@ -80,6 +90,11 @@ struct Tables32 {
 
 template <int D>
 void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& M);
+
+// class record layout: [0] meta (bits), [1 + dir] d, [1 + 2D + dir*H + k] wf, [1 + 2D + 2D*H + dir*(D-1) + j] q,
+// [1 + 2D + 2D*H + 2D*(D-1) + r*D + c] correction
+template <int D>
+LSG_HD constexpr int cls_words() { return 1 + 2 * D + 2 * D * Dim<D>::HALF + 2 * D * (D - 1) + D * D; }
 
 // Cross-term coefficients of one record, exactly as correct_naive_second_derivatives computes them.
 template <int D>

@@ -14,6 +14,7 @@
 //              naive second derivatives, so it is evaluated in FP64 on the unit vectors).
 // Regular nodes come first, each group keeps the node order (tree-major Morton) of the grid.
 #include <algorithm>
+#include <cstring>
 #include <stdexcept>
 
 #include "tables.hpp"
@@ -128,8 +129,11 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
   for (int a = 0; a < D; ++a)
     for (int c = 0; c < 16; ++c) M.level_size[a * 16 + c] = (float)ldexp(tree_size[a], -(base + c));
 
-  std::vector<uint64_t> key((size_t)N);
+  // classification and geometry classes of the irregular nodes
+  constexpr int CW = cls_words<D>();
+  std::vector<uint8_t> is_reg((size_t)N, 0);
   std::vector<uint32_t> icount((size_t)N);
+  std::vector<double> rec((size_t)N * CW, 0.0);  // class record per node (irregular only)
 #pragma omp parallel for schedule(static)
   for (long long nn = 0; nn < (long long)N; ++nn) {
     const size_t n = (size_t)nn;
@@ -147,21 +151,64 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
       if (lc < base || lc > base + 15) regular = false;
     }
     icount[n] = counts;
-    const uint64_t pattern = (uint64_t)counts | ((uint64_t)(T.cidx[n] >= 0) << 16) | ((uint64_t)T.wall[n] << 17);
-    // regular nodes first in node order; irregular ones by (pattern, node)
-    key[n] = regular ? (uint64_t)n : ((uint64_t)1 << 63) | (pattern << 32) | (uint64_t)n;
+    is_reg[n] = regular ? 1 : 0;
+    if (regular) continue;
+    double* r = &rec[n * CW];
+    uint32_t meta = counts | ((T.cidx[n] >= 0) ? (1u << 16) : 0u) | ((uint32_t)T.wall[n] << 24);
+    r[0] = (double)meta;
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int cnt = (int)((counts >> (2 * dir)) & 3) + 1;
+      r[1 + dir] = T.d[(size_t)dir * N + n];
+      const double nrm = T.nrm[(size_t)dir * N + n];
+      for (int k = 0; k < H; ++k) r[1 + 2 * D + dir * H + k] = k < cnt ? T.w[(size_t)(dir * H + k) * N + n] / nrm : 0.0;
+      for (int j = 0; j < D - 1; ++j) r[1 + 2 * D + 2 * D * H + dir * (D - 1) + j] = T.q[(size_t)(dir * (D - 1) + j) * N + n];
+    }
+    double* cm = r + 1 + 2 * D + 2 * D * H + 2 * D * (D - 1);
+    for (int c = 0; c < D; ++c) {
+      double e[3] = {0, 0, 0};
+      e[c] = 1.0;
+      if (T.cidx[n] >= 0) apply_correction_host<D>(&T.crec[6 * (size_t)T.cidx[n]], e);
+      for (int rr = 0; rr < D; ++rr) cm[rr * D + c] = e[rr];
+    }
   }
-  std::vector<uint64_t> sorted = key;
-  std::sort(sorted.begin(), sorted.end());
+  // deduplicate class records (exact double keys)
+  std::vector<int64_t> irr_nodes;
+  for (int64_t n = 0; n < N; ++n)
+    if (!is_reg[n]) irr_nodes.push_back(n);
+  std::vector<int64_t> order(irr_nodes);
+  std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
+    const int c = memcmp(&rec[x * CW], &rec[y * CW], CW * sizeof(double));
+    return c != 0 ? c < 0 : x < y;
+  });
+  std::vector<int32_t> node_cls((size_t)N, -1);
+  M.cls64.clear();
+  int64_t ncls = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    if (i == 0 || memcmp(&rec[order[i] * CW], &rec[order[i - 1] * CW], CW * sizeof(double)) != 0) {
+      M.cls64.insert(M.cls64.end(), &rec[order[i] * CW], &rec[order[i] * CW] + CW);
+      ++ncls;
+    }
+    node_cls[order[i]] = (int32_t)(ncls - 1);
+  }
+  M.ncls = ncls;
+  M.cls32.resize(M.cls64.size());
+  for (size_t i = 0; i < M.cls64.size(); ++i) M.cls32[i] = (float)M.cls64[i];
+  // meta words are bit patterns, not values
+  for (int64_t c = 0; c < ncls; ++c) {
+    const uint32_t meta = (uint32_t)M.cls64[(size_t)c * CW];
+    memcpy(&M.cls32[(size_t)c * CW], &meta, sizeof(uint32_t));
+  }
+  // device order: regular nodes (node order), then irregular nodes by (class, node)
   M.perm.resize((size_t)N);
   M.iperm.resize((size_t)N);
   int64_t nR = 0;
-  for (int64_t i = 0; i < N; ++i) {
-    const int64_t n = (int64_t)(sorted[i] & 0xFFFFFFFFull);
-    M.perm[i] = (int32_t)n;
-    M.iperm[n] = (int32_t)i;
-    if (!(sorted[i] >> 63)) ++nR;
+  for (int64_t n = 0; n < N; ++n)
+    if (is_reg[n]) M.perm[nR++] = (int32_t)n;
+  {
+    int64_t i = nR;
+    for (int64_t n : order) M.perm[i++] = (int32_t)n;
   }
+  for (int64_t i = 0; i < N; ++i) M.iperm[M.perm[i]] = (int32_t)i;
   M.nR = nR;
   const int64_t nI = N - nR;
   M.nI = nI;
@@ -194,8 +241,14 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
         all = false;
       }
     }
-    M.r_meta2[ii] = far | (all ? (1u << 31) : 0u);
+    // uniform: every own and outer distance has the same level code
+    bool uniform = all;
+    const uint32_t c0 = M.r_meta[ii] & 15u;
+    for (int dir = 0; dir < 2 * D && uniform; ++dir)
+      uniform = ((M.r_meta[ii] >> (4 * dir)) & 15u) == c0 && ((far >> (4 * dir)) & 15u) == c0;
+    M.r_meta2[ii] = far | (all ? (1u << 31) : 0u) | (uniform ? (1u << 30) : 0u);
   }
+
   // irregular group
   M.i_meta.assign((size_t)nI, 0u);
   M.i_nbr.assign((size_t)NS * nI, 0);
@@ -203,6 +256,7 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
   M.i_d.assign((size_t)2 * D * nI, 0.0f);
   M.i_q.assign((size_t)2 * D * (D - 1) * nI, 0.0f);
   M.i_cidx.assign((size_t)nI, -1);
+  M.i_cls.assign((size_t)nI, 0u);
   M.i_wf64.assign((size_t)NS * nI, 0.0);
   M.i_d64.assign((size_t)2 * D * nI, 0.0);
   M.i_q64.assign((size_t)2 * D * (D - 1) * nI, 0.0);
@@ -213,6 +267,7 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     if (T.cidx[n] >= 0) meta |= 1u << 16;
     meta |= (uint32_t)T.wall[n] << 24;
     M.i_meta[ii] = meta;
+    M.i_cls[ii] = (uint32_t)node_cls[n];
     for (int dir = 0; dir < 2 * D; ++dir) {
       const int cnt = (int)((icount[n] >> (2 * dir)) & 3) + 1;
       const double nrm = T.nrm[(size_t)dir * N + n];
@@ -231,6 +286,25 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
       }
     }
     M.i_cidx[ii] = T.cidx[n];
+  }
+  // extended second-derivative set: regular face nodes of irregular nodes, and face nodes of regular
+  // nodes whose second neighbour is not recorded (irregular nodes are always in the set)
+  {
+    std::vector<uint8_t> inx((size_t)nR, 0);
+    for (int64_t ii = 0; ii < nI; ++ii)
+      for (int s_ = 0; s_ < NS; ++s_) {
+        const int32_t j = M.i_nbr[(size_t)s_ * nI + ii];
+        if (j < nR) inx[j] = 1;
+      }
+    for (int64_t ii = 0; ii < nR; ++ii)
+      for (int dir = 0; dir < 2 * D; ++dir)
+        if (M.r_nbr2[(size_t)dir * nR + ii] < 0) {
+          const int32_t j = M.r_nbr[(size_t)dir * nR + ii];
+          if (j < nR) inx[j] = 1;
+        }
+    M.x_list.clear();
+    for (int64_t j = 0; j < nR; ++j)
+      if (inx[j]) M.x_list.push_back((int32_t)j);
   }
   const size_t R = T.crec.size() / 6;
   M.corr.assign((size_t)D * D * R, 0.0f);
