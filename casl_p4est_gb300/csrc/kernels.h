@@ -35,6 +35,8 @@ struct DTab32 {
   int64_t N, nR, nI;
   int base;              // base level of the regular nodes' level codes
   float tsize[3];        // tree size per axis
+  float inv_tsize[3];
+  int64_t nU;            // regular nodes [0, nU) have uniform stencils
   const uint32_t* r_meta;
   const int32_t* r_nbr;  // 2D x nR
   const int32_t* r_nbr2; // 2D x nR, -1 when absent

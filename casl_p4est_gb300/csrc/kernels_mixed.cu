@@ -407,10 +407,11 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                             const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                            const float* __restrict__ dd_irr, float* out, const float* avg_with) {
+                                                            const float* __restrict__ dd_irr, float* out, const float* avg_with,
+                                                            int first, int last) {
   const int nR = (int)T.nR;
   const int stride = gridDim.x * blockDim.x;
-  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = first + blockIdx.x * blockDim.x + threadIdx.x;
   uint16_t p_st = 0;
   uint32_t p_codes = 0, p_far = 0;
   int32_t p_nb[2 * D], p_nb2[2 * D];
@@ -427,8 +428,8 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     p_f0 = __ldg(phin + m);
     if (AVG) p_avg = avg_with[m];
   };
-  if (n < nR) prefetch(n);
-  for (; n < nR; n += stride) {
+  if (n < last) prefetch(n);
+  for (; n < last; n += stride) {
     const uint16_t st = p_st;
     const uint32_t codes = p_codes, far = p_far;
     int32_t nb[2 * D], nb2[2 * D];
@@ -438,36 +439,12 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
       nb2[dir] = p_nb2[dir];
     }
     const float f0 = p_f0, avg = p_avg;
-    if (n + stride < nR) prefetch(n + stride);
+    if (n + stride < last) prefetch(n + stride);
     float r;
     if (st & ST_ANCHORED) {
       r = 0.0f;
     } else if (st & ST_OUTSIDE) {
       r = f0;
-    } else if (ORDER_SPACE > 1 && ((far >> 30) & 1u) && !(st & ST_NEAR)) {
-      // uniform stencil: equal spacing h_a along each axis for the node and its face nodes
-      const uint32_t code = codes & 15u;
-      const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
-      float hmin = 3.0e38f, hsum = 0.0f;
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        const float h = level_size(T.tsize[a], T.base, code);
-        const float ih = __frcp_rn(h);
-        const float ih2 = ih * ih;
-        const float fm = __ldg(phin + nb[2 * a]), fp = __ldg(phin + nb[2 * a + 1]);
-        const float fmm = __ldg(phin + nb2[2 * a]), fpp = __ldg(phin + nb2[2 * a + 1]);
-        const float xx0 = (fp + fm - 2.0f * f0) * ih2;
-        const float xm = (f0 + fmm - 2.0f * fm) * ih2;
-        const float xp = (fpp + f0 - 2.0f * fp) * ih2;
-        float gm = fmaf(0.5f * h, minmodf(xm, xx0), (f0 - fm) * ih);
-        float gp = fmaf(-0.5f * h, minmodf(xp, xx0), (fp - f0) * ih);
-        if (sgn * gp > 0.0f) gp = 0.0f;
-        if (sgn * gm < 0.0f) gm = 0.0f;
-        hsum += fmaxf(gp * gp, gm * gm);
-        hmin = fminf(hmin, h);
-      }
-      r = f0 - hmin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
-      if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
     } else {
       float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fn2[2 * D];
 #pragma unroll
@@ -507,6 +484,88 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
         }
       }
       r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+    }
+    if (AVG) r = 0.5f * (avg + r);
+    out[n] = r;
+  }
+}
+
+// Regular nodes with uniform stencils (second order in space): the node and its face nodes have the
+// same spacing h_a along each axis, so every second derivative is (f_+ + f_- - 2 f_0)/h_a^2 and all
+// reciprocals are exponent shifts. Persistent and software-pipelined like k_reinit_fused_reg32;
+// interface-adjacent nodes take their subcell distances from s_near.
+template <int D, bool AVG>
+__global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uint16_t* __restrict__ status,
+                                                          const float* __restrict__ s_near, const float* __restrict__ phin,
+                                                          float* out, const float* avg_with) {
+  const int nR = (int)T.nR, nU = (int)T.nU;
+  const int stride = gridDim.x * blockDim.x;
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  uint16_t p_st = 0;
+  uint32_t p_code = 0;
+  int32_t p_nb[2 * D], p_nb2[2 * D];
+  float p_f0 = 0.0f, p_avg = 0.0f;
+  auto prefetch = [&](int m) {
+    p_st = status[m];
+    p_code = __ldg(T.r_meta + m) & 15u;
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      p_nb[dir] = __ldg(T.r_nbr + dir * nR + m);
+      p_nb2[dir] = __ldg(T.r_nbr2 + dir * nR + m);
+    }
+    p_f0 = __ldg(phin + m);
+    if (AVG) p_avg = avg_with[m];
+  };
+  if (n < nU) prefetch(n);
+  for (; n < nU; n += stride) {
+    const uint16_t st = p_st;
+    const int lvl = T.base + (int)p_code;
+    int32_t nb[2 * D], nb2[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      nb[dir] = p_nb[dir];
+      nb2[dir] = p_nb2[dir];
+    }
+    const float f0 = p_f0, avg = p_avg;
+    if (n + stride < nU) prefetch(n + stride);
+    float r;
+    if (st & ST_ANCHORED) {
+      r = 0.0f;
+    } else if (st & ST_OUTSIDE) {
+      r = f0;
+    } else {
+      const bool near = (st & ST_NEAR) != 0;
+      const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
+      float smin = 3.0e38f, hsum = 0.0f;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const float h = __int_as_float(__float_as_int(T.tsize[a]) - (lvl << 23));
+        const float ih = __int_as_float(__float_as_int(T.inv_tsize[a]) + (lvl << 23));
+        const float ih2 = ih * ih;
+        float fm = __ldg(phin + nb[2 * a]), fp = __ldg(phin + nb[2 * a + 1]);
+        const float fmm = __ldg(phin + nb2[2 * a]), fpp = __ldg(phin + nb2[2 * a + 1]);
+        const float xx0 = (fp + fm - 2.0f * f0) * ih2;
+        const float mm = minmodf((f0 + fmm - 2.0f * fm) * ih2, xx0);
+        const float mp = minmodf((fpp + f0 - 2.0f * fp) * ih2, xx0);
+        float gm, gp;
+        if (!near) {
+          gm = fmaf(0.5f * h, mm, (f0 - fm) * ih);
+          gp = fmaf(-0.5f * h, mp, (fp - f0) * ih);
+          smin = fminf(smin, h);
+        } else {
+          const float sm = __ldg(s_near + (int64_t)(2 * a) * T.N + n), sp = __ldg(s_near + (int64_t)(2 * a + 1) * T.N + n);
+          if (st & (1u << (ST_CUT_SHIFT + 2 * a))) fm = 0.0f;
+          if (st & (1u << (ST_CUT_SHIFT + 2 * a + 1))) fp = 0.0f;
+          gm = fmaf(0.5f * sm, mm, __fdividef(f0 - fm, sm));
+          gp = fmaf(-0.5f * sp, mp, __fdividef(fp - f0, sp));
+          smin = fminf(smin, fminf(sm, sp));
+        }
+        if (sgn * gp > 0.0f) gp = 0.0f;
+        if (sgn * gm < 0.0f) gm = 0.0f;
+        hsum += fmaxf(gp * gp, gm * gm);
+      }
+      r = f0 - smin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
+      if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
     }
     if (AVG) r = 0.5f * (avg + r);
     out[n] = r;
@@ -849,36 +908,39 @@ void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t 
 }
 
 template <int D>
+static int persistent_blocks(const void* kernel) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
+  return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+template <int D, int OS, bool AVG>
+static void fused_launch(const DTab32<D>& T, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
+                         float* out, const float* avg_with, cudaStream_t s) {
+  static int gb_reg = 0, gb_uni = 0;
+  if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
+  if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG>);
+  const int64_t uni_end = (OS > 1) ? T.nU : 0;  // the uniform kernel is second order in space only
+  if (T.nI) k_reinit_fused32<D, OS, AVG><<<nblocks(T.nI), TPB, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
+  if (T.nR > uni_end)
+    k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb_reg, nblocks(T.nR - uni_end)), TPB, 0, s>>>(
+        T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
+  if (uni_end > 0)
+    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb_uni, nblocks(uni_end)), TPB, 0, s>>>(T, status, s_near, phin, out, avg_with);
+}
+
+template <int D>
 void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
                            const float* dd_irr, float* out, const float* avg_with, cudaStream_t s) {
   if (T.N == 0) return;
-  static int reg_blocks = 0;
-  if (reg_blocks == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reinit_fused_reg32<D, 2, true>, TPB, 0);
-    reg_blocks = sms * (per_sm > 0 ? per_sm : 1);
-  }
-  const unsigned gi = nblocks(T.nI);
-  const int64_t lo = T.nR, hi = T.N;
-  const unsigned gr = (unsigned)std::min<int64_t>(reg_blocks, nblocks(T.nR));
   if (order_space > 1) {
-    if (avg_with) {
-      if (T.nI) k_reinit_fused32<D, 2, true><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
-      if (T.nR) k_reinit_fused_reg32<D, 2, true><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    } else {
-      if (T.nI) k_reinit_fused32<D, 2, false><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
-      if (T.nR) k_reinit_fused_reg32<D, 2, false><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    }
+    if (avg_with) fused_launch<D, 2, true>(T, status, s_near, phin, dd_irr, out, avg_with, s);
+    else fused_launch<D, 2, false>(T, status, s_near, phin, dd_irr, out, avg_with, s);
   } else {
-    if (avg_with) {
-      if (T.nI) k_reinit_fused32<D, 1, true><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
-      if (T.nR) k_reinit_fused_reg32<D, 1, true><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    } else {
-      if (T.nI) k_reinit_fused32<D, 1, false><<<gi, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with, lo, hi);
-      if (T.nR) k_reinit_fused_reg32<D, 1, false><<<gr, TPB, 0, s>>>(T, status, s_near, phin, dd_irr, out, avg_with);
-    }
+    if (avg_with) fused_launch<D, 1, true>(T, status, s_near, phin, dd_irr, out, avg_with, s);
+    else fused_launch<D, 1, false>(T, status, s_near, phin, dd_irr, out, avg_with, s);
   }
 }
 

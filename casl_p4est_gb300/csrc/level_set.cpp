@@ -219,6 +219,8 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   T32.nI = M.nI;
   T32.base = M.base_level;
   for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)(F->brick.tmax[a] - F->brick.tmin[a]) : 1.0f;
+  for (int a = 0; a < 3; ++a) T32.inv_tsize[a] = 1.0f / T32.tsize[a];
+  T32.nU = M.nU;
   T32.r_meta = r_meta.p;
   T32.r_nbr = r_nbr.p;
   T32.r_nbr2 = r_nbr2.p;

@@ -54,6 +54,7 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T);
 template <int D>
 struct Tables32 {
   int64_t N = 0, nR = 0, nI = 0;
+  int64_t nU = 0;                   // regular nodes 0 .. nU-1 have uniform stencils (see r_meta2 bit 30)
   int base_level = 0;
   float level_size[3 * 16] = {0};   // [axis*16 + code] cell size tree_size * 2^-(base_level + code)
   std::vector<int32_t> perm;        // device index -> node

@@ -249,6 +249,37 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     M.r_meta2[ii] = far | (all ? (1u << 31) : 0u) | (uniform ? (1u << 30) : 0u);
   }
 
+  // uniform regular nodes first (node order kept within each part); indices are remapped
+  {
+    std::vector<int32_t> new_of_old((size_t)nR), old_of_new;
+    old_of_new.reserve((size_t)nR);
+    for (int64_t ii = 0; ii < nR; ++ii)
+      if ((M.r_meta2[ii] >> 30) & 1u) old_of_new.push_back((int32_t)ii);
+    M.nU = (int64_t)old_of_new.size();
+    for (int64_t ii = 0; ii < nR; ++ii)
+      if (!((M.r_meta2[ii] >> 30) & 1u)) old_of_new.push_back((int32_t)ii);
+    for (int64_t k = 0; k < nR; ++k) new_of_old[old_of_new[k]] = (int32_t)k;
+    auto remap = [&](int32_t j) -> int32_t { return (j >= 0 && j < nR) ? new_of_old[j] : j; };
+    std::vector<uint32_t> meta_n((size_t)nR), meta2_n((size_t)nR);
+    std::vector<int32_t> nbr_n((size_t)2 * D * nR), nbr2_n((size_t)2 * D * nR);
+    std::vector<int32_t> perm_n((size_t)nR);
+    for (int64_t k = 0; k < nR; ++k) {
+      const int64_t o = old_of_new[k];
+      meta_n[k] = M.r_meta[o];
+      meta2_n[k] = M.r_meta2[o];
+      perm_n[k] = M.perm[o];
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        nbr_n[(size_t)dir * nR + k] = remap(M.r_nbr[(size_t)dir * nR + o]);
+        nbr2_n[(size_t)dir * nR + k] = remap(M.r_nbr2[(size_t)dir * nR + o]);
+      }
+    }
+    M.r_meta.swap(meta_n);
+    M.r_meta2.swap(meta2_n);
+    M.r_nbr.swap(nbr_n);
+    M.r_nbr2.swap(nbr2_n);
+    for (int64_t k = 0; k < nR; ++k) M.perm[k] = perm_n[k];
+    for (int64_t i = 0; i < N; ++i) M.iperm[M.perm[i]] = (int32_t)i;
+  }
   // irregular group
   M.i_meta.assign((size_t)nI, 0u);
   M.i_nbr.assign((size_t)NS * nI, 0);
