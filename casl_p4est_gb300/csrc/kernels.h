@@ -91,9 +91,12 @@ void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* 
 // ddx (D x N, written by launch_dd_x32 for the same phi on the extended set)
 template <int D>
 void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s);
+// One RK stage of the mixed reinitialisation is split in three parts that write disjoint node ranges:
+// uniform regular nodes (no dependence on ddx), other regular nodes and irregular nodes (both read ddx).
+enum { STAGE_PART_UNIFORM = 0, STAGE_PART_REGULAR = 1, STAGE_PART_IRREGULAR = 2 };
 template <int D>
-void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
-                           const float* dd_irr, float* out, const float* avg_with, cudaStream_t s);
+void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, int uniform_blocks);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);

@@ -917,30 +917,33 @@ static int persistent_blocks(const void* kernel) {
 }
 
 template <int D, int OS, bool AVG>
-static void fused_launch(const DTab32<D>& T, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
-                         float* out, const float* avg_with, cudaStream_t s) {
+static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
+                         float* out, const float* avg_with, cudaStream_t s, int uniform_blocks) {
   static int gb_reg = 0, gb_uni = 0;
   if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
   if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG>);
   const int64_t uni_end = (OS > 1) ? T.nU : 0;  // the uniform kernel is second order in space only
-  if (T.nI) k_reinit_fused32<D, OS, AVG><<<nblocks(T.nI), TPB, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
-  if (T.nR > uni_end)
+  if (part == STAGE_PART_IRREGULAR && T.nI)
+    k_reinit_fused32<D, OS, AVG><<<nblocks(T.nI), TPB, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
+  if (part == STAGE_PART_REGULAR && T.nR > uni_end)
     k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb_reg, nblocks(T.nR - uni_end)), TPB, 0, s>>>(
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
-  if (uni_end > 0)
-    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb_uni, nblocks(uni_end)), TPB, 0, s>>>(T, status, s_near, phin, out, avg_with);
+  if (part == STAGE_PART_UNIFORM && uni_end > 0) {
+    const int gb = uniform_blocks > 0 ? std::min(uniform_blocks, gb_uni) : gb_uni;
+    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb, nblocks(uni_end)), TPB, 0, s>>>(T, status, s_near, phin, out, avg_with);
+  }
 }
 
 template <int D>
-void launch_reinit_fused32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
-                           const float* dd_irr, float* out, const float* avg_with, cudaStream_t s) {
+void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, int uniform_blocks) {
   if (T.N == 0) return;
   if (order_space > 1) {
-    if (avg_with) fused_launch<D, 2, true>(T, status, s_near, phin, dd_irr, out, avg_with, s);
-    else fused_launch<D, 2, false>(T, status, s_near, phin, dd_irr, out, avg_with, s);
+    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
+    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
   } else {
-    if (avg_with) fused_launch<D, 1, true>(T, status, s_near, phin, dd_irr, out, avg_with, s);
-    else fused_launch<D, 1, false>(T, status, s_near, phin, dd_irr, out, avg_with, s);
+    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
+    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
   }
 }
 
@@ -972,8 +975,8 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \
                                          const float*, cudaStream_t);                                                           \
   template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                       \
-  template void launch_reinit_fused32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
-                                         float*, const float*, cudaStream_t);
+  template void launch_reinit_part32<D>(const DTab32<D>&, int, int, const uint16_t*, const float*, const float*, const float*,  \
+                                        float*, const float*, cudaStream_t, int);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

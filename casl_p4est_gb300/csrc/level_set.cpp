@@ -3,6 +3,7 @@
 
 #include <float.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 
@@ -78,6 +79,7 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
   zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   own_stream = true;
+  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) uniform_blocks = atoi(ub);
   Tables64<D> T;
   build_tables64<D>(forest, T);
   num_corrections = (int64_t)(T.crec.size() / 6);
@@ -112,6 +114,13 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
 template <int D>
 LevelSet<D>::~LevelSet() {
   if (stream) cudaStreamSynchronize(stream);
+  if (side_stream) {
+    cudaStreamSynchronize(side_stream);
+    cudaStreamDestroy(side_stream);
+    cudaEventDestroy(ev_fork);
+    cudaEventDestroy(ev_ddx);
+    cudaEventDestroy(ev_join);
+  }
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -244,6 +253,32 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   mixed_ready = true;
 }
 
+// One RK stage of the mixed path on two streams: the side stream computes the extended second
+// derivatives and then the irregular nodes while the main stream runs the uniform regular nodes;
+// the remaining regular nodes follow once the extended second derivatives are ready.
+template <int D>
+void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with) {
+  if (!side_stream) {
+    cuda_check(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&ev_ddx, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  timer.begin(K_STAGE32, stream);
+  cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(side_stream, ev_fork, 0), "cudaStreamWaitEvent");
+  launch_dd_x32<D>(T32, phin, f_dd.p, side_stream);
+  cuda_check(cudaEventRecord(ev_ddx, side_stream), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, 0);
+  cuda_check(cudaEventRecord(ev_join, side_stream), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, uniform_blocks);
+  cuda_check(cudaStreamWaitEvent(stream, ev_ddx, 0), "cudaStreamWaitEvent");
+  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, 0);
+  cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
+  timer.end(stream);
+  timer.launches += 3;  // four kernels per stage
+}
+
 // Mixed precision: phi_n and all per-iteration work in FP32 (device node order); the phi_0-only
 // subcell step in FP64.
 template <int D>
@@ -261,11 +296,9 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   timer.launches += 3;  // the FP64 subcell step is four kernels
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
-    LSG_LAUNCH(K_DD32, launch_dd_x32<D>(T32, f_phi.p, f_dd.p, stream));
-    LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi.p, f_dd.p, f_phi1.p, nullptr, stream));
+    mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
     if (ot > 1) {
-      LSG_LAUNCH(K_DD32, launch_dd_x32<D>(T32, f_phi1.p, f_dd.p, stream));
-      LSG_LAUNCH(K_STAGE32, launch_reinit_fused32<D>(T32, os, status.p, f_snear.p, f_phi1.p, f_dd.p, f_phi.p, f_phi.p, stream));
+      mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
     } else {
       std::swap(f_phi.p, f_phi1.p);
     }

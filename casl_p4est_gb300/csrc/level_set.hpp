@@ -50,6 +50,9 @@ struct LevelSet {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   KernelTimer timer;
+  cudaStream_t side_stream = nullptr;  // second stream of the mixed stage (fork/join with events)
+  cudaEvent_t ev_fork = nullptr, ev_ddx = nullptr, ev_join = nullptr;
+  int uniform_blocks = 0;              // grid cap of the uniform kernel (0: full occupancy)
   int64_t num_corrections = 0;
 
   // FP64 tables
@@ -95,6 +98,7 @@ struct LevelSet {
   void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
+  void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
 };
 
 double largest_dbl_smaller_than_dbl_max();
