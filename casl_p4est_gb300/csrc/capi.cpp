@@ -431,6 +431,14 @@ int lsg_reinitialize_device(lsg_level_set* ls, double* phi_dev, int order_space,
   });
 }
 
+int lsg_reinitialize_device_noalloc(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime,
+                                    double limit_high, double limit_low, int iterations) {
+  return guard([&] {
+    need(phi_dev != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) { L.reinitialize_fp64_noalloc(phi_dev, order_space, order_pseudotime, limit_high, limit_low, iterations); });
+  });
+}
+
 int lsg_reinit_2nd(lsg_level_set* ls, double* phi, int iterations, double limit, int precision) {
   return lsg_reinitialize(ls, phi, 2, 2, limit, -limit, iterations, precision);
 }

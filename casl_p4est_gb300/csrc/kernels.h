@@ -74,6 +74,11 @@ void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double*
                            double* out, const double* avg_with, cudaStream_t s);
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
 void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
+// reinit_fp64's kernel sequence with its work vectors in a static device array (noalloc.cu);
+// throws std::invalid_argument when the grid does not fit the array. hi/lo: widened phi_0 limits.
+template <int D>
+void reinit_fp64_static(const DTab64<D>& T, double zdt, double* phi, int order_space, int order_pseudotime, double lim_hi,
+                        double lim_lo, int iterations, cudaStream_t s);
 
 // Mixed precision.
 template <int D>

@@ -157,6 +157,19 @@ void LevelSet<D>::reinitialize(double* phi, int os, int ot, double limit_high, d
     throw std::invalid_argument("reinitialize: unknown precision mode");
 }
 
+template <int D>
+void LevelSet<D>::reinitialize_fp64_noalloc(double* phi, int os, int ot, double limit_high, double limit_low, int iterations) {
+  if (os < 1 || os > 2 || ot < 1 || ot > 2)
+    throw std::invalid_argument(
+        "reinitialize_within_range_of_phi_0: valid orders of orders of accuracy for space and pseudotime are 1 and 2 only!");
+  if (!(limit_high > limit_low)) throw std::invalid_argument("reinitialize: limit_high must exceed limit_low");
+  if (iterations < 0) throw std::invalid_argument("reinitialize: negative number of iterations");
+  const double big = largest_dbl_smaller_than_dbl_max();
+  const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
+  const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
+  reinit_fp64_static<D>(T64, zdt, phi, os, ot, hi, lo, iterations, stream);
+}
+
 // reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557) on one device:
 // the ghost updates of a single process are no-ops and the layer/local split merges into one launch.
 template <int D>

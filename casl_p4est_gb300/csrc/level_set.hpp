@@ -89,6 +89,10 @@ struct LevelSet {
   // dt of the CF overload: min over nodes of 0.8*|s_min/vn| (src/my_p4est_level_set.cpp:752-776).
   double cfl_dt(const double* vn);
 
+  // reinitialize() in FP64 with no allocation: the work vectors come from a static device array
+  // (reinit_fp64_static) that holds grids up to LSG_NOALLOC_SCRATCH_BYTES of scratch.
+  void reinitialize_fp64_noalloc(double* phi, int os, int ot, double limit_high, double limit_low, int iterations);
+
   // host-buffer conveniences (copies inside)
   void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision);
 

@@ -110,6 +110,19 @@ int lsg_reinitialize(lsg_level_set* ls, double* phi, int order_space, int order_
                      double limit_low, int iterations, int precision);
 int lsg_reinitialize_device(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime, double limit_high,
                             double limit_low, int iterations, int precision);
+/* No counterpart in the reference. lsg_reinitialize_device with precision LSG_FP64, allocating no
+ * memory: the work vectors (114 bytes per node in 3D, 82 in 2D, each array padded to 256 bytes)
+ * come from one static device array of LSG_NOALLOC_SCRATCH_BYTES per device; larger grids return
+ * LSG_EINVAL. It serves callers that cannot allocate inside the call: a solver whose device memory
+ * is handed out by another pool (cudaMalloc there fails or fragments it), a time loop that cannot
+ * take the device-wide synchronisation of cudaFree, and programs with many level-set objects on
+ * small grids, which would otherwise each keep their own work vectors.
+ * The first call on a device (with that device current) takes the array's address with
+ * cudaGetSymbolAddress; make it before any stream capture. Nothing in the array must start at
+ * zero. Calls that overlap on one device race on the array: serialise them. */
+#define LSG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int lsg_reinitialize_device_noalloc(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime,
+                                    double limit_high, double limit_low, int iterations);
 /* reinitialize_2nd_order(phi, iterations, limit) (src/my_p4est_level_set.h:468-472) */
 int lsg_reinit_2nd(lsg_level_set* ls, double* phi, int iterations, double limit, int precision);
 
