@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "liblsgpu.so")
 
 LSG_OK, LSG_EINVAL, LSG_ENOMEM, LSG_EDEVICE, LSG_ETIMEOUT, LSG_ENAN, LSG_ESTATE = range(7)
 LSG_FP64, LSG_MIXED = 0, 1
+LSG_VELOCITY_VORTEX = 0
 
 _P = C.c_void_p
 _I = C.c_int
@@ -63,11 +64,18 @@ SIGNATURES = {
     "lsg_second_derivatives_device": (_I, [_P, _P, _P]),
     "lsg_perturb_level_set_function": (_I, [_P, _DP, _D]),
     "lsg_level_set_enable_kernel_timing": (_I, [_P, _I]),
+    "lsg_interpolate_nodes": (_I, [_P, _DP, _I64, _DP, _I, _DP, _I, _DP]),
+    "lsg_interpolate_nodes_device": (_I, [_P, _P, _I64, _P, _I, _P, _I, _P]),
+    "lsg_locate_points_device": (_I, [_P, _P, _I64, _P]),
+    "lsg_semi_lagrangian_advect": (_I, [_P, _DP, _I64, _D, _DP, _DP, _DP, _DP, _I, _I, _DP]),
+    "lsg_semi_lagrangian_advect_device": (_I, [_P, _P, _I64, _D, _P, _P, _P, _P, _I, _I, _P]),
+    "lsg_semi_lagrangian_advect_cf": (_I, [_P, _DP, _I64, _D, _I, _DP, _I, _DP, _DP, _I, _DP]),
+    "lsg_semi_lagrangian_advect_cf_device": (_I, [_P, _P, _I64, _D, _I, _DP, _I, _P, _P, _I, _P]),
     "lsg_level_set_kernel_times": (_I, [_P, _DP, C.POINTER(_I64), _I, _I]),
     "lsg_level_set_launch_count": (_I64, [_P]),
 }
 
-KERNEL_KINDS = ["dd64", "prep64", "stage64", "advect64", "dd32", "prep_mixed", "stage32", "advect32", "convert", "copy"]
+KERNEL_KINDS = ["dd64", "prep64", "stage64", "advect64", "dd32", "prep_mixed", "stage32", "advect32", "convert", "copy", "interp"]
 
 
 class LsgError(RuntimeError):

@@ -520,6 +520,70 @@ int lsg_perturb_level_set_function(lsg_level_set* ls, double* phi, double epsilo
   });
 }
 
+int lsg_interpolate_nodes(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
+                          int method, double* out) {
+  return guard([&] {
+    need(F != nullptr && out != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    with_ls(ls, [&](auto& L) { L.interpolate_host(xyz, npts, nfields, F, Fdd, method, out); });
+  });
+}
+
+int lsg_interpolate_nodes_device(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
+                                 int method, double* out) {
+  return guard([&] {
+    need(F != nullptr && out != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    with_ls(ls, [&](auto& L) { L.interpolate(xyz, npts, nfields, F, Fdd, method, out); });
+  });
+}
+
+int lsg_locate_points_device(lsg_level_set* ls, const double* xyz, int64_t npts, int32_t* leaf) {
+  return guard([&] {
+    need(leaf != nullptr && (xyz != nullptr || npts == 0) && npts >= 0, "null argument");
+    with_ls(ls, [&](auto& L) { L.locate(xyz, npts, leaf); });
+  });
+}
+
+int lsg_semi_lagrangian_advect(lsg_level_set* ls, const double* xyz, int64_t npts, double dt, const double* v, const double* vdd,
+                               const double* phi, const double* phi_dd, int velo_method, int phi_method, double* phi_np1) {
+  return guard([&] {
+    need(v != nullptr && phi != nullptr && phi_np1 != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    with_ls(ls, [&](auto& L) { L.sl_advect_host(xyz, npts, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1); });
+  });
+}
+
+int lsg_semi_lagrangian_advect_device(lsg_level_set* ls, const double* xyz, int64_t npts, double dt, const double* v,
+                                      const double* vdd, const double* phi, const double* phi_dd, int velo_method, int phi_method,
+                                      double* phi_np1) {
+  return guard([&] {
+    need(v != nullptr && phi != nullptr && phi_np1 != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    with_ls(ls, [&](auto& L) { L.sl_advect(xyz, npts, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1); });
+  });
+}
+
+static double velocity_scale(int velocity, const double* params, int nparams) {
+  need(velocity == LSG_VELOCITY_VORTEX, "unknown analytic velocity");
+  return (params != nullptr && nparams > 0) ? params[0] : 1.0;
+}
+
+int lsg_semi_lagrangian_advect_cf(lsg_level_set* ls, const double* xyz, int64_t npts, double dt, int velocity, const double* params,
+                                  int nparams, const double* phi, const double* phi_dd, int phi_method, double* phi_np1) {
+  return guard([&] {
+    need(phi != nullptr && phi_np1 != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    const double s = velocity_scale(velocity, params, nparams);
+    with_ls(ls, [&](auto& L) { L.sl_advect_vortex_host(xyz, npts, dt, s, phi, phi_dd, phi_method, phi_np1); });
+  });
+}
+
+int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz, int64_t npts, double dt, int velocity,
+                                         const double* params, int nparams, const double* phi, const double* phi_dd, int phi_method,
+                                         double* phi_np1) {
+  return guard([&] {
+    need(phi != nullptr && phi_np1 != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    const double s = velocity_scale(velocity, params, nparams);
+    with_ls(ls, [&](auto& L) { L.sl_advect_vortex(xyz, npts, dt, s, phi, phi_dd, phi_method, phi_np1); });
+  });
+}
+
 int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on) {
   return guard([&] { with_ls(ls, [&](auto& L) { L.timer.enabled = on != 0; }); });
 }

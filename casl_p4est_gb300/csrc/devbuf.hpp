@@ -36,6 +36,10 @@ struct DevBuf {
     cuda_check(cudaMalloc((void**)&p, count * sizeof(T)), "cudaMalloc");
     n = count;
   }
+  // grow-only allocation for work buffers whose size varies between calls
+  void ensure(size_t count) {
+    if (count > n) alloc(count);
+  }
   void upload(const std::vector<T>& v, cudaStream_t s) {
     alloc(v.size());
     if (!v.empty()) cuda_check(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");

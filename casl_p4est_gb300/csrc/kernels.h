@@ -29,6 +29,27 @@ struct DTab64 {
   const uint8_t* wall;  // N
 };
 
+// Point location and corner gathers for node interpolation (my_p4est_hierarchy_t +
+// p4est_nodes_t::local_nodes). Leaves in tree-major Morton order; ctab[t*ncoarse + c] is the
+// leaf containing the first logical point of coarse cell c (level L0) of tree t, so the leaf that
+// contains a point lies in [ctab[i], ctab[i+1]] and is found by a short binary search on the keys.
+template <int D>
+struct DLoc {
+  int64_t nleaves;
+  int64_t N;                  // nodes (stride of the field arrays)
+  const uint64_t* key;        // (tree << D*MAXLEVEL) | morton(leaf corner)
+  const int8_t* level;
+  const int32_t* local_nodes; // CHILDREN per leaf
+  const int32_t* ctab;        // ntrees * ncoarse + 1
+  int L0;
+  int64_t ncoarse;
+  int n[3];                   // brick size in trees
+  const int32_t* ijk_to_tree;
+  const double* tmin;         // 3 per tree: tree vertex 0
+  const double* tmax;         // 3 per tree: last tree vertex
+  double xyz_min[3], xyz_max[3], tree_dim[3];
+};
+
 // Mixed-precision tables in device node order (layout described in tables32.cpp).
 template <int D>
 struct DTab32 {
@@ -74,6 +95,21 @@ void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double*
                            double* out, const double* avg_with, cudaStream_t s);
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
 void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
+// Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p
+// is first moved to xyz[p] - coef*shift[:, p] and clipped into the domain (the semi-Lagrangian
+// backtrace). F: nf x N values, Fdd: nf x D x N second derivatives (ignored for linear), out: nf x np.
+template <int D>
+void launch_interp64(const DLoc<D>& L, int method, const double* xyz, int64_t np, const double* shift, double coef, int nf,
+                     const double* F, const double* Fdd, double* out, cudaStream_t s);
+// Semi-Lagrangian step with the analytic single-vortex velocity scaled by vscale: RK2 backtrace from
+// xyz, then interpolation of phi at the departure point.
+template <int D>
+void launch_sl_vortex64(const DLoc<D>& L, int method, const double* xyz, int64_t np, double dt, double vscale, const double* phi,
+                        const double* phi_dd, double* out, cudaStream_t s);
+// Leaf chosen by the point location for each point (clipped first).
+template <int D>
+void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* leaf, cudaStream_t s);
+
 // reinit_fp64's kernel sequence with its work vectors in a static device array (noalloc.cu);
 // throws std::invalid_argument when the grid does not fit the array. hi/lo: widened phi_0 limits.
 template <int D>

@@ -391,6 +391,179 @@ void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, doub
   cuda_check(cudaStreamSynchronize(stream), "reinitialize sync");
 }
 
+// Point location tables: sorted leaf keys and levels, local_nodes, and the coarse-cell table
+// (my_p4est_hierarchy_t's role, src/my_p4est_hierarchy.cpp:264-567).
+template <int D>
+void LevelSet<D>::build_locator() {
+  if (loc_ready) return;
+  using DD = Dim<D>;
+  const Forest<D>& f = *F;
+  const int64_t nl = (int64_t)f.leaves.size();
+  const int nt = f.brick.num_trees;
+  int L0 = 0;
+  while (L0 < DD::MAXLEVEL && ((int64_t)nt << (D * (L0 + 1))) <= 2 * nl) ++L0;
+  const int64_t ncoarse = int64_t(1) << (D * L0);
+  std::vector<int32_t> ctab((size_t)(nt * ncoarse + 1));
+  // merge the coarse cells' first points (in key order) with the sorted leaf keys
+  int64_t j = 0;
+  for (int64_t i = 0; i < nt * ncoarse; ++i) {
+    const uint64_t t = (uint64_t)(i / ncoarse), c = (uint64_t)(i % ncoarse);
+    const uint64_t key = (t << tree_shift<D>()) | (c << (D * (DD::MAXLEVEL - L0)));
+    while (j + 1 < nl && f.leaf_key[(size_t)(j + 1)] <= key) ++j;
+    ctab[(size_t)i] = (int32_t)j;
+  }
+  ctab[(size_t)(nt * ncoarse)] = (int32_t)(nl - 1);
+  std::vector<int8_t> lvl((size_t)nl);
+  for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
+  loc_key.upload(f.leaf_key, stream);
+  loc_level.upload(lvl, stream);
+  loc_nodes.upload(f.local_nodes, stream);
+  loc_ctab.upload(ctab, stream);
+  loc_ijk.upload(f.brick.ijk_to_tree, stream);
+  loc_tmin.upload(f.brick.tmin, stream);
+  loc_tmax.upload(f.brick.tmax, stream);
+  cuda_check(cudaStreamSynchronize(stream), "locator upload");
+  TL.nleaves = nl;
+  TL.N = N;
+  TL.key = loc_key.p;
+  TL.level = loc_level.p;
+  TL.local_nodes = loc_nodes.p;
+  TL.ctab = loc_ctab.p;
+  TL.L0 = L0;
+  TL.ncoarse = ncoarse;
+  TL.ijk_to_tree = loc_ijk.p;
+  TL.tmin = loc_tmin.p;
+  TL.tmax = loc_tmax.p;
+  for (int a = 0; a < 3; ++a) {
+    TL.n[a] = f.brick.n[a];
+    TL.xyz_min[a] = f.brick.xyz_min[a];
+    TL.xyz_max[a] = f.brick.xyz_max[a];
+    TL.tree_dim[a] = (f.brick.xyz_max[a] - f.brick.xyz_min[a]) / f.brick.n[a];
+  }
+  loc_ready = true;
+}
+
+// Second derivatives of nf fields (nf x D x N): the caller's, or computed as compute_derivatives does.
+template <int D>
+const double* LevelSet<D>::derivatives_of(int nf, const double* Fv, const double* Fdd, DevBuf<double>& store) {
+  if (Fdd) return Fdd;
+  store.ensure((size_t)nf * D * N);
+  for (int k = 0; k < nf; ++k) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, Fv + (size_t)k * N, store.p + (size_t)k * D * N, stream));
+  return store.p;
+}
+
+static void check_method(int m) {
+  if (m < 0 || m > 4) throw std::invalid_argument("unknown interpolation_method");
+}
+
+template <int D>
+void LevelSet<D>::interpolate(const double* xyz, int64_t np, int nf, const double* Fv, const double* Fdd, int method, double* out) {
+  check_method(method);
+  if (nf < 1) throw std::invalid_argument("interpolate: at least one input field is needed");
+  if (np < 0) throw std::invalid_argument("interpolate: negative number of points");
+  build_locator();
+  const double* dd = method == 0 ? nullptr : derivatives_of(nf, Fv, Fdd, ws_fdd);
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, method, xyz, np, nullptr, 0.0, nf, Fv, dd, out, stream));
+  cuda_check(cudaGetLastError(), "interpolate");
+}
+
+template <int D>
+void LevelSet<D>::locate(const double* xyz, int64_t np, int32_t* leaf) {
+  build_locator();
+  LSG_LAUNCH(K_INTERP, launch_locate64<D>(TL, xyz, np, leaf, stream));
+  cuda_check(cudaGetLastError(), "locate");
+}
+
+// advect_from_n_to_np1 (src/my_p4est_semi_lagrangian.cpp:148-223): three interpolation rounds, the
+// second and third at x - dt/2 v and x - dt v* (clipped), each one launch.
+template <int D>
+void LevelSet<D>::sl_advect(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi,
+                            const double* phi_dd, int velo_method, int phi_method, double* phi_np1) {
+  check_method(velo_method);
+  check_method(phi_method);
+  if (np < 0) throw std::invalid_argument("advect_from_n_to_np1: negative number of points");
+  build_locator();
+  const double* vd = velo_method == 0 ? nullptr : derivatives_of(D, v, vdd, ws_fdd);
+  const double* pd = phi_method == 0 ? nullptr : derivatives_of(1, phi, phi_dd, ws_fdd2);
+  ws_v1.ensure((size_t)D * np);
+  ws_v2.ensure((size_t)D * np);
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, velo_method, xyz, np, nullptr, 0.0, D, v, vd, ws_v1.p, stream));
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, velo_method, xyz, np, ws_v1.p, 0.5 * dt, D, v, vd, ws_v2.p, stream));
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, phi_method, xyz, np, ws_v2.p, dt, 1, phi, pd, phi_np1, stream));
+  cuda_check(cudaGetLastError(), "advect_from_n_to_np1");
+}
+
+template <int D>
+void LevelSet<D>::sl_advect_vortex(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd,
+                                   int phi_method, double* phi_np1) {
+  check_method(phi_method);
+  if (np < 0) throw std::invalid_argument("advect_from_n_to_np1: negative number of points");
+  build_locator();
+  const double* pd = phi_method == 0 ? nullptr : derivatives_of(1, phi, phi_dd, ws_fdd2);
+  LSG_LAUNCH(K_INTERP, launch_sl_vortex64<D>(TL, phi_method, xyz, np, dt, vscale, phi, pd, phi_np1, stream));
+  cuda_check(cudaGetLastError(), "advect_from_n_to_np1 (single vortex)");
+}
+
+static void h2d(double* dst, const double* src, size_t n, cudaStream_t s) {
+  if (n) cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+}
+
+template <int D>
+void LevelSet<D>::interpolate_host(const double* xyz, int64_t np, int nf, const double* Fv, const double* Fdd, int method, double* out) {
+  ws_xyz.ensure((size_t)D * np + 1);
+  ws_f.ensure((size_t)nf * N);
+  ws_out.ensure((size_t)nf * np + 1);
+  h2d(ws_xyz.p, xyz, (size_t)D * np, stream);
+  h2d(ws_f.p, Fv, (size_t)nf * N, stream);
+  const double* dd = nullptr;
+  if (Fdd && method != 0) {
+    ws_fdd.ensure((size_t)nf * D * N);
+    h2d(ws_fdd.p, Fdd, (size_t)nf * D * N, stream);
+    dd = ws_fdd.p;
+  }
+  interpolate(ws_xyz.p, np, nf, ws_f.p, dd, method, ws_out.p);
+  if (np) cuda_check(cudaMemcpyAsync(out, ws_out.p, (size_t)nf * np * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+  cuda_check(cudaStreamSynchronize(stream), "interpolate sync");
+}
+
+template <int D>
+void LevelSet<D>::sl_advect_host(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi,
+                                 const double* phi_dd, int velo_method, int phi_method, double* phi_np1) {
+  // staging: xyz | v | phi | vdd | phi_dd in ws_f, the result in ws_out
+  const size_t nx = (size_t)D * np, nv = (size_t)D * N, nvd = vdd ? (size_t)D * D * N : 0, npd = phi_dd ? (size_t)D * N : 0;
+  ws_xyz.ensure(nx + 1);
+  ws_f.ensure(nv + N + nvd + npd);
+  ws_out.ensure((size_t)np + 1);
+  double* dv = ws_f.p;
+  double* dphi = dv + nv;
+  double* dvdd = vdd ? dphi + N : nullptr;
+  double* dpdd = phi_dd ? dphi + N + nvd : nullptr;
+  h2d(ws_xyz.p, xyz, nx, stream);
+  h2d(dv, v, nv, stream);
+  h2d(dphi, phi, N, stream);
+  if (vdd) h2d(dvdd, vdd, nvd, stream);
+  if (phi_dd) h2d(dpdd, phi_dd, npd, stream);
+  sl_advect(ws_xyz.p, np, dt, dv, dvdd, dphi, dpdd, velo_method, phi_method, ws_out.p);
+  if (np) cuda_check(cudaMemcpyAsync(phi_np1, ws_out.p, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+  cuda_check(cudaStreamSynchronize(stream), "advect_from_n_to_np1 sync");
+}
+
+template <int D>
+void LevelSet<D>::sl_advect_vortex_host(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd,
+                                        int phi_method, double* phi_np1) {
+  const size_t nx = (size_t)D * np, npd = phi_dd ? (size_t)D * N : 0;
+  ws_xyz.ensure(nx + 1);
+  ws_f.ensure(N + npd);
+  ws_out.ensure((size_t)np + 1);
+  h2d(ws_xyz.p, xyz, nx, stream);
+  h2d(ws_f.p, phi, N, stream);
+  double* dpdd = phi_dd ? ws_f.p + N : nullptr;
+  if (phi_dd) h2d(dpdd, phi_dd, npd, stream);
+  sl_advect_vortex(ws_xyz.p, np, dt, vscale, ws_f.p, dpdd, phi_method, ws_out.p);
+  if (np) cuda_check(cudaMemcpyAsync(phi_np1, ws_out.p, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+  cuda_check(cudaStreamSynchronize(stream), "advect_from_n_to_np1 sync");
+}
+
 template struct LevelSet<2>;
 template struct LevelSet<3>;
 

@@ -22,7 +22,7 @@ enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 // Kernel classes for the optional per-launch timing (CUDA events around each launch).
 enum KernelKind {
-  K_DD64 = 0, K_PREP64, K_STAGE64, K_ADVECT64, K_DD32, K_PREP_MIXED, K_STAGE32, K_ADVECT32, K_CONVERT, K_COPY, K_NUM_KINDS
+  K_DD64 = 0, K_PREP64, K_STAGE64, K_ADVECT64, K_DD32, K_PREP_MIXED, K_STAGE32, K_ADVECT32, K_CONVERT, K_COPY, K_INTERP, K_NUM_KINDS
 };
 
 struct KernelTimer {
@@ -69,8 +69,16 @@ struct LevelSet {
   DevBuf<double> i_wf64, i_d64, i_q64, corr64;
   DTab32<D> T32{};
   int64_t nR = 0, nI = 0;
+  // point location tables for node interpolation (built on first use)
+  bool loc_ready = false;
+  DevBuf<uint64_t> loc_key;
+  DevBuf<int8_t> loc_level;
+  DevBuf<int32_t> loc_nodes, loc_ctab, loc_ijk, loc_leaf;
+  DevBuf<double> loc_tmin, loc_tmax;
+  DLoc<D> TL{};
   // work vectors
   DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
+  DevBuf<double> ws_xyz, ws_f, ws_fdd, ws_out, ws_v1, ws_v2, ws_fdd2;
   DevBuf<uint16_t> status;
   DevBuf<float> f_phi0, f_phi, f_phi1, f_dd, f_ddm, f_snear, f_vn;
 
@@ -93,8 +101,28 @@ struct LevelSet {
   // (reinit_fp64_static) that holds grids up to LSG_NOALLOC_SCRATCH_BYTES of scratch.
   void reinitialize_fp64_noalloc(double* phi, int os, int ot, double limit_high, double limit_low, int iterations);
 
+  // my_p4est_interpolation_nodes_t: nf fields (nf x N) interpolated at np points (D doubles each)
+  // with `method` (interpolation_method); Fdd (nf x D x N) may be null and is then computed with
+  // compute_derivatives. out: nf x np. Device pointers.
+  void interpolate(const double* xyz, int64_t np, int nf, const double* F, const double* Fdd, int method, double* out);
+  // leaf index chosen for each point by the point location (clipped into the domain first)
+  void locate(const double* xyz, int64_t np, int32_t* leaf);
+  // my_p4est_semi_lagrangian_t::advect_from_n_to_np1(dt, v, vxx, phi_n, phi_xx_n, phi_np1): this
+  // object's grid is time n; xyz are the np nodes of the grid at n+1. v: D x N, vdd: D x D x N
+  // (component, axis, node) or null; phi_dd: D x N or null. Device pointers.
+  void sl_advect(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi, const double* phi_dd,
+                 int velo_method, int phi_method, double* phi_np1);
+  // the CF overload with the single-vortex velocity scaled by vscale
+  void sl_advect_vortex(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd, int phi_method,
+                        double* phi_np1);
+
   // host-buffer conveniences (copies inside)
   void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision);
+  void interpolate_host(const double* xyz, int64_t np, int nf, const double* F, const double* Fdd, int method, double* out);
+  void sl_advect_host(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi,
+                      const double* phi_dd, int velo_method, int phi_method, double* phi_np1);
+  void sl_advect_vortex_host(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd,
+                             int phi_method, double* phi_np1);
 
  private:
   void build_mixed();
@@ -103,6 +131,8 @@ struct LevelSet {
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
+  void build_locator();
+  const double* derivatives_of(int nf, const double* F, const double* Fdd, DevBuf<double>& store);
 };
 
 double largest_dbl_smaller_than_dbl_max();

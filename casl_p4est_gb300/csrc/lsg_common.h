@@ -71,11 +71,41 @@ LSG_HD uint64_t spread3(uint64_t v) {
   v = (v | (v << 2)) & 0x1249249249249249ull;
   return v;
 }
+// Inverse of spread2 / spread3: gather every D-th bit.
+LSG_HD uint32_t compact2(uint64_t v) {
+  v &= 0x5555555555555555ull;
+  v = (v | (v >> 1)) & 0x3333333333333333ull;
+  v = (v | (v >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+  v = (v | (v >> 4)) & 0x00FF00FF00FF00FFull;
+  v = (v | (v >> 8)) & 0x0000FFFF0000FFFFull;
+  v = (v | (v >> 16)) & 0x00000000FFFFFFFFull;
+  return (uint32_t)v;
+}
+LSG_HD uint32_t compact3(uint64_t v) {
+  v &= 0x1249249249249249ull;
+  v = (v | (v >> 2)) & 0x10C30C30C30C30C3ull;
+  v = (v | (v >> 4)) & 0x100F00F00F00F00Full;
+  v = (v | (v >> 8)) & 0x1F0000FF0000FFull;
+  v = (v | (v >> 16)) & 0x1F00000000FFFFull;
+  v = (v | (v >> 32)) & 0x1FFFFFull;
+  return (uint32_t)v;
+}
 // Morton index of logical coordinates (x fastest), p4est linear order within one tree.
 template <int D>
 LSG_HD uint64_t morton(const int32_t* xyz) {
   if (D == 2) return spread2((uint64_t)xyz[0]) | (spread2((uint64_t)xyz[1]) << 1);
   return spread3((uint64_t)xyz[0]) | (spread3((uint64_t)xyz[1]) << 1) | (spread3((uint64_t)xyz[2]) << 2);
+}
+template <int D>
+LSG_HD void unmorton(uint64_t m, int32_t* xyz) {
+  if (D == 2) {
+    xyz[0] = (int32_t)compact2(m);
+    xyz[1] = (int32_t)compact2(m >> 1);
+  } else {
+    xyz[0] = (int32_t)compact3(m);
+    xyz[1] = (int32_t)compact3(m >> 1);
+    xyz[2] = (int32_t)compact3(m >> 2);
+  }
 }
 // Tree index goes above the Morton bits: (tree, morton) lexicographic order as p4est sorts
 // quadrants and nodes (src/my_p4est_nodes.c:606-627).

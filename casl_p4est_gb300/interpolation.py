@@ -1,0 +1,154 @@
+"""Node interpolation and the semi-Lagrangian step on the GPU (FP64).
+
+Mirrors my_p4est_interpolation_nodes_t (src/my_p4est_interpolation_nodes.h:33-103, set_input /
+add_point / interpolate) and my_p4est_semi_lagrangian_t::advect_from_n_to_np1
+(src/my_p4est_semi_lagrangian.cpp:108-223). Arrays are numpy float64 in node order (host, copied
+inside each call) or CUDA tensors (device-resident).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .level_set import _is_device, my_p4est_level_set_t
+
+# interpolation_method, src/my_p4est_utils.h:332-338
+linear = 0
+quadratic = 1
+quadratic_non_oscillatory = 2
+quadratic_non_oscillatory_continuous_v1 = 3
+quadratic_non_oscillatory_continuous_v2 = 4
+METHODS = (linear, quadratic, quadratic_non_oscillatory, quadratic_non_oscillatory_continuous_v1,
+           quadratic_non_oscillatory_continuous_v2)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_device(a):
+        return C.c_void_p(a.data_ptr())
+    return L.dptr(a)
+
+
+def _f64(a, name, size=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if size is not None and a.size != size:
+        raise ValueError(f"{name} has {a.size} entries, expected {size}")
+    return a
+
+
+class my_p4est_interpolation_nodes_t:
+    """Interpolation of node fields of one grid at arbitrary points.
+
+    ``ls`` is the grid's my_p4est_level_set_t (it owns the device image of the node neighbours)."""
+
+    def __init__(self, ls: my_p4est_level_set_t):
+        self.ls = ls
+        self.dim = ls.ngbd.dim
+        self.clear()
+        self._F = None
+
+    def clear(self):
+        self._idx = []
+        self._pts = []
+
+    def add_point(self, node_idx_on_output, xyz):
+        self._idx.append(int(node_idx_on_output))
+        self._pts.append(np.asarray(xyz, np.float64).reshape(self.dim))
+
+    def add_points(self, xyz):
+        """Vectorised add_point for points 0..np-1 (xyz: (np, dim))."""
+        xyz = np.asarray(xyz, np.float64).reshape(-1, self.dim)
+        base = len(self._idx)
+        self._idx.extend(range(base, base + len(xyz)))
+        self._pts.extend(xyz)
+
+    def set_input(self, F, method, Fxxyyzz=None):
+        """F: (N,) or (nf, N); Fxxyyzz: (dim, N) or (nf, dim, N) second derivatives, or None to compute them."""
+        if method not in METHODS:
+            raise ValueError("unknown interpolation_method")
+        self._F, self._Fdd, self.method = F, Fxxyyzz, method
+
+    def interpolate(self, out=None):
+        if self._F is None:
+            raise RuntimeError("set_input was not called")
+        pts = np.ascontiguousarray(np.array(self._pts, np.float64).reshape(-1, self.dim))
+        vals = self.interpolate_points(pts, self._F, self.method, self._Fdd)
+        if out is None:
+            out = np.empty(vals.shape[:-1] + (max(self._idx) + 1 if self._idx else 0,), np.float64)
+        out[..., np.asarray(self._idx, np.int64)] = vals
+        return out
+
+    def interpolate_points(self, xyz, F, method, Fdd=None):
+        """Direct form: F (N,) or (nf, N) host arrays at points (np, dim); returns (np,) or (nf, np)."""
+        N = self.ls.num_nodes
+        F = _f64(F, "F")
+        single = F.ndim == 1
+        F2 = F.reshape(-1, N)
+        nf = F2.shape[0]
+        pts = _f64(xyz, "xyz").reshape(-1, self.dim)
+        dd = None if (Fdd is None or method == linear) else _f64(Fdd, "Fdd", nf * self.dim * N)
+        out = np.empty((nf, len(pts)), np.float64)
+        L.check(L.load().lsg_interpolate_nodes(self.ls.handle, L.dptr(pts), len(pts), L.dptr(F2), nf, _ptr(dd), int(method),
+                                               L.dptr(out)))
+        return out[0] if single else out
+
+    def interpolate_device(self, xyz, F, nf, method, out, Fdd=None):
+        """Device form: CUDA tensors xyz (np*dim), F (nf*N), out (nf*np), Fdd (nf*dim*N) or None."""
+        npts = xyz.numel() // self.dim
+        L.check(L.load().lsg_interpolate_nodes_device(self.ls.handle, _ptr(xyz), npts, _ptr(F), int(nf), _ptr(Fdd), int(method),
+                                                      _ptr(out)))
+
+
+class VortexVelocity:
+    """Single-vortex velocity of examples/level_set_advection/main_2d.cpp:116-181, scaled by
+    `scale` (the example's direction sign, or cos(pi t/T))."""
+
+    def __init__(self, scale=1.0):
+        self.scale = float(scale)
+
+
+class my_p4est_semi_lagrangian_t:
+    """advect_from_n_to_np1 from the grid at time n (ls_n) onto the nodes of the grid at n+1."""
+
+    def __init__(self, forest_np1, ls_n: my_p4est_level_set_t):
+        self.forest_np1 = forest_np1
+        self.ls_n = ls_n
+        self.dim = ls_n.ngbd.dim
+        self.velo_interpolation = quadratic_non_oscillatory_continuous_v2
+        self.phi_interpolation = quadratic_non_oscillatory_continuous_v2
+
+    def set_velo_interpolation(self, method):
+        if method not in METHODS:
+            raise ValueError("unknown interpolation_method")
+        self.velo_interpolation = method
+
+    def set_phi_interpolation(self, method):
+        if method not in METHODS:
+            raise ValueError("unknown interpolation_method")
+        self.phi_interpolation = method
+
+    def advect_from_n_to_np1(self, dt, v, phi_n, vxx=None, phi_xx_n=None, xyz_np1=None):
+        """v: (dim, N_n) node velocities, or a VortexVelocity (the CF overload). Returns phi at the
+        nodes of forest_np1 (host arrays)."""
+        lib = L.load()
+        N = self.ls_n.num_nodes
+        xyz = xyz_np1 if xyz_np1 is not None else self.forest_np1.node_xyz()
+        xyz = _f64(xyz, "xyz_np1").reshape(-1, self.dim)
+        phi_n = _f64(phi_n, "phi_n", N)
+        pdd = None if phi_xx_n is None else _f64(phi_xx_n, "phi_xx_n", self.dim * N)
+        out = np.empty(len(xyz), np.float64)
+        if isinstance(v, VortexVelocity):
+            par = np.array([v.scale], np.float64)
+            L.check(lib.lsg_semi_lagrangian_advect_cf(self.ls_n.handle, L.dptr(xyz), len(xyz), float(dt), L.LSG_VELOCITY_VORTEX,
+                                                      L.dptr(par), 1, L.dptr(phi_n), _ptr(pdd), int(self.phi_interpolation),
+                                                      L.dptr(out)))
+            return out
+        v = _f64(v, "v", self.dim * N)
+        vdd = None if vxx is None else _f64(vxx, "vxx", self.dim * self.dim * N)
+        L.check(lib.lsg_semi_lagrangian_advect(self.ls_n.handle, L.dptr(xyz), len(xyz), float(dt), L.dptr(v), _ptr(vdd),
+                                               L.dptr(phi_n), _ptr(pdd), int(self.velo_interpolation), int(self.phi_interpolation),
+                                               L.dptr(out)))
+        return out

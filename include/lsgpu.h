@@ -142,10 +142,52 @@ int lsg_second_derivatives_device(lsg_level_set* ls, const double* f_dev, double
 int lsg_perturb_level_set_function(lsg_level_set* ls, double* phi, double epsilon);
 
 /* ---- instrumentation (no reference counterpart; replaces PETSc log events) --------------------- */
+/* ---- node interpolation and the semi-Lagrangian step (FP64) --------------------------------- */
+
+/* my_p4est_interpolation_nodes_t(ngbd) + set_input(F, Fxx, Fyy[, Fzz], method) + add_point +
+ * interpolate (src/my_p4est_interpolation_nodes.h:33-103, src/my_p4est_interpolation_nodes.cpp:107-288,
+ * src/my_p4est_interpolation.cpp:68-124): nfields fields F (nfields x N, node order) evaluated at
+ * npts points xyz (dim doubles per point) on the level set's grid. Each point is located after
+ * clip_in_domain (src/my_p4est_utils.h:2177-2187) with the face rule of
+ * find_smallest_quadrant_containing_point (src/my_p4est_hierarchy.cpp:264-567); the weights use the
+ * point as given. Fdd: nfields x dim x N second derivatives (all xx, then yy[, zz]) or NULL to compute
+ * them as compute_derivatives does (the reference's on-the-fly laplace at the corners). method: an
+ * LSG_LINEAR..LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2 value. out: nfields x npts. */
+int lsg_interpolate_nodes(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
+                          int method, double* out);
+int lsg_interpolate_nodes_device(lsg_level_set* ls, const double* xyz_dev, int64_t npts, const double* F_dev, int nfields,
+                                 const double* Fdd_dev, int method, double* out_dev);
+/* index (in lsg_forest_leaves order) of the leaf find_smallest_quadrant_containing_point picks for
+ * each point after clipping (device pointers) */
+int lsg_locate_points_device(lsg_level_set* ls, const double* xyz_dev, int64_t npts, int32_t* leaf_dev);
+
+/* my_p4est_semi_lagrangian_t::advect_from_n_to_np1(dt, Vec* v, Vec** vxx, phi_n, phi_xx_n, phi_np1)
+ * (src/my_p4est_semi_lagrangian.cpp:148-223): ls is the grid at time n; xyz_np1 holds the npts nodes
+ * of the grid at n+1 (lsg_forest_node_xyz of that forest). v: dim x N velocity components; vdd:
+ * dim x dim x N (component, axis, node) or NULL; phi_dd: dim x N or NULL. RK2 backtrace
+ * x* = x - dt/2 v(x), x_d = x - dt v(x*), both clipped; phi_np1 = phi_n(x_d). */
+int lsg_semi_lagrangian_advect(lsg_level_set* ls, const double* xyz_np1, int64_t npts, double dt, const double* v, const double* vdd,
+                               const double* phi_n, const double* phi_dd, int velo_method, int phi_method, double* phi_np1);
+int lsg_semi_lagrangian_advect_device(lsg_level_set* ls, const double* xyz_np1_dev, int64_t npts, double dt, const double* v_dev,
+                                      const double* vdd_dev, const double* phi_n_dev, const double* phi_dd_dev, int velo_method,
+                                      int phi_method, double* phi_np1_dev);
+
+/* the CF overload advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1)
+ * (src/my_p4est_semi_lagrangian.cpp:108-146) with an analytic velocity evaluated on the device:
+ * velocity LSG_VELOCITY_VORTEX is the single vortex of examples/level_set_advection/main_2d.cpp:116-181
+ * times params[0] (the example's direction sign, or cos(pi t/T)). */
+enum { LSG_VELOCITY_VORTEX = 0 };
+int lsg_semi_lagrangian_advect_cf(lsg_level_set* ls, const double* xyz_np1, int64_t npts, double dt, int velocity,
+                                  const double* params, int nparams, const double* phi_n, const double* phi_dd, int phi_method,
+                                  double* phi_np1);
+int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz_np1_dev, int64_t npts, double dt, int velocity,
+                                         const double* params, int nparams, const double* phi_n_dev, const double* phi_dd_dev,
+                                         int phi_method, double* phi_np1_dev);
+
 /* kernel classes reported by lsg_level_set_kernel_times */
 enum {
   LSG_K_DD64 = 0, LSG_K_PREP64, LSG_K_STAGE64, LSG_K_ADVECT64, LSG_K_DD32, LSG_K_PREP_MIXED, LSG_K_STAGE32, LSG_K_ADVECT32,
-  LSG_K_CONVERT, LSG_K_COPY, LSG_K_NUM
+  LSG_K_CONVERT, LSG_K_COPY, LSG_K_INTERP, LSG_K_NUM
 };
 /* record CUDA events around every launch (adds a little overhead) */
 int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on);

@@ -808,6 +808,250 @@ void advect_normal(const Ctx& cx, const double* vn, const double* vn_np1, double
   for (int64_t n = 0; n < N; ++n) phi[n] = 0.5 * (phi_n[n] + phi_np2[n]);
 }
 
+// ---- node interpolation ------------------------------------------------------------------------
+// PI of src/casl_math.h:15
+const double ORA_PI = 3.1415926535897932384626433832795;
+
+// clip_in_domain, non-periodic (src/my_p4est_utils.h:2177-2187)
+template <int D>
+void clip_in_domain(const Grid<D>& g, double* xyz) {
+  for (int a = 0; a < D; ++a)
+    if (xyz[a] < g.xyz_min[a] || xyz[a] > g.xyz_max[a]) xyz[a] = MAX(g.xyz_min[a], MIN(g.xyz_max[a], xyz[a]));
+}
+
+// find_smallest_quadrant_containing_point + find_quadrant_containing_point, single process,
+// non-periodic (src/my_p4est_hierarchy.cpp:264-425, 427-567): the point is scaled to tree units,
+// pushed qeps inside the brick, and probed at +-threshold along every axis on which it lies within
+// threshold of a cell face; the first probe landing in the finest leaf wins.
+template <int D>
+int32_t find_smallest_quadrant(const Grid<D>& g, const double* xyz) {
+  const double ROOT = (double)Grid<D>::ROOT_LEN;
+  const double qeps = (double)1 / ROOT;
+  const double threshold = 0.01 * (double)1;
+  double xs[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    xs[a] = xyz[a] - g.xyz_min[a];
+    xs[a] /= (g.xyz_max[a] - g.xyz_min[a]) / g.n[a];
+  }
+  int tr[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    xs[a] = MAX(qeps, MIN(xs[a], g.n[a] - qeps));
+    tr[a] = (int)floor(xs[a]);
+  }
+  double c[3] = {0, 0, 0};
+  bool face[3] = {false, false, false};
+  for (int a = 0; a < D; ++a) {
+    c[a] = (xs[a] - tr[a]) * ROOT;
+    face[a] = (fabs(c[a] - floor(c[a])) < threshold || fabs(ceil(c[a]) - c[a]) < threshold);
+  }
+  int best = -1, best_level = -1;
+  for (int i = (face[0] ? -1 : 0); i < 2; i += 2)
+    for (int j = (face[1] ? -1 : 0); j < 2; j += 2)
+      for (int k = (D == 3 && face[2] ? -1 : 0); k < (D == 3 ? 2 : 1); k += 2) {
+        const int off[3] = {i, j, k};
+        double s[3];
+        int t[3] = {tr[0], tr[1], tr[2]};
+        for (int a = 0; a < D; ++a) {
+          s[a] = (off[a] == 0 ? c[a] : c[a] + off[a] * threshold);
+          if (s[a] < 0 || s[a] >= ROOT) {
+            const int slide = (int)floor(s[a] / ROOT);
+            s[a] -= ((double)slide) * ROOT;
+            t[a] = tr[a] + slide;
+          }
+          if (t[a] < 0 || t[a] >= g.n[a]) throw std::runtime_error("oracle: point outside the brick");
+        }
+        const int tt = g.tree_at(t[0], t[1], D == 3 ? t[2] : 0);
+        const int32_t q = descend(g, tt, s);
+        if (g.leaves[q].level > best_level) {
+          best_level = g.leaves[q].level;
+          best = q;
+        }
+      }
+  return best;
+}
+
+enum { ORA_LINEAR = 0, ORA_QUADRATIC, ORA_QUADRATIC_NON_OSCILLATORY, ORA_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V1,
+       ORA_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2 };
+
+// get_local_interpolation_weights (src/my_p4est_utils.cpp:367-408)
+template <int D>
+void local_weights(const Grid<D>& g, const Leaf& Q, const double* xyz_global, double* lw, double* sdw) {
+  const double* tmin = &g.tv_min[3 * Q.tree];
+  const double* tmax = &g.tv_max[3 * Q.tree];
+  const double qh = (double)(Grid<D>::ROOT_LEN >> Q.level) / (double)Grid<D>::ROOT_LEN;
+  double xyz[3], d_[3][2];
+  for (int a = 0; a < D; ++a) {
+    const double qmin = (double)Q.x[a] / (double)Grid<D>::ROOT_LEN;
+    xyz[a] = (xyz_global[a] - tmin[a]) / (tmax[a] - tmin[a]);
+    xyz[a] = (xyz[a] - qmin) / qh;
+    d_[a][0] = 1.0 - xyz[a];
+    d_[a][1] = xyz[a];
+  }
+  for (int c = 0; c < Grid<D>::CH; ++c) {
+    const int ix = c & 1, iy = (c >> 1) & 1, iz = (c >> 2) & 1;
+    lw[c] = (D == 3 ? d_[0][ix] * d_[1][iy] * d_[2][iz] : d_[0][ix] * d_[1][iy]);
+  }
+  for (int a = 0; a < D; ++a) {
+    const double h = (tmax[a] - tmin[a]) * qh;
+    sdw[a] = h * h * d_[a][0] * d_[a][1];
+  }
+}
+
+// the five interpolation kernels (src/my_p4est_utils.cpp:410-576), one function value f[CH] with
+// second derivatives fdd[CH][D] at the corners
+template <int D>
+double interpolate_local(int method, const double* lw, const double* sdw, const double* f, const double (*fdd)[3]) {
+  const int CH = Grid<D>::CH;
+  double r = 0.0;
+  if (method == ORA_LINEAR) {
+    for (int j = 0; j < CH; ++j) r += +f[j] * lw[j];
+    return r;
+  }
+  double dd[3] = {0, 0, 0};
+  if (method == ORA_QUADRATIC) {
+    for (int j = 0; j < CH; ++j) {
+      for (int i = 0; i < D; ++i) dd[i] = ((j == 0) ? 0.0 : dd[i]) + fdd[j][i] * lw[j];
+      r += f[j] * lw[j];
+    }
+  } else if (method == ORA_QUADRATIC_NON_OSCILLATORY) {
+    for (int j = 0; j < CH; ++j) {
+      for (int i = 0; i < D; ++i) dd[i] = (j == 0 ? fdd[j][i] : MINMOD(dd[i], fdd[j][i]));
+      r += f[j] * lw[j];
+    }
+  } else if (method == ORA_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V1) {
+    for (int i = 0; i < D; ++i) {
+      dd[i] = 0.0;
+      for (int jm = 0; jm < CH; ++jm) {
+        if ((jm >> i) & 1) continue;
+        const int jp = jm | (1 << i);
+        dd[i] += MINMOD(fdd[jm][i], fdd[jp][i]) * (lw[jm] + lw[jp]);
+      }
+    }
+    for (int j = 0; j < CH; ++j) r += f[j] * lw[j];
+  } else {
+    for (int i = 0; i < D; ++i) {
+      double m = 0, p = 0;
+      for (int jm = 0; jm < CH; ++jm) {
+        if ((jm >> i) & 1) continue;
+        const int jp = jm | (1 << i);
+        m += fdd[jm][i] * (lw[jm] + lw[jp]);
+        p += fdd[jp][i] * (lw[jm] + lw[jp]);
+      }
+      dd[i] = MINMOD(m, p);
+    }
+    for (int j = 0; j < CH; ++j) r += f[j] * lw[j];
+  }
+  if (D == 3)
+    r -= 0.5 * (sdw[0] * dd[0] + sdw[1] * dd[1] + sdw[2] * dd[2]);
+  else
+    r -= 0.5 * (sdw[0] * dd[0] + sdw[1] * dd[1]);
+  return r;
+}
+
+// my_p4est_interpolation_t::add_point_general + my_p4est_interpolation_nodes_t::interpolate
+// (src/my_p4est_interpolation.cpp:68-124, src/my_p4est_interpolation_nodes.cpp:107-288): the leaf
+// is located from the clipped point, the weights use the point as given. F: nf fields of N values;
+// Fdd: nf x D x N second derivatives (required unless method is linear). out: nf x np.
+template <int D>
+void interpolate_points(const Ctx& cx, int method, int nf, const double* F, const double* Fdd, int64_t np, const double* xyz,
+                        double* out, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
+  const int64_t N = cx.N;
+  const int CH = Grid<D>::CH;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (int64_t p = 0; p < np; ++p) {
+    double xc[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) xc[a] = xyz[p * D + a];
+    clip_in_domain(g, xc);
+    const int32_t q = find_smallest_quadrant(g, xc);
+    double lw[8], sdw[3];
+    local_weights(g, g.leaves[q], xyz + p * D, lw, sdw);
+    for (int k = 0; k < nf; ++k) {
+      double f[8], fdd[8][3];
+      for (int j = 0; j < CH; ++j) {
+        const int32_t node = g.local_nodes[(size_t)q * CH + j];
+        f[j] = F[(size_t)k * N + node];
+        for (int a = 0; a < D; ++a) fdd[j][a] = (method == ORA_LINEAR ? 0.0 : Fdd[((size_t)k * D + a) * N + node]);
+      }
+      out[(size_t)k * np + p] = interpolate_local<D>(method, lw, sdw, f, fdd);
+    }
+  }
+}
+
+// single-vortex velocity of examples/level_set_advection/main_2d.cpp:116-181, scaled by s (the
+// example's sign, or cos(pi t/T))
+template <int D>
+void vortex(const double* x, double s, double* v) {
+  if (D == 3) {
+    v[0] = 2.0 * (sin(ORA_PI * x[0]) * sin(ORA_PI * x[0])) * sin(2 * ORA_PI * x[1]) * sin(2 * ORA_PI * x[2]) * s;
+    v[1] = -(sin(ORA_PI * x[1]) * sin(ORA_PI * x[1])) * sin(2 * ORA_PI * x[0]) * sin(2 * ORA_PI * x[2]) * s;
+    v[2] = -(sin(ORA_PI * x[2]) * sin(ORA_PI * x[2])) * sin(2 * ORA_PI * x[0]) * sin(2 * ORA_PI * x[1]) * s;
+  } else {
+    v[0] = -(sin(ORA_PI * x[0]) * sin(ORA_PI * x[0])) * sin(2 * ORA_PI * x[1]) * s;
+    v[1] = (sin(ORA_PI * x[1]) * sin(ORA_PI * x[1])) * sin(2 * ORA_PI * x[0]) * s;
+  }
+}
+
+// second derivatives of nf fields (nf x D x N) when the caller gives none
+template <int D>
+const double* derivatives_of(const Ctx& cx, int nf, const double* F, const double* Fdd, std::vector<double>& store, int nthreads) {
+  if (Fdd) return Fdd;
+  store.resize((size_t)nf * D * cx.N);
+  for (int k = 0; k < nf; ++k) compute_derivatives<D>(cx, F + (size_t)k * cx.N, store.data() + (size_t)k * D * cx.N, nthreads);
+  return store.data();
+}
+
+// advect_from_n_to_np1(dt, Vec* v, Vec** vxx, phi_n, phi_xx_n, phi_np1) (src/my_p4est_semi_lagrangian.cpp:148-223):
+// v at the new nodes, v at x* = x - dt/2 v (clipped), phi at x_d = x - dt v* (clipped).
+template <int D>
+void sl_advect(const Ctx& cx, int64_t np, const double* xyz, double dt, const double* v, const double* vdd, const double* phi,
+               const double* phi_dd, int velo_method, int phi_method, double* phi_np1, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
+  std::vector<double> vs, ps;
+  vdd = (velo_method == ORA_LINEAR ? nullptr : derivatives_of<D>(cx, D, v, vdd, vs, nthreads));
+  phi_dd = (phi_method == ORA_LINEAR ? nullptr : derivatives_of<D>(cx, 1, phi, phi_dd, ps, nthreads));
+  std::vector<double> vt((size_t)D * np), pts((size_t)D * np);
+  interpolate_points<D>(cx, velo_method, D, v, vdd, np, xyz, vt.data(), nthreads);
+  for (int64_t n = 0; n < np; ++n) {
+    double x[3];
+    for (int a = 0; a < D; ++a) x[a] = xyz[n * D + a];
+    for (int a = 0; a < D; ++a) x[a] -= 0.5 * dt * vt[(size_t)a * np + n];
+    clip_in_domain(g, x);
+    for (int a = 0; a < D; ++a) pts[n * D + a] = x[a];
+  }
+  interpolate_points<D>(cx, velo_method, D, v, vdd, np, pts.data(), vt.data(), nthreads);
+  for (int64_t n = 0; n < np; ++n) {
+    double x[3];
+    for (int a = 0; a < D; ++a) x[a] = xyz[n * D + a];
+    for (int a = 0; a < D; ++a) x[a] -= dt * vt[(size_t)a * np + n];
+    clip_in_domain(g, x);
+    for (int a = 0; a < D; ++a) pts[n * D + a] = x[a];
+  }
+  interpolate_points<D>(cx, phi_method, 1, phi, phi_dd, np, pts.data(), phi_np1, nthreads);
+}
+
+// advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1) (src/my_p4est_semi_lagrangian.cpp:108-146)
+// with the single-vortex velocity scaled by vscale.
+template <int D>
+void sl_advect_vortex(const Ctx& cx, int64_t np, const double* xyz, double dt, double vscale, const double* phi, const double* phi_dd,
+                      int phi_method, double* phi_np1, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
+  std::vector<double> ps;
+  phi_dd = (phi_method == ORA_LINEAR ? nullptr : derivatives_of<D>(cx, 1, phi, phi_dd, ps, nthreads));
+  std::vector<double> pts((size_t)D * np);
+  for (int64_t n = 0; n < np; ++n) {
+    double x[3], xs[3], v[3];
+    for (int a = 0; a < D; ++a) x[a] = xyz[n * D + a];
+    vortex<D>(x, vscale, v);
+    for (int a = 0; a < D; ++a) xs[a] = x[a] - 0.5 * dt * v[a];
+    clip_in_domain(g, xs);
+    vortex<D>(xs, vscale, v);
+    for (int a = 0; a < D; ++a) pts[n * D + a] = x[a] - dt * v[a];
+    clip_in_domain(g, &pts[n * D]);
+  }
+  interpolate_points<D>(cx, phi_method, 1, phi, phi_dd, np, pts.data(), phi_np1, nthreads);
+}
+
 template <int D>
 Ctx* build_from_leaves(const int* n_xyz, const double* lo, const double* hi, int64_t nleaves, const int32_t* tree,
                        const int32_t* level, const int32_t* xyz) {
@@ -975,6 +1219,75 @@ int ora_advect_cfl_dt(void* h, const double* vn, double* dt_out) {
       dt = MIN(dt, 0.8 * fabs(smin / vn[n]));
     }
     *dt_out = dt;
+  });
+}
+
+int ora_interpolate(void* h, int method, int nfields, const double* F, const double* Fdd, int64_t npts, const double* xyz,
+                    double* out, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("interpolation needs a grid built from leaves");
+    if (method < 0 || method > 4) throw std::invalid_argument("unknown interpolation method");
+    std::vector<double> store;
+    if (cx->dim == 2) {
+      const double* dd = method == ORA_LINEAR ? nullptr : derivatives_of<2>(*cx, nfields, F, Fdd, store, nthreads);
+      interpolate_points<2>(*cx, method, nfields, F, dd, npts, xyz, out, nthreads);
+    } else {
+      const double* dd = method == ORA_LINEAR ? nullptr : derivatives_of<3>(*cx, nfields, F, Fdd, store, nthreads);
+      interpolate_points<3>(*cx, method, nfields, F, dd, npts, xyz, out, nthreads);
+    }
+  });
+}
+
+// leaf chosen by the point location for each point (after clipping)
+int ora_locate(void* h, int64_t npts, const double* xyz, int32_t* leaf) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("point location needs a grid built from leaves");
+    for (int64_t p = 0; p < npts; ++p) {
+      double x[3] = {0, 0, 0};
+      for (int a = 0; a < cx->dim; ++a) x[a] = xyz[p * cx->dim + a];
+      if (cx->dim == 2) {
+        clip_in_domain(*static_cast<Grid<2>*>(cx->grid), x);
+        leaf[p] = find_smallest_quadrant(*static_cast<Grid<2>*>(cx->grid), x);
+      } else {
+        clip_in_domain(*static_cast<Grid<3>*>(cx->grid), x);
+        leaf[p] = find_smallest_quadrant(*static_cast<Grid<3>*>(cx->grid), x);
+      }
+    }
+  });
+}
+
+int ora_sl_advect(void* h, int64_t npts, const double* xyz, double dt, const double* v, const double* vdd, const double* phi,
+                  const double* phi_dd, int velo_method, int phi_method, double* phi_np1, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("semi-Lagrangian step needs a grid built from leaves");
+    if (cx->dim == 2) sl_advect<2>(*cx, npts, xyz, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
+    else sl_advect<3>(*cx, npts, xyz, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
+  });
+}
+
+int ora_sl_advect_vortex(void* h, int64_t npts, const double* xyz, double dt, double vscale, const double* phi, const double* phi_dd,
+                         int phi_method, double* phi_np1, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("semi-Lagrangian step needs a grid built from leaves");
+    if (cx->dim == 2) sl_advect_vortex<2>(*cx, npts, xyz, dt, vscale, phi, phi_dd, phi_method, phi_np1, nthreads);
+    else sl_advect_vortex<3>(*cx, npts, xyz, dt, vscale, phi, phi_dd, phi_method, phi_np1, nthreads);
+  });
+}
+
+// velocity of the single vortex at points (D per point), D x np output
+int ora_vortex(int dim, int64_t npts, const double* xyz, double vscale, double* v) {
+  return guard([&] {
+    for (int64_t p = 0; p < npts; ++p) {
+      double x[3] = {0, 0, 0}, w[3];
+      for (int a = 0; a < dim; ++a) x[a] = xyz[p * dim + a];
+      if (dim == 2) vortex<2>(x, vscale, w);
+      else vortex<3>(x, vscale, w);
+      for (int a = 0; a < dim; ++a) v[(size_t)a * npts + p] = w[a];
+    }
   });
 }
 

@@ -31,6 +31,11 @@ SIG = {
     "ora_reinitialize": (_I, [_P, _DP, _I, _I, _D, _D, _I, _I]),
     "ora_advect_in_normal_direction": (_I, [_P, _DP, _DP, _DP, _D, _DP, _I]),
     "ora_advect_cfl_dt": (_I, [_P, _DP, _DP]),
+    "ora_interpolate": (_I, [_P, _I, _I, _DP, _DP, _I64, _DP, _DP, _I]),
+    "ora_locate": (_I, [_P, _I64, _DP, _P]),
+    "ora_sl_advect": (_I, [_P, _I64, _DP, _D, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
+    "ora_sl_advect_vortex": (_I, [_P, _I64, _DP, _D, _D, _DP, _DP, _I, _DP, _I]),
+    "ora_vortex": (_I, [_I, _I64, _DP, _D, _DP]),
 }
 _lib = None
 
@@ -135,3 +140,49 @@ class OracleGrid:
         out = C.c_double()
         _chk(load().ora_advect_cfl_dt(self._h, _dp(np.ascontiguousarray(vn, np.float64)), C.byref(out)))
         return out.value
+
+    # ---- node interpolation and the semi-Lagrangian step ------------------------------------
+    def interpolate(self, method, F, xyz, Fdd=None, nthreads=1):
+        """F: (nf, N) or (N,); xyz: (np, dim); Fdd: (nf, dim, N) or None. Returns (nf, np) or (np,)."""
+        F = np.ascontiguousarray(F, np.float64)
+        single = F.ndim == 1
+        F2 = F.reshape(1, -1) if single else F
+        pts = np.ascontiguousarray(xyz, np.float64).reshape(-1, self.dim)
+        dd = None if Fdd is None else np.ascontiguousarray(Fdd, np.float64)
+        out = np.empty((F2.shape[0], len(pts)), np.float64)
+        _chk(load().ora_interpolate(self._h, int(method), F2.shape[0], _dp(F2), _dp(dd), len(pts), _dp(pts), _dp(out), nthreads))
+        return out[0] if single else out
+
+    def locate(self, xyz):
+        pts = np.ascontiguousarray(xyz, np.float64).reshape(-1, self.dim)
+        out = np.empty(len(pts), np.int32)
+        _chk(load().ora_locate(self._h, len(pts), _dp(pts), out.ctypes.data))
+        return out
+
+    def sl_advect(self, xyz_np1, dt, v, phi, vdd=None, phi_dd=None, velo_method=4, phi_method=4, nthreads=1):
+        pts = np.ascontiguousarray(xyz_np1, np.float64).reshape(-1, self.dim)
+        v = np.ascontiguousarray(v, np.float64)
+        phi = np.ascontiguousarray(phi, np.float64)
+        vdd = None if vdd is None else np.ascontiguousarray(vdd, np.float64)
+        phi_dd = None if phi_dd is None else np.ascontiguousarray(phi_dd, np.float64)
+        out = np.empty(len(pts), np.float64)
+        _chk(load().ora_sl_advect(self._h, len(pts), _dp(pts), float(dt), _dp(v), _dp(vdd), _dp(phi), _dp(phi_dd), int(velo_method),
+                                  int(phi_method), _dp(out), nthreads))
+        return out
+
+    def sl_advect_vortex(self, xyz_np1, dt, vscale, phi, phi_dd=None, phi_method=4, nthreads=1):
+        pts = np.ascontiguousarray(xyz_np1, np.float64).reshape(-1, self.dim)
+        phi = np.ascontiguousarray(phi, np.float64)
+        phi_dd = None if phi_dd is None else np.ascontiguousarray(phi_dd, np.float64)
+        out = np.empty(len(pts), np.float64)
+        _chk(load().ora_sl_advect_vortex(self._h, len(pts), _dp(pts), float(dt), float(vscale), _dp(phi), _dp(phi_dd),
+                                         int(phi_method), _dp(out), nthreads))
+        return out
+
+
+def vortex(dim, xyz, vscale=1.0):
+    """Single-vortex velocity at points (np, dim) -> (dim, np)."""
+    pts = np.ascontiguousarray(xyz, np.float64).reshape(-1, dim)
+    out = np.empty((dim, len(pts)), np.float64)
+    _chk(load().ora_vortex(dim, len(pts), _dp(pts), float(vscale), _dp(out)))
+    return out
