@@ -33,6 +33,9 @@ SIGNATURES = {
     "lsg_forest_dim": (_I, [_P]),
     "lsg_forest_num_leaves": (_I64, [_P]),
     "lsg_forest_leaves": (_I, [_P, _I32P, _I32P, _I32P]),
+    "lsg_forest_copy": (_I, [_P, C.POINTER(_P)]),
+    "lsg_forest_set_leaves": (_I, [_P, _I64, _I32P, _I32P, _I32P]),
+    "lsg_forest_refine_and_coarsen": (_I, [_P, _I, _I, _D, _D, _DP, C.POINTER(_I)]),
     "lsg_forest_refine": (_I, [_P, _U8P, _I64]),
     "lsg_forest_coarsen": (_I, [_P, _U8P, _I64]),
     "lsg_forest_tag_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _U8P]),

@@ -5,6 +5,7 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/lsgpu.h"
@@ -221,6 +222,47 @@ int lsg_forest_coarsen(lsg_forest* f, const uint8_t* tags, int64_t n) {
     with_forest(f, [&](auto& F) {
       need(tags != nullptr && n == (int64_t)F.num_leaves(), "coarsen: one tag per leaf required");
       F.coarsen(tags);
+    });
+  });
+}
+
+int lsg_forest_copy(const lsg_forest* f, lsg_forest** out) {
+  return guard([&] {
+    need(f != nullptr && out != nullptr, "null argument");
+    lsg_forest* c = new lsg_forest();
+    c->dim = f->dim;
+    try {
+      if (f->dim == 2)
+        c->f2 = new Forest<2>(*f->f2);
+      else
+        c->f3 = new Forest<3>(*f->f3);
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+int lsg_forest_set_leaves(lsg_forest* f, int64_t n, const int32_t* tree, const int32_t* level, const int32_t* xyz) {
+  return guard([&] {
+    need(tree != nullptr && level != nullptr && xyz != nullptr && n > 0, "set_leaves: null arguments");
+    with_forest(f, [&](auto& F) { F.set_leaves((size_t)n, tree, level, xyz); });
+  });
+}
+
+int lsg_forest_refine_and_coarsen(lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, const double* phi,
+                                  int* changed) {
+  return guard([&] {
+    need(phi != nullptr && changed != nullptr, "refine_and_coarsen: null arguments");
+    need(min_lvl >= 0 && min_lvl <= max_lvl, "refine_and_coarsen: need 0 <= min_lvl <= max_lvl");
+    with_forest(f, [&](auto& F) {
+      using FT = std::decay_t<decltype(F)>;
+      need(max_lvl <= FT::DD::QMAXLEVEL, "refine_and_coarsen: max_lvl above the maximum quadrant level");
+      need_nodes(F);
+      std::vector<int8_t> tag(F.num_leaves());
+      F.tag_refine_coarsen(min_lvl, max_lvl, lip, band, phi, tag.data());
+      *changed = F.coarsen_then_refine(tag.data()) ? 1 : 0;
     });
   });
 }

@@ -117,6 +117,24 @@ void Forest<D>::refine(const uint8_t* tags) {
 }
 
 template <int D>
+bool Forest<D>::family_at(size_t i, const uint8_t* tags) const {
+  const size_t nl = leaves.size();
+  const Quad& q = leaves[i];
+  if (q.level == 0 || i + DD::CHILDREN > nl) return false;
+  const int32_t hp = quadrant_len(DD::MAXLEVEL, q.level - 1);
+  for (int a = 0; a < D; ++a)
+    if (q.x[a] % hp != 0) return false;
+  const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
+  for (int c = 0; c < DD::CHILDREN; ++c) {
+    const Quad& s = leaves[i + c];
+    if (s.level != q.level || s.tree != q.tree || !tags[i + c]) return false;
+    for (int a = 0; a < D; ++a)
+      if (s.x[a] != q.x[a] + (((c >> a) & 1) ? h : 0)) return false;
+  }
+  return true;
+}
+
+template <int D>
 void Forest<D>::coarsen(const uint8_t* tags) {
   const size_t nl = leaves.size();
   std::vector<Quad> out;
@@ -126,22 +144,7 @@ void Forest<D>::coarsen(const uint8_t* tags) {
   size_t i = 0;
   while (i < nl) {
     const Quad& q = leaves[i];
-    bool family = false;
-    if (q.level > 0 && i + DD::CHILDREN <= nl) {
-      const int32_t hp = quadrant_len(DD::MAXLEVEL, q.level - 1);
-      bool first_child = true;
-      for (int a = 0; a < D; ++a) first_child = first_child && (q.x[a] % hp == 0);
-      if (first_child) {
-        family = true;
-        const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
-        for (int c = 0; c < DD::CHILDREN && family; ++c) {
-          const Quad& s = leaves[i + c];
-          if (s.level != q.level || s.tree != q.tree || !tags[i + c]) family = false;
-          for (int a = 0; a < D && family; ++a)
-            if (s.x[a] != q.x[a] + (((c >> a) & 1) ? h : 0)) family = false;
-        }
-      }
-    }
+    const bool family = family_at(i, tags);
     if (family) {
       Quad p = q;
       p.level = q.level - 1;
@@ -155,6 +158,129 @@ void Forest<D>::coarsen(const uint8_t* tags) {
     }
   }
   leaves.swap(out);
+  leaf_key.swap(keys);
+  nodes_built = false;
+}
+
+template <int D>
+bool Forest<D>::coarsen_then_refine(const int8_t* tag) {
+  const size_t nl = leaves.size();
+  const bool had_nodes = nodes_built;
+  std::vector<uint8_t> ctag(nl);
+  for (size_t i = 0; i < nl; ++i) ctag[i] = tag[i] < 0;
+  std::vector<Quad> out;
+  std::vector<uint64_t> keys;
+  std::vector<uint8_t> rtag;
+  out.reserve(nl);
+  keys.reserve(nl);
+  rtag.reserve(nl);
+  bool changed = false;
+  size_t i = 0;
+  while (i < nl) {
+    const Quad& q = leaves[i];
+    if (family_at(i, ctag.data())) {
+      Quad p = q;
+      p.level = q.level - 1;
+      out.push_back(p);
+      keys.push_back(leaf_key[i]);
+      rtag.push_back(0);
+      changed = true;
+      i += DD::CHILDREN;
+    } else {
+      out.push_back(q);
+      keys.push_back(leaf_key[i]);
+      rtag.push_back(tag[i] > 0 ? 1 : 0);
+      ++i;
+    }
+  }
+  leaves.swap(out);
+  leaf_key.swap(keys);
+  nodes_built = false;
+  for (uint8_t t : rtag) changed = changed || t;
+  if (!changed) {
+    nodes_built = had_nodes;  // same leaves: the node numbering still holds
+    return false;
+  }
+  refine(rtag.data());
+  return true;
+}
+
+template <int D>
+void Forest<D>::tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double band, const double* phi, int8_t* tag) const {
+  if (!nodes_built) throw std::invalid_argument("refine_and_coarsen: the forest's nodes are not built");
+  const size_t nl = leaves.size();
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii) {
+    const Quad& qd = leaves[(size_t)ii];
+    if (qd.level < min_lvl) {
+      tag[ii] = 1;
+      continue;
+    }
+    if (qd.level > max_lvl) {
+      tag[ii] = -1;
+      continue;
+    }
+    double f[DD::CHILDREN];
+    for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[local_nodes[(size_t)ii * DD::CHILDREN + c]];
+    const double* tmn = &brick.tmin[3 * qd.tree];
+    const double* tmx = &brick.tmax[3 * qd.tree];
+    const double dmin = (double)quadrant_len(DD::MAXLEVEL, qd.level) / (double)DD::ROOT_LEN;
+    const double lmax_len = (double)quadrant_len(DD::MAXLEVEL, max_lvl) / (double)DD::ROOT_LEN;
+    const double dx = (tmx[0] - tmn[0]) * dmin;
+    const double dy = (tmx[1] - tmn[1]) * dmin;
+    double smallest_dxyz_max = max2((tmx[0] - tmn[0]), (tmx[1] - tmn[1])) * lmax_len;
+    double d;
+    if (D == 3) {
+      const double dz = (tmx[2] - tmn[2]) * dmin;
+      smallest_dxyz_max = max2(smallest_dxyz_max, (tmx[2] - tmn[2]) * lmax_len);
+      d = sqrt(dx * dx + dy * dy + dz * dz);
+    } else {
+      d = sqrt(dx * dx + dy * dy);
+    }
+    const double band_real = band * smallest_dxyz_max;
+    bool refine = false, coarsen = true;
+    for (int i = 0; i < DD::CHILDREN; ++i) {
+      refine = refine || (qd.level < max_lvl &&
+                          (fabs(f[i]) - band_real <= 0.5 * lip * d ||
+                           (i == 0 ? false : ((f[i] > 0.0 && f[0] <= 0.0) || (f[i] <= 0.0 && f[0] > 0.0)))));
+      coarsen = coarsen && qd.level > min_lvl && fabs(f[i]) - band_real >= 1.0 * lip * d &&
+                (i == 0 ? true : ((f[i] > 0.0 && f[0] > 0.0) || (f[i] <= 0.0 && f[0] <= 0.0)));
+    }
+    tag[ii] = refine ? 1 : (coarsen ? -1 : 0);
+  }
+}
+
+template <int D>
+void Forest<D>::set_leaves(size_t n, const int32_t* tree, const int32_t* level, const int32_t* xyz) {
+  std::vector<Quad> ls(n);
+  std::vector<uint64_t> keys(n);
+  int32_t expect_tree = 0;
+  uint64_t expect_key = 0;
+  for (size_t i = 0; i < n; ++i) {
+    Quad q;
+    q.tree = tree[i];
+    q.level = level[i];
+    for (int a = 0; a < 3; ++a) q.x[a] = a < D ? xyz[3 * i + a] : 0;
+    if (q.tree < 0 || q.tree >= brick.num_trees || q.level < 0 || q.level > DD::QMAXLEVEL)
+      throw std::invalid_argument("set_leaves: tree or level out of range");
+    const int32_t h = quadrant_len(DD::MAXLEVEL, q.level);
+    for (int a = 0; a < D; ++a)
+      if (q.x[a] < 0 || q.x[a] >= DD::ROOT_LEN || q.x[a] % h != 0) throw std::invalid_argument("set_leaves: misaligned leaf");
+    const uint64_t m = morton<D>(q.x);
+    if (q.tree != expect_tree || m != expect_key)
+      throw std::invalid_argument("set_leaves: leaves must form a complete forest in tree-major Morton order");
+    const uint64_t next = m + (uint64_t(1) << (D * (DD::MAXLEVEL - q.level)));
+    if (next == (uint64_t(1) << (D * DD::MAXLEVEL))) {
+      ++expect_tree;
+      expect_key = 0;
+    } else {
+      expect_key = next;
+    }
+    ls[i] = q;
+    keys[i] = (((uint64_t)q.tree) << tree_shift<D>()) | m;
+  }
+  if (expect_tree != brick.num_trees || expect_key != 0) throw std::invalid_argument("set_leaves: the leaves do not cover every tree");
+  leaves.swap(ls);
   leaf_key.swap(keys);
   nodes_built = false;
 }

@@ -65,6 +65,18 @@ struct Forest {
   // Coarsening pass: each complete family of CHILDREN sibling leaves with all tags set is merged.
   void coarsen(const uint8_t* tags);
   void build_nodes();
+  // Replace the leaves with a caller-supplied complete linear forest (tree-major Morton order,
+  // every tree covered exactly once); throws std::invalid_argument otherwise.
+  void set_leaves(size_t n, const int32_t* tree, const int32_t* level, const int32_t* xyz);
+  // splitting_criteria_tag_t::refine_and_coarsen after tagging (src/my_p4est_refine_coarsen.cpp:1170-1205):
+  // one coarsening pass over complete families whose leaves are all tagged -1, then one refinement
+  // pass over the surviving leaves tagged +1 (a parent made by coarsening is not refined).
+  // Returns true if any leaf was created.
+  bool coarsen_then_refine(const int8_t* tag);
+  // splitting_criteria_tag_t::tag_quadrant (src/my_p4est_refine_coarsen.cpp:422-479,
+  // finest_in_negative_flag = false) from the node values phi (nodes must be built):
+  // +1 refine, -1 coarsen, 0 keep.
+  void tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double band, const double* phi, int8_t* tag) const;
 
   size_t num_leaves() const { return leaves.size(); }
   size_t num_nodes() const { return node_tree.size(); }
@@ -82,6 +94,8 @@ struct Forest {
       x[a] = (v == DD::ROOT_LEN - 1) ? DD::ROOT_LEN : v;
     }
   }
+  // Leaves i..i+CHILDREN-1 form a complete family with every tag set.
+  bool family_at(size_t i, const uint8_t* tags) const;
   // Finest leaf level present (for dx_min reporting).
   int max_level() const;
   int min_level() const;

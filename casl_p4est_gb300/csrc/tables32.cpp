@@ -14,6 +14,7 @@
 //              naive second derivatives, so it is evaluated in FP64 on the unit vectors).
 // Regular nodes come first, each group keeps the node order (tree-major Morton) of the grid.
 #include <algorithm>
+#include <parallel/algorithm>
 #include <cstring>
 #include <stdexcept>
 
@@ -133,7 +134,6 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
   constexpr int CW = cls_words<D>();
   std::vector<uint8_t> is_reg((size_t)N, 0);
   std::vector<uint32_t> icount((size_t)N);
-  std::vector<double> rec((size_t)N * CW, 0.0);  // class record per node (irregular only)
 #pragma omp parallel for schedule(static)
   for (long long nn = 0; nn < (long long)N; ++nn) {
     const size_t n = (size_t)nn;
@@ -152,8 +152,19 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     }
     icount[n] = counts;
     is_reg[n] = regular ? 1 : 0;
-    if (regular) continue;
-    double* r = &rec[n * CW];
+  }
+  // class record of every irregular node (compact: slot k of irr_nodes[k])
+  std::vector<int64_t> irr_nodes;
+  for (int64_t n = 0; n < N; ++n)
+    if (!is_reg[n]) irr_nodes.push_back(n);
+  const int64_t nIrr = (int64_t)irr_nodes.size();
+  std::vector<double> rec((size_t)nIrr * CW);
+#pragma omp parallel for schedule(static)
+  for (long long kk = 0; kk < (long long)nIrr; ++kk) {
+    const size_t n = (size_t)irr_nodes[(size_t)kk];
+    const uint32_t counts = icount[n];
+    double* r = &rec[(size_t)kk * CW];
+    for (int w = 0; w < CW; ++w) r[w] = 0.0;
     uint32_t meta = counts | ((T.cidx[n] >= 0) ? (1u << 16) : 0u) | ((uint32_t)T.wall[n] << 24);
     r[0] = (double)meta;
     for (int dir = 0; dir < 2 * D; ++dir) {
@@ -171,21 +182,22 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
       for (int rr = 0; rr < D; ++rr) cm[rr * D + c] = e[rr];
     }
   }
-  // deduplicate class records (exact double keys)
-  std::vector<int64_t> irr_nodes;
-  for (int64_t n = 0; n < N; ++n)
-    if (!is_reg[n]) irr_nodes.push_back(n);
-  std::vector<int64_t> order(irr_nodes);
-  std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
-    const int c = memcmp(&rec[x * CW], &rec[y * CW], CW * sizeof(double));
+  // deduplicate class records (exact double keys): sort record slots by (record bytes, node)
+  std::vector<int64_t> slots((size_t)nIrr);
+  for (int64_t k = 0; k < nIrr; ++k) slots[(size_t)k] = k;
+  __gnu_parallel::sort(slots.begin(), slots.end(), [&](int64_t x, int64_t y) {
+    const int c = memcmp(&rec[(size_t)x * CW], &rec[(size_t)y * CW], CW * sizeof(double));
     return c != 0 ? c < 0 : x < y;
   });
+  std::vector<int64_t> order((size_t)nIrr);
+  for (int64_t i = 0; i < nIrr; ++i) order[(size_t)i] = irr_nodes[(size_t)slots[(size_t)i]];
   std::vector<int32_t> node_cls((size_t)N, -1);
   M.cls64.clear();
   int64_t ncls = 0;
   for (size_t i = 0; i < order.size(); ++i) {
-    if (i == 0 || memcmp(&rec[order[i] * CW], &rec[order[i - 1] * CW], CW * sizeof(double)) != 0) {
-      M.cls64.insert(M.cls64.end(), &rec[order[i] * CW], &rec[order[i] * CW] + CW);
+    const double* ri = &rec[(size_t)slots[i] * CW];
+    if (i == 0 || memcmp(ri, &rec[(size_t)slots[i - 1] * CW], CW * sizeof(double)) != 0) {
+      M.cls64.insert(M.cls64.end(), ri, ri + CW);
       ++ncls;
     }
     node_cls[order[i]] = (int32_t)(ncls - 1);
@@ -322,16 +334,24 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
   // nodes whose second neighbour is not recorded (irregular nodes are always in the set)
   {
     std::vector<uint8_t> inx((size_t)nR, 0);
-    for (int64_t ii = 0; ii < nI; ++ii)
+#pragma omp parallel for schedule(static)
+    for (long long ii = 0; ii < (long long)nI; ++ii)
       for (int s_ = 0; s_ < NS; ++s_) {
         const int32_t j = M.i_nbr[(size_t)s_ * nI + ii];
-        if (j < nR) inx[j] = 1;
+        if (j < nR) {
+#pragma omp atomic write
+          inx[j] = 1;
+        }
       }
-    for (int64_t ii = 0; ii < nR; ++ii)
+#pragma omp parallel for schedule(static)
+    for (long long ii = 0; ii < (long long)nR; ++ii)
       for (int dir = 0; dir < 2 * D; ++dir)
         if (M.r_nbr2[(size_t)dir * nR + ii] < 0) {
           const int32_t j = M.r_nbr[(size_t)dir * nR + ii];
-          if (j < nR) inx[j] = 1;
+          if (j < nR) {
+#pragma omp atomic write
+            inx[j] = 1;
+          }
         }
     M.x_list.clear();
     for (int64_t j = 0; j < nR; ++j)

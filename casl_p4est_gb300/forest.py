@@ -85,6 +85,39 @@ class Forest:
         L.check(L.load().lsg_forest_refine_levelset(self._h, min_lvl, max_lvl, lip, band, kind, L.dptr(params), params.size,
                                                     passes))
 
+    def copy(self) -> "Forest":
+        """p4est_copy: an independent forest with the same leaves (and nodes, if built)."""
+        h = C.c_void_p()
+        L.check(L.load().lsg_forest_copy(self._h, C.byref(h)))
+        c = Forest.__new__(Forest)
+        c._h = h
+        c.dim, c.n_xyz, c.xyz_min, c.xyz_max = self.dim, self.n_xyz, self.xyz_min, self.xyz_max
+        c.max_lvl_requested = self.max_lvl_requested
+        return c
+
+    def set_leaves(self, tree, level, xyz):
+        """Adopt a complete forest given leaf by leaf in tree-major Morton order (e.g. from p4est)."""
+        tree = np.ascontiguousarray(tree, np.int32)
+        level = np.ascontiguousarray(level, np.int32)
+        xyz3 = np.zeros((len(tree), 3), np.int32)
+        xyz = np.asarray(xyz, np.int32).reshape(len(tree), -1)
+        xyz3[:, :xyz.shape[1]] = xyz
+        L.check(L.load().lsg_forest_set_leaves(self._h, len(tree), L.i32ptr(tree), L.i32ptr(level), L.i32ptr(xyz3)))
+        self.max_lvl_requested = max(self.max_lvl_requested, int(level.max()))
+
+    def refine_and_coarsen(self, min_lvl, max_lvl, phi, lip=1.2, band=0.0) -> bool:
+        """splitting_criteria_tag_t(min_lvl, max_lvl, lip).refine_and_coarsen(p4est, nodes, phi): one
+        coarsening and one refinement pass tagged from the node values phi. Returns whether the grid
+        changed; the nodes must be rebuilt."""
+        phi = np.ascontiguousarray(phi, np.float64)
+        if phi.size != self.num_nodes:
+            raise ValueError("phi must hold one value per node")
+        changed = C.c_int(0)
+        L.check(L.load().lsg_forest_refine_and_coarsen(self._h, int(min_lvl), int(max_lvl), float(lip), float(band), L.dptr(phi),
+                                                       C.byref(changed)))
+        self.max_lvl_requested = max(self.max_lvl_requested, int(max_lvl))
+        return bool(changed.value)
+
     # ---- nodes --------------------------------------------------------------------------------
     def build_nodes(self):
         L.check(L.load().lsg_forest_build_nodes(self._h))

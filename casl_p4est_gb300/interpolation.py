@@ -111,11 +111,15 @@ class VortexVelocity:
 
 
 class my_p4est_semi_lagrangian_t:
-    """advect_from_n_to_np1 from the grid at time n (ls_n) onto the nodes of the grid at n+1."""
+    """advect_from_n_to_np1 from the grid at time n (ls_n) onto the nodes of the grid at n+1.
 
-    def __init__(self, forest_np1, ls_n: my_p4est_level_set_t):
+    splitting: (min_lvl, max_lvl, lip) of the grid's splitting criterion (the reference reads it from
+    p4est->user_pointer), used by update_p4est."""
+
+    def __init__(self, forest_np1, ls_n: my_p4est_level_set_t, splitting=None):
         self.forest_np1 = forest_np1
         self.ls_n = ls_n
+        self.splitting = splitting
         self.dim = ls_n.ngbd.dim
         self.velo_interpolation = quadratic_non_oscillatory_continuous_v2
         self.phi_interpolation = quadratic_non_oscillatory_continuous_v2
@@ -152,3 +156,29 @@ class my_p4est_semi_lagrangian_t:
                                                L.dptr(phi_n), _ptr(pdd), int(self.velo_interpolation), int(self.phi_interpolation),
                                                L.dptr(out)))
         return out
+
+    def update_p4est(self, v, dt, phi, phi_xx=None, vxx=None):
+        """update_p4est(v, dt, phi[, phi_xx]) (src/my_p4est_semi_lagrangian.cpp:321-392 for an analytic
+        velocity, :394-529 for node velocities): advect phi onto forest_np1, regrid it with
+        splitting_criteria_tag_t::refine_and_coarsen from the advected values, and repeat until the grid
+        stops changing. Second derivatives on the grid at n are computed once. Returns phi at the
+        nodes of the final forest_np1 (which is modified in place)."""
+        if self.splitting is None:
+            raise ValueError("update_p4est needs the splitting criterion (min_lvl, max_lvl, lip)")
+        min_lvl, max_lvl, lip = self.splitting
+        N = self.ls_n.num_nodes
+        phi = _f64(phi, "phi", N)
+        if phi_xx is None and self.phi_interpolation != linear:
+            phi_xx = self.ls_n.compute_derivatives(phi)
+        if not isinstance(v, VortexVelocity):
+            v = _f64(v, "v", self.dim * N).reshape(self.dim, N)
+            if vxx is None and self.velo_interpolation != linear:
+                vxx = np.stack([self.ls_n.compute_derivatives(np.ascontiguousarray(v[k])) for k in range(self.dim)])
+        f = self.forest_np1
+        self.iterations = 0
+        while True:
+            phi_np1 = self.advect_from_n_to_np1(dt, v, phi, vxx=vxx, phi_xx_n=phi_xx)
+            self.iterations += 1
+            if not f.refine_and_coarsen(min_lvl, max_lvl, phi_np1, lip=lip):
+                return phi_np1
+            f.build_nodes()

@@ -61,6 +61,18 @@ int lsg_forest_leaves(const lsg_forest* f, int32_t* tree, int32_t* level, int32_
 /* one pass of my_p4est_refine / my_p4est_coarsen with per-leaf tags (nonzero = refine/coarsen) */
 int lsg_forest_refine(lsg_forest* f, const uint8_t* tags, int64_t n);
 int lsg_forest_coarsen(lsg_forest* f, const uint8_t* tags, int64_t n);
+/* p4est_copy: an independent copy of the forest (leaves and, if built, nodes) */
+int lsg_forest_copy(const lsg_forest* f, lsg_forest** out);
+/* Replace the leaves by a caller-supplied complete forest in tree-major Morton order (e.g. the
+ * quadrants of a p4est_t, tree by tree: tree index, level, logical x y z); LSG_EINVAL unless the
+ * leaves cover every tree exactly once. Nodes must be rebuilt afterwards. */
+int lsg_forest_set_leaves(lsg_forest* f, int64_t n, const int32_t* tree, const int32_t* level, const int32_t* xyz);
+/* splitting_criteria_tag_t::refine_and_coarsen(p4est, nodes, phi) with tag_quadrant
+ * (src/my_p4est_refine_coarsen.cpp:422-479, 1170-1205): phi holds one value per node (nodes built);
+ * one coarsening pass then one refinement pass; *changed = 1 if any leaf was created. The nodes
+ * must be rebuilt afterwards. */
+int lsg_forest_refine_and_coarsen(lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, const double* phi,
+                                  int* changed);
 /* refine_levelset_cf (src/my_p4est_refine_coarsen.cpp:18-90) evaluated on every leaf for an
  * analytic shape (kind and parameters as in shapes.h); tags has one byte per leaf. */
 int lsg_forest_tag_levelset(const lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, int shape,

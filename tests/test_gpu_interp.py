@@ -161,3 +161,38 @@ def test_bad_method_is_rejected(case):
                                                L.dptr(np.zeros(1))))
     with pytest.raises(ValueError):
         interp.set_input(fields(f)[0], 9)
+
+
+@pytest.mark.parametrize("velocity", ["nodes", "vortex"])
+def test_update_p4est_matches_oracle_loop(velocity):
+    """update_p4est: repeated advect + refine_and_coarsen until the grid settles, against the same loop
+    driven by the oracle's semi-Lagrangian step (same host regrid)."""
+    f = G.my_p4est_brick_new([1, 1, 1], [0, 0, 0], [1, 1, 1])
+    sphere = G.shapes.sphere([0.35, 0.35, 0.35], 0.15)
+    f.refine_levelset(sphere, 2, 6, lip=1.2)
+    f.build_nodes()
+    phi = f.sample(sphere)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    og = O.OracleGrid.from_forest(f)
+    dt = 4.0 / 64
+    x = f.node_xyz()
+    v = G.VortexVelocity(1.0) if velocity == "vortex" else np.ascontiguousarray(O.vortex(3, x, 1.0))
+    sl = G.my_p4est_semi_lagrangian_t(f.copy(), ls, splitting=(2, 6, 1.2))
+    got = sl.update_p4est(v, dt, phi)
+    # oracle-driven loop
+    g = f.copy()
+    while True:
+        xyz = g.node_xyz()
+        if velocity == "vortex":
+            ref = og.sl_advect_vortex(xyz, dt, 1.0, phi)
+        else:
+            ref = og.sl_advect(xyz, dt, v, phi)
+        if not g.refine_and_coarsen(2, 6, ref, lip=1.2):
+            break
+        g.build_nodes()
+    assert sl.iterations >= 2
+    assert np.array_equal(sl.forest_np1.leaves()[2], g.leaves()[2])
+    if velocity == "vortex":
+        assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(phi))
+    else:
+        assert np.array_equal(got, ref)
