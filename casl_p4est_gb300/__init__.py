@@ -7,12 +7,12 @@ C ABI (include/lsgpu.h). The Python classes mirror the reference's C++ class API
 from . import shapes
 from ._lib import LSG_FP64, LSG_MIXED, LsgError, LsgInvalidArgument, load
 from .forest import Forest, my_p4est_brick_new, my_p4est_node_neighbors_t, qnnn_dtype
-from .level_set import DBL_MAX, my_p4est_level_set_t
+from .level_set import DBL_MAX, my_p4est_level_set_batch_t, my_p4est_level_set_t
 from .interpolation import VortexVelocity, my_p4est_interpolation_nodes_t, my_p4est_semi_lagrangian_t
 from . import interpolation
 
 __all__ = [
     "shapes", "load", "LsgError", "LsgInvalidArgument", "LSG_FP64", "LSG_MIXED", "Forest", "my_p4est_brick_new",
     "my_p4est_node_neighbors_t", "qnnn_dtype", "my_p4est_level_set_t", "DBL_MAX", "interpolation",
-    "my_p4est_interpolation_nodes_t", "my_p4est_semi_lagrangian_t", "VortexVelocity",
+    "my_p4est_interpolation_nodes_t", "my_p4est_semi_lagrangian_t", "VortexVelocity", "my_p4est_level_set_batch_t",
 ]

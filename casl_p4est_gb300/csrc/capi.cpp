@@ -626,6 +626,106 @@ int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz, i
   });
 }
 
+int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set** out) {
+  return guard([&] {
+    need(out != nullptr && forests != nullptr && count > 0, "batch: null arguments or no grids");
+    const int dim = forests[0] ? forests[0]->dim : 0;
+    need(dim == 2 || dim == 3, "batch: null forest");
+    for (int k = 0; k < count; ++k) need(forests[k] != nullptr && forests[k]->dim == dim, "batch: grids of one dimension required");
+    lsg_level_set* ls = new lsg_level_set();
+    ls->dim = dim;
+    try {
+      if (dim == 2) {
+        std::vector<const Forest<2>*> parts;
+        for (int k = 0; k < count; ++k) parts.push_back(forests[k]->f2);
+        ls->l2 = new LevelSet<2>(parts);
+      } else {
+        std::vector<const Forest<3>*> parts;
+        for (int k = 0; k < count; ++k) parts.push_back(forests[k]->f3);
+        ls->l3 = new LevelSet<3>(parts);
+      }
+    } catch (...) {
+      delete ls;
+      throw;
+    }
+    *out = ls;
+  });
+}
+
+int lsg_batch_count(const lsg_level_set* ls) {
+  if (!ls) return -1;
+  return (int)((ls->dim == 2 ? ls->l2->part_offsets.size() : ls->l3->part_offsets.size()) - 1);
+}
+
+int lsg_batch_offsets(const lsg_level_set* ls, int64_t* offsets) {
+  return guard([&] {
+    need(ls != nullptr && offsets != nullptr, "null argument");
+    const auto& o = ls->dim == 2 ? ls->l2->part_offsets : ls->l3->part_offsets;
+    for (size_t k = 0; k < o.size(); ++k) offsets[k] = o[k];
+  });
+}
+
+int lsg_batch_reinitialize_device(lsg_level_set* ls, double* phi_dev, const int* iterations, int use_graph) {
+  return guard([&] {
+    need(phi_dev != nullptr && iterations != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.reinitialize_batch(phi_dev, iterations, use_graph != 0); });
+  });
+}
+
+int lsg_batch_reinitialize(lsg_level_set* ls, double* phi, const int* iterations, int use_graph) {
+  return guard([&] {
+    need(phi != nullptr && iterations != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      L.ws_phi.alloc(L.N);
+      cuda_check(cudaMemcpyAsync(L.ws_phi.p, phi, L.N * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D phi");
+      L.reinitialize_batch(L.ws_phi.p, iterations, use_graph != 0);
+      cuda_check(cudaMemcpyAsync(phi, L.ws_phi.p, L.N * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H phi");
+      cuda_check(cudaStreamSynchronize(L.stream), "batch sync");
+    });
+  });
+}
+
+int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int* config) {
+  return guard([&] {
+    need(phi != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) {
+      L.ws_phi.alloc(L.N);
+      cuda_check(cudaMemcpyAsync(L.ws_phi.p, phi, L.N * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D phi");
+      L.autotune(L.ws_phi.p, trials);
+      cuda_check(cudaStreamSynchronize(L.stream), "autotune sync");
+      if (config) {
+        config[0] = L.cfg.tpb;
+        config[1] = L.cfg.uniform_blocks;
+        config[2] = L.cfg.regular_blocks;
+      }
+    });
+  });
+}
+
+int lsg_level_set_stage_config(const lsg_level_set* ls, int* config) {
+  return guard([&] {
+    need(ls != nullptr && config != nullptr, "null argument");
+    const StageCfg& c = ls->dim == 2 ? ls->l2->cfg : ls->l3->cfg;
+    config[0] = c.tpb;
+    config[1] = c.uniform_blocks;
+    config[2] = c.regular_blocks;
+  });
+}
+
+int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
+  return guard([&] {
+    need(config != nullptr, "null config");
+    need(config[0] == 32 || config[0] == 64 || config[0] == 128 || config[0] == 256, "threads per block must be 32, 64, 128 or 256");
+    need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
+    with_ls(ls, [&](auto& L) {
+      L.cfg.tpb = config[0];
+      L.cfg.uniform_blocks = config[1];
+      L.cfg.regular_blocks = config[2];
+      L.drop_graph();
+    });
+  });
+}
+
 int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on) {
   return guard([&] { with_ls(ls, [&](auto& L) { L.timer.enabled = on != 0; }); });
 }

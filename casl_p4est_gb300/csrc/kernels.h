@@ -13,7 +13,16 @@ enum : uint16_t {
   ST_OUTSIDE = 2,    // phi_0 outside (limit_low, limit_high) -> phi_0
   ST_NEAR = 4,       // a neighbour of phi_0 has the opposite sign: subcell distances in s_near
   ST_POSITIVE = 8,   // phi_0 > 0
+  ST_FROZEN = 16,    // batched runs: the node's field finished its iterations -> phi_n (set by launch_freeze32)
   ST_CUT_SHIFT = 8,  // bit (8 + dir): the neighbour in direction dir is across the interface
+};
+
+// Launch shape of the mixed stage kernels (chosen by the autotuner): grid of the persistent uniform
+// and regular kernels (0: one full wave at maximum occupancy) and threads per block of every stage kernel.
+struct StageCfg {
+  int uniform_blocks = 0;
+  int regular_blocks = 0;
+  int tpb = 256;
 };
 
 template <int D>
@@ -131,13 +140,15 @@ void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* 
 // fused stage: second derivatives of face nodes rebuilt from recorded second neighbours, or read from
 // ddx (D x N, written by launch_dd_x32 for the same phi on the extended set)
 template <int D>
-void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s);
+void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s, int tpb = 256);
+// Batched runs: nodes whose field stops at iteration `it` (lim[i] <= it, device order) are frozen.
+void launch_freeze32(const uint16_t* lim, int it, uint16_t* status, int64_t n, cudaStream_t s);
 // One RK stage of the mixed reinitialisation is split in three parts that write disjoint node ranges:
 // uniform regular nodes (no dependence on ddx), other regular nodes and irregular nodes (both read ddx).
 enum { STAGE_PART_UNIFORM = 0, STAGE_PART_REGULAR = 1, STAGE_PART_IRREGULAR = 2 };
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
-                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, int uniform_blocks);
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);

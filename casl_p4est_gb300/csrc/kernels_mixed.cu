@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
   float r;
   if (st & ST_ANCHORED) {
     r = 0.0f;
-  } else if (st & ST_OUTSIDE) {
+  } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
     r = phin[n];
   } else {
     const float f0 = __ldg(phin + n);
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
   float r;
   if (st & ST_ANCHORED) {
     r = 0.0f;
-  } else if (st & ST_OUTSIDE) {
+  } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
     r = phin[n];
   } else {
     const float f0 = __ldg(phin + n);
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     float r;
     if (st & ST_ANCHORED) {
       r = 0.0f;
-    } else if (st & ST_OUTSIDE) {
+    } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
       r = f0;
     } else {
       float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fn2[2 * D];
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uin
     float r;
     if (st & ST_ANCHORED) {
       r = 0.0f;
-    } else if (st & ST_OUTSIDE) {
+    } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
       r = f0;
     } else {
       const bool near = (st & ST_NEAR) != 0;
@@ -903,8 +903,18 @@ void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* 
 }
 
 template <int D>
-void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s) {
-  if (T.nI + T.nX) k_dd_x32<D><<<nblocks(T.nI + T.nX), TPB, 0, s>>>(T, f, ddx);
+void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s, int tpb) {
+  const int64_t n = T.nI + T.nX;
+  if (n) k_dd_x32<D><<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, s>>>(T, f, ddx);
+}
+
+__global__ void k_freeze32(const uint16_t* __restrict__ lim, int it, uint16_t* __restrict__ status, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && lim[i] <= it) status[i] |= ST_FROZEN;
+}
+
+void launch_freeze32(const uint16_t* lim, int it, uint16_t* status, int64_t n, cudaStream_t s) {
+  if (n) k_freeze32<<<nblocks(n), TPB, 0, s>>>(lim, it, status, n);
 }
 
 template <int D>
@@ -918,32 +928,38 @@ static int persistent_blocks(const void* kernel) {
 
 template <int D, int OS, bool AVG>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
-                         float* out, const float* avg_with, cudaStream_t s, int uniform_blocks) {
+                         float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg) {
   static int gb_reg = 0, gb_uni = 0;
   if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
   if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG>);
+  const int tpb = (cfg.tpb > 0 && cfg.tpb <= TPB) ? cfg.tpb : TPB;
+  // a persistent grid sized for TPB-thread blocks keeps the same thread count with smaller blocks
+  const int scale = TPB / tpb;
+  auto grid_of = [&](int64_t n) { return (unsigned)((n + tpb - 1) / tpb); };
   const int64_t uni_end = (OS > 1) ? T.nU : 0;  // the uniform kernel is second order in space only
   if (part == STAGE_PART_IRREGULAR && T.nI)
-    k_reinit_fused32<D, OS, AVG><<<nblocks(T.nI), TPB, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
-  if (part == STAGE_PART_REGULAR && T.nR > uni_end)
-    k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb_reg, nblocks(T.nR - uni_end)), TPB, 0, s>>>(
+    k_reinit_fused32<D, OS, AVG><<<grid_of(T.nI), tpb, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
+  if (part == STAGE_PART_REGULAR && T.nR > uni_end) {
+    const int gb = cfg.regular_blocks > 0 ? std::min(cfg.regular_blocks, gb_reg * scale) : gb_reg * scale;
+    k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(T.nR - uni_end)), tpb, 0, s>>>(
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
+  }
   if (part == STAGE_PART_UNIFORM && uni_end > 0) {
-    const int gb = uniform_blocks > 0 ? std::min(uniform_blocks, gb_uni) : gb_uni;
-    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb, nblocks(uni_end)), TPB, 0, s>>>(T, status, s_near, phin, out, avg_with);
+    const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, gb_uni * scale) : gb_uni * scale;
+    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(uni_end)), tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
   }
 }
 
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
-                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, int uniform_blocks) {
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg) {
   if (T.N == 0) return;
   if (order_space > 1) {
-    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
-    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
+    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
+    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
   } else {
-    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
-    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, uniform_blocks);
+    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
+    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
   }
 }
 
@@ -974,9 +990,9 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
                                          float*, const float*, cudaStream_t);                                                   \
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \
                                          const float*, cudaStream_t);                                                           \
-  template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                       \
+  template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t, int);                                  \
   template void launch_reinit_part32<D>(const DTab32<D>&, int, int, const uint16_t*, const float*, const float*, const float*,  \
-                                        float*, const float*, cudaStream_t, int);
+                                        float*, const float*, cudaStream_t, const StageCfg&);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

@@ -3,6 +3,8 @@
 
 #include <float.h>
 
+#include <algorithm>
+
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
@@ -73,15 +75,57 @@ void KernelTimer::reset() {
 template <int D>
 LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
   if (!forest.nodes_built) throw std::invalid_argument("level set: the forest's nodes are not built");
-  N = (int64_t)forest.num_nodes();
   double tdim[3];
   for (int a = 0; a < D; ++a) tdim[a] = (forest.brick.xyz_max[a] - forest.brick.xyz_min[a]) / forest.brick.n[a];
   zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
-  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  own_stream = true;
-  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) uniform_blocks = atoi(ub);
   Tables64<D> T;
   build_tables64<D>(forest, T);
+  double ts[3];
+  for (int a = 0; a < D; ++a) ts[a] = forest.brick.tmax[a] - forest.brick.tmin[a];
+  init_tables(T, ts, with_mixed);
+  part_offsets = {0, N};
+}
+
+template <int D>
+LevelSet<D>::LevelSet(const std::vector<const Forest<D>*>& parts) : F(nullptr) {
+  if (parts.empty()) throw std::invalid_argument("batch: no grids");
+  std::vector<Tables64<D>> T(parts.size());
+  std::vector<const Tables64<D>*> ptr(parts.size());
+  double ts[3] = {0, 0, 0}, tdim[3] = {0, 0, 0};
+  for (size_t k = 0; k < parts.size(); ++k) {
+    const Forest<D>& f = *parts[k];
+    if (!f.nodes_built) throw std::invalid_argument("batch: a forest's nodes are not built");
+    for (int a = 0; a < D; ++a) {
+      const double t = f.brick.tmax[a] - f.brick.tmin[a];
+      const double dim_a = (f.brick.xyz_max[a] - f.brick.xyz_min[a]) / f.brick.n[a];
+      if (k == 0) {
+        ts[a] = t;
+        tdim[a] = dim_a;
+      } else if (t != ts[a] || dim_a != tdim[a]) {
+        throw std::invalid_argument("batch: every grid must have the same tree size");
+      }
+    }
+  }
+  zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
+  part_offsets.assign(1, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long long k = 0; k < (long long)parts.size(); ++k) build_tables64<D>(*parts[(size_t)k], T[(size_t)k]);
+  for (size_t k = 0; k < parts.size(); ++k) {
+    ptr[k] = &T[k];
+    part_offsets.push_back(part_offsets.back() + T[k].N);
+  }
+  Tables64<D> U;
+  concat_tables64<D>(ptr, U);
+  T.clear();
+  init_tables(U, ts, true);
+}
+
+template <int D>
+void LevelSet<D>::init_tables(const Tables64<D>& T, const double* ts, bool with_mixed) {
+  N = T.N;
+  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  own_stream = true;
+  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) cfg.uniform_blocks = atoi(ub);
   num_corrections = (int64_t)(T.crec.size() / 6);
   nbr.upload(T.nbr, stream);
   w.upload(T.w, stream);
@@ -94,10 +138,8 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
   smin.upload(T.smin, stream);
   if (with_mixed) {
     Tables32<D> M;
-    double ts[3];
-    for (int a = 0; a < D; ++a) ts[a] = forest.brick.tmax[a] - forest.brick.tmin[a];
     build_tables32<D>(T, ts, M);
-    upload_mixed(M);
+    upload_mixed(M, ts);
   }
   cuda_check(cudaStreamSynchronize(stream), "table upload");
   T64.N = N;
@@ -114,6 +156,7 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
 template <int D>
 LevelSet<D>::~LevelSet() {
   if (stream) cudaStreamSynchronize(stream);
+  drop_graph();
   if (side_stream) {
     cudaStreamSynchronize(side_stream);
     cudaStreamDestroy(side_stream);
@@ -122,6 +165,7 @@ LevelSet<D>::~LevelSet() {
     cudaEventDestroy(ev_join);
   }
   if (own_stream && stream) cudaStreamDestroy(stream);
+  if (capture_stream) cudaStreamDestroy(capture_stream);
 }
 
 template <int D>
@@ -199,6 +243,7 @@ void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo,
 template <int D>
 void LevelSet<D>::build_mixed() {
   if (mixed_ready) return;
+  if (!F) throw std::invalid_argument("level set: mixed tables of a grid union are built at construction");
   // The FP32 tables derive from the FP64 ones; rebuild those on the host.
   Tables64<D> T;
   build_tables64<D>(*F, T);
@@ -206,11 +251,11 @@ void LevelSet<D>::build_mixed() {
   double ts[3];
   for (int a = 0; a < D; ++a) ts[a] = F->brick.tmax[a] - F->brick.tmin[a];
   build_tables32<D>(T, ts, M);
-  upload_mixed(M);
+  upload_mixed(M, ts);
 }
 
 template <int D>
-void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
+void LevelSet<D>::upload_mixed(const Tables32<D>& M, const double* ts) {
   r_meta.upload(M.r_meta, stream);
   r_nbr.upload(M.r_nbr, stream);
   r_nbr2.upload(M.r_nbr2, stream);
@@ -230,6 +275,7 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   i_q64.upload(M.i_q64, stream);
   corr64.upload(M.corr64, stream);
   perm.upload(M.perm, stream);
+  h_perm = M.perm;
   iperm.upload(M.iperm, stream);
   near_list.alloc((size_t)N);
   near_count.alloc(1);
@@ -240,7 +286,7 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   T32.nR = M.nR;
   T32.nI = M.nI;
   T32.base = M.base_level;
-  for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)(F->brick.tmax[a] - F->brick.tmin[a]) : 1.0f;
+  for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)ts[a] : 1.0f;
   for (int a = 0; a < 3; ++a) T32.inv_tsize[a] = 1.0f / T32.tsize[a];
   T32.nU = M.nU;
   T32.r_meta = r_meta.p;
@@ -258,7 +304,7 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
   T32.i_q = i_q.p;
   T32.i_cidx = i_cidx.p;
   T32.corr = corr32.p;
-  for (int a = 0; a < 3; ++a) T32.tsize64[a] = a < D ? F->brick.tmax[a] - F->brick.tmin[a] : 1.0;
+  for (int a = 0; a < 3; ++a) T32.tsize64[a] = a < D ? ts[a] : 1.0;
   T32.i_wf64 = i_wf64.p;
   T32.i_d64 = i_d64.p;
   T32.i_q64 = i_q64.p;
@@ -270,23 +316,27 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M) {
 // derivatives and then the irregular nodes while the main stream runs the uniform regular nodes;
 // the remaining regular nodes follow once the extended second derivatives are ready.
 template <int D>
+void LevelSet<D>::ensure_side_stream() {
+  if (side_stream) return;
+  cuda_check(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_ddx, cudaEventDisableTiming), "cudaEventCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+}
+
+template <int D>
 void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with) {
-  if (!side_stream) {
-    cuda_check(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
-    cuda_check(cudaEventCreateWithFlags(&ev_ddx, cudaEventDisableTiming), "cudaEventCreate");
-    cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
-  }
+  ensure_side_stream();
   timer.begin(K_STAGE32, stream);
   cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
   cuda_check(cudaStreamWaitEvent(side_stream, ev_fork, 0), "cudaStreamWaitEvent");
-  launch_dd_x32<D>(T32, phin, f_dd.p, side_stream);
+  launch_dd_x32<D>(T32, phin, f_dd.p, side_stream, cfg.tpb);
   cuda_check(cudaEventRecord(ev_ddx, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, 0);
+  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, cfg);
   cuda_check(cudaEventRecord(ev_join, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, uniform_blocks);
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg);
   cuda_check(cudaStreamWaitEvent(stream, ev_ddx, 0), "cudaStreamWaitEvent");
-  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, 0);
+  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg);
   cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
   timer.end(stream);
   timer.launches += 3;  // four kernels per stage
@@ -318,6 +368,189 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   }
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
+}
+
+template <int D>
+void LevelSet<D>::drop_graph() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  graph_exec = nullptr;
+  graph = nullptr;
+  graph_key.clear();
+}
+
+// The pseudo-time loop of the mixed path (os: order in space, second order in time); before
+// iteration `it` the nodes of every grid whose iteration count is `it` are frozen.
+template <int D>
+void LevelSet<D>::mixed_loop(int os, int iters, const std::vector<int>& freeze_at) {
+  for (int it = 0; it < iters; ++it) {
+    if (std::binary_search(freeze_at.begin(), freeze_at.end(), it)) {
+      timer.launches += 1;
+      launch_freeze32(iter_lim.p, it, status.p, N, stream);
+    }
+    mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
+    mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
+  }
+}
+
+// phi_0-only preparation of a batched call (reinitialize_2nd_order: limits +-DBL_MAX, second order).
+template <int D>
+void LevelSet<D>::prep_batch(const double* phi) {
+  build_mixed();
+  f_phi.alloc(N);
+  f_phi1.alloc(N);
+  f_dd.alloc((size_t)D * N);
+  f_snear.alloc((size_t)2 * D * N);
+  status.alloc(N);
+  phi0.alloc(N);
+  dd0.alloc((size_t)D * (nI > 0 ? nI : 1));
+  LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T32, perm.p, phi, zdt, -DBL_MAX, DBL_MAX, 2, phi0.p, dd0.p, status.p,
+                                                       f_snear.p, near_list.p, near_count.p, stream));
+  timer.launches += 3;
+  LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
+}
+
+template <int D>
+void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool use_graph) {
+  const size_t nparts = part_offsets.size() - 1;
+  std::vector<int> its(iterations, iterations + nparts);
+  int max_it = 0;
+  for (int v : its) {
+    if (v < 0 || v > 65535) throw std::invalid_argument("batch: iteration counts must lie in [0, 65535]");
+    max_it = std::max(max_it, v);
+  }
+  if (its != part_iters) {
+    std::vector<uint16_t> lim_node((size_t)N), lim((size_t)N);
+    for (size_t k = 0; k < nparts; ++k)
+      for (int64_t n = part_offsets[k]; n < part_offsets[k + 1]; ++n) lim_node[(size_t)n] = (uint16_t)its[k];
+    for (int64_t i = 0; i < N; ++i) lim[(size_t)i] = lim_node[(size_t)h_perm[(size_t)i]];
+    iter_lim.upload(lim, stream);
+    part_iters = its;
+  }
+  std::vector<int> freeze_at;
+  for (int v : its)
+    if (v < max_it) freeze_at.push_back(v);
+  std::sort(freeze_at.begin(), freeze_at.end());
+  freeze_at.erase(std::unique(freeze_at.begin(), freeze_at.end()), freeze_at.end());
+  prep_batch(phi);
+  if (use_graph) {
+    std::vector<int> key(1, max_it);
+    key.insert(key.end(), freeze_at.begin(), freeze_at.end());
+    if (!graph_exec || key != graph_key) {
+      drop_graph();
+      ensure_side_stream();
+      const bool timing = timer.enabled;
+      timer.enabled = false;
+      const int64_t before = timer.launches;
+      if (!capture_stream) cuda_check(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      // capture records work without running it, so it may use a stream of its own; the graph is
+      // then launched on the caller's stream
+      const cudaStream_t user = stream;
+      stream = capture_stream;
+      cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        try {
+          mixed_loop(2, max_it, freeze_at);
+        } catch (...) {
+          cudaGraph_t g = nullptr;
+          cudaStreamEndCapture(stream, &g);
+          if (g) cudaGraphDestroy(g);
+          stream = user;
+          timer.enabled = timing;
+          timer.launches = before;
+          throw;
+        }
+        e = cudaStreamEndCapture(stream, &graph);
+      }
+      stream = user;
+      timer.enabled = timing;
+      timer.launches = before;
+      cuda_check(e, "graph capture");
+      cuda_check(cudaGraphInstantiate(&graph_exec, graph, 0), "cudaGraphInstantiate");
+      size_t nodes = 0;
+      cuda_check(cudaGraphGetNodes(graph, nullptr, &nodes), "cudaGraphGetNodes");
+      graph_launches = (int64_t)(4 * 2 * (int64_t)max_it + (int64_t)freeze_at.size());
+      graph_key = key;
+    }
+    timer.begin(K_STAGE32, stream);
+    cuda_check(cudaGraphLaunch(graph_exec, stream), "cudaGraphLaunch");
+    timer.end(stream);
+    timer.launches += graph_launches - 1;
+  } else {
+    mixed_loop(2, max_it, freeze_at);
+  }
+  LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
+  cuda_check(cudaGetLastError(), "reinitialize (batch)");
+}
+
+// Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, grid of
+// the persistent uniform and regular kernels), timing `trials` iterations per candidate with CUDA
+// events on the object's stream.
+template <int D>
+void LevelSet<D>::autotune(const double* phi, int trials) {
+  if (trials < 1) trials = 1;
+  prep_batch(phi);
+  ensure_side_stream();
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+  int sms = 152, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const bool timing = timer.enabled;
+  timer.enabled = false;
+  auto run = [&](const StageCfg& c) -> float {
+    cfg = c;
+    mixed_stage(2, f_phi.p, f_phi1.p, nullptr);  // warm-up
+    mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
+    cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
+    for (int t = 0; t < trials; ++t) {
+      mixed_stage(2, f_phi.p, f_phi1.p, nullptr);
+      mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
+    }
+    cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0;
+    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    return ms;
+  };
+  StageCfg best;
+  float best_ms = 1e30f;
+  const int grids[] = {0, 2, 3, 4, 6};
+  for (int tpb : {256, 128}) {
+    StageCfg c;
+    c.tpb = tpb;
+    float c_ms = 1e30f;
+    for (int g : grids) {
+      StageCfg t = c;
+      t.uniform_blocks = g * sms * (256 / tpb);
+      const float ms = run(t);
+      if (ms < c_ms) {
+        c_ms = ms;
+        c.uniform_blocks = t.uniform_blocks;
+      }
+    }
+    for (int g : grids) {
+      if (g == 6) continue;
+      StageCfg t = c;
+      t.regular_blocks = g * sms * (256 / tpb);
+      const float ms = run(t);
+      if (ms < c_ms) {
+        c_ms = ms;
+        c.regular_blocks = t.regular_blocks;
+      }
+    }
+    if (c_ms < best_ms) {
+      best_ms = c_ms;
+      best = c;
+    }
+  }
+  cfg = best;
+  timer.enabled = timing;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  drop_graph();  // launch shapes are baked into a captured graph
+  cuda_check(cudaGetLastError(), "autotune");
 }
 
 // advect_in_normal_direction (src/my_p4est_level_set.cpp:656-725).
@@ -396,6 +629,7 @@ void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, doub
 template <int D>
 void LevelSet<D>::build_locator() {
   if (loc_ready) return;
+  if (!F) throw std::invalid_argument("interpolation needs a single grid's level set, not a batch");
   using DD = Dim<D>;
   const Forest<D>& f = *F;
   const int64_t nl = (int64_t)f.leaves.size();

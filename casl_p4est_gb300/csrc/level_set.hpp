@@ -52,7 +52,7 @@ struct LevelSet {
   KernelTimer timer;
   cudaStream_t side_stream = nullptr;  // second stream of the mixed stage (fork/join with events)
   cudaEvent_t ev_fork = nullptr, ev_ddx = nullptr, ev_join = nullptr;
-  int uniform_blocks = 0;              // grid cap of the uniform kernel (0: full occupancy)
+  StageCfg cfg;                        // launch shape of the mixed stage kernels (see autotune)
   int64_t num_corrections = 0;
 
   // FP64 tables
@@ -82,7 +82,21 @@ struct LevelSet {
   DevBuf<uint16_t> status;
   DevBuf<float> f_phi0, f_phi, f_phi1, f_dd, f_ddm, f_snear, f_vn;
 
+  // batched runs over the disjoint union of several grids (constructed from their tables)
+  std::vector<int64_t> part_offsets;   // node offset of each grid (+ total)
+  DevBuf<uint16_t> iter_lim;           // device order: iteration count of the node's grid
+  std::vector<int> part_iters;         // iteration count of each grid (last batched call)
+  cudaStream_t capture_stream = nullptr;  // graphs are captured here (the caller's stream may be the legacy default stream)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<int> graph_key;          // iteration counts the captured graph was built for
+  int64_t graph_launches = 0;          // kernels in the captured graph
+  std::vector<int32_t> h_perm;         // device index -> node (host copy of the mixed tables' perm)
+
   explicit LevelSet(const Forest<D>& forest, bool with_mixed = true);
+  // level set over the disjoint union of grids with equal tree sizes: tables concatenated in node
+  // order (parts[k] occupies nodes part_offsets[k] .. part_offsets[k+1]-1)
+  LevelSet(const std::vector<const Forest<D>*>& parts);
   ~LevelSet();
   void set_stream(cudaStream_t s);
 
@@ -116,6 +130,14 @@ struct LevelSet {
   void sl_advect_vortex(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd, int phi_method,
                         double* phi_np1);
 
+  // Batched reinitialize_2nd_order (mixed precision) of every grid of a union with its own iteration
+  // count: phi on the device in union node order. With use_graph the iteration loop runs as one CUDA
+  // graph (captured on the first call with these iteration counts, replayed afterwards).
+  void reinitialize_batch(double* phi, const int* iterations, bool use_graph);
+  // Times candidate launch shapes of the mixed stage on phi (device, node order) and keeps the fastest.
+  void autotune(const double* phi, int trials);
+  void drop_graph();  // forget a captured graph (after a launch-shape change)
+
   // host-buffer conveniences (copies inside)
   void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision);
   void interpolate_host(const double* xyz, int64_t np, int nf, const double* F, const double* Fdd, int method, double* out);
@@ -125,8 +147,12 @@ struct LevelSet {
                              int phi_method, double* phi_np1);
 
  private:
+  void init_tables(const Tables64<D>& T, const double* tree_size, bool with_mixed);
+  void mixed_loop(int os, int iters, const std::vector<int>& freeze_at);
+  void ensure_side_stream();
+  void prep_batch(const double* phi);
   void build_mixed();
-  void upload_mixed(const Tables32<D>& M);
+  void upload_mixed(const Tables32<D>& M, const double* tree_size);
   void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);

@@ -91,6 +91,58 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T) {
   }
 }
 
+template <int D>
+void concat_tables64(const std::vector<const Tables64<D>*>& parts, Tables64<D>& out) {
+  constexpr int H = Dim<D>::HALF;
+  constexpr int NS = 2 * D * H;
+  int64_t N = 0;
+  size_t R = 0;
+  for (const auto* t : parts) {
+    N += t->N;
+    R += t->crec.size() / 6;
+  }
+  out.N = N;
+  out.nbr.resize((size_t)NS * N);
+  out.w.resize((size_t)NS * N);
+  out.nrm.resize((size_t)2 * D * N);
+  out.d.resize((size_t)2 * D * N);
+  out.q.resize((size_t)2 * D * (D - 1) * N);
+  out.cidx.resize((size_t)N);
+  out.crec.clear();
+  out.crec.reserve(6 * R);
+  out.wall.resize((size_t)N);
+  out.smin.resize((size_t)N);
+  int64_t off = 0;
+  int32_t roff = 0;
+  for (const auto* t : parts) {
+    const int64_t n = t->N;
+    for (int sl = 0; sl < NS; ++sl)
+      for (int64_t i = 0; i < n; ++i) {
+        const int32_t j = t->nbr[(size_t)sl * n + i];
+        out.nbr[(size_t)sl * N + off + i] = j >= 0 ? (int32_t)(j + off) : j;
+        out.w[(size_t)sl * N + off + i] = t->w[(size_t)sl * n + i];
+      }
+    for (int dir = 0; dir < 2 * D; ++dir)
+      for (int64_t i = 0; i < n; ++i) {
+        out.nrm[(size_t)dir * N + off + i] = t->nrm[(size_t)dir * n + i];
+        out.d[(size_t)dir * N + off + i] = t->d[(size_t)dir * n + i];
+      }
+    for (int sl = 0; sl < 2 * D * (D - 1); ++sl)
+      for (int64_t i = 0; i < n; ++i) out.q[(size_t)sl * N + off + i] = t->q[(size_t)sl * n + i];
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t c = t->cidx[(size_t)i];
+      out.cidx[(size_t)(off + i)] = c >= 0 ? c + roff : c;
+      out.wall[(size_t)(off + i)] = t->wall[(size_t)i];
+      out.smin[(size_t)(off + i)] = t->smin[(size_t)i];
+    }
+    out.crec.insert(out.crec.end(), t->crec.begin(), t->crec.end());
+    off += n;
+    roff += (int32_t)(t->crec.size() / 6);
+  }
+}
+
+template void concat_tables64<2>(const std::vector<const Tables64<2>*>&, Tables64<2>&);
+template void concat_tables64<3>(const std::vector<const Tables64<3>*>&, Tables64<3>&);
 template void build_tables64<2>(const Forest<2>&, Tables64<2>&);
 template void build_tables64<3>(const Forest<3>&, Tables64<3>&);
 

@@ -51,6 +51,11 @@ struct Tables64 {
 template <int D>
 void build_tables64(const Forest<D>& F, Tables64<D>& T);
 
+// Tables of the disjoint union of several grids: node indices of part k are offset by the node count
+// of the parts before it (the union's node order is the parts' node orders one after the other).
+template <int D>
+void concat_tables64(const std::vector<const Tables64<D>*>& parts, Tables64<D>& out);
+
 template <int D>
 struct Tables32 {
   int64_t N = 0, nR = 0, nI = 0;

@@ -165,6 +165,102 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_second_derivatives(self._h, L.dptr(phi), L.dptr(out)))
         return out
 
+    # ---- launch shape of the mixed stage -----------------------------------------------------------
+    def autotune(self, phi, trials=3):
+        """Time candidate launch shapes of the mixed stage on phi (host) and keep the fastest."""
+        return _autotune(self._h, phi, trials)
+
+    @property
+    def stage_config(self):
+        return _stage_config(self._h)
+
+    @stage_config.setter
+    def stage_config(self, cfg):
+        _set_stage_config(self._h, cfg)
+
     def perturb_level_set_function(self, phi, epsilon):
         _host_f64(phi, self.num_nodes, "phi")
         L.check(L.load().lsg_perturb_level_set_function(self._h, L.dptr(phi), float(epsilon)))
+
+
+def _autotune(handle, phi, trials):
+    phi = np.ascontiguousarray(phi, np.float64)
+    cfg = np.zeros(3, np.int32)
+    L.check(L.load().lsg_level_set_autotune(handle, L.dptr(phi), int(trials), L.i32ptr(cfg)))
+    return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2])}
+
+
+def _stage_config(handle):
+    cfg = np.zeros(3, np.int32)
+    L.check(L.load().lsg_level_set_stage_config(handle, L.i32ptr(cfg)))
+    return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2])}
+
+
+def _set_stage_config(handle, cfg):
+    arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"]], np.int32)
+    L.check(L.load().lsg_level_set_set_stage_config(handle, L.i32ptr(arr)))
+
+
+class my_p4est_level_set_batch_t:
+    """Many level-set fields on separate grids (same dimension and tree size) reinitialised together.
+
+    The grids' tables are concatenated on the device; reinitialize_2nd_order runs every stage kernel
+    once over all grids, grid k for its own iteration count, the loop captured as a CUDA graph."""
+
+    def __init__(self, forests):
+        self.forests = list(forests)  # kept alive: the batch borrows them
+        arr = (C.c_void_p * len(self.forests))(*[f.handle.value for f in self.forests])
+        h = C.c_void_p()
+        L.check(L.load().lsg_batch_create(len(self.forests), C.cast(arr, C.POINTER(C.c_void_p)), C.byref(h)))
+        self._h = h
+        self.count = int(L.load().lsg_batch_count(h))
+        off = np.zeros(self.count + 1, np.int64)
+        L.check(L.load().lsg_batch_offsets(h, off.ctypes.data_as(C.POINTER(C.c_int64))))
+        self.offsets = off
+        self.num_nodes = int(off[-1])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                L.load().lsg_level_set_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        L.check(L.load().lsg_level_set_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def split(self, phi):
+        return [phi[self.offsets[k]:self.offsets[k + 1]] for k in range(self.count)]
+
+    def concat(self, phis):
+        return np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64) for p in phis]))
+
+    def reinitialize_2nd_order(self, phi, number_of_iterations=50, use_graph=True):
+        """phi: concatenated float64 host array (updated in place) or CUDA tensor; number_of_iterations:
+        one count for all grids or one per grid."""
+        its = np.full(self.count, number_of_iterations, np.int32) if np.isscalar(number_of_iterations) else \
+            np.ascontiguousarray(number_of_iterations, np.int32)
+        if its.size != self.count:
+            raise ValueError("one iteration count per grid is required")
+        if _is_device(phi):
+            L.check(L.load().lsg_batch_reinitialize_device(self._h, C.c_void_p(phi.data_ptr()), L.i32ptr(its), int(use_graph)))
+            return
+        _host_f64(phi, self.num_nodes, "phi")
+        L.check(L.load().lsg_batch_reinitialize(self._h, L.dptr(phi), L.i32ptr(its), int(use_graph)))
+
+    def autotune(self, phi, trials=3):
+        return _autotune(self._h, phi, trials)
+
+    @property
+    def stage_config(self):
+        return _stage_config(self._h)
+
+    @stage_config.setter
+    def stage_config(self, cfg):
+        _set_stage_config(self._h, cfg)

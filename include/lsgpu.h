@@ -196,6 +196,31 @@ int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz_np
                                          const double* params, int nparams, const double* phi_n_dev, const double* phi_dd_dev,
                                          int phi_method, double* phi_np1_dev);
 
+/* ---- batched reinitialisation (mixed precision) --------------------------------------------- */
+
+/* No single counterpart in the reference, which reinitialises each field with its own
+ * my_p4est_level_set_t::reinitialize_2nd_order(phi_k, iterations_k) call (src/my_p4est_level_set.h:468-472).
+ * A batch is a level set over the disjoint union of `count` grids of one dimension and equal tree
+ * sizes: their tables are concatenated (grid k owns union nodes offsets[k] .. offsets[k+1]-1, in its
+ * own node order) so every stage kernel covers all grids in one launch. The returned handle is a
+ * level-set handle, destroyed with lsg_level_set_destroy; the forests must outlive it. */
+int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set** out);
+int lsg_batch_count(const lsg_level_set* batch);
+int lsg_batch_offsets(const lsg_level_set* batch, int64_t* offsets); /* count + 1 values */
+/* reinitialize_2nd_order of every grid, grid k for iterations[k] pseudo-time iterations (mixed
+ * precision, limits +-DBL_MAX): phi holds all grids' values in union node order. use_graph: run the
+ * iteration loop as one CUDA graph, captured on the first call with these iteration counts and
+ * replayed afterwards (make that first call outside any stream capture). */
+int lsg_batch_reinitialize(lsg_level_set* batch, double* phi, const int* iterations, int use_graph);
+int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const int* iterations, int use_graph);
+/* Launch shape of the mixed stage kernels: config[0] threads per block (32..256), config[1] grid of
+ * the persistent uniform-stencil kernel, config[2] grid of the persistent regular kernel (0: one full
+ * wave). lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials`
+ * iterations each, keeps the fastest and returns it in config (may be NULL). */
+int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int* config);
+int lsg_level_set_stage_config(const lsg_level_set* ls, int* config);
+int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config);
+
 /* kernel classes reported by lsg_level_set_kernel_times */
 enum {
   LSG_K_DD64 = 0, LSG_K_PREP64, LSG_K_STAGE64, LSG_K_ADVECT64, LSG_K_DD32, LSG_K_PREP_MIXED, LSG_K_STAGE32, LSG_K_ADVECT32,
