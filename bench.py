@@ -44,11 +44,12 @@ def parse():
     p.add_argument("--iters", type=int, default=ITERS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--fp64-steps", type=int, default=2)
-    p.add_argument("--workload", default="reinit3d", choices=["reinit3d", "transport3d", "batch2d"],
+    p.add_argument("--workload", default="reinit3d", choices=["reinit3d", "transport3d", "batch2d", "large3d"],
                    help="reinit3d: the headline reinitialisation line; transport3d: the level-set transport run "
                         "(semi-Lagrangian step + host regrid + 5 reinitialisation iterations per step; --steps time steps); "
                         "batch2d: 256 quadtrees reinitialised together (--steps timed batch calls)")
     p.add_argument("--batch", type=int, default=256, help="batch2d: number of quadtrees")
+    p.add_argument("--large-levels", type=int, nargs=2, default=[6, 11], help="large3d: min and max level")
     return p.parse_args()
 
 
@@ -403,6 +404,113 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_large(args):
+    """Large 3D: octree on [-1,1]^3 around 64 random spheres (centres U[-0.8,0.8]^3, radii U[0.05,0.15],
+    seed 5), refined where |d| <= 1.2 diag; phi0 = min signed distance x (0.1 + |x - c0|^2);
+    reinitialize_2nd_order 50 iterations and advect_in_normal_direction with vn = 1 for 20 steps,
+    mixed and FP64, on one GPU."""
+    import torch
+    import casl_p4est_gb300 as G
+    from casl_p4est_gb300 import shapes
+    torch.cuda.set_device(0)
+    lmin, lmax = args.large_levels
+    rng = np.random.default_rng(5)
+    centres = rng.uniform(-0.8, 0.8, (64, 3))
+    radii = rng.uniform(0.05, 0.15, 64)
+    t0 = time.perf_counter()
+    f = G.my_p4est_brick_new([1, 1, 1], [-1, -1, -1], [1, 1, 1])
+    f.refine_levelset(shapes.spheres(centres, radii), lmin, lmax, lip=LIP)
+    f.build_nodes()
+    t_grid = time.perf_counter() - t0
+    phi0 = f.sample(shapes.spheres(centres, radii, scale=(0.1, centres[0])))
+    N = f.num_nodes
+    t0 = time.perf_counter()
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
+    t_tables = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    ls.set_stream(stream.cuda_stream)
+    _, dmin, _ = f.dxyz_min(lmax)
+    cfg = ls.autotune(phi0, trials=2)
+    phi0_d = torch.from_numpy(phi0).cuda()
+    del phi0
+    phi_d = torch.empty_like(phi0_d)
+    iters = 50
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(steps):
+            phi_d.copy_(phi0_d)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / steps
+
+    reinit = lambda prec: ls.reinitialize_2nd_order(phi_d, iters, precision=prec)
+    phi_d.copy_(phi0_d)
+    reinit("mixed")  # warm-up
+    ms_mixed = timed(lambda: reinit("mixed"), args.steps)
+    mixed_d = phi_d.clone()
+    ms_fp64 = timed(lambda: reinit("fp64"), 1)
+    band_err, band_nodes = ls.band_linf(mixed_d, phi_d, 3 * dmin)
+    iface_err, _ = ls.band_linf(mixed_d, phi_d, dmin)
+    del mixed_d
+    # normal advection, vn = 1, 20 steps from the reinitialised field
+    vn = torch.ones_like(phi0_d)
+    dt = 0.8 * dmin  # CFL 0.8 on the finest cells (vn = 1)
+    adv_ms = {}
+    adv_out = {}
+    for prec in ("mixed", "fp64"):
+        start = phi_d.clone()
+
+        def adv():
+            for _ in range(20):
+                ls.advect_in_normal_direction(vn, phi_d, dt, precision=prec)
+
+        phi_d.copy_(start)
+        adv()  # warm-up
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        phi_d.copy_(start)
+        e0.record(stream)
+        adv()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        adv_ms[prec] = e0.elapsed_time(e1)
+        adv_out[prec] = phi_d.clone()
+        phi_d.copy_(start)
+    adv_err, _ = ls.band_linf(adv_out["mixed"], adv_out["fp64"], 3 * dmin)
+    peak, peak_kind = measured_peak()
+    value = N * iters / (ms_mixed / 1e3)
+    gbs = 284 * value / 1e9
+    out = {
+        "metric": "large-grid reinit node-iters/s on 1 GB300 (mixed vs FP64) + normal advection", "value": value,
+        "unit": "node-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": ms_mixed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"3D octree [-1,1]^3 levels {lmin}-{lmax} (lip 2.4) around 64 random spheres, {N} nodes, "
+                               f"reinitialize_2nd_order {iters} iterations + advect_in_normal_direction vn=1 x 20",
+                   "nodes": N, "leaves": f.num_leaves, "l2": "working set > L2 (no flush needed)"},
+        "fp64": {"ms_per_step": ms_fp64, "value": N * iters / (ms_fp64 / 1e3)},
+        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
+        "band_nodes": band_nodes, "dx_min": dmin,
+        "roofline_per_iteration": {"alg_bytes_per_node_iter": 284, "achieved_GBps": gbs, "peak": peak, "frac": gbs / peak,
+                                   "peak_source": peak_kind},
+        "advect_20_steps": {"mixed_ms": adv_ms["mixed"], "fp64_ms": adv_ms["fp64"],
+                            "mixed_node_steps_per_s": N * 20 / (adv_ms["mixed"] / 1e3),
+                            "fp64_node_steps_per_s": N * 20 / (adv_ms["fp64"] / 1e3),
+                            "band_linf_mixed_vs_fp64": adv_err, "dt": dt},
+        "autotuned_stage_config": cfg, "setup_s": {"grid": t_grid, "tables": t_tables},
+        "device_memory_used_gb": (lambda fr: (fr[1] - fr[0]) / 1e9)(torch.cuda.mem_get_info()),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -417,6 +525,10 @@ def main():
     if args.workload == "batch2d":
         if rank == 0:
             run_batch(args)
+        return
+    if args.workload == "large3d":
+        if rank == 0:
+            run_large(args)
         return
 
     import torch
@@ -442,6 +554,7 @@ def main():
     ls = G.my_p4est_level_set_t(ngbd, precision="mixed")
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
+    stage_cfg = ls.autotune(phi0, trials=3)
     setup_s = time.perf_counter() - t0
     _, dmin, _ = f.dxyz_min(args.levels[1])
 
@@ -452,15 +565,14 @@ def main():
         phi_d.copy_(phi0_d)
         ls.reinitialize_2nd_order(phi_d, args.iters, precision=prec)
 
-    # accuracy of mixed vs FP64 (untimed): band L-infinity and near-interface error
+    # accuracy of mixed vs FP64 (untimed): band L-infinity and near-interface error, checked in FP64
+    # on the device
     step("fp64")
-    ref64 = phi_d.cpu().numpy().copy()
+    ref64_d = phi_d.clone()
     step("mixed")
-    mixed = phi_d.cpu().numpy().copy()
-    band = np.abs(ref64) < 3 * dmin
-    band_err = float(np.max(np.abs(mixed[band] - ref64[band])))
-    near = np.abs(ref64) < dmin
-    iface_err = float(np.max(np.abs(mixed[near] - ref64[near])))
+    band_err, band_nodes = ls.band_linf(phi_d, ref64_d, 3 * dmin)
+    iface_err, _ = ls.band_linf(phi_d, ref64_d, dmin)
+    del ref64_d
 
     # warm-up and timed region (mixed)
     for _ in range(args.warmup):
@@ -574,9 +686,11 @@ def main():
             "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
             "speedup_mixed_vs_fp64": value / value64,
             "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
+            "band_nodes": band_nodes,
             "dx_min": dmin,
             "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
             "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
+            "autotuned_stage_config": stage_cfg,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -74,6 +74,7 @@ SIGNATURES = {
     "lsg_semi_lagrangian_advect_device": (_I, [_P, _P, _I64, _D, _P, _P, _P, _P, _I, _I, _P]),
     "lsg_semi_lagrangian_advect_cf": (_I, [_P, _DP, _I64, _D, _I, _DP, _I, _DP, _DP, _I, _DP]),
     "lsg_semi_lagrangian_advect_cf_device": (_I, [_P, _P, _I64, _D, _I, _DP, _I, _P, _P, _I, _P]),
+    "lsg_band_linf_device": (_I, [_P, _P, _P, _D, _DP, C.POINTER(_I64)]),
     "lsg_batch_create": (_I, [_I, C.POINTER(_P), C.POINTER(_P)]),
     "lsg_batch_count": (_I, [_P]),
     "lsg_batch_offsets": (_I, [_P, C.POINTER(_I64)]),

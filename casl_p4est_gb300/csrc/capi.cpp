@@ -726,6 +726,14 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
   });
 }
 
+int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double band, double* out, int64_t* count) {
+  return guard([&] {
+    need(a_dev != nullptr && b_dev != nullptr && out != nullptr, "null argument");
+    need(band > 0, "band must be positive");
+    with_ls(ls, [&](auto& L) { *out = L.band_linf(a_dev, b_dev, band, count); });
+  });
+}
+
 int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on) {
   return guard([&] { with_ls(ls, [&](auto& L) { L.timer.enabled = on != 0; }); });
 }

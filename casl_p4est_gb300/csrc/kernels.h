@@ -104,6 +104,8 @@ void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double*
                            double* out, const double* avg_with, cudaStream_t s);
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
 void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
+// FP64 band L-infinity: out3 = {bits of max |a-b| over |b| < band, band node count, NaN flag}
+void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s);
 // Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p
 // is first moved to xyz[p] - coef*shift[:, p] and clipped into the domain (the semi-Lagrangian
 // backtrace). F: nf x N values, Fdd: nf x D x N second derivatives (ignored for linear), out: nf x np.

@@ -10,6 +10,8 @@
 //   interface_Location[_With_Second_Order_Derivative]  src/casl_math.cpp:55-97
 //   advect_in_normal_direction_one_iteration   src/my_p4est_level_set.cpp:559-654
 //   CFL of the CF overload                     src/my_p4est_level_set.cpp:745-783
+#include <algorithm>
+
 #include "kernels.h"
 #include "stencil64.cuh"
 #include "tables.hpp"
@@ -255,9 +257,69 @@ __global__ void k_min_cfl(const double* __restrict__ smin, const double* __restr
   if ((threadIdx.x & 31) == 0) atomicMin(out, (unsigned long long)__double_as_longlong(v));
 }
 
+// Band L-infinity check in FP64: max |a - b| over the nodes with |b| < band (b the reference field),
+// with the number of band nodes and a NaN flag. Warp shuffles, then one shared-memory pass per block,
+// then one atomic per block; non-negative doubles order like their bit patterns, so atomicMax on the
+// bits is exact and the result does not depend on the reduction order.
+__global__ void __launch_bounds__(TPB) k_band_linf64(const double* __restrict__ a, const double* __restrict__ b, double band, int64_t n,
+                                                     unsigned long long* __restrict__ out) {
+  __shared__ double s_max[TPB / 32];
+  __shared__ unsigned long long s_cnt[TPB / 32];
+  __shared__ int s_nan[TPB / 32];
+  double m = 0.0;
+  unsigned long long cnt = 0;
+  int nan = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double r = b[i];
+    if (fabs(r) < band) {
+      const double e = fabs(a[i] - r);
+      if (e != e) nan = 1;
+      else m = fmax(m, e);
+      ++cnt;
+    } else if (r != r) {
+      nan = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    nan |= __shfl_xor_sync(0xffffffffu, nan, o);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    s_max[w] = m;
+    s_cnt[w] = cnt;
+    s_nan[w] = nan;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    m = lane < nw ? s_max[lane] : 0.0;
+    cnt = lane < nw ? s_cnt[lane] : 0ull;
+    nan = lane < nw ? s_nan[lane] : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      nan |= __shfl_xor_sync(0xffffffffu, nan, o);
+    }
+    if (lane == 0) {
+      atomicMax(out, (unsigned long long)__double_as_longlong(m));
+      atomicAdd(out + 1, cnt);
+      if (nan) atomicOr(out + 2, 1ull);
+    }
+  }
+}
+
 inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 
 }  // namespace
+
+void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
+  cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
+  if (n == 0) return;
+  const unsigned g = std::min<unsigned>(nblocks(n), 152u * 8u);
+  k_band_linf64<<<g, TPB, 0, s>>>(a, b, band, n, out3);
+}
 
 template <int D>
 void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s) {

@@ -616,6 +616,20 @@ double LevelSet<D>::cfl_dt(const double* vn) {
 }
 
 template <int D>
+double LevelSet<D>::band_linf(const double* a, const double* b, double band, int64_t* count) {
+  linf_buf.ensure(3);
+  LSG_LAUNCH(K_CONVERT, launch_band_linf64(a, b, band, N, linf_buf.p, stream));
+  unsigned long long h[3] = {0, 0, 0};
+  cuda_check(cudaMemcpyAsync(h, linf_buf.p, sizeof(h), cudaMemcpyDeviceToHost, stream), "band check");
+  cuda_check(cudaStreamSynchronize(stream), "band check sync");
+  if (count) *count = (int64_t)h[1];
+  if (h[2]) return NAN;
+  double v;
+  memcpy(&v, &h[0], sizeof(v));
+  return v;
+}
+
+template <int D>
 void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision) {
   ws_phi.alloc(N);
   cuda_check(cudaMemcpyAsync(ws_phi.p, phi, N * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D phi");

@@ -79,6 +79,7 @@ struct LevelSet {
   // work vectors
   DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
   DevBuf<double> ws_xyz, ws_f, ws_fdd, ws_out, ws_v1, ws_v2, ws_fdd2;
+  DevBuf<unsigned long long> linf_buf;
   DevBuf<uint16_t> status;
   DevBuf<float> f_phi0, f_phi, f_phi1, f_dd, f_ddm, f_snear, f_vn;
 
@@ -110,6 +111,9 @@ struct LevelSet {
   void second_derivatives(const double* f, double* dd);
   // dt of the CF overload: min over nodes of 0.8*|s_min/vn| (src/my_p4est_level_set.cpp:752-776).
   double cfl_dt(const double* vn);
+  // FP64 band check: max |a - b| over the nodes with |b| < band (device pointers, N values each);
+  // NaN if a NaN was met; count: nodes in the band.
+  double band_linf(const double* a, const double* b, double band, int64_t* count);
 
   // reinitialize() in FP64 with no allocation: the work vectors come from a static device array
   // (reinit_fp64_static) that holds grids up to LSG_NOALLOC_SCRATCH_BYTES of scratch.

@@ -165,6 +165,16 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_second_derivatives(self._h, L.dptr(phi), L.dptr(out)))
         return out
 
+    def band_linf(self, a, b, band):
+        """FP64 max |a - b| over |b| < band on the device (CUDA tensors); returns (value, band node count)."""
+        if not (_is_device(a) and _is_device(b)):
+            raise TypeError("band_linf takes CUDA tensors")
+        out = C.c_double()
+        cnt = C.c_int64()
+        L.check(L.load().lsg_band_linf_device(self._h, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), float(band),
+                                              C.byref(out), C.byref(cnt)))
+        return out.value, cnt.value
+
     # ---- launch shape of the mixed stage -----------------------------------------------------------
     def autotune(self, phi, trials=3):
         """Time candidate launch shapes of the mixed stage on phi (host) and keep the fastest."""

@@ -196,6 +196,13 @@ int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz_np
                                          const double* params, int nparams, const double* phi_n_dev, const double* phi_dd_dev,
                                          int phi_method, double* phi_np1_dev);
 
+/* The band check that accompanies every result: max |a - b| over the nodes with |b| < band, in FP64
+ * on the device (warp-shuffle reduction), b the reference field (e.g. the FP64 result), a the field
+ * checked; *out is NaN if a NaN was met, *count (may be NULL) the number of nodes in the band. Device
+ * pointers of N values; no counterpart in the reference, whose examples compute the same norm on the
+ * host (examples/reinitialization/main_2d.cpp:254-262). */
+int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double band, double* out, int64_t* count);
+
 /* ---- batched reinitialisation (mixed precision) --------------------------------------------- */
 
 /* No single counterpart in the reference, which reinitialises each field with its own

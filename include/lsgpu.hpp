@@ -1,0 +1,348 @@
+/*
+ * lsgpu.hpp: C++ facade over the C ABI (lsgpu.h) with parCASL's class names and method signatures,
+ * so C++ code written against my_p4est_level_set_t, my_p4est_interpolation_nodes_t and
+ * my_p4est_semi_lagrangian_t keeps its calls:
+ *
+ *   my_p4est_level_set_t(my_p4est_node_neighbors_t*)                  src/my_p4est_level_set.h:385-414
+ *   reinitialize_{1st,2nd}_order[_above_threshold|_time_...](Vec phi, iterations, limit)
+ *                                                                      src/my_p4est_level_set.h:434-613
+ *   perturb_level_set_function(Vec phi, epsilon)                       src/my_p4est_level_set.h:621
+ *   advect_in_normal_direction(CF / Vec vn[, Vec vn_np1], Vec phi, dt, phi_xx, phi_yy[, phi_zz])
+ *                                                                      src/my_p4est_level_set.h:632-659
+ *   my_p4est_interpolation_nodes_t: set_input, add_point, interpolate  src/my_p4est_interpolation_nodes.h:33-103
+ *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1                   src/my_p4est_semi_lagrangian.h:83-196
+ *
+ * Vec: with LSGPU_WITH_PETSC defined before inclusion, PETSc's Vec (read through VecGetArray);
+ * otherwise a minimal host vector with the same accessor names (VecGetArray / VecRestoreArray /
+ * VecGetLocalSize). Node values are in lsgpu's node order (the order my_p4est_nodes_new gives in a
+ * single process). Status codes become exceptions: LSG_EINVAL -> std::invalid_argument, anything
+ * else -> std::runtime_error, carrying lsg_last_error().
+ *
+ * The grid side (my_p4est_brick_new, refinement, my_p4est_nodes_new, init_neighbors) is the
+ * forest of lsgpu.h; my_p4est_node_neighbors_t here owns the device image of the node neighbours
+ * (built on first use) that every object of one grid shares.
+ */
+#ifndef LSGPU_HPP
+#define LSGPU_HPP
+
+#include <float.h>
+
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "lsgpu.h"
+
+#ifdef LSGPU_WITH_PETSC
+#include <petscvec.h>
+#else
+struct lsgpu_vec {
+  std::vector<double> values;
+};
+typedef lsgpu_vec* Vec;
+inline int VecGetArray(Vec x, double** a) {
+  *a = x->values.data();
+  return 0;
+}
+inline int VecRestoreArray(Vec, double** a) {
+  *a = nullptr;
+  return 0;
+}
+inline int VecGetLocalSize(Vec x, int* n) {
+  *n = (int)x->values.size();
+  return 0;
+}
+#endif
+
+namespace lsgpu {
+
+inline void check(int status) {
+  if (status == LSG_OK) return;
+  const std::string msg = std::string("lsgpu: ") + lsg_last_error();
+  if (status == LSG_EINVAL) throw std::invalid_argument(msg);
+  throw std::runtime_error(msg);
+}
+
+// Evaluate a function object of the node coordinates: (x, y) in 2D, (x, y, z) in 3D (C++17).
+template <typename CF>
+double eval_cf(const CF& f, const double* x, int dim) {
+  if constexpr (std::is_invocable_v<const CF&, double, double, double>) {
+    if (dim == 3) return f(x[0], x[1], x[2]);
+  }
+  if constexpr (std::is_invocable_v<const CF&, double, double>) {
+    if (dim == 2) return f(x[0], x[1]);
+  }
+  throw std::invalid_argument("lsgpu: the velocity function does not take the grid's number of coordinates");
+}
+
+// Borrow the host array of a Vec for the duration of one call.
+struct VecArray {
+  Vec v;
+  double* p = nullptr;
+  explicit VecArray(Vec v_) : v(v_) {
+    if (v) VecGetArray(v, &p);
+  }
+  ~VecArray() {
+    if (v) VecRestoreArray(v, &p);
+  }
+  VecArray(const VecArray&) = delete;
+  VecArray& operator=(const VecArray&) = delete;
+};
+
+}  // namespace lsgpu
+
+enum interpolation_method {
+  linear = LSG_LINEAR,
+  quadratic = LSG_QUADRATIC,
+  quadratic_non_oscillatory = LSG_QUADRATIC_NON_OSCILLATORY,
+  quadratic_non_oscillatory_continuous_v1 = LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V1,
+  quadratic_non_oscillatory_continuous_v2 = LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2
+};
+
+// Node neighbours of one grid (the forest must have its nodes built and outlive this object).
+class my_p4est_node_neighbors_t {
+ public:
+  explicit my_p4est_node_neighbors_t(lsg_forest* forest) : forest_(forest) {}
+  ~my_p4est_node_neighbors_t() {
+    if (ls_) lsg_level_set_destroy(ls_);
+  }
+  my_p4est_node_neighbors_t(const my_p4est_node_neighbors_t&) = delete;
+  my_p4est_node_neighbors_t& operator=(const my_p4est_node_neighbors_t&) = delete;
+  void init_neighbors() { device(); }
+  lsg_forest* forest() const { return forest_; }
+  int dim() const { return lsg_forest_dim(forest_); }
+  int64_t num_nodes() const { return lsg_forest_num_nodes(forest_); }
+  // device image shared by the level-set, interpolation and semi-Lagrangian objects of this grid
+  lsg_level_set* device() const {
+    if (!ls_) lsgpu::check(lsg_level_set_create(forest_, &ls_));
+    return ls_;
+  }
+  std::vector<double> node_xyz() const {
+    std::vector<double> xyz((size_t)num_nodes() * dim());
+    lsgpu::check(lsg_forest_node_xyz(forest_, xyz.data()));
+    return xyz;
+  }
+
+ private:
+  lsg_forest* forest_;
+  mutable lsg_level_set* ls_ = nullptr;
+};
+
+class my_p4est_level_set_t {
+ public:
+  // precision: LSG_FP64 (the reference's arithmetic) or LSG_MIXED (FP32 stencil, FP64 subcell step)
+  explicit my_p4est_level_set_t(my_p4est_node_neighbors_t* ngbd, int precision = LSG_FP64) : ngbd_(ngbd), precision_(precision) {}
+  explicit my_p4est_level_set_t(const my_p4est_node_neighbors_t* ngbd, int precision = LSG_FP64)
+      : ngbd_(const_cast<my_p4est_node_neighbors_t*>(ngbd)), precision_(precision) {}
+  void update(my_p4est_node_neighbors_t* ngbd) { ngbd_ = ngbd; }
+
+  void reinitialize_within_range_of_phi_0(Vec phi, const unsigned char order_space, const unsigned char order_pseudotime,
+                                          const double& limit_high, const double& limit_low, const int& number_of_iterations) const {
+    lsgpu::VecArray p(phi);
+    lsgpu::check(lsg_reinitialize(ngbd_->device(), p.p, order_space, order_pseudotime, limit_high, limit_low, number_of_iterations,
+                                  precision_));
+  }
+  void reinitialize_1st_order(Vec phi, const int& number_of_iterations = 50, const double& limit_absolute_value_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 1, 1, limit_absolute_value_phi_0, -limit_absolute_value_phi_0, number_of_iterations);
+  }
+  void reinitialize_1st_order_above_threshold(Vec phi, const double& threshold, const int& number_of_iterations = 50,
+                                              const double& upper_limit_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 1, 1, upper_limit_phi_0, threshold, number_of_iterations);
+  }
+  void reinitialize_2nd_order(Vec phi, const int& number_of_iterations = 50, const double& limit_absolute_value_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 2, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0, number_of_iterations);
+  }
+  void reinitialize_2nd_order_above_threshold(Vec phi, const double& threshold, const int& number_of_iterations = 50,
+                                              const double& upper_limit_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 2, 2, upper_limit_phi_0, threshold, number_of_iterations);
+  }
+  void reinitialize_2nd_order_time_1st_order_space(Vec phi, const int& number_of_iterations = 50,
+                                                   const double& limit_absolute_value_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 1, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0, number_of_iterations);
+  }
+  void reinitialize_2nd_order_time_1st_order_space_above_threshold(Vec phi, const double& threshold, const int& number_of_iterations = 50,
+                                                                  const double& upper_limit_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 1, 2, upper_limit_phi_0, threshold, number_of_iterations);
+  }
+  void reinitialize_1st_order_time_2nd_order_space(Vec phi, const int& number_of_iterations = 50,
+                                                   const double& limit_absolute_value_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 2, 1, limit_absolute_value_phi_0, -limit_absolute_value_phi_0, number_of_iterations);
+  }
+  void reinitialize_1st_order_time_2nd_order_space_above_threshold(Vec phi, const double& threshold, const int& number_of_iterations = 50,
+                                                                  const double& upper_limit_phi_0 = DBL_MAX) const {
+    reinitialize_within_range_of_phi_0(phi, 2, 1, upper_limit_phi_0, threshold, number_of_iterations);
+  }
+  void perturb_level_set_function(Vec phi, const double& epsilon) const {
+    lsgpu::VecArray p(phi);
+    lsgpu::check(lsg_perturb_level_set_function(ngbd_->device(), p.p, epsilon));
+  }
+
+  // node-sampled velocity: returns dt unchanged
+  double advect_in_normal_direction(const Vec vn, Vec phi, const double& dt, Vec phi_xx = nullptr, Vec phi_yy = nullptr,
+                                    Vec phi_zz = nullptr) const {
+    return advect_in_normal_direction(vn, nullptr, phi, dt, phi_xx, phi_yy, phi_zz);
+  }
+  double advect_in_normal_direction(const Vec vn, const Vec vn_np1, Vec phi, const double& dt, Vec phi_xx = nullptr,
+                                    Vec phi_yy = nullptr, Vec phi_zz = nullptr) const {
+    lsgpu::VecArray v(vn), v1(vn_np1), p(phi);
+    const int D = ngbd_->dim();
+    const size_t N = (size_t)ngbd_->num_nodes();
+    // the derivative Vecs are separate in the reference; the ABI takes them as D blocks of N
+    std::vector<double> dd;
+    Vec xx[3] = {phi_xx, phi_yy, phi_zz};
+    const bool given = phi_xx != nullptr;
+    if (given) {
+      dd.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(xx[a]);
+        for (size_t n = 0; n < N; ++n) dd[a * N + n] = x.p[n];
+      }
+    }
+    lsgpu::check(lsg_advect_in_normal_direction(ngbd_->device(), v.p, vn_np1 ? v1.p : nullptr, p.p, dt, given ? dd.data() : nullptr,
+                                                precision_));
+    if (given)
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(xx[a]);
+        for (size_t n = 0; n < N; ++n) x.p[n] = dd[a * N + n];
+      }
+    return dt;
+  }
+  // velocity given as a function object of the node coordinates (x, y[, z]): dt from CFL 0.8, returned
+  template <typename CF>
+  double advect_in_normal_direction(const CF& vn, Vec phi, Vec phi_xx = nullptr, Vec phi_yy = nullptr, Vec phi_zz = nullptr) const {
+    const int D = ngbd_->dim();
+    const std::vector<double> xyz = ngbd_->node_xyz();
+    const size_t N = xyz.size() / D;
+    lsgpu_vec_values v(N);
+    for (size_t n = 0; n < N; ++n) v.data[n] = lsgpu::eval_cf(vn, &xyz[(size_t)D * n], D);
+    double dt = 0;
+    lsgpu::check(lsg_advect_cfl_dt(ngbd_->device(), v.data.data(), &dt));
+    lsgpu::VecArray p(phi);
+    std::vector<double> dd;
+    Vec xx[3] = {phi_xx, phi_yy, phi_zz};
+    if (phi_xx) {
+      dd.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(xx[a]);
+        for (size_t n = 0; n < N; ++n) dd[a * N + n] = x.p[n];
+      }
+    }
+    lsgpu::check(lsg_advect_in_normal_direction(ngbd_->device(), v.data.data(), nullptr, p.p, dt, phi_xx ? dd.data() : nullptr,
+                                                precision_));
+    return dt;
+  }
+
+ private:
+  struct lsgpu_vec_values {
+    explicit lsgpu_vec_values(size_t n) : data(n) {}
+    std::vector<double> data;
+  };
+  my_p4est_node_neighbors_t* ngbd_;
+  int precision_;
+};
+
+// Node interpolation at buffered points (one process: every point is local).
+class my_p4est_interpolation_nodes_t {
+ public:
+  explicit my_p4est_interpolation_nodes_t(const my_p4est_node_neighbors_t* ngbd) : ngbd_(ngbd) {}
+  void clear() {
+    idx_.clear();
+    xyz_.clear();
+  }
+  void add_point(int64_t node_idx_on_output, const double* xyz) {
+    idx_.push_back(node_idx_on_output);
+    for (int a = 0; a < ngbd_->dim(); ++a) xyz_.push_back(xyz[a]);
+  }
+  void set_input(Vec F, interpolation_method method) {
+    F_ = F;
+    Fdd_[0] = Fdd_[1] = Fdd_[2] = nullptr;
+    method_ = method;
+  }
+  void set_input(Vec F, Vec Fxx, Vec Fyy, Vec Fzz, interpolation_method method) {
+    F_ = F;
+    Fdd_[0] = Fxx;
+    Fdd_[1] = Fyy;
+    Fdd_[2] = Fzz;
+    method_ = method;
+  }
+  void set_input(Vec F, Vec Fxx, Vec Fyy, interpolation_method method) { set_input(F, Fxx, Fyy, nullptr, method); }
+  // results[node_idx_on_output] for every buffered point
+  void interpolate(double* results) const {
+    const int D = ngbd_->dim();
+    const size_t N = (size_t)ngbd_->num_nodes();
+    lsgpu::VecArray f(F_);
+    std::vector<double> dd;
+    if (Fdd_[0] && method_ != linear) {
+      dd.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(Fdd_[a]);
+        for (size_t n = 0; n < N; ++n) dd[a * N + n] = x.p[n];
+      }
+    }
+    std::vector<double> out(idx_.size());
+    lsgpu::check(lsg_interpolate_nodes(ngbd_->device(), xyz_.data(), (int64_t)idx_.size(), f.p, 1, dd.empty() ? nullptr : dd.data(),
+                                       (int)method_, out.data()));
+    for (size_t i = 0; i < idx_.size(); ++i) results[idx_[i]] = out[i];
+  }
+  void interpolate(Vec out) const {
+    lsgpu::VecArray o(out);
+    interpolate(o.p);
+  }
+
+ private:
+  const my_p4est_node_neighbors_t* ngbd_;
+  std::vector<int64_t> idx_;
+  std::vector<double> xyz_;
+  Vec F_ = nullptr;
+  Vec Fdd_[3] = {nullptr, nullptr, nullptr};
+  interpolation_method method_ = linear;
+};
+
+// Semi-Lagrangian step from the grid at n (ngbd_n) onto the nodes of the grid at n+1.
+class my_p4est_semi_lagrangian_t {
+ public:
+  my_p4est_semi_lagrangian_t(lsg_forest* forest_np1, my_p4est_node_neighbors_t* ngbd_n) : forest_np1_(forest_np1), ngbd_n_(ngbd_n) {}
+  void set_velo_interpolation(interpolation_method m) { velo_ = m; }
+  void set_phi_interpolation(interpolation_method m) { phi_ = m; }
+  // advect_from_n_to_np1(dt, v, vxx, phi_n, phi_xx_n, phi_np1): v[D] node velocities of grid n;
+  // vxx[D][D] and phi_xx_n[D] may be null (computed); phi_np1 has one value per node of grid n+1.
+  void advect_from_n_to_np1(double dt, Vec* v, Vec** vxx, Vec phi_n, Vec* phi_xx_n, double* phi_np1) const {
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes();
+    std::vector<double> vv((size_t)D * N), vdd, pdd;
+    for (int a = 0; a < D; ++a) {
+      lsgpu::VecArray x(v[a]);
+      for (size_t n = 0; n < N; ++n) vv[a * N + n] = x.p[n];
+    }
+    if (vxx) {
+      vdd.resize((size_t)D * D * N);
+      for (int c = 0; c < D; ++c)
+        for (int a = 0; a < D; ++a) {
+          lsgpu::VecArray x(vxx[c][a]);
+          for (size_t n = 0; n < N; ++n) vdd[((size_t)c * D + a) * N + n] = x.p[n];
+        }
+    }
+    if (phi_xx_n) {
+      pdd.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(phi_xx_n[a]);
+        for (size_t n = 0; n < N; ++n) pdd[a * N + n] = x.p[n];
+      }
+    }
+    const int64_t np = lsg_forest_num_nodes(forest_np1_);
+    std::vector<double> xyz((size_t)np * D);
+    lsgpu::check(lsg_forest_node_xyz(forest_np1_, xyz.data()));
+    lsgpu::VecArray p(phi_n);
+    lsgpu::check(lsg_semi_lagrangian_advect(ngbd_n_->device(), xyz.data(), np, dt, vv.data(), vdd.empty() ? nullptr : vdd.data(), p.p,
+                                            pdd.empty() ? nullptr : pdd.data(), (int)velo_, (int)phi_, phi_np1));
+  }
+
+ private:
+  lsg_forest* forest_np1_;
+  my_p4est_node_neighbors_t* ngbd_n_;
+  interpolation_method velo_ = quadratic_non_oscillatory_continuous_v2;
+  interpolation_method phi_ = quadratic_non_oscillatory_continuous_v2;
+};
+
+#endif  // LSGPU_HPP

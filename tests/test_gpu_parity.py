@@ -152,3 +152,22 @@ def test_errors_are_reported():
         ls.reinitialize_2nd_order(phi[:-1], 5)
     with pytest.raises(G.LsgInvalidArgument):
         ls.reinitialize_2nd_order(phi, -1)
+
+
+def test_band_linf_device_matches_numpy():
+    """FP64 band check on the device: same value and count as numpy; NaN reported."""
+    import torch
+    f = flower_3d(3, 6)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    ls.set_stream(torch.cuda.current_stream().cuda_stream)
+    ref = phi0_flower_3d(f)
+    rng = np.random.default_rng(5)
+    a = ref + rng.normal(0, 1e-6, ref.size)
+    _, dmin, _ = f.dxyz_min()
+    band = 3 * dmin
+    val, cnt = ls.band_linf(torch.from_numpy(a).cuda(), torch.from_numpy(ref).cuda(), band)
+    m = np.abs(ref) < band
+    assert cnt == int(m.sum()) and val == float(np.max(np.abs(a[m] - ref[m])))
+    a[np.flatnonzero(m)[0]] = np.nan
+    val, _ = ls.band_linf(torch.from_numpy(a).cuda(), torch.from_numpy(ref).cuda(), band)
+    assert np.isnan(val)
