@@ -1278,6 +1278,12 @@ int ora_sl_advect_vortex(void* h, int64_t npts, const double* xyz, double dt, do
   });
 }
 
+// interface_Location / interface_Location_With_Second_Order_Derivative (src/casl_math.cpp:55-97)
+double ora_interface_location(double a, double b, double fa, double fb) { return interface_Location(a, b, fa, fb); }
+double ora_interface_location_2nd(double a, double b, double fa, double fb, double fxxa, double fxxb) {
+  return interface_Location_With_Second_Order_Derivative(a, b, fa, fb, fxxa, fxxb);
+}
+
 // velocity of the single vortex at points (D per point), D x np output
 int ora_vortex(int dim, int64_t npts, const double* xyz, double vscale, double* v) {
   return guard([&] {

@@ -36,6 +36,8 @@ SIG = {
     "ora_sl_advect": (_I, [_P, _I64, _DP, _D, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
     "ora_sl_advect_vortex": (_I, [_P, _I64, _DP, _D, _D, _DP, _DP, _I, _DP, _I]),
     "ora_vortex": (_I, [_I, _I64, _DP, _D, _DP]),
+    "ora_interface_location": (_D, [_D, _D, _D, _D]),
+    "ora_interface_location_2nd": (_D, [_D, _D, _D, _D, _D, _D]),
 }
 _lib = None
 
