@@ -554,7 +554,7 @@ def main():
     ls = G.my_p4est_level_set_t(ngbd, precision="mixed")
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
-    stage_cfg = ls.autotune(phi0, trials=3)
+    stage_cfg = ls.autotune(phi0, trials=8)
     setup_s = time.perf_counter() - t0
     _, dmin, _ = f.dxyz_min(args.levels[1])
 
@@ -690,7 +690,7 @@ def main():
             "dx_min": dmin,
             "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
             "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
-            "autotuned_stage_config": stage_cfg,
+            "autotuned_stage_config": stage_cfg, "mixed_tables": ls.table_stats(),
         }
         print(json.dumps(out), flush=True)
     if dist is not None:

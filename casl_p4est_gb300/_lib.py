@@ -83,6 +83,7 @@ SIGNATURES = {
     "lsg_level_set_autotune": (_I, [_P, _DP, _I, _I32P]),
     "lsg_level_set_stage_config": (_I, [_P, _I32P]),
     "lsg_level_set_set_stage_config": (_I, [_P, _I32P]),
+    "lsg_level_set_table_stats": (_I, [_P, C.POINTER(_I64)]),
     "lsg_level_set_kernel_times": (_I, [_P, _DP, C.POINTER(_I64), _I, _I]),
     "lsg_level_set_launch_count": (_I64, [_P]),
 }

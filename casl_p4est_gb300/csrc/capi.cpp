@@ -697,6 +697,7 @@ int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int
         config[0] = L.cfg.tpb;
         config[1] = L.cfg.uniform_blocks;
         config[2] = L.cfg.regular_blocks;
+        config[3] = L.cfg.depth;
       }
     });
   });
@@ -709,6 +710,7 @@ int lsg_level_set_stage_config(const lsg_level_set* ls, int* config) {
     config[0] = c.tpb;
     config[1] = c.uniform_blocks;
     config[2] = c.regular_blocks;
+    config[3] = c.depth;
   });
 }
 
@@ -717,10 +719,12 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config != nullptr, "null config");
     need(config[0] == 32 || config[0] == 64 || config[0] == 128 || config[0] == 256, "threads per block must be 32, 64, 128 or 256");
     need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
+    need(config[3] == 1 || config[3] == 2, "pipeline depth must be 1 or 2");
     with_ls(ls, [&](auto& L) {
       L.cfg.tpb = config[0];
       L.cfg.uniform_blocks = config[1];
       L.cfg.regular_blocks = config[2];
+      L.cfg.depth = config[3];
       L.drop_graph();
     });
   });
@@ -731,6 +735,22 @@ int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b
     need(a_dev != nullptr && b_dev != nullptr && out != nullptr, "null argument");
     need(band > 0, "band must be positive");
     with_ls(ls, [&](auto& L) { *out = L.band_linf(a_dev, b_dev, band, count); });
+  });
+}
+
+int lsg_level_set_table_stats(lsg_level_set* ls, int64_t* out) {
+  return guard([&] {
+    need(out != nullptr, "null output");
+    with_ls(ls, [&](auto& L) {
+      if (!L.mixed_ready) throw StateError("the mixed tables are not built");
+      out[0] = L.N;
+      out[1] = L.T32.nR;
+      out[2] = L.T32.nU;
+      out[3] = L.T32.nI;
+      out[4] = L.T32.nX;
+      out[5] = L.ncls;
+      out[6] = L.num_corrections;
+    });
   });
 }
 

@@ -18,11 +18,13 @@ enum : uint16_t {
 };
 
 // Launch shape of the mixed stage kernels (chosen by the autotuner): grid of the persistent uniform
-// and regular kernels (0: one full wave at maximum occupancy) and threads per block of every stage kernel.
+// and regular kernels (0: one full wave at maximum occupancy), threads per block of every stage
+// kernel, and the pipeline depth of the uniform kernel.
 struct StageCfg {
   int uniform_blocks = 0;
   int regular_blocks = 0;
   int tpb = 256;
+  int depth = 1;  // pipeline depth of the uniform kernel: nodes whose gathers are in flight per thread
 };
 
 template <int D>
@@ -80,8 +82,7 @@ struct DTab32 {
   const float* corr;     // D*D x R
   const uint32_t* i_cls; // nI: geometry class of each irregular node
   const float* cls32;    // class records (cls_words<D>() floats each)
-  const int32_t* x_list; // regular nodes of the extended second-derivative set
-  int64_t nX;
+  int64_t x_first, nX;   // regular nodes of the extended second-derivative set: [x_first, x_first + nX)
   // FP64 coefficients of the irregular nodes (subcell step)
   double tsize64[3];
   const double* i_wf64;

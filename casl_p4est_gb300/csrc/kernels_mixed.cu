@@ -43,12 +43,12 @@ __device__ __forceinline__ float lin_irr(const DTab32<D>& T, uint32_t meta, int 
   const int64_t nI = T.nI;
   const int64_t base = (int64_t)(dir * H) * nI + i;
   const int c = face_count(meta, dir);
-  const int32_t i0 = __ldg(T.i_nbr + base);
+  const int32_t i0 = __ldcs(T.i_nbr + base);
   if (c == 1) return __ldg(f + i0);
   float acc = __ldg(T.i_wf + base) * __ldg(f + i0);
 #pragma unroll
   for (int k = 1; k < H; ++k)
-    if (k < c) acc = fmaf(__ldg(T.i_wf + base + k * nI), __ldg(f + __ldg(T.i_nbr + base + k * nI)), acc);
+    if (k < c) acc = fmaf(__ldg(T.i_wf + base + k * nI), __ldg(f + __ldcs(T.i_nbr + base + k * nI)), acc);
   return acc;
 }
 
@@ -81,11 +81,11 @@ __global__ void __launch_bounds__(TPB) k_dd32(DTab32<D> T, const float* __restri
   const float f0 = __ldg(f + n);
   float Dv[D];
   if (n < T.nR) {
-    const Reg<D> R{__ldg(T.r_meta + n)};
+    const Reg<D> R{__ldcs(T.r_meta + n)};
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      const float fm = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a) * T.nR + n));
-      const float fp = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a + 1) * T.nR + n));
+      const float fm = __ldg(f + __ldcs(T.r_nbr + (int64_t)(2 * a) * T.nR + n));
+      const float fp = __ldg(f + __ldcs(T.r_nbr + (int64_t)(2 * a + 1) * T.nR + n));
       Dv[a] = central_dd(fp, f0, fm, R.d(T, 2 * a + 1), R.d(T, 2 * a));
     }
   } else {
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= N) return;
-  const uint16_t st = status[n];
+  const uint16_t st = __ldcs(status + n);
   float r;
   if (st & ST_ANCHORED) {
     r = 0.0f;
@@ -148,10 +148,10 @@ __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint1
     // second derivatives at the node are recomputed from the gathered neighbours (same arithmetic
     // as k_dd32) rather than re-read
     if (n < T.nR) {
-      const Reg<D> R{__ldg(T.r_meta + n)};
+      const Reg<D> R{__ldcs(T.r_meta + n)};
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
-        const int32_t nb = __ldg(T.r_nbr + (int64_t)dir * T.nR + n);
+        const int32_t nb = __ldcs(T.r_nbr + (int64_t)dir * T.nR + n);
         fnb[dir] = __ldg(phin + nb);
         if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd + (int64_t)(dir >> 1) * N + nb);
         s[dir] = R.d(T, dir);
@@ -242,7 +242,7 @@ struct Cls {
 
 template <int D>
 __device__ __forceinline__ Cls<D> cls_of(const DTab32<D>& T, int64_t i) {
-  return Cls<D>{T.cls32 + (int64_t)__ldg(T.i_cls + i) * cls_words<D>()};
+  return Cls<D>{T.cls32 + (int64_t)__ldcs(T.i_cls + i) * cls_words<D>()};
 }
 
 // linear interpolation over the face nodes of an irregular node (class weights)
@@ -251,11 +251,11 @@ __device__ __forceinline__ float lin_cls(const DTab32<D>& T, const Cls<D>& C, ui
   constexpr int H = Dim<D>::HALF;
   const int64_t base = (int64_t)(dir * H) * T.nI + i;
   const int c = face_count(meta, dir);
-  if (c == 1) return __ldg(f + __ldg(T.i_nbr + base));
+  if (c == 1) return __ldg(f + __ldcs(T.i_nbr + base));
   float acc = 0.0f;
 #pragma unroll
   for (int k = 0; k < H; ++k)
-    if (k < c) acc = fmaf(C.wf(dir, k), __ldg(f + __ldg(T.i_nbr + base + k * T.nI)), acc);
+    if (k < c) acc = fmaf(C.wf(dir, k), __ldg(f + __ldcs(T.i_nbr + base + k * T.nI)), acc);
   return acc;
 }
 
@@ -289,13 +289,13 @@ __global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __rest
       for (int r = 0; r < D; ++r) Dv[r] = o[r];
     }
   } else if (t < T.nI + T.nX) {
-    n = __ldg(T.x_list + (t - T.nI));
-    const Reg<D> R{__ldg(T.r_meta + n)};
+    n = T.x_first + (t - T.nI);
+    const Reg<D> R{__ldcs(T.r_meta + n)};
     const float f0 = __ldg(f + n);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      const float fm = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a) * T.nR + n));
-      const float fp = __ldg(f + __ldg(T.r_nbr + (int64_t)(2 * a + 1) * T.nR + n));
+      const float fm = __ldg(f + __ldcs(T.r_nbr + (int64_t)(2 * a) * T.nR + n));
+      const float fp = __ldg(f + __ldcs(T.r_nbr + (int64_t)(2 * a + 1) * T.nR + n));
       Dv[a] = central_dd(fp, f0, fm, R.d(T, 2 * a + 1), R.d(T, 2 * a));
     }
   } else {
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
   const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= last) return;
-  const uint16_t st = status[n];
+  const uint16_t st = __ldcs(status + n);
   float r;
   if (st & ST_ANCHORED) {
     r = 0.0f;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         const int64_t base = (int64_t)(dir * H) * T.nI + i;
         s[dir] = C.d(dir);
         if (c == 1) {
-          const int32_t j = __ldg(T.i_nbr + base);
+          const int32_t j = __ldcs(T.i_nbr + base);
           fnb[dir] = __ldg(phin + j);
           if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd_irr + (int64_t)axis * N + j);
         } else {
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
 #pragma unroll
           for (int k = 0; k < H; ++k) {
             if (k < c) {
-              const int32_t j = __ldg(T.i_nbr + base + k * T.nI);
+              const int32_t j = __ldcs(T.i_nbr + base + k * T.nI);
               const float w = C.wf(dir, k);
               v = fmaf(w, __ldg(phin + j), v);
               if (ORDER_SPACE > 1) x = fmaf(w, __ldg(dd_irr + (int64_t)axis * N + j), x);
@@ -417,16 +417,16 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
   int32_t p_nb[2 * D], p_nb2[2 * D];
   float p_f0 = 0.0f, p_avg = 0.0f;
   auto prefetch = [&](int m) {
-    p_st = status[m];
-    p_codes = __ldg(T.r_meta + m);
-    p_far = __ldg(T.r_meta2 + m);
+    p_st = __ldcs(status + m);
+    p_codes = __ldcs(T.r_meta + m);
+    p_far = __ldcs(T.r_meta2 + m);
 #pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
-      p_nb[dir] = __ldg(T.r_nbr + dir * nR + m);
-      if (ORDER_SPACE > 1) p_nb2[dir] = __ldg(T.r_nbr2 + dir * nR + m);
+      p_nb[dir] = __ldcs(T.r_nbr + dir * nR + m);
+      if (ORDER_SPACE > 1) p_nb2[dir] = __ldcs(T.r_nbr2 + dir * nR + m);
     }
     p_f0 = __ldg(phin + m);
-    if (AVG) p_avg = avg_with[m];
+    if (AVG) p_avg = __ldcs(avg_with + m);
   };
   if (n < last) prefetch(n);
   for (; n < last; n += stride) {
@@ -492,83 +492,135 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
 
 // Regular nodes with uniform stencils (second order in space): the node and its face nodes have the
 // same spacing h_a along each axis, so every second derivative is (f_+ + f_- - 2 f_0)/h_a^2 and all
-// reciprocals are exponent shifts. Persistent and software-pipelined like k_reinit_fused_reg32;
-// interface-adjacent nodes take their subcell distances from s_near.
+// reciprocals are exponent shifts. Persistent and software-pipelined: with DEPTH 1 a thread loads the
+// next node's indices while the current node's face values are gathered; with DEPTH 2 it also gathers
+// the next node's face values while the current node is computed (two nodes' gathers in flight).
+// Interface-adjacent nodes take their subcell distances from s_near.
+template <int D>
+struct UniIdx {  // a node's own words and stencil indices
+  int n;
+  uint16_t st;
+  uint32_t code;
+  float f0, avg;
+  int32_t nb[2 * D], nb2[2 * D];
+};
+template <int D>
+struct UniVal {  // the same node with its face and second-neighbour values gathered
+  int n;
+  uint16_t st;
+  uint32_t code;
+  float f0, avg;
+  float v[2 * D], v2[2 * D];
+};
+
 template <int D, bool AVG>
+__device__ __forceinline__ void uni_load(const DTab32<D>& T, int nR, const uint16_t* __restrict__ status, const float* __restrict__ phin,
+                                         const float* avg_with, int m, UniIdx<D>& I) {
+  I.n = m;
+  I.st = __ldcs(status + m);
+  I.code = __ldcs(T.r_meta + m) & 15u;
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    I.nb[dir] = __ldcs(T.r_nbr + dir * nR + m);
+    I.nb2[dir] = __ldcs(T.r_nbr2 + dir * nR + m);
+  }
+  I.f0 = __ldg(phin + m);
+  I.avg = AVG ? __ldcs(avg_with + m) : 0.0f;
+}
+
+template <int D>
+__device__ __forceinline__ void uni_gather(const UniIdx<D>& I, const float* __restrict__ phin, UniVal<D>& V) {
+  V.n = I.n;
+  V.st = I.st;
+  V.code = I.code;
+  V.f0 = I.f0;
+  V.avg = I.avg;
+  const bool active = !(I.st & (ST_ANCHORED | ST_OUTSIDE | ST_FROZEN));
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    V.v[dir] = active ? __ldg(phin + I.nb[dir]) : 0.0f;
+    V.v2[dir] = active ? __ldg(phin + I.nb2[dir]) : 0.0f;
+  }
+}
+
+template <int D, bool AVG>
+__device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __restrict__ s_near, const UniVal<D>& V) {
+  const uint16_t st = V.st;
+  const float f0 = V.f0;
+  float r;
+  if (st & ST_ANCHORED) {
+    r = 0.0f;
+  } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
+    r = f0;
+  } else {
+    const int lvl = T.base + (int)V.code;
+    const bool near = (st & ST_NEAR) != 0;
+    const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
+    float smin = 3.0e38f, hsum = 0.0f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const float h = __int_as_float(__float_as_int(T.tsize[a]) - (lvl << 23));
+      const float ih = __int_as_float(__float_as_int(T.inv_tsize[a]) + (lvl << 23));
+      const float ih2 = ih * ih;
+      float fm = V.v[2 * a], fp = V.v[2 * a + 1];
+      const float fmm = V.v2[2 * a], fpp = V.v2[2 * a + 1];
+      const float xx0 = (fp + fm - 2.0f * f0) * ih2;
+      const float mm = minmodf((f0 + fmm - 2.0f * fm) * ih2, xx0);
+      const float mp = minmodf((fpp + f0 - 2.0f * fp) * ih2, xx0);
+      float gm, gp;
+      if (!near) {
+        gm = fmaf(0.5f * h, mm, (f0 - fm) * ih);
+        gp = fmaf(-0.5f * h, mp, (fp - f0) * ih);
+        smin = fminf(smin, h);
+      } else {
+        const float sm = __ldg(s_near + (int64_t)(2 * a) * T.N + V.n), sp = __ldg(s_near + (int64_t)(2 * a + 1) * T.N + V.n);
+        if (st & (1u << (ST_CUT_SHIFT + 2 * a))) fm = 0.0f;
+        if (st & (1u << (ST_CUT_SHIFT + 2 * a + 1))) fp = 0.0f;
+        gm = fmaf(0.5f * sm, mm, __fdividef(f0 - fm, sm));
+        gp = fmaf(-0.5f * sp, mp, __fdividef(fp - f0, sp));
+        smin = fminf(smin, fminf(sm, sp));
+      }
+      if (sgn * gp > 0.0f) gp = 0.0f;
+      if (sgn * gm < 0.0f) gm = 0.0f;
+      hsum += fmaxf(gp * gp, gm * gm);
+    }
+    r = f0 - smin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
+    if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
+  }
+  if (AVG) r = 0.5f * (V.avg + r);
+  return r;
+}
+
+template <int D, bool AVG, int DEPTH>
 __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                           const float* __restrict__ s_near, const float* __restrict__ phin,
                                                           float* out, const float* avg_with) {
   const int nR = (int)T.nR, nU = (int)T.nU;
   const int stride = gridDim.x * blockDim.x;
   int n = blockIdx.x * blockDim.x + threadIdx.x;
-  uint16_t p_st = 0;
-  uint32_t p_code = 0;
-  int32_t p_nb[2 * D], p_nb2[2 * D];
-  float p_f0 = 0.0f, p_avg = 0.0f;
-  auto prefetch = [&](int m) {
-    p_st = status[m];
-    p_code = __ldg(T.r_meta + m) & 15u;
-#pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) {
-      p_nb[dir] = __ldg(T.r_nbr + dir * nR + m);
-      p_nb2[dir] = __ldg(T.r_nbr2 + dir * nR + m);
+  if (n >= nU) return;
+  UniIdx<D> I;
+  uni_load<D, AVG>(T, nR, status, phin, avg_with, n, I);
+  if (DEPTH == 1) {
+    for (; n < nU; n += stride) {
+      UniVal<D> V;
+      uni_gather<D>(I, phin, V);
+      if (n + stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + stride, I);
+      out[V.n] = uni_update<D, AVG>(T, s_near, V);
     }
-    p_f0 = __ldg(phin + m);
-    if (AVG) p_avg = avg_with[m];
-  };
-  if (n < nU) prefetch(n);
-  for (; n < nU; n += stride) {
-    const uint16_t st = p_st;
-    const int lvl = T.base + (int)p_code;
-    int32_t nb[2 * D], nb2[2 * D];
-#pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) {
-      nb[dir] = p_nb[dir];
-      nb2[dir] = p_nb2[dir];
+  } else {
+    UniVal<D> V;
+    uni_gather<D>(I, phin, V);
+    if (n + stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + stride, I);
+    for (; n < nU; n += stride) {
+      // gathers of the next node and index loads of the one after are issued before this node's update
+      UniVal<D> Vn;
+      const bool more = n + stride < nU;
+      if (more) uni_gather<D>(I, phin, Vn);
+      if (n + 2 * stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + 2 * stride, I);
+      out[V.n] = uni_update<D, AVG>(T, s_near, V);
+      if (more) V = Vn;
     }
-    const float f0 = p_f0, avg = p_avg;
-    if (n + stride < nU) prefetch(n + stride);
-    float r;
-    if (st & ST_ANCHORED) {
-      r = 0.0f;
-    } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
-      r = f0;
-    } else {
-      const bool near = (st & ST_NEAR) != 0;
-      const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
-      float smin = 3.0e38f, hsum = 0.0f;
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        const float h = __int_as_float(__float_as_int(T.tsize[a]) - (lvl << 23));
-        const float ih = __int_as_float(__float_as_int(T.inv_tsize[a]) + (lvl << 23));
-        const float ih2 = ih * ih;
-        float fm = __ldg(phin + nb[2 * a]), fp = __ldg(phin + nb[2 * a + 1]);
-        const float fmm = __ldg(phin + nb2[2 * a]), fpp = __ldg(phin + nb2[2 * a + 1]);
-        const float xx0 = (fp + fm - 2.0f * f0) * ih2;
-        const float mm = minmodf((f0 + fmm - 2.0f * fm) * ih2, xx0);
-        const float mp = minmodf((fpp + f0 - 2.0f * fp) * ih2, xx0);
-        float gm, gp;
-        if (!near) {
-          gm = fmaf(0.5f * h, mm, (f0 - fm) * ih);
-          gp = fmaf(-0.5f * h, mp, (fp - f0) * ih);
-          smin = fminf(smin, h);
-        } else {
-          const float sm = __ldg(s_near + (int64_t)(2 * a) * T.N + n), sp = __ldg(s_near + (int64_t)(2 * a + 1) * T.N + n);
-          if (st & (1u << (ST_CUT_SHIFT + 2 * a))) fm = 0.0f;
-          if (st & (1u << (ST_CUT_SHIFT + 2 * a + 1))) fp = 0.0f;
-          gm = fmaf(0.5f * sm, mm, __fdividef(f0 - fm, sm));
-          gp = fmaf(-0.5f * sp, mp, __fdividef(fp - f0, sp));
-          smin = fminf(smin, fminf(sm, sp));
-        }
-        if (sgn * gp > 0.0f) gp = 0.0f;
-        if (sgn * gm < 0.0f) gm = 0.0f;
-        hsum += fmaxf(gp * gp, gm * gm);
-      }
-      r = f0 - smin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
-      if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
-    }
-    if (AVG) r = 0.5f * (avg + r);
-    out[n] = r;
   }
 }
 
@@ -584,10 +636,10 @@ __global__ void __launch_bounds__(TPB) k_advect_stage32(DTab32<D> T, const float
 #pragma unroll
   for (int a = 0; a < D; ++a) xx0[a] = __ldg(ddm + (int64_t)a * N + n);
   if (n < T.nR) {
-    const Reg<D> R{__ldg(T.r_meta + n)};
+    const Reg<D> R{__ldcs(T.r_meta + n)};
 #pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
-      const int32_t nb = __ldg(T.r_nbr + (int64_t)dir * T.nR + n);
+      const int32_t nb = __ldcs(T.r_nbr + (int64_t)dir * T.nR + n);
       fnb[dir] = __ldg(phin + nb);
       xxnb[dir] = __ldg(ddm + (int64_t)(dir >> 1) * N + nb);
       s[dir] = R.d(T, dir);
@@ -929,9 +981,10 @@ static int persistent_blocks(const void* kernel) {
 template <int D, int OS, bool AVG>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
                          float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg) {
-  static int gb_reg = 0, gb_uni = 0;
+  static int gb_reg = 0, gb_uni = 0, gb_uni2 = 0;
   if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
-  if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG>);
+  if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1>);
+  if (!gb_uni2) gb_uni2 = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 2>);
   const int tpb = (cfg.tpb > 0 && cfg.tpb <= TPB) ? cfg.tpb : TPB;
   // a persistent grid sized for TPB-thread blocks keeps the same thread count with smaller blocks
   const int scale = TPB / tpb;
@@ -945,8 +998,13 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
   }
   if (part == STAGE_PART_UNIFORM && uni_end > 0) {
-    const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, gb_uni * scale) : gb_uni * scale;
-    k_reinit_uniform32<D, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(uni_end)), tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
+    const int full = (cfg.depth == 2 ? gb_uni2 : gb_uni) * scale;
+    const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
+    const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
+    if (cfg.depth == 2)
+      k_reinit_uniform32<D, AVG, 2><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
+    else
+      k_reinit_uniform32<D, AVG, 1><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
   }
 }
 

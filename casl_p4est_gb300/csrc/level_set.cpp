@@ -261,7 +261,6 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M, const double* ts) {
   r_nbr2.upload(M.r_nbr2, stream);
   i_cls.upload(M.i_cls, stream);
   cls32.upload(M.cls32, stream);
-  x_list.upload(M.x_list, stream);
   r_meta2.upload(M.r_meta2, stream);
   i_meta.upload(M.i_meta, stream);
   i_nbr.upload(M.i_nbr, stream);
@@ -282,6 +281,7 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M, const double* ts) {
   cuda_check(cudaStreamSynchronize(stream), "mixed table upload");
   nR = M.nR;
   nI = M.nI;
+  ncls = M.ncls;
   T32.N = N;
   T32.nR = M.nR;
   T32.nI = M.nI;
@@ -294,7 +294,7 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M, const double* ts) {
   T32.r_nbr2 = r_nbr2.p;
   T32.i_cls = i_cls.p;
   T32.cls32 = cls32.p;
-  T32.x_list = x_list.p;
+  T32.x_first = M.x_first;
   T32.nX = (int64_t)M.x_list.size();
   T32.r_meta2 = r_meta2.p;
   T32.i_meta = i_meta.p;
@@ -483,9 +483,9 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
   cuda_check(cudaGetLastError(), "reinitialize (batch)");
 }
 
-// Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, grid of
-// the persistent uniform and regular kernels), timing `trials` iterations per candidate with CUDA
-// events on the object's stream.
+// Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, pipeline
+// depth and grid of the persistent uniform kernel, grid of the persistent regular kernel), timing
+// `trials` iterations per candidate with CUDA events on the object's stream.
 template <int D>
 void LevelSet<D>::autotune(const double* phi, int trials) {
   if (trials < 1) trials = 1;
@@ -521,15 +521,18 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     StageCfg c;
     c.tpb = tpb;
     float c_ms = 1e30f;
-    for (int g : grids) {
-      StageCfg t = c;
-      t.uniform_blocks = g * sms * (256 / tpb);
-      const float ms = run(t);
-      if (ms < c_ms) {
-        c_ms = ms;
-        c.uniform_blocks = t.uniform_blocks;
+    for (int depth : {1, 2})
+      for (int g : grids) {
+        StageCfg t = c;
+        t.depth = depth;
+        t.uniform_blocks = g * sms * (256 / tpb);
+        const float ms = run(t);
+        if (ms < c_ms) {
+          c_ms = ms;
+          c.depth = depth;
+          c.uniform_blocks = t.uniform_blocks;
+        }
       }
-    }
     for (int g : grids) {
       if (g == 6) continue;
       StageCfg t = c;

@@ -63,12 +63,12 @@ struct LevelSet {
   // mixed tables (built on first mixed call)
   bool mixed_ready = false;
   DevBuf<uint32_t> r_meta, i_meta, r_meta2, i_cls;
-  DevBuf<int32_t> r_nbr, r_nbr2, x_list, i_nbr, i_cidx, perm, iperm, near_list;
+  DevBuf<int32_t> r_nbr, r_nbr2, i_nbr, i_cidx, perm, iperm, near_list;
   DevBuf<unsigned> near_count;
   DevBuf<float> i_wf, i_d, i_q, corr32, cls32;
   DevBuf<double> i_wf64, i_d64, i_q64, corr64;
   DTab32<D> T32{};
-  int64_t nR = 0, nI = 0;
+  int64_t nR = 0, nI = 0, ncls = 0;
   // point location tables for node interpolation (built on first use)
   bool loc_ready = false;
   DevBuf<uint64_t> loc_key;

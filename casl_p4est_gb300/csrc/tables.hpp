@@ -84,7 +84,8 @@ struct Tables32 {
   int64_t ncls = 0;
   // nodes whose second derivatives are computed by the extended pass: the irregular nodes and every
   // face node that the fused stage cannot rebuild from a second neighbour (regular ones listed here)
-  std::vector<int32_t> x_list;
+  std::vector<int32_t> x_list;     // x_first, x_first + 1, ... (the regular part of the set is contiguous)
+  int64_t x_first = 0;
   std::vector<float> i_wf;          // NS * nI
   std::vector<float> i_d;           // 2D * nI
   std::vector<float> i_q;           // 2D*(D-1) * nI

@@ -353,9 +353,49 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
             inx[j] = 1;
           }
         }
-    M.x_list.clear();
-    for (int64_t j = 0; j < nR; ++j)
-      if (inx[j]) M.x_list.push_back((int32_t)j);
+    // regular order [uniform, not in the set | uniform in the set | other in the set | other]: the
+    // regular part of the extended set becomes one contiguous range (coalesced second-derivative
+    // writes, no index list) and the uniform nodes stay in front
+    std::vector<int32_t> old_of_new;
+    old_of_new.reserve((size_t)nR);
+    for (int pass = 0; pass < 4; ++pass)
+      for (int64_t j = 0; j < nR; ++j) {
+        const bool uni = j < M.nU, inset = inx[(size_t)j] != 0;
+        const int cls = uni ? (inset ? 1 : 0) : (inset ? 2 : 3);
+        if (cls == pass) old_of_new.push_back((int32_t)j);
+      }
+    std::vector<int32_t> new_of_old((size_t)nR);
+    for (int64_t k = 0; k < nR; ++k) new_of_old[(size_t)old_of_new[(size_t)k]] = (int32_t)k;
+    auto remap = [&](int32_t j) -> int32_t { return (j >= 0 && j < nR) ? new_of_old[(size_t)j] : j; };
+    std::vector<uint32_t> meta_n((size_t)nR), meta2_n((size_t)nR);
+    std::vector<int32_t> nbr_n((size_t)2 * D * nR), nbr2_n((size_t)2 * D * nR), perm_n((size_t)nR);
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < (long long)nR; ++k) {
+      const int64_t o = old_of_new[(size_t)k];
+      meta_n[(size_t)k] = M.r_meta[(size_t)o];
+      meta2_n[(size_t)k] = M.r_meta2[(size_t)o];
+      perm_n[(size_t)k] = M.perm[(size_t)o];
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        nbr_n[(size_t)dir * nR + k] = remap(M.r_nbr[(size_t)dir * nR + o]);
+        nbr2_n[(size_t)dir * nR + k] = remap(M.r_nbr2[(size_t)dir * nR + o]);
+      }
+    }
+#pragma omp parallel for schedule(static)
+    for (long long q = 0; q < (long long)((size_t)NS * nI); ++q) M.i_nbr[(size_t)q] = remap(M.i_nbr[(size_t)q]);
+    M.r_meta.swap(meta_n);
+    M.r_meta2.swap(meta2_n);
+    M.r_nbr.swap(nbr_n);
+    M.r_nbr2.swap(nbr2_n);
+    for (int64_t k = 0; k < nR; ++k) M.perm[(size_t)k] = perm_n[(size_t)k];
+    for (int64_t i = 0; i < N; ++i) M.iperm[(size_t)M.perm[(size_t)i]] = (int32_t)i;
+    int64_t uni_out = 0, nset = 0;
+    for (int64_t j = 0; j < nR; ++j) {
+      if (inx[(size_t)j]) ++nset;
+      else if (j < M.nU) ++uni_out;
+    }
+    M.x_first = uni_out;
+    M.x_list.resize((size_t)nset);
+    for (int64_t k = 0; k < nset; ++k) M.x_list[(size_t)k] = (int32_t)(uni_out + k);
   }
   const size_t R = T.crec.size() / 6;
   M.corr.assign((size_t)D * D * R, 0.0f);

@@ -175,6 +175,13 @@ class my_p4est_level_set_t:
                                               C.byref(out), C.byref(cnt)))
         return out.value, cnt.value
 
+    def table_stats(self):
+        """Sizes of the mixed tables: nodes, regular, uniform, irregular, extended set, classes, corrections."""
+        out = np.zeros(7, np.int64)
+        L.check(L.load().lsg_level_set_table_stats(self._h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        keys = ("nodes", "regular", "uniform", "irregular", "extended_regular", "classes", "corrections")
+        return {k: int(v) for k, v in zip(keys, out)}
+
     # ---- launch shape of the mixed stage -----------------------------------------------------------
     def autotune(self, phi, trials=3):
         """Time candidate launch shapes of the mixed stage on phi (host) and keep the fastest."""
@@ -193,21 +200,27 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_perturb_level_set_function(self._h, L.dptr(phi), float(epsilon)))
 
 
+def _cfg_dict(cfg):
+    return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2]),
+            "uniform_depth": int(cfg[3])}
+
+
 def _autotune(handle, phi, trials):
     phi = np.ascontiguousarray(phi, np.float64)
-    cfg = np.zeros(3, np.int32)
+    cfg = np.zeros(4, np.int32)
     L.check(L.load().lsg_level_set_autotune(handle, L.dptr(phi), int(trials), L.i32ptr(cfg)))
-    return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2])}
+    return _cfg_dict(cfg)
 
 
 def _stage_config(handle):
-    cfg = np.zeros(3, np.int32)
+    cfg = np.zeros(4, np.int32)
     L.check(L.load().lsg_level_set_stage_config(handle, L.i32ptr(cfg)))
-    return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2])}
+    return _cfg_dict(cfg)
 
 
 def _set_stage_config(handle, cfg):
-    arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"]], np.int32)
+    arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"], cfg.get("uniform_depth", 1)],
+                   np.int32)
     L.check(L.load().lsg_level_set_set_stage_config(handle, L.i32ptr(arr)))
 
 

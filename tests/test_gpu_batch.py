@@ -66,7 +66,8 @@ def test_autotuned_shape_keeps_results(batch2d):
     assert b.stage_config == cfg
     phi = phi0.copy()
     b.reinitialize_2nd_order(phi, 6)
-    b.stage_config = {"threads_per_block": 64, "uniform_blocks": 152, "regular_blocks": 304}
+    b.stage_config = {"threads_per_block": 64, "uniform_blocks": 152, "regular_blocks": 304,
+                      "uniform_depth": 3 - cfg["uniform_depth"]}
     phi2 = phi0.copy()
     b.reinitialize_2nd_order(phi2, 6)
     assert np.array_equal(phi, phi2)

@@ -171,3 +171,19 @@ def test_band_linf_device_matches_numpy():
     a[np.flatnonzero(m)[0]] = np.nan
     val, _ = ls.band_linf(torch.from_numpy(a).cuda(), torch.from_numpy(ref).cuda(), band)
     assert np.isnan(val)
+
+
+@pytest.mark.parametrize("shape", [(256, 0, 0, 1), (128, 912, 304, 2), (64, 152, 0, 2)])
+def test_mixed_result_independent_of_launch_shape(shape):
+    """The mixed stages are Jacobi updates: threads per block, persistent grids and the uniform kernel's
+    pipeline depth change no bit of the result."""
+    f = flower_3d(3, 6)
+    phi0 = phi0_flower_3d(f)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
+    ref = phi0.copy()
+    ls.reinitialize_2nd_order(ref, 7)
+    tpb, ub, rb, depth = shape
+    ls.stage_config = {"threads_per_block": tpb, "uniform_blocks": ub, "regular_blocks": rb, "uniform_depth": depth}
+    got = phi0.copy()
+    ls.reinitialize_2nd_order(got, 7)
+    assert np.array_equal(got, ref)
