@@ -67,6 +67,14 @@ SIGNATURES = {
     "lsg_second_derivatives_device": (_I, [_P, _P, _P]),
     "lsg_perturb_level_set_function": (_I, [_P, _DP, _D]),
     "lsg_level_set_enable_kernel_timing": (_I, [_P, _I]),
+    "lsg_first_derivatives": (_I, [_P, _DP, _DP]),
+    "lsg_first_derivatives_device": (_I, [_P, _P, _P]),
+    "lsg_compute_normals": (_I, [_P, _DP, _DP]),
+    "lsg_compute_normals_device": (_I, [_P, _P, _P]),
+    "lsg_compute_mean_curvature": (_I, [_P, _DP, _DP]),
+    "lsg_compute_mean_curvature_device": (_I, [_P, _P, _P]),
+    "lsg_compute_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP]),
+    "lsg_compute_normals_and_mean_curvature_device": (_I, [_P, _P, _P, _P]),
     "lsg_interpolate_nodes": (_I, [_P, _DP, _I64, _DP, _I, _DP, _I, _DP]),
     "lsg_interpolate_nodes_device": (_I, [_P, _P, _I64, _P, _I, _P, _I, _P]),
     "lsg_locate_points_device": (_I, [_P, _P, _I64, _P]),

@@ -151,6 +151,21 @@ void tag_levelset(const Forest<D>& F, int min_lvl, int max_lvl, double lip, doub
   }
 }
 
+// Host forms of the derivative family: inputs of n_in x N doubles, outputs of n_out x N (+ N).
+template <typename L, typename Fn>
+void host_fields(L& ls, const double* in, size_t n_in, double* out, size_t n_out, double* out2, Fn&& fn) {
+  const size_t N = (size_t)ls.N;
+  ls.ws_f.ensure(n_in * N + (n_out + (out2 ? 1 : 0)) * N + 1);
+  double* din = ls.ws_f.p;
+  double* dout = din + n_in * N;
+  double* dout2 = dout + n_out * N;
+  if (N) cuda_check(cudaMemcpyAsync(din, in, n_in * N * sizeof(double), cudaMemcpyHostToDevice, ls.stream), "H2D");
+  fn(din, dout, dout2);
+  if (N) cuda_check(cudaMemcpyAsync(out, dout, n_out * N * sizeof(double), cudaMemcpyDeviceToHost, ls.stream), "D2H");
+  if (N && out2) cuda_check(cudaMemcpyAsync(out2, dout2, N * sizeof(double), cudaMemcpyDeviceToHost, ls.stream), "D2H");
+  cuda_check(cudaStreamSynchronize(ls.stream), "sync");
+}
+
 }  // namespace
 
 extern "C" {
@@ -559,6 +574,72 @@ int lsg_perturb_level_set_function(lsg_level_set* ls, double* phi, double epsilo
       for (int64_t n = 0; n < L.N; ++n)
         if (fabs(phi[n]) < epsilon) phi[n] = (phi[n] > 0) ? epsilon : -epsilon;
     });
+  });
+}
+
+int lsg_first_derivatives(lsg_level_set* ls, const double* f, double* out) {
+  return guard([&] {
+    need(f != nullptr && out != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      const int D = ls->dim;
+      host_fields(L, f, 1, out, D, nullptr, [&](double* i, double* o, double*) { L.first_derivatives(i, o); });
+    });
+  });
+}
+
+int lsg_first_derivatives_device(lsg_level_set* ls, const double* f, double* out) {
+  return guard([&] {
+    need(f != nullptr && out != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.first_derivatives(f, out); });
+  });
+}
+
+int lsg_compute_normals(lsg_level_set* ls, const double* phi, double* normals) {
+  return guard([&] {
+    need(phi != nullptr && normals != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      host_fields(L, phi, 1, normals, ls->dim, nullptr, [&](double* i, double* o, double*) { L.compute_normals(i, o); });
+    });
+  });
+}
+
+int lsg_compute_normals_device(lsg_level_set* ls, const double* phi, double* normals) {
+  return guard([&] {
+    need(phi != nullptr && normals != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.compute_normals(phi, normals); });
+  });
+}
+
+int lsg_compute_mean_curvature(lsg_level_set* ls, const double* normals, double* kappa) {
+  return guard([&] {
+    need(normals != nullptr && kappa != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      host_fields(L, normals, ls->dim, kappa, 1, nullptr, [&](double* i, double* o, double*) { L.mean_curvature_from_normals(i, o); });
+    });
+  });
+}
+
+int lsg_compute_mean_curvature_device(lsg_level_set* ls, const double* normals, double* kappa) {
+  return guard([&] {
+    need(normals != nullptr && kappa != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.mean_curvature_from_normals(normals, kappa); });
+  });
+}
+
+int lsg_compute_normals_and_mean_curvature(lsg_level_set* ls, const double* phi, double* normals, double* kappa) {
+  return guard([&] {
+    need(phi != nullptr && normals != nullptr && kappa != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      host_fields(L, phi, 1, normals, ls->dim, kappa,
+                  [&](double* i, double* o, double* o2) { L.normals_and_mean_curvature(i, o, o2); });
+    });
+  });
+}
+
+int lsg_compute_normals_and_mean_curvature_device(lsg_level_set* ls, const double* phi, double* normals, double* kappa) {
+  return guard([&] {
+    need(phi != nullptr && normals != nullptr && kappa != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.normals_and_mean_curvature(phi, normals, kappa); });
   });
 }
 

@@ -40,6 +40,14 @@ struct DTab64 {
   const uint8_t* wall;  // N
 };
 
+// First-derivative correction records (build_gradient_tables): record index per node (-1: none),
+// D*(D-1) weights per record, and the mask of the weights that apply.
+struct DGrad {
+  const int32_t* gidx;
+  const double* grec;
+  const uint8_t* gmask;
+};
+
 // Point location and corner gathers for node interpolation (my_p4est_hierarchy_t +
 // p4est_nodes_t::local_nodes). Leaves in tree-major Morton order; ctab[t*ncoarse + c] is the
 // leaf containing the first logical point of coarse cell c (level L0) of tree t, so the leaf that
@@ -105,6 +113,22 @@ void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double*
                            double* out, const double* avg_with, cudaStream_t s);
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
 void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
+// First derivatives (FP64, the reference's expression order). fdd: second derivatives of f (D x N,
+// from launch_dd64), read only at nodes with a correction record. which: bit a -> component a.
+template <int D>
+void launch_grad64(const DTab64<D>& T, const DGrad& G, const double* f, const double* fdd, double* out, int which, cudaStream_t s);
+// n / |n| per node, 0 where |n| < EPS (compute_normals), in place on D x N
+template <int D>
+void launch_normalize64(double* g, int64_t N, cudaStream_t s);
+// kappa = sum_a d_a(n_a) (compute_mean_curvature from normals); ndd: D x D x N second derivatives
+// of the components
+template <int D>
+void launch_div64(const DTab64<D>& T, const DGrad& G, const double* nrm, const double* ndd, double* kappa, cudaStream_t s);
+// get_curvature from the gradient g (D x N), the second derivatives of phi (D x N) and of the
+// gradient components x and y (D x N each)
+template <int D>
+void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const double* phidd, const double* gxdd, const double* gydd,
+                    double* kappa, cudaStream_t s);
 // FP64 band L-infinity: out3 = {bits of max |a-b| over |b| < band, band node count, NaN flag}
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s);
 // Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p

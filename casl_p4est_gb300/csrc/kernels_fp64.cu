@@ -257,6 +257,93 @@ __global__ void k_min_cfl(const double* __restrict__ smin, const double* __restr
   if ((threadIdx.x & 31) == 0) atomicMin(out, (unsigned long long)__double_as_longlong(v));
 }
 
+// d_a f at node n: central_derivative of the linearly interpolated neighbours along a
+// (src/my_p4est_quad_neighbor_nodes_of_node.h:193-199), minus the tangential second-derivative
+// corrections that apply (correct_naive_first_derivatives, .cpp:575-640)
+template <int D>
+__device__ __forceinline__ double grad_comp64(const DTab64<D>& T, const DGrad& G, int64_t n, const double* __restrict__ f,
+                                              const double* __restrict__ fdd, int a, int32_t r) {
+  const int64_t N = T.N;
+  const double f0 = f[n];
+  const double fm = lin64<D>(T, 2 * a, n, f), fp = lin64<D>(T, 2 * a + 1, n, f);
+  const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
+  double g = ((fp - f0) * dm / dp + (f0 - fm) * dp / dm) / (dp + dm);
+  if (r >= 0) {
+    const uint8_t mask = G.gmask[r];
+#pragma unroll
+    for (int j = 0; j < D - 1; ++j) {
+      const int b = (j == 0) ? (a == 0 ? 1 : 0) : (a == 2 ? 1 : 2);
+      if ((mask >> (a * (D - 1) + j)) & 1) g -= fdd[(int64_t)b * N + n] * G.grec[(int64_t)r * (D * (D - 1)) + a * (D - 1) + j];
+    }
+  }
+  return g;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_grad64(DTab64<D> T, DGrad G, const double* __restrict__ f, const double* __restrict__ fdd,
+                                                double* __restrict__ out, int which) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= T.N) return;
+  const int32_t r = G.gidx[n];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    if ((which >> a) & 1) out[(int64_t)a * T.N + n] = grad_comp64<D>(T, G, n, f, fdd, a, r);
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_normalize64(double* __restrict__ g, int64_t N) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double s = g[n] * g[n] + g[N + n] * g[N + n];
+  if (D == 3) s = s + g[2 * N + n] * g[2 * N + n];
+  const double abs = sqrt(s);
+#pragma unroll
+  for (int a = 0; a < D; ++a) g[(int64_t)a * N + n] = abs < EPS ? 0.0 : g[(int64_t)a * N + n] / abs;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_div64(DTab64<D> T, DGrad G, const double* __restrict__ nrm, const double* __restrict__ ndd,
+                                               double* __restrict__ kappa) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const int32_t r = G.gidx[n];
+  double k = grad_comp64<D>(T, G, n, nrm, ndd, 0, r) + grad_comp64<D>(T, G, n, nrm + N, ndd + (int64_t)D * N, 1, r);
+  if (D == 3) k = k + grad_comp64<D>(T, G, n, nrm + 2 * N, ndd + (int64_t)2 * D * N, 2, r);
+  kappa[n] = k;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_kappa64(DTab64<D> T, DGrad G, const double* __restrict__ g, const double* __restrict__ phidd,
+                                                 const double* __restrict__ gxdd, const double* __restrict__ gydd,
+                                                 double* __restrict__ kappa) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const double dx = g[n], dy = g[N + n], dz = D == 3 ? g[2 * N + n] : 0.0;
+  double mag = 0.0;
+  mag += dx * dx;
+  mag += dy * dy;
+  if (D == 3) mag += dz * dz;
+  mag = sqrt(mag);
+  if (!(mag > EPS)) {
+    kappa[n] = 0.0;
+    return;
+  }
+  const int32_t r = G.gidx[n];
+  const double d0 = phidd[n], d1 = phidd[N + n];
+  const double dxy = grad_comp64<D>(T, G, n, g, gxdd, 1, r);
+  if (D == 3) {
+    const double d2 = phidd[2 * N + n];
+    const double dxz = grad_comp64<D>(T, G, n, g, gxdd, 2, r);
+    const double dyz = grad_comp64<D>(T, G, n, g + N, gydd, 2, r);
+    kappa[n] = ((d1 + d2) * (dx * dx) + (d0 + d2) * (dy * dy) + (d0 + d1) * (dz * dz) - 2.0 * (dx * dy * dxy + dx * dz * dxz + dy * dz * dyz)) /
+               (mag * mag * mag);
+  } else {
+    kappa[n] = ((d1) * (dx * dx) + (d0) * (dy * dy) - 2.0 * (dx * dy * dxy)) / (mag * mag * mag);
+  }
+}
+
 // Band L-infinity check in FP64: max |a - b| over the nodes with |b| < band (b the reference field),
 // with the number of band nodes and a NaN flag. Warp shuffles, then one shared-memory pass per block,
 // then one atomic per block; non-negative doubles order like their bit patterns, so atomicMax on the
@@ -313,6 +400,24 @@ __global__ void __launch_bounds__(TPB) k_band_linf64(const double* __restrict__ 
 inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 
 }  // namespace
+
+template <int D>
+void launch_grad64(const DTab64<D>& T, const DGrad& G, const double* f, const double* fdd, double* out, int which, cudaStream_t s) {
+  if (T.N) k_grad64<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, f, fdd, out, which);
+}
+template <int D>
+void launch_normalize64(double* g, int64_t N, cudaStream_t s) {
+  if (N) k_normalize64<D><<<nblocks(N), TPB, 0, s>>>(g, N);
+}
+template <int D>
+void launch_div64(const DTab64<D>& T, const DGrad& G, const double* nrm, const double* ndd, double* kappa, cudaStream_t s) {
+  if (T.N) k_div64<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, nrm, ndd, kappa);
+}
+template <int D>
+void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const double* phidd, const double* gxdd, const double* gydd,
+                    double* kappa, cudaStream_t s) {
+  if (T.N) k_kappa64<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, g, phidd, gxdd, gydd, kappa);
+}
 
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
   cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
@@ -381,7 +486,12 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
   template void launch_reinit_stage64<D>(const DTab64<D>&, int, const uint16_t*, const double*, const double*, const double*, \
                                          const double*, double*, const double*, cudaStream_t);                               \
   template void launch_advect_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, double,  \
-                                         double*, const double*, cudaStream_t);
+                                         double*, const double*, cudaStream_t);                                              \
+  template void launch_grad64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, int, cudaStream_t);      \
+  template void launch_normalize64<D>(double*, int64_t, cudaStream_t);                                                        \
+  template void launch_div64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, cudaStream_t);            \
+  template void launch_kappa64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,    \
+                                  double*, cudaStream_t);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

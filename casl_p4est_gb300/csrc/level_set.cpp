@@ -641,6 +641,61 @@ void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, doub
   cuda_check(cudaStreamSynchronize(stream), "reinitialize sync");
 }
 
+template <int D>
+void LevelSet<D>::build_gradient() {
+  if (grad_ready) return;
+  if (!F) throw std::invalid_argument("first derivatives need a single grid's level set, not a batch");
+  std::vector<int32_t> gidx;
+  std::vector<double> grec;
+  std::vector<uint8_t> gmask;
+  build_gradient_tables<D>(*F, gidx, grec, gmask);
+  if (grec.empty()) grec.push_back(0.0);
+  if (gmask.empty()) gmask.push_back(0);
+  g_idx.upload(gidx, stream);
+  g_rec.upload(grec, stream);
+  g_mask.upload(gmask, stream);
+  cuda_check(cudaStreamSynchronize(stream), "gradient tables upload");
+  TG.gidx = g_idx.p;
+  TG.grec = g_rec.p;
+  TG.gmask = g_mask.p;
+  grad_ready = true;
+}
+
+template <int D>
+void LevelSet<D>::first_derivatives(const double* f, double* out) {
+  build_gradient();
+  ws_gdd.ensure((size_t)D * N);
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, f, ws_gdd.p, stream));
+  LSG_LAUNCH(K_DD64, launch_grad64<D>(T64, TG, f, ws_gdd.p, out, (1 << D) - 1, stream));
+  cuda_check(cudaGetLastError(), "first_derivatives_central");
+}
+
+template <int D>
+void LevelSet<D>::compute_normals(const double* phi, double* out) {
+  first_derivatives(phi, out);
+  LSG_LAUNCH(K_CONVERT, launch_normalize64<D>(out, N, stream));
+  cuda_check(cudaGetLastError(), "compute_normals");
+}
+
+template <int D>
+void LevelSet<D>::mean_curvature_from_normals(const double* nrm, double* kappa) {
+  build_gradient();
+  ws_gdd2.ensure((size_t)D * D * N);
+  for (int a = 0; a < D; ++a) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, nrm + (size_t)a * N, ws_gdd2.p + (size_t)a * D * N, stream));
+  LSG_LAUNCH(K_DD64, launch_div64<D>(T64, TG, nrm, ws_gdd2.p, kappa, stream));
+  cuda_check(cudaGetLastError(), "compute_mean_curvature");
+}
+
+template <int D>
+void LevelSet<D>::normals_and_mean_curvature(const double* phi, double* nrm, double* kappa) {
+  first_derivatives(phi, nrm);  // ws_gdd holds the second derivatives of phi
+  ws_gdd2.ensure((size_t)D * D * N);
+  for (int a = 0; a < D - 1; ++a) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, nrm + (size_t)a * N, ws_gdd2.p + (size_t)a * D * N, stream));
+  LSG_LAUNCH(K_DD64, launch_kappa64<D>(T64, TG, nrm, ws_gdd.p, ws_gdd2.p, ws_gdd2.p + (size_t)D * N, kappa, stream));
+  LSG_LAUNCH(K_CONVERT, launch_normalize64<D>(nrm, N, stream));
+  cuda_check(cudaGetLastError(), "compute_normals_and_mean_curvature");
+}
+
 // Point location tables: sorted leaf keys and levels, local_nodes, and the coarse-cell table
 // (my_p4est_hierarchy_t's role, src/my_p4est_hierarchy.cpp:264-567).
 template <int D>

@@ -76,8 +76,15 @@ struct LevelSet {
   DevBuf<int32_t> loc_nodes, loc_ctab, loc_ijk, loc_leaf;
   DevBuf<double> loc_tmin, loc_tmax;
   DLoc<D> TL{};
+  // first-derivative correction records (built on first use)
+  bool grad_ready = false;
+  DevBuf<int32_t> g_idx;
+  DevBuf<double> g_rec;
+  DevBuf<uint8_t> g_mask;
+  DGrad TG{};
   // work vectors
   DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
+  DevBuf<double> ws_gdd, ws_gdd2;
   DevBuf<double> ws_xyz, ws_f, ws_fdd, ws_out, ws_v1, ws_v2, ws_fdd2;
   DevBuf<unsigned long long> linf_buf;
   DevBuf<uint16_t> status;
@@ -118,6 +125,15 @@ struct LevelSet {
   // reinitialize() in FP64 with no allocation: the work vectors come from a static device array
   // (reinit_fp64_static) that holds grids up to LSG_NOALLOC_SCRATCH_BYTES of scratch.
   void reinitialize_fp64_noalloc(double* phi, int os, int ot, double limit_high, double limit_low, int iterations);
+
+  // first_derivatives_central (src/my_p4est_node_neighbors.cpp:1643-1948): out = D x N gradient of f.
+  void first_derivatives(const double* f, double* out);
+  // compute_normals (src/my_p4est_utils.cpp:1717-1739): out = D x N unit normals of phi.
+  void compute_normals(const double* phi, double* out);
+  // compute_mean_curvature(neighbors, normals, kappa) (src/my_p4est_utils.cpp:1658-1696).
+  void mean_curvature_from_normals(const double* normals, double* kappa);
+  // compute_normals_and_mean_curvature (src/my_p4est_utils.cpp:2776-2802).
+  void normals_and_mean_curvature(const double* phi, double* normals, double* kappa);
 
   // my_p4est_interpolation_nodes_t: nf fields (nf x N) interpolated at np points (D doubles each)
   // with `method` (interpolation_method); Fdd (nf x D x N) may be null and is then computed with
@@ -162,6 +178,7 @@ struct LevelSet {
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
   void build_locator();
+  void build_gradient();
   const double* derivatives_of(int nf, const double* F, const double* Fdd, DevBuf<double>& store);
 };
 

@@ -92,6 +92,46 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T) {
 }
 
 template <int D>
+void build_gradient_tables(const Forest<D>& F, std::vector<int32_t>& gidx, std::vector<double>& grec, std::vector<uint8_t>& gmask) {
+  constexpr int W = D * (D - 1);
+  const int64_t N = (int64_t)F.num_nodes();
+  std::vector<double> wbuf((size_t)W * N);
+  std::vector<uint8_t> mbuf((size_t)N, 0);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long long nn = 0; nn < (long long)N; ++nn) {
+    Qnnn<D> q;
+    construct_neighbors<D>(F, (int32_t)nn, q);
+    uint8_t mask = 0;
+    for (int a = 0; a < D; ++a)
+      for (int j = 0; j < D - 1; ++j) {
+        // dd_correction_weight_to_naive_first_derivative(d_m, d_p, d_m_m, d_m_p, d_p_m, d_p_p)
+        const double d_m = q.d[2 * a], d_p = q.d[2 * a + 1];
+        const double d_m_m = q.dt[2 * a][2 * j], d_m_p = q.dt[2 * a][2 * j + 1];
+        const double d_p_m = q.dt[2 * a + 1][2 * j], d_p_p = q.dt[2 * a + 1][2 * j + 1];
+        const double w = 0.5 * (d_p_m * d_p_p * d_m / d_p - d_m_m * d_m_p * d_p / d_m) / (d_m + d_p);
+        wbuf[(size_t)nn * W + a * (D - 1) + j] = w;
+        if (!(fabs(w * q.inverse_d_max) < EPS)) mask |= (uint8_t)(1u << (a * (D - 1) + j));
+      }
+    mbuf[(size_t)nn] = mask;
+  }
+  gidx.assign((size_t)N, -1);
+  int32_t R = 0;
+  for (int64_t n = 0; n < N; ++n)
+    if (mbuf[(size_t)n]) gidx[(size_t)n] = R++;
+  grec.assign((size_t)W * R, 0.0);
+  gmask.assign((size_t)R, 0);
+  for (int64_t n = 0; n < N; ++n) {
+    const int32_t r = gidx[(size_t)n];
+    if (r < 0) continue;
+    for (int k = 0; k < W; ++k) grec[(size_t)r * W + k] = wbuf[(size_t)n * W + k];
+    gmask[(size_t)r] = mbuf[(size_t)n];
+  }
+}
+
+template void build_gradient_tables<2>(const Forest<2>&, std::vector<int32_t>&, std::vector<double>&, std::vector<uint8_t>&);
+template void build_gradient_tables<3>(const Forest<3>&, std::vector<int32_t>&, std::vector<double>&, std::vector<uint8_t>&);
+
+template <int D>
 void concat_tables64(const std::vector<const Tables64<D>*>& parts, Tables64<D>& out) {
   constexpr int H = Dim<D>::HALF;
   constexpr int NS = 2 * D * H;

@@ -51,6 +51,14 @@ struct Tables64 {
 template <int D>
 void build_tables64(const Forest<D>& F, Tables64<D>& T);
 
+// Correction records of the first derivatives (correct_naive_first_derivatives,
+// src/my_p4est_quad_neighbor_nodes_of_node.cpp:575-640): for every node whose naive central first
+// derivative along some axis a needs the second derivative along a tangential axis, gidx[n] is a
+// record index; the record holds the D*(D-1) weights dd_correction_weight_to_naive_first_derivative
+// ([a*(D-1) + j], j-th axis other than a) and gmask bit a*(D-1)+j says which are applied.
+template <int D>
+void build_gradient_tables(const Forest<D>& F, std::vector<int32_t>& gidx, std::vector<double>& grec, std::vector<uint8_t>& gmask);
+
 // Tables of the disjoint union of several grids: node indices of part k are offset by the node count
 // of the parts before it (the union's node order is the parts' node orders one after the other).
 template <int D>

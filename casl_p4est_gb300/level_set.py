@@ -165,6 +165,35 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_second_derivatives(self._h, L.dptr(phi), L.dptr(out)))
         return out
 
+    # ---- first derivatives, normals, curvature (FP64) ----------------------------------------------
+    def first_derivatives_central(self, f) -> np.ndarray:
+        """Gradient of f, (dim, N) (my_p4est_node_neighbors_t::first_derivatives_central)."""
+        f = _host_f64(np.ascontiguousarray(f, np.float64), self.num_nodes, "f")
+        out = np.empty((self.ngbd.dim, self.num_nodes), np.float64)
+        L.check(L.load().lsg_first_derivatives(self._h, L.dptr(f), L.dptr(out)))
+        return out
+
+    def compute_normals(self, phi) -> np.ndarray:
+        phi = _host_f64(np.ascontiguousarray(phi, np.float64), self.num_nodes, "phi")
+        out = np.empty((self.ngbd.dim, self.num_nodes), np.float64)
+        L.check(L.load().lsg_compute_normals(self._h, L.dptr(phi), L.dptr(out)))
+        return out
+
+    def compute_mean_curvature(self, normals) -> np.ndarray:
+        nrm = np.ascontiguousarray(normals, np.float64)
+        if nrm.size != self.ngbd.dim * self.num_nodes:
+            raise ValueError("normals must be (dim, N)")
+        out = np.empty(self.num_nodes, np.float64)
+        L.check(L.load().lsg_compute_mean_curvature(self._h, L.dptr(nrm), L.dptr(out)))
+        return out
+
+    def compute_normals_and_mean_curvature(self, phi):
+        phi = _host_f64(np.ascontiguousarray(phi, np.float64), self.num_nodes, "phi")
+        nrm = np.empty((self.ngbd.dim, self.num_nodes), np.float64)
+        kappa = np.empty(self.num_nodes, np.float64)
+        L.check(L.load().lsg_compute_normals_and_mean_curvature(self._h, L.dptr(phi), L.dptr(nrm), L.dptr(kappa)))
+        return nrm, kappa
+
     def band_linf(self, a, b, band):
         """FP64 max |a - b| over |b| < band on the device (CUDA tensors); returns (value, band node count)."""
         if not (_is_device(a) and _is_device(b)):

@@ -154,6 +154,29 @@ int lsg_second_derivatives_device(lsg_level_set* ls, const double* f_dev, double
 int lsg_perturb_level_set_function(lsg_level_set* ls, double* phi, double epsilon);
 
 /* ---- instrumentation (no reference counterpart; replaces PETSc log events) --------------------- */
+/* ---- first derivatives, normals, curvature (FP64, the reference's arithmetic) ---------------- */
+
+/* my_p4est_node_neighbors_t::first_derivatives_central (src/my_p4est_node_neighbors.cpp:1643-1948):
+ * out = dim x N gradient of f (quad_neighbor_nodes_of_node_t::gradient, central differences of the
+ * linearly interpolated neighbours with the tangential second-derivative correction,
+ * src/my_p4est_quad_neighbor_nodes_of_node.cpp:575-640). */
+int lsg_first_derivatives(lsg_level_set* ls, const double* f, double* out);
+int lsg_first_derivatives_device(lsg_level_set* ls, const double* f_dev, double* out_dev);
+/* compute_normals(neighbors, phi, normals[]) (src/my_p4est_utils.cpp:1717-1739): dim x N unit normals,
+ * 0 where |grad phi| < EPS. */
+int lsg_compute_normals(lsg_level_set* ls, const double* phi, double* normals);
+int lsg_compute_normals_device(lsg_level_set* ls, const double* phi_dev, double* normals_dev);
+/* compute_mean_curvature(neighbors, normals[], kappa) (src/my_p4est_utils.cpp:1658-1696): divergence of
+ * the normals. */
+int lsg_compute_mean_curvature(lsg_level_set* ls, const double* normals, double* kappa);
+int lsg_compute_mean_curvature_device(lsg_level_set* ls, const double* normals_dev, double* kappa_dev);
+/* compute_normals_and_mean_curvature(neighbors, phi, normals[], kappa) (src/my_p4est_utils.cpp:2776-2802):
+ * kappa from the gradient and phi (get_curvature, src/my_p4est_quad_neighbor_nodes_of_node.h:2051-2087),
+ * then the normals. */
+int lsg_compute_normals_and_mean_curvature(lsg_level_set* ls, const double* phi, double* normals, double* kappa);
+int lsg_compute_normals_and_mean_curvature_device(lsg_level_set* ls, const double* phi_dev, double* normals_dev,
+                                                  double* kappa_dev);
+
 /* ---- node interpolation and the semi-Lagrangian step (FP64) --------------------------------- */
 
 /* my_p4est_interpolation_nodes_t(ngbd) + set_input(F, Fxx, Fyy[, Fzz], method) + add_point +

@@ -808,6 +808,130 @@ void advect_normal(const Ctx& cx, const double* vn, const double* vn_np1, double
   for (int64_t n = 0; n < N; ++n) phi[n] = 0.5 * (phi_n[n] + phi_np2[n]);
 }
 
+// ---- first derivatives, normals, curvature -------------------------------------------------------
+// central_derivative and dd_correction_weight_to_naive_first_derivative
+// (src/my_p4est_quad_neighbor_nodes_of_node.h:186-199)
+inline double central_derivative(double fp, double f0, double fm, double dp, double dm) {
+  return ((fp - f0) * dm / dp + (f0 - fm) * dp / dm) / (dp + dm);
+}
+inline double dd_correction_weight(double d_m, double d_p, double d_m_m, double d_m_p, double d_p_m, double d_p_p) {
+  return 0.5 * (d_p_m * d_p_p * d_m / d_p - d_m_m * d_m_p * d_p / d_m) / (d_m + d_p);
+}
+
+// gradient / d{x,y,z}_central of f at the node: naive central differences of the linearly
+// interpolated neighbours, corrected by the second derivatives along the tangential axes where
+// the neighbours are offset (correct_naive_first_derivatives, .cpp:575-640); only the components
+// in `which` (bit a) are computed
+template <int D>
+void gradient(const Qnnn<D>& q, const double* f, double* g, int which = 7) {
+  double f0 = f[q.node_000], fnb[6];
+  for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = f_linear(q, dir, f);
+  double w[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  bool need[3][2] = {{false, false}, {false, false}, {false, false}};
+  bool any = false;
+  for (int a = 0; a < D; ++a) {
+    if (!((which >> a) & 1)) continue;
+    g[a] = central_derivative(fnb[2 * a + 1], f0, fnb[2 * a], q.d[2 * a + 1], q.d[2 * a]);
+    for (int j = 0; j < D - 1; ++j) {
+      w[a][j] = dd_correction_weight(q.d[2 * a], q.d[2 * a + 1], q.dt[2 * a][2 * j], q.dt[2 * a][2 * j + 1], q.dt[2 * a + 1][2 * j],
+                                     q.dt[2 * a + 1][2 * j + 1]);
+      need[a][j] = !check_if_zero(w[a][j] * q.inverse_d_max);
+      any = any || need[a][j];
+    }
+  }
+  if (!any) return;
+  double fdd[3] = {0, 0, 0}, fz, fn[6];
+  laplace(q, f, &fz, fn, fdd);
+  for (int a = 0; a < D; ++a) {
+    if (!((which >> a) & 1)) continue;
+    for (int j = 0; j < D - 1; ++j) {
+      const int b = (j == 0) ? (a == 0 ? 1 : 0) : (a == 2 ? 1 : 2);  // j-th axis other than a
+      if (need[a][j]) g[a] -= fdd[b] * w[a][j];
+    }
+  }
+}
+
+// first_derivatives_central (src/my_p4est_node_neighbors.cpp:1643-1948): D x N
+template <int D>
+void first_derivatives(const Ctx& cx, const double* f, double* out, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long n = 0; n < (long long)N; ++n) {
+    double g[3] = {0, 0, 0};
+    gradient<D>(Q[n], f, g);
+    for (int a = 0; a < D; ++a) out[(size_t)a * N + n] = g[a];
+  }
+}
+
+// normalisation of compute_normals (src/my_p4est_utils.cpp:1717-1739), in place on D x N
+template <int D>
+void normalize(int64_t N, double* g) {
+  for (int64_t n = 0; n < N; ++n) {
+    double s = g[n] * g[n] + g[N + n] * g[N + n];
+    if (D == 3) s = s + g[2 * N + n] * g[2 * N + n];
+    const double abs = sqrt(s);
+    for (int a = 0; a < D; ++a) g[(size_t)a * N + n] = abs < ORA_EPS ? 0 : g[(size_t)a * N + n] / abs;
+  }
+}
+
+// compute_mean_curvature(neighbors, normals, kappa) (src/my_p4est_utils.cpp:1658-1696):
+// dx_central(nx) + dy_central(ny) [+ dz_central(nz)]
+template <int D>
+void curvature_from_normals(const Ctx& cx, const double* nrm, double* kappa, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long n = 0; n < (long long)N; ++n) {
+    double gx[3], gy[3], gz[3];
+    gradient<D>(Q[n], nrm, gx, 1);
+    gradient<D>(Q[n], nrm + N, gy, 2);
+    double k = gx[0] + gy[1];
+    if (D == 3) {
+      gradient<D>(Q[n], nrm + 2 * N, gz, 4);
+      k = k + gz[2];
+    }
+    kappa[n] = k;
+  }
+}
+
+// compute_normals_and_mean_curvature (src/my_p4est_utils.cpp:2776-2802) with get_curvature from the
+// gradient and phi (src/my_p4est_quad_neighbor_nodes_of_node.h:2051-2087)
+template <int D>
+void normals_and_curvature(const Ctx& cx, const double* phi, double* nrm, double* kappa, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+  first_derivatives<D>(cx, phi, nrm, nthreads);
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long n = 0; n < (long long)N; ++n) {
+    const double dx = nrm[n], dy = nrm[N + n], dz = D == 3 ? nrm[2 * N + n] : 0.0;
+    double mag = 0.0;
+    mag += dx * dx;
+    mag += dy * dy;
+    if (D == 3) mag += dz * dz;
+    mag = sqrt(mag);
+    if (!(mag > ORA_EPS)) {
+      kappa[n] = 0.0;
+      continue;
+    }
+    double dd[3] = {0, 0, 0}, f0, fn[6];
+    laplace(Q[n], phi, &f0, fn, dd);
+    double gx[3], gy[3];
+    gradient<D>(Q[n], nrm, gx, D == 3 ? 6 : 2);  // d/dy (and d/dz) of phi_x
+    const double dxy = gx[1];
+    if (D == 3) {
+      gradient<D>(Q[n], nrm + N, gy, 4);  // d/dz of phi_y
+      const double dxz = gx[2], dyz = gy[2];
+      kappa[n] = ((dd[1] + dd[2]) * (dx * dx) + (dd[0] + dd[2]) * (dy * dy) + (dd[0] + dd[1]) * (dz * dz) -
+                  2.0 * (dx * dy * dxy + dx * dz * dxz + dy * dz * dyz)) /
+                 (mag * mag * mag);
+    } else {
+      kappa[n] = ((dd[1]) * (dx * dx) + (dd[0]) * (dy * dy) - 2.0 * (dx * dy * dxy)) / (mag * mag * mag);
+    }
+  }
+  normalize<D>(N, nrm);
+}
+
 // ---- node interpolation ------------------------------------------------------------------------
 // PI of src/casl_math.h:15
 const double ORA_PI = 3.1415926535897932384626433832795;
@@ -1275,6 +1399,43 @@ int ora_sl_advect_vortex(void* h, int64_t npts, const double* xyz, double dt, do
     if (!cx->grid) throw std::runtime_error("semi-Lagrangian step needs a grid built from leaves");
     if (cx->dim == 2) sl_advect_vortex<2>(*cx, npts, xyz, dt, vscale, phi, phi_dd, phi_method, phi_np1, nthreads);
     else sl_advect_vortex<3>(*cx, npts, xyz, dt, vscale, phi, phi_dd, phi_method, phi_np1, nthreads);
+  });
+}
+
+int ora_first_derivatives(void* h, const double* f, double* out, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) first_derivatives<2>(*cx, f, out, nthreads);
+    else first_derivatives<3>(*cx, f, out, nthreads);
+  });
+}
+
+int ora_compute_normals(void* h, const double* phi, double* out, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) {
+      first_derivatives<2>(*cx, phi, out, nthreads);
+      normalize<2>(cx->N, out);
+    } else {
+      first_derivatives<3>(*cx, phi, out, nthreads);
+      normalize<3>(cx->N, out);
+    }
+  });
+}
+
+int ora_mean_curvature_from_normals(void* h, const double* normals, double* kappa, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) curvature_from_normals<2>(*cx, normals, kappa, nthreads);
+    else curvature_from_normals<3>(*cx, normals, kappa, nthreads);
+  });
+}
+
+int ora_normals_and_mean_curvature(void* h, const double* phi, double* normals, double* kappa, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) normals_and_curvature<2>(*cx, phi, normals, kappa, nthreads);
+    else normals_and_curvature<3>(*cx, phi, normals, kappa, nthreads);
   });
 }
 

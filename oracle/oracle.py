@@ -36,6 +36,10 @@ SIG = {
     "ora_sl_advect": (_I, [_P, _I64, _DP, _D, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
     "ora_sl_advect_vortex": (_I, [_P, _I64, _DP, _D, _D, _DP, _DP, _I, _DP, _I]),
     "ora_vortex": (_I, [_I, _I64, _DP, _D, _DP]),
+    "ora_first_derivatives": (_I, [_P, _DP, _DP, _I]),
+    "ora_compute_normals": (_I, [_P, _DP, _DP, _I]),
+    "ora_mean_curvature_from_normals": (_I, [_P, _DP, _DP, _I]),
+    "ora_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP, _I]),
     "ora_interface_location": (_D, [_D, _D, _D, _D]),
     "ora_interface_location_2nd": (_D, [_D, _D, _D, _D, _D, _D]),
 }
@@ -142,6 +146,32 @@ class OracleGrid:
         out = C.c_double()
         _chk(load().ora_advect_cfl_dt(self._h, _dp(np.ascontiguousarray(vn, np.float64)), C.byref(out)))
         return out.value
+
+    # ---- first derivatives, normals, curvature ------------------------------------------------
+    def first_derivatives(self, f, nthreads=1):
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.empty((self.dim, self.N), np.float64)
+        _chk(load().ora_first_derivatives(self._h, _dp(f), _dp(out), nthreads))
+        return out
+
+    def compute_normals(self, phi, nthreads=1):
+        phi = np.ascontiguousarray(phi, np.float64)
+        out = np.empty((self.dim, self.N), np.float64)
+        _chk(load().ora_compute_normals(self._h, _dp(phi), _dp(out), nthreads))
+        return out
+
+    def mean_curvature_from_normals(self, normals, nthreads=1):
+        nrm = np.ascontiguousarray(normals, np.float64)
+        out = np.empty(self.N, np.float64)
+        _chk(load().ora_mean_curvature_from_normals(self._h, _dp(nrm), _dp(out), nthreads))
+        return out
+
+    def normals_and_mean_curvature(self, phi, nthreads=1):
+        phi = np.ascontiguousarray(phi, np.float64)
+        nrm = np.empty((self.dim, self.N), np.float64)
+        kappa = np.empty(self.N, np.float64)
+        _chk(load().ora_normals_and_mean_curvature(self._h, _dp(phi), _dp(nrm), _dp(kappa), nthreads))
+        return nrm, kappa
 
     # ---- node interpolation and the semi-Lagrangian step ------------------------------------
     def interpolate(self, method, F, xyz, Fdd=None, nthreads=1):
