@@ -643,6 +643,40 @@ int lsg_compute_normals_and_mean_curvature_device(lsg_level_set* ls, const doubl
   });
 }
 
+int lsg_extend_over_interface_tvd_device(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                         double band_extend, const double* normals, const double* mask) {
+  return guard([&] {
+    need(phi != nullptr && q != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.extend_over_interface(phi, q, iterations, order, band_use, band_extend, normals, mask); });
+  });
+}
+
+int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                  double band_extend, const double* normals, const double* mask) {
+  return guard([&] {
+    need(phi != nullptr && q != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      const int D = ls->dim;
+      const size_t N = (size_t)L.N;
+      L.ws_f.ensure((2 + (normals ? D : 0) + (mask ? 1 : 0)) * N + 1);
+      double* dphi = L.ws_f.p;
+      double* dq = dphi + N;
+      double* dn = normals ? dq + N : nullptr;
+      double* dm = mask ? dq + N + (normals ? (size_t)D * N : 0) : nullptr;
+      auto up = [&](double* dst, const double* src, size_t cnt) {
+        if (cnt) cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      };
+      up(dphi, phi, N);
+      up(dq, q, N);
+      if (dn) up(dn, normals, (size_t)D * N);
+      if (dm) up(dm, mask, N);
+      L.extend_over_interface(dphi, dq, iterations, order, band_use, band_extend, dn, dm);
+      if (N) cuda_check(cudaMemcpyAsync(q, dq, N * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H");
+      cuda_check(cudaStreamSynchronize(L.stream), "sync");
+    });
+  });
+}
+
 int lsg_interpolate_nodes(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
                           int method, double* out) {
   return guard([&] {

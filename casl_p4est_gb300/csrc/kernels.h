@@ -129,6 +129,25 @@ void launch_div64(const DTab64<D>& T, const DGrad& G, const double* nrm, const d
 template <int D>
 void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const double* phidd, const double* gxdd, const double* gydd,
                     double* kappa, cudaStream_t s);
+// extend_Over_Interface_TVD (FP64). ext_init1: normal derivative qn, gradient qx (D x N) and the
+// well-defined flag bqn (-1/+1) of every node; ext_init2: second normal derivative qnn and bqnn, from
+// the second derivatives of the normals (nrmdd, D x D x N) and of qx (qxdd, D x D x N) and the
+// edge-diagonal neighbours cnb; ext_march: one upwind marching step of v into tmp on the nodes with
+// b > 0 and phi < band_extend (minus src when given); ext_q: one marching step of q with the order-2
+// minmod correction from qdd.
+template <int D>
+void launch_ext_init1(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
+                      const double* nrm, double band_use, double* qx, double* qn, int8_t* bqn, cudaStream_t s);
+template <int D>
+void launch_ext_init2(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
+                      const double* nrm, const double* nrmdd, const double* qx, const double* qxdd, const int8_t* bqn, const int32_t* cnb,
+                      double band_use, double* qnn, int8_t* bqnn, cudaStream_t s);
+template <int D>
+void launch_ext_march(const DTab64<D>& T, const double* v, double* tmp, const int8_t* b, const double* phi, const double* nrm,
+                      const double* src, double band_extend, cudaStream_t s);
+template <int D>
+void launch_ext_q(const DTab64<D>& T, const double* q, double* tmp, const double* qdd, const double* phi, const double* mask,
+                  const double* nrm, const double* qn, int order, double band_extend, cudaStream_t s);
 // FP64 band L-infinity: out3 = {bits of max |a-b| over |b| < band, band node count, NaN flag}
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s);
 // Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p

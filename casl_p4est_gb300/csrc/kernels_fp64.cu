@@ -344,6 +344,212 @@ __global__ void __launch_bounds__(TPB) k_kappa64(DTab64<D> T, DGrad G, const dou
   }
 }
 
+// ---- extend_Over_Interface_TVD (src/my_p4est_level_set.cpp:969-1764) ------------------------------
+// is_stencil_in_negative_domain (src/my_p4est_quad_neighbor_nodes_of_node.h:2492-2530): the node and
+// every face node with a nonzero interpolation weight below -EPS
+template <int D>
+__device__ __forceinline__ bool stencil_negative64(const DTab64<D>& T, int64_t n, const double* __restrict__ f) {
+  constexpr int NS = 2 * D * Dim<D>::HALF;
+  if (!(f[n] < -EPS)) return false;
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    const int32_t j = T.nbr[(int64_t)sl * T.N + n];
+    if (j >= 0 && !(f[j] < -EPS)) return false;
+  }
+  return true;
+}
+template <int D>
+__device__ __forceinline__ bool stencil_negative_flag(const DTab64<D>& T, int64_t n, const int8_t* __restrict__ b) {
+  constexpr int NS = 2 * D * Dim<D>::HALF;
+  if (!(b[n] < 0)) return false;
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    const int32_t j = T.nbr[(int64_t)sl * T.N + n];
+    if (j >= 0 && !(b[j] < 0)) return false;
+  }
+  return true;
+}
+
+template <int D>
+__device__ __forceinline__ double ext_dt(const DTab64<D>& T, int64_t n) {
+  const int64_t N = T.N;
+  auto d = [&](int dir) { return fabs(T.d[(int64_t)dir * N + n]); };
+  const double m = D == 3 ? min2(min3(d(0), d(2), d(4)), min3(d(1), d(3), d(5))) : min2(min2(d(0), d(2)), min2(d(1), d(3)));
+  return m / double(D);
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_ext_init1(DTab64<D> T, DGrad G, const double* __restrict__ phi, const double* __restrict__ mask,
+                                                   const double* __restrict__ q, const double* __restrict__ qdd, const double* __restrict__ nrm,
+                                                   double band_use, double* __restrict__ qx, double* __restrict__ qn, int8_t* __restrict__ bqn) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  if (phi[n] > band_use && stencil_negative64<D>(T, n, mask)) {
+    const int32_t r = G.gidx[n];
+    double g[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      g[a] = grad_comp64<D>(T, G, n, q, qdd, a, r);
+      qx[(int64_t)a * N + n] = g[a];
+    }
+    double s = nrm[n] * g[0] + nrm[N + n] * g[1];
+    if (D == 3) s = s + nrm[2 * N + n] * g[2];
+    qn[n] = s;
+    bqn[n] = -1;
+  } else {
+    bqn[n] = phi[n] > band_use ? 1 : -1;
+    qn[n] = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) qx[(int64_t)a * N + n] = 0;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const double* __restrict__ phi, const double* __restrict__ mask,
+                                                   const double* __restrict__ q, const double* __restrict__ qdd, const double* __restrict__ nrm,
+                                                   const double* __restrict__ nrmdd, const double* __restrict__ qx,
+                                                   const double* __restrict__ qxdd, const int8_t* __restrict__ bqn,
+                                                   const int32_t* __restrict__ cnb, double band_use, double* __restrict__ qnn,
+                                                   int8_t* __restrict__ bqnn) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  if (!(phi[n] > band_use)) {
+    bqnn[n] = -1;
+    qnn[n] = 0;
+    return;
+  }
+  if (!stencil_negative64<D>(T, n, mask)) {
+    bqnn[n] = 1;
+    qnn[n] = 0;
+    return;
+  }
+  const int32_t r = G.gidx[n];
+  const int64_t DN = (int64_t)D * N;
+  double Qxy = 0, Qyz = 0, Qzx = 0;
+  bool ok = false;
+  if (stencil_negative_flag<D>(T, n, bqn)) {
+    ok = true;
+    Qxy = .5 * (grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 0, r) + grad_comp64<D>(T, G, n, qx, qxdd, 1, r));
+    if (D == 3) {
+      Qyz = .5 * (grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 1, r) + grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 2, r));
+      Qzx = .5 * (grad_comp64<D>(T, G, n, qx, qxdd, 2, r) + grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 0, r));
+    }
+  } else {
+    constexpr int K = D == 3 ? 12 : 4;
+    int32_t nb[K];
+    bool exist = true;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      nb[k] = cnb[(int64_t)k * N + n];
+      exist = exist && nb[k] >= 0;
+    }
+    if (exist) {
+      bool neg = true;
+#pragma unroll
+      for (int k = 0; k < K; ++k) neg = neg && mask[nb[k]] < 0;
+      if (neg) {
+        const double dx = T.d[n] + T.d[N + n], dy = T.d[2 * N + n] + T.d[3 * N + n];
+        const int mm0 = D == 3 ? 8 : 0, pm0 = D == 3 ? 9 : 1, mp0 = D == 3 ? 10 : 2, pp0 = D == 3 ? 11 : 3;
+        Qxy = (q[nb[pp0]] + q[nb[mm0]] - q[nb[mp0]] - q[nb[pm0]]) / dx / dy;
+        if (D == 3) {
+          const double dz = T.d[4 * N + n] + T.d[5 * N + n];
+          Qyz = (q[nb[7]] + q[nb[4]] - q[nb[6]] - q[nb[5]]) / dy / dz;
+          Qzx = (q[nb[3]] + q[nb[0]] - q[nb[1]] - q[nb[2]]) / dz / dx;
+        }
+        ok = true;
+      }
+    }
+  }
+  if (!ok) {
+    bqnn[n] = 1;
+    qnn[n] = 0;
+    return;
+  }
+  bqnn[n] = -1;
+  // dxx_central etc. of q: central second differences of the quadratically corrected neighbours
+  // (x_ngbd_with_quadratic_interpolation, src/my_p4est_quad_neighbor_nodes_of_node.cpp:365-390)
+  double Dq[D], Qaa[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) Dq[a] = qdd[(int64_t)a * N + n];
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double fp = quad_nb64<D>(T, 2 * a + 1, n, q, Dq), fm = quad_nb64<D>(T, 2 * a, n, q, Dq);
+    const double dp = T.d[(int64_t)(2 * a + 1) * N + n], dm = T.d[(int64_t)(2 * a) * N + n];
+    Qaa[a] = ((fp - q[n]) / dp + (fm - q[n]) / dm) * 2. / (dp + dm);
+  }
+  const double Qx = qx[n], Qy = qx[N + n];
+  const double Nx = nrm[n], Ny = nrm[N + n];
+  const double Nxx = grad_comp64<D>(T, G, n, nrm, nrmdd, 0, r), Nyx = grad_comp64<D>(T, G, n, nrm + N, nrmdd + DN, 0, r);
+  const double Nxy = grad_comp64<D>(T, G, n, nrm, nrmdd, 1, r), Nyy = grad_comp64<D>(T, G, n, nrm + N, nrmdd + DN, 1, r);
+  if (D == 3) {
+    const double Qz = qx[2 * N + n], Nz = nrm[2 * N + n];
+    const double Nzx = grad_comp64<D>(T, G, n, nrm + 2 * N, nrmdd + 2 * DN, 0, r);
+    const double Nzy = grad_comp64<D>(T, G, n, nrm + 2 * N, nrmdd + 2 * DN, 1, r);
+    const double Nxz = grad_comp64<D>(T, G, n, nrm, nrmdd, 2, r), Nyz = grad_comp64<D>(T, G, n, nrm + N, nrmdd + DN, 2, r);
+    const double Nzz = grad_comp64<D>(T, G, n, nrm + 2 * N, nrmdd + 2 * DN, 2, r);
+    qnn[n] = Nx * (Nx * Qaa[0] + 2. * Ny * Qxy + Qx * Nxx + Qy * Nyx + Qz * Nzx) +
+             Ny * (Ny * Qaa[1] + 2. * Nz * Qyz + Qx * Nxy + Qy * Nyy + Qz * Nzy) +
+             Nz * (Nz * Qaa[D == 3 ? 2 : 0] + 2. * Nx * Qzx + Qx * Nxz + Qy * Nyz + Qz * Nzz);
+  } else {
+    qnn[n] = Nx * (Nx * Qaa[0] + 2. * Ny * Qxy + Qx * Nxx + Qy * Nyx) + Ny * (Ny * Qaa[1] + Qx * Nxy + Qy * Nyy);
+  }
+}
+
+template <int D, bool SRC>
+__global__ void __launch_bounds__(TPB) k_ext_march(DTab64<D> T, const double* __restrict__ v, double* __restrict__ tmp,
+                                                   const int8_t* __restrict__ b, const double* __restrict__ phi,
+                                                   const double* __restrict__ nrm, const double* __restrict__ src, double band_extend) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  if (!(b[n] > 0 && phi[n] < band_extend)) return;
+  const double dt = ext_dt<D>(T, n);
+  double g[3];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    g[a] = nrm[(int64_t)a * N + n] > 0 ? (v[n] - lin64<D>(T, 2 * a, n, v)) / T.d[(int64_t)(2 * a) * N + n]
+                                        : (lin64<D>(T, 2 * a + 1, n, v) - v[n]) / T.d[(int64_t)(2 * a + 1) * N + n];
+  double s = nrm[n] * g[0] + nrm[N + n] * g[1];
+  if (D == 3) s = s + nrm[2 * N + n] * g[2];
+  tmp[n] = SRC ? v[n] - dt * (s - src[n]) : v[n] - dt * s;
+}
+
+template <int D, int ORDER>
+__global__ void __launch_bounds__(TPB) k_ext_q(DTab64<D> T, const double* __restrict__ q, double* __restrict__ tmp,
+                                               const double* __restrict__ qdd, const double* __restrict__ phi, const double* __restrict__ mask,
+                                               const double* __restrict__ nrm, const double* __restrict__ qn, double band_extend) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  if (!(mask[n] > -EPS && phi[n] < band_extend)) return;
+  const double dt = ext_dt<D>(T, n);
+  double g[3];
+#pragma unroll
+  for (int a = 0; a < D; ++a)
+    g[a] = nrm[(int64_t)a * N + n] > 0 ? (q[n] - lin64<D>(T, 2 * a, n, q)) / T.d[(int64_t)(2 * a) * N + n]
+                                        : (lin64<D>(T, 2 * a + 1, n, q) - q[n]) / T.d[(int64_t)(2 * a + 1) * N + n];
+  if (ORDER == 2) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const double* qaa = qdd + (int64_t)a * N;
+      const double c = qaa[n];
+      double qm = lin64<D>(T, 2 * a, n, qaa), qp = lin64<D>(T, 2 * a + 1, n, qaa);
+      qm = c * qm < 0 ? 0 : (fabs(c) < fabs(qm) ? c : qm);
+      qp = c * qp < 0 ? 0 : (fabs(c) < fabs(qp) ? c : qp);
+      if (nrm[(int64_t)a * N + n] < 0)
+        g[a] -= .5 * T.d[(int64_t)(2 * a + 1) * N + n] * qp;
+      else
+        g[a] += .5 * T.d[(int64_t)(2 * a) * N + n] * qm;
+    }
+  }
+  double s = nrm[n] * g[0] + nrm[N + n] * g[1];
+  if (D == 3) s = s + nrm[2 * N + n] * g[2];
+  const double change = dt * (s - (ORDER >= 1 ? qn[n] : 0));
+  tmp[n] = q[n] - change;
+}
+
 // Band L-infinity check in FP64: max |a - b| over the nodes with |b| < band (b the reference field),
 // with the number of band nodes and a NaN flag. Warp shuffles, then one shared-memory pass per block,
 // then one atomic per block; non-negative doubles order like their bit patterns, so atomicMax on the
@@ -419,6 +625,38 @@ void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const d
   if (T.N) k_kappa64<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, g, phidd, gxdd, gydd, kappa);
 }
 
+template <int D>
+void launch_ext_init1(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
+                      const double* nrm, double band_use, double* qx, double* qn, int8_t* bqn, cudaStream_t s) {
+  if (T.N) k_ext_init1<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, band_use, qx, qn, bqn);
+}
+template <int D>
+void launch_ext_init2(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
+                      const double* nrm, const double* nrmdd, const double* qx, const double* qxdd, const int8_t* bqn, const int32_t* cnb,
+                      double band_use, double* qnn, int8_t* bqnn, cudaStream_t s) {
+  if (T.N) k_ext_init2<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, bqn, cnb, band_use, qnn, bqnn);
+}
+template <int D>
+void launch_ext_march(const DTab64<D>& T, const double* v, double* tmp, const int8_t* b, const double* phi, const double* nrm,
+                      const double* src, double band_extend, cudaStream_t s) {
+  if (!T.N) return;
+  if (src)
+    k_ext_march<D, true><<<nblocks(T.N), TPB, 0, s>>>(T, v, tmp, b, phi, nrm, src, band_extend);
+  else
+    k_ext_march<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, v, tmp, b, phi, nrm, src, band_extend);
+}
+template <int D>
+void launch_ext_q(const DTab64<D>& T, const double* q, double* tmp, const double* qdd, const double* phi, const double* mask,
+                  const double* nrm, const double* qn, int order, double band_extend, cudaStream_t s) {
+  if (!T.N) return;
+  if (order == 2)
+    k_ext_q<D, 2><<<nblocks(T.N), TPB, 0, s>>>(T, q, tmp, qdd, phi, mask, nrm, qn, band_extend);
+  else if (order == 1)
+    k_ext_q<D, 1><<<nblocks(T.N), TPB, 0, s>>>(T, q, tmp, qdd, phi, mask, nrm, qn, band_extend);
+  else
+    k_ext_q<D, 0><<<nblocks(T.N), TPB, 0, s>>>(T, q, tmp, qdd, phi, mask, nrm, qn, band_extend);
+}
+
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
   cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
   if (n == 0) return;
@@ -491,7 +729,16 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
   template void launch_normalize64<D>(double*, int64_t, cudaStream_t);                                                        \
   template void launch_div64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, cudaStream_t);            \
   template void launch_kappa64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,    \
-                                  double*, cudaStream_t);
+                                  double*, cudaStream_t);                                                                     \
+  template void launch_ext_init1<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,  \
+                                    const double*, double, double*, double*, int8_t*, cudaStream_t);                          \
+  template void launch_ext_init2<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,  \
+                                    const double*, const double*, const double*, const double*, const int8_t*, const int32_t*, \
+                                    double, double*, int8_t*, cudaStream_t);                                                  \
+  template void launch_ext_march<D>(const DTab64<D>&, const double*, double*, const int8_t*, const double*, const double*,     \
+                                    const double*, double, cudaStream_t);                                                     \
+  template void launch_ext_q<D>(const DTab64<D>&, const double*, double*, const double*, const double*, const double*,         \
+                                const double*, const double*, int, double, cudaStream_t);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

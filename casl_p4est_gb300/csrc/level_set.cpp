@@ -696,6 +696,76 @@ void LevelSet<D>::normals_and_mean_curvature(const double* phi, double* nrm, dou
   cuda_check(cudaGetLastError(), "compute_normals_and_mean_curvature");
 }
 
+template <int D>
+void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterations, int order, double band_use, double band_extend,
+                                        const double* normals, const double* mask) {
+  if (order < 0 || order > 2) throw std::invalid_argument("extend_Over_Interface_TVD: order must be 0, 1 or 2.");
+  if (iterations < 0) throw std::invalid_argument("extend_Over_Interface_TVD: negative number of iterations");
+  build_gradient();
+  if (band_use > 0) band_use = -band_use;
+  if (!mask) mask = phi;
+  const size_t n = (size_t)N;
+  // layout of ext_buf: normals D | qx D | qn | qnn | tmp | qdd D | nrmdd D*D | qxdd D*D
+  ext_buf.ensure((size_t)(2 * D + 3 + D + 2 * D * D) * n + 1);
+  double* nrm_own = ext_buf.p;
+  double* qx = nrm_own + (size_t)D * n;
+  double* qn = qx + (size_t)D * n;
+  double* qnn = qn + n;
+  double* tmp = qnn + n;
+  double* qdd = tmp + n;
+  double* nrmdd = qdd + (size_t)D * n;
+  double* qxdd = nrmdd + (size_t)D * D * n;
+  ext_b1.ensure(n + 1);
+  ext_b2.ensure(n + 1);
+  const double* nrm = normals;
+  if (!nrm) {
+    compute_normals(phi, nrm_own);
+    nrm = nrm_own;
+  }
+  if (order >= 1) {
+    LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, q, qdd, stream));
+    LSG_LAUNCH(K_DD64, launch_ext_init1<D>(T64, TG, phi, mask, q, qdd, nrm, band_use, qx, qn, ext_b1.p, stream));
+  }
+  if (order == 2) {
+    if (!cnb.p) {
+      std::vector<int32_t> c;
+      build_corner_neighbors<D>(*F, c);
+      cnb.upload(c, stream);
+    }
+    for (int a = 0; a < D; ++a) {
+      LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, nrm + (size_t)a * n, nrmdd + (size_t)a * D * n, stream));
+      LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qx + (size_t)a * n, qxdd + (size_t)a * D * n, stream));
+    }
+    LSG_LAUNCH(K_DD64, launch_ext_init2<D>(T64, TG, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, ext_b1.p, cnb.p, band_use, qnn, ext_b2.p,
+                                           stream));
+  }
+  // marching: ping-pong between a field and tmp; nodes not marched keep their value in both
+  auto march = [&](double* v, const int8_t* b, const double* src) {
+    double* a = v;
+    double* t = tmp;
+    cuda_check(cudaMemcpyAsync(t, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    for (int it = 0; it < iterations; ++it) {
+      LSG_LAUNCH(K_ADVECT64, launch_ext_march<D>(T64, a, t, b, phi, nrm, src, band_extend, stream));
+      std::swap(a, t);
+    }
+    if (a != v) cuda_check(cudaMemcpyAsync(v, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  };
+  if (order == 2) march(qnn, ext_b2.p, nullptr);
+  if (order >= 1) march(qn, ext_b1.p, order == 2 ? qnn : nullptr);
+  {
+    double* a = q;
+    double* t = tmp;
+    cuda_check(cudaMemcpyAsync(t, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    for (int it = 0; it < iterations; ++it) {
+      if (order == 2) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, a, qdd, stream));
+      LSG_LAUNCH(K_ADVECT64, launch_ext_q<D>(T64, a, t, qdd, phi, mask, nrm, qn, order, band_extend, stream));
+      std::swap(a, t);
+    }
+    if (a != q) cuda_check(cudaMemcpyAsync(q, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  }
+  cuda_check(cudaGetLastError(), "extend_Over_Interface_TVD");
+}
+
 // Point location tables: sorted leaf keys and levels, local_nodes, and the coarse-cell table
 // (my_p4est_hierarchy_t's role, src/my_p4est_hierarchy.cpp:264-567).
 template <int D>

@@ -76,6 +76,10 @@ struct LevelSet {
   DevBuf<int32_t> loc_nodes, loc_ctab, loc_ijk, loc_leaf;
   DevBuf<double> loc_tmin, loc_tmax;
   DLoc<D> TL{};
+  // edge-diagonal neighbours for the order-2 extension (built on first use)
+  DevBuf<int32_t> cnb;
+  DevBuf<int8_t> ext_b1, ext_b2;
+  DevBuf<double> ext_buf;
   // first-derivative correction records (built on first use)
   bool grad_ready = false;
   DevBuf<int32_t> g_idx;
@@ -134,6 +138,13 @@ struct LevelSet {
   void mean_curvature_from_normals(const double* normals, double* kappa);
   // compute_normals_and_mean_curvature (src/my_p4est_utils.cpp:2776-2802).
   void normals_and_mean_curvature(const double* phi, double* normals, double* kappa);
+
+  // extend_Over_Interface_TVD(phi, q, iterations, order, band_use, band_extend, normal, mask)
+  // (src/my_p4est_level_set.cpp:969-1764) without boundary conditions or initial guesses, one-step
+  // extrapolation: q (device, N) is extended from the region phi < 0 (or mask < 0) along the normals.
+  // normals (D x N) and mask (N) may be null (computed from phi / taken as phi).
+  void extend_over_interface(const double* phi, double* q, int iterations, int order, double band_use, double band_extend,
+                             const double* normals, const double* mask);
 
   // my_p4est_interpolation_nodes_t: nf fields (nf x N) interpolated at np points (D doubles each)
   // with `method` (interpolation_method); Fdd (nf x D x N) may be null and is then computed with

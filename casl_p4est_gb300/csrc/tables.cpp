@@ -132,6 +132,52 @@ template void build_gradient_tables<2>(const Forest<2>&, std::vector<int32_t>&, 
 template void build_gradient_tables<3>(const Forest<3>&, std::vector<int32_t>&, std::vector<double>&, std::vector<uint8_t>&);
 
 template <int D>
+void build_corner_neighbors(const Forest<D>& F, std::vector<int32_t>& out) {
+  constexpr int CH = Dim<D>::CHILDREN;
+  constexpr int K = D == 3 ? 12 : 4;
+  const int64_t N = (int64_t)F.num_nodes();
+  out.assign((size_t)K * N, -1);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long long nn = 0; nn < (long long)N; ++nn) {
+    const int32_t n = (int32_t)nn;
+    // the 2^D diagonal cells, index bit a set for the + side along a
+    int32_t cell[8];
+    for (int v = 0; v < CH; ++v) {
+      const int c[3] = {(v & 1) ? 1 : -1, (v & 2) ? 1 : -1, (v & 4) ? 1 : -1};
+      int32_t quad, tree;
+      find_neighbor_cell_of_node<D>(F, n, c, quad, tree);
+      cell[v] = quad;
+    }
+    auto node = [&](int32_t quad, int v) { return F.local_nodes[(size_t)quad * CH + v]; };
+    auto pick = [&](int c1, int v1, int c2, int v2) -> int32_t {
+      return cell[c1] >= 0 ? node(cell[c1], v1) : (cell[c2] >= 0 ? node(cell[c2], v2) : -1);
+    };
+    int32_t r[12];
+    if (D == 2) {
+      for (int v = 0; v < 4; ++v) r[v] = cell[v] >= 0 ? node(cell[v], v) : -1;
+    } else {
+      // cells: mmm=0 pmm=1 mpm=2 ppm=3 mmp=4 pmp=5 mpp=6 ppp=7; corners v = x + 2y + 4z
+      r[0] = pick(0, 2, 2, 0);    // m0m
+      r[1] = pick(1, 3, 3, 1);    // p0m
+      r[2] = pick(4, 6, 6, 4);    // m0p
+      r[3] = pick(5, 7, 7, 5);    // p0p
+      r[4] = pick(0, 1, 1, 0);    // 0mm
+      r[5] = pick(2, 3, 3, 2);    // 0pm
+      r[6] = pick(4, 5, 5, 4);    // 0mp
+      r[7] = pick(6, 7, 7, 6);    // 0pp
+      r[8] = pick(0, 4, 4, 0);    // mm0
+      r[9] = pick(1, 5, 5, 1);    // pm0
+      r[10] = pick(2, 6, 6, 2);   // mp0
+      r[11] = pick(3, 7, 7, 3);   // pp0
+    }
+    for (int k = 0; k < K; ++k) out[(size_t)k * N + n] = r[k];
+  }
+}
+
+template void build_corner_neighbors<2>(const Forest<2>&, std::vector<int32_t>&);
+template void build_corner_neighbors<3>(const Forest<3>&, std::vector<int32_t>&);
+
+template <int D>
 void concat_tables64(const std::vector<const Tables64<D>*>& parts, Tables64<D>& out) {
   constexpr int H = Dim<D>::HALF;
   constexpr int NS = 2 * D * H;

@@ -59,6 +59,12 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T);
 template <int D>
 void build_gradient_tables(const Forest<D>& F, std::vector<int32_t>& gidx, std::vector<double>& grec, std::vector<uint8_t>& gmask);
 
+// Edge-diagonal neighbours of every node as my_p4est_node_neighbors_t::get_all_neighbors finds them
+// (src/my_p4est_node_neighbors.cpp:2001-2153): 3D m0m p0m m0p p0p 0mm 0pm 0mp 0pp mm0 pm0 mp0 pp0,
+// 2D mm0 pm0 mp0 pp0; -1 where absent. [k * N + n].
+template <int D>
+void build_corner_neighbors(const Forest<D>& F, std::vector<int32_t>& out);
+
 // Tables of the disjoint union of several grids: node indices of part k are offset by the node count
 // of the parts before it (the union's node order is the parts' node orders one after the other).
 template <int D>

@@ -194,6 +194,20 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_compute_normals_and_mean_curvature(self._h, L.dptr(phi), L.dptr(nrm), L.dptr(kappa)))
         return nrm, kappa
 
+    def extend_Over_Interface_TVD(self, phi, q, iterations=20, order=2, band_use=-DBL_MAX, band_extend=DBL_MAX,
+                                  normal=None, mask=None):
+        """Extend q (updated in place) from phi < 0 (or mask < 0) along the normals (FP64)."""
+        if order not in (0, 1, 2):
+            raise ValueError("[CASL_ERROR]: my_p4est_level_set_t->extend_Over_Interface_TVD: order must be 0, 1 or 2.")
+        n = self.num_nodes
+        phi = _host_f64(np.ascontiguousarray(phi, np.float64), n, "phi")
+        _host_f64(q, n, "q")
+        nrm = None if normal is None else np.ascontiguousarray(normal, np.float64)
+        msk = None if mask is None else _host_f64(np.ascontiguousarray(mask, np.float64), n, "mask")
+        L.check(L.load().lsg_extend_over_interface_tvd(self._h, L.dptr(phi), L.dptr(q), int(iterations), int(order), float(band_use),
+                                                       float(band_extend), L.dptr(nrm) if nrm is not None else None,
+                                                       L.dptr(msk) if msk is not None else None))
+
     def band_linf(self, a, b, band):
         """FP64 max |a - b| over |b| < band on the device (CUDA tensors); returns (value, band node count)."""
         if not (_is_device(a) and _is_device(b)):

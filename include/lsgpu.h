@@ -177,6 +177,21 @@ int lsg_compute_normals_and_mean_curvature(lsg_level_set* ls, const double* phi,
 int lsg_compute_normals_and_mean_curvature_device(lsg_level_set* ls, const double* phi_dev, double* normals_dev,
                                                   double* kappa_dev);
 
+/* ---- extension over the interface (FP64, the reference's arithmetic) ------------------------ */
+
+/* my_p4est_level_set_t::extend_Over_Interface_TVD(phi, q, iterations, order, band_use, band_extend,
+ * normal, mask) (src/my_p4est_level_set.h:732-735, src/my_p4est_level_set.cpp:969-1764) with no
+ * boundary conditions, no initial guesses (use_nonzero_guess false, q_n and q_nn NULL) and one-step
+ * extrapolation: q (N values) is extended in place from the region where mask < 0 along the normals
+ * by `iterations` upwind pseudo-time steps of the constant (order 0), linear (order 1) or quadratic
+ * (order 2) extension. normals (dim x N) may be NULL (computed from phi as compute_normals does);
+ * mask (N) may be NULL (phi is used). The reference's defaults are band_use = -DBL_MAX and
+ * band_extend = DBL_MAX. */
+int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                  double band_extend, const double* normals, const double* mask);
+int lsg_extend_over_interface_tvd_device(lsg_level_set* ls, const double* phi_dev, double* q_dev, int iterations, int order,
+                                         double band_use, double band_extend, const double* normals_dev, const double* mask_dev);
+
 /* ---- node interpolation and the semi-Lagrangian step (FP64) --------------------------------- */
 
 /* my_p4est_interpolation_nodes_t(ngbd) + set_input(F, Fxx, Fyy[, Fzz], method) + add_point +

@@ -9,6 +9,8 @@
  *   perturb_level_set_function(Vec phi, epsilon)                       src/my_p4est_level_set.h:621
  *   advect_in_normal_direction(CF / Vec vn[, Vec vn_np1], Vec phi, dt, phi_xx, phi_yy[, phi_zz])
  *                                                                      src/my_p4est_level_set.h:632-659
+ *   extend_Over_Interface_TVD(phi, q, iterations, order, band_use, band_extend, normal, mask)
+ *                                                                      src/my_p4est_level_set.h:732-735
  *   my_p4est_interpolation_nodes_t: set_input, add_point, interpolate  src/my_p4est_interpolation_nodes.h:33-103
  *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1                   src/my_p4est_semi_lagrangian.h:83-196
  *
@@ -176,6 +178,28 @@ class my_p4est_level_set_t {
   void perturb_level_set_function(Vec phi, const double& epsilon) const {
     lsgpu::VecArray p(phi);
     lsgpu::check(lsg_perturb_level_set_function(ngbd_->device(), p.p, epsilon));
+  }
+
+  // boundary conditions and initial guesses are not supported: passing them raises std::invalid_argument
+  template <typename BC = void>
+  void extend_Over_Interface_TVD(Vec phi, Vec q, int iterations = 20, int order = 2, double band_use = -DBL_MAX,
+                                 double band_extend = DBL_MAX, Vec normal[] = nullptr, Vec mask = nullptr, BC* bc = nullptr,
+                                 bool use_nonzero_guess = false, Vec q_n = nullptr, Vec q_nn = nullptr) const {
+    if (bc != nullptr || use_nonzero_guess || q_n != nullptr || q_nn != nullptr)
+      throw std::invalid_argument("extend_Over_Interface_TVD: boundary conditions and initial guesses are not supported");
+    lsgpu::VecArray p(phi), v(q), m(mask);
+    const int D = ngbd_->dim();
+    const size_t N = (size_t)ngbd_->num_nodes();
+    std::vector<double> nrm;
+    if (normal != nullptr) {
+      nrm.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(normal[a]);
+        for (size_t n = 0; n < N; ++n) nrm[a * N + n] = x.p[n];
+      }
+    }
+    lsgpu::check(lsg_extend_over_interface_tvd(ngbd_->device(), p.p, v.p, iterations, order, band_use, band_extend,
+                                               normal ? nrm.data() : nullptr, mask ? m.p : nullptr));
   }
 
   // node-sampled velocity: returns dt unchanged

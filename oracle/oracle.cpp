@@ -932,6 +932,248 @@ void normals_and_curvature(const Ctx& cx, const double* phi, double* nrm, double
   normalize<D>(N, nrm);
 }
 
+// ---- extension over the interface -------------------------------------------------------------
+// edge-diagonal neighbours of get_all_neighbors (src/my_p4est_node_neighbors.cpp:2001-2153), in the
+// order 3D: m0m p0m m0p p0p 0mm 0pm 0mp 0pp mm0 pm0 mp0 pp0; 2D: mm0 pm0 mp0 pp0; -1 if absent
+template <int D>
+void corner_neighbors(const Grid<D>& g, int32_t n, int32_t* out) {
+  auto cell = [&](int i, int j, int k) {
+    const int c[3] = {i, j, k};
+    return find_neighbor_cell_of_node(g, n, c);
+  };
+  auto node = [&](int32_t quad, int v) { return g.local_nodes[(size_t)quad * Grid<D>::CH + v]; };
+  if (D == 2) {
+    const int32_t mm = cell(-1, -1, 0), pm = cell(1, -1, 0), mp = cell(-1, 1, 0), pp = cell(1, 1, 0);
+    out[0] = mm >= 0 ? node(mm, 0) : -1;
+    out[1] = pm >= 0 ? node(pm, 1) : -1;
+    out[2] = mp >= 0 ? node(mp, 2) : -1;
+    out[3] = pp >= 0 ? node(pp, 3) : -1;
+    return;
+  }
+  const int32_t mmm = cell(-1, -1, -1), mpm = cell(-1, 1, -1), pmm = cell(1, -1, -1), ppm = cell(1, 1, -1);
+  const int32_t mmp = cell(-1, -1, 1), mpp = cell(-1, 1, 1), pmp = cell(1, -1, 1), ppp = cell(1, 1, 1);
+  auto pick = [&](int32_t q1, int v1, int32_t q2, int v2) { return q1 >= 0 ? node(q1, v1) : (q2 >= 0 ? node(q2, v2) : -1); };
+  out[0] = pick(mmm, 2, mpm, 0);   // m0m
+  out[1] = pick(pmm, 3, ppm, 1);   // p0m
+  out[2] = pick(mmp, 6, mpp, 4);   // m0p
+  out[3] = pick(pmp, 7, ppp, 5);   // p0p
+  out[4] = pick(mmm, 1, pmm, 0);   // 0mm
+  out[5] = pick(mpm, 3, ppm, 2);   // 0pm
+  out[6] = pick(mmp, 5, pmp, 4);   // 0mp
+  out[7] = pick(mpp, 7, ppp, 6);   // 0pp
+  out[8] = pick(mmm, 4, mmp, 0);   // mm0
+  out[9] = pick(pmm, 5, pmp, 1);   // pm0
+  out[10] = pick(mpm, 6, mpp, 2);  // mp0
+  out[11] = pick(ppm, 7, ppp, 3);  // pp0
+}
+
+// is_stencil_in_negative_domain (src/my_p4est_quad_neighbor_nodes_of_node.h:2492-2530): the node and
+// every face node with a nonzero interpolation weight below -EPS
+template <int D>
+bool stencil_negative(const Qnnn<D>& q, const double* f) {
+  if (!(f[q.node_000] < -ORA_EPS)) return false;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const double m0 = q.dt[dir][0], p0 = q.dt[dir][1];
+    const double m1 = D == 3 ? q.dt[dir][2] : 0.0, p1 = D == 3 ? q.dt[dir][3] : 0.0;
+    for (int k = 0; k < Grid<D>::CH / 2; ++k) {
+      // face node k: bit 0 along the first tangential axis (m/p), bit 1 along the second
+      bool zero;
+      if (D == 2)
+        zero = (k == 0) ? fabs(p0) < ORA_EPS : fabs(m0) < ORA_EPS;
+      else {
+        const bool a = (k & 1) ? fabs(m0) < ORA_EPS : fabs(p0) < ORA_EPS;
+        const bool b = (k & 2) ? fabs(m1) < ORA_EPS : fabs(p1) < ORA_EPS;
+        zero = a || b;
+      }
+      if (!(f[q.nb[dir][k]] < -ORA_EPS || zero)) return false;
+    }
+  }
+  return true;
+}
+
+// d_a of f at the node (dx_central, dy_central, dz_central)
+template <int D>
+double dcentral(const Qnnn<D>& q, const double* f, int a) {
+  double g[3] = {0, 0, 0};
+  gradient<D>(q, f, g, 1 << a);
+  return g[a];
+}
+
+// one marching iteration of a field v along the normals, upwind first-order one-sided differences:
+// tmp = v - dt (n . grad v - src) on the nodes selected by `on`
+template <int D>
+double march(const Qnnn<D>& q, const double* v, const double* const* nrm, int64_t n, double src, bool with_src) {
+  const double dt = (D == 3 ? MIN(MIN(fabs(q.d[0]), fabs(q.d[2]), fabs(q.d[4])), MIN(fabs(q.d[1]), fabs(q.d[3]), fabs(q.d[5])))
+                            : MIN(MIN(fabs(q.d[0]), fabs(q.d[2])), MIN(fabs(q.d[1]), fabs(q.d[3])))) /
+                    double(D);
+  double g[3];
+  for (int a = 0; a < D; ++a)
+    g[a] = nrm[a][n] > 0 ? (v[n] - f_linear(q, 2 * a, v)) / q.d[2 * a] : (f_linear(q, 2 * a + 1, v) - v[n]) / q.d[2 * a + 1];
+  double s = nrm[0][n] * g[0] + nrm[1][n] * g[1];
+  if (D == 3) s = s + nrm[2][n] * g[2];
+  return with_src ? v[n] - dt * (s - src) : v[n] - dt * s;
+}
+
+// extend_Over_Interface_TVD(phi, q, iterations, order, band_use, band_extend, normal, mask) with no
+// boundary conditions, no initial guesses and one-step extrapolation (src/my_p4est_level_set.cpp:969-1764)
+template <int D>
+void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_in, double* q, int iterations, int order,
+                           double band_use, double band_extend, const double* normal_in, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+  const double* mask = mask_in ? mask_in : phi;
+  if (band_use > 0) band_use = -band_use;
+  std::vector<double> nstore;
+  const double* nrm_flat = normal_in;
+  if (!nrm_flat) {
+    nstore.resize((size_t)D * N);
+    first_derivatives<D>(cx, phi, nstore.data(), nthreads);
+    normalize<D>(N, nstore.data());
+    nrm_flat = nstore.data();
+  }
+  const double* nrm[3] = {nrm_flat, nrm_flat + N, D == 3 ? nrm_flat + 2 * N : nrm_flat};
+  std::vector<double> qn((size_t)N, 0.0), qnn((size_t)N, 0.0), bqn((size_t)N, 0.0), bqnn((size_t)N, 0.0);
+  std::vector<double> qx((size_t)D * N, 0.0);
+  if (order >= 1) {
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+    for (long long n = 0; n < (long long)N; ++n) {
+      if (phi[n] > band_use) {
+        if (stencil_negative<D>(Q[n], mask)) {
+          bqn[n] = -1;
+          double gq[3] = {0, 0, 0};
+          gradient<D>(Q[n], q, gq);
+          for (int a = 0; a < D; ++a) qx[(size_t)a * N + n] = gq[a];
+          double s = nrm[0][n] * qx[n] + nrm[1][n] * qx[N + n];
+          if (D == 3) s = s + nrm[2][n] * qx[2 * N + n];
+          qn[n] = s;
+        } else {
+          bqn[n] = 1;
+          qn[n] = 0;
+          for (int a = 0; a < D; ++a) qx[(size_t)a * N + n] = 0;
+        }
+      } else {
+        bqn[n] = -1;
+        qn[n] = 0;
+        for (int a = 0; a < D; ++a) qx[(size_t)a * N + n] = 0;
+      }
+    }
+  }
+  if (order == 2) {
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+    for (long long n = 0; n < (long long)N; ++n) {
+      const Qnnn<D>& qq = Q[n];
+      if (!(phi[n] > band_use)) {
+        bqnn[n] = -1;
+        qnn[n] = 0;
+        continue;
+      }
+      bqnn[n] = 1;
+      if (!stencil_negative<D>(qq, mask)) {
+        qnn[n] = 0;
+        continue;
+      }
+      double Qxy = 0, Qyz = 0, Qzx = 0;
+      const double* qxa = qx.data();
+      const double* qya = qx.data() + N;
+      const double* qza = D == 3 ? qx.data() + 2 * N : qx.data();
+      if (stencil_negative<D>(qq, bqn.data())) {
+        bqnn[n] = -1;
+        Qxy = .5 * (dcentral<D>(qq, qya, 0) + dcentral<D>(qq, qxa, 1));
+        if (D == 3) {
+          Qyz = .5 * (dcentral<D>(qq, qza, 1) + dcentral<D>(qq, qya, 2));
+          Qzx = .5 * (dcentral<D>(qq, qxa, 2) + dcentral<D>(qq, qza, 0));
+        }
+      } else {
+        int32_t nb[12];
+        corner_neighbors<D>(g, (int32_t)n, nb);
+        const int cnt = D == 3 ? 12 : 4;
+        bool exist = true, neg = true;
+        for (int k = 0; k < cnt; ++k) exist = exist && nb[k] >= 0;
+        if (exist) {
+          for (int k = 0; k < cnt; ++k) neg = neg && mask[nb[k]] < 0;
+          if (neg) {
+            const int mm0 = D == 3 ? 8 : 0, pm0 = D == 3 ? 9 : 1, mp0 = D == 3 ? 10 : 2, pp0 = D == 3 ? 11 : 3;
+            Qxy = (q[nb[pp0]] + q[nb[mm0]] - q[nb[mp0]] - q[nb[pm0]]) / (qq.d[0] + qq.d[1]) / (qq.d[2] + qq.d[3]);
+            if (D == 3) {
+              Qyz = (q[nb[7]] + q[nb[4]] - q[nb[6]] - q[nb[5]]) / (qq.d[2] + qq.d[3]) / (qq.d[D == 3 ? 4 : 0] + qq.d[D == 3 ? 5 : 0]);
+              Qzx = (q[nb[3]] + q[nb[0]] - q[nb[1]] - q[nb[2]]) / (qq.d[D == 3 ? 4 : 0] + qq.d[D == 3 ? 5 : 0]) / (qq.d[0] + qq.d[1]);
+            }
+            bqnn[n] = -1;
+          }
+        }
+      }
+      if (bqnn[n] < 0) {
+        // dxx_central etc.: central second differences of the quadratically corrected neighbours
+        // (x_ngbd_with_quadratic_interpolation, src/my_p4est_quad_neighbor_nodes_of_node.cpp:365-390)
+        double fz, fn[6], dd[3] = {0, 0, 0};
+        ngbd_quadratic(qq, q, &fz, fn);
+        for (int a = 0; a < D; ++a) dd[a] = central_second_derivative(fn[2 * a + 1], fz, fn[2 * a], qq.d[2 * a + 1], qq.d[2 * a]);
+        const double Qx = qx[n], Qy = qx[N + n];
+        const double Nx = nrm[0][n], Ny = nrm[1][n];
+        const double Nxx = dcentral<D>(qq, nrm[0], 0), Nyx = dcentral<D>(qq, nrm[1], 0);
+        const double Nxy = dcentral<D>(qq, nrm[0], 1), Nyy = dcentral<D>(qq, nrm[1], 1);
+        if (D == 3) {
+          const double Qz = qx[2 * N + n], Nz = nrm[2][n];
+          const double Nzx = dcentral<D>(qq, nrm[2], 0), Nzy = dcentral<D>(qq, nrm[2], 1);
+          const double Nxz = dcentral<D>(qq, nrm[0], 2), Nyz = dcentral<D>(qq, nrm[1], 2), Nzz = dcentral<D>(qq, nrm[2], 2);
+          qnn[n] = Nx * (Nx * dd[0] + 2. * Ny * Qxy + Qx * Nxx + Qy * Nyx + Qz * Nzx) +
+                   Ny * (Ny * dd[1] + 2. * Nz * Qyz + Qx * Nxy + Qy * Nyy + Qz * Nzy) +
+                   Nz * (Nz * dd[2] + 2. * Nx * Qzx + Qx * Nxz + Qy * Nyz + Qz * Nzz);
+        } else {
+          qnn[n] = Nx * (Nx * dd[0] + 2. * Ny * Qxy + Qx * Nxx + Qy * Nyx) + Ny * (Ny * dd[1] + Qx * Nxy + Qy * Nyy);
+        }
+      } else {
+        qnn[n] = 0;
+      }
+    }
+  }
+  // marching loops: qnn, then qn, then q (ping-pong; nodes not marched keep their value)
+  auto run = [&](std::vector<double>& v, const std::vector<double>& b, const double* src, bool with_src) {
+    std::vector<double> tmp(v);
+    for (int it = 0; it < iterations; ++it) {
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+      for (long long n = 0; n < (long long)N; ++n)
+        if (b[n] > 0 && phi[n] < band_extend) tmp[n] = march<D>(Q[n], v.data(), nrm, n, src ? src[n] : 0.0, with_src);
+      v.swap(tmp);
+    }
+  };
+  if (order == 2) run(qnn, bqnn, nullptr, false);
+  if (order >= 1) run(qn, bqn, order == 2 ? qnn.data() : nullptr, true);
+  std::vector<double> cur(q, q + N), tmp(q, q + N), qdd((size_t)D * N);
+  for (int it = 0; it < iterations; ++it) {
+    compute_derivatives<D>(cx, cur.data(), qdd.data(), nthreads);
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+    for (long long n = 0; n < (long long)N; ++n) {
+      if (!(mask[n] > -ORA_EPS && phi[n] < band_extend)) continue;
+      const Qnnn<D>& qq = Q[n];
+      const double dt = (D == 3 ? MIN(MIN(fabs(qq.d[0]), fabs(qq.d[2]), fabs(qq.d[4])), MIN(fabs(qq.d[1]), fabs(qq.d[3]), fabs(qq.d[5])))
+                                : MIN(MIN(fabs(qq.d[0]), fabs(qq.d[2])), MIN(fabs(qq.d[1]), fabs(qq.d[3])))) /
+                        double(D);
+      double gq[3];
+      for (int a = 0; a < D; ++a)
+        gq[a] = nrm[a][n] > 0 ? (cur[n] - f_linear(qq, 2 * a, cur.data())) / qq.d[2 * a]
+                              : (f_linear(qq, 2 * a + 1, cur.data()) - cur[n]) / qq.d[2 * a + 1];
+      if (order == 2) {
+        for (int a = 0; a < D; ++a) {
+          const double* qaa = qdd.data() + (size_t)a * N;
+          double qm = f_linear(qq, 2 * a, qaa), qp = f_linear(qq, 2 * a + 1, qaa);
+          qm = qaa[n] * qm < 0 ? 0 : (fabs(qaa[n]) < fabs(qm) ? qaa[n] : qm);
+          qp = qaa[n] * qp < 0 ? 0 : (fabs(qaa[n]) < fabs(qp) ? qaa[n] : qp);
+          if (nrm[a][n] < 0) gq[a] -= .5 * qq.d[2 * a + 1] * qp;
+          else gq[a] += .5 * qq.d[2 * a] * qm;
+        }
+      }
+      double sum = nrm[0][n] * gq[0] + nrm[1][n] * gq[1];
+      if (D == 3) sum = sum + nrm[2][n] * gq[2];
+      const double change = dt * (sum - (order >= 1 ? qn[n] : 0));
+      tmp[n] = cur[n] - change;
+    }
+    cur.swap(tmp);
+  }
+  memcpy(q, cur.data(), (size_t)N * sizeof(double));
+}
+
 // ---- node interpolation ------------------------------------------------------------------------
 // PI of src/casl_math.h:15
 const double ORA_PI = 3.1415926535897932384626433832795;
@@ -1436,6 +1678,17 @@ int ora_normals_and_mean_curvature(void* h, const double* phi, double* normals, 
     Ctx* cx = static_cast<Ctx*>(h);
     if (cx->dim == 2) normals_and_curvature<2>(*cx, phi, normals, kappa, nthreads);
     else normals_and_curvature<3>(*cx, phi, normals, kappa, nthreads);
+  });
+}
+
+int ora_extend_over_interface(void* h, const double* phi, const double* mask, double* q, int iterations, int order, double band_use,
+                              double band_extend, const double* normals, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("extension needs a grid built from leaves");
+    if (order < 0 || order > 2) throw std::invalid_argument("order must be 0, 1 or 2");
+    if (cx->dim == 2) extend_over_interface<2>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads);
+    else extend_over_interface<3>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads);
   });
 }
 

@@ -40,6 +40,7 @@ SIG = {
     "ora_compute_normals": (_I, [_P, _DP, _DP, _I]),
     "ora_mean_curvature_from_normals": (_I, [_P, _DP, _DP, _I]),
     "ora_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP, _I]),
+    "ora_extend_over_interface": (_I, [_P, _DP, _DP, _DP, _I, _I, _D, _D, _DP, _I]),
     "ora_interface_location": (_D, [_D, _D, _D, _D]),
     "ora_interface_location_2nd": (_D, [_D, _D, _D, _D, _D, _D]),
 }
@@ -172,6 +173,16 @@ class OracleGrid:
         kappa = np.empty(self.N, np.float64)
         _chk(load().ora_normals_and_mean_curvature(self._h, _dp(phi), _dp(nrm), _dp(kappa), nthreads))
         return nrm, kappa
+
+    def extend_over_interface_tvd(self, phi, q, iterations=20, order=2, band_use=-np.finfo(np.float64).max,
+                                  band_extend=np.finfo(np.float64).max, normals=None, mask=None, nthreads=1):
+        """In place on q (float64, node order)."""
+        phi = np.ascontiguousarray(phi, np.float64)
+        assert q.dtype == np.float64 and q.flags.c_contiguous and q.size == self.N
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float64)
+        msk = None if mask is None else np.ascontiguousarray(mask, np.float64)
+        _chk(load().ora_extend_over_interface(self._h, _dp(phi), _dp(msk), _dp(q), int(iterations), int(order), float(band_use),
+                                              float(band_extend), _dp(nrm), nthreads))
 
     # ---- node interpolation and the semi-Lagrangian step ------------------------------------
     def interpolate(self, method, F, xyz, Fdd=None, nthreads=1):

@@ -1,6 +1,6 @@
 // The C++ facade (include/lsgpu.hpp) gives exactly the results of the C ABI it wraps:
-// reinitialisation, normal advection with a function-object velocity, node interpolation and the
-// semi-Lagrangian step. Prints "facade ok" on success; exits non-zero otherwise.
+// reinitialisation, normal advection with a function-object velocity, extension over the interface,
+// node interpolation and the semi-Lagrangian step. Prints "facade ok" on success; exits non-zero otherwise.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -88,6 +88,23 @@ int main() {
                                           LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2,
                                           np1_ref.data()));
   if (memcmp(np1.data(), np1_ref.data(), N * sizeof(double)) != 0) return fail("advect_from_n_to_np1");
+
+  // extension over the interface with given normals and a mask
+  lsgpu_vec q{std::vector<double>((size_t)N)}, nx{std::vector<double>((size_t)N)}, ny{std::vector<double>((size_t)N)};
+  for (int64_t i = 0; i < N; ++i) {
+    q.values[i] = phi.values[i] < 0 ? xyz[2 * i] * xyz[2 * i + 1] + 1.0 : 0.0;
+    const double r = sqrt(xyz[2 * i] * xyz[2 * i] + xyz[2 * i + 1] * xyz[2 * i + 1]) + 1e-3;
+    nx.values[i] = xyz[2 * i] / r;
+    ny.values[i] = xyz[2 * i + 1] / r;
+  }
+  std::vector<double> q_ref(q.values), nrm_ref((size_t)2 * N);
+  memcpy(nrm_ref.data(), nx.values.data(), N * sizeof(double));
+  memcpy(nrm_ref.data() + N, ny.values.data(), N * sizeof(double));
+  Vec nrm[2] = {&nx, &ny};
+  ls.extend_Over_Interface_TVD(&phi, &q, 8, 2, -DBL_MAX, DBL_MAX, nrm, &phi);
+  lsgpu::check(lsg_extend_over_interface_tvd(raw, phi.values.data(), q_ref.data(), 8, 2, -DBL_MAX, DBL_MAX, nrm_ref.data(),
+                                             phi.values.data()));
+  if (memcmp(q.values.data(), q_ref.data(), N * sizeof(double)) != 0) return fail("extend_Over_Interface_TVD");
 
   // errors come back as exceptions
   try {
