@@ -677,6 +677,46 @@ int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* 
   });
 }
 
+int lsg_extend_from_interface_to_whole_domain_tvd_device(lsg_level_set* ls, const double* phi, const double* q_interface, double* q,
+                                                         int nfields, int iterations, const double* mask, double band_zero,
+                                                         double band_smooth, const double* grad_phi, int method) {
+  return guard([&] {
+    need(phi != nullptr && q_interface != nullptr && q != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      L.extend_from_interface(phi, q_interface, q, nfields, iterations, mask, band_zero, band_smooth, grad_phi, method);
+    });
+  });
+}
+
+int lsg_extend_from_interface_to_whole_domain_tvd(lsg_level_set* ls, const double* phi, const double* q_interface, double* q, int nfields,
+                                                  int iterations, const double* mask, double band_zero, double band_smooth,
+                                                  const double* grad_phi, int method) {
+  return guard([&] {
+    need(phi != nullptr && q_interface != nullptr && q != nullptr, "null argument");
+    need(nfields >= 1, "nfields must be at least 1");
+    with_ls(ls, [&](auto& L) {
+      const int D = ls->dim;
+      const size_t N = (size_t)L.N, nf = (size_t)nfields;
+      L.ws_f.ensure((1 + 2 * nf + (mask ? 1 : 0) + (grad_phi ? D : 0)) * N + 1);
+      double* dphi = L.ws_f.p;
+      double* dqi = dphi + N;
+      double* dq = dqi + nf * N;
+      double* dm = mask ? dq + nf * N : nullptr;
+      double* dg = grad_phi ? dq + nf * N + (mask ? N : 0) : nullptr;
+      auto up = [&](double* dst, const double* src, size_t cnt) {
+        if (cnt) cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      };
+      up(dphi, phi, N);
+      up(dqi, q_interface, nf * N);
+      if (dm) up(dm, mask, N);
+      if (dg) up(dg, grad_phi, (size_t)D * N);
+      L.extend_from_interface(dphi, dqi, dq, nfields, iterations, dm, band_zero, band_smooth, dg, method);
+      if (N) cuda_check(cudaMemcpyAsync(q, dq, nf * N * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H");
+      cuda_check(cudaStreamSynchronize(L.stream), "sync");
+    });
+  });
+}
+
 int lsg_interpolate_nodes(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
                           int method, double* out) {
   return guard([&] {

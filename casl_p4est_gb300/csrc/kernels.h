@@ -164,6 +164,16 @@ void launch_sl_vortex64(const DLoc<D>& L, int method, const double* xyz, int64_t
 // Leaf chosen by the point location for each point (clipped first).
 template <int D>
 void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* leaf, cudaStream_t s);
+// extend_from_interface_to_whole_domain_TVD: set-up (start value of q, interface values and distances
+// per direction, crossing bits) and one TVD-RK2 stage (average = second stage fused with the RK average)
+template <int D>
+void launch_efi_init64(const DTab64<D>& T, const DLoc<D>& L, int method, const double* xyz, const double* phi, const double* pdd,
+                       const double* qi, const double* qidd, const double* mask, double dl, double band_zero_dl, double band_smooth_dl,
+                       double* q, double* qi_nb, double* s_nb, uint8_t* cross, cudaStream_t s);
+template <int D>
+void launch_efi_stage64(const DTab64<D>& T, const double* phi, const double* grad, const double* q, const double* qdd, const double* qdd2,
+                        const double* qi_nb, const double* s_nb, const uint8_t* cross, double zdt, bool average, double* out,
+                        cudaStream_t s);
 
 // reinit_fp64's kernel sequence with its work vectors in a static device array (noalloc.cu);
 // throws std::invalid_argument when the grid does not fit the array. hi/lo: widened phi_0 limits.

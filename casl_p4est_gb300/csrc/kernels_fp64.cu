@@ -550,6 +550,83 @@ __global__ void __launch_bounds__(TPB) k_ext_q(DTab64<D> T, const double* __rest
   tmp[n] = q[n] - change;
 }
 
+// ---- extend_from_interface_to_whole_domain_TVD_one_iteration (src/my_p4est_level_set.cpp:3181-3323) --------
+// One TVD-RK2 stage for one field: Godunov upwinding along sgn(phi) grad(phi)/|grad(phi)| with
+// second-order one-sided differences (minmod of the quadratically interpolated second derivatives),
+// the neighbour across the interface replaced by the interface value at the subcell distance
+// (qi_nb, s_nb, cross from the set-up kernel), Neumann walls. qdd: D x N second derivatives of q;
+// qdd2: D x D x N second derivatives of each of them. AVG: out = 0.5 (out + stage), the RK average.
+template <int D, bool AVG>
+__global__ void __launch_bounds__(TPB) k_efi_stage64(DTab64<D> T, const double* __restrict__ phi, const double* __restrict__ grad,
+                                                     const double* __restrict__ q, const double* __restrict__ qdd,
+                                                     const double* __restrict__ qdd2, const double* __restrict__ qi_nb,
+                                                     const double* __restrict__ s_nb, const uint8_t* __restrict__ cross, double zdt,
+                                                     double* __restrict__ out) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  double res;
+  if (fabs(phi[n]) < zdt) {
+    res = q[n];
+  } else {
+    double Dq[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) Dq[a] = qdd[(int64_t)a * N + n];
+    const double q0 = q[n];
+    const uint8_t cr = cross[n];
+    double qn[2 * D], s[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      s[dir] = s_nb[(int64_t)dir * N + n];
+      qn[dir] = (cr >> dir) & 1 ? qi_nb[(int64_t)dir * N + n] : quad_nb64<D>(T, dir, n, q, Dq);
+    }
+    double d0[D], dm[D], dp[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const double* qaa = qdd + (int64_t)a * N;
+      double Da[D];
+#pragma unroll
+      for (int b = 0; b < D; ++b) Da[b] = qdd2[(int64_t)(a * D + b) * N + n];
+      d0[a] = qaa[n];
+      dm[a] = quad_nb64<D>(T, 2 * a, n, qaa, Da);
+      dp[a] = quad_nb64<D>(T, 2 * a + 1, n, qaa, Da);
+    }
+    const uint8_t wl = T.wall[n];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      if (wl & (1u << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        qn[2 * a] = qn[2 * a + 1];
+        d0[a] = dm[a] = dp[a] = 0.0;
+      } else if (wl & (1u << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        qn[2 * a + 1] = qn[2 * a];
+        d0[a] = dm[a] = dp[a] = 0.0;
+      }
+    }
+    double dt = min2(s[0], s[1]);
+    dt = min3(dt, s[2], s[3]);
+    if (D == 3) dt = min3(dt, s[D == 3 ? 4 : 0], s[D == 3 ? 5 : 0]);
+    dt /= ((double)D);
+    const double gx = grad[n], gy = grad[N + n], gz = D == 3 ? grad[(D == 3 ? 2 : 0) * N + n] : 0.0;
+    const double mag = D == 3 ? sqrt(gx * gx + gy * gy + gz * gz) : sqrt(gx * gx + gy * gy);
+    const double sg = phi[n] < 0.0 ? -1.0 : +1.0;
+    const double nv[3] = {mag > EPS ? sg * gx / mag : 0.0, mag > EPS ? sg * gy / mag : 0.0, mag > EPS ? sg * gz / mag : 0.0};
+    double t[3];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      const double qm = (q0 - qn[2 * a]) / s[2 * a] + 0.5 * s[2 * a] * minmod(dm[a], d0[a]);
+      const double qp = (qn[2 * a + 1] - q0) / s[2 * a + 1] - 0.5 * s[2 * a + 1] * minmod(dp[a], d0[a]);
+      t[a] = nv[a] * (nv[a] > 0.0 ? qm : qp);
+    }
+    res = q0 - dt * (D == 3 ? (t[0] + t[1] + t[D == 3 ? 2 : 0]) : (t[0] + t[1]));
+  }
+  if (AVG)
+    out[n] = .5 * (out[n] + res);
+  else
+    out[n] = res;
+}
+
 // Band L-infinity check in FP64: max |a - b| over the nodes with |b| < band (b the reference field),
 // with the number of band nodes and a NaN flag. Warp shuffles, then one shared-memory pass per block,
 // then one atomic per block; non-negative doubles order like their bit patterns, so atomicMax on the
@@ -657,6 +734,17 @@ void launch_ext_q(const DTab64<D>& T, const double* q, double* tmp, const double
     k_ext_q<D, 0><<<nblocks(T.N), TPB, 0, s>>>(T, q, tmp, qdd, phi, mask, nrm, qn, band_extend);
 }
 
+template <int D>
+void launch_efi_stage64(const DTab64<D>& T, const double* phi, const double* grad, const double* q, const double* qdd, const double* qdd2,
+                        const double* qi_nb, const double* s_nb, const uint8_t* cross, double zdt, bool average, double* out,
+                        cudaStream_t s) {
+  if (!T.N) return;
+  if (average)
+    k_efi_stage64<D, true><<<nblocks(T.N), TPB, 0, s>>>(T, phi, grad, q, qdd, qdd2, qi_nb, s_nb, cross, zdt, out);
+  else
+    k_efi_stage64<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, phi, grad, q, qdd, qdd2, qi_nb, s_nb, cross, zdt, out);
+}
+
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
   cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
   if (n == 0) return;
@@ -726,6 +814,8 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
   template void launch_advect_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, double,  \
                                          double*, const double*, cudaStream_t);                                              \
   template void launch_grad64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, int, cudaStream_t);      \
+  template void launch_efi_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, const double*,  \
+                                      const double*, const double*, const uint8_t*, double, bool, double*, cudaStream_t);          \
   template void launch_normalize64<D>(double*, int64_t, cudaStream_t);                                                        \
   template void launch_div64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, cudaStream_t);            \
   template void launch_kappa64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,    \

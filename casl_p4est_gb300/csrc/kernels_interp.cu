@@ -10,11 +10,13 @@
 //                      (src/my_p4est_utils.cpp:410-576)
 //   per-point driver   my_p4est_interpolation_nodes_t::interpolate (src/my_p4est_interpolation_nodes.cpp:107-288)
 //   backtrace          my_p4est_semi_lagrangian_t::advect_from_n_to_np1 (src/my_p4est_semi_lagrangian.cpp:108-223)
+//   interface values   extend_from_interface_to_whole_domain_TVD, set-up part (src/my_p4est_level_set.cpp:3325-3633)
 //
 // One thread per point. The reference walks a cell tree from the root; here the leaf holding a
 // logical point is found from a coarse-cell table plus a binary search over the sorted leaf keys
 // (the same leaf: a leaf [x0, x0+h) holds the real coordinate s exactly when it holds floor(s)).
 #include "kernels.h"
+#include "stencil64.cuh"
 
 namespace lsg {
 namespace {
@@ -292,7 +294,87 @@ __global__ void __launch_bounds__(TPB) k_locate64(DLoc<D> L, const double* __res
   leaf[p] = locate<D>(L, x);
 }
 
+// smoothstep(N, x) with its pascalTriangle coefficients (src/my_p4est_utils.cpp:3350-3370)
+__device__ double pascal_triangle(int a, int b) {
+  double result = 1.;
+  for (int i = 0; i < b; ++i) result *= double(a - i) / double(i + 1);
+  return result;
+}
+__device__ double smoothstep(int N, double x) {
+  if (x <= 0) return 0;
+  if (x >= 1) return 1;
+  double result = 0;
+  for (int n = 0; n <= N; ++n) result += pascal_triangle(-N - 1, n) * pascal_triangle(2 * N + 1, N - n) * pow(x, (double)(N + n + 1));
+  return result;
+}
+
+// Set-up of extend_from_interface_to_whole_domain_TVD for one field, one thread per node: the start
+// value of q, and along each of the 2D grid directions whose quadratically interpolated phi neighbour
+// has the other sign, the subcell distance to the interface (second-order location, at least EPS) and
+// qi interpolated there with method M (times 1 - smoothstep(1, (mask - band_zero)/band_smooth) when a
+// mask is given, the mask interpolated linearly); elsewhere qi at the node and the grid distance.
+template <int D, int M>
+__global__ void __launch_bounds__(TPB) k_efi_init64(DTab64<D> T, DLoc<D> L, const double* __restrict__ xyz, const double* __restrict__ phi,
+                                                    const double* __restrict__ pdd, const double* __restrict__ qi,
+                                                    const double* __restrict__ qidd, const double* __restrict__ mask, double dl,
+                                                    double band_zero, double band_smooth, double* __restrict__ q,
+                                                    double* __restrict__ qi_nb, double* __restrict__ s_nb, uint8_t* __restrict__ cross) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  const double p0 = phi[n];
+  q[n] = (mask ? max2(mask[n], fabs(p0)) : fabs(p0)) < 1.5 * dl ? qi[n] : 0;
+  double Dp[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) Dp[a] = pdd[(int64_t)a * N + n];
+  uint8_t bits = 0;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int a = dir >> 1;
+    const double pn = st64::quad_nb64<D>(T, dir, n, phi, Dp);
+    const double dd = T.d[(int64_t)dir * N + n];
+    if (p0 * pn < 0.0) {
+      double dist = st64::interface_location_2nd(0, dd, p0, pn, Dp[a], st64::lin64<D>(T, dir, n, pdd + (int64_t)a * N));
+      dist = max2(dist, EPS);
+      double x[3] = {0, 0, 0};
+#pragma unroll
+      for (int b = 0; b < D; ++b) x[b] = xyz[n * D + b];
+      x[a] = (dir & 1) ? x[a] + dist : x[a] - dist;
+      double v;
+      interpolate_at<D, M>(L, x, 1, qi, qidd, 1, 0, &v);
+      if (mask) {
+        double m;
+        interpolate_at<D, 0>(L, x, 1, mask, nullptr, 1, 0, &m);
+        v *= 1. - smoothstep(1, (m - band_zero) / band_smooth);
+      }
+      qi_nb[(int64_t)dir * N + n] = v;
+      s_nb[(int64_t)dir * N + n] = dist;
+      bits |= (uint8_t)(1u << dir);
+    } else {
+      qi_nb[(int64_t)dir * N + n] = qi[n];
+      s_nb[(int64_t)dir * N + n] = dd;
+    }
+  }
+  cross[n] = bits;
+}
+
 }  // namespace
+
+template <int D>
+void launch_efi_init64(const DTab64<D>& T, const DLoc<D>& L, int method, const double* xyz, const double* phi, const double* pdd,
+                       const double* qi, const double* qidd, const double* mask, double dl, double band_zero, double band_smooth,
+                       double* q, double* qi_nb, double* s_nb, uint8_t* cross, cudaStream_t s) {
+  if (T.N == 0) return;
+  const int64_t g = nblocks(T.N);
+#define LSG_EFI(M) k_efi_init64<D, M><<<g, TPB, 0, s>>>(T, L, xyz, phi, pdd, qi, qidd, mask, dl, band_zero, band_smooth, q, qi_nb, s_nb, cross)
+  switch (method) {
+    case 0: LSG_EFI(0); break;
+    case 1: LSG_EFI(1); break;
+    case 2: LSG_EFI(2); break;
+    case 3: LSG_EFI(3); break;
+    default: LSG_EFI(4); break;
+  }
+#undef LSG_EFI
+}
 
 template <int D>
 void launch_interp64(const DLoc<D>& L, int method, const double* xyz, int64_t np, const double* shift, double coef, int nf,
@@ -333,7 +415,10 @@ void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* l
                                    const double*, double*, cudaStream_t);                                                      \
   template void launch_sl_vortex64<D>(const DLoc<D>&, int, const double*, int64_t, double, double, const double*, const double*, \
                                       double*, cudaStream_t);                                                                  \
-  template void launch_locate64<D>(const DLoc<D>&, const double*, int64_t, int32_t*, cudaStream_t);
+  template void launch_locate64<D>(const DLoc<D>&, const double*, int64_t, int32_t*, cudaStream_t);                              \
+  template void launch_efi_init64<D>(const DTab64<D>&, const DLoc<D>&, int, const double*, const double*, const double*,        \
+                                     const double*, const double*, const double*, double, double, double, double*, double*,     \
+                                     double*, uint8_t*, cudaStream_t);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

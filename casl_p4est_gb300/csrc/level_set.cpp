@@ -4,6 +4,7 @@
 #include <float.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include <cstdlib>
 #include <cstring>
@@ -764,6 +765,64 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
     if (a != q) cuda_check(cudaMemcpyAsync(q, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   }
   cuda_check(cudaGetLastError(), "extend_Over_Interface_TVD");
+}
+
+template <int D>
+void LevelSet<D>::extend_from_interface(const double* phi, const double* qi, double* q, int nf, int iterations, const double* mask,
+                                        double band_zero, double band_smooth, const double* grad_phi, int method) {
+  if (nf < 1) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: at least one field");
+  if (mask && nf > 1) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: a mask needs a block size of 1");
+  if (method < 0 || method > 4) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: unknown interpolation method");
+  if (iterations < 0) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: negative number of iterations");
+  const size_t n = (size_t)N;
+  if (n && q < qi + (size_t)nf * n && qi < q + (size_t)nf * n)
+    throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: q and q_interface overlap");
+  build_gradient();
+  build_locator();
+  if (!node_xyz_dev.p) {
+    std::vector<double> x((size_t)D * n + 1);
+    for (int64_t k = 0; k < N; ++k) F->node_xyz((int32_t)k, &x[(size_t)D * k]);
+    node_xyz_dev.upload(x, stream);
+  }
+  // dl = max over the axes of the tree size / 2^max_lvl
+  const int max_lvl = F->max_level();
+  double dl = TL.tree_dim[0] / pow(2., (double)max_lvl);
+  for (int a = 1; a < D; ++a) dl = std::max(dl, TL.tree_dim[a] / pow(2., (double)max_lvl));
+  // layout of efi_buf: grad D | phi dd D | qi dd D | qi_nb 2D | s_nb 2D | q1 | qdd D | qdd2 D*D
+  efi_buf.ensure((size_t)(8 * D + 1 + D * D) * n + 1);
+  double* grad_own = efi_buf.p;
+  double* pdd = grad_own + (size_t)D * n;
+  double* qidd = pdd + (size_t)D * n;
+  double* qi_nb = qidd + (size_t)D * n;
+  double* s_nb = qi_nb + (size_t)2 * D * n;
+  double* q1 = s_nb + (size_t)2 * D * n;
+  double* qdd = q1 + n;
+  double* qdd2 = qdd + (size_t)D * n;
+  efi_cross.ensure(n + 1);
+  const double* grad = grad_phi;
+  if (!grad) {
+    first_derivatives(phi, grad_own);
+    grad = grad_own;
+  }
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, pdd, stream));
+  auto derivatives = [&](const double* f) {
+    LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, f, qdd, stream));
+    for (int a = 0; a < D; ++a) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qdd + (size_t)a * n, qdd2 + (size_t)a * D * n, stream));
+  };
+  for (int k = 0; k < nf; ++k) {
+    const double* qik = qi + (size_t)k * n;
+    double* qk = q + (size_t)k * n;
+    LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qik, qidd, stream));
+    LSG_LAUNCH(K_INTERP, launch_efi_init64<D>(T64, TL, method, node_xyz_dev.p, phi, pdd, qik, qidd, mask, dl, band_zero * dl,
+                                              band_smooth * dl, qk, qi_nb, s_nb, efi_cross.p, stream));
+    for (int it = 0; it < iterations; ++it) {
+      derivatives(qk);
+      LSG_LAUNCH(K_ADVECT64, launch_efi_stage64<D>(T64, phi, grad, qk, qdd, qdd2, qi_nb, s_nb, efi_cross.p, zdt, false, q1, stream));
+      derivatives(q1);
+      LSG_LAUNCH(K_ADVECT64, launch_efi_stage64<D>(T64, phi, grad, q1, qdd, qdd2, qi_nb, s_nb, efi_cross.p, zdt, true, qk, stream));
+    }
+  }
+  cuda_check(cudaGetLastError(), "extend_from_interface_to_whole_domain_TVD");
 }
 
 // Point location tables: sorted leaf keys and levels, local_nodes, and the coarse-cell table

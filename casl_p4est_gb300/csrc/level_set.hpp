@@ -80,6 +80,9 @@ struct LevelSet {
   DevBuf<int32_t> cnb;
   DevBuf<int8_t> ext_b1, ext_b2;
   DevBuf<double> ext_buf;
+  // extension from the interface: node coordinates (N x D, built on first use), work vectors, crossing bits
+  DevBuf<double> node_xyz_dev, efi_buf;
+  DevBuf<uint8_t> efi_cross;
   // first-derivative correction records (built on first use)
   bool grad_ready = false;
   DevBuf<int32_t> g_idx;
@@ -145,6 +148,13 @@ struct LevelSet {
   // normals (D x N) and mask (N) may be null (computed from phi / taken as phi).
   void extend_over_interface(const double* phi, double* q, int iterations, int order, double band_use, double band_extend,
                              const double* normals, const double* mask);
+
+  // extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero, band_smooth, cf = NULL,
+  // grad_phi) (src/my_p4est_level_set.cpp:3181-3767) for nf fields (nf x N; the reference's blocksize):
+  // q (device, nf x N, not overlapping qi) receives qi's interface values extended along the normals.
+  // mask (only with nf == 1) and grad_phi (D x N) may be null; method = interpolation_on_interface.
+  void extend_from_interface(const double* phi, const double* qi, double* q, int nf, int iterations, const double* mask,
+                             double band_zero, double band_smooth, const double* grad_phi, int method);
 
   // my_p4est_interpolation_nodes_t: nf fields (nf x N) interpolated at np points (D doubles each)
   // with `method` (interpolation_method); Fdd (nf x D x N) may be null and is then computed with

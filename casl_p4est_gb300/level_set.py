@@ -196,10 +196,15 @@ class my_p4est_level_set_t:
 
     def extend_Over_Interface_TVD(self, phi, q, iterations=20, order=2, band_use=-DBL_MAX, band_extend=DBL_MAX,
                                   normal=None, mask=None):
-        """Extend q (updated in place) from phi < 0 (or mask < 0) along the normals (FP64)."""
+        """Extend q (updated in place) from phi < 0 (or mask < 0) along the normals (FP64). normal: (dim, N)."""
         if order not in (0, 1, 2):
             raise ValueError("[CASL_ERROR]: my_p4est_level_set_t->extend_Over_Interface_TVD: order must be 0, 1 or 2.")
         n = self.num_nodes
+        if _is_device(phi):
+            ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+            L.check(L.load().lsg_extend_over_interface_tvd_device(self._h, ptr(phi), ptr(q), int(iterations), int(order),
+                                                                  float(band_use), float(band_extend), ptr(normal), ptr(mask)))
+            return
         phi = _host_f64(np.ascontiguousarray(phi, np.float64), n, "phi")
         _host_f64(q, n, "q")
         nrm = None if normal is None else np.ascontiguousarray(normal, np.float64)
@@ -207,6 +212,45 @@ class my_p4est_level_set_t:
         L.check(L.load().lsg_extend_over_interface_tvd(self._h, L.dptr(phi), L.dptr(q), int(iterations), int(order), float(band_use),
                                                        float(band_extend), L.dptr(nrm) if nrm is not None else None,
                                                        L.dptr(msk) if msk is not None else None))
+
+    interpolation_on_interface = 4  # quadratic_non_oscillatory_continuous_v2 (src/my_p4est_level_set.h:389)
+
+    def set_interpolation_on_interface(self, method):
+        """set_interpolation_on_interface (src/my_p4est_level_set.h:843)."""
+        if int(method) not in range(5):
+            raise ValueError("unknown interpolation_method")
+        self.interpolation_on_interface = int(method)
+
+    def extend_from_interface_to_whole_domain_TVD(self, phi, q_interface, q=None, iterations=20, mask=None, band_zero=2.0,
+                                                  band_smooth=10.0, grad_phi_in=None):
+        """q = the interface values of q_interface extended in the normal direction on both sides (FP64).
+
+        q_interface: (N,) or (nfields, N) (the reference's blocksize, components as blocks); q: output of the
+        same shape (allocated and returned when None; must not overlap q_interface); grad_phi_in: (dim, N)."""
+        if _is_device(phi):
+            if q is None:
+                q = q_interface.new_empty(q_interface.shape)
+            nf = 1 if q_interface.dim() == 1 else int(q_interface.shape[0])
+            ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+            L.check(L.load().lsg_extend_from_interface_to_whole_domain_tvd_device(
+                self._h, ptr(phi), ptr(q_interface), ptr(q), nf, int(iterations), ptr(mask), float(band_zero), float(band_smooth),
+                ptr(grad_phi_in), self.interpolation_on_interface))
+            return q
+        n = self.num_nodes
+        phi = _host_f64(np.ascontiguousarray(phi, np.float64), n, "phi")
+        qi = np.ascontiguousarray(q_interface, np.float64)
+        nf = 1 if qi.ndim == 1 else qi.shape[0]
+        if qi.size != nf * n:
+            raise ValueError(f"q_interface has {qi.size} entries, expected {nf} x {n}")
+        out = np.empty_like(qi) if q is None else q
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous and out.size == qi.size):
+            raise TypeError("q must be a C-contiguous float64 numpy array shaped like q_interface")
+        msk = None if mask is None else _host_f64(np.ascontiguousarray(mask, np.float64), n, "mask")
+        g = None if grad_phi_in is None else np.ascontiguousarray(grad_phi_in, np.float64)
+        L.check(L.load().lsg_extend_from_interface_to_whole_domain_tvd(
+            self._h, L.dptr(phi), L.dptr(qi), L.dptr(out), nf, int(iterations), L.dptr(msk) if msk is not None else None,
+            float(band_zero), float(band_smooth), L.dptr(g) if g is not None else None, self.interpolation_on_interface))
+        return out
 
     def band_linf(self, a, b, band):
         """FP64 max |a - b| over |b| < band on the device (CUDA tensors); returns (value, band node count)."""

@@ -192,6 +192,22 @@ int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* 
 int lsg_extend_over_interface_tvd_device(lsg_level_set* ls, const double* phi_dev, double* q_dev, int iterations, int order,
                                          double band_use, double band_extend, const double* normals_dev, const double* mask_dev);
 
+/* my_p4est_level_set_t::extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero,
+ * band_smooth, cf, grad_phi, blocksize) (src/my_p4est_level_set.h:775-776,
+ * src/my_p4est_level_set.cpp:3181-3767) without the cf callback: q (nfields x N, the reference's
+ * blocksize with the components as consecutive blocks of N) receives the values of q_interface
+ * (nfields x N) on the interface, interpolated with `method` (the reference's
+ * interpolation_on_interface, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2 by default) where a grid line
+ * crosses the interface, extended in the normal direction on both sides by `iterations` TVD-RK2 steps.
+ * mask (N, only with nfields == 1) and grad_phi (dim x N) may be NULL. q and q_interface must not
+ * overlap. The reference's defaults are iterations 20, band_zero 2 and band_smooth 10. */
+int lsg_extend_from_interface_to_whole_domain_tvd(lsg_level_set* ls, const double* phi, const double* q_interface, double* q, int nfields,
+                                                  int iterations, const double* mask, double band_zero, double band_smooth,
+                                                  const double* grad_phi, int method);
+int lsg_extend_from_interface_to_whole_domain_tvd_device(lsg_level_set* ls, const double* phi_dev, const double* q_interface_dev,
+                                                         double* q_dev, int nfields, int iterations, const double* mask_dev,
+                                                         double band_zero, double band_smooth, const double* grad_phi_dev, int method);
+
 /* ---- node interpolation and the semi-Lagrangian step (FP64) --------------------------------- */
 
 /* my_p4est_interpolation_nodes_t(ngbd) + set_input(F, Fxx, Fyy[, Fzz], method) + add_point +

@@ -11,6 +11,9 @@
  *                                                                      src/my_p4est_level_set.h:632-659
  *   extend_Over_Interface_TVD(phi, q, iterations, order, band_use, band_extend, normal, mask)
  *                                                                      src/my_p4est_level_set.h:732-735
+ *   extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero, band_smooth,
+ *                                             cf, grad_phi, blocksize), set_interpolation_on_interface
+ *                                                                      src/my_p4est_level_set.h:775-776, 843
  *   my_p4est_interpolation_nodes_t: set_input, add_point, interpolate  src/my_p4est_interpolation_nodes.h:33-103
  *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1                   src/my_p4est_semi_lagrangian.h:83-196
  *
@@ -202,6 +205,33 @@ class my_p4est_level_set_t {
                                                normal ? nrm.data() : nullptr, mask ? m.p : nullptr));
   }
 
+  void set_interpolation_on_interface(interpolation_method value) { interpolation_on_interface_ = value; }
+
+  // q_interface, q: blocksize values per node, interleaved as in the reference's block vectors; grad_phi_in:
+  // dim values per node, interleaved. The cf callback is not supported (std::invalid_argument).
+  void extend_from_interface_to_whole_domain_TVD(Vec phi, Vec q_interface, Vec q, int iterations = 20, Vec mask = nullptr,
+                                                 double band_zero = 2, double band_smooth = 10,
+                                                 double (*cf)(int32_t, int, double) = nullptr, Vec grad_phi_in = nullptr,
+                                                 const unsigned int& blocksize = 1) const {
+    if (cf != nullptr) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: the cf callback is not supported");
+    const int D = ngbd_->dim();
+    const size_t N = (size_t)ngbd_->num_nodes(), bs = blocksize;
+    lsgpu::VecArray p(phi), qi(q_interface), qo(q), m(mask), g(grad_phi_in);
+    std::vector<double> qi_b(bs * N), q_b(bs * N), g_b;
+    for (size_t n = 0; n < N; ++n)
+      for (size_t k = 0; k < bs; ++k) qi_b[k * N + n] = qi.p[bs * n + k];
+    if (grad_phi_in != nullptr) {
+      g_b.resize((size_t)D * N);
+      for (size_t n = 0; n < N; ++n)
+        for (int a = 0; a < D; ++a) g_b[a * N + n] = g.p[(size_t)D * n + a];
+    }
+    lsgpu::check(lsg_extend_from_interface_to_whole_domain_tvd(ngbd_->device(), p.p, qi_b.data(), q_b.data(), (int)bs, iterations,
+                                                               mask ? m.p : nullptr, band_zero, band_smooth,
+                                                               grad_phi_in ? g_b.data() : nullptr, interpolation_on_interface_));
+    for (size_t n = 0; n < N; ++n)
+      for (size_t k = 0; k < bs; ++k) qo.p[bs * n + k] = q_b[k * N + n];
+  }
+
   // node-sampled velocity: returns dt unchanged
   double advect_in_normal_direction(const Vec vn, Vec phi, const double& dt, Vec phi_xx = nullptr, Vec phi_yy = nullptr,
                                     Vec phi_zz = nullptr) const {
@@ -264,6 +294,7 @@ class my_p4est_level_set_t {
   };
   my_p4est_node_neighbors_t* ngbd_;
   int precision_;
+  interpolation_method interpolation_on_interface_ = quadratic_non_oscillatory_continuous_v2;
 };
 
 // Node interpolation at buffered points (one process: every point is local).

@@ -1418,6 +1418,175 @@ void sl_advect_vortex(const Ctx& cx, int64_t np, const double* xyz, double dt, d
   interpolate_points<D>(cx, phi_method, 1, phi, phi_dd, np, pts.data(), phi_np1, nthreads);
 }
 
+// ---- extension from the interface to the whole domain -----------------------------------------
+// pascalTriangle / smoothstep (src/my_p4est_utils.cpp:3350-3370)
+double pascal_triangle(int a, int b) {
+  double result = 1.;
+  for (int i = 0; i < b; ++i) result *= double(a - i) / double(i + 1);
+  return result;
+}
+double smoothstep(int N, double x) {
+  if (x <= 0) return 0;
+  if (x >= 1) return 1;
+  double result = 0;
+  for (int n = 0; n <= N; ++n) result += pascal_triangle(-N - 1, n) * pascal_triangle(2 * N + 1, N - n) * pow(x, N + n + 1);
+  return result;
+}
+
+// node_x_fr_n(n, p4est, nodes) (src/my_p4est_utils.h:1346-1370)
+template <int D>
+void node_coordinates(const Grid<D>& g, int32_t n, double* xyz) {
+  const int t = g.node_tree[n];
+  for (int a = 0; a < D; ++a) {
+    const int64_t v = g.node_x[(size_t)n * D + a];
+    const double r = v == Grid<D>::ROOT_LEN - 1 ? 1.0 : static_cast<double>(v) / static_cast<double>(Grid<D>::ROOT_LEN);
+    xyz[a] = (g.tv_max[3 * t + a] - g.tv_min[3 * t + a]) * r + g.tv_min[3 * t + a];
+  }
+}
+
+// extend_from_interface_to_whole_domain_TVD_one_iteration (src/my_p4est_level_set.cpp:3181-3323), one
+// field: Godunov upwinding along sgn(phi) grad(phi)/|grad(phi)| with second-order one-sided differences,
+// the neighbour across the interface replaced by the interface value at the subcell distance, Neumann
+// walls. qdd: D x N second derivatives of q.
+template <int D>
+void efi_one_iteration(const Ctx& cx, const double* phi, const double* grad, const double* q, const double* qdd, const double* qi_nb,
+                       const double* s_nb, double* q_out, int nthreads) {
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+  const double zdt = cx.zero_distance_threshold;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+  for (long long n = 0; n < (long long)N; ++n) {
+    if (fabs(phi[n]) < zdt) {
+      q_out[n] = q[n];
+      continue;
+    }
+    const Qnnn<D>& qq = Q[n];
+    double p_000, p_nb[6], q_000, q_nb[6], s[6];
+    ngbd_quadratic(qq, phi, &p_000, p_nb);
+    ngbd_quadratic(qq, q, &q_000, q_nb);
+    for (int dir = 0; dir < 2 * D; ++dir) s[dir] = qq.d[dir];
+    for (int dir = 0; dir < 2 * D; ++dir)
+      if (p_000 * p_nb[dir] < 0.0) {
+        s[dir] = s_nb[(size_t)dir * N + n];
+        q_nb[dir] = qi_nb[(size_t)dir * N + n];
+      }
+    // second derivative of q along each axis at the node and at its two neighbours on that axis
+    double dd_000[3], dd_m[3], dd_p[3];
+    for (int a = 0; a < D; ++a) {
+      double z, nb[6];
+      ngbd_quadratic(qq, qdd + (size_t)a * N, &z, nb);
+      dd_000[a] = z;
+      dd_m[a] = nb[2 * a];
+      dd_p[a] = nb[2 * a + 1];
+    }
+    const uint8_t w = cx.wall[n];
+    for (int a = 0; a < D; ++a) {
+      if (w & (1 << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        q_nb[2 * a] = q_nb[2 * a + 1];
+        dd_000[a] = dd_m[a] = dd_p[a] = 0.0;
+      } else if (w & (1 << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        q_nb[2 * a + 1] = q_nb[2 * a];
+        dd_000[a] = dd_m[a] = dd_p[a] = 0.0;
+      }
+    }
+    double dt = MIN(s[0], s[1]);
+    dt = MIN(dt, s[2], s[3]);
+    if (D == 3) dt = MIN(dt, s[D == 3 ? 4 : 0], s[D == 3 ? 5 : 0]);
+    dt /= ((double)D);
+    const double gx = grad[n], gy = grad[N + n], gz = D == 3 ? grad[2 * N + n] : 0.0;
+    const double mag = D == 3 ? sqrt(gx * gx + gy * gy + gz * gz) : sqrt(gx * gx + gy * gy);
+    const double sg = phi[n] < 0.0 ? -1.0 : +1.0;
+    const double nv[3] = {mag > ORA_EPS ? sg * gx / mag : 0.0, mag > ORA_EPS ? sg * gy / mag : 0.0,
+                          mag > ORA_EPS ? sg * gz / mag : 0.0};
+    double t[3];
+    for (int a = 0; a < D; ++a) {
+      const double qm = (q_000 - q_nb[2 * a]) / s[2 * a] + 0.5 * s[2 * a] * MINMOD(dd_m[a], dd_000[a]);
+      const double qp = (q_nb[2 * a + 1] - q_000) / s[2 * a + 1] - 0.5 * s[2 * a + 1] * MINMOD(dd_p[a], dd_000[a]);
+      t[a] = nv[a] * (nv[a] > 0.0 ? qm : qp);
+    }
+    q_out[n] = q_000 - dt * (D == 3 ? (t[0] + t[1] + t[D == 3 ? 2 : 0]) : (t[0] + t[1]));
+  }
+}
+
+// extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero, band_smooth, cf = NULL,
+// grad_phi) (src/my_p4est_level_set.cpp:3325-3767) for one field with the interpolation method used on
+// the interface (interpolation_on_interface, quadratic_non_oscillatory_continuous_v2 by default):
+// interface values along each grid line crossing the interface, q started from qi within 1.5 dl of the
+// interface, then `iterations` TVD-RK2 steps. grad_in (D x N) may be null (first derivatives of phi).
+template <int D>
+void extend_from_interface(const Ctx& cx, const double* phi, const double* qi, double* q, int iterations, const double* mask,
+                           double band_zero, double band_smooth, const double* grad_in, int method, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
+  const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
+  const int64_t N = cx.N;
+  int max_lvl = 0;
+  for (const Leaf& l : g.leaves) max_lvl = MAX(max_lvl, (int)l.level);
+  double dl = g.tree_dim[0] / pow(2., (double)max_lvl);
+  for (int a = 1; a < D; ++a) dl = MAX(dl, g.tree_dim[a] / pow(2., (double)max_lvl));
+  std::vector<double> qdd((size_t)D * N), grad_store, pdd((size_t)D * N);
+  compute_derivatives<D>(cx, qi, qdd.data(), nthreads);
+  const double* grad = grad_in;
+  if (!grad) {
+    grad_store.resize((size_t)D * N);
+    first_derivatives<D>(cx, phi, grad_store.data(), nthreads);
+    grad = grad_store.data();
+  }
+  compute_derivatives<D>(cx, phi, pdd.data(), nthreads);
+  for (int64_t n = 0; n < N; ++n)
+    q[n] = (mask ? MAX(mask[n], fabs(phi[n])) : fabs(phi[n])) < 1.5 * dl ? qi[n] : 0;
+  // interface values and distances along the 2D directions
+  std::vector<double> qi_nb((size_t)2 * D * N), s_nb((size_t)2 * D * N);
+  std::vector<uint8_t> cross((size_t)N, 0);
+  std::vector<std::vector<double>> pts(2 * D);
+  std::vector<std::vector<int32_t>> who(2 * D);
+  for (int64_t n = 0; n < N; ++n) {
+    const Qnnn<D>& qq = Q[n];
+    double x[3];
+    node_coordinates(g, (int32_t)n, x);
+    double p_000, p_nb[6];
+    ngbd_quadratic(qq, phi, &p_000, p_nb);
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int a = dir / 2;
+      const double* paa = pdd.data() + (size_t)a * N;
+      if (p_000 * p_nb[dir] < 0.0) {
+        double dist = interface_Location_With_Second_Order_Derivative(0, qq.d[dir], p_000, p_nb[dir], paa[n], f_linear(qq, dir, paa));
+        dist = MAX(dist, ORA_EPS);
+        for (int b = 0; b < D; ++b) pts[dir].push_back(b == a ? ((dir & 1) ? x[b] + dist : x[b] - dist) : x[b]);
+        who[dir].push_back((int32_t)n);
+        s_nb[(size_t)dir * N + n] = dist;
+        cross[n] |= (uint8_t)(1u << dir);
+      } else {
+        qi_nb[(size_t)dir * N + n] = qi[n];
+        s_nb[(size_t)dir * N + n] = qq.d[dir];
+      }
+    }
+  }
+  const double a_ = band_zero * dl, b_ = band_smooth * dl;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int64_t np = (int64_t)who[dir].size();
+    std::vector<double> v((size_t)np), m((size_t)np);
+    interpolate_points<D>(cx, method, 1, qi, qdd.data(), np, pts[dir].data(), v.data(), nthreads);
+    if (mask) interpolate_points<D>(cx, ORA_LINEAR, 1, mask, nullptr, np, pts[dir].data(), m.data(), nthreads);
+    for (int64_t k = 0; k < np; ++k) {
+      const int32_t n = who[dir][k];
+      double val = v[k];
+      if (mask) val *= 1. - smoothstep(1, (m[k] - a_) / b_);
+      qi_nb[(size_t)dir * N + n] = val;
+    }
+  }
+  std::vector<double> q1((size_t)N), q2((size_t)N);
+  for (int it = 0; it < iterations; ++it) {
+    compute_derivatives<D>(cx, q, qdd.data(), nthreads);
+    efi_one_iteration<D>(cx, phi, grad, q, qdd.data(), qi_nb.data(), s_nb.data(), q1.data(), nthreads);
+    compute_derivatives<D>(cx, q1.data(), qdd.data(), nthreads);
+    efi_one_iteration<D>(cx, phi, grad, q1.data(), qdd.data(), qi_nb.data(), s_nb.data(), q2.data(), nthreads);
+    for (int64_t n = 0; n < N; ++n) q[n] = .5 * (q[n] + q2[n]);
+  }
+}
+
+
 template <int D>
 Ctx* build_from_leaves(const int* n_xyz, const double* lo, const double* hi, int64_t nleaves, const int32_t* tree,
                        const int32_t* level, const int32_t* xyz) {
@@ -1689,6 +1858,16 @@ int ora_extend_over_interface(void* h, const double* phi, const double* mask, do
     if (order < 0 || order > 2) throw std::invalid_argument("order must be 0, 1 or 2");
     if (cx->dim == 2) extend_over_interface<2>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads);
     else extend_over_interface<3>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads);
+  });
+}
+
+int ora_extend_from_interface(void* h, const double* phi, const double* qi, double* q, int iterations, const double* mask,
+                              double band_zero, double band_smooth, const double* grad, int method, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("extension needs a grid built from leaves");
+    if (cx->dim == 2) extend_from_interface<2>(*cx, phi, qi, q, iterations, mask, band_zero, band_smooth, grad, method, nthreads);
+    else extend_from_interface<3>(*cx, phi, qi, q, iterations, mask, band_zero, band_smooth, grad, method, nthreads);
   });
 }
 

@@ -41,6 +41,7 @@ SIG = {
     "ora_mean_curvature_from_normals": (_I, [_P, _DP, _DP, _I]),
     "ora_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP, _I]),
     "ora_extend_over_interface": (_I, [_P, _DP, _DP, _DP, _I, _I, _D, _D, _DP, _I]),
+    "ora_extend_from_interface": (_I, [_P, _DP, _DP, _DP, _I, _DP, _D, _D, _DP, _I, _I]),
     "ora_interface_location": (_D, [_D, _D, _D, _D]),
     "ora_interface_location_2nd": (_D, [_D, _D, _D, _D, _D, _D]),
 }
@@ -183,6 +184,18 @@ class OracleGrid:
         msk = None if mask is None else np.ascontiguousarray(mask, np.float64)
         _chk(load().ora_extend_over_interface(self._h, _dp(phi), _dp(msk), _dp(q), int(iterations), int(order), float(band_use),
                                               float(band_extend), _dp(nrm), nthreads))
+
+    def extend_from_interface_to_whole_domain_tvd(self, phi, qi, iterations=20, mask=None, band_zero=2.0, band_smooth=10.0,
+                                                  grad_phi=None, method=4, nthreads=1):
+        """Returns q (float64, node order): qi's interface values extended along the normals."""
+        phi = np.ascontiguousarray(phi, np.float64)
+        qi = np.ascontiguousarray(qi, np.float64)
+        q = np.empty(self.N, np.float64)
+        msk = None if mask is None else np.ascontiguousarray(mask, np.float64)
+        g = None if grad_phi is None else np.ascontiguousarray(grad_phi, np.float64)
+        _chk(load().ora_extend_from_interface(self._h, _dp(phi), _dp(qi), _dp(q), int(iterations), _dp(msk), float(band_zero),
+                                              float(band_smooth), _dp(g), int(method), nthreads))
+        return q
 
     # ---- node interpolation and the semi-Lagrangian step ------------------------------------
     def interpolate(self, method, F, xyz, Fdd=None, nthreads=1):

@@ -1,5 +1,5 @@
 // The C++ facade (include/lsgpu.hpp) gives exactly the results of the C ABI it wraps:
-// reinitialisation, normal advection with a function-object velocity, extension over the interface,
+// reinitialisation, normal advection with a function-object velocity, both extensions,
 // node interpolation and the semi-Lagrangian step. Prints "facade ok" on success; exits non-zero otherwise.
 #include <math.h>
 #include <stdio.h>
@@ -105,6 +105,20 @@ int main() {
   lsgpu::check(lsg_extend_over_interface_tvd(raw, phi.values.data(), q_ref.data(), 8, 2, -DBL_MAX, DBL_MAX, nrm_ref.data(),
                                              phi.values.data()));
   if (memcmp(q.values.data(), q_ref.data(), N * sizeof(double)) != 0) return fail("extend_Over_Interface_TVD");
+
+  // extension from the interface, two interleaved components against the ABI's component blocks
+  lsgpu_vec qi2{std::vector<double>((size_t)2 * N)}, qe2{std::vector<double>((size_t)2 * N)};
+  std::vector<double> qi_blocks((size_t)2 * N), qe_ref((size_t)2 * N);
+  for (int64_t i = 0; i < N; ++i) {
+    qi2.values[2 * i] = qi_blocks[i] = xyz[2 * i] + 2.0 * xyz[2 * i + 1];
+    qi2.values[2 * i + 1] = qi_blocks[N + i] = xyz[2 * i] * xyz[2 * i];
+  }
+  ls.set_interpolation_on_interface(quadratic);
+  ls.extend_from_interface_to_whole_domain_TVD(&phi, &qi2, &qe2, 6, nullptr, 2, 10, nullptr, nullptr, 2);
+  lsgpu::check(lsg_extend_from_interface_to_whole_domain_tvd(raw, phi.values.data(), qi_blocks.data(), qe_ref.data(), 2, 6, nullptr, 2,
+                                                             10, nullptr, LSG_QUADRATIC));
+  for (int64_t i = 0; i < N; ++i)
+    if (qe2.values[2 * i] != qe_ref[i] || qe2.values[2 * i + 1] != qe_ref[N + i]) return fail("extend_from_interface_to_whole_domain_TVD");
 
   // errors come back as exceptions
   try {

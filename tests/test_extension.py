@@ -1,10 +1,17 @@
-"""Extension of a field over the interface (extend_Over_Interface_TVD, src/my_p4est_level_set.cpp:969-1764,
-without boundary conditions or initial guesses, one-step extrapolation).
+"""Extension of fields across the interface.
 
-CPU: the oracle's constant / linear / quadratic extensions of a smooth field from the inside of a circle
-converge at orders 1 / 2 / 3 in a band of three cells outside it (to the value at the projection on the
-interface for the constant extension, to the field itself for the others).
-GPU: the FP64 kernels reproduce the oracle bit for bit, with computed or given normals and with a mask."""
+extend_Over_Interface_TVD (src/my_p4est_level_set.cpp:969-1764, without boundary conditions or initial
+guesses, one-step extrapolation): on the CPU the oracle's constant / linear / quadratic extensions of a
+smooth field from the inside of a circle converge at orders 1 / 2 / 3 in a band of three cells outside it
+(to the value at the projection on the interface for the constant extension, to the field itself for the
+others); on the GPU the FP64 kernels reproduce the oracle bit for bit, with computed or given normals and
+with a mask.
+
+extend_from_interface_to_whole_domain_TVD (src/my_p4est_level_set.cpp:3181-3767): the oracle's extension
+of a field's interface values converges at third order in a band of three cells on both sides of a
+circle (to the value at the projection on the interface); on the GPU the kernels reproduce the oracle bit
+for bit for every interpolation method, several fields and a given gradient, and within 1e-12 relative
+with a mask (whose smoothstep goes through pow, rounded differently by the device library)."""
 import numpy as np
 import pytest
 
@@ -124,3 +131,84 @@ def test_gpu_extension_device_entry_and_errors():
     with pytest.raises(ValueError):
         ls.extend_Over_Interface_TVD(phi, q0.copy(), 7, 3)
     assert lib.lsg_extend_over_interface_tvd(ls._h, G._lib.dptr(phi), G._lib.dptr(q0.copy()), 7, 3, 0.0, 1.0, None, None) != 0
+
+
+def test_oracle_whole_domain_extension_converges():
+    errs = []
+    for lmax in (6, 7, 8):
+        f = sphere_grid(2, lmax)
+        og = O.OracleGrid.from_forest(f)
+        x = f.node_xyz()
+        r = np.sqrt(np.sum(x ** 2, axis=1))
+        phi = r - 0.5
+        q = og.extend_from_interface_to_whole_domain_tvd(phi, field(x), iterations=40, nthreads=8)
+        want = field(0.5 * x / np.maximum(r, 1e-12)[:, None])
+        band = np.abs(phi) < 3 * (2.0 / (1 << lmax))
+        errs.append(np.max(np.abs(q[band] - want[band])))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(rates > 2.5), (errs, rates)
+
+
+def test_oracle_whole_domain_extension_keeps_constants():
+    f = sphere_grid(3, 5)
+    og = O.OracleGrid.from_forest(f)
+    x = f.node_xyz()
+    phi = np.sqrt(np.sum(x ** 2, axis=1)) - 0.5
+    q = og.extend_from_interface_to_whole_domain_tvd(phi, np.full(len(phi), 0.75), iterations=60, nthreads=8)
+    near = np.abs(phi) < 0.1  # 1.6 cells: filled from zero by the march, to round-off in 60 steps
+    assert np.max(np.abs(q[near] - 0.75)) < 1e-12
+    assert np.all(q[np.abs(phi) < 0.05] == 0.75)  # started at qi, constant interface values
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(GRIDS))
+def test_gpu_whole_domain_extension_bitwise(name):
+    f = GRIDS[name]()
+    og = O.OracleGrid.from_forest(f)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    x, phi, _ = case(f)
+    qi = field(x)
+    want = og.extend_from_interface_to_whole_domain_tvd(phi, qi, iterations=9, nthreads=8)
+    assert np.array_equal(ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=9), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["circle2d", "flower3d"])
+def test_gpu_whole_domain_extension_options(name):
+    f = GRIDS[name]()
+    og = O.OracleGrid.from_forest(f)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    x, phi, _ = case(f)
+    qi = np.stack([field(x), np.sin(2 * x[:, 0]) * x[:, 1]])
+    grad = og.first_derivatives(phi) * 1.1  # any gradient field
+    for method in range(5):
+        ls.set_interpolation_on_interface(method)
+        got = ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=6, grad_phi_in=grad)
+        for k in range(2):
+            want = og.extend_from_interface_to_whole_domain_tvd(phi, qi[k], iterations=6, grad_phi=grad, method=method, nthreads=8)
+            assert np.array_equal(got[k], want), (method, k)
+    ls.set_interpolation_on_interface(4)
+    mask = 0.3 * x[:, 0] + 0.05
+    want = og.extend_from_interface_to_whole_domain_tvd(phi, qi[1], iterations=6, mask=mask, band_zero=1.0, band_smooth=8.0,
+                                                        nthreads=8)
+    got = ls.extend_from_interface_to_whole_domain_TVD(phi, qi[1], iterations=6, mask=mask, band_zero=1.0, band_smooth=8.0)
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
+    with pytest.raises(G.LsgInvalidArgument):
+        ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=2, mask=mask)
+
+
+@pytest.mark.gpu
+def test_gpu_whole_domain_extension_device_tensors():
+    import torch
+    f = GRIDS["brick3d"]()
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    x, phi, _ = case(f)
+    qi = field(x)
+    host = ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=5)
+    ls.set_stream(torch.cuda.current_stream().cuda_stream)
+    tqi = torch.from_numpy(qi).cuda()
+    tq = ls.extend_from_interface_to_whole_domain_TVD(torch.from_numpy(phi).cuda(), tqi, iterations=5)
+    torch.cuda.synchronize()
+    assert np.array_equal(tq.cpu().numpy(), host)
+    with pytest.raises(G.LsgInvalidArgument):  # output over the input
+        ls.extend_from_interface_to_whole_domain_TVD(torch.from_numpy(phi).cuda(), tqi, q=tqi, iterations=1)
