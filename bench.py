@@ -227,7 +227,8 @@ def run_transport(args):
     (0.35,0.35,0.35); single-vortex velocity u = 2 sin^2(pi x) sin(2 pi y) sin(2 pi z) cos(pi t/T), ...,
     T = 3; dt = dx_min; per step update_p4est (semi-Lagrangian RK2 backtrace with quadratic node
     interpolation + host regrid until the grid settles, velocity at the step's midpoint), a new level
-    set on the new grid, and 5 reinitialisation iterations; mixed and FP64 runs side by side."""
+    set on the new grid (node-neighbour tables built on the GPU), and 5 reinitialisation iterations; mixed
+    and FP64 runs side by side."""
     import math
 
     import torch
@@ -248,7 +249,7 @@ def run_transport(args):
         t = 0.0
         times = {"update_p4est": 0.0, "level_set_setup": 0.0, "reinit": 0.0}
         nodes = []
-        ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+        ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), device_build=True)
         regrid_iters = 0
         torch.cuda.synchronize()
         t_all = time.perf_counter()
@@ -259,7 +260,7 @@ def run_transport(args):
             regrid_iters += sl.iterations
             f = sl.forest_np1
             t1 = time.perf_counter()
-            ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+            ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), device_build=True)
             t2 = time.perf_counter()
             ls.reinitialize_2nd_order(phi, 5, precision=prec)
             t3 = time.perf_counter()

@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "liblsgpu.so")
 
 LSG_OK, LSG_EINVAL, LSG_ENOMEM, LSG_EDEVICE, LSG_ETIMEOUT, LSG_ENAN, LSG_ESTATE = range(7)
 LSG_FP64, LSG_MIXED = 0, 1
+LSG_BUILD_ON_DEVICE = 1
 LSG_VELOCITY_VORTEX = 0
 
 _P = C.c_void_p
@@ -51,6 +52,7 @@ SIGNATURES = {
     "lsg_forest_wall_mask": (_I, [_P, _U8P]),
     "lsg_forest_dxyz_min": (_I, [_P, _DP]),
     "lsg_level_set_create": (_I, [_P, C.POINTER(_P)]),
+    "lsg_level_set_create_ex": (_I, [_P, _I, C.POINTER(_P)]),
     "lsg_level_set_destroy": (_I, [_P]),
     "lsg_level_set_set_stream": (_I, [_P, _P]),
     "lsg_level_set_stream": (_P, [_P]),

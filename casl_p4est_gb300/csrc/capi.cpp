@@ -427,19 +427,21 @@ int lsg_forest_dxyz_min(const lsg_forest* f, double* dxyz) {
   });
 }
 
-int lsg_level_set_create(const lsg_forest* f, lsg_level_set** out) {
+int lsg_level_set_create_ex(const lsg_forest* f, int flags, lsg_level_set** out) {
   return guard([&] {
     need(out != nullptr, "null output pointer");
     need(f != nullptr, "null forest");
+    need((flags & ~LSG_BUILD_ON_DEVICE) == 0, "unknown level set flags");
+    const bool on_device = (flags & LSG_BUILD_ON_DEVICE) != 0;
     lsg_level_set* ls = new lsg_level_set();
     ls->dim = f->dim;
     try {
       if (f->dim == 2) {
         need_nodes(*f->f2);
-        ls->l2 = new LevelSet<2>(*f->f2);
+        ls->l2 = new LevelSet<2>(*f->f2, true, on_device);
       } else {
         need_nodes(*f->f3);
-        ls->l3 = new LevelSet<3>(*f->f3);
+        ls->l3 = new LevelSet<3>(*f->f3, true, on_device);
       }
     } catch (...) {
       delete ls;
@@ -448,6 +450,8 @@ int lsg_level_set_create(const lsg_forest* f, lsg_level_set** out) {
     *out = ls;
   });
 }
+
+int lsg_level_set_create(const lsg_forest* f, lsg_level_set** out) { return lsg_level_set_create_ex(f, 0, out); }
 
 int lsg_level_set_destroy(lsg_level_set* ls) {
   return guard([&] { delete ls; });

@@ -1,0 +1,610 @@
+// Device flattener: the node-neighbour tables built on the GPU from the grid, so that a new grid
+// (every step of a semi-Lagrangian regrid) does not wait on the host.
+//
+//   FP64 tables   construct_neighbors (src/my_p4est_node_neighbors.cpp:114-1201) per node through a
+//                 view over device arrays, then the same row fill as the host flattener
+//                 (fill_row64): one thread per node; correction records numbered by an exclusive
+//                 scan in node order, as the host numbers them.
+//   mixed tables  the classification, geometry classes and device node order of the host's
+//                 build_tables32, restated with sorts and scans (see the second half of this file).
+//
+// Compiled with -fmad=false: every double expression rounds as the host flattener's
+// (-ffp-contract=off) does, so the FP64 tables are bit-identical to the host's.
+#include <cub/cub.cuh>
+
+#include "flatten.hpp"
+#include "tables.hpp"
+
+namespace lsg {
+
+// The grid as construct_neighbors_v reads it, over device arrays.
+template <int D>
+struct DeviceForestView {
+  DForest<D> F;
+  __device__ int32_t node_tree(int32_t n) const { return F.node_tree[n]; }
+  __device__ int32_t node_x(int32_t n, int a) const { return F.node_x[(int64_t)D * n + a]; }
+  __device__ void node_unclamped(int32_t n, int32_t* x) const {
+    for (int a = 0; a < D; ++a) {
+      const int32_t v = F.node_x[(int64_t)D * n + a];
+      x[a] = (v == Dim<D>::ROOT_LEN - 1) ? Dim<D>::ROOT_LEN : v;
+    }
+  }
+  __device__ int nt(int a) const { return F.n[a]; }
+  __device__ int tree_ijk(int32_t t, int a) const { return F.tree_ijk[3 * t + a]; }
+  __device__ int32_t tree_at(const int* ijk) const {
+    return F.ijk_to_tree[(int64_t)F.n[0] * F.n[1] * (D == 3 ? ijk[2] : 0) + (int64_t)F.n[0] * ijk[1] + ijk[0]];
+  }
+  __device__ double tmin(int32_t t, int a) const { return F.tmin[3 * t + a]; }
+  __device__ double tmax(int32_t t, int a) const { return F.tmax[3 * t + a]; }
+  // leaf of `tree` containing the logical point X: coarse-cell table, then a binary search on the keys
+  __device__ int32_t find_leaf(int32_t tree, const int32_t* X) const {
+    int32_t c[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) c[a] = X[a] >> (Dim<D>::MAXLEVEL - F.L0);
+    const int64_t idx = (int64_t)tree * F.ncoarse + (int64_t)morton<D>(c);
+    int32_t lo = F.ctab[idx], hi = F.ctab[idx + 1];
+    const uint64_t key = ((uint64_t)tree << tree_shift<D>()) | morton<D>(X);
+    while (lo < hi) {
+      const int32_t mid = (lo + hi + 1) >> 1;
+      if (F.key[mid] <= key)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    if (leaf_tree(lo) != tree) return -1;
+    const int32_t h = quadrant_len(Dim<D>::MAXLEVEL, F.level[lo]);
+    for (int a = 0; a < D; ++a) {
+      const int32_t x0 = leaf_x(lo, a);
+      if (X[a] < x0 || X[a] >= x0 + h) return -1;
+    }
+    return lo;
+  }
+  __device__ int leaf_level(int32_t q) const { return F.level[q]; }
+  __device__ int32_t leaf_tree(int32_t q) const { return (int32_t)(F.key[q] >> tree_shift<D>()); }
+  __device__ int32_t leaf_x(int32_t q, int a) const {
+    int32_t x[3] = {0, 0, 0};
+    unmorton<D>(F.key[q] & ((uint64_t(1) << tree_shift<D>()) - 1), x);
+    return x[a];
+  }
+  __device__ int32_t local_node(int32_t q, int c) const { return F.local_nodes[(int64_t)Dim<D>::CHILDREN * q + c]; }
+};
+
+namespace {
+
+constexpr int TPB = 256;
+
+// irregular-group outputs of the mixed tables
+struct DMixedOut {
+  uint32_t* i_meta;
+  uint32_t* i_cls;
+  int32_t* i_nbr;
+  float* i_wf;
+  float* i_d;
+  float* i_q;
+  int32_t* i_cidx;
+  double* i_wf64;
+  double* i_d64;
+  double* i_q64;
+};
+inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_rows64(DForest<D> F, int32_t* __restrict__ nbr, double* __restrict__ w, double* __restrict__ nrm,
+                                                double* __restrict__ d, double* __restrict__ q, uint8_t* __restrict__ wall,
+                                                double* __restrict__ smin, int32_t* __restrict__ needs, int* __restrict__ failed) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = F.N;
+  if (n >= N) return;
+  const DeviceForestView<D> V{F};
+  Qnnn<D> rec;
+  if (construct_neighbors_v<D>(V, (int32_t)n, rec)) {
+    atomicAdd(failed, 1);
+    needs[n] = 0;
+    return;
+  }
+  needs[n] = fill_row64<D>(rec, N, n, nbr, w, nrm, d, q, smin) ? 1 : 0;
+  wall[n] = (uint8_t)wall_mask_v<D>(V, (int32_t)n);
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_crec64(DForest<D> F, const int32_t* __restrict__ needs, const int32_t* __restrict__ scan,
+                                                int32_t* __restrict__ cidx, double* __restrict__ crec) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= F.N) return;
+  if (!needs[n]) {
+    cidx[n] = -1;
+    return;
+  }
+  const int32_t r = scan[n];
+  cidx[n] = r;
+  const DeviceForestView<D> V{F};
+  Qnnn<D> rec;
+  construct_neighbors_v<D>(V, (int32_t)n, rec);
+  cross_terms<D>(rec, crec + (int64_t)6 * r);
+}
+
+// ---- mixed tables -------------------------------------------------------------------------------
+// level code of every neighbour distance: l with tree_size * 2^-l == d exactly (-1 if none), and the
+// smallest code present (the base level)
+template <int D>
+__global__ void __launch_bounds__(TPB) k_lvl_codes(const double* __restrict__ d, int64_t N, double ts0, double ts1, double ts2,
+                                                   int8_t* __restrict__ code, int* __restrict__ base_min) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  int best = 64;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const double dv = d[(int64_t)dir * N + n];
+    const int a = dir >> 1;
+    const double size = a == 0 ? ts0 : (a == 1 ? ts1 : ts2);
+    int8_t c = -1;
+    if (dv > 0) {
+      int l = 0;
+      double h = size;
+      while (h > dv && l < 63) {
+        h *= 0.5;
+        ++l;
+      }
+      if (h == dv) {
+        c = (int8_t)l;
+        best = min(best, l);
+      }
+    }
+    code[(int64_t)dir * N + n] = c;
+  }
+  if (best < 64) atomicMin(base_min, best);
+}
+
+// regular: no wall, no correction, one face node with weight 1 and no third-order factor per
+// direction, every level code within [base, base + 15]; face-node counts of every node
+template <int D>
+__global__ void __launch_bounds__(TPB) k_classify(DTab64<D> T, const int8_t* __restrict__ code, int base, uint8_t* __restrict__ is_reg,
+                                                  uint32_t* __restrict__ icount, int32_t* __restrict__ irr_flag) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N) return;
+  uint32_t counts = 0;
+  bool regular = T.wall[n] == 0 && T.cidx[n] < 0;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    int cnt = 0;
+    for (int k = 0; k < H; ++k)
+      if (T.nbr[(int64_t)(dir * H + k) * N + n] >= 0) cnt = k + 1;
+    counts |= (uint32_t)(cnt - 1) << (2 * dir);
+    if (cnt != 1) regular = false;
+    for (int j = 0; j < D - 1; ++j)
+      if (T.q[(int64_t)(dir * (D - 1) + j) * N + n] != 0.0) regular = false;
+    const int lc = code[(int64_t)dir * N + n];
+    if (lc < base || lc > base + 15) regular = false;
+  }
+  icount[n] = counts;
+  is_reg[n] = regular ? 1 : 0;
+  irr_flag[n] = regular ? 0 : 1;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t h) {
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdull;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ull;
+  h ^= h >> 33;
+  return h;
+}
+
+// geometry class record of every irregular node (slot k = its rank among the irregular nodes in
+// node order), with a hash of its bits for grouping equal records
+template <int D>
+__global__ void __launch_bounds__(TPB) k_records(DTab64<D> T, const uint8_t* __restrict__ is_reg, const uint32_t* __restrict__ icount,
+                                                 const int32_t* __restrict__ irr_pos, double* __restrict__ rec, uint64_t* __restrict__ hash,
+                                                 int32_t* __restrict__ slot, int32_t* __restrict__ irr_node) {
+  constexpr int H = Dim<D>::HALF;
+  constexpr int CW = cls_words<D>();
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N || is_reg[n]) return;
+  const int32_t k = irr_pos[n];
+  const uint32_t counts = icount[n];
+  double r[CW];
+  for (int w = 0; w < CW; ++w) r[w] = 0.0;
+  const uint32_t meta = counts | ((T.cidx[n] >= 0) ? (1u << 16) : 0u) | ((uint32_t)T.wall[n] << 24);
+  r[0] = (double)meta;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int cnt = (int)((counts >> (2 * dir)) & 3) + 1;
+    r[1 + dir] = T.d[(int64_t)dir * N + n];
+    const double nr = T.nrm[(int64_t)dir * N + n];
+    for (int kk = 0; kk < H; ++kk) r[1 + 2 * D + dir * H + kk] = kk < cnt ? T.w[(int64_t)(dir * H + kk) * N + n] / nr : 0.0;
+    for (int j = 0; j < D - 1; ++j) r[1 + 2 * D + 2 * D * H + dir * (D - 1) + j] = T.q[(int64_t)(dir * (D - 1) + j) * N + n];
+  }
+  double* cm = r + 1 + 2 * D + 2 * D * H + 2 * D * (D - 1);
+  for (int c = 0; c < D; ++c) {
+    double e[3] = {0, 0, 0};
+    e[c] = 1.0;
+    if (T.cidx[n] >= 0) apply_correction<D>(T.crec + (int64_t)6 * T.cidx[n], e);
+    for (int rr = 0; rr < D; ++rr) cm[rr * D + c] = e[rr];
+  }
+  uint64_t h = 0x9E3779B97F4A7C15ull;
+  for (int w = 0; w < CW; ++w) {
+    const uint64_t b = (uint64_t)__double_as_longlong(r[w]);
+    rec[(int64_t)k * CW + w] = r[w];
+    h = mix64(h ^ b) + 0x9E3779B97F4A7C15ull;
+  }
+  hash[k] = h;
+  slot[k] = k;
+  irr_node[k] = (int32_t)n;
+}
+
+// first of each run of equal records in hash order
+template <int D>
+__global__ void __launch_bounds__(TPB) k_class_flags(const double* __restrict__ rec, const int32_t* __restrict__ sorted_slot, int64_t nI,
+                                                     int32_t* __restrict__ flag) {
+  constexpr int CW = cls_words<D>();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nI) return;
+  int f = 1;
+  if (i > 0) {
+    const double* a = rec + (int64_t)sorted_slot[i] * CW;
+    const double* b = rec + (int64_t)sorted_slot[i - 1] * CW;
+    f = 0;
+    for (int w = 0; w < CW; ++w)
+      if (__double_as_longlong(a[w]) != __double_as_longlong(b[w])) f = 1;
+  }
+  flag[i] = f;
+}
+
+// class index of every irregular node, the class records (FP64, and FP32 with the meta word as bits),
+// and each irregular node's rank in (class, node) order
+template <int D>
+__global__ void __launch_bounds__(TPB) k_class_write(const double* __restrict__ rec, const int32_t* __restrict__ sorted_slot,
+                                                     const int32_t* __restrict__ irr_node, const int32_t* __restrict__ flag,
+                                                     const int32_t* __restrict__ excl, int64_t nI, double* __restrict__ cls64,
+                                                     float* __restrict__ cls32, int32_t* __restrict__ node_cls, int32_t* __restrict__ irr_rank) {
+  constexpr int CW = cls_words<D>();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nI) return;
+  const int32_t c = excl[i] + flag[i] - 1;
+  const int32_t k = sorted_slot[i];
+  const int32_t n = irr_node[k];
+  node_cls[n] = c;
+  irr_rank[n] = (int32_t)i;
+  if (flag[i]) {
+    const double* r = rec + (int64_t)k * CW;
+    for (int w = 0; w < CW; ++w) {
+      cls64[(int64_t)c * CW + w] = r[w];
+      cls32[(int64_t)c * CW + w] = (float)r[w];
+    }
+    const uint32_t meta = (uint32_t)r[0];
+    cls32[(int64_t)c * CW] = __uint_as_float(meta);
+  }
+}
+
+// regular nodes: second neighbour along each direction (the face node's own face node further out,
+// when the face node is regular and points back), outer level codes, and the uniform flag
+// (every own and outer code equal); face nodes without a recorded second neighbour join the extended
+// second-derivative set. meta2: far codes | all << 31 | uniform << 30.
+template <int D>
+__global__ void __launch_bounds__(TPB) k_regular_info(DTab64<D> T, const int8_t* __restrict__ code, int base, const uint8_t* __restrict__ is_reg,
+                                                      uint32_t* __restrict__ meta2, uint8_t* __restrict__ in_x) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N || !is_reg[n]) return;
+  uint32_t far = 0;
+  bool all = true;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int32_t j = T.nbr[(int64_t)(dir * H) * N + n];
+    const int back = dir ^ 1;
+    if (is_reg[j] && T.nbr[(int64_t)(back * H) * N + j] == (int32_t)n) {
+      far |= ((uint32_t)(code[(int64_t)dir * N + j] - base) & 15u) << (4 * dir);
+    } else {
+      all = false;
+      if (is_reg[j]) in_x[j] = 1;
+    }
+  }
+  bool uniform = all;
+  const int c0 = code[n] - base;
+  for (int dir = 0; dir < 2 * D && uniform; ++dir)
+    uniform = (code[(int64_t)dir * N + n] - base) == c0 && (int)((far >> (4 * dir)) & 15u) == c0;
+  meta2[n] = far | (all ? (1u << 31) : 0u) | (uniform ? (1u << 30) : 0u);
+}
+
+// regular face nodes of irregular nodes join the extended set
+template <int D>
+__global__ void __launch_bounds__(TPB) k_mark_irregular(DTab64<D> T, const uint8_t* __restrict__ is_reg, uint8_t* __restrict__ in_x) {
+  constexpr int NS = 2 * D * Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (n >= N || is_reg[n]) return;
+  for (int sl = 0; sl < NS; ++sl) {
+    const int32_t j = T.nbr[(int64_t)sl * N + n];
+    if (j >= 0 && is_reg[j]) in_x[j] = 1;
+  }
+}
+
+// device order key: regular groups [uniform outside the set | uniform in the set | other in the set |
+// other outside] in node order, then the irregular nodes by (class, node)
+__global__ void __launch_bounds__(TPB) k_perm_keys(const uint8_t* __restrict__ is_reg, const uint32_t* __restrict__ meta2,
+                                                   const uint8_t* __restrict__ in_x, const int32_t* __restrict__ irr_rank, int64_t N,
+                                                   uint64_t* __restrict__ keys, int32_t* __restrict__ vals,
+                                                   unsigned long long* __restrict__ counts) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  uint64_t group, pos;
+  if (is_reg[n]) {
+    const bool uni = (meta2[n] >> 30) & 1u, inset = in_x[n] != 0;
+    group = uni ? (inset ? 1 : 0) : (inset ? 2 : 3);
+    pos = (uint64_t)n;
+  } else {
+    group = 4;
+    pos = (uint64_t)irr_rank[n];
+  }
+  keys[n] = (group << 40) | pos;
+  vals[n] = (int32_t)n;
+  atomicAdd(counts + group, 1ull);
+}
+
+__global__ void __launch_bounds__(TPB) k_iperm(const int32_t* __restrict__ perm, int64_t N, int32_t* __restrict__ iperm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) iperm[perm[i]] = (int32_t)i;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_fill_regular(DTab64<D> T, const int8_t* __restrict__ code, int base,
+                                                      const uint8_t* __restrict__ is_reg, const uint32_t* __restrict__ meta2n,
+                                                      const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm, int64_t nR,
+                                                      uint32_t* __restrict__ r_meta, int32_t* __restrict__ r_nbr, int32_t* __restrict__ r_nbr2,
+                                                      uint32_t* __restrict__ r_meta2) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nR) return;
+  const int64_t N = T.N;
+  const int64_t n = perm[i];
+  uint32_t codes = 0;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    codes |= (uint32_t)(code[(int64_t)dir * N + n] - base) << (4 * dir);
+    const int32_t j = T.nbr[(int64_t)(dir * H) * N + n];
+    r_nbr[(int64_t)dir * nR + i] = iperm[j];
+    const bool two = is_reg[j] && T.nbr[(int64_t)((dir ^ 1) * H) * N + j] == (int32_t)n;
+    r_nbr2[(int64_t)dir * nR + i] = two ? iperm[T.nbr[(int64_t)(dir * H) * N + j]] : -1;
+  }
+  r_meta[i] = codes;
+  r_meta2[i] = meta2n[n];
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_fill_irregular(DTab64<D> T, const uint32_t* __restrict__ icount, const int32_t* __restrict__ node_cls,
+                                                        const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm, int64_t nR,
+                                                        DMixedOut O) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t N = T.N;
+  const int64_t nI = N - nR;
+  const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= nI) return;
+  const int64_t n = perm[nR + ii];
+  uint32_t meta = icount[n];
+  if (T.cidx[n] >= 0) meta |= 1u << 16;
+  meta |= (uint32_t)T.wall[n] << 24;
+  O.i_meta[ii] = meta;
+  O.i_cls[ii] = (uint32_t)node_cls[n];
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const int cnt = (int)((icount[n] >> (2 * dir)) & 3) + 1;
+    const double nr = T.nrm[(int64_t)dir * N + n];
+    for (int k = 0; k < H; ++k) {
+      const int32_t nb = T.nbr[(int64_t)(dir * H + k) * N + n];
+      O.i_nbr[(int64_t)(dir * H + k) * nI + ii] = k < cnt ? iperm[nb] : iperm[T.nbr[(int64_t)(dir * H) * N + n]];
+      const double wn = k < cnt ? T.w[(int64_t)(dir * H + k) * N + n] / nr : 0.0;
+      O.i_wf[(int64_t)(dir * H + k) * nI + ii] = (float)wn;
+      O.i_wf64[(int64_t)(dir * H + k) * nI + ii] = wn;
+    }
+    O.i_d[(int64_t)dir * nI + ii] = (float)T.d[(int64_t)dir * N + n];
+    O.i_d64[(int64_t)dir * nI + ii] = T.d[(int64_t)dir * N + n];
+    for (int j = 0; j < D - 1; ++j) {
+      O.i_q[(int64_t)(dir * (D - 1) + j) * nI + ii] = (float)T.q[(int64_t)(dir * (D - 1) + j) * N + n];
+      O.i_q64[(int64_t)(dir * (D - 1) + j) * nI + ii] = T.q[(int64_t)(dir * (D - 1) + j) * N + n];
+    }
+  }
+  O.i_cidx[ii] = T.cidx[n];
+}
+
+// correction matrices: correct_naive_second_derivatives applied to the unit vectors
+template <int D>
+__global__ void __launch_bounds__(TPB) k_corr(const double* __restrict__ crec, int64_t R, float* __restrict__ corr, double* __restrict__ corr64) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  for (int c = 0; c < D; ++c) {
+    double e[3] = {0, 0, 0};
+    e[c] = 1.0;
+    apply_correction<D>(crec + 6 * r, e);
+    for (int rr = 0; rr < D; ++rr) {
+      corr[(int64_t)D * D * r + D * rr + c] = (float)e[rr];
+      corr64[(int64_t)D * D * r + D * rr + c] = e[rr];
+    }
+  }
+}
+
+}  // namespace
+
+// exclusive prefix sum of n int32 values (CUB), temp storage from a grow-only buffer
+static void exclusive_sum(const int32_t* in, int32_t* out, int64_t n, DevBuf<uint8_t>& temp, cudaStream_t s) {
+  if (n == 0) return;
+  size_t bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)n, s);
+  temp.ensure(bytes + 1);
+  cuda_check(cub::DeviceScan::ExclusiveSum(temp.p, bytes, in, out, (int)n, s), "exclusive scan");
+}
+
+// total of a 0/1 flag array given its exclusive scan
+static int64_t scan_total(const int32_t* flags, const int32_t* excl, int64_t n, cudaStream_t s) {
+  if (n == 0) return 0;
+  int32_t a = 0, b = 0;
+  cuda_check(cudaMemcpyAsync(&a, flags + n - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaMemcpyAsync(&b, excl + n - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "scan total");
+  return (int64_t)a + b;
+}
+
+template <int D>
+int64_t build_tables64_device(const DForest<D>& F, const Tab64Dev<D>& out, cudaStream_t s) {
+  constexpr int NS = 2 * D * Dim<D>::HALF;
+  const int64_t N = F.N;
+  out.nbr->alloc((size_t)NS * N);
+  out.w->alloc((size_t)NS * N);
+  out.nrm->alloc((size_t)2 * D * N);
+  out.d->alloc((size_t)2 * D * N);
+  out.q->alloc((size_t)2 * D * (D - 1) * N);
+  out.cidx->alloc((size_t)N);
+  out.wall->alloc((size_t)N);
+  out.smin->alloc((size_t)N);
+  DevBuf<int32_t> needs, scan;
+  DevBuf<int> failed;
+  DevBuf<uint8_t> temp;
+  needs.alloc((size_t)N + 1);
+  scan.alloc((size_t)N + 1);
+  failed.alloc(1);
+  cuda_check(cudaMemsetAsync(failed.p, 0, sizeof(int), s), "memset");
+  if (N) k_rows64<D><<<nblocks(N), TPB, 0, s>>>(F, out.nbr->p, out.w->p, out.nrm->p, out.d->p, out.q->p, out.wall->p, out.smin->p, needs.p,
+                                                failed.p);
+  cuda_check(cudaGetLastError(), "device flattener rows");
+  exclusive_sum(needs.p, scan.p, N, temp, s);
+  int nfail = 0;
+  cuda_check(cudaMemcpyAsync(&nfail, failed.p, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+  const int64_t R = scan_total(needs.p, scan.p, N, s);
+  if (nfail) throw std::runtime_error("node neighbours: incomplete stencil in a single-process forest");
+  out.crec->alloc((size_t)6 * R + 6);
+  if (N) k_crec64<D><<<nblocks(N), TPB, 0, s>>>(F, needs.p, scan.p, out.cidx->p, out.crec->p);
+  cuda_check(cudaGetLastError(), "device flattener corrections");
+  cuda_check(cudaStreamSynchronize(s), "device flattener");
+  return R;
+}
+
+template <int D>
+void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDev<D>& M, cudaStream_t s) {
+  constexpr int H = Dim<D>::HALF;
+  constexpr int NS = 2 * D * H;
+  constexpr int CW = cls_words<D>();
+  const int64_t N = T.N;
+  DevBuf<uint8_t> temp, is_reg, in_x;
+  DevBuf<int8_t> code;
+  DevBuf<int> base_min;
+  DevBuf<uint32_t> icount, meta2n;
+  DevBuf<int32_t> irr_flag, irr_pos, slot, slot_sorted, irr_node, flag, excl, node_cls, irr_rank, vals;
+  DevBuf<uint64_t> hash, hash_sorted, keys, keys_sorted;
+  DevBuf<double> rec;
+  DevBuf<unsigned long long> counts;
+  code.alloc((size_t)2 * D * N + 1);
+  base_min.alloc(1);
+  is_reg.alloc((size_t)N + 1);
+  in_x.alloc((size_t)N + 1);
+  icount.alloc((size_t)N + 1);
+  meta2n.alloc((size_t)N + 1);
+  irr_flag.alloc((size_t)N + 1);
+  irr_pos.alloc((size_t)N + 1);
+  node_cls.alloc((size_t)N + 1);
+  irr_rank.alloc((size_t)N + 1);
+  counts.alloc(5);
+  // base level
+  int h_base = 64;
+  cuda_check(cudaMemcpyAsync(base_min.p, &h_base, sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+  if (N) k_lvl_codes<D><<<nblocks(N), TPB, 0, s>>>(T.d, N, ts[0], ts[1], D == 3 ? ts[2] : 1.0, code.p, base_min.p);
+  cuda_check(cudaMemcpyAsync(&h_base, base_min.p, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "base level");
+  const int base = h_base == 64 ? 0 : h_base;
+  M.base = base;
+  // classification
+  if (N) k_classify<D><<<nblocks(N), TPB, 0, s>>>(T, code.p, base, is_reg.p, icount.p, irr_flag.p);
+  exclusive_sum(irr_flag.p, irr_pos.p, N, temp, s);
+  const int64_t nI = scan_total(irr_flag.p, irr_pos.p, N, s);
+  const int64_t nR = N - nI;
+  // geometry classes: records, grouped by hash (stable: node order inside a group), runs of equal records
+  rec.alloc((size_t)nI * CW + 1);
+  hash.alloc((size_t)nI + 1);
+  hash_sorted.alloc((size_t)nI + 1);
+  slot.alloc((size_t)nI + 1);
+  slot_sorted.alloc((size_t)nI + 1);
+  irr_node.alloc((size_t)nI + 1);
+  flag.alloc((size_t)nI + 1);
+  excl.alloc((size_t)nI + 1);
+  int64_t ncls = 0;
+  if (nI) {
+    k_records<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg.p, icount.p, irr_pos.p, rec.p, hash.p, slot.p, irr_node.p);
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, hash.p, hash_sorted.p, slot.p, slot_sorted.p, (int)nI, 0, 64, s);
+    temp.ensure(bytes + 1);
+    cuda_check(cub::DeviceRadixSort::SortPairs(temp.p, bytes, hash.p, hash_sorted.p, slot.p, slot_sorted.p, (int)nI, 0, 64, s),
+               "class sort");
+    k_class_flags<D><<<nblocks(nI), TPB, 0, s>>>(rec.p, slot_sorted.p, nI, flag.p);
+    exclusive_sum(flag.p, excl.p, nI, temp, s);
+    ncls = scan_total(flag.p, excl.p, nI, s);
+  }
+  M.cls32->alloc((size_t)ncls * CW + 1);
+  DevBuf<double> cls64;
+  cls64.alloc((size_t)ncls * CW + 1);
+  if (nI)
+    k_class_write<D><<<nblocks(nI), TPB, 0, s>>>(rec.p, slot_sorted.p, irr_node.p, flag.p, excl.p, nI, cls64.p, M.cls32->p, node_cls.p,
+                                                 irr_rank.p);
+  M.ncls = ncls;
+  // regular nodes: second neighbours, uniform flag, extended set
+  cuda_check(cudaMemsetAsync(in_x.p, 0, (size_t)N + 1, s), "memset");
+  cuda_check(cudaMemsetAsync(meta2n.p, 0, ((size_t)N + 1) * sizeof(uint32_t), s), "memset");
+  cuda_check(cudaMemsetAsync(counts.p, 0, 5 * sizeof(unsigned long long), s), "memset");
+  if (N) {
+    k_regular_info<D><<<nblocks(N), TPB, 0, s>>>(T, code.p, base, is_reg.p, meta2n.p, in_x.p);
+    k_mark_irregular<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg.p, in_x.p);
+  }
+  // device order
+  keys.alloc((size_t)N + 1);
+  keys_sorted.alloc((size_t)N + 1);
+  vals.alloc((size_t)N + 1);
+  M.perm->alloc((size_t)N);
+  M.iperm->alloc((size_t)N);
+  if (N) {
+    k_perm_keys<<<nblocks(N), TPB, 0, s>>>(is_reg.p, meta2n.p, in_x.p, irr_rank.p, N, keys.p, vals.p, counts.p);
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys.p, keys_sorted.p, vals.p, M.perm->p, (int)N, 0, 43, s);
+    temp.ensure(bytes + 1);
+    cuda_check(cub::DeviceRadixSort::SortPairs(temp.p, bytes, keys.p, keys_sorted.p, vals.p, M.perm->p, (int)N, 0, 43, s), "order sort");
+    k_iperm<<<nblocks(N), TPB, 0, s>>>(M.perm->p, N, M.iperm->p);
+  }
+  unsigned long long g[5] = {0, 0, 0, 0, 0};
+  cuda_check(cudaMemcpyAsync(g, counts.p, sizeof(g), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "group counts");
+  if ((int64_t)(g[0] + g[1] + g[2] + g[3]) != nR || (int64_t)g[4] != nI) throw std::runtime_error("device flattener: group counts");
+  M.nR = nR;
+  M.nI = nI;
+  M.nU = (int64_t)(g[0] + g[1]);
+  M.x_first = (int64_t)g[0];
+  M.nX = (int64_t)(g[1] + g[2]);
+  // regular group
+  M.r_meta->alloc((size_t)nR + 1);
+  M.r_nbr->alloc((size_t)2 * D * nR + 1);
+  M.r_nbr2->alloc((size_t)2 * D * nR + 1);
+  M.r_meta2->alloc((size_t)nR + 1);
+  if (nR)
+    k_fill_regular<D><<<nblocks(nR), TPB, 0, s>>>(T, code.p, base, is_reg.p, meta2n.p, M.perm->p, M.iperm->p, nR, M.r_meta->p, M.r_nbr->p,
+                                                  M.r_nbr2->p, M.r_meta2->p);
+  // irregular group
+  M.i_meta->alloc((size_t)nI + 1);
+  M.i_cls->alloc((size_t)nI + 1);
+  M.i_nbr->alloc((size_t)NS * nI + 1);
+  M.i_wf->alloc((size_t)NS * nI + 1);
+  M.i_d->alloc((size_t)2 * D * nI + 1);
+  M.i_q->alloc((size_t)2 * D * (D - 1) * nI + 1);
+  M.i_cidx->alloc((size_t)nI + 1);
+  M.i_wf64->alloc((size_t)NS * nI + 1);
+  M.i_d64->alloc((size_t)2 * D * nI + 1);
+  M.i_q64->alloc((size_t)2 * D * (D - 1) * nI + 1);
+  DMixedOut O{M.i_meta->p, M.i_cls->p, M.i_nbr->p, M.i_wf->p, M.i_d->p, M.i_q->p, M.i_cidx->p, M.i_wf64->p, M.i_d64->p, M.i_q64->p};
+  if (nI) k_fill_irregular<D><<<nblocks(nI), TPB, 0, s>>>(T, icount.p, node_cls.p, M.perm->p, M.iperm->p, nR, O);
+  // correction matrices
+  M.corr->alloc((size_t)D * D * R + 1);
+  M.corr64->alloc((size_t)D * D * R + 1);
+  if (R) k_corr<D><<<nblocks(R), TPB, 0, s>>>(T.crec, R, M.corr->p, M.corr64->p);
+  cuda_check(cudaGetLastError(), "device flattener (mixed)");
+  cuda_check(cudaStreamSynchronize(s), "device flattener (mixed)");
+}
+
+#define LSG_INST(D)                                                                          \
+  template int64_t build_tables64_device<D>(const DForest<D>&, const Tab64Dev<D>&, cudaStream_t); \
+  template void build_mixed_device<D>(const DTab64<D>&, int64_t, const double*, MixedDev<D>&, cudaStream_t);
+LSG_INST(2)
+LSG_INST(3)
+#undef LSG_INST
+
+}  // namespace lsg

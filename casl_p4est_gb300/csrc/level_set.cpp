@@ -1,6 +1,8 @@
 // Host drivers of the device level-set operator (see level_set.hpp).
 #include "level_set.hpp"
 
+#include "flatten.hpp"
+
 #include <float.h>
 
 #include <algorithm>
@@ -74,17 +76,62 @@ void KernelTimer::reset() {
   } while (0)
 
 template <int D>
-LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed) : F(&forest) {
+LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed, bool device_build) : F(&forest) {
   if (!forest.nodes_built) throw std::invalid_argument("level set: the forest's nodes are not built");
   double tdim[3];
   for (int a = 0; a < D; ++a) tdim[a] = (forest.brick.xyz_max[a] - forest.brick.xyz_min[a]) / forest.brick.n[a];
   zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
-  Tables64<D> T;
-  build_tables64<D>(forest, T);
   double ts[3];
   for (int a = 0; a < D; ++a) ts[a] = forest.brick.tmax[a] - forest.brick.tmin[a];
-  init_tables(T, ts, with_mixed);
+  if (!device_build) {
+    Tables64<D> T;
+    build_tables64<D>(forest, T);
+    init_tables(T, ts, with_mixed);
+  } else {
+    N = (int64_t)forest.num_nodes();
+    init_stream();
+    build_locator();
+    fl_tree_ijk.upload(forest.brick.tree_ijk, stream);
+    fl_node_tree.upload(forest.node_tree, stream);
+    fl_node_x.upload(forest.node_x, stream);
+    DForest<D> DF{};
+    DF.nleaves = TL.nleaves;
+    DF.N = N;
+    DF.key = TL.key;
+    DF.level = TL.level;
+    DF.local_nodes = TL.local_nodes;
+    DF.ctab = TL.ctab;
+    DF.L0 = TL.L0;
+    DF.ncoarse = TL.ncoarse;
+    for (int a = 0; a < 3; ++a) DF.n[a] = TL.n[a];
+    DF.ijk_to_tree = TL.ijk_to_tree;
+    DF.tree_ijk = fl_tree_ijk.p;
+    DF.tmin = TL.tmin;
+    DF.tmax = TL.tmax;
+    DF.node_tree = fl_node_tree.p;
+    DF.node_x = fl_node_x.p;
+    const Tab64Dev<D> out{&nbr, &w, &nrm, &d, &q, &cidx, &crec, &wall, &smin};
+    num_corrections = build_tables64_device<D>(DF, out, stream);
+    T64.N = N;
+    T64.nbr = nbr.p;
+    T64.w = w.p;
+    T64.nrm = nrm.p;
+    T64.d = d.p;
+    T64.q = q.p;
+    T64.cidx = cidx.p;
+    T64.crec = crec.p;
+    T64.wall = wall.p;
+    device_flat = true;
+    if (with_mixed) build_mixed();
+  }
   part_offsets = {0, N};
+}
+
+template <int D>
+void LevelSet<D>::init_stream() {
+  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  own_stream = true;
+  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) cfg.uniform_blocks = atoi(ub);
 }
 
 template <int D>
@@ -124,9 +171,7 @@ LevelSet<D>::LevelSet(const std::vector<const Forest<D>*>& parts) : F(nullptr) {
 template <int D>
 void LevelSet<D>::init_tables(const Tables64<D>& T, const double* ts, bool with_mixed) {
   N = T.N;
-  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  own_stream = true;
-  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) cfg.uniform_blocks = atoi(ub);
+  init_stream();
   num_corrections = (int64_t)(T.crec.size() / 6);
   nbr.upload(T.nbr, stream);
   w.upload(T.w, stream);
@@ -245,6 +290,17 @@ template <int D>
 void LevelSet<D>::build_mixed() {
   if (mixed_ready) return;
   if (!F) throw std::invalid_argument("level set: mixed tables of a grid union are built at construction");
+  if (device_flat) {
+    double ts[3];
+    for (int a = 0; a < D; ++a) ts[a] = F->brick.tmax[a] - F->brick.tmin[a];
+    MixedDev<D> M{&r_meta, &r_nbr, &r_nbr2, &r_meta2, &i_meta, &i_cls, &i_nbr, &i_wf, &i_d, &i_q, &i_cidx, &corr32, &cls32,
+                  &i_wf64, &i_d64, &i_q64, &corr64, &perm, &iperm};
+    build_mixed_device<D>(T64, num_corrections, ts, M, stream);
+    near_list.alloc((size_t)N);
+    near_count.alloc(1);
+    set_mixed_views(M.nR, M.nI, M.nU, M.base, M.x_first, M.nX, M.ncls, ts);
+    return;
+  }
   // The FP32 tables derive from the FP64 ones; rebuild those on the host.
   Tables64<D> T;
   build_tables64<D>(*F, T);
@@ -280,23 +336,29 @@ void LevelSet<D>::upload_mixed(const Tables32<D>& M, const double* ts) {
   near_list.alloc((size_t)N);
   near_count.alloc(1);
   cuda_check(cudaStreamSynchronize(stream), "mixed table upload");
-  nR = M.nR;
-  nI = M.nI;
-  ncls = M.ncls;
+  set_mixed_views(M.nR, M.nI, M.nU, M.base_level, M.x_first, (int64_t)M.x_list.size(), M.ncls, ts);
+}
+
+template <int D>
+void LevelSet<D>::set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int base, int64_t x_first, int64_t nX, int64_t ncls_,
+                                  const double* ts) {
+  nR = nR_;
+  nI = nI_;
+  ncls = ncls_;
   T32.N = N;
-  T32.nR = M.nR;
-  T32.nI = M.nI;
-  T32.base = M.base_level;
+  T32.nR = nR_;
+  T32.nI = nI_;
+  T32.base = base;
   for (int a = 0; a < 3; ++a) T32.tsize[a] = a < D ? (float)ts[a] : 1.0f;
   for (int a = 0; a < 3; ++a) T32.inv_tsize[a] = 1.0f / T32.tsize[a];
-  T32.nU = M.nU;
+  T32.nU = nU_;
   T32.r_meta = r_meta.p;
   T32.r_nbr = r_nbr.p;
   T32.r_nbr2 = r_nbr2.p;
   T32.i_cls = i_cls.p;
   T32.cls32 = cls32.p;
-  T32.x_first = M.x_first;
-  T32.nX = (int64_t)M.x_list.size();
+  T32.x_first = x_first;
+  T32.nX = nX;
   T32.r_meta2 = r_meta2.p;
   T32.i_meta = i_meta.p;
   T32.i_nbr = i_nbr.p;
@@ -424,6 +486,11 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
     std::vector<uint16_t> lim_node((size_t)N), lim((size_t)N);
     for (size_t k = 0; k < nparts; ++k)
       for (int64_t n = part_offsets[k]; n < part_offsets[k + 1]; ++n) lim_node[(size_t)n] = (uint16_t)its[k];
+    if (h_perm.empty() && N) {
+      h_perm.resize((size_t)N);
+      cuda_check(cudaMemcpyAsync(h_perm.data(), perm.p, (size_t)N * sizeof(int32_t), cudaMemcpyDeviceToHost, stream), "D2H");
+      cuda_check(cudaStreamSynchronize(stream), "perm download");
+    }
     for (int64_t i = 0; i < N; ++i) lim[(size_t)i] = lim_node[(size_t)h_perm[(size_t)i]];
     iter_lim.upload(lim, stream);
     part_iters = its;

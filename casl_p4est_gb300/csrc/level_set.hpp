@@ -107,8 +107,13 @@ struct LevelSet {
   std::vector<int> graph_key;          // iteration counts the captured graph was built for
   int64_t graph_launches = 0;          // kernels in the captured graph
   std::vector<int32_t> h_perm;         // device index -> node (host copy of the mixed tables' perm)
+  // device flattener inputs: the brick's tree coordinates and the nodes
+  bool device_flat = false;
+  DevBuf<int32_t> fl_tree_ijk, fl_node_tree, fl_node_x;
 
-  explicit LevelSet(const Forest<D>& forest, bool with_mixed = true);
+  // device_build: the tables are built on the GPU by the device flattener (same FP64 tables; the
+  // mixed tables, built on first use, differ only in the numbering of the irregular geometry classes)
+  explicit LevelSet(const Forest<D>& forest, bool with_mixed = true, bool device_build = false);
   // level set over the disjoint union of grids with equal tree sizes: tables concatenated in node
   // order (parts[k] occupies nodes part_offsets[k] .. part_offsets[k+1]-1)
   LevelSet(const std::vector<const Forest<D>*>& parts);
@@ -194,6 +199,8 @@ struct LevelSet {
   void prep_batch(const double* phi);
   void build_mixed();
   void upload_mixed(const Tables32<D>& M, const double* tree_size);
+  void set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int base, int64_t x_first, int64_t nX, int64_t ncls_, const double* ts);
+  void init_stream();
   void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);

@@ -32,38 +32,68 @@ struct Qnnn {
   double inverse_d_max;
 };
 
+// The construction below reads the grid through a view, so that one restatement serves the host
+// builder (HostForestView over Forest) and the device builder (a view over device arrays):
+//   node_tree(n), node_x(n, a) (clamped), node_unclamped(n, x), nt(a) (trees per axis), tree_ijk(t, a),
+//   tree_at(ijk), tmin(t, a), tmax(t, a), find_leaf(tree, x) (-1 if none), leaf_level(q), leaf_tree(q),
+//   leaf_x(q, a), local_node(q, c).
+template <int D>
+struct HostForestView {
+  const Forest<D>& F;
+  int32_t node_tree(int32_t n) const { return F.node_tree[n]; }
+  int32_t node_x(int32_t n, int a) const { return F.node_x[(size_t)D * n + a]; }
+  void node_unclamped(int32_t n, int32_t* x) const { F.node_unclamped(n, x); }
+  int nt(int a) const { return F.brick.n[a]; }
+  int tree_ijk(int32_t t, int a) const { return F.brick.tree_ijk[3 * t + a]; }
+  int32_t tree_at(const int* ijk) const { return F.brick.tree_at(ijk); }
+  double tmin(int32_t t, int a) const { return F.brick.tmin[3 * t + a]; }
+  double tmax(int32_t t, int a) const { return F.brick.tmax[3 * t + a]; }
+  int32_t find_leaf(int32_t tree, const int32_t* x) const { return F.find_leaf(tree, x); }
+  int leaf_level(int32_t q) const { return F.leaves[q].level; }
+  int32_t leaf_tree(int32_t q) const { return F.leaves[q].tree; }
+  int32_t leaf_x(int32_t q, int a) const { return F.leaves[q].x[a]; }
+  int32_t local_node(int32_t q, int c) const { return F.local_nodes[(size_t)Dim<D>::CHILDREN * q + c]; }
+};
+
 // find_neighbor_cell_of_node (src/my_p4est_hierarchy.cpp:569-600): perturb the unclamped node by one
 // logical unit along the diagonal direction c and return the leaf containing that point.
-template <int D>
-inline bool find_neighbor_cell_of_node(const Forest<D>& F, int32_t n, const int* c, int32_t& quad, int32_t& tree) {
+template <int D, class V>
+LSG_HD bool find_neighbor_cell_of_node_v(const V& F, int32_t n, const int* c, int32_t& quad, int32_t& tree) {
   using DD = Dim<D>;
-  int32_t xu[3];
+  int32_t xu[3] = {0, 0, 0};
   F.node_unclamped(n, xu);
-  const int32_t t = F.node_tree[n];
-  int64_t G[3] = {0, 0, 0};
-  for (int a = 0; a < D; ++a) G[a] = (int64_t)F.brick.tree_ijk[3 * t + a] * DD::ROOT_LEN + xu[a] + c[a];
+  const int32_t t = F.node_tree(n);
+  int ijk[3] = {0, 0, 0};
   int32_t xl[3] = {0, 0, 0};
-  if (!F.global_to_tree(G, tree, xl)) {
-    quad = -1;
-    return false;
+  for (int a = 0; a < D; ++a) {
+    const int64_t G = (int64_t)F.tree_ijk(t, a) * DD::ROOT_LEN + xu[a] + c[a];
+    if (G < 0 || G >= (int64_t)F.nt(a) * DD::ROOT_LEN) {
+      quad = -1;
+      tree = -1;
+      return false;
+    }
+    ijk[a] = (int)(G / DD::ROOT_LEN);
+    xl[a] = (int32_t)(G - (int64_t)ijk[a] * DD::ROOT_LEN);
   }
+  tree = F.tree_at(ijk);
   quad = F.find_leaf(tree, xl);
   return quad >= 0;
 }
 
-template <int D>
-inline void tangential_offsets(const Forest<D>& F, const Quad& q, int axis, const double* cxyz, double* out) {
+template <int D, class V>
+LSG_HD void tangential_offsets_v(const V& F, int32_t quad, int axis, const double* cxyz, double* out) {
   using DD = Dim<D>;
   const int t1 = (axis == 0) ? 1 : 0;
   const int t2 = (axis == 2) ? 1 : 2;
   const int tan[2] = {t1, t2};
-  const double qh = quadrant_len(DD::MAXLEVEL, q.level) / (double)DD::ROOT_LEN;
+  const int32_t qt_ = F.leaf_tree(quad);
+  const double qh = quadrant_len(DD::MAXLEVEL, F.leaf_level(quad)) / (double)DD::ROOT_LEN;
   for (int j = 0; j < D - 1; ++j) {
     const int t = tan[j];
-    const double tmin = F.brick.tmin[3 * q.tree + t];
-    const double tmax = F.brick.tmax[3 * q.tree + t];
+    const double tmin = F.tmin(qt_, t);
+    const double tmax = F.tmax(qt_, t);
     const double thr = (tmax - tmin) * ((double)1) / ((double)DD::ROOT_LEN);
-    const double qt = (tmax - tmin) * (q.x[t] / (double)DD::ROOT_LEN) + tmin;
+    const double qt = (tmax - tmin) * (F.leaf_x(quad, t) / (double)DD::ROOT_LEN) + tmin;
     const double m0 = (fabs(cxyz[t] - qt) > thr) ? (cxyz[t] - qt) : 0.0;
     const double p0 = (fabs((tmax - tmin) * qh - m0) > thr) ? ((tmax - tmin) * qh - m0) : 0.0;
     out[2 * j + 0] = m0;
@@ -73,7 +103,7 @@ inline void tangential_offsets(const Forest<D>& F, const Quad& q, int axis, cons
 
 // Corner index of a cell: bit `axis` = abit, tangential bits from k.
 template <int D>
-inline int face_corner(int axis, int abit, int k) {
+LSG_HD int face_corner(int axis, int abit, int k) {
   const int t1 = (axis == 0) ? 1 : 0;
   const int t2 = (axis == 2) ? 1 : 2;
   int c = (abit << axis) | ((k & 1) << t1);
@@ -83,25 +113,25 @@ inline int face_corner(int axis, int abit, int k) {
 
 // Returns true if a stencil could not be completed (cannot happen for a complete single-process
 // forest); fills q otherwise. Mirrors construct_neighbors (src/my_p4est_node_neighbors.cpp:114-1201).
-template <int D>
-inline bool construct_neighbors(const Forest<D>& F, int32_t n, Qnnn<D>& q) {
+template <int D, class V>
+LSG_HD bool construct_neighbors_v(const V& F, int32_t n, Qnnn<D>& q) {
   using DD = Dim<D>;
   constexpr int NC = DD::CHILDREN;
-  const int32_t t = F.node_tree[n];
+  const int32_t t = F.node_tree(n);
   int32_t xu[3] = {0, 0, 0};
   F.node_unclamped(n, xu);
   double cxyz[3] = {0, 0, 0};
   for (int a = 0; a < D; ++a) {
-    const double tmin = F.brick.tmin[3 * t + a], tmax = F.brick.tmax[3 * t + a];
+    const double tmin = F.tmin(t, a), tmax = F.tmax(t, a);
     cxyz[a] = (tmax - tmin) * (xu[a] / (double)DD::ROOT_LEN) + tmin;
   }
   int32_t cq[NC], ct[NC];
   for (int v = 0; v < NC; ++v) {
     int c[3] = {0, 0, 0};
     for (int a = 0; a < D; ++a) c[a] = ((v >> a) & 1) ? 1 : -1;
-    find_neighbor_cell_of_node(F, n, c, cq[v], ct[v]);
+    find_neighbor_cell_of_node_v<D>(F, n, c, cq[v], ct[v]);
   }
-  auto lvl = [&](int32_t quad) -> int { return quad < 0 ? -1 : F.leaves[quad].level; };
+  auto lvl = [&](int32_t quad) -> int { return quad < 0 ? -1 : F.leaf_level(quad); };
 
   q.node_000 = n;
   for (int dir = 0; dir < 2 * D; ++dir) {
@@ -119,11 +149,10 @@ inline bool construct_neighbors(const Forest<D>& F, int32_t n, Qnnn<D>& q) {
     }
     wall[dir] = (best < 0);
     if (wall[dir]) continue;
-    const Quad& Q = F.leaves[best];
-    q.d[dir] = (F.brick.tmax[3 * Q.tree + axis] - F.brick.tmin[3 * Q.tree + axis]) *
-               (quadrant_len(DD::MAXLEVEL, Q.level) / (double)DD::ROOT_LEN);
-    for (int k = 0; k < DD::HALF; ++k) q.nb[dir][k] = F.local_nodes[(size_t)NC * best + face_corner<D>(axis, side, k)];
-    tangential_offsets<D>(F, Q, axis, cxyz, q.dt[dir]);
+    const int32_t bt = F.leaf_tree(best);
+    q.d[dir] = (F.tmax(bt, axis) - F.tmin(bt, axis)) * (quadrant_len(DD::MAXLEVEL, F.leaf_level(best)) / (double)DD::ROOT_LEN);
+    for (int k = 0; k < DD::HALF; ++k) q.nb[dir][k] = F.local_node(best, face_corner<D>(axis, side, k));
+    tangential_offsets_v<D>(F, best, axis, cxyz, q.dt[dir]);
   }
   for (int dir = 0; dir < 2 * D; ++dir) {
     if (!wall[dir]) continue;
@@ -143,14 +172,14 @@ inline bool construct_neighbors(const Forest<D>& F, int32_t n, Qnnn<D>& q) {
       const int bit = (a == axis) ? opp : (cvec[a] != 1 ? 1 : 0);
       corner |= bit << a;
     }
-    const int32_t ntmp = F.local_nodes[(size_t)NC * qmin + corner];
+    const int32_t ntmp = F.local_node(qmin, corner);
     int32_t qtmp, ttmp;
-    if (!find_neighbor_cell_of_node(F, ntmp, cvec, qtmp, ttmp)) return true;
-    const Quad& Q = F.leaves[qtmp];
-    q.d[dir] = -q.d[2 * axis + opp] - (F.brick.tmax[3 * Q.tree + axis] - F.brick.tmin[3 * Q.tree + axis]) *
-                                          (quadrant_len(DD::MAXLEVEL, Q.level) / (double)DD::ROOT_LEN);
-    for (int k = 0; k < DD::HALF; ++k) q.nb[dir][k] = F.local_nodes[(size_t)NC * qtmp + face_corner<D>(axis, opp, k)];
-    tangential_offsets<D>(F, Q, axis, cxyz, q.dt[dir]);
+    if (!find_neighbor_cell_of_node_v<D>(F, ntmp, cvec, qtmp, ttmp)) return true;
+    const int32_t tt = F.leaf_tree(qtmp);
+    q.d[dir] = -q.d[2 * axis + opp] - (F.tmax(tt, axis) - F.tmin(tt, axis)) *
+                                          (quadrant_len(DD::MAXLEVEL, F.leaf_level(qtmp)) / (double)DD::ROOT_LEN);
+    for (int k = 0; k < DD::HALF; ++k) q.nb[dir][k] = F.local_node(qtmp, face_corner<D>(axis, opp, k));
+    tangential_offsets_v<D>(F, qtmp, axis, cxyz, q.dt[dir]);
   }
   // inverse_d_max (src/my_p4est_node_neighbors.cpp:1171-1187)
   double m = max2(q.d[0], q.d[1]);
@@ -174,20 +203,34 @@ inline bool construct_neighbors(const Forest<D>& F, int32_t n, Qnnn<D>& q) {
   return false;
 }
 
+// host entry points over the Forest
+template <int D>
+inline bool find_neighbor_cell_of_node(const Forest<D>& F, int32_t n, const int* c, int32_t& quad, int32_t& tree) {
+  return find_neighbor_cell_of_node_v<D>(HostForestView<D>{F}, n, c, quad, tree);
+}
+template <int D>
+inline bool construct_neighbors(const Forest<D>& F, int32_t n, Qnnn<D>& q) {
+  return construct_neighbors_v<D>(HostForestView<D>{F}, n, q);
+}
+
 // Wall flags of a node, bit dir set when the node lies on that domain face
 // (is_node_xmWall ... is_node_zpWall, src/my_p4est_utils.cpp:1815-1905; non-periodic brick).
-template <int D>
-inline unsigned wall_mask(const Forest<D>& F, int32_t n) {
+template <int D, class V>
+LSG_HD unsigned wall_mask_v(const V& F, int32_t n) {
   using DD = Dim<D>;
   unsigned m = 0;
-  const int32_t t = F.node_tree[n];
+  const int32_t t = F.node_tree(n);
   for (int a = 0; a < D; ++a) {
-    const int32_t v = F.node_x[(size_t)D * n + a];
-    const int ijk = F.brick.tree_ijk[3 * t + a];
+    const int32_t v = F.node_x(n, a);
+    const int ijk = F.tree_ijk(t, a);
     if (v == 0 && ijk == 0) m |= 1u << (2 * a);
-    if ((v == DD::ROOT_LEN - 1 || v == DD::ROOT_LEN) && ijk == F.brick.n[a] - 1) m |= 1u << (2 * a + 1);
+    if ((v == DD::ROOT_LEN - 1 || v == DD::ROOT_LEN) && ijk == F.nt(a) - 1) m |= 1u << (2 * a + 1);
   }
   return m;
+}
+template <int D>
+inline unsigned wall_mask(const Forest<D>& F, int32_t n) {
+  return wall_mask_v<D>(HostForestView<D>{F}, n);
 }
 
 }  // namespace lsg

@@ -5,14 +5,6 @@
 
 namespace lsg {
 
-// Order in which interpolate_linearly sums the face nodes (.h:290-306): pp, pm, mp, mm (3D); pm, mm (2D).
-template <int D>
-static inline int eval_slot(int e) {
-  if (D == 2) return e == 0 ? 1 : 0;
-  static const int order3[4] = {3, 1, 2, 0};
-  return order3[e];
-}
-
 template <int D>
 void build_tables64(const Forest<D>& F, Tables64<D>& T) {
   constexpr int H = Dim<D>::HALF;
@@ -37,44 +29,8 @@ void build_tables64(const Forest<D>& F, Tables64<D>& T) {
       ++failed;
       continue;
     }
-    for (int dir = 0; dir < 2 * D; ++dir) {
-      const double dm0 = q.dt[dir][0], dp0 = q.dt[dir][1];
-      const double d0m = (D == 3) ? q.dt[dir][2] : 0.0, d0p = (D == 3) ? q.dt[dir][3] : 0.0;
-      double wk[4];
-      double nrm;
-      if (D == 2) {
-        wk[0] = dp0;  // mm
-        wk[1] = dm0;  // pm
-        nrm = dm0 + dp0;
-      } else {
-        wk[0] = dp0 * d0p;  // mm
-        wk[1] = dm0 * d0p;  // pm
-        wk[2] = dp0 * d0m;  // mp
-        wk[3] = dm0 * d0m;  // pp
-        nrm = (dm0 + dp0) * (d0m + d0p);
-      }
-      int o = 0;
-      for (int e = 0; e < H; ++e) {
-        const int k = eval_slot<D>(e);
-        if (wk[k] == 0.0) continue;
-        T.nbr[(size_t)(dir * H + o) * N + n] = q.nb[dir][k];
-        T.w[(size_t)(dir * H + o) * N + n] = wk[k];
-        ++o;
-      }
-      T.nrm[(size_t)dir * N + n] = nrm;
-      T.d[(size_t)dir * N + n] = q.d[dir];
-      for (int j = 0; j < D - 1; ++j) T.q[(size_t)(dir * (D - 1) + j) * N + n] = 0.5 * q.dt[dir][2 * j] * q.dt[dir][2 * j + 1];
-    }
-    double m[6];
-    cross_terms<D>(q, m);
-    bool any = false;
-    for (int i = 0; i < 6; ++i) any = any || !(fabs(m[i]) < EPS);
-    needs[n] = any ? 1 : 0;
+    needs[n] = fill_row64<D>(q, N, n, T.nbr.data(), T.w.data(), T.nrm.data(), T.d.data(), T.q.data(), T.smin.data()) ? 1 : 0;
     T.wall[n] = (uint8_t)wall_mask<D>(F, n);
-    double s = min2(fabs(q.d[1]), fabs(q.d[0]));
-    s = (D == 3) ? min3(s, min2(fabs(q.d[3]), fabs(q.d[2])), min2(fabs(q.d[5]), fabs(q.d[4])))
-                 : min2(s, min2(fabs(q.d[3]), fabs(q.d[2])));
-    T.smin[n] = s;
   }
   if (failed) throw std::runtime_error("node neighbours: incomplete stencil in a single-process forest");
   int32_t R = 0;

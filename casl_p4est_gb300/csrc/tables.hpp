@@ -119,7 +119,7 @@ LSG_HD constexpr int cls_words() { return 1 + 2 * D + 2 * D * Dim<D>::HALF + 2 *
 
 // Cross-term coefficients of one record, exactly as correct_naive_second_derivatives computes them.
 template <int D>
-inline void cross_terms(const Qnnn<D>& q, double* m) {
+LSG_HD void cross_terms(const Qnnn<D>& q, double* m) {
   for (int i = 0; i < 6; ++i) m[i] = 0.0;
   // m_ab: correction of the naive second derivative along axis a by the one along axis b, built from
   // the offsets of the two neighbours along a, in the tangential axis b.
@@ -136,6 +136,142 @@ inline void cross_terms(const Qnnn<D>& q, double* m) {
     m[CM31] = mab(2, 0);
     m[CM32] = mab(2, 1);
   }
+}
+
+// correct_naive_second_derivatives (src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298) applied to the
+// naive second derivatives Dv from the six cross-term coefficients m, every branch (host and device).
+template <int D>
+LSG_HD void apply_correction(const double* m, double* Dv) {
+  auto z = [](double v) { return fabs(v) < EPS; };
+  if (D == 2) {
+    const double m12 = m[CM12], m21 = m[CM21];
+    if (z(m12)) {
+      if (!z(m21)) Dv[1] = Dv[1] - m21 * Dv[0];
+    } else if (z(m21)) {
+      Dv[0] = Dv[0] - m12 * Dv[1];
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const double nx = Dv[0], ny = Dv[1];
+      Dv[0] = nx * idet - ny * (m12 * idet);
+      Dv[1] = ny * idet - nx * (m21 * idet);
+    }
+    return;
+  }
+  const double m12 = m[CM12], m13 = m[CM13], m21 = m[CM21], m23 = m[CM23], m31 = m[CM31], m32 = m[CM32];
+  double &Dxx = Dv[0], &Dyy = Dv[1], &Dzz = Dv[2];
+  if (z(m12) && z(m13)) {
+    if (z(m23)) {
+      if (!z(m21)) Dyy -= m21 * Dxx;
+      if (!z(m31)) Dzz -= m31 * Dxx;
+      if (!z(m32)) Dzz -= m32 * Dyy;
+    } else if (z(m32)) {
+      if (!z(m31)) Dzz -= m31 * Dxx;
+      Dyy -= m23 * Dzz;
+      if (!z(m21)) Dyy -= m21 * Dxx;
+    } else {
+      const double idet = 1.0 / (1.0 - m23 * m32);
+      const bool m21z = z(m21), m31z = z(m31);
+      const double nDyy = Dyy, nDzz = Dzz;
+      Dyy = ((m21z ? nDyy : (nDyy - m21 * Dxx)) - m23 * (m31z ? nDzz : (nDzz - m31 * Dxx))) * idet;
+      Dzz = ((m31z ? nDzz : (nDzz - m31 * Dxx)) - m32 * (m21z ? nDyy : (nDyy - m21 * Dxx))) * idet;
+    }
+  } else if (z(m21) && z(m23)) {
+    if (z(m13)) {
+      if (!z(m12)) Dxx -= m12 * Dyy;
+      if (!z(m31)) Dzz -= m31 * Dxx;
+      if (!z(m32)) Dzz -= m32 * Dyy;
+    } else if (z(m31)) {
+      if (!z(m32)) Dzz -= m32 * Dyy;
+      Dxx -= m13 * Dzz;
+      if (!z(m12)) Dxx -= m12 * Dyy;
+    } else {
+      const double idet = 1.0 / (1.0 - m13 * m31);
+      const bool m12z = z(m12), m32z = z(m32);
+      const double nDxx = Dxx, nDzz = Dzz;
+      Dxx = ((m12z ? nDxx : (nDxx - m12 * Dyy)) - m13 * (m32z ? nDzz : (nDzz - m32 * Dyy))) * idet;
+      Dzz = ((m32z ? nDzz : (nDzz - m32 * Dyy)) - m31 * (m12z ? nDxx : (nDxx - m12 * Dyy))) * idet;
+    }
+  } else if (z(m31) && z(m32)) {
+    if (z(m12)) {
+      if (!z(m13)) Dxx -= m13 * Dzz;
+      if (!z(m21)) Dyy -= m21 * Dxx;
+      if (!z(m23)) Dyy -= m23 * Dzz;
+    } else if (z(m21)) {
+      if (!z(m23)) Dyy -= m23 * Dzz;
+      Dxx -= m12 * Dyy;
+      if (!z(m13)) Dxx -= m13 * Dzz;
+    } else {
+      const double idet = 1.0 / (1.0 - m12 * m21);
+      const bool m13z = z(m13), m23z = z(m23);
+      const double nDxx = Dxx, nDyy = Dyy;
+      Dxx = ((m13z ? nDxx : (nDxx - m13 * Dzz)) - m12 * (m23z ? nDyy : (nDyy - m23 * Dzz))) * idet;
+      Dyy = ((m23z ? nDyy : (nDyy - m23 * Dzz)) - m21 * (m13z ? nDxx : (nDxx - m13 * Dzz))) * idet;
+    }
+  } else {
+    const double idet = 1.0 / (1.0 + m12 * m23 * m31 + m13 * m21 * m32 - m12 * m21 - m13 * m31 - m23 * m32);
+    const double nDxx = Dxx, nDyy = Dyy, nDzz = Dzz;
+    Dxx = (nDxx * (idet * (1.0 - m23 * m32)) + nDyy * (idet * (m32 * m13 - m12)) + nDzz * (idet * (m12 * m23 - m13)));
+    Dyy = (nDxx * (idet * (m31 * m23 - m21)) + nDyy * (idet * (1.0 - m31 * m13)) + nDzz * (idet * (m21 * m13 - m23)));
+    Dzz = (nDxx * (idet * (m21 * m32 - m31)) + nDyy * (idet * (m31 * m12 - m32)) + nDzz * (idet * (1.0 - m21 * m12)));
+  }
+}
+
+// Order in which interpolate_linearly sums the face nodes (.h:290-306): pp, pm, mp, mm (3D); pm, mm (2D).
+template <int D>
+LSG_HD int eval_slot(int e) {
+  if (D == 2) return e == 0 ? 1 : 0;
+  return e == 0 ? 3 : (e == 1 ? 1 : (e == 2 ? 2 : 0));
+}
+
+// One node's row of the FP64 tables from its record (the same code on the host and the device):
+// face nodes with a nonzero weight in summation order, unused slots -1 / 0; normalisations,
+// distances, third-order factors, the smallest |d| (smin). Returns whether the node needs a
+// cross-term correction record.
+template <int D>
+LSG_HD bool fill_row64(const Qnnn<D>& q, int64_t N, int64_t n, int32_t* nbr, double* w, double* nrm, double* d, double* qf,
+                       double* smin) {
+  constexpr int H = Dim<D>::HALF;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    const double dm0 = q.dt[dir][0], dp0 = q.dt[dir][1];
+    const double d0m = (D == 3) ? q.dt[dir][2] : 0.0, d0p = (D == 3) ? q.dt[dir][3] : 0.0;
+    double wk[4] = {0, 0, 0, 0};
+    double nr;
+    if (D == 2) {
+      wk[0] = dp0;  // mm
+      wk[1] = dm0;  // pm
+      nr = dm0 + dp0;
+    } else {
+      wk[0] = dp0 * d0p;  // mm
+      wk[1] = dm0 * d0p;  // pm
+      wk[2] = dp0 * d0m;  // mp
+      wk[3] = dm0 * d0m;  // pp
+      nr = (dm0 + dp0) * (d0m + d0p);
+    }
+    int o = 0;
+    for (int e = 0; e < H; ++e) {
+      const int k = eval_slot<D>(e);
+      if (wk[k] == 0.0) continue;
+      nbr[(int64_t)(dir * H + o) * N + n] = q.nb[dir][k];
+      w[(int64_t)(dir * H + o) * N + n] = wk[k];
+      ++o;
+    }
+    for (; o < H; ++o) {
+      nbr[(int64_t)(dir * H + o) * N + n] = -1;
+      w[(int64_t)(dir * H + o) * N + n] = 0.0;
+    }
+    nrm[(int64_t)dir * N + n] = nr;
+    d[(int64_t)dir * N + n] = q.d[dir];
+    for (int j = 0; j < D - 1; ++j) qf[(int64_t)(dir * (D - 1) + j) * N + n] = 0.5 * q.dt[dir][2 * j] * q.dt[dir][2 * j + 1];
+  }
+  double s = min2(fabs(q.d[1]), fabs(q.d[0]));
+  s = (D == 3) ? min3(s, min2(fabs(q.d[3]), fabs(q.d[2])), min2(fabs(q.d[5 % (2 * D)]), fabs(q.d[4 % (2 * D)])))
+               : min2(s, min2(fabs(q.d[3]), fabs(q.d[2])));
+  smin[n] = s;
+  double m[6];
+  cross_terms<D>(q, m);
+  bool any = false;
+  for (int i = 0; i < 6; ++i) any = any || !(fabs(m[i]) < EPS);
+  return any;
 }
 
 }  // namespace lsg

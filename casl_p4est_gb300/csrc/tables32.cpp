@@ -22,81 +22,6 @@
 
 namespace lsg {
 
-template <int D>
-static void apply_correction_host(const double* m, double* Dv) {
-  auto z = [](double v) { return fabs(v) < EPS; };
-  if (D == 2) {
-    const double m12 = m[CM12], m21 = m[CM21];
-    if (z(m12)) {
-      if (!z(m21)) Dv[1] = Dv[1] - m21 * Dv[0];
-    } else if (z(m21)) {
-      Dv[0] = Dv[0] - m12 * Dv[1];
-    } else {
-      const double idet = 1.0 / (1.0 - m12 * m21);
-      const double nx = Dv[0], ny = Dv[1];
-      Dv[0] = nx * idet - ny * (m12 * idet);
-      Dv[1] = ny * idet - nx * (m21 * idet);
-    }
-    return;
-  }
-  const double m12 = m[CM12], m13 = m[CM13], m21 = m[CM21], m23 = m[CM23], m31 = m[CM31], m32 = m[CM32];
-  double &Dxx = Dv[0], &Dyy = Dv[1], &Dzz = Dv[2];
-  if (z(m12) && z(m13)) {
-    if (z(m23)) {
-      if (!z(m21)) Dyy -= m21 * Dxx;
-      if (!z(m31)) Dzz -= m31 * Dxx;
-      if (!z(m32)) Dzz -= m32 * Dyy;
-    } else if (z(m32)) {
-      if (!z(m31)) Dzz -= m31 * Dxx;
-      Dyy -= m23 * Dzz;
-      if (!z(m21)) Dyy -= m21 * Dxx;
-    } else {
-      const double idet = 1.0 / (1.0 - m23 * m32);
-      const bool m21z = z(m21), m31z = z(m31);
-      const double nDyy = Dyy, nDzz = Dzz;
-      Dyy = ((m21z ? nDyy : (nDyy - m21 * Dxx)) - m23 * (m31z ? nDzz : (nDzz - m31 * Dxx))) * idet;
-      Dzz = ((m31z ? nDzz : (nDzz - m31 * Dxx)) - m32 * (m21z ? nDyy : (nDyy - m21 * Dxx))) * idet;
-    }
-  } else if (z(m21) && z(m23)) {
-    if (z(m13)) {
-      if (!z(m12)) Dxx -= m12 * Dyy;
-      if (!z(m31)) Dzz -= m31 * Dxx;
-      if (!z(m32)) Dzz -= m32 * Dyy;
-    } else if (z(m31)) {
-      if (!z(m32)) Dzz -= m32 * Dyy;
-      Dxx -= m13 * Dzz;
-      if (!z(m12)) Dxx -= m12 * Dyy;
-    } else {
-      const double idet = 1.0 / (1.0 - m13 * m31);
-      const bool m12z = z(m12), m32z = z(m32);
-      const double nDxx = Dxx, nDzz = Dzz;
-      Dxx = ((m12z ? nDxx : (nDxx - m12 * Dyy)) - m13 * (m32z ? nDzz : (nDzz - m32 * Dyy))) * idet;
-      Dzz = ((m32z ? nDzz : (nDzz - m32 * Dyy)) - m31 * (m12z ? nDxx : (nDxx - m12 * Dyy))) * idet;
-    }
-  } else if (z(m31) && z(m32)) {
-    if (z(m12)) {
-      if (!z(m13)) Dxx -= m13 * Dzz;
-      if (!z(m21)) Dyy -= m21 * Dxx;
-      if (!z(m23)) Dyy -= m23 * Dzz;
-    } else if (z(m21)) {
-      if (!z(m23)) Dyy -= m23 * Dzz;
-      Dxx -= m12 * Dyy;
-      if (!z(m13)) Dxx -= m13 * Dzz;
-    } else {
-      const double idet = 1.0 / (1.0 - m12 * m21);
-      const bool m13z = z(m13), m23z = z(m23);
-      const double nDxx = Dxx, nDyy = Dyy;
-      Dxx = ((m13z ? nDxx : (nDxx - m13 * Dzz)) - m12 * (m23z ? nDyy : (nDyy - m23 * Dzz))) * idet;
-      Dyy = ((m23z ? nDyy : (nDyy - m23 * Dzz)) - m21 * (m13z ? nDxx : (nDxx - m13 * Dzz))) * idet;
-    }
-  } else {
-    const double idet = 1.0 / (1.0 + m12 * m23 * m31 + m13 * m21 * m32 - m12 * m21 - m13 * m31 - m23 * m32);
-    const double nDxx = Dxx, nDyy = Dyy, nDzz = Dzz;
-    Dxx = (nDxx * (idet * (1.0 - m23 * m32)) + nDyy * (idet * (m32 * m13 - m12)) + nDzz * (idet * (m12 * m23 - m13)));
-    Dyy = (nDxx * (idet * (m31 * m23 - m21)) + nDyy * (idet * (1.0 - m31 * m13)) + nDzz * (idet * (m21 * m13 - m23)));
-    Dzz = (nDxx * (idet * (m21 * m32 - m31)) + nDyy * (idet * (m31 * m12 - m32)) + nDzz * (idet * (1.0 - m21 * m12)));
-  }
-}
 
 template <int D>
 void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& M) {
@@ -178,7 +103,7 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     for (int c = 0; c < D; ++c) {
       double e[3] = {0, 0, 0};
       e[c] = 1.0;
-      if (T.cidx[n] >= 0) apply_correction_host<D>(&T.crec[6 * (size_t)T.cidx[n]], e);
+      if (T.cidx[n] >= 0) apply_correction<D>(&T.crec[6 * (size_t)T.cidx[n]], e);
       for (int rr = 0; rr < D; ++rr) cm[rr * D + c] = e[rr];
     }
   }
@@ -404,7 +329,7 @@ void build_tables32(const Tables64<D>& T, const double* tree_size, Tables32<D>& 
     for (int c = 0; c < D; ++c) {
       double e[3] = {0, 0, 0};
       e[c] = 1.0;
-      apply_correction_host<D>(&T.crec[6 * r], e);
+      apply_correction<D>(&T.crec[6 * r], e);
       for (int rr = 0; rr < D; ++rr) {
         M.corr[(size_t)D * D * r + D * rr + c] = (float)e[rr];
         M.corr64[(size_t)D * D * r + D * rr + c] = e[rr];

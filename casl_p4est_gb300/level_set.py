@@ -32,17 +32,20 @@ def _host_f64(v, n, name):
 
 
 class my_p4est_level_set_t:
-    def __init__(self, ngbd: my_p4est_node_neighbors_t, precision: str = "fp64"):
+    def __init__(self, ngbd: my_p4est_node_neighbors_t, precision: str = "fp64", device_build: bool = False):
+        """device_build: build the node-neighbour tables on the GPU (same results, no host table work)."""
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {list(PRECISIONS)}")
         self.ngbd = ngbd
         self.precision = precision
+        self.device_build = bool(device_build)
         self._h = None
         self._build(ngbd)
 
     def _build(self, ngbd):
         h = C.c_void_p()
-        L.check(L.load().lsg_level_set_create(ngbd.forest.handle, C.byref(h)))
+        L.check(L.load().lsg_level_set_create_ex(ngbd.forest.handle, L.LSG_BUILD_ON_DEVICE if self.device_build else 0,
+                                                 C.byref(h)))
         self._h = h
         self.num_nodes = int(L.load().lsg_level_set_num_nodes(h))
         self.zero_distance_threshold = float(L.load().lsg_level_set_zero_distance_threshold(h))

@@ -108,6 +108,12 @@ int lsg_forest_dxyz_min(const lsg_forest* f, double* dxyz);
 /* my_p4est_level_set_t(my_p4est_node_neighbors_t*) (src/my_p4est_level_set.h:385-392): builds the
  * device tables of the grid. The forest must outlive the object and keep its nodes. */
 int lsg_level_set_create(const lsg_forest* f, lsg_level_set** out);
+/* The same with flags. LSG_BUILD_ON_DEVICE: the node-neighbour tables are built on the GPU (the
+ * neighbour construction of src/my_p4est_node_neighbors.cpp:114-1201 runs one thread per node) instead
+ * of on the host; results are bit-identical either way. No reference counterpart (the reference
+ * builds its neighbours on the host). */
+#define LSG_BUILD_ON_DEVICE 1
+int lsg_level_set_create_ex(const lsg_forest* f, int flags, lsg_level_set** out);
 int lsg_level_set_destroy(lsg_level_set* ls);
 /* run on the caller's cudaStream_t (NULL keeps the object's own stream) */
 int lsg_level_set_set_stream(lsg_level_set* ls, void* cuda_stream);
