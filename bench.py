@@ -227,8 +227,9 @@ def run_transport(args):
     (0.35,0.35,0.35); single-vortex velocity u = 2 sin^2(pi x) sin(2 pi y) sin(2 pi z) cos(pi t/T), ...,
     T = 3; dt = dx_min; per step update_p4est (semi-Lagrangian RK2 backtrace with quadratic node
     interpolation + host regrid until the grid settles, velocity at the step's midpoint), a new level
-    set on the new grid (node-neighbour tables built on the GPU), and 5 reinitialisation iterations; mixed
-    and FP64 runs side by side."""
+    set on the new grid, and 5 reinitialisation iterations; mixed and FP64 runs side by side. The fields
+    stay on the GPU: node numbering, node coordinates, refinement tags and the node-neighbour tables are
+    computed there, and only the tags (one byte per leaf) go to the host for its regrid passes."""
     import math
 
     import torch
@@ -244,8 +245,9 @@ def run_transport(args):
     results = {}
     for prec in ("mixed", "fp64"):
         f = f0.copy()
-        phi = f.sample(sphere)
-        vol0 = negative_volume(f, phi)
+        phi_h = f.sample(sphere)
+        vol0 = negative_volume(f, phi_h)
+        phi = torch.from_numpy(phi_h).cuda()
         t = 0.0
         times = {"update_p4est": 0.0, "level_set_setup": 0.0, "reinit": 0.0}
         nodes = []
@@ -256,13 +258,15 @@ def run_transport(args):
         for step in range(args.steps):
             t0 = time.perf_counter()
             sl = G.my_p4est_semi_lagrangian_t(f.copy(), ls, splitting=(lmin, lmax, 1.2))
-            phi = sl.update_p4est(G.VortexVelocity(math.cos(math.pi * (t + 0.5 * dt) / T)), dt, phi)
+            phi = sl.update_p4est(G.VortexVelocity(math.cos(math.pi * (t + 0.5 * dt) / T)), dt, phi)  # device fields
             regrid_iters += sl.iterations
             f = sl.forest_np1
             t1 = time.perf_counter()
             ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), device_build=True)
+            ls.set_stream(torch.cuda.current_stream().cuda_stream)
             t2 = time.perf_counter()
             ls.reinitialize_2nd_order(phi, 5, precision=prec)
+            torch.cuda.synchronize()
             t3 = time.perf_counter()
             times["update_p4est"] += t1 - t0
             times["level_set_setup"] += t2 - t1
@@ -270,6 +274,7 @@ def run_transport(args):
             nodes.append(f.num_nodes)
             t += dt
         wall = time.perf_counter() - t_all
+        phi = phi.cpu().numpy()
         results[prec] = {"forest": f, "phi": phi, "ls": ls, "vol0": vol0, "vol": negative_volume(f, phi), "wall_s": wall,
                          "times_s": times, "nodes_mean": float(np.mean(nodes)), "nodes_last": nodes[-1],
                          "regrid_iterations": regrid_iters, "t_final": t}

@@ -42,6 +42,9 @@ SIGNATURES = {
     "lsg_forest_tag_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _U8P]),
     "lsg_forest_refine_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _I]),
     "lsg_forest_build_nodes": (_I, [_P]),
+    "lsg_forest_build_nodes_device": (_I, [_P, _P]),
+    "lsg_forest_node_xyz_device": (_I, [_P, _P, _P]),
+    "lsg_forest_refine_and_coarsen_device": (_I, [_P, _I, _I, _D, _D, _P, C.POINTER(C.c_int), _P]),
     "lsg_forest_num_nodes": (_I64, [_P]),
     "lsg_forest_node_xyz": (_I, [_P, _DP]),
     "lsg_forest_nodes": (_I, [_P, _I32P, _I32P]),

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/lsgpu.h"
+#include "flatten.hpp"
 #include "level_set.hpp"
 #include "shapes.h"
 
@@ -317,6 +318,36 @@ int lsg_forest_refine_levelset(lsg_forest* f, int min_lvl, int max_lvl, double l
 
 int lsg_forest_build_nodes(lsg_forest* f) {
   return guard([&] { with_forest(f, [&](auto& F) { const_cast<std::decay_t<decltype(F)>&>(F).build_nodes(); }); });
+}
+
+int lsg_forest_build_nodes_device(lsg_forest* f, void* stream) {
+  return guard([&] {
+    with_forest(f, [&](auto& F) { build_nodes_device(const_cast<std::decay_t<decltype(F)>&>(F), (cudaStream_t)stream); });
+  });
+}
+
+int lsg_forest_node_xyz_device(lsg_forest* f, double* xyz_dev, void* stream) {
+  return guard([&] {
+    need(xyz_dev != nullptr, "null output");
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      node_xyz_device(const_cast<std::decay_t<decltype(F)>&>(F), xyz_dev, (cudaStream_t)stream);
+    });
+  });
+}
+
+int lsg_forest_refine_and_coarsen_device(lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, const double* phi_dev,
+                                         int* changed, void* stream) {
+  return guard([&] {
+    need(phi_dev != nullptr && changed != nullptr, "refine_and_coarsen: null arguments");
+    need(min_lvl >= 0 && min_lvl <= max_lvl, "refine_and_coarsen: need 0 <= min_lvl <= max_lvl");
+    with_forest(f, [&](auto& F) {
+      using FT = std::decay_t<decltype(F)>;
+      need(max_lvl <= FT::DD::QMAXLEVEL, "refine_and_coarsen: max_lvl above the maximum quadrant level");
+      need_nodes(F);
+      *changed = refine_and_coarsen_device(const_cast<FT&>(F), min_lvl, max_lvl, lip, band, phi_dev, (cudaStream_t)stream) ? 1 : 0;
+    });
+  });
 }
 
 int64_t lsg_forest_num_nodes(const lsg_forest* f) {

@@ -419,6 +419,140 @@ __global__ void __launch_bounds__(TPB) k_corr(const double* __restrict__ crec, i
   }
 }
 
+// ---- node numbering ----------------------------------------------------------------------------
+// canonical key of every leaf corner: the corner in global logical coordinates, owned by the lowest
+// tree touching it and clamped inside that tree (p4est_node_canonicalize / p4est_node_clamp_inside)
+template <int D>
+__global__ void __launch_bounds__(TPB) k_corner_keys(const uint64_t* __restrict__ leaf_key, const int8_t* __restrict__ level, int64_t nl,
+                                                     int n0, int n1, int n2, const int32_t* __restrict__ tree_ijk,
+                                                     const int32_t* __restrict__ ijk_to_tree, uint64_t* __restrict__ corner_key) {
+  using DD = Dim<D>;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nl * DD::CHILDREN) return;
+  const int64_t ii = e / DD::CHILDREN;
+  const int c = (int)(e % DD::CHILDREN);
+  const uint64_t lk = leaf_key[ii];
+  const int32_t tree = (int32_t)(lk >> tree_shift<D>());
+  int32_t x[3] = {0, 0, 0};
+  unmorton<D>(lk & ((uint64_t(1) << tree_shift<D>()) - 1), x);
+  const int32_t h = quadrant_len(DD::MAXLEVEL, level[ii]);
+  const int nn[3] = {n0, n1, n2};
+  int64_t G[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) G[a] = (int64_t)tree_ijk[3 * tree + a] * DD::ROOT_LEN + x[a] + (((c >> a) & 1) ? h : 0);
+  int cand[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  int ncand[3] = {1, 1, 1};
+  for (int a = 0; a < D; ++a) {
+    const int64_t L = (int64_t)nn[a] * DD::ROOT_LEN;
+    const int64_t t = G[a] / DD::ROOT_LEN;
+    if (G[a] == L) {
+      cand[a][0] = (int)(t - 1);
+    } else if (G[a] % DD::ROOT_LEN == 0 && G[a] > 0) {
+      cand[a][0] = (int)(t - 1);
+      cand[a][1] = (int)t;
+      ncand[a] = 2;
+    } else {
+      cand[a][0] = (int)t;
+    }
+  }
+  int32_t owner = -1;
+  int owner_ijk[3] = {0, 0, 0};
+  for (int k = 0; k < ncand[2]; ++k)
+    for (int j = 0; j < ncand[1]; ++j)
+      for (int i = 0; i < ncand[0]; ++i) {
+        const int ijk[3] = {cand[0][i], cand[1][j], cand[2][k]};
+        const int32_t t = ijk_to_tree[(int64_t)n0 * n1 * ijk[2] + (int64_t)n0 * ijk[1] + ijk[0]];
+        if (owner < 0 || t < owner) {
+          owner = t;
+          owner_ijk[0] = ijk[0];
+          owner_ijk[1] = ijk[1];
+          owner_ijk[2] = ijk[2];
+        }
+      }
+  int32_t xl[3] = {0, 0, 0};
+  for (int a = 0; a < D; ++a) {
+    int64_t v = G[a] - (int64_t)owner_ijk[a] * DD::ROOT_LEN;
+    if (v == DD::ROOT_LEN) v = DD::ROOT_LEN - 1;
+    xl[a] = (int32_t)v;
+  }
+  corner_key[e] = (((uint64_t)owner) << tree_shift<D>()) | morton<D>(xl);
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_decode_nodes(const uint64_t* __restrict__ node_key, int64_t nn, int32_t* __restrict__ node_tree,
+                                                      int32_t* __restrict__ node_x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const uint64_t key = node_key[i];
+  node_tree[i] = (int32_t)(key >> tree_shift<D>());
+  int32_t x[3] = {0, 0, 0};
+  unmorton<D>(key & ((uint64_t(1) << tree_shift<D>()) - 1), x);
+  for (int a = 0; a < D; ++a) node_x[i * D + a] = x[a];
+}
+
+// node index of every leaf corner: position of its key among the sorted unique node keys
+__global__ void __launch_bounds__(TPB) k_local_nodes(const uint64_t* __restrict__ corner_key, int64_t nc, const uint64_t* __restrict__ node_key,
+                                                     int64_t nn, int32_t* __restrict__ local_nodes) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nc) return;
+  const uint64_t k = corner_key[e];
+  int64_t lo = 0, hi = nn;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (node_key[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  local_nodes[e] = (int32_t)lo;
+}
+
+// splitting_criteria_tag_t::tag_quadrant from the node values (same rule as Forest::tag_refine_coarsen)
+template <int D>
+__global__ void __launch_bounds__(TPB) k_tag_leaves(const uint64_t* __restrict__ leaf_key, const int8_t* __restrict__ level, int64_t nl,
+                                                    const int32_t* __restrict__ local_nodes, const double* __restrict__ tmin_,
+                                                    const double* __restrict__ tmax_, const double* __restrict__ phi, int min_lvl, int max_lvl,
+                                                    double lip, double band, int8_t* __restrict__ tag) {
+  using DD = Dim<D>;
+  const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= nl) return;
+  const int lv = level[ii];
+  if (lv < min_lvl) {
+    tag[ii] = 1;
+    return;
+  }
+  if (lv > max_lvl) {
+    tag[ii] = -1;
+    return;
+  }
+  const int32_t tree = (int32_t)(leaf_key[ii] >> tree_shift<D>());
+  double f[DD::CHILDREN];
+  for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[local_nodes[ii * DD::CHILDREN + c]];
+  const double* tmn = tmin_ + 3 * tree;
+  const double* tmx = tmax_ + 3 * tree;
+  const double dmin = (double)quadrant_len(DD::MAXLEVEL, lv) / (double)DD::ROOT_LEN;
+  const double lmax_len = (double)quadrant_len(DD::MAXLEVEL, max_lvl) / (double)DD::ROOT_LEN;
+  const double dx = (tmx[0] - tmn[0]) * dmin;
+  const double dy = (tmx[1] - tmn[1]) * dmin;
+  double smallest_dxyz_max = max2((tmx[0] - tmn[0]), (tmx[1] - tmn[1])) * lmax_len;
+  double d;
+  if (D == 3) {
+    const double dz = (tmx[2] - tmn[2]) * dmin;
+    smallest_dxyz_max = max2(smallest_dxyz_max, (tmx[2] - tmn[2]) * lmax_len);
+    d = sqrt(dx * dx + dy * dy + dz * dz);
+  } else {
+    d = sqrt(dx * dx + dy * dy);
+  }
+  const double band_real = band * smallest_dxyz_max;
+  bool refine = false, coarsen = true;
+  for (int i = 0; i < DD::CHILDREN; ++i) {
+    refine = refine || (lv < max_lvl && (fabs(f[i]) - band_real <= 0.5 * lip * d ||
+                                         (i == 0 ? false : ((f[i] > 0.0 && f[0] <= 0.0) || (f[i] <= 0.0 && f[0] > 0.0)))));
+    coarsen = coarsen && lv > min_lvl && fabs(f[i]) - band_real >= 1.0 * lip * d &&
+              (i == 0 ? true : ((f[i] > 0.0 && f[0] > 0.0) || (f[i] <= 0.0 && f[0] <= 0.0)));
+  }
+  tag[ii] = refine ? 1 : (coarsen ? -1 : 0);
+}
+
 }  // namespace
 
 // exclusive prefix sum of n int32 values (CUB), temp storage from a grow-only buffer
@@ -600,7 +734,125 @@ void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDe
   cuda_check(cudaStreamSynchronize(s), "device flattener (mixed)");
 }
 
+template <int D>
+__global__ void __launch_bounds__(TPB) k_node_xyz(const int32_t* __restrict__ node_tree, const int32_t* __restrict__ node_x, int64_t nn,
+                                                  const double* __restrict__ tmin, const double* __restrict__ tmax, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const int32_t t = node_tree[i];
+  for (int a = 0; a < D; ++a) {
+    const int32_t v = node_x[i * D + a];
+    const double r = (v == Dim<D>::ROOT_LEN - 1) ? 1.0 : (double)v / (double)Dim<D>::ROOT_LEN;
+    out[i * D + a] = (tmax[3 * t + a] - tmin[3 * t + a]) * r + tmin[3 * t + a];
+  }
+}
+
+template <int D>
+static void upload_leaves_and_brick(const Forest<D>& F, ForestDevice<D>& X, cudaStream_t s) {
+  X.nl = (int64_t)F.leaves.size();
+  X.leaf_key.upload(F.leaf_key, s);
+  std::vector<int8_t> lvl((size_t)X.nl);
+  for (int64_t q = 0; q < X.nl; ++q) lvl[(size_t)q] = (int8_t)F.leaves[(size_t)q].level;
+  X.level.upload(lvl, s);
+  X.tree_ijk.upload(F.brick.tree_ijk, s);
+  X.ijk_to_tree.upload(F.brick.ijk_to_tree, s);
+  X.tmin.upload(F.brick.tmin, s);
+  X.tmax.upload(F.brick.tmax, s);
+  cuda_check(cudaStreamSynchronize(s), "forest upload");  // the host level copy goes out of scope
+}
+
+template <int D>
+ForestDevice<D>& forest_device(Forest<D>& F, cudaStream_t s) {
+  if (F.device) return *static_cast<ForestDevice<D>*>(F.device.get());
+  if (!F.nodes_built) throw std::invalid_argument("the forest's nodes are not built");
+  auto X = std::make_shared<ForestDevice<D>>();
+  upload_leaves_and_brick(F, *X, s);
+  X->nn = (int64_t)F.num_nodes();
+  X->node_key.upload(F.node_key, s);
+  X->node_tree.upload(F.node_tree, s);
+  X->node_x.upload(F.node_x, s);
+  X->local_nodes.upload(F.local_nodes, s);
+  cuda_check(cudaStreamSynchronize(s), "forest upload");
+  F.device = X;
+  return *X;
+}
+
+template <int D>
+void build_nodes_device(Forest<D>& F, cudaStream_t s) {
+  using DD = Dim<D>;
+  auto X = std::make_shared<ForestDevice<D>>();
+  upload_leaves_and_brick(F, *X, s);
+  const int64_t nl = X->nl, nc = nl * DD::CHILDREN;
+  DevBuf<uint64_t> corner, sorted;
+  DevBuf<uint8_t> temp;
+  DevBuf<int64_t> nsel;
+  corner.alloc((size_t)nc + 1);
+  sorted.alloc((size_t)nc + 1);
+  X->node_key.alloc((size_t)nc + 1);
+  nsel.alloc(1);
+  if (nc) {
+    k_corner_keys<D><<<nblocks(nc), TPB, 0, s>>>(X->leaf_key.p, X->level.p, nl, F.brick.n[0], F.brick.n[1], F.brick.n[2], X->tree_ijk.p,
+                                                 X->ijk_to_tree.p, corner.p);
+    size_t b1 = 0, b2 = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, b1, corner.p, sorted.p, (int)nc, 0, 64, s);
+    cub::DeviceSelect::Unique(nullptr, b2, sorted.p, X->node_key.p, nsel.p, (int)nc, s);
+    temp.ensure(std::max(b1, b2) + 1);
+    cuda_check(cub::DeviceRadixSort::SortKeys(temp.p, b1, corner.p, sorted.p, (int)nc, 0, 64, s), "corner sort");
+    cuda_check(cub::DeviceSelect::Unique(temp.p, b2, sorted.p, X->node_key.p, nsel.p, (int)nc, s), "corner unique");
+  }
+  int64_t nn = 0;
+  if (nc) cuda_check(cudaMemcpyAsync(&nn, nsel.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "node count");
+  if (nn >= (int64_t)INT32_MAX) throw std::runtime_error("too many nodes for 32-bit node indices");
+  X->nn = nn;
+  X->node_tree.alloc((size_t)nn + 1);
+  X->node_x.alloc((size_t)nn * D + 1);
+  X->local_nodes.alloc((size_t)nc + 1);
+  if (nn) k_decode_nodes<D><<<nblocks(nn), TPB, 0, s>>>(X->node_key.p, nn, X->node_tree.p, X->node_x.p);
+  if (nc) k_local_nodes<<<nblocks(nc), TPB, 0, s>>>(corner.p, nc, X->node_key.p, nn, X->local_nodes.p);
+  cuda_check(cudaGetLastError(), "device node numbering");
+  F.node_key.resize((size_t)nn);
+  F.node_tree.resize((size_t)nn);
+  F.node_x.resize((size_t)nn * D);
+  F.local_nodes.resize((size_t)nc);
+  if (nn) {
+    cuda_check(cudaMemcpyAsync(F.node_key.data(), X->node_key.p, (size_t)nn * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(F.node_tree.data(), X->node_tree.p, (size_t)nn * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(F.node_x.data(), X->node_x.p, (size_t)nn * D * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  }
+  if (nc) cuda_check(cudaMemcpyAsync(F.local_nodes.data(), X->local_nodes.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "node download");
+  F.nodes_built = true;
+  F.device = X;
+}
+
+template <int D>
+void node_xyz_device(Forest<D>& F, double* out, cudaStream_t s) {
+  ForestDevice<D>& X = forest_device(F, s);
+  if (X.nn) k_node_xyz<D><<<nblocks(X.nn), TPB, 0, s>>>(X.node_tree.p, X.node_x.p, X.nn, X.tmin.p, X.tmax.p, out);
+  cuda_check(cudaGetLastError(), "node coordinates");
+}
+
+template <int D>
+bool refine_and_coarsen_device(Forest<D>& F, int min_lvl, int max_lvl, double lip, double band, const double* phi, cudaStream_t s) {
+  ForestDevice<D>& X = forest_device(F, s);
+  DevBuf<int8_t> tag;
+  tag.alloc((size_t)X.nl + 1);
+  if (X.nl)
+    k_tag_leaves<D><<<nblocks(X.nl), TPB, 0, s>>>(X.leaf_key.p, X.level.p, X.nl, X.local_nodes.p, X.tmin.p, X.tmax.p, phi, min_lvl, max_lvl,
+                                                  lip, band, tag.p);
+  cuda_check(cudaGetLastError(), "device tags");
+  std::vector<int8_t> h((size_t)X.nl);
+  if (X.nl) cuda_check(cudaMemcpyAsync(h.data(), tag.p, (size_t)X.nl, cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaStreamSynchronize(s), "tag download");
+  return F.coarsen_then_refine(h.data());
+}
+
 #define LSG_INST(D)                                                                          \
+  template void build_nodes_device<D>(Forest<D>&, cudaStream_t);                             \
+  template ForestDevice<D>& forest_device<D>(Forest<D>&, cudaStream_t);                      \
+  template void node_xyz_device<D>(Forest<D>&, double*, cudaStream_t);                       \
+  template bool refine_and_coarsen_device<D>(Forest<D>&, int, int, double, double, const double*, cudaStream_t); \
   template int64_t build_tables64_device<D>(const DForest<D>&, const Tab64Dev<D>&, cudaStream_t); \
   template void build_mixed_device<D>(const DTab64<D>&, int64_t, const double*, MixedDev<D>&, cudaStream_t);
 LSG_INST(2)

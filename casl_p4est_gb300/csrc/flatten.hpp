@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "devbuf.hpp"
+#include "forest.hpp"
 #include "kernels.h"
 
 namespace lsg {
@@ -28,6 +29,33 @@ struct DForest {
   const int32_t* node_tree;
   const int32_t* node_x;    // D per node
 };
+
+// Device copy of a forest's leaves (keys, levels), brick (tree coordinates, tree lookup, tree
+// corners) and nodes (keys, owner tree, clamped coordinates, corner nodes of every leaf). Held by
+// Forest::device and dropped when the leaves or nodes change.
+template <int D>
+struct ForestDevice {
+  int64_t nl = 0, nn = 0;
+  DevBuf<uint64_t> leaf_key, node_key;
+  DevBuf<int8_t> level;
+  DevBuf<int32_t> local_nodes, node_tree, node_x, tree_ijk, ijk_to_tree;
+  DevBuf<double> tmin, tmax;
+};
+
+// Node numbering on the device (the same keys, order and corner map as Forest::build_nodes), copied
+// back into the forest's host arrays; the device copy stays attached to the forest.
+template <int D>
+void build_nodes_device(Forest<D>& F, cudaStream_t s);
+// The forest's device copy, uploaded from the host arrays if the forest has none (nodes must be built).
+template <int D>
+ForestDevice<D>& forest_device(Forest<D>& F, cudaStream_t s);
+// Node coordinates (N x D, node_x_fr_n) from the device copy.
+template <int D>
+void node_xyz_device(Forest<D>& F, double* out, cudaStream_t s);
+// splitting_criteria_tag_t::refine_and_coarsen with the tags evaluated on the device from the node
+// values phi (device): only one byte per leaf comes back to the host for the coarsen/refine passes.
+template <int D>
+bool refine_and_coarsen_device(Forest<D>& F, int min_lvl, int max_lvl, double lip, double band, const double* phi, cudaStream_t s);
 
 // FP64 tables (sizes as Tables64); returns the number of correction records.
 template <int D>

@@ -80,6 +80,7 @@ void Forest<D>::init(const int* n, const double* xyz_min, const double* xyz_max,
     leaf_key.push_back(((uint64_t)t) << tree_shift<D>());
   }
   nodes_built = false;
+  device.reset();
 }
 
 template <int D>
@@ -114,6 +115,7 @@ void Forest<D>::refine(const uint8_t* tags) {
   leaves.swap(out);
   leaf_key.swap(keys);
   nodes_built = false;
+  device.reset();
 }
 
 template <int D>
@@ -160,12 +162,14 @@ void Forest<D>::coarsen(const uint8_t* tags) {
   leaves.swap(out);
   leaf_key.swap(keys);
   nodes_built = false;
+  device.reset();
 }
 
 template <int D>
 bool Forest<D>::coarsen_then_refine(const int8_t* tag) {
   const size_t nl = leaves.size();
   const bool had_nodes = nodes_built;
+  std::shared_ptr<void> had_device = device;
   std::vector<uint8_t> ctag(nl);
   for (size_t i = 0; i < nl; ++i) ctag[i] = tag[i] < 0;
   std::vector<Quad> out;
@@ -196,9 +200,11 @@ bool Forest<D>::coarsen_then_refine(const int8_t* tag) {
   leaves.swap(out);
   leaf_key.swap(keys);
   nodes_built = false;
+  device.reset();
   for (uint8_t t : rtag) changed = changed || t;
   if (!changed) {
-    nodes_built = had_nodes;  // same leaves: the node numbering still holds
+    nodes_built = had_nodes;  // same leaves: the node numbering (and its device copy) still holds
+    device = had_device;
     return false;
   }
   refine(rtag.data());
@@ -283,6 +289,7 @@ void Forest<D>::set_leaves(size_t n, const int32_t* tree, const int32_t* level, 
   leaves.swap(ls);
   leaf_key.swap(keys);
   nodes_built = false;
+  device.reset();
 }
 
 template <int D>
@@ -393,6 +400,7 @@ void Forest<D>::build_nodes() {
     local_nodes[(size_t)ii] = (int32_t)(it - node_key.begin());
   }
   nodes_built = true;
+  device.reset();
 }
 
 template <int D>

@@ -19,6 +19,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "lsg_common.h"
@@ -58,6 +59,9 @@ struct Forest {
   std::vector<uint64_t> node_key;
   std::vector<int32_t> local_nodes;  // CHILDREN per leaf, corner c = xbit + 2 ybit + 4 zbit
   bool nodes_built = false;
+  // device copy of the leaves and nodes (ForestDevice, flatten.hpp), set by the device node numbering
+  // or on first device use, dropped whenever the leaves or the nodes change
+  std::shared_ptr<void> device;
 
   void init(const int* n, const double* xyz_min, const double* xyz_max, const int* periodic);
   // One refinement pass: every leaf with tags[i] != 0 is replaced by its CHILDREN children.

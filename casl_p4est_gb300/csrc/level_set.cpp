@@ -90,10 +90,10 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed, bool device_buil
   } else {
     N = (int64_t)forest.num_nodes();
     init_stream();
+    // the forest's device copy (made by the device node numbering, else uploaded now) is shared
+    const ForestDevice<D>& X = forest_device(const_cast<Forest<D>&>(forest), stream);
+    fdev = forest.device;
     build_locator();
-    fl_tree_ijk.upload(forest.brick.tree_ijk, stream);
-    fl_node_tree.upload(forest.node_tree, stream);
-    fl_node_x.upload(forest.node_x, stream);
     DForest<D> DF{};
     DF.nleaves = TL.nleaves;
     DF.N = N;
@@ -105,11 +105,11 @@ LevelSet<D>::LevelSet(const Forest<D>& forest, bool with_mixed, bool device_buil
     DF.ncoarse = TL.ncoarse;
     for (int a = 0; a < 3; ++a) DF.n[a] = TL.n[a];
     DF.ijk_to_tree = TL.ijk_to_tree;
-    DF.tree_ijk = fl_tree_ijk.p;
+    DF.tree_ijk = X.tree_ijk.p;
     DF.tmin = TL.tmin;
     DF.tmax = TL.tmax;
-    DF.node_tree = fl_node_tree.p;
-    DF.node_x = fl_node_x.p;
+    DF.node_tree = X.node_tree.p;
+    DF.node_x = X.node_x.p;
     const Tab64Dev<D> out{&nbr, &w, &nrm, &d, &q, &cidx, &crec, &wall, &smin};
     num_corrections = build_tables64_device<D>(DF, out, stream);
     T64.N = N;
@@ -915,27 +915,38 @@ void LevelSet<D>::build_locator() {
     ctab[(size_t)i] = (int32_t)j;
   }
   ctab[(size_t)(nt * ncoarse)] = (int32_t)(nl - 1);
-  std::vector<int8_t> lvl((size_t)nl);
-  for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
-  loc_key.upload(f.leaf_key, stream);
-  loc_level.upload(lvl, stream);
-  loc_nodes.upload(f.local_nodes, stream);
   loc_ctab.upload(ctab, stream);
-  loc_ijk.upload(f.brick.ijk_to_tree, stream);
-  loc_tmin.upload(f.brick.tmin, stream);
-  loc_tmax.upload(f.brick.tmax, stream);
+  if (fdev) {
+    // the forest's device copy already holds the leaves, corner nodes and brick
+    const ForestDevice<D>& X = *static_cast<const ForestDevice<D>*>(fdev.get());
+    TL.key = X.leaf_key.p;
+    TL.level = X.level.p;
+    TL.local_nodes = X.local_nodes.p;
+    TL.ijk_to_tree = X.ijk_to_tree.p;
+    TL.tmin = X.tmin.p;
+    TL.tmax = X.tmax.p;
+  } else {
+    std::vector<int8_t> lvl((size_t)nl);
+    for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
+    loc_key.upload(f.leaf_key, stream);
+    loc_level.upload(lvl, stream);
+    loc_nodes.upload(f.local_nodes, stream);
+    loc_ijk.upload(f.brick.ijk_to_tree, stream);
+    loc_tmin.upload(f.brick.tmin, stream);
+    loc_tmax.upload(f.brick.tmax, stream);
+    TL.key = loc_key.p;
+    TL.level = loc_level.p;
+    TL.local_nodes = loc_nodes.p;
+    TL.ijk_to_tree = loc_ijk.p;
+    TL.tmin = loc_tmin.p;
+    TL.tmax = loc_tmax.p;
+  }
   cuda_check(cudaStreamSynchronize(stream), "locator upload");
   TL.nleaves = nl;
   TL.N = N;
-  TL.key = loc_key.p;
-  TL.level = loc_level.p;
-  TL.local_nodes = loc_nodes.p;
   TL.ctab = loc_ctab.p;
   TL.L0 = L0;
   TL.ncoarse = ncoarse;
-  TL.ijk_to_tree = loc_ijk.p;
-  TL.tmin = loc_tmin.p;
-  TL.tmax = loc_tmax.p;
   for (int a = 0; a < 3; ++a) {
     TL.n[a] = f.brick.n[a];
     TL.xyz_min[a] = f.brick.xyz_min[a];

@@ -107,9 +107,9 @@ struct LevelSet {
   std::vector<int> graph_key;          // iteration counts the captured graph was built for
   int64_t graph_launches = 0;          // kernels in the captured graph
   std::vector<int32_t> h_perm;         // device index -> node (host copy of the mixed tables' perm)
-  // device flattener inputs: the brick's tree coordinates and the nodes
+  // tables built by the device flattener from the forest's device copy (kept alive here)
   bool device_flat = false;
-  DevBuf<int32_t> fl_tree_ijk, fl_node_tree, fl_node_x;
+  std::shared_ptr<void> fdev;
 
   // device_build: the tables are built on the GPU by the device flattener (same FP64 tables; the
   // mixed tables, built on first use, differ only in the numbering of the irregular geometry classes)

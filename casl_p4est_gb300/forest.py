@@ -16,6 +16,10 @@ import numpy as np
 from . import _lib as L
 
 
+def _is_cuda(v) -> bool:
+    return hasattr(v, "data_ptr") and getattr(getattr(v, "device", None), "type", "cpu") == "cuda"
+
+
 class Forest:
     """p4est_t + p4est_nodes_t for one process (brick of trees, non-periodic)."""
 
@@ -108,7 +112,18 @@ class Forest:
     def refine_and_coarsen(self, min_lvl, max_lvl, phi, lip=1.2, band=0.0) -> bool:
         """splitting_criteria_tag_t(min_lvl, max_lvl, lip).refine_and_coarsen(p4est, nodes, phi): one
         coarsening and one refinement pass tagged from the node values phi. Returns whether the grid
-        changed; the nodes must be rebuilt."""
+        changed; the nodes must be rebuilt. With phi a CUDA tensor the tags are evaluated on the GPU
+        (on the tensor's current stream) and only one byte per leaf comes back to the host."""
+        if _is_cuda(phi):
+            import torch
+            if phi.dtype != torch.float64 or not phi.is_contiguous() or phi.numel() != self.num_nodes:
+                raise ValueError("phi must be a contiguous float64 tensor with one value per node")
+            changed = C.c_int(0)
+            L.check(L.load().lsg_forest_refine_and_coarsen_device(self._h, int(min_lvl), int(max_lvl), float(lip), float(band),
+                                                                  C.c_void_p(phi.data_ptr()), C.byref(changed),
+                                                                  C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            self.max_lvl_requested = max(self.max_lvl_requested, int(max_lvl))
+            return bool(changed.value)
         phi = np.ascontiguousarray(phi, np.float64)
         if phi.size != self.num_nodes:
             raise ValueError("phi must hold one value per node")
@@ -119,9 +134,24 @@ class Forest:
         return bool(changed.value)
 
     # ---- nodes --------------------------------------------------------------------------------
-    def build_nodes(self):
-        L.check(L.load().lsg_forest_build_nodes(self._h))
+    def build_nodes(self, device=False):
+        """my_p4est_nodes_new. device=True: the numbering is computed on the GPU (same result) and a
+        device copy of the leaves and nodes stays with the forest for node_xyz_device, device tagging and
+        level sets built on the device."""
+        if device:
+            import torch
+            L.check(L.load().lsg_forest_build_nodes_device(self._h, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        else:
+            L.check(L.load().lsg_forest_build_nodes(self._h))
         return self
+
+    def node_xyz_device(self):
+        """Node coordinates as a (N, dim) float64 CUDA tensor, computed on the GPU."""
+        import torch
+        out = torch.empty((self.num_nodes, self.dim), dtype=torch.float64, device="cuda")
+        L.check(L.load().lsg_forest_node_xyz_device(self._h, C.c_void_p(out.data_ptr()),
+                                                    C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return out
 
     @property
     def num_nodes(self) -> int:

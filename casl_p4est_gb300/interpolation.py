@@ -165,6 +165,8 @@ class my_p4est_semi_lagrangian_t:
         nodes of the final forest_np1 (which is modified in place)."""
         if self.splitting is None:
             raise ValueError("update_p4est needs the splitting criterion (min_lvl, max_lvl, lip)")
+        if _is_device(phi):
+            return self._update_p4est_device(v, dt, phi, phi_xx, vxx)
         min_lvl, max_lvl, lip = self.splitting
         N = self.ls_n.num_nodes
         phi = _f64(phi, "phi", N)
@@ -182,3 +184,44 @@ class my_p4est_semi_lagrangian_t:
             if not f.refine_and_coarsen(min_lvl, max_lvl, phi_np1, lip=lip):
                 return phi_np1
             f.build_nodes()
+
+    def _update_p4est_device(self, v, dt, phi, phi_xx, vxx):
+        """update_p4est with every field on the GPU (phi a CUDA tensor; v a VortexVelocity or a (dim, N)
+        CUDA tensor): node numbering, node coordinates, the semi-Lagrangian step and the refinement tags
+        run on the device, on the current torch stream (which ls_n is switched to); only one byte per
+        leaf goes to the host for each coarsening/refinement pass. Returns phi at the nodes of the final
+        forest_np1 as a CUDA tensor."""
+        import torch
+        min_lvl, max_lvl, lip = self.splitting
+        stream = torch.cuda.current_stream().cuda_stream
+        self.ls_n.set_stream(stream)
+        lib = L.load()
+        N = self.ls_n.num_nodes
+        if phi.dtype != torch.float64 or phi.numel() != N:
+            raise ValueError("phi must be a float64 tensor with one value per node of grid n")
+        phi = phi.contiguous()
+        if phi_xx is None and self.phi_interpolation != linear:
+            phi_xx = self.ls_n.compute_derivatives(phi)
+        vortex = isinstance(v, VortexVelocity)
+        if not vortex:
+            v = v.contiguous()
+            if vxx is None and self.velo_interpolation != linear:
+                vxx = torch.stack([self.ls_n.compute_derivatives(v[k].contiguous()) for k in range(self.dim)])
+        f = self.forest_np1
+        self.iterations = 0
+        while True:
+            xyz = f.node_xyz_device()
+            out = torch.empty(f.num_nodes, dtype=torch.float64, device=phi.device)
+            if vortex:
+                par = np.array([v.scale], np.float64)
+                L.check(lib.lsg_semi_lagrangian_advect_cf_device(self.ls_n.handle, _ptr(xyz), f.num_nodes, float(dt), L.LSG_VELOCITY_VORTEX,
+                                                                 L.dptr(par), 1, _ptr(phi), _ptr(phi_xx), int(self.phi_interpolation),
+                                                                 _ptr(out)))
+            else:
+                L.check(lib.lsg_semi_lagrangian_advect_device(self.ls_n.handle, _ptr(xyz), f.num_nodes, float(dt), _ptr(v), _ptr(vxx),
+                                                              _ptr(phi), _ptr(phi_xx), int(self.velo_interpolation),
+                                                              int(self.phi_interpolation), _ptr(out)))
+            self.iterations += 1
+            if not f.refine_and_coarsen(min_lvl, max_lvl, out, lip=lip):
+                return out
+            f.build_nodes(device=True)

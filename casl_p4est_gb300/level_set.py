@@ -161,8 +161,12 @@ class my_p4est_level_set_t:
         return dt
 
     def compute_derivatives(self, phi) -> np.ndarray:
-        """second_derivatives_central of phi: returns (dim, N)."""
+        """second_derivatives_central of phi: returns (dim, N) (a CUDA tensor for a CUDA tensor phi)."""
         n = self.num_nodes
+        if _is_device(phi):
+            out = phi.new_empty((self.ngbd.dim, n))
+            L.check(L.load().lsg_second_derivatives_device(self._h, C.c_void_p(phi.data_ptr()), C.c_void_p(out.data_ptr())))
+            return out
         _host_f64(phi, n, "phi")
         out = np.empty((self.ngbd.dim, n), np.float64)
         L.check(L.load().lsg_second_derivatives(self._h, L.dptr(phi), L.dptr(out)))

@@ -82,6 +82,21 @@ int lsg_forest_refine_levelset(lsg_forest* f, int min_lvl, int max_lvl, double l
                                const double* params, int nparams, int passes);
 /* my_p4est_nodes_new (src/my_p4est_nodes.c:292-1000): every leaf corner is a node */
 int lsg_forest_build_nodes(lsg_forest* f);
+/* The same node numbering computed on the GPU (corner keys canonicalised, sorted and made unique on
+ * the device), copied back into the forest; the device copy of the leaves and nodes stays with the
+ * forest for the two calls below and for LSG_BUILD_ON_DEVICE level sets. stream: a cudaStream_t or
+ * NULL. No reference counterpart (my_p4est_nodes_new runs on the host). */
+int lsg_forest_build_nodes_device(lsg_forest* f, void* stream);
+/* node_x_fr_n / node_y_fr_n / node_z_fr_n of every node (src/my_p4est_utils.h:1346-1405) into device
+ * memory, N x dim. */
+int lsg_forest_node_xyz_device(lsg_forest* f, double* xyz_dev, void* stream);
+/* lsg_forest_refine_and_coarsen with phi in device memory: the tags
+ * (splitting_criteria_tag_t::tag_quadrant, src/my_p4est_refine_coarsen.cpp:422-479) are evaluated on
+ * the GPU and only one byte per leaf is copied to the host for the coarsening and refinement passes
+ * (src/my_p4est_refine_coarsen.cpp:1170-1205, used by update_p4est at
+ * src/my_p4est_semi_lagrangian.cpp:480-490). */
+int lsg_forest_refine_and_coarsen_device(lsg_forest* f, int min_lvl, int max_lvl, double lip, double band, const double* phi_dev,
+                                         int* changed, void* stream);
 int64_t lsg_forest_num_nodes(const lsg_forest* f);
 /* node_xyz_fr_n (src/my_p4est_utils.h:1398-1405): dim doubles per node */
 int lsg_forest_node_xyz(const lsg_forest* f, double* xyz);
