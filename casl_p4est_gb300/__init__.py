@@ -9,10 +9,14 @@ from ._lib import LSG_FP64, LSG_MIXED, LsgError, LsgInvalidArgument, load
 from .forest import Forest, my_p4est_brick_new, my_p4est_node_neighbors_t, qnnn_dtype
 from .level_set import DBL_MAX, my_p4est_level_set_batch_t, my_p4est_level_set_t
 from .interpolation import VortexVelocity, my_p4est_interpolation_nodes_t, my_p4est_semi_lagrangian_t
-from . import interpolation
+from . import interpolation, save_load
+from .save_load import (VecDump, VecLoad, my_p4est_load_forest_and_data, my_p4est_save_forest_and_data,
+                        my_p4est_vtk_write_all)
 
 __all__ = [
     "shapes", "load", "LsgError", "LsgInvalidArgument", "LSG_FP64", "LSG_MIXED", "Forest", "my_p4est_brick_new",
     "my_p4est_node_neighbors_t", "qnnn_dtype", "my_p4est_level_set_t", "DBL_MAX", "interpolation",
     "my_p4est_interpolation_nodes_t", "my_p4est_semi_lagrangian_t", "VortexVelocity", "my_p4est_level_set_batch_t",
+    "save_load", "VecDump", "VecLoad", "my_p4est_save_forest_and_data", "my_p4est_load_forest_and_data",
+    "my_p4est_vtk_write_all",
 ]

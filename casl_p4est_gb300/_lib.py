@@ -43,6 +43,11 @@ SIGNATURES = {
     "lsg_forest_refine_levelset": (_I, [_P, _I, _I, _D, _D, _I, _DP, _I, _I]),
     "lsg_forest_build_nodes": (_I, [_P]),
     "lsg_forest_build_nodes_device": (_I, [_P, _P]),
+    "lsg_vtk_write_all": (_I, [_P, C.c_char_p, _I, _I, _P, _P, _I, _P, _P, _I]),
+    "lsg_vec_dump": (_I, [C.c_char_p, _I, _P, _I64, _I]),
+    "lsg_vec_load": (_I, [C.c_char_p, _I, _P, _I64, _I]),
+    "lsg_forest_save": (_I, [_P, C.c_char_p]),
+    "lsg_forest_load": (_I, [C.c_char_p, C.POINTER(_P)]),
     "lsg_forest_node_xyz_device": (_I, [_P, _P, _P]),
     "lsg_forest_refine_and_coarsen_device": (_I, [_P, _I, _I, _D, _D, _P, C.POINTER(C.c_int), _P]),
     "lsg_forest_num_nodes": (_I64, [_P]),

@@ -21,7 +21,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liblsgpu.so")
 
-HOST_SOURCES = ["forest.cpp", "tables.cpp", "tables32.cpp", "level_set.cpp", "capi.cpp"]
+HOST_SOURCES = ["forest.cpp", "tables.cpp", "tables32.cpp", "level_set.cpp", "capi.cpp", "io.cpp"]
 CUDA_SOURCES = {"kernels_fp64.cu": ["-fmad=false"], "kernels_interp.cu": ["-fmad=false"], "kernels_mixed.cu": [], "noalloc.cu": [],
                 "flatten.cu": ["-fmad=false"]}
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"

@@ -10,6 +10,7 @@
 
 #include "../../include/lsgpu.h"
 #include "flatten.hpp"
+#include "io.hpp"
 #include "level_set.hpp"
 #include "shapes.h"
 
@@ -347,6 +348,84 @@ int lsg_forest_refine_and_coarsen_device(lsg_forest* f, int min_lvl, int max_lvl
       need_nodes(F);
       *changed = refine_and_coarsen_device(const_cast<FT&>(F), min_lvl, max_lvl, lip, band, phi_dev, (cudaStream_t)stream) ? 1 : 0;
     });
+  });
+}
+
+int lsg_vtk_write_all(const lsg_forest* f, const char* filename, int write_tree, int num_point, const char* const* point_names,
+                      const double* const* point_values, int num_cell, const char* const* cell_names, const double* const* cell_values,
+                      int binary) {
+  return guard([&] {
+    need(filename != nullptr && num_point >= 0 && num_cell >= 0, "vtk: bad arguments");
+    need(num_point == 0 || (point_names != nullptr && point_values != nullptr), "vtk: null point data");
+    need(num_cell == 0 || (cell_names != nullptr && cell_values != nullptr), "vtk: null cell data");
+    std::vector<std::string> pn, cn;
+    std::vector<const double*> pv, cv;
+    for (int k = 0; k < num_point; ++k) {
+      need(point_names[k] != nullptr && point_values[k] != nullptr, "vtk: null point field");
+      pn.push_back(point_names[k]);
+      pv.push_back(point_values[k]);
+    }
+    for (int k = 0; k < num_cell; ++k) {
+      need(cell_names[k] != nullptr && cell_values[k] != nullptr, "vtk: null cell field");
+      cn.push_back(cell_names[k]);
+      cv.push_back(cell_values[k]);
+    }
+    with_forest(f, [&](auto& F) {
+      need_nodes(F);
+      vtk_write_all(F, filename, write_tree != 0, pn, pv, cn, cv, binary != 0);
+    });
+  });
+}
+
+int lsg_vec_dump(const char* fname, int nvecs, const double* const* vecs, int64_t n, int petsc_int64) {
+  return guard([&] {
+    need(fname != nullptr && nvecs >= 1 && vecs != nullptr && n >= 0, "VecDump: bad arguments");
+    std::vector<const double*> v(vecs, vecs + nvecs);
+    for (const double* p : v) need(p != nullptr || n == 0, "VecDump: null vector");
+    vec_dump(fname, v, n, petsc_int64 != 0);
+  });
+}
+
+int lsg_vec_load(const char* fname, int nvecs, double* const* vecs, int64_t n, int petsc_int64) {
+  return guard([&] {
+    need(fname != nullptr && nvecs >= 1 && vecs != nullptr && n >= 0, "VecLoad: bad arguments");
+    std::vector<double*> v(vecs, vecs + nvecs);
+    for (double* p : v) need(p != nullptr || n == 0, "VecLoad: null vector");
+    vec_load(fname, v, n, petsc_int64 != 0);
+  });
+}
+
+int lsg_forest_save(const lsg_forest* f, const char* fname) {
+  return guard([&] {
+    need(fname != nullptr, "forest save: null file name");
+    with_forest(f, [&](auto& F) { forest_save(F, fname); });
+  });
+}
+
+int lsg_forest_load(const char* fname, lsg_forest** out) {
+  return guard([&] {
+    need(fname != nullptr && out != nullptr, "forest load: null argument");
+    int dim = 0, n[3] = {1, 1, 1};
+    double lo[3], hi[3];
+    int64_t nl = 0;
+    forest_header(fname, &dim, n, lo, hi, &nl);
+    lsg_forest* f = new lsg_forest();
+    f->dim = dim;
+    try {
+      if (dim == 2) {
+        f->f2 = new Forest<2>();
+        f->f2->init(n, lo, hi, nullptr);
+        forest_load_leaves(*f->f2, fname);
+      } else {
+        f->f3 = new Forest<3>();
+        f->f3->init(n, lo, hi, nullptr);
+        forest_load_leaves(*f->f3, fname);
+      }
+    } catch (...) {
+      delete f;
+      throw;
+    }
+    *out = f;
   });
 }
 

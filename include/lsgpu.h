@@ -118,6 +118,28 @@ int lsg_forest_wall_mask(const lsg_forest* f, uint8_t* out);
 /* smallest cell size per axis at the finest level present (dxyz_min, src/my_p4est_utils.cpp:1136) */
 int lsg_forest_dxyz_min(const lsg_forest* f, double* dxyz);
 
+/* ---- on-disk formats (host) ------------------------------------------------------------------- */
+
+/* my_p4est_vtk_write_all (src/my_p4est_vtk.h:132-135, src/my_p4est_vtk.cpp:440-1872) for one process:
+ * <filename>.pvtu and <filename>.vtu/0000.vtu, an XML unstructured grid with the nodes as points
+ * ("Position"), the leaves as VTK_PIXEL / VTK_VOXEL cells, cell arrays proc_rank (and tree_idx when
+ * write_tree), then the node fields (N values each) and cell fields (one value per leaf). binary = 0
+ * writes ascii (the reference's default), 1 inline base64. */
+int lsg_vtk_write_all(const lsg_forest* f, const char* filename, int write_tree, int num_point, const char* const* point_names,
+                      const double* const* point_values, int num_cell, const char* const* cell_names, const double* const* cell_values,
+                      int binary);
+/* VecDump (src/my_p4est_save_load.h:61, src/my_p4est_save_load.cpp:77-98) as one process writes it:
+ * nvecs vectors of n doubles as PETSc binary Vec records (big-endian; int32 class id 1211214, the size
+ * as a 32-bit PetscInt, or 64-bit when petsc_int64, then the values), readable by PETSc's VecLoad.
+ * my_p4est_save_forest_and_data (src/my_p4est_save_load.cpp:350-380) writes one such file,
+ * <folder>/<name>.petscbin, per group of vectors. */
+int lsg_vec_dump(const char* fname, int nvecs, const double* const* vecs, int64_t n, int petsc_int64);
+int lsg_vec_load(const char* fname, int nvecs, double* const* vecs, int64_t n, int petsc_int64);
+/* The forest's leaves (and brick) in this library's own file format (p4est's own format is not
+ * written); load rebuilds the forest, nodes not built. */
+int lsg_forest_save(const lsg_forest* f, const char* fname);
+int lsg_forest_load(const char* fname, lsg_forest** out);
+
 /* ---- level set (device) ----------------------------------------------------------------------- */
 
 /* my_p4est_level_set_t(my_p4est_node_neighbors_t*) (src/my_p4est_level_set.h:385-392): builds the
