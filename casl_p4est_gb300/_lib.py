@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "liblsgpu.so")
 LSG_OK, LSG_EINVAL, LSG_ENOMEM, LSG_EDEVICE, LSG_ETIMEOUT, LSG_ENAN, LSG_ESTATE = range(7)
 LSG_FP64, LSG_MIXED = 0, 1
 LSG_BUILD_ON_DEVICE = 1
+# int (*lsg_velocity_fn)(void* ctx, int64_t npts, const double* xyz, double* v)
+VELOCITY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double))
 LSG_VELOCITY_VORTEX = 0
 
 _P = C.c_void_p
@@ -96,6 +98,7 @@ SIGNATURES = {
     "lsg_semi_lagrangian_advect_device": (_I, [_P, _P, _I64, _D, _P, _P, _P, _P, _I, _I, _P]),
     "lsg_semi_lagrangian_advect_cf": (_I, [_P, _DP, _I64, _D, _I, _DP, _I, _DP, _DP, _I, _DP]),
     "lsg_semi_lagrangian_advect_cf_device": (_I, [_P, _P, _I64, _D, _I, _DP, _I, _P, _P, _I, _P]),
+    "lsg_semi_lagrangian_advect_callback": (_I, [_P, _DP, _I64, _D, _P, _P, _DP, _DP, _I, _DP]),
     "lsg_band_linf_device": (_I, [_P, _P, _P, _D, _DP, C.POINTER(_I64)]),
     "lsg_batch_create": (_I, [_I, C.POINTER(_P), C.POINTER(_P)]),
     "lsg_batch_count": (_I, [_P]),

@@ -895,6 +895,41 @@ int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz, i
   });
 }
 
+int lsg_semi_lagrangian_advect_callback(lsg_level_set* ls, const double* xyz, int64_t npts, double dt, lsg_velocity_fn velocity,
+                                        void* ctx, const double* phi, const double* phi_dd, int phi_method, double* phi_np1) {
+  return guard([&] {
+    need(velocity != nullptr && phi != nullptr && phi_np1 != nullptr && (xyz != nullptr || npts == 0), "null argument");
+    need(npts >= 0, "negative number of points");
+    with_ls(ls, [&](auto& L) {
+      using LT = std::decay_t<decltype(L)>;
+      constexpr int D = LT::DIM;
+      need(L.F != nullptr, "advect_from_n_to_np1: needs a single grid's level set");
+      const Brick& B = L.F->brick;
+      const size_t n = (size_t)npts * D;
+      std::vector<double> v(n + 1), xs(n + 1), xd(n + 1);
+      auto clip = [&](double* x) {
+        for (int a = 0; a < D; ++a)
+          if (x[a] < B.xyz_min[a] || x[a] > B.xyz_max[a]) x[a] = max2(B.xyz_min[a], min2(B.xyz_max[a], x[a]));
+      };
+      auto eval = [&](const double* pts) {
+        if (npts && velocity(ctx, npts, pts, v.data()) != 0) throw std::runtime_error("advect_from_n_to_np1: the velocity callback failed");
+      };
+      // x* = x - dt/2 v(x), clipped; x_d = x - dt v(x*), clipped (src/my_p4est_semi_lagrangian.cpp:108-146)
+      eval(xyz);
+      for (int64_t p = 0; p < npts; ++p) {
+        for (int a = 0; a < D; ++a) xs[(size_t)p * D + a] = xyz[(size_t)p * D + a] - 0.5 * dt * v[(size_t)p * D + a];
+        clip(&xs[(size_t)p * D]);
+      }
+      eval(xs.data());
+      for (int64_t p = 0; p < npts; ++p) {
+        for (int a = 0; a < D; ++a) xd[(size_t)p * D + a] = xyz[(size_t)p * D + a] - dt * v[(size_t)p * D + a];
+        clip(&xd[(size_t)p * D]);
+      }
+      L.interpolate_host(xd.data(), npts, 1, phi, phi_dd, phi_method, phi_np1);
+    });
+  });
+}
+
 int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set** out) {
   return guard([&] {
     need(out != nullptr && forests != nullptr && count > 0, "batch: null arguments or no grids");

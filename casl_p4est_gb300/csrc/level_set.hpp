@@ -42,6 +42,7 @@ struct KernelTimer {
 
 template <int D>
 struct LevelSet {
+  static constexpr int DIM = D;
   static constexpr int H = Dim<D>::HALF;
   static constexpr int NS = 2 * D * H;
   const Forest<D>* F = nullptr;

@@ -135,8 +135,9 @@ class my_p4est_semi_lagrangian_t:
         self.phi_interpolation = method
 
     def advect_from_n_to_np1(self, dt, v, phi_n, vxx=None, phi_xx_n=None, xyz_np1=None):
-        """v: (dim, N_n) node velocities, or a VortexVelocity (the CF overload). Returns phi at the
-        nodes of forest_np1 (host arrays)."""
+        """v: (dim, N_n) node velocities, a VortexVelocity, or a callable velocity(xyz) -> (dim, npts)
+        evaluated on the host at points xyz (npts, dim) (the CF overload). Returns phi at the nodes of
+        forest_np1 (host arrays)."""
         lib = L.load()
         N = self.ls_n.num_nodes
         xyz = xyz_np1 if xyz_np1 is not None else self.forest_np1.node_xyz()
@@ -144,6 +145,27 @@ class my_p4est_semi_lagrangian_t:
         phi_n = _f64(phi_n, "phi_n", N)
         pdd = None if phi_xx_n is None else _f64(phi_xx_n, "phi_xx_n", self.dim * N)
         out = np.empty(len(xyz), np.float64)
+        if callable(v) and not isinstance(v, VortexVelocity):
+            dim = self.dim
+            failure = []
+
+            def trampoline(ctx, npts, pts, vout):
+                try:
+                    p = np.ctypeslib.as_array(pts, shape=(npts, dim))
+                    val = np.asarray(v(p.copy()), np.float64).reshape(dim, npts)
+                    np.ctypeslib.as_array(vout, shape=(npts, dim))[:] = val.T
+                    return 0
+                except Exception as e:  # reported after the call
+                    failure.append(e)
+                    return 1
+
+            cb = L.VELOCITY_FN(trampoline)
+            code = lib.lsg_semi_lagrangian_advect_callback(self.ls_n.handle, L.dptr(xyz), len(xyz), float(dt), cb, None, L.dptr(phi_n),
+                                                           _ptr(pdd), int(self.phi_interpolation), L.dptr(out))
+            if failure:
+                raise failure[0]
+            L.check(code)
+            return out
         if isinstance(v, VortexVelocity):
             par = np.array([v.scale], np.float64)
             L.check(lib.lsg_semi_lagrangian_advect_cf(self.ls_n.handle, L.dptr(xyz), len(xyz), float(dt), L.LSG_VELOCITY_VORTEX,

@@ -292,6 +292,14 @@ int lsg_semi_lagrangian_advect_cf(lsg_level_set* ls, const double* xyz_np1, int6
 int lsg_semi_lagrangian_advect_cf_device(lsg_level_set* ls, const double* xyz_np1_dev, int64_t npts, double dt, int velocity,
                                          const double* params, int nparams, const double* phi_n_dev, const double* phi_dd_dev,
                                          int phi_method, double* phi_np1_dev);
+/* advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1) (src/my_p4est_semi_lagrangian.cpp:108-146)
+ * for any velocity: the callback evaluates it on the host at npts points (xyz and v both npts x dim,
+ * interleaved; return 0 on success), the departure points x* = x - dt/2 v(x) and x_d = x - dt v(x*)
+ * (each clipped to the domain) are formed on the host as the reference does, and phi (host, N) is
+ * interpolated at x_d on the GPU with phi_method. */
+typedef int (*lsg_velocity_fn)(void* ctx, int64_t npts, const double* xyz, double* v);
+int lsg_semi_lagrangian_advect_callback(lsg_level_set* ls, const double* xyz_np1, int64_t npts, double dt, lsg_velocity_fn velocity,
+                                        void* ctx, const double* phi, const double* phi_dd, int phi_method, double* phi_np1);
 
 /* The band check that accompanies every result: max |a - b| over the nodes with |b| < band, in FP64
  * on the device (warp-shuffle reduction), b the reference field (e.g. the FP64 result), a the field

@@ -392,6 +392,41 @@ class my_p4est_semi_lagrangian_t {
     lsgpu::check(lsg_semi_lagrangian_advect(ngbd_n_->device(), xyz.data(), np, dt, vv.data(), vdd.empty() ? nullptr : vdd.data(), p.p,
                                             pdd.empty() ? nullptr : pdd.data(), (int)velo_, (int)phi_, phi_np1));
   }
+  // advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1): v[D] function objects of the
+  // coordinates, evaluated on the host at the nodes of grid n+1 and at the midpoints.
+  template <typename CF>
+  void advect_from_n_to_np1(double dt, const CF* const* v, Vec phi_n, Vec* phi_xx_n, double* phi_np1) const {
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes();
+    std::vector<double> pdd;
+    if (phi_xx_n) {
+      pdd.resize((size_t)D * N);
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(phi_xx_n[a]);
+        for (size_t n = 0; n < N; ++n) pdd[a * N + n] = x.p[n];
+      }
+    }
+    struct Ctx {
+      const CF* const* v;
+      int D;
+    } ctx{v, D};
+    lsg_velocity_fn fn = [](void* c, int64_t npts, const double* xyz, double* out) -> int {
+      const Ctx* k = static_cast<const Ctx*>(c);
+      try {
+        for (int64_t p = 0; p < npts; ++p)
+          for (int a = 0; a < k->D; ++a) out[p * k->D + a] = lsgpu::eval_cf(*k->v[a], &xyz[p * k->D], k->D);
+      } catch (...) {
+        return 1;
+      }
+      return 0;
+    };
+    const int64_t np = lsg_forest_num_nodes(forest_np1_);
+    std::vector<double> xyz((size_t)np * D);
+    lsgpu::check(lsg_forest_node_xyz(forest_np1_, xyz.data()));
+    lsgpu::VecArray p(phi_n);
+    lsgpu::check(lsg_semi_lagrangian_advect_callback(ngbd_n_->device(), xyz.data(), np, dt, fn, &ctx, p.p, pdd.empty() ? nullptr : pdd.data(),
+                                                     (int)phi_, phi_np1));
+  }
 
  private:
   lsg_forest* forest_np1_;

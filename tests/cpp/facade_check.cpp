@@ -120,6 +120,25 @@ int main() {
   for (int64_t i = 0; i < N; ++i)
     if (qe2.values[2 * i] != qe_ref[i] || qe2.values[2 * i + 1] != qe_ref[N + i]) return fail("extend_from_interface_to_whole_domain_TVD");
 
+  // the CF overload with a constant velocity: departure points x - dt c, clipped, then the phi
+  // interpolation of the C ABI at those points
+  struct constant_velocity {
+    double c;
+    double operator()(double, double) const { return c; }
+  };
+  const constant_velocity cx{0.3}, cy{-0.2};
+  const constant_velocity* cf[2] = {&cx, &cy};
+  std::vector<double> np1_cf((size_t)N), xd((size_t)2 * N), np1_cf_ref((size_t)N);
+  sl.advect_from_n_to_np1(0.05, cf, &phi, nullptr, np1_cf.data());
+  for (int64_t i = 0; i < N; ++i) {
+    xd[2 * i] = xyz[2 * i] - 0.05 * 0.3;
+    xd[2 * i + 1] = xyz[2 * i + 1] - 0.05 * -0.2;
+    for (int a = 0; a < 2; ++a) xd[2 * i + a] = xd[2 * i + a] < lo[a] ? lo[a] : (xd[2 * i + a] > hi[a] ? hi[a] : xd[2 * i + a]);
+  }
+  lsgpu::check(lsg_interpolate_nodes(raw, xd.data(), N, phi.values.data(), 1, nullptr, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2,
+                                     np1_cf_ref.data()));
+  if (memcmp(np1_cf.data(), np1_cf_ref.data(), N * sizeof(double)) != 0) return fail("advect_from_n_to_np1 (CF)");
+
   // errors come back as exceptions
   try {
     ls.reinitialize_within_range_of_phi_0(&phi, 3, 2, 1.0, -1.0, 5);

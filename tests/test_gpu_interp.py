@@ -153,6 +153,20 @@ def test_semi_lagrangian_vortex(case):
         assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(phi))
 
 
+def test_semi_lagrangian_callback_velocity(case):
+    """The CF overload with a host callback: departure points formed on the host with the same
+    velocity the oracle uses (its single vortex), so the result is the oracle's bit for bit."""
+    name, f, ls, og = case
+    x = f.node_xyz()
+    phi = fields(f)[0]
+    _, dmin, _ = f.dxyz_min()
+    sl = G.my_p4est_semi_lagrangian_t(f, ls)
+    got = sl.advect_from_n_to_np1(3.0 * dmin, lambda p: O.vortex(f.dim, p, -0.5), phi)
+    assert np.array_equal(got, og.sl_advect_vortex(x, 3.0 * dmin, -0.5, phi))
+    with pytest.raises(ZeroDivisionError):
+        sl.advect_from_n_to_np1(dmin, lambda p: 1 / 0, phi)
+
+
 def test_bad_method_is_rejected(case):
     name, f, ls, og = case
     interp = G.my_p4est_interpolation_nodes_t(ls)
