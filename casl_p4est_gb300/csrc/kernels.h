@@ -213,6 +213,7 @@ void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* d
 void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64_t n, int64_t src_stride, int64_t dst_stride,
                        int blocks, cudaStream_t s);
 void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* status, double* dst, int64_t n, int64_t src_stride,
-                        int64_t dst_stride, int blocks, cudaStream_t s);
+                        int64_t dst_stride, int blocks, cudaStream_t s,
+                        const uint16_t* lim = nullptr);
 
 }  // namespace lsg

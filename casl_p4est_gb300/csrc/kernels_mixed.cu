@@ -906,10 +906,12 @@ __global__ void k_gather_f32(const double* __restrict__ src, const int32_t* __re
   for (int b = 0; b < blocks; ++b) dst[b * dst_stride + i] = (float)src[b * src_stride + p];
 }
 __global__ void k_scatter_f64(const float* __restrict__ src, const int32_t* __restrict__ perm, const uint16_t* __restrict__ status,
-                              double* __restrict__ dst, int64_t n, int64_t src_stride, int64_t dst_stride, int blocks) {
+                              const uint16_t* __restrict__ lim, double* __restrict__ dst, int64_t n, int64_t src_stride,
+                              int64_t dst_stride, int blocks) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (status && (status[i] & ST_OUTSIDE)) return;
+  if (lim && lim[i] == 0) return;  // a grid of a batch run for zero iterations keeps its values
   const int64_t p = perm[i];
   for (int b = 0; b < blocks; ++b) dst[b * dst_stride + p] = (double)src[b * src_stride + i];
 }
@@ -1036,8 +1038,8 @@ void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64
   if (n) k_gather_f32<<<nblocks(n), TPB, 0, s>>>(src, perm, dst, n, src_stride, dst_stride, blocks);
 }
 void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* status, double* dst, int64_t n, int64_t src_stride,
-                        int64_t dst_stride, int blocks, cudaStream_t s) {
-  if (n) k_scatter_f64<<<nblocks(n), TPB, 0, s>>>(src, perm, status, dst, n, src_stride, dst_stride, blocks);
+                        int64_t dst_stride, int blocks, cudaStream_t s, const uint16_t* lim) {
+  if (n) k_scatter_f64<<<nblocks(n), TPB, 0, s>>>(src, perm, status, lim, dst, n, src_stride, dst_stride, blocks);
 }
 
 #define LSG_INST(D)                                                                                                             \

@@ -409,6 +409,7 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
 // subcell step in FP64.
 template <int D>
 void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters) {
+  if (iters == 0) return;  // phi unchanged, as with no iteration in FP64
   build_mixed();
   f_phi.alloc(N);
   f_phi1.alloc(N);
@@ -547,7 +548,7 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
   } else {
     mixed_loop(2, max_it, freeze_at);
   }
-  LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
+  LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream, iter_lim.p));
   cuda_check(cudaGetLastError(), "reinitialize (batch)");
 }
 
