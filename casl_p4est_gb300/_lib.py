@@ -70,6 +70,8 @@ SIGNATURES = {
     "lsg_level_set_zero_distance_threshold": (_D, [_P]),
     "lsg_reinitialize": (_I, [_P, _DP, _I, _I, _D, _D, _I, _I]),
     "lsg_reinitialize_device": (_I, [_P, _P, _I, _I, _D, _D, _I, _I]),
+    "lsg_reinitialize_with_mask": (_I, [_P, _DP, _DP, _I, _I, _D, _D, _I, _I]),
+    "lsg_reinitialize_with_mask_device": (_I, [_P, _P, _P, _I, _I, _D, _D, _I, _I]),
     "lsg_reinitialize_device_noalloc": (_I, [_P, _P, _I, _I, _D, _D, _I]),
     "lsg_reinit_2nd": (_I, [_P, _DP, _I, _D, _I]),
     "lsg_advect_in_normal_direction": (_I, [_P, _DP, _DP, _DP, _D, _DP, _I]),

@@ -602,6 +602,26 @@ int lsg_reinitialize_device(lsg_level_set* ls, double* phi_dev, int order_space,
   });
 }
 
+int lsg_reinitialize_with_mask(lsg_level_set* ls, double* phi, const double* mask, int order_space, int order_pseudotime,
+                               double limit_high, double limit_low, int iterations, int precision) {
+  return guard([&] {
+    need(phi != nullptr && mask != nullptr, "null phi or mask");
+    with_ls(ls, [&](auto& L) {
+      L.reinitialize_host(phi, order_space, order_pseudotime, limit_high, limit_low, iterations, precision, mask);
+    });
+  });
+}
+
+int lsg_reinitialize_with_mask_device(lsg_level_set* ls, double* phi_dev, const double* mask_dev, int order_space, int order_pseudotime,
+                                      double limit_high, double limit_low, int iterations, int precision) {
+  return guard([&] {
+    need(phi_dev != nullptr && mask_dev != nullptr, "null phi or mask");
+    with_ls(ls, [&](auto& L) {
+      L.reinitialize(phi_dev, order_space, order_pseudotime, limit_high, limit_low, iterations, precision, mask_dev);
+    });
+  });
+}
+
 int lsg_reinitialize_device_noalloc(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime,
                                     double limit_high, double limit_low, int iterations) {
   return guard([&] {

@@ -149,6 +149,8 @@ template <int D>
 void launch_ext_q(const DTab64<D>& T, const double* q, double* tmp, const double* qdd, const double* phi, const double* mask,
                   const double* nrm, const double* qn, int order, double band_extend, cudaStream_t s);
 // FP64 band L-infinity: out3 = {bits of max |a-b| over |b| < band, band node count, NaN flag}
+// nodes whose mask is 0 (mask in node order; perm maps status indices to nodes, or null) become ST_OUTSIDE
+void launch_apply_mask(const double* mask, const int32_t* perm, uint16_t* status, int64_t n, cudaStream_t s);
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s);
 // Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p
 // is first moved to xyz[p] - coef*shift[:, p] and clipped into the domain (the semi-Lagrangian

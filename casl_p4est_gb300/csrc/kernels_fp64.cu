@@ -745,6 +745,19 @@ void launch_efi_stage64(const DTab64<D>& T, const double* phi, const double* gra
     k_efi_stage64<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, phi, grad, q, qdd, qdd2, qi_nb, s_nb, cross, zdt, out);
 }
 
+// reinitialize_2nd_order_with_mask (src/my_p4est_level_set.h:487-525): nodes whose mask is 0 are left out
+// of the updates and keep their value, which is what ST_OUTSIDE gives (phi_np1 = phi_np2 = phi_0 = phi_n at
+// those nodes). perm (device index -> node) is null for node-ordered status arrays.
+__global__ void k_apply_mask(const double* __restrict__ mask, const int32_t* __restrict__ perm, uint16_t* __restrict__ status, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (mask[perm ? perm[i] : i] == 0.0) status[i] = ST_OUTSIDE;
+}
+
+void launch_apply_mask(const double* mask, const int32_t* perm, uint16_t* status, int64_t n, cudaStream_t s) {
+  if (n) k_apply_mask<<<nblocks(n), TPB, 0, s>>>(mask, perm, status, n);
+}
+
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
   cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
   if (n == 0) return;

@@ -229,7 +229,8 @@ void LevelSet<D>::second_derivatives(const double* f, double* dd) {
 }
 
 template <int D>
-void LevelSet<D>::reinitialize(double* phi, int os, int ot, double limit_high, double limit_low, int iterations, int precision) {
+void LevelSet<D>::reinitialize(double* phi, int os, int ot, double limit_high, double limit_low, int iterations, int precision,
+                               const double* mask) {
   if (os < 1 || os > 2 || ot < 1 || ot > 2)
     throw std::invalid_argument(
         "reinitialize_within_range_of_phi_0: valid orders of orders of accuracy for space and pseudotime are 1 and 2 only!");
@@ -240,9 +241,9 @@ void LevelSet<D>::reinitialize(double* phi, int os, int ot, double limit_high, d
   const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
   const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
   if (precision == PREC_FP64)
-    reinit_fp64(phi, os, ot, hi, lo, iterations);
+    reinit_fp64(phi, os, ot, hi, lo, iterations, mask);
   else if (precision == PREC_MIXED)
-    reinit_mixed(phi, os, ot, hi, lo, iterations);
+    reinit_mixed(phi, os, ot, hi, lo, iterations, mask);
   else
     throw std::invalid_argument("reinitialize: unknown precision mode");
 }
@@ -263,7 +264,7 @@ void LevelSet<D>::reinitialize_fp64_noalloc(double* phi, int os, int ot, double 
 // reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557) on one device:
 // the ghost updates of a single process are no-ops and the layer/local split merges into one launch.
 template <int D>
-void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo, int iters) {
+void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo, int iters, const double* mask) {
   phi0.alloc(N);
   phi1.alloc(N);
   dd0.alloc((size_t)D * N);
@@ -273,6 +274,7 @@ void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo,
   cuda_check(cudaMemcpyAsync(phi0.p, phi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_0");
   LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi0.p, dd0.p, stream));
   LSG_LAUNCH(K_PREP64, launch_reinit_prep64<D>(T64, phi0.p, dd0.p, zdt, lo, hi, os, status.p, snear.p, stream));
+  if (mask) LSG_LAUNCH(K_PREP64, launch_apply_mask(mask, nullptr, status.p, N, stream));
   for (int it = 0; it < iters; ++it) {
     LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, ddc.p, stream));
     LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0.p, phi, ddc.p, phi1.p, nullptr, stream));
@@ -408,7 +410,7 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
 // Mixed precision: phi_n and all per-iteration work in FP32 (device node order); the phi_0-only
 // subcell step in FP64.
 template <int D>
-void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters) {
+void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters, const double* mask) {
   if (iters == 0) return;  // phi unchanged, as with no iteration in FP64
   build_mixed();
   f_phi.alloc(N);
@@ -421,6 +423,7 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   LSG_LAUNCH(K_PREP_MIXED, launch_reinit_prep_mixed<D>(T32, perm.p, phi, zdt, lo, hi, os, phi0.p, dd0.p, status.p, f_snear.p,
                                                        near_list.p, near_count.p, stream));
   timer.launches += 3;  // the FP64 subcell step is four kernels
+  if (mask) LSG_LAUNCH(K_PREP_MIXED, launch_apply_mask(mask, perm.p, status.p, N, stream));
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
   for (int it = 0; it < iters; ++it) {
     mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
@@ -702,10 +705,16 @@ double LevelSet<D>::band_linf(const double* a, const double* b, double band, int
 }
 
 template <int D>
-void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision) {
+void LevelSet<D>::reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision, const double* mask) {
   ws_phi.alloc(N);
   cuda_check(cudaMemcpyAsync(ws_phi.p, phi, N * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D phi");
-  reinitialize(ws_phi.p, os, ot, hi, lo, iters, precision);
+  const double* dmask = nullptr;
+  if (mask) {
+    ws_vn.ensure((size_t)N + 1);
+    if (N) cuda_check(cudaMemcpyAsync(ws_vn.p, mask, N * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D mask");
+    dmask = ws_vn.p;
+  }
+  reinitialize(ws_phi.p, os, ot, hi, lo, iters, precision, dmask);
   cuda_check(cudaMemcpyAsync(phi, ws_phi.p, N * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H phi");
   cuda_check(cudaStreamSynchronize(stream), "reinitialize sync");
 }

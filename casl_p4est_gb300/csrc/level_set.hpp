@@ -123,7 +123,7 @@ struct LevelSet {
 
   // phi: device pointer, N doubles, updated in place (reinitialize_within_range_of_phi_0).
   void reinitialize(double* phi, int order_space, int order_pseudotime, double limit_high, double limit_low, int iterations,
-                    int precision);
+                    int precision, const double* mask = nullptr);
   // advect_in_normal_direction(vn[, vn_np1], phi, dt, phi_xx...): device pointers; phi_dd may be null
   // (D*N doubles, overwritten with the derivatives of the intermediate stage as the reference does).
   void advect_normal(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd, int precision);
@@ -186,7 +186,7 @@ struct LevelSet {
   void drop_graph();  // forget a captured graph (after a launch-shape change)
 
   // host-buffer conveniences (copies inside)
-  void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision);
+  void reinitialize_host(double* phi, int os, int ot, double hi, double lo, int iters, int precision, const double* mask = nullptr);
   void interpolate_host(const double* xyz, int64_t np, int nf, const double* F, const double* Fdd, int method, double* out);
   void sl_advect_host(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi,
                       const double* phi_dd, int velo_method, int phi_method, double* phi_np1);
@@ -202,8 +202,8 @@ struct LevelSet {
   void upload_mixed(const Tables32<D>& M, const double* tree_size);
   void set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int base, int64_t x_first, int64_t nX, int64_t ncls_, const double* ts);
   void init_stream();
-  void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
-  void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters);
+  void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
+  void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
   void build_locator();

@@ -108,6 +108,20 @@ class my_p4est_level_set_t:
         self.reinitialize_within_range_of_phi_0(phi, 2, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
                                                 number_of_iterations, precision)
 
+    def reinitialize_2nd_order_with_mask(self, phi, mask, number_of_masked=0, number_of_iterations=50,
+                                         limit_absolute_value_phi_0=DBL_MAX, precision=None):
+        """reinitialize_2nd_order_with_mask (src/my_p4est_level_set.h:487-525): nodes where mask == 0 keep
+        their value (number_of_masked is the reference's reservation hint and is not needed here)."""
+        p = self._prec(precision)
+        lim = float(limit_absolute_value_phi_0)
+        if _is_device(phi):
+            L.check(L.load().lsg_reinitialize_with_mask_device(self._h, C.c_void_p(phi.data_ptr()), C.c_void_p(mask.data_ptr()), 2, 2,
+                                                               lim, -lim, int(number_of_iterations), p))
+            return
+        _host_f64(phi, self.num_nodes, "phi")
+        m = _host_f64(np.ascontiguousarray(mask, np.float64), self.num_nodes, "mask")
+        L.check(L.load().lsg_reinitialize_with_mask(self._h, L.dptr(phi), L.dptr(m), 2, 2, lim, -lim, int(number_of_iterations), p))
+
     def reinitialize_2nd_order_above_threshold(self, phi, threshold, number_of_iterations=50, upper_limit_phi_0=DBL_MAX,
                                                precision=None):
         self.reinitialize_within_range_of_phi_0(phi, 2, 2, upper_limit_phi_0, threshold, number_of_iterations, precision)

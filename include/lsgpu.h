@@ -165,6 +165,14 @@ int lsg_reinitialize(lsg_level_set* ls, double* phi, int order_space, int order_
                      double limit_low, int iterations, int precision);
 int lsg_reinitialize_device(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime, double limit_high,
                             double limit_low, int iterations, int precision);
+/* reinitialize_2nd_order_with_mask(phi, mask, number_of_masked, iterations, limit)
+ * (src/my_p4est_level_set.h:487-525) generalised to every order: the nodes where mask == 0 are left out
+ * of the updates (their value is kept, their neighbours still read it). mask: N values, host or device
+ * like phi. The reference's call is orders (2, 2) with limits (limit, -limit). */
+int lsg_reinitialize_with_mask(lsg_level_set* ls, double* phi, const double* mask, int order_space, int order_pseudotime,
+                               double limit_high, double limit_low, int iterations, int precision);
+int lsg_reinitialize_with_mask_device(lsg_level_set* ls, double* phi_dev, const double* mask_dev, int order_space, int order_pseudotime,
+                                      double limit_high, double limit_low, int iterations, int precision);
 /* No counterpart in the reference. lsg_reinitialize_device with precision LSG_FP64, allocating no
  * memory: the work vectors (114 bytes per node in 3D, 82 in 2D, each array padded to 256 bytes)
  * come from one static device array of LSG_NOALLOC_SCRATCH_BYTES per device; larger grids return

@@ -6,6 +6,8 @@
  *   my_p4est_level_set_t(my_p4est_node_neighbors_t*)                  src/my_p4est_level_set.h:385-414
  *   reinitialize_{1st,2nd}_order[_above_threshold|_time_...](Vec phi, iterations, limit)
  *                                                                      src/my_p4est_level_set.h:434-613
+ *   reinitialize_2nd_order_with_mask(Vec phi, Vec mask, number_of_masked, iterations, limit)
+ *                                                                      src/my_p4est_level_set.h:487-525
  *   perturb_level_set_function(Vec phi, epsilon)                       src/my_p4est_level_set.h:621
  *   advect_in_normal_direction(CF / Vec vn[, Vec vn_np1], Vec phi, dt, phi_xx, phi_yy[, phi_zz])
  *                                                                      src/my_p4est_level_set.h:632-659
@@ -177,6 +179,13 @@ class my_p4est_level_set_t {
   void reinitialize_1st_order_time_2nd_order_space_above_threshold(Vec phi, const double& threshold, const int& number_of_iterations = 50,
                                                                   const double& upper_limit_phi_0 = DBL_MAX) const {
     reinitialize_within_range_of_phi_0(phi, 2, 1, upper_limit_phi_0, threshold, number_of_iterations);
+  }
+  void reinitialize_2nd_order_with_mask(Vec phi, Vec mask, const int& number_of_masked, const int& number_of_iterations = 50,
+                                        const double& limit_absolute_value_phi_0 = DBL_MAX) const {
+    (void)number_of_masked;  // a reservation hint in the reference
+    lsgpu::VecArray p(phi), m(mask);
+    lsgpu::check(lsg_reinitialize_with_mask(ngbd_->device(), p.p, m.p, 2, 2, limit_absolute_value_phi_0, -limit_absolute_value_phi_0,
+                                            number_of_iterations, precision_));
   }
   void perturb_level_set_function(Vec phi, const double& epsilon) const {
     lsgpu::VecArray p(phi);

@@ -709,9 +709,12 @@ void compute_derivatives(const Ctx& cx, const double* f, double* fdd, int nthrea
   }
 }
 
-// reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557)
+// reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557); with a mask
+// (reinitialize_2nd_order_with_mask, src/my_p4est_level_set.h:487-525) the nodes where mask == 0 are
+// left out of the update lists and copy their value into phi_np1 and phi_np2 (:377-400, :439-461).
 template <int D>
-void reinitialize(const Ctx& cx, double* phi, int order_space, int order_pseudotime, double hi, double lo, int iters, int nthreads) {
+void reinitialize(const Ctx& cx, double* phi, int order_space, int order_pseudotime, double hi, double lo, int iters, int nthreads,
+                  const double* mask = nullptr) {
   const int64_t N = cx.N;
   std::vector<double> phi_np1(N), phi_np2(order_pseudotime > 1 ? N : 0), phi_0(phi, phi + N);
   std::vector<double> dd0, ddc;
@@ -724,10 +727,16 @@ void reinitialize(const Ctx& cx, double* phi, int order_space, int order_pseudot
     if (order_space > 1) compute_derivatives<D>(cx, phi, ddc.data(), nthreads);
     reinitialize_one_iteration<D>(cx, phi_np1.data(), phi_0.data(), phi, hi, lo, order_space > 1 ? dd0.data() : nullptr,
                                   order_space > 1 ? ddc.data() : nullptr, nthreads);
+    if (mask)
+      for (int64_t n = 0; n < N; ++n)
+        if (mask[n] == 0) phi_np1[n] = phi[n];
     if (order_pseudotime > 1) {
       if (order_space > 1) compute_derivatives<D>(cx, phi_np1.data(), ddc.data(), nthreads);
       reinitialize_one_iteration<D>(cx, phi_np2.data(), phi_0.data(), phi_np1.data(), hi, lo, order_space > 1 ? dd0.data() : nullptr,
                                     order_space > 1 ? ddc.data() : nullptr, nthreads);
+      if (mask)
+        for (int64_t n = 0; n < N; ++n)
+          if (mask[n] == 0) phi_np2[n] = phi_np1[n];
       for (int64_t n = 0; n < N; ++n) phi[n] = .5 * (phi[n] + phi_np2[n]);
     } else {
       memcpy(phi, phi_np1.data(), N * sizeof(double));
@@ -1714,6 +1723,17 @@ int ora_compute_derivatives(void* h, const double* f, double* fdd, int nthreads)
     Ctx* cx = static_cast<Ctx*>(h);
     if (cx->dim == 2) compute_derivatives<2>(*cx, f, fdd, nthreads);
     else compute_derivatives<3>(*cx, f, fdd, nthreads);
+  });
+}
+
+int ora_reinitialize_masked(void* h, double* phi, const double* mask, int order_space, int order_pseudotime, double limit_high,
+                            double limit_low, int iters, int nthreads) {
+  return guard([&] {
+    if (order_space < 1 || order_space > 2 || order_pseudotime < 1 || order_pseudotime > 2)
+      throw std::invalid_argument("valid orders of accuracy are 1 and 2 only");
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (cx->dim == 2) reinitialize<2>(*cx, phi, order_space, order_pseudotime, limit_high, limit_low, iters, nthreads, mask);
+    else reinitialize<3>(*cx, phi, order_space, order_pseudotime, limit_high, limit_low, iters, nthreads, mask);
   });
 }
 

@@ -29,6 +29,7 @@ SIG = {
     "ora_grid_wall_mask": (_I, [_P, _P]),
     "ora_compute_derivatives": (_I, [_P, _DP, _DP, _I]),
     "ora_reinitialize": (_I, [_P, _DP, _I, _I, _D, _D, _I, _I]),
+    "ora_reinitialize_masked": (_I, [_P, _DP, _DP, _I, _I, _D, _D, _I, _I]),
     "ora_advect_in_normal_direction": (_I, [_P, _DP, _DP, _DP, _D, _DP, _I]),
     "ora_advect_cfl_dt": (_I, [_P, _DP, _DP]),
     "ora_interpolate": (_I, [_P, _I, _I, _DP, _DP, _I64, _DP, _DP, _I]),
@@ -140,6 +141,14 @@ class OracleGrid:
         """In place on a float64 numpy array."""
         assert phi.dtype == np.float64 and phi.flags.c_contiguous and phi.size == self.N
         _chk(load().ora_reinitialize(self._h, _dp(phi), order_space, order_pseudotime, limit_high, limit_low, iterations, nthreads))
+
+    def reinitialize_with_mask(self, phi, mask, order_space=2, order_pseudotime=2, limit_high=np.finfo(np.float64).max,
+                               limit_low=-np.finfo(np.float64).max, iterations=50, nthreads=1):
+        """In place; nodes where mask == 0 are not updated."""
+        assert phi.dtype == np.float64 and phi.flags.c_contiguous and phi.size == self.N
+        mask = np.ascontiguousarray(mask, np.float64)
+        _chk(load().ora_reinitialize_masked(self._h, _dp(phi), _dp(mask), order_space, order_pseudotime, limit_high, limit_low,
+                                            iterations, nthreads))
 
     def advect_in_normal_direction(self, vn, phi, dt, vn_np1=None, phi_dd=None, nthreads=1):
         _chk(load().ora_advect_in_normal_direction(self._h, _dp(vn), _dp(vn_np1), _dp(phi), dt, _dp(phi_dd), nthreads))
