@@ -15,6 +15,9 @@ LSG_OK, LSG_EINVAL, LSG_ENOMEM, LSG_EDEVICE, LSG_ETIMEOUT, LSG_ENAN, LSG_ESTATE 
 LSG_FP64, LSG_MIXED = 0, 1
 LSG_BUILD_ON_DEVICE = 1
 # int (*lsg_velocity_fn)(void* ctx, int64_t npts, const double* xyz, double* v)
+# int (*lsg_interface_values_fn)(void* ctx, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists, double* values)
+INTERFACE_VALUES_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double))
 VELOCITY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double))
 LSG_VELOCITY_VORTEX = 0
 
@@ -93,6 +96,7 @@ SIGNATURES = {
     "lsg_extend_over_interface_tvd_device": (_I, [_P, _P, _P, _I, _I, _D, _D, _P, _P]),
     "lsg_extend_from_interface_to_whole_domain_tvd": (_I, [_P, _DP, _DP, _DP, _I, _I, _DP, _D, _D, _DP, _I]),
     "lsg_extend_from_interface_to_whole_domain_tvd_device": (_I, [_P, _P, _P, _P, _I, _I, _P, _D, _D, _P, _I]),
+    "lsg_extend_from_interface_to_whole_domain_tvd_cf": (_I, [_P, _DP, _DP, _DP, _I, _P, _P, _DP]),
     "lsg_interpolate_nodes": (_I, [_P, _DP, _I64, _DP, _I, _DP, _I, _DP]),
     "lsg_interpolate_nodes_device": (_I, [_P, _P, _I64, _P, _I, _P, _I, _P]),
     "lsg_locate_points_device": (_I, [_P, _P, _I64, _P]),

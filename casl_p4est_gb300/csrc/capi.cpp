@@ -851,6 +851,31 @@ int lsg_extend_from_interface_to_whole_domain_tvd(lsg_level_set* ls, const doubl
   });
 }
 
+int lsg_extend_from_interface_to_whole_domain_tvd_cf(lsg_level_set* ls, const double* phi, const double* q_interface, double* q,
+                                                     int iterations, lsg_interface_values_fn cf, void* ctx, const double* grad_phi) {
+  return guard([&] {
+    need(phi != nullptr && q_interface != nullptr && q != nullptr && cf != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      const int D = ls->dim;
+      const size_t N = (size_t)L.N;
+      L.ws_f.ensure((3 + (grad_phi ? D : 0)) * N + 1);
+      double* dphi = L.ws_f.p;
+      double* dqi = dphi + N;
+      double* dq = dqi + N;
+      double* dg = grad_phi ? dq + N : nullptr;
+      auto up = [&](double* dst, const double* src, size_t cnt) {
+        if (cnt) cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      };
+      up(dphi, phi, N);
+      up(dqi, q_interface, N);
+      if (dg) up(dg, grad_phi, (size_t)D * N);
+      L.extend_from_interface(dphi, dqi, dq, 1, iterations, nullptr, 0.0, 1.0, dg, 0, cf, ctx);
+      if (N) cuda_check(cudaMemcpyAsync(q, dq, N * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H");
+      cuda_check(cudaStreamSynchronize(L.stream), "sync");
+    });
+  });
+}
+
 int lsg_interpolate_nodes(lsg_level_set* ls, const double* xyz, int64_t npts, const double* F, int nfields, const double* Fdd,
                           int method, double* out) {
   return guard([&] {

@@ -172,6 +172,9 @@ template <int D>
 void launch_efi_init64(const DTab64<D>& T, const DLoc<D>& L, int method, const double* xyz, const double* phi, const double* pdd,
                        const double* qi, const double* qidd, const double* mask, double dl, double band_zero_dl, double band_smooth_dl,
                        double* q, double* qi_nb, double* s_nb, uint8_t* cross, cudaStream_t s);
+// dst[i] = src[idx[i]] / dst[idx[i]] = src[i] for i < m
+void launch_gather_idx64(const double* src, const int64_t* idx, int64_t m, double* dst, cudaStream_t s);
+void launch_scatter_idx64(const double* src, const int64_t* idx, int64_t m, double* dst, cudaStream_t s);
 template <int D>
 void launch_efi_stage64(const DTab64<D>& T, const double* phi, const double* grad, const double* q, const double* qdd, const double* qdd2,
                         const double* qi_nb, const double* s_nb, const uint8_t* cross, double zdt, bool average, double* out,

@@ -313,6 +313,8 @@ __device__ double smoothstep(int N, double x) {
 // has the other sign, the subcell distance to the interface (second-order location, at least EPS) and
 // qi interpolated there with method M (times 1 - smoothstep(1, (mask - band_zero)/band_smooth) when a
 // mask is given, the mask interpolated linearly); elsewhere qi at the node and the grid distance.
+// M < 0: the interface values come from the caller's cf function instead (filled in afterwards), q
+// starts at zero everywhere and the crossing entries of qi_nb are left at zero.
 template <int D, int M>
 __global__ void __launch_bounds__(TPB) k_efi_init64(DTab64<D> T, DLoc<D> L, const double* __restrict__ xyz, const double* __restrict__ phi,
                                                     const double* __restrict__ pdd, const double* __restrict__ qi,
@@ -323,7 +325,10 @@ __global__ void __launch_bounds__(TPB) k_efi_init64(DTab64<D> T, DLoc<D> L, cons
   const int64_t N = T.N;
   if (n >= N) return;
   const double p0 = phi[n];
-  q[n] = (mask ? max2(mask[n], fabs(p0)) : fabs(p0)) < 1.5 * dl ? qi[n] : 0;
+  if (M < 0)
+    q[n] = 0.0;
+  else
+    q[n] = (mask ? max2(mask[n], fabs(p0)) : fabs(p0)) < 1.5 * dl ? qi[n] : 0;
   double Dp[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) Dp[a] = pdd[(int64_t)a * N + n];
@@ -335,16 +340,18 @@ __global__ void __launch_bounds__(TPB) k_efi_init64(DTab64<D> T, DLoc<D> L, cons
     if (p0 * pn < 0.0) {
       double dist = st64::interface_location_2nd(0, dd, p0, pn, Dp[a], st64::lin64<D>(T, dir, n, pdd + (int64_t)a * N));
       dist = max2(dist, EPS);
-      double x[3] = {0, 0, 0};
+      double v = 0.0;
+      if constexpr (M >= 0) {
+        double x[3] = {0, 0, 0};
 #pragma unroll
-      for (int b = 0; b < D; ++b) x[b] = xyz[n * D + b];
-      x[a] = (dir & 1) ? x[a] + dist : x[a] - dist;
-      double v;
-      interpolate_at<D, M>(L, x, 1, qi, qidd, 1, 0, &v);
-      if (mask) {
-        double m;
-        interpolate_at<D, 0>(L, x, 1, mask, nullptr, 1, 0, &m);
-        v *= 1. - smoothstep(1, (m - band_zero) / band_smooth);
+        for (int b = 0; b < D; ++b) x[b] = xyz[n * D + b];
+        x[a] = (dir & 1) ? x[a] + dist : x[a] - dist;
+        interpolate_at<D, M>(L, x, 1, qi, qidd, 1, 0, &v);
+        if (mask) {
+          double m;
+          interpolate_at<D, 0>(L, x, 1, mask, nullptr, 1, 0, &m);
+          v *= 1. - smoothstep(1, (m - band_zero) / band_smooth);
+        }
       }
       qi_nb[(int64_t)dir * N + n] = v;
       s_nb[(int64_t)dir * N + n] = dist;
@@ -357,7 +364,25 @@ __global__ void __launch_bounds__(TPB) k_efi_init64(DTab64<D> T, DLoc<D> L, cons
   cross[n] = bits;
 }
 
+__global__ void __launch_bounds__(TPB) k_gather_idx64(const double* __restrict__ src, const int64_t* __restrict__ idx, int64_t m,
+                                                      double* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[i] = src[idx[i]];
+}
+__global__ void __launch_bounds__(TPB) k_scatter_idx64(const double* __restrict__ src, const int64_t* __restrict__ idx, int64_t m,
+                                                       double* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[idx[i]] = src[i];
+}
+
 }  // namespace
+
+void launch_gather_idx64(const double* src, const int64_t* idx, int64_t m, double* dst, cudaStream_t s) {
+  if (m) k_gather_idx64<<<nblocks(m), TPB, 0, s>>>(src, idx, m, dst);
+}
+void launch_scatter_idx64(const double* src, const int64_t* idx, int64_t m, double* dst, cudaStream_t s) {
+  if (m) k_scatter_idx64<<<nblocks(m), TPB, 0, s>>>(src, idx, m, dst);
+}
 
 template <int D>
 void launch_efi_init64(const DTab64<D>& T, const DLoc<D>& L, int method, const double* xyz, const double* phi, const double* pdd,
@@ -367,6 +392,7 @@ void launch_efi_init64(const DTab64<D>& T, const DLoc<D>& L, int method, const d
   const int64_t g = nblocks(T.N);
 #define LSG_EFI(M) k_efi_init64<D, M><<<g, TPB, 0, s>>>(T, L, xyz, phi, pdd, qi, qidd, mask, dl, band_zero, band_smooth, q, qi_nb, s_nb, cross)
   switch (method) {
+    case -1: LSG_EFI(-1); break;
     case 0: LSG_EFI(0); break;
     case 1: LSG_EFI(1); break;
     case 2: LSG_EFI(2); break;

@@ -846,8 +846,11 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
 
 template <int D>
 void LevelSet<D>::extend_from_interface(const double* phi, const double* qi, double* q, int nf, int iterations, const double* mask,
-                                        double band_zero, double band_smooth, const double* grad_phi, int method) {
+                                        double band_zero, double band_smooth, const double* grad_phi, int method, InterfaceValuesFn cf,
+                                        void* cf_ctx) {
   if (nf < 1) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: at least one field");
+  if (cf && mask) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: no mask and cf simultaneously");
+  if (cf && nf > 1) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: cf needs a block size of 1");
   if (mask && nf > 1) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: a mask needs a block size of 1");
   if (method < 0 || method > 4) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: unknown interpolation method");
   if (iterations < 0) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: negative number of iterations");
@@ -890,8 +893,39 @@ void LevelSet<D>::extend_from_interface(const double* phi, const double* qi, dou
     const double* qik = qi + (size_t)k * n;
     double* qk = q + (size_t)k * n;
     LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qik, qidd, stream));
-    LSG_LAUNCH(K_INTERP, launch_efi_init64<D>(T64, TL, method, node_xyz_dev.p, phi, pdd, qik, qidd, mask, dl, band_zero * dl,
+    LSG_LAUNCH(K_INTERP, launch_efi_init64<D>(T64, TL, cf ? -1 : method, node_xyz_dev.p, phi, pdd, qik, qidd, mask, dl, band_zero * dl,
                                               band_smooth * dl, qk, qi_nb, s_nb, efi_cross.p, stream));
+    if (cf) {
+      // the crossing (node, direction) pairs in node order, their distances to the host, the caller's
+      // values back into qi_nb
+      std::vector<uint8_t> cross(n);
+      if (n) cuda_check(cudaMemcpyAsync(cross.data(), efi_cross.p, n, cudaMemcpyDeviceToHost, stream), "D2H");
+      cuda_check(cudaStreamSynchronize(stream), "interface crossings");
+      std::vector<int64_t> idx;
+      std::vector<int32_t> nodes, dirs;
+      for (size_t m = 0; m < n; ++m)
+        for (int dir = 0; dir < 2 * D; ++dir)
+          if ((cross[m] >> dir) & 1) {
+            idx.push_back((int64_t)dir * N + (int64_t)m);
+            nodes.push_back((int32_t)m);
+            dirs.push_back(dir);
+          }
+      const int64_t cnt = (int64_t)idx.size();
+      std::vector<double> dist((size_t)cnt), val((size_t)cnt);
+      efi_idx.ensure((size_t)cnt + 1);
+      efi_val.ensure((size_t)cnt + 1);
+      if (cnt) {
+        cuda_check(cudaMemcpyAsync(efi_idx.p, idx.data(), (size_t)cnt * sizeof(int64_t), cudaMemcpyHostToDevice, stream), "H2D");
+        LSG_LAUNCH(K_INTERP, launch_gather_idx64(s_nb, efi_idx.p, cnt, efi_val.p, stream));
+        cuda_check(cudaMemcpyAsync(dist.data(), efi_val.p, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+        cuda_check(cudaStreamSynchronize(stream), "interface distances");
+        if (cf(cf_ctx, cnt, nodes.data(), dirs.data(), dist.data(), val.data()) != 0)
+          throw std::runtime_error("extend_from_interface_to_whole_domain_TVD: the cf callback failed");
+        cuda_check(cudaMemcpyAsync(efi_val.p, val.data(), (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice, stream), "H2D");
+        LSG_LAUNCH(K_INTERP, launch_scatter_idx64(efi_val.p, efi_idx.p, cnt, qi_nb, stream));
+        cuda_check(cudaStreamSynchronize(stream), "interface values");  // the host vectors go out of scope
+      }
+    }
     for (int it = 0; it < iterations; ++it) {
       derivatives(qk);
       LSG_LAUNCH(K_ADVECT64, launch_efi_stage64<D>(T64, phi, grad, qk, qdd, qdd2, qi_nb, s_nb, efi_cross.p, zdt, false, q1, stream));

@@ -84,6 +84,8 @@ struct LevelSet {
   // extension from the interface: node coordinates (N x D, built on first use), work vectors, crossing bits
   DevBuf<double> node_xyz_dev, efi_buf;
   DevBuf<uint8_t> efi_cross;
+  DevBuf<int64_t> efi_idx;
+  DevBuf<double> efi_val;
   // first-derivative correction records (built on first use)
   bool grad_ready = false;
   DevBuf<int32_t> g_idx;
@@ -159,8 +161,14 @@ struct LevelSet {
   // grad_phi) (src/my_p4est_level_set.cpp:3181-3767) for nf fields (nf x N; the reference's blocksize):
   // q (device, nf x N, not overlapping qi) receives qi's interface values extended along the normals.
   // mask (only with nf == 1) and grad_phi (D x N) may be null; method = interpolation_on_interface.
+  // cf (the reference's cf argument, batched): interface values given by the caller for the crossing
+  // (node, direction, distance) triples, in node order; with it q starts at zero and qi only supplies the
+  // values of the other directions; no mask and one field only, as in the reference.
+  using InterfaceValuesFn = int (*)(void* ctx, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists,
+                                    double* values);
   void extend_from_interface(const double* phi, const double* qi, double* q, int nf, int iterations, const double* mask,
-                             double band_zero, double band_smooth, const double* grad_phi, int method);
+                             double band_zero, double band_smooth, const double* grad_phi, int method, InterfaceValuesFn cf = nullptr,
+                             void* cf_ctx = nullptr);
 
   // my_p4est_interpolation_nodes_t: nf fields (nf x N) interpolated at np points (D doubles each)
   // with `method` (interpolation_method); Fdd (nf x D x N) may be null and is then computed with

@@ -243,11 +243,43 @@ class my_p4est_level_set_t:
         self.interpolation_on_interface = int(method)
 
     def extend_from_interface_to_whole_domain_TVD(self, phi, q_interface, q=None, iterations=20, mask=None, band_zero=2.0,
-                                                  band_smooth=10.0, grad_phi_in=None):
+                                                  band_smooth=10.0, cf=None, grad_phi_in=None):
         """q = the interface values of q_interface extended in the normal direction on both sides (FP64).
 
         q_interface: (N,) or (nfields, N) (the reference's blocksize, components as blocks); q: output of the
-        same shape (allocated and returned when None; must not overlap q_interface); grad_phi_in: (dim, N)."""
+        same shape (allocated and returned when None; must not overlap q_interface); grad_phi_in: (dim, N).
+        cf: the interface values given by the caller instead of interpolated, as a vectorised function
+        cf(nodes, dirs, dists) -> values over the crossing grid lines (host arrays, one field, no mask)."""
+        if cf is not None:
+            if mask is not None:
+                raise ValueError("No mask and cf simultaneously at the moment")
+            n = self.num_nodes
+            phi_h = _host_f64(np.ascontiguousarray(phi, np.float64), n, "phi")
+            qi = _host_f64(np.ascontiguousarray(q_interface, np.float64).reshape(-1), n, "q_interface")
+            out = np.empty(n, np.float64) if q is None else q
+            _host_f64(out, n, "q")
+            g = None if grad_phi_in is None else np.ascontiguousarray(grad_phi_in, np.float64)
+            failure = []
+
+            def tramp(ctx, count, nodes, dirs, dists, values):
+                try:
+                    nd = np.ctypeslib.as_array(nodes, shape=(count,)).copy()
+                    dr = np.ctypeslib.as_array(dirs, shape=(count,)).copy()
+                    ds = np.ctypeslib.as_array(dists, shape=(count,)).copy()
+                    np.ctypeslib.as_array(values, shape=(count,))[:] = np.asarray(cf(nd, dr, ds), np.float64).reshape(count)
+                    return 0
+                except Exception as e:
+                    failure.append(e)
+                    return 1
+
+            cb = L.INTERFACE_VALUES_FN(tramp)
+            code = L.load().lsg_extend_from_interface_to_whole_domain_tvd_cf(self._h, L.dptr(phi_h), L.dptr(qi), L.dptr(out),
+                                                                             int(iterations), C.cast(cb, C.c_void_p), None,
+                                                                             L.dptr(g) if g is not None else None)
+            if failure:
+                raise failure[0]
+            L.check(code)
+            return out
         if _is_device(phi):
             if q is None:
                 q = q_interface.new_empty(q_interface.shape)

@@ -258,6 +258,16 @@ int lsg_extend_from_interface_to_whole_domain_tvd(lsg_level_set* ls, const doubl
 int lsg_extend_from_interface_to_whole_domain_tvd_device(lsg_level_set* ls, const double* phi_dev, const double* q_interface_dev,
                                                          double* q_dev, int nfields, int iterations, const double* mask_dev,
                                                          double band_zero, double band_smooth, const double* grad_phi_dev, int method);
+/* The cf form of extend_from_interface_to_whole_domain_TVD (the reference's
+ * double (*cf)(p4est_locidx_t node, int dir, double dist), src/my_p4est_level_set.cpp:3388-3590): the
+ * caller gives the interface value of every grid line that crosses the interface, batched: count
+ * (node, direction, distance) triples in the reference's call order (node by node, directions m00, p00,
+ * 0m0, 0p0[, 00m, 00p]); return 0 on success. q starts at zero; q_interface supplies the values of the
+ * other directions. One field, host arrays. */
+typedef int (*lsg_interface_values_fn)(void* ctx, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists,
+                                       double* values);
+int lsg_extend_from_interface_to_whole_domain_tvd_cf(lsg_level_set* ls, const double* phi, const double* q_interface, double* q,
+                                                     int iterations, lsg_interface_values_fn cf, void* ctx, const double* grad_phi);
 
 /* ---- node interpolation and the semi-Lagrangian step (FP64) --------------------------------- */
 

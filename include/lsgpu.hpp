@@ -217,13 +217,34 @@ class my_p4est_level_set_t {
   void set_interpolation_on_interface(interpolation_method value) { interpolation_on_interface_ = value; }
 
   // q_interface, q: blocksize values per node, interleaved as in the reference's block vectors; grad_phi_in:
-  // dim values per node, interleaved. The cf callback is not supported (std::invalid_argument).
+  // dim values per node, interleaved. cf (interface values by node, direction and distance) needs no mask
+  // and a block size of 1, as in the reference.
   void extend_from_interface_to_whole_domain_TVD(Vec phi, Vec q_interface, Vec q, int iterations = 20, Vec mask = nullptr,
                                                  double band_zero = 2, double band_smooth = 10,
                                                  double (*cf)(int32_t, int, double) = nullptr, Vec grad_phi_in = nullptr,
                                                  const unsigned int& blocksize = 1) const {
-    if (cf != nullptr) throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: the cf callback is not supported");
     const int D = ngbd_->dim();
+    if (cf != nullptr) {
+      if (mask != nullptr || blocksize != 1)
+        throw std::invalid_argument("extend_from_interface_to_whole_domain_TVD: cf needs no mask and a block size of 1");
+      lsg_interface_values_fn fn = [](void* c, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists,
+                                      double* values) -> int {
+        auto f = reinterpret_cast<double (*)(int32_t, int, double)>(c);
+        for (int64_t k = 0; k < count; ++k) values[k] = f(nodes[k], dirs[k], dists[k]);
+        return 0;
+      };
+      lsgpu::VecArray p(phi), qi(q_interface), qo(q), g(grad_phi_in);
+      const size_t N = (size_t)ngbd_->num_nodes();
+      std::vector<double> g_b;
+      if (grad_phi_in != nullptr) {
+        g_b.resize((size_t)D * N);
+        for (size_t n = 0; n < N; ++n)
+          for (int a = 0; a < D; ++a) g_b[a * N + n] = g.p[(size_t)D * n + a];
+      }
+      lsgpu::check(lsg_extend_from_interface_to_whole_domain_tvd_cf(ngbd_->device(), p.p, qi.p, qo.p, iterations, fn,
+                                                                    reinterpret_cast<void*>(cf), grad_phi_in ? g_b.data() : nullptr));
+      return;
+    }
     const size_t N = (size_t)ngbd_->num_nodes(), bs = blocksize;
     lsgpu::VecArray p(phi), qi(q_interface), qo(q), m(mask), g(grad_phi_in);
     std::vector<double> qi_b(bs * N), q_b(bs * N), g_b;

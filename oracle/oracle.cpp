@@ -1524,9 +1524,14 @@ void efi_one_iteration(const Ctx& cx, const double* phi, const double* grad, con
 // the interface (interpolation_on_interface, quadratic_non_oscillatory_continuous_v2 by default):
 // interface values along each grid line crossing the interface, q started from qi within 1.5 dl of the
 // interface, then `iterations` TVD-RK2 steps. grad_in (D x N) may be null (first derivatives of phi).
+// cf: the caller's interface values, asked one crossing at a time in the reference's order (node by
+// node, then direction), as (*cf)(n, dir, dist) is in src/my_p4est_level_set.cpp:3488-3585; q then
+// starts at zero.
+typedef int (*ora_values_fn)(void* ctx, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists, double* values);
 template <int D>
 void extend_from_interface(const Ctx& cx, const double* phi, const double* qi, double* q, int iterations, const double* mask,
-                           double band_zero, double band_smooth, const double* grad_in, int method, int nthreads) {
+                           double band_zero, double band_smooth, const double* grad_in, int method, int nthreads,
+                           ora_values_fn cf = nullptr, void* cf_ctx = nullptr) {
   const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
   const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
   const int64_t N = cx.N;
@@ -1544,7 +1549,7 @@ void extend_from_interface(const Ctx& cx, const double* phi, const double* qi, d
   }
   compute_derivatives<D>(cx, phi, pdd.data(), nthreads);
   for (int64_t n = 0; n < N; ++n)
-    q[n] = (mask ? MAX(mask[n], fabs(phi[n])) : fabs(phi[n])) < 1.5 * dl ? qi[n] : 0;
+    q[n] = cf ? 0 : ((mask ? MAX(mask[n], fabs(phi[n])) : fabs(phi[n])) < 1.5 * dl ? qi[n] : 0);
   // interface values and distances along the 2D directions
   std::vector<double> qi_nb((size_t)2 * D * N), s_nb((size_t)2 * D * N);
   std::vector<uint8_t> cross((size_t)N, 0);
@@ -1562,8 +1567,15 @@ void extend_from_interface(const Ctx& cx, const double* phi, const double* qi, d
       if (p_000 * p_nb[dir] < 0.0) {
         double dist = interface_Location_With_Second_Order_Derivative(0, qq.d[dir], p_000, p_nb[dir], paa[n], f_linear(qq, dir, paa));
         dist = MAX(dist, ORA_EPS);
-        for (int b = 0; b < D; ++b) pts[dir].push_back(b == a ? ((dir & 1) ? x[b] + dist : x[b] - dist) : x[b]);
-        who[dir].push_back((int32_t)n);
+        if (cf) {
+          const int32_t nn = (int32_t)n, dd_ = dir;
+          double v = 0;
+          if (cf(cf_ctx, 1, &nn, &dd_, &dist, &v) != 0) throw std::runtime_error("oracle: cf failed");
+          qi_nb[(size_t)dir * N + n] = v;
+        } else {
+          for (int b = 0; b < D; ++b) pts[dir].push_back(b == a ? ((dir & 1) ? x[b] + dist : x[b] - dist) : x[b]);
+          who[dir].push_back((int32_t)n);
+        }
         s_nb[(size_t)dir * N + n] = dist;
         cross[n] |= (uint8_t)(1u << dir);
       } else {
@@ -1888,6 +1900,16 @@ int ora_extend_from_interface(void* h, const double* phi, const double* qi, doub
     if (!cx->grid) throw std::runtime_error("extension needs a grid built from leaves");
     if (cx->dim == 2) extend_from_interface<2>(*cx, phi, qi, q, iterations, mask, band_zero, band_smooth, grad, method, nthreads);
     else extend_from_interface<3>(*cx, phi, qi, q, iterations, mask, band_zero, band_smooth, grad, method, nthreads);
+  });
+}
+
+int ora_extend_from_interface_cf(void* h, const double* phi, const double* qi, double* q, int iterations, ora_values_fn cf, void* ctx,
+                                 const double* grad, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("extension needs a grid built from leaves");
+    if (cx->dim == 2) extend_from_interface<2>(*cx, phi, qi, q, iterations, nullptr, 0.0, 1.0, grad, 4, nthreads, cf, ctx);
+    else extend_from_interface<3>(*cx, phi, qi, q, iterations, nullptr, 0.0, 1.0, grad, 4, nthreads, cf, ctx);
   });
 }
 

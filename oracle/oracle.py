@@ -43,6 +43,7 @@ SIG = {
     "ora_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP, _I]),
     "ora_extend_over_interface": (_I, [_P, _DP, _DP, _DP, _I, _I, _D, _D, _DP, _I]),
     "ora_extend_from_interface": (_I, [_P, _DP, _DP, _DP, _I, _DP, _D, _D, _DP, _I, _I]),
+    "ora_extend_from_interface_cf": (_I, [_P, _DP, _DP, _DP, _I, _P, _P, _DP, _I]),
     "ora_interface_location": (_D, [_D, _D, _D, _D]),
     "ora_interface_location_2nd": (_D, [_D, _D, _D, _D, _D, _D]),
 }
@@ -204,6 +205,25 @@ class OracleGrid:
         g = None if grad_phi is None else np.ascontiguousarray(grad_phi, np.float64)
         _chk(load().ora_extend_from_interface(self._h, _dp(phi), _dp(qi), _dp(q), int(iterations), _dp(msk), float(band_zero),
                                               float(band_smooth), _dp(g), int(method), nthreads))
+        return q
+
+    def extend_from_interface_to_whole_domain_tvd_cf(self, phi, qi, cf, iterations=20, grad_phi=None, nthreads=1):
+        """cf(node, dir, dist) -> interface value, called once per crossing in the reference's order."""
+        phi = np.ascontiguousarray(phi, np.float64)
+        qi = np.ascontiguousarray(qi, np.float64)
+        q = np.empty(self.N, np.float64)
+        g = None if grad_phi is None else np.ascontiguousarray(grad_phi, np.float64)
+        proto = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                            C.POINTER(C.c_double))
+
+        def tramp(ctx, count, nodes, dirs, dists, values):
+            for k in range(count):
+                values[k] = float(cf(int(nodes[k]), int(dirs[k]), float(dists[k])))
+            return 0
+
+        cb = proto(tramp)
+        _chk(load().ora_extend_from_interface_cf(self._h, _dp(phi), _dp(qi), _dp(q), int(iterations), C.cast(cb, C.c_void_p), None,
+                                                 _dp(g), nthreads))
         return q
 
     # ---- node interpolation and the semi-Lagrangian step ------------------------------------

@@ -9,6 +9,12 @@
 
 #include "lsgpu.hpp"
 
+static double iface_value(int32_t n, int dir, double dist) { return 1.0 + 2.0 * dist + 0.01 * dir + 1e-4 * n; }
+static int iface_values(void*, int64_t count, const int32_t* nodes, const int32_t* dirs, const double* dists, double* values) {
+  for (int64_t k = 0; k < count; ++k) values[k] = iface_value(nodes[k], dirs[k], dists[k]);
+  return 0;
+}
+
 static int fail(const char* what) {
   fprintf(stderr, "facade mismatch: %s\n", what);
   return 1;
@@ -138,6 +144,15 @@ int main() {
   lsgpu::check(lsg_interpolate_nodes(raw, xd.data(), N, phi.values.data(), 1, nullptr, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2,
                                      np1_cf_ref.data()));
   if (memcmp(np1_cf.data(), np1_cf_ref.data(), N * sizeof(double)) != 0) return fail("advect_from_n_to_np1 (CF)");
+
+  // the cf form: interface values from a function of (node, direction, distance)
+  lsgpu_vec qi1{std::vector<double>((size_t)N)}, qcf{std::vector<double>((size_t)N)};
+  for (int64_t i = 0; i < N; ++i) qi1.values[i] = xyz[2 * i] - xyz[2 * i + 1];
+  std::vector<double> qcf_ref((size_t)N);
+  ls.extend_from_interface_to_whole_domain_TVD(&phi, &qi1, &qcf, 5, nullptr, 2, 10, iface_value, nullptr, 1);
+  lsgpu::check(lsg_extend_from_interface_to_whole_domain_tvd_cf(raw, phi.values.data(), qi1.values.data(), qcf_ref.data(), 5, iface_values,
+                                                                nullptr, nullptr));
+  if (memcmp(qcf.values.data(), qcf_ref.data(), N * sizeof(double)) != 0) return fail("extend_from_interface_to_whole_domain_TVD (cf)");
 
   // errors come back as exceptions
   try {

@@ -212,3 +212,40 @@ def test_gpu_whole_domain_extension_device_tensors():
     assert np.array_equal(tq.cpu().numpy(), host)
     with pytest.raises(G.LsgInvalidArgument):  # output over the input
         ls.extend_from_interface_to_whole_domain_TVD(torch.from_numpy(phi).cuda(), tqi, q=tqi, iterations=1)
+
+
+def iface_value(n, d, dist):
+    """interface values of the cf form: any function of (node, direction, distance); exact arithmetic"""
+    return 1.0 + 2.0 * dist + 0.01 * d + 1e-4 * n
+
+
+def test_oracle_whole_domain_extension_cf():
+    """cf form: q starts at zero and takes the caller's values at the crossings; a constant cf
+    extends to that constant near the interface."""
+    f = sphere_grid(2, 6)
+    og = O.OracleGrid.from_forest(f)
+    x = f.node_xyz()
+    phi = np.sqrt(np.sum(x ** 2, axis=1)) - 0.47  # no node on the interface (those keep q = 0)
+    calls = []
+    q = og.extend_from_interface_to_whole_domain_tvd_cf(phi, np.zeros(len(phi)), lambda n, d, s: (calls.append((n, d)), 0.25)[1],
+                                                        iterations=60)
+    assert calls == sorted(calls) and len(calls) > 0  # node by node, directions in order
+    near = np.abs(phi) < 0.06  # two cells: converged to round-off from zero in 60 steps
+    assert np.max(np.abs(q[near] - 0.25)) < 1e-11
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["circle2d", "flower3d", "brick3d"])
+def test_gpu_whole_domain_extension_cf_bitwise(name):
+    f = GRIDS[name]()
+    og = O.OracleGrid.from_forest(f)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    x, phi, _ = case(f)
+    qi = field(x)
+    want = og.extend_from_interface_to_whole_domain_tvd_cf(phi, qi, iface_value, iterations=7)
+    got = ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=7, cf=iface_value)
+    assert np.array_equal(got, want)
+    with pytest.raises(ValueError):
+        ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=2, cf=iface_value, mask=phi)
+    with pytest.raises(ZeroDivisionError):
+        ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=2, cf=lambda n, d, s: 1 / 0)
