@@ -94,6 +94,8 @@ SIGNATURES = {
     "lsg_compute_normals_and_mean_curvature_device": (_I, [_P, _P, _P, _P]),
     "lsg_extend_over_interface_tvd": (_I, [_P, _DP, _DP, _I, _I, _D, _D, _DP, _DP]),
     "lsg_extend_over_interface_tvd_device": (_I, [_P, _P, _P, _I, _I, _D, _D, _P, _P]),
+    "lsg_extend_over_interface_tvd_ex": (_I, [_P, _DP, _DP, _I, _I, _D, _D, _DP, _DP, _I, _DP, _DP]),
+    "lsg_extend_over_interface_tvd_ex_device": (_I, [_P, _P, _P, _I, _I, _D, _D, _P, _P, _I, _P, _P]),
     "lsg_extend_from_interface_to_whole_domain_tvd": (_I, [_P, _DP, _DP, _DP, _I, _I, _DP, _D, _D, _DP, _I]),
     "lsg_extend_from_interface_to_whole_domain_tvd_device": (_I, [_P, _P, _P, _P, _I, _I, _P, _D, _D, _P, _I]),
     "lsg_extend_from_interface_to_whole_domain_tvd_cf": (_I, [_P, _DP, _DP, _DP, _I, _P, _P, _DP]),

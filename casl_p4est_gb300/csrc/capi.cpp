@@ -785,6 +785,59 @@ int lsg_extend_over_interface_tvd_device(lsg_level_set* ls, const double* phi, d
   });
 }
 
+int lsg_extend_over_interface_tvd_ex_device(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                            double band_extend, const double* normals, const double* mask, int use_nonzero_guess,
+                                            double* q_n, double* q_nn) {
+  return guard([&] {
+    need(phi != nullptr && q != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      L.extend_over_interface(phi, q, iterations, order, band_use, band_extend, normals, mask, use_nonzero_guess != 0, q_n, q_nn);
+    });
+  });
+}
+
+int lsg_extend_over_interface_tvd_ex(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                     double band_extend, const double* normals, const double* mask, int use_nonzero_guess, double* q_n,
+                                     double* q_nn) {
+  return guard([&] {
+    need(phi != nullptr && q != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) {
+      const int D = ls->dim;
+      const size_t N = (size_t)L.N;
+      L.ws_f.ensure((2 + (normals ? D : 0) + (mask ? 1 : 0) + (q_n ? 1 : 0) + (q_nn ? 1 : 0)) * N + 1);
+      double* cur = L.ws_f.p;
+      auto take = [&](size_t cnt) {
+        double* p = cur;
+        cur += cnt;
+        return p;
+      };
+      auto up = [&](double* dst, const double* src, size_t cnt) {
+        if (cnt) cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, L.stream), "H2D");
+      };
+      auto down = [&](double* dst, const double* src, size_t cnt) {
+        if (cnt) cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyDeviceToHost, L.stream), "D2H");
+      };
+      double* dphi = take(N);
+      double* dq = take(N);
+      double* dn = normals ? take((size_t)D * N) : nullptr;
+      double* dm = mask ? take(N) : nullptr;
+      double* dqn = q_n ? take(N) : nullptr;
+      double* dqnn = q_nn ? take(N) : nullptr;
+      up(dphi, phi, N);
+      up(dq, q, N);
+      if (dn) up(dn, normals, (size_t)D * N);
+      if (dm) up(dm, mask, N);
+      if (dqn) up(dqn, q_n, N);
+      if (dqnn) up(dqnn, q_nn, N);
+      L.extend_over_interface(dphi, dq, iterations, order, band_use, band_extend, dn, dm, use_nonzero_guess != 0, dqn, dqnn);
+      down(q, dq, N);
+      if (dqn) down(q_n, dqn, N);
+      if (dqnn) down(q_nn, dqnn, N);
+      cuda_check(cudaStreamSynchronize(L.stream), "sync");
+    });
+  });
+}
+
 int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
                                   double band_extend, const double* normals, const double* mask) {
   return guard([&] {

@@ -135,13 +135,18 @@ void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const d
 // edge-diagonal neighbours cnb; ext_march: one upwind marching step of v into tmp on the nodes with
 // b > 0 and phi < band_extend (minus src when given); ext_q: one marching step of q with the order-2
 // minmod correction from qdd.
+// guess for q_n / q_nn where no value can be computed (bits): GRADIENT, the normal derivative of q / q_n
+// (use_nonzero_guess); else KEEP, the value already in the array (the caller's q_n / q_nn); else zero.
+// Where the reference leaves q_nn as it was, KEEP keeps it and no KEEP writes zero.
+enum { EXT_GUESS_ZERO = 0, EXT_GUESS_KEEP = 1, EXT_GUESS_GRADIENT = 2 };
 template <int D>
 void launch_ext_init1(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
-                      const double* nrm, double band_use, double* qx, double* qn, int8_t* bqn, cudaStream_t s);
+                      const double* nrm, double band_use, int guess, double* qx, double* qn, int8_t* bqn, cudaStream_t s);
+// EXT_GUESS_GRADIENT needs qn and its second derivatives qndd
 template <int D>
 void launch_ext_init2(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
                       const double* nrm, const double* nrmdd, const double* qx, const double* qxdd, const int8_t* bqn, const int32_t* cnb,
-                      double band_use, double* qnn, int8_t* bqnn, cudaStream_t s);
+                      double band_use, int guess, const double* qn, const double* qndd, double* qnn, int8_t* bqnn, cudaStream_t s);
 template <int D>
 void launch_ext_march(const DTab64<D>& T, const double* v, double* tmp, const int8_t* b, const double* phi, const double* nrm,
                       const double* src, double band_extend, cudaStream_t s);

@@ -381,11 +381,28 @@ __device__ __forceinline__ double ext_dt(const DTab64<D>& T, int64_t n) {
 template <int D>
 __global__ void __launch_bounds__(TPB) k_ext_init1(DTab64<D> T, DGrad G, const double* __restrict__ phi, const double* __restrict__ mask,
                                                    const double* __restrict__ q, const double* __restrict__ qdd, const double* __restrict__ nrm,
-                                                   double band_use, double* __restrict__ qx, double* __restrict__ qn, int8_t* __restrict__ bqn) {
+                                                   double band_use, int guess, double* __restrict__ qx, double* __restrict__ qn,
+                                                   int8_t* __restrict__ bqn) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= N) return;
-  if (phi[n] > band_use && stencil_negative64<D>(T, n, mask)) {
+  if (phi[n] > band_use && !stencil_negative64<D>(T, n, mask)) {
+    // no value can be computed here: the caller's guess (use_nonzero_guess: n . grad q; a given q_n: its
+    // value), else zero
+    bqn[n] = 1;
+    if (guess & EXT_GUESS_GRADIENT) {
+      const int32_t r = G.gidx[n];
+      double s = nrm[n] * grad_comp64<D>(T, G, n, q, qdd, 0, r) + nrm[N + n] * grad_comp64<D>(T, G, n, q, qdd, 1, r);
+      if (D == 3) s = s + nrm[2 * N + n] * grad_comp64<D>(T, G, n, q, qdd, D == 3 ? 2 : 0, r);
+      qn[n] = s;
+    } else if (!(guess & EXT_GUESS_KEEP)) {
+      qn[n] = 0;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) qx[(int64_t)a * N + n] = 0;
+    return;
+  }
+  if (phi[n] > band_use) {
     const int32_t r = G.gidx[n];
     double g[3];
 #pragma unroll
@@ -398,7 +415,7 @@ __global__ void __launch_bounds__(TPB) k_ext_init1(DTab64<D> T, DGrad G, const d
     qn[n] = s;
     bqn[n] = -1;
   } else {
-    bqn[n] = phi[n] > band_use ? 1 : -1;
+    bqn[n] = -1;
     qn[n] = 0;
 #pragma unroll
     for (int a = 0; a < D; ++a) qx[(int64_t)a * N + n] = 0;
@@ -410,8 +427,8 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
                                                    const double* __restrict__ q, const double* __restrict__ qdd, const double* __restrict__ nrm,
                                                    const double* __restrict__ nrmdd, const double* __restrict__ qx,
                                                    const double* __restrict__ qxdd, const int8_t* __restrict__ bqn,
-                                                   const int32_t* __restrict__ cnb, double band_use, double* __restrict__ qnn,
-                                                   int8_t* __restrict__ bqnn) {
+                                                   const int32_t* __restrict__ cnb, double band_use, int guess, const double* __restrict__ qn,
+                                                   const double* __restrict__ qndd, double* __restrict__ qnn, int8_t* __restrict__ bqnn) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= N) return;
@@ -420,12 +437,19 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
     qnn[n] = 0;
     return;
   }
+  const int32_t r = G.gidx[n];
   if (!stencil_negative64<D>(T, n, mask)) {
     bqnn[n] = 1;
-    qnn[n] = 0;
+    if (guess & EXT_GUESS_GRADIENT) {
+      const int64_t N_ = N;
+      double s = nrm[n] * grad_comp64<D>(T, G, n, qn, qndd, 0, r) + nrm[N_ + n] * grad_comp64<D>(T, G, n, qn, qndd, 1, r);
+      if (D == 3) s = s + nrm[2 * N_ + n] * grad_comp64<D>(T, G, n, qn, qndd, D == 3 ? 2 : 0, r);
+      qnn[n] = s;
+    } else if (!(guess & EXT_GUESS_KEEP)) {
+      qnn[n] = 0;
+    }
     return;
   }
-  const int32_t r = G.gidx[n];
   const int64_t DN = (int64_t)D * N;
   double Qxy = 0, Qyz = 0, Qzx = 0;
   bool ok = false;
@@ -464,7 +488,7 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
   }
   if (!ok) {
     bqnn[n] = 1;
-    qnn[n] = 0;
+    if (!(guess & EXT_GUESS_KEEP)) qnn[n] = 0;  // left as it was: zero, or the caller's q_nn
     return;
   }
   bqnn[n] = -1;
@@ -704,14 +728,15 @@ void launch_kappa64(const DTab64<D>& T, const DGrad& G, const double* g, const d
 
 template <int D>
 void launch_ext_init1(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
-                      const double* nrm, double band_use, double* qx, double* qn, int8_t* bqn, cudaStream_t s) {
-  if (T.N) k_ext_init1<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, band_use, qx, qn, bqn);
+                      const double* nrm, double band_use, int guess, double* qx, double* qn, int8_t* bqn, cudaStream_t s) {
+  if (T.N) k_ext_init1<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, band_use, guess, qx, qn, bqn);
 }
 template <int D>
 void launch_ext_init2(const DTab64<D>& T, const DGrad& G, const double* phi, const double* mask, const double* q, const double* qdd,
                       const double* nrm, const double* nrmdd, const double* qx, const double* qxdd, const int8_t* bqn, const int32_t* cnb,
-                      double band_use, double* qnn, int8_t* bqnn, cudaStream_t s) {
-  if (T.N) k_ext_init2<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, bqn, cnb, band_use, qnn, bqnn);
+                      double band_use, int guess, const double* qn, const double* qndd, double* qnn, int8_t* bqnn, cudaStream_t s) {
+  if (T.N)
+    k_ext_init2<D><<<nblocks(T.N), TPB, 0, s>>>(T, G, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, bqn, cnb, band_use, guess, qn, qndd, qnn, bqnn);
 }
 template <int D>
 void launch_ext_march(const DTab64<D>& T, const double* v, double* tmp, const int8_t* b, const double* phi, const double* nrm,
@@ -834,10 +859,10 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
   template void launch_kappa64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,    \
                                   double*, cudaStream_t);                                                                     \
   template void launch_ext_init1<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,  \
-                                    const double*, double, double*, double*, int8_t*, cudaStream_t);                          \
+                                    const double*, double, int, double*, double*, int8_t*, cudaStream_t);                     \
   template void launch_ext_init2<D>(const DTab64<D>&, const DGrad&, const double*, const double*, const double*, const double*,  \
                                     const double*, const double*, const double*, const double*, const int8_t*, const int32_t*, \
-                                    double, double*, int8_t*, cudaStream_t);                                                  \
+                                    double, int, const double*, const double*, double*, int8_t*, cudaStream_t);              \
   template void launch_ext_march<D>(const DTab64<D>&, const double*, double*, const int8_t*, const double*, const double*,     \
                                     const double*, double, cudaStream_t);                                                     \
   template void launch_ext_q<D>(const DTab64<D>&, const double*, double*, const double*, const double*, const double*,         \

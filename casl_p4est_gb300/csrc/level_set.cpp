@@ -776,15 +776,15 @@ void LevelSet<D>::normals_and_mean_curvature(const double* phi, double* nrm, dou
 
 template <int D>
 void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterations, int order, double band_use, double band_extend,
-                                        const double* normals, const double* mask) {
+                                        const double* normals, const double* mask, bool nonzero_guess, double* q_n, double* q_nn) {
   if (order < 0 || order > 2) throw std::invalid_argument("extend_Over_Interface_TVD: order must be 0, 1 or 2.");
   if (iterations < 0) throw std::invalid_argument("extend_Over_Interface_TVD: negative number of iterations");
   build_gradient();
   if (band_use > 0) band_use = -band_use;
   if (!mask) mask = phi;
   const size_t n = (size_t)N;
-  // layout of ext_buf: normals D | qx D | qn | qnn | tmp | qdd D | nrmdd D*D | qxdd D*D
-  ext_buf.ensure((size_t)(2 * D + 3 + D + 2 * D * D) * n + 1);
+  // layout of ext_buf: normals D | qx D | qn | qnn | tmp | qdd D | nrmdd D*D | qxdd D*D | qndd D
+  ext_buf.ensure((size_t)(2 * D + 3 + D + 2 * D * D + D) * n + 1);
   double* nrm_own = ext_buf.p;
   double* qx = nrm_own + (size_t)D * n;
   double* qn = qx + (size_t)D * n;
@@ -793,6 +793,7 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
   double* qdd = tmp + n;
   double* nrmdd = qdd + (size_t)D * n;
   double* qxdd = nrmdd + (size_t)D * D * n;
+  double* qndd = qxdd + (size_t)D * D * n;
   ext_b1.ensure(n + 1);
   ext_b2.ensure(n + 1);
   const double* nrm = normals;
@@ -802,7 +803,10 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
   }
   if (order >= 1) {
     LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, q, qdd, stream));
-    LSG_LAUNCH(K_DD64, launch_ext_init1<D>(T64, TG, phi, mask, q, qdd, nrm, band_use, qx, qn, ext_b1.p, stream));
+    // a caller's q_n starts the marching where nothing is computed (the reference works in it)
+    if (q_n) cuda_check(cudaMemcpyAsync(qn, q_n, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy q_n");
+    const int guess1 = (nonzero_guess ? EXT_GUESS_GRADIENT : 0) | (q_n ? EXT_GUESS_KEEP : 0);
+    LSG_LAUNCH(K_DD64, launch_ext_init1<D>(T64, TG, phi, mask, q, qdd, nrm, band_use, guess1, qx, qn, ext_b1.p, stream));
   }
   if (order == 2) {
     if (!cnb.p) {
@@ -814,8 +818,11 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
       LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, nrm + (size_t)a * n, nrmdd + (size_t)a * D * n, stream));
       LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qx + (size_t)a * n, qxdd + (size_t)a * D * n, stream));
     }
-    LSG_LAUNCH(K_DD64, launch_ext_init2<D>(T64, TG, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, ext_b1.p, cnb.p, band_use, qnn, ext_b2.p,
-                                           stream));
+    if (q_nn) cuda_check(cudaMemcpyAsync(qnn, q_nn, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy q_nn");
+    if (nonzero_guess) LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, qn, qndd, stream));
+    const int guess2 = (nonzero_guess ? EXT_GUESS_GRADIENT : 0) | (q_nn ? EXT_GUESS_KEEP : 0);
+    LSG_LAUNCH(K_DD64, launch_ext_init2<D>(T64, TG, phi, mask, q, qdd, nrm, nrmdd, qx, qxdd, ext_b1.p, cnb.p, band_use, guess2, qn, qndd,
+                                           qnn, ext_b2.p, stream));
   }
   // marching: ping-pong between a field and tmp; nodes not marched keep their value in both
   auto march = [&](double* v, const int8_t* b, const double* src) {
@@ -841,6 +848,9 @@ void LevelSet<D>::extend_over_interface(const double* phi, double* q, int iterat
     }
     if (a != q) cuda_check(cudaMemcpyAsync(q, a, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   }
+  // the extended normal derivatives back to the caller
+  if (q_n && order >= 1) cuda_check(cudaMemcpyAsync(q_n, qn, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy q_n");
+  if (q_nn && order == 2) cuda_check(cudaMemcpyAsync(q_nn, qnn, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy q_nn");
   cuda_check(cudaGetLastError(), "extend_Over_Interface_TVD");
 }
 

@@ -154,8 +154,12 @@ struct LevelSet {
   // (src/my_p4est_level_set.cpp:969-1764) without boundary conditions or initial guesses, one-step
   // extrapolation: q (device, N) is extended from the region phi < 0 (or mask < 0) along the normals.
   // normals (D x N) and mask (N) may be null (computed from phi / taken as phi).
+  // nonzero_guess, q_n, q_nn (device, N each, nullable, in/out): use_nonzero_guess and the q_n / q_nn
+  // arguments of the reference; a given q_n / q_nn starts the marching where nothing is computed and
+  // receives the extended normal derivative.
   void extend_over_interface(const double* phi, double* q, int iterations, int order, double band_use, double band_extend,
-                             const double* normals, const double* mask);
+                             const double* normals, const double* mask, bool nonzero_guess = false, double* q_n = nullptr,
+                             double* q_nn = nullptr);
 
   // extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero, band_smooth, cf = NULL,
   // grad_phi) (src/my_p4est_level_set.cpp:3181-3767) for nf fields (nf x N; the reference's blocksize):

@@ -216,23 +216,33 @@ class my_p4est_level_set_t:
         return nrm, kappa
 
     def extend_Over_Interface_TVD(self, phi, q, iterations=20, order=2, band_use=-DBL_MAX, band_extend=DBL_MAX,
-                                  normal=None, mask=None):
-        """Extend q (updated in place) from phi < 0 (or mask < 0) along the normals (FP64). normal: (dim, N)."""
+                                  normal=None, mask=None, bc=None, use_nonzero_guess=False, q_n=None, q_nn=None):
+        """Extend q (updated in place) from phi < 0 (or mask < 0) along the normals (FP64). normal: (dim, N).
+        q_n / q_nn (optional, N each, in place): starting guesses where no normal derivative can be
+        computed, and on return the extended first / second normal derivatives. bc (boundary conditions of
+        the Poisson solvers) is not supported."""
         if order not in (0, 1, 2):
             raise ValueError("[CASL_ERROR]: my_p4est_level_set_t->extend_Over_Interface_TVD: order must be 0, 1 or 2.")
+        if bc is not None:
+            raise ValueError("extend_Over_Interface_TVD: boundary conditions are not supported")
         n = self.num_nodes
         if _is_device(phi):
             ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
-            L.check(L.load().lsg_extend_over_interface_tvd_device(self._h, ptr(phi), ptr(q), int(iterations), int(order),
-                                                                  float(band_use), float(band_extend), ptr(normal), ptr(mask)))
+            L.check(L.load().lsg_extend_over_interface_tvd_ex_device(self._h, ptr(phi), ptr(q), int(iterations), int(order),
+                                                                     float(band_use), float(band_extend), ptr(normal), ptr(mask),
+                                                                     int(bool(use_nonzero_guess)), ptr(q_n), ptr(q_nn)))
             return
         phi = _host_f64(np.ascontiguousarray(phi, np.float64), n, "phi")
         _host_f64(q, n, "q")
+        for v, name in ((q_n, "q_n"), (q_nn, "q_nn")):
+            if v is not None:
+                _host_f64(v, n, name)
         nrm = None if normal is None else np.ascontiguousarray(normal, np.float64)
         msk = None if mask is None else _host_f64(np.ascontiguousarray(mask, np.float64), n, "mask")
-        L.check(L.load().lsg_extend_over_interface_tvd(self._h, L.dptr(phi), L.dptr(q), int(iterations), int(order), float(band_use),
-                                                       float(band_extend), L.dptr(nrm) if nrm is not None else None,
-                                                       L.dptr(msk) if msk is not None else None))
+        opt = lambda a: L.dptr(a) if a is not None else None
+        L.check(L.load().lsg_extend_over_interface_tvd_ex(self._h, L.dptr(phi), L.dptr(q), int(iterations), int(order), float(band_use),
+                                                          float(band_extend), opt(nrm), opt(msk), int(bool(use_nonzero_guess)),
+                                                          opt(q_n), opt(q_nn)))
 
     interpolation_on_interface = 4  # quadratic_non_oscillatory_continuous_v2 (src/my_p4est_level_set.h:389)
 

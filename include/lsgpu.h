@@ -242,6 +242,17 @@ int lsg_extend_over_interface_tvd(lsg_level_set* ls, const double* phi, double* 
                                   double band_extend, const double* normals, const double* mask);
 int lsg_extend_over_interface_tvd_device(lsg_level_set* ls, const double* phi_dev, double* q_dev, int iterations, int order,
                                          double band_use, double band_extend, const double* normals_dev, const double* mask_dev);
+/* The same with the reference's remaining arguments except bc (boundary conditions belong to the
+ * Poisson solvers): use_nonzero_guess (where no normal derivative can be computed, start from n . grad q
+ * and n . grad q_n instead of zero) and q_n / q_nn (N values each or NULL, in and out: their values are
+ * the starting guesses where nothing is computed, and they receive the extended first and second
+ * normal derivatives), as in src/my_p4est_level_set.cpp:1049-1360. */
+int lsg_extend_over_interface_tvd_ex(lsg_level_set* ls, const double* phi, double* q, int iterations, int order, double band_use,
+                                     double band_extend, const double* normals, const double* mask, int use_nonzero_guess, double* q_n,
+                                     double* q_nn);
+int lsg_extend_over_interface_tvd_ex_device(lsg_level_set* ls, const double* phi_dev, double* q_dev, int iterations, int order,
+                                            double band_use, double band_extend, const double* normals_dev, const double* mask_dev,
+                                            int use_nonzero_guess, double* q_n_dev, double* q_nn_dev);
 
 /* my_p4est_level_set_t::extend_from_interface_to_whole_domain_TVD(phi, qi, q, iterations, mask, band_zero,
  * band_smooth, cf, grad_phi, blocksize) (src/my_p4est_level_set.h:775-776,

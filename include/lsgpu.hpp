@@ -192,14 +192,13 @@ class my_p4est_level_set_t {
     lsgpu::check(lsg_perturb_level_set_function(ngbd_->device(), p.p, epsilon));
   }
 
-  // boundary conditions and initial guesses are not supported: passing them raises std::invalid_argument
+  // boundary conditions (bc) are not supported: passing them raises std::invalid_argument
   template <typename BC = void>
   void extend_Over_Interface_TVD(Vec phi, Vec q, int iterations = 20, int order = 2, double band_use = -DBL_MAX,
                                  double band_extend = DBL_MAX, Vec normal[] = nullptr, Vec mask = nullptr, BC* bc = nullptr,
                                  bool use_nonzero_guess = false, Vec q_n = nullptr, Vec q_nn = nullptr) const {
-    if (bc != nullptr || use_nonzero_guess || q_n != nullptr || q_nn != nullptr)
-      throw std::invalid_argument("extend_Over_Interface_TVD: boundary conditions and initial guesses are not supported");
-    lsgpu::VecArray p(phi), v(q), m(mask);
+    if (bc != nullptr) throw std::invalid_argument("extend_Over_Interface_TVD: boundary conditions are not supported");
+    lsgpu::VecArray p(phi), v(q), m(mask), qn(q_n), qnn(q_nn);
     const int D = ngbd_->dim();
     const size_t N = (size_t)ngbd_->num_nodes();
     std::vector<double> nrm;
@@ -210,8 +209,9 @@ class my_p4est_level_set_t {
         for (size_t n = 0; n < N; ++n) nrm[a * N + n] = x.p[n];
       }
     }
-    lsgpu::check(lsg_extend_over_interface_tvd(ngbd_->device(), p.p, v.p, iterations, order, band_use, band_extend,
-                                               normal ? nrm.data() : nullptr, mask ? m.p : nullptr));
+    lsgpu::check(lsg_extend_over_interface_tvd_ex(ngbd_->device(), p.p, v.p, iterations, order, band_use, band_extend,
+                                                  normal ? nrm.data() : nullptr, mask ? m.p : nullptr, use_nonzero_guess ? 1 : 0,
+                                                  q_n ? qn.p : nullptr, q_nn ? qnn.p : nullptr));
   }
 
   void set_interpolation_on_interface(interpolation_method value) { interpolation_on_interface_ = value; }

@@ -1027,7 +1027,8 @@ double march(const Qnnn<D>& q, const double* v, const double* const* nrm, int64_
 // boundary conditions, no initial guesses and one-step extrapolation (src/my_p4est_level_set.cpp:969-1764)
 template <int D>
 void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_in, double* q, int iterations, int order,
-                           double band_use, double band_extend, const double* normal_in, int nthreads) {
+                           double band_use, double band_extend, const double* normal_in, int nthreads, bool nonzero_guess = false,
+                           double* q_n_io = nullptr, double* q_nn_io = nullptr) {
   const Grid<D>& g = *static_cast<const Grid<D>*>(cx.grid);
   const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
   const int64_t N = cx.N;
@@ -1042,7 +1043,11 @@ void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_
     nrm_flat = nstore.data();
   }
   const double* nrm[3] = {nrm_flat, nrm_flat + N, D == 3 ? nrm_flat + 2 * N : nrm_flat};
+  // q_n / q_nn given by the caller: their values start the marching where no value is computed (the
+  // reference then works in the caller's vectors); otherwise fresh zero vectors
   std::vector<double> qn((size_t)N, 0.0), qnn((size_t)N, 0.0), bqn((size_t)N, 0.0), bqnn((size_t)N, 0.0);
+  if (q_n_io) qn.assign(q_n_io, q_n_io + N);
+  if (q_nn_io) qnn.assign(q_nn_io, q_nn_io + N);
   std::vector<double> qx((size_t)D * N, 0.0);
   if (order >= 1) {
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
@@ -1058,7 +1063,13 @@ void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_
           qn[n] = s;
         } else {
           bqn[n] = 1;
-          qn[n] = 0;
+          if (nonzero_guess) {
+            double s = nrm[0][n] * dcentral<D>(Q[n], q, 0) + nrm[1][n] * dcentral<D>(Q[n], q, 1);
+            if (D == 3) s = s + nrm[2][n] * dcentral<D>(Q[n], q, 2);
+            qn[n] = s;
+          } else if (!q_n_io) {
+            qn[n] = 0;
+          }
           for (int a = 0; a < D; ++a) qx[(size_t)a * N + n] = 0;
         }
       } else {
@@ -1079,7 +1090,13 @@ void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_
       }
       bqnn[n] = 1;
       if (!stencil_negative<D>(qq, mask)) {
-        qnn[n] = 0;
+        if (nonzero_guess) {
+          double s = nrm[0][n] * dcentral<D>(qq, qn.data(), 0) + nrm[1][n] * dcentral<D>(qq, qn.data(), 1);
+          if (D == 3) s = s + nrm[2][n] * dcentral<D>(qq, qn.data(), 2);
+          qnn[n] = s;
+        } else if (!q_nn_io) {
+          qnn[n] = 0;
+        }
         continue;
       }
       double Qxy = 0, Qyz = 0, Qzx = 0;
@@ -1133,7 +1150,7 @@ void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_
           qnn[n] = Nx * (Nx * dd[0] + 2. * Ny * Qxy + Qx * Nxx + Qy * Nyx) + Ny * (Ny * dd[1] + Qx * Nxy + Qy * Nyy);
         }
       } else {
-        qnn[n] = 0;
+        if (!q_nn_io) qnn[n] = 0;  // left as it was (a fresh vector is zero)
       }
     }
   }
@@ -1181,6 +1198,8 @@ void extend_over_interface(const Ctx& cx, const double* phi, const double* mask_
     cur.swap(tmp);
   }
   memcpy(q, cur.data(), (size_t)N * sizeof(double));
+  if (q_n_io && order >= 1) memcpy(q_n_io, qn.data(), (size_t)N * sizeof(double));
+  if (q_nn_io && order == 2) memcpy(q_nn_io, qnn.data(), (size_t)N * sizeof(double));
 }
 
 // ---- node interpolation ------------------------------------------------------------------------
@@ -1879,6 +1898,19 @@ int ora_normals_and_mean_curvature(void* h, const double* phi, double* normals, 
     Ctx* cx = static_cast<Ctx*>(h);
     if (cx->dim == 2) normals_and_curvature<2>(*cx, phi, normals, kappa, nthreads);
     else normals_and_curvature<3>(*cx, phi, normals, kappa, nthreads);
+  });
+}
+
+int ora_extend_over_interface_ex(void* h, const double* phi, const double* mask, double* q, int iterations, int order, double band_use,
+                                 double band_extend, const double* normals, int nonzero_guess, double* q_n, double* q_nn, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (!cx->grid) throw std::runtime_error("extension needs a grid built from leaves");
+    if (order < 0 || order > 2) throw std::invalid_argument("order must be 0, 1 or 2");
+    if (cx->dim == 2)
+      extend_over_interface<2>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads, nonzero_guess != 0, q_n, q_nn);
+    else
+      extend_over_interface<3>(*cx, phi, mask, q, iterations, order, band_use, band_extend, normals, nthreads, nonzero_guess != 0, q_n, q_nn);
   });
 }
 

@@ -42,6 +42,7 @@ SIG = {
     "ora_mean_curvature_from_normals": (_I, [_P, _DP, _DP, _I]),
     "ora_normals_and_mean_curvature": (_I, [_P, _DP, _DP, _DP, _I]),
     "ora_extend_over_interface": (_I, [_P, _DP, _DP, _DP, _I, _I, _D, _D, _DP, _I]),
+    "ora_extend_over_interface_ex": (_I, [_P, _DP, _DP, _DP, _I, _I, _D, _D, _DP, _I, _DP, _DP, _I]),
     "ora_extend_from_interface": (_I, [_P, _DP, _DP, _DP, _I, _DP, _D, _D, _DP, _I, _I]),
     "ora_extend_from_interface_cf": (_I, [_P, _DP, _DP, _DP, _I, _P, _P, _DP, _I]),
     "ora_interface_location": (_D, [_D, _D, _D, _D]),
@@ -186,14 +187,18 @@ class OracleGrid:
         return nrm, kappa
 
     def extend_over_interface_tvd(self, phi, q, iterations=20, order=2, band_use=-np.finfo(np.float64).max,
-                                  band_extend=np.finfo(np.float64).max, normals=None, mask=None, nthreads=1):
-        """In place on q (float64, node order)."""
+                                  band_extend=np.finfo(np.float64).max, normals=None, mask=None, nthreads=1,
+                                  use_nonzero_guess=False, q_n=None, q_nn=None):
+        """In place on q (float64, node order); q_n / q_nn (optional, in place): the normal derivatives."""
         phi = np.ascontiguousarray(phi, np.float64)
         assert q.dtype == np.float64 and q.flags.c_contiguous and q.size == self.N
+        for v in (q_n, q_nn):
+            assert v is None or (v.dtype == np.float64 and v.flags.c_contiguous and v.size == self.N)
         nrm = None if normals is None else np.ascontiguousarray(normals, np.float64)
         msk = None if mask is None else np.ascontiguousarray(mask, np.float64)
-        _chk(load().ora_extend_over_interface(self._h, _dp(phi), _dp(msk), _dp(q), int(iterations), int(order), float(band_use),
-                                              float(band_extend), _dp(nrm), nthreads))
+        _chk(load().ora_extend_over_interface_ex(self._h, _dp(phi), _dp(msk), _dp(q), int(iterations), int(order), float(band_use),
+                                                 float(band_extend), _dp(nrm), int(bool(use_nonzero_guess)), _dp(q_n), _dp(q_nn),
+                                                 nthreads))
 
     def extend_from_interface_to_whole_domain_tvd(self, phi, qi, iterations=20, mask=None, band_zero=2.0, band_smooth=10.0,
                                                   grad_phi=None, method=4, nthreads=1):

@@ -249,3 +249,56 @@ def test_gpu_whole_domain_extension_cf_bitwise(name):
         ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=2, cf=iface_value, mask=phi)
     with pytest.raises(ZeroDivisionError):
         ls.extend_from_interface_to_whole_domain_TVD(phi, qi, iterations=2, cf=lambda n, d, s: 1 / 0)
+
+
+def test_oracle_extension_normal_derivative_outputs():
+    """q_n / q_nn given: zero guesses give the same q as without them, and they come back holding the
+    extended normal derivatives (for q = x + 2y inside a circle: n . (1, 2) near the interface)."""
+    f = sphere_grid(2, 7)
+    og = O.OracleGrid.from_forest(f)
+    x = f.node_xyz()
+    r = np.sqrt(np.sum(x ** 2, axis=1))
+    phi = r - 0.47
+    q0 = np.where(phi < 0, x[:, 0] + 2 * x[:, 1], 0.0)
+    a = q0.copy()
+    og.extend_over_interface_tvd(phi, a, 40, 2)
+    b = q0.copy()
+    qn, qnn = np.zeros(len(phi)), np.zeros(len(phi))
+    og.extend_over_interface_tvd(phi, b, 40, 2, q_n=qn, q_nn=qnn)
+    assert np.array_equal(a, b)
+    nrm = x / np.maximum(r, 1e-12)[:, None]
+    err = np.abs(qn - (nrm[:, 0] + 2 * nrm[:, 1]))
+    inside = (phi < -0.05) & (phi > -0.2)  # computed by central differences
+    assert np.max(err[inside]) < 0.05
+    outside = (phi > 0) & (phi < 0.05)  # marched along the normals with the q_nn source
+    assert np.median(err[outside]) < 0.05
+    c = q0.copy()
+    og.extend_over_interface_tvd(phi, c, 40, 2, use_nonzero_guess=True)
+    band = np.abs(phi) < 0.05
+    assert np.max(np.abs(c[band] - a[band])) < 1e-3  # the steady state does not depend on the guess
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["circle2d", "flower3d", "brick3d"])
+@pytest.mark.parametrize("order", [1, 2])
+def test_gpu_extension_guesses_and_outputs(name, order):
+    f = GRIDS[name]()
+    og = O.OracleGrid.from_forest(f)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    x, phi, q0 = case(f)
+    rng = np.random.default_rng(7)
+    for guess, give in ((False, True), (True, False), (True, True)):
+        init_n = rng.uniform(-1, 1, len(phi)) if give else None
+        init_nn = rng.uniform(-1, 1, len(phi)) if give else None
+        w, g = q0.copy(), q0.copy()
+        wn = None if init_n is None else init_n.copy()
+        wnn = None if init_nn is None else init_nn.copy()
+        gn = None if init_n is None else init_n.copy()
+        gnn = None if init_nn is None else init_nn.copy()
+        og.extend_over_interface_tvd(phi, w, 9, order, use_nonzero_guess=guess, q_n=wn, q_nn=wnn, nthreads=8)
+        ls.extend_Over_Interface_TVD(phi, g, 9, order, use_nonzero_guess=guess, q_n=gn, q_nn=gnn)
+        assert np.array_equal(g, w), (guess, give)
+        if give:
+            assert np.array_equal(gn, wn) and np.array_equal(gnn, wnn), (guess, give)
+    with pytest.raises(ValueError):
+        ls.extend_Over_Interface_TVD(phi, q0.copy(), 2, order, bc=object())
