@@ -33,7 +33,9 @@
 #define LSGPU_HPP
 
 #include <float.h>
+#include <limits.h>
 
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -330,6 +332,7 @@ class my_p4est_level_set_t {
 // Node interpolation at buffered points (one process: every point is local).
 class my_p4est_interpolation_nodes_t {
  public:
+  static const unsigned int ALL_COMPONENTS = UINT_MAX;
   explicit my_p4est_interpolation_nodes_t(const my_p4est_node_neighbors_t* ngbd) : ngbd_(ngbd) {}
   void clear() {
     idx_.clear();
@@ -339,48 +342,100 @@ class my_p4est_interpolation_nodes_t {
     idx_.push_back(node_idx_on_output);
     for (int a = 0; a < ngbd_->dim(); ++a) xyz_.push_back(xyz[a]);
   }
-  void set_input(Vec F, interpolation_method method) {
-    F_ = F;
-    Fdd_[0] = Fdd_[1] = Fdd_[2] = nullptr;
+  // n_vecs input fields, each a block vector of block_size_f components per node (interleaved)
+  void set_input(Vec* F, interpolation_method method, size_t n_vecs, unsigned int block_size_f = 1) {
+    F_.assign(F, F + n_vecs);
+    for (auto& v : Fdd_) v.clear();
+    Fblock_.clear();
+    bs_ = block_size_f;
     method_ = method;
   }
-  void set_input(Vec F, Vec Fxx, Vec Fyy, Vec Fzz, interpolation_method method) {
-    F_ = F;
-    Fdd_[0] = Fxx;
-    Fdd_[1] = Fyy;
-    Fdd_[2] = Fzz;
-    method_ = method;
+  void set_input(Vec F, interpolation_method method, unsigned int block_size_f = 1) { set_input(&F, method, 1, block_size_f); }
+  // second derivatives given component by component (Fxx[k], Fyy[k][, Fzz[k]] block vectors like F[k])
+  void set_input(Vec* F, Vec* Fxx, Vec* Fyy, Vec* Fzz, interpolation_method method, size_t n_vecs, unsigned int block_size_f = 1) {
+    set_input(F, method, n_vecs, block_size_f);
+    Vec* dd[3] = {Fxx, Fyy, Fzz};
+    for (int a = 0; a < ngbd_->dim(); ++a)
+      if (dd[a]) Fdd_[a].assign(dd[a], dd[a] + n_vecs);
+  }
+  void set_input(Vec F, Vec Fxx, Vec Fyy, Vec Fzz, interpolation_method method, unsigned int block_size_f = 1) {
+    set_input(&F, &Fxx, &Fyy, Fzz ? &Fzz : nullptr, method, 1, block_size_f);
   }
   void set_input(Vec F, Vec Fxx, Vec Fyy, interpolation_method method) { set_input(F, Fxx, Fyy, nullptr, method); }
-  // results[node_idx_on_output] for every buffered point
-  void interpolate(double* results) const {
+  // second derivatives as one block vector per field: [(node * block_size_f + component) * dim + direction]
+  void set_input(Vec* F, Vec* Fxxyyzz_block, interpolation_method method, size_t n_vecs, unsigned int block_size_f = 1) {
+    set_input(F, method, n_vecs, block_size_f);
+    Fblock_.assign(Fxxyyzz_block, Fxxyyzz_block + n_vecs);
+  }
+  void set_input(Vec F, Vec Fxxyyzz_block, interpolation_method method, unsigned int block_size_f = 1) {
+    set_input(&F, &Fxxyyzz_block, method, 1, block_size_f);
+  }
+  // Fo[k][bs * node_idx_on_output + c] (all components) or Fo[k][node_idx_on_output] (one component)
+  void interpolate(double* const* Fo, unsigned int comp = ALL_COMPONENTS) const {
     const int D = ngbd_->dim();
-    const size_t N = (size_t)ngbd_->num_nodes();
-    lsgpu::VecArray f(F_);
-    std::vector<double> dd;
-    if (Fdd_[0] && method_ != linear) {
-      dd.resize((size_t)D * N);
-      for (int a = 0; a < D; ++a) {
-        lsgpu::VecArray x(Fdd_[a]);
-        for (size_t n = 0; n < N; ++n) dd[a * N + n] = x.p[n];
+    const size_t N = (size_t)ngbd_->num_nodes(), nv = F_.size();
+    if (comp != ALL_COMPONENTS && comp >= bs_) throw std::invalid_argument("interpolate: component out of range");
+    const unsigned int nc = (comp == ALL_COMPONENTS) ? bs_ : 1;
+    const size_t nf = nv * nc;
+    const bool have_dd = method_ != linear && (!Fblock_.empty() || !Fdd_[0].empty());
+    std::vector<double> f(nf * N), dd(have_dd ? nf * D * N : 0);
+    for (size_t k = 0; k < nv; ++k) {
+      lsgpu::VecArray x(F_[k]);
+      for (unsigned int c = 0; c < nc; ++c) {
+        const unsigned int cc = comp == ALL_COMPONENTS ? c : comp;
+        const size_t fi = k * nc + c;
+        for (size_t n = 0; n < N; ++n) f[fi * N + n] = x.p[bs_ * n + cc];
+        if (!have_dd) continue;
+        if (!Fblock_.empty()) {
+          lsgpu::VecArray b(Fblock_[k]);
+          for (int a = 0; a < D; ++a)
+            for (size_t n = 0; n < N; ++n) dd[(fi * D + a) * N + n] = b.p[(n * bs_ + cc) * D + a];
+        } else {
+          for (int a = 0; a < D; ++a) {
+            lsgpu::VecArray y(Fdd_[a][k]);
+            for (size_t n = 0; n < N; ++n) dd[(fi * D + a) * N + n] = y.p[bs_ * n + cc];
+          }
+        }
       }
     }
-    std::vector<double> out(idx_.size());
-    lsgpu::check(lsg_interpolate_nodes(ngbd_->device(), xyz_.data(), (int64_t)idx_.size(), f.p, 1, dd.empty() ? nullptr : dd.data(),
+    const size_t np = idx_.size();
+    std::vector<double> out(nf * np);
+    lsgpu::check(lsg_interpolate_nodes(ngbd_->device(), xyz_.data(), (int64_t)np, f.data(), (int)nf, have_dd ? dd.data() : nullptr,
                                        (int)method_, out.data()));
-    for (size_t i = 0; i < idx_.size(); ++i) results[idx_[i]] = out[i];
+    for (size_t k = 0; k < nv; ++k)
+      for (unsigned int c = 0; c < nc; ++c)
+        for (size_t i = 0; i < np; ++i) {
+          const double v = out[(k * nc + c) * np + i];
+          if (comp == ALL_COMPONENTS)
+            Fo[k][bs_ * idx_[i] + c] = v;
+          else
+            Fo[k][idx_[i]] = v;
+        }
   }
+  // one field: results[node_idx_on_output] (block size 1) or results[bs * node_idx_on_output + c]
+  void interpolate(double* results) const { interpolate(&results); }
   void interpolate(Vec out) const {
     lsgpu::VecArray o(out);
     interpolate(o.p);
+  }
+  void interpolate(Vec* out, unsigned int comp = ALL_COMPONENTS) const {
+    std::vector<std::unique_ptr<lsgpu::VecArray>> arr;
+    std::vector<double*> ptr;
+    for (size_t k = 0; k < F_.size(); ++k) {
+      arr.emplace_back(new lsgpu::VecArray(out[k]));
+      ptr.push_back(arr.back()->p);
+    }
+    interpolate(ptr.data(), comp);
   }
 
  private:
   const my_p4est_node_neighbors_t* ngbd_;
   std::vector<int64_t> idx_;
   std::vector<double> xyz_;
-  Vec F_ = nullptr;
-  Vec Fdd_[3] = {nullptr, nullptr, nullptr};
+  std::vector<Vec> F_;
+  std::vector<Vec> Fdd_[3];
+  std::vector<Vec> Fblock_;
+  unsigned int bs_ = 1;
   interpolation_method method_ = linear;
 };
 

@@ -78,6 +78,50 @@ int main() {
   for (int k = 0; k < 500; ++k)
     if (got[499 - k] != want[k]) return fail("interpolate");
 
+  // two block vectors of two components each, with the second derivatives as block vectors
+  {
+    const unsigned bs = 2;
+    lsgpu_vec A{std::vector<double>((size_t)bs * N)}, B{std::vector<double>((size_t)bs * N)};
+    std::vector<double> comps((size_t)4 * N);
+    for (int64_t i = 0; i < N; ++i) {
+      const double x = xyz[2 * i], y = xyz[2 * i + 1];
+      const double v[4] = {x, y * y, x * y, 1.0 + x * x};
+      A.values[bs * i] = v[0];
+      A.values[bs * i + 1] = v[1];
+      B.values[bs * i] = v[2];
+      B.values[bs * i + 1] = v[3];
+      for (int c = 0; c < 4; ++c) comps[(size_t)c * N + i] = v[c];
+    }
+    std::vector<double> dd((size_t)4 * 2 * N);
+    for (int c = 0; c < 4; ++c) lsgpu::check(lsg_second_derivatives(raw, &comps[(size_t)c * N], &dd[(size_t)c * 2 * N]));
+    lsgpu_vec Ab{std::vector<double>((size_t)bs * 2 * N)}, Bb{std::vector<double>((size_t)bs * 2 * N)};
+    for (int64_t i = 0; i < N; ++i)
+      for (unsigned c = 0; c < bs; ++c)
+        for (int a = 0; a < 2; ++a) {
+          Ab.values[(i * bs + c) * 2 + a] = dd[((size_t)c * 2 + a) * N + i];
+          Bb.values[(i * bs + c) * 2 + a] = dd[((size_t)(2 + c) * 2 + a) * N + i];
+        }
+    Vec F[2] = {&A, &B}, Fb[2] = {&Ab, &Bb};
+    my_p4est_interpolation_nodes_t multi(&ngbd);
+    for (int k = 0; k < 500; ++k) multi.add_point(k, &pts[2 * k]);
+    std::vector<double> oa((size_t)bs * 500), ob((size_t)bs * 500), ref((size_t)4 * 500);
+    double* Fo[2] = {oa.data(), ob.data()};
+    multi.set_input(F, Fb, quadratic_non_oscillatory, 2, bs);
+    multi.interpolate(Fo);
+    lsgpu::check(lsg_interpolate_nodes(raw, pts.data(), 500, comps.data(), 4, dd.data(), LSG_QUADRATIC_NON_OSCILLATORY, ref.data()));
+    for (int k = 0; k < 500; ++k)
+      for (unsigned c = 0; c < bs; ++c)
+        if (oa[bs * k + c] != ref[(size_t)c * 500 + k] || ob[bs * k + c] != ref[(size_t)(2 + c) * 500 + k])
+          return fail("interpolate (block vectors)");
+    std::vector<double> one(500);
+    double* Fo1[2] = {one.data(), one.data()};
+    multi.set_input(F, quadratic, 2, bs);
+    multi.interpolate(Fo1, 1);  // component 1 of every field (the second field's values end in the buffer)
+    lsgpu::check(lsg_interpolate_nodes(raw, pts.data(), 500, &comps[(size_t)3 * N], 1, nullptr, LSG_QUADRATIC, ref.data()));
+    for (int k = 0; k < 500; ++k)
+      if (one[k] != ref[k]) return fail("interpolate (one component)");
+  }
+
   // semi-Lagrangian step onto the same grid with a rotating node velocity
   lsgpu_vec vx{std::vector<double>((size_t)N)}, vy{std::vector<double>((size_t)N)};
   for (int64_t i = 0; i < N; ++i) {
