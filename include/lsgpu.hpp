@@ -17,7 +17,7 @@
  *                                             cf, grad_phi, blocksize), set_interpolation_on_interface
  *                                                                      src/my_p4est_level_set.h:775-776, 843
  *   my_p4est_interpolation_nodes_t: set_input, add_point, interpolate  src/my_p4est_interpolation_nodes.h:33-103
- *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1                   src/my_p4est_semi_lagrangian.h:83-196
+ *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1, update_p4est     src/my_p4est_semi_lagrangian.h:83-196
  *
  * Vec: with LSGPU_WITH_PETSC defined before inclusion, PETSc's Vec (read through VecGetArray);
  * otherwise a minimal host vector with the same accessor names (VecGetArray / VecRestoreArray /
@@ -443,6 +443,60 @@ class my_p4est_interpolation_nodes_t {
 class my_p4est_semi_lagrangian_t {
  public:
   my_p4est_semi_lagrangian_t(lsg_forest* forest_np1, my_p4est_node_neighbors_t* ngbd_n) : forest_np1_(forest_np1), ngbd_n_(ngbd_n) {}
+  // with the splitting criterion of grid n+1 (the reference reads it from p4est->user_pointer)
+  my_p4est_semi_lagrangian_t(lsg_forest* forest_np1, my_p4est_node_neighbors_t* ngbd_n, int min_lvl, int max_lvl, double lip)
+      : forest_np1_(forest_np1), ngbd_n_(ngbd_n), min_lvl_(min_lvl), max_lvl_(max_lvl), lip_(lip) {}
+  void set_splitting(int min_lvl, int max_lvl, double lip) {
+    min_lvl_ = min_lvl;
+    max_lvl_ = max_lvl;
+    lip_ = lip;
+  }
+  // update_p4est(v, dt, phi) (src/my_p4est_semi_lagrangian.cpp:394-529) with node velocities v[D] of
+  // grid n: phi is advected onto forest_np1, which is refined and coarsened from the advected values
+  // until it no longer changes; phi is then replaced by its values at the final nodes. Returns the number
+  // of advection passes.
+  // phi_xx: phi's second derivatives on grid n (computed when null); band: the splitting criterion's band.
+  // phi_add_refine (an extra refinement field) is not supported.
+  int update_p4est(Vec* v, double dt, Vec& phi, Vec* phi_xx = nullptr, Vec phi_add_refine = nullptr, const double& band = 0) {
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes();
+    std::vector<double> vv((size_t)D * N), vdd((size_t)D * D * N);
+    for (int a = 0; a < D; ++a) {
+      lsgpu::VecArray x(v[a]);
+      for (size_t n = 0; n < N; ++n) vv[a * N + n] = x.p[n];
+    }
+    // the velocity's second derivatives on grid n once, as the reference computes them once
+    for (int a = 0; a < D; ++a) lsgpu::check(lsg_second_derivatives(ngbd_n_->device(), &vv[a * N], &vdd[(size_t)a * D * N]));
+    return regrid(dt, phi, phi_xx, phi_add_refine, band, [&](const std::vector<double>& xyz, const std::vector<double>& pn,
+                                                              const std::vector<double>& pdd, std::vector<double>& out) {
+      lsgpu::check(lsg_semi_lagrangian_advect(ngbd_n_->device(), xyz.data(), (int64_t)out.size(), dt, vv.data(), vdd.data(), pn.data(),
+                                              pdd.data(), (int)velo_, (int)phi_, out.data()));
+    });
+  }
+  // update_p4est(const CF** v, dt, phi, phi_xx) (src/my_p4est_semi_lagrangian.cpp:321-392): v[D] function
+  // objects of the coordinates, evaluated on the host at the nodes of grid n+1 and at the midpoints.
+  template <typename CF>
+  int update_p4est(const CF* const* v, double dt, Vec& phi, Vec* phi_xx = nullptr) {
+    struct Ctx {
+      const CF* const* v;
+      int D;
+    } ctx{v, ngbd_n_->dim()};
+    lsg_velocity_fn fn = [](void* c, int64_t npts, const double* xyz, double* out) -> int {
+      const Ctx* k = static_cast<const Ctx*>(c);
+      try {
+        for (int64_t p = 0; p < npts; ++p)
+          for (int a = 0; a < k->D; ++a) out[p * k->D + a] = lsgpu::eval_cf(*k->v[a], &xyz[p * k->D], k->D);
+      } catch (...) {
+        return 1;
+      }
+      return 0;
+    };
+    return regrid(dt, phi, phi_xx, nullptr, 0.0, [&](const std::vector<double>& xyz, const std::vector<double>& pn,
+                                                       const std::vector<double>& pdd, std::vector<double>& out) {
+      lsgpu::check(lsg_semi_lagrangian_advect_callback(ngbd_n_->device(), xyz.data(), (int64_t)out.size(), dt, fn, &ctx, pn.data(),
+                                                       pdd.data(), (int)phi_, out.data()));
+    });
+  }
   void set_velo_interpolation(interpolation_method m) { velo_ = m; }
   void set_phi_interpolation(interpolation_method m) { phi_ = m; }
   // advect_from_n_to_np1(dt, v, vxx, phi_n, phi_xx_n, phi_np1): v[D] node velocities of grid n;
@@ -514,8 +568,58 @@ class my_p4est_semi_lagrangian_t {
   }
 
  private:
+  // advect phi onto forest_np1 with `advect`, refine/coarsen from the result, repeat until the grid
+  // settles; phi becomes the values at the final nodes
+  template <typename Advect>
+  int regrid(double dt, Vec& phi, Vec* phi_xx, Vec phi_add_refine, double band, Advect advect) {
+    (void)dt;
+    if (max_lvl_ < 0) throw std::invalid_argument("update_p4est: set the splitting criterion first");
+    if (phi_add_refine != nullptr) throw std::invalid_argument("update_p4est: phi_add_refine is not supported");
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes();
+    std::vector<double> pn(N), pdd((size_t)D * N);
+    {
+      lsgpu::VecArray p(phi);
+      for (size_t n = 0; n < N; ++n) pn[n] = p.p[n];
+    }
+    if (phi_xx) {
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(phi_xx[a]);
+        for (size_t n = 0; n < N; ++n) pdd[a * N + n] = x.p[n];
+      }
+    } else {
+      lsgpu::check(lsg_second_derivatives(ngbd_n_->device(), pn.data(), pdd.data()));
+    }
+    std::vector<double> out, xyz;
+    int passes = 0;
+    for (;;) {
+      if (lsg_forest_num_nodes(forest_np1_) < 0) lsgpu::check(lsg_forest_build_nodes(forest_np1_));
+      const int64_t np = lsg_forest_num_nodes(forest_np1_);
+      xyz.resize((size_t)np * D);
+      out.resize((size_t)np);
+      lsgpu::check(lsg_forest_node_xyz(forest_np1_, xyz.data()));
+      advect(xyz, pn, pdd, out);
+      ++passes;
+      int changed = 0;
+      lsgpu::check(lsg_forest_refine_and_coarsen(forest_np1_, min_lvl_, max_lvl_, lip_, band, out.data(), &changed));
+      if (!changed) break;
+      lsgpu::check(lsg_forest_build_nodes(forest_np1_));
+    }
+#ifdef LSGPU_WITH_PETSC
+    VecDestroy(&phi);
+    VecCreateSeq(PETSC_COMM_SELF, (PetscInt)out.size(), &phi);
+    lsgpu::VecArray p(phi);
+    for (size_t n = 0; n < out.size(); ++n) p.p[n] = out[n];
+#else
+    phi->values = out;
+#endif
+    return passes;
+  }
+
   lsg_forest* forest_np1_;
   my_p4est_node_neighbors_t* ngbd_n_;
+  int min_lvl_ = 0, max_lvl_ = -1;
+  double lip_ = 1.2;
   interpolation_method velo_ = quadratic_non_oscillatory_continuous_v2;
   interpolation_method phi_ = quadratic_non_oscillatory_continuous_v2;
 };

@@ -198,6 +198,50 @@ int main() {
                                                                 nullptr, nullptr));
   if (memcmp(qcf.values.data(), qcf_ref.data(), N * sizeof(double)) != 0) return fail("extend_from_interface_to_whole_domain_TVD (cf)");
 
+  // update_p4est with node velocities: the regrid loop against the same loop written with the C ABI
+  {
+    lsg_forest *fa = nullptr, *fb = nullptr;
+    lsgpu::check(lsg_forest_copy(f, &fa));
+    lsgpu::check(lsg_forest_copy(f, &fb));
+    my_p4est_semi_lagrangian_t up(fa, &ngbd, 3, 7, 2.4);
+    lsgpu_vec phi_up{phi.values};
+    Vec pv = &phi_up;
+    const int passes = up.update_p4est(v, 0.05, pv);
+    std::vector<double> vv((size_t)2 * N), vdd((size_t)4 * N), pdd((size_t)2 * N), out;
+    memcpy(vv.data(), vx.values.data(), N * sizeof(double));
+    memcpy(vv.data() + N, vy.values.data(), N * sizeof(double));
+    for (int a = 0; a < 2; ++a) lsgpu::check(lsg_second_derivatives(raw, &vv[(size_t)a * N], &vdd[(size_t)a * 2 * N]));
+    lsgpu::check(lsg_second_derivatives(raw, phi.values.data(), pdd.data()));
+    int ref_passes = 0;
+    for (;;) {
+      const int64_t np = lsg_forest_num_nodes(fb);
+      std::vector<double> x2((size_t)np * 2);
+      out.assign((size_t)np, 0.0);
+      lsgpu::check(lsg_forest_node_xyz(fb, x2.data()));
+      lsgpu::check(lsg_semi_lagrangian_advect(raw, x2.data(), np, 0.05, vv.data(), vdd.data(), phi.values.data(), pdd.data(),
+                                              LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2,
+                                              out.data()));
+      ++ref_passes;
+      int changed = 0;
+      lsgpu::check(lsg_forest_refine_and_coarsen(fb, 3, 7, 2.4, 0.0, out.data(), &changed));
+      if (!changed) break;
+      lsgpu::check(lsg_forest_build_nodes(fb));
+    }
+    if (passes != ref_passes || phi_up.values.size() != out.size() ||
+        memcmp(phi_up.values.data(), out.data(), out.size() * sizeof(double)) != 0)
+      return fail("update_p4est");
+    // the CF form with a constant velocity runs the same loop through the callback
+    lsg_forest* fc = nullptr;
+    lsgpu::check(lsg_forest_copy(f, &fc));
+    my_p4est_semi_lagrangian_t upc(fc, &ngbd, 3, 7, 2.4);
+    lsgpu_vec phi_c{phi.values};
+    Vec pc = &phi_c;
+    if (upc.update_p4est(cf, 0.05, pc) < 1 || phi_c.values.size() != (size_t)lsg_forest_num_nodes(fc)) return fail("update_p4est (CF)");
+    lsg_forest_destroy(fa);
+    lsg_forest_destroy(fb);
+    lsg_forest_destroy(fc);
+  }
+
   // errors come back as exceptions
   try {
     ls.reinitialize_within_range_of_phi_0(&phi, 3, 2, 1.0, -1.0, 5);
