@@ -52,6 +52,9 @@ int guard(Fn&& fn) {
   try {
     fn();
     return LSG_OK;
+  } catch (const CudaOutOfMemory& e) {
+    g_last_error = e.what();
+    return LSG_ENOMEM;
   } catch (const CudaError& e) {
     g_last_error = e.what();
     return LSG_EDEVICE;

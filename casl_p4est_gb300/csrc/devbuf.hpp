@@ -11,6 +11,10 @@ namespace lsg {
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
+// device memory exhausted (reported as LSG_ENOMEM)
+struct CudaOutOfMemory : CudaError {
+  using CudaError::CudaError;
+};
 
 inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
@@ -33,7 +37,13 @@ struct DevBuf {
     if (count == n && p) return;
     release();
     if (count == 0) return;
-    cuda_check(cudaMalloc((void**)&p, count * sizeof(T)), "cudaMalloc");
+    const cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();  // not a sticky error: clear it so that later calls proceed
+      p = nullptr;
+      throw CudaOutOfMemory("cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes: out of device memory");
+    }
+    cuda_check(e, "cudaMalloc");
     n = count;
   }
   // grow-only allocation for work buffers whose size varies between calls
