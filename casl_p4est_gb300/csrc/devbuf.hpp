@@ -2,6 +2,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <stdint.h>
+
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -20,16 +24,113 @@ inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Device memory cache behind every DevBuf. A released block is kept for reuse instead of going back
+// to the driver (cudaMalloc and cudaFree cost tens of microseconds each, and cudaFree waits for the
+// whole device); a level set built for every new grid otherwise pays that for each of its tables.
+// Reuse keeps cudaFree's guarantee: a block released since the last device synchronisation is handed
+// out again only after a cudaDeviceSynchronize, so no kernel still in flight can see it change owner.
+// Blocks are grouped by size class (eight classes per power of two, at most 12.5% unused).
+class DeviceCache {
+ public:
+  static DeviceCache& get() {
+    static DeviceCache* c = new DeviceCache();  // never destroyed: the driver frees everything at exit
+    return *c;
+  }
+  static size_t size_class(size_t bytes) {
+    if (bytes <= 4096) return 4096;
+    int e = 63 - __builtin_clzll((unsigned long long)(bytes - 1));  // 2^e < bytes <= 2^(e+1)
+    const size_t step = (size_t)1 << (e - 3);
+    return (bytes + step - 1) / step * step;
+  }
+  // a block of size_class(bytes) on the current device; nullptr when the device is out of memory
+  void* take(size_t bytes, int& dev) {
+    const size_t cls = size_class(bytes);
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      auto it = free_.find(Key{dev, cls});
+      if (it != free_.end() && !it->second.empty()) {
+        Block b = it->second.back();
+        it->second.pop_back();
+        cached_ -= cls;
+        if (b.epoch == epoch_) {
+          cuda_check(cudaDeviceSynchronize(), "device synchronisation before reuse");
+          ++epoch_;
+        }
+        return b.p;
+      }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, cls);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();  // not a sticky error: clear it so that later calls proceed
+      trim();
+      e = cudaMalloc(&p, cls);
+      if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return nullptr;
+      }
+    }
+    cuda_check(e, "cudaMalloc");
+    return p;
+  }
+  void give(void* p, size_t bytes, int dev) {
+    const size_t cls = size_class(bytes);
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      if (cls <= kMaxBlock && cached_ + cls <= kMaxCached) {
+        free_[Key{dev, cls}].push_back(Block{p, epoch_});
+        cached_ += cls;
+        return;
+      }
+    }
+    cudaFree(p);
+  }
+  // return every cached block to the driver
+  void trim() {
+    std::lock_guard<std::mutex> g(mu_);
+    if (cached_ == 0) return;
+    cudaDeviceSynchronize();
+    for (auto& kv : free_)
+      for (const Block& b : kv.second) cudaFree(b.p);
+    free_.clear();
+    cached_ = 0;
+    ++epoch_;
+  }
+  size_t cached_bytes() {
+    std::lock_guard<std::mutex> g(mu_);
+    return cached_;
+  }
+
+ private:
+  static constexpr size_t kMaxBlock = (size_t)4 << 30;    // larger blocks go straight back
+  static constexpr size_t kMaxCached = (size_t)16 << 30;  // total kept
+  struct Key {
+    int dev;
+    size_t cls;
+    bool operator<(const Key& o) const { return dev != o.dev ? dev < o.dev : cls < o.cls; }
+  };
+  struct Block {
+    void* p;
+    uint64_t epoch;  // the synchronisation count at release
+  };
+  std::mutex mu_;
+  std::map<Key, std::vector<Block>> free_;
+  size_t cached_ = 0;
+  uint64_t epoch_ = 0;
+};
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  int dev = 0;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) DeviceCache::get().give(p, n * sizeof(T), dev);
     p = nullptr;
     n = 0;
   }
@@ -37,13 +138,8 @@ struct DevBuf {
     if (count == n && p) return;
     release();
     if (count == 0) return;
-    const cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
-    if (e == cudaErrorMemoryAllocation) {
-      cudaGetLastError();  // not a sticky error: clear it so that later calls proceed
-      p = nullptr;
-      throw CudaOutOfMemory("cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes: out of device memory");
-    }
-    cuda_check(e, "cudaMalloc");
+    p = static_cast<T*>(DeviceCache::get().take(count * sizeof(T), dev));
+    if (!p) throw CudaOutOfMemory("cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes: out of device memory");
     n = count;
   }
   // grow-only allocation for work buffers whose size varies between calls

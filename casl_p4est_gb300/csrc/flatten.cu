@@ -90,7 +90,8 @@ inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 template <int D>
 __global__ void __launch_bounds__(TPB) k_rows64(DForest<D> F, int32_t* __restrict__ nbr, double* __restrict__ w, double* __restrict__ nrm,
                                                 double* __restrict__ d, double* __restrict__ q, uint8_t* __restrict__ wall,
-                                                double* __restrict__ smin, int32_t* __restrict__ needs, int* __restrict__ failed) {
+                                                double* __restrict__ smin, int32_t* __restrict__ needs, double* __restrict__ cross,
+                                                int* __restrict__ failed) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = F.N;
   if (n >= N) return;
@@ -101,25 +102,26 @@ __global__ void __launch_bounds__(TPB) k_rows64(DForest<D> F, int32_t* __restric
     needs[n] = 0;
     return;
   }
-  needs[n] = fill_row64<D>(rec, N, n, nbr, w, nrm, d, q, smin) ? 1 : 0;
+  const bool need = fill_row64<D>(rec, N, n, nbr, w, nrm, d, q, smin);
+  needs[n] = need ? 1 : 0;
+  // the cross terms of a node that needs a correction record, at its node index until the records
+  // are numbered
+  if (need) cross_terms<D>(rec, cross + (int64_t)6 * n);
   wall[n] = (uint8_t)wall_mask_v<D>(V, (int32_t)n);
 }
 
-template <int D>
-__global__ void __launch_bounds__(TPB) k_crec64(DForest<D> F, const int32_t* __restrict__ needs, const int32_t* __restrict__ scan,
-                                                int32_t* __restrict__ cidx, double* __restrict__ crec) {
+// correction records numbered in node order (the exclusive scan of the needs flags)
+__global__ void __launch_bounds__(TPB) k_crec64(int64_t N, const int32_t* __restrict__ needs, const int32_t* __restrict__ scan,
+                                                const double* __restrict__ cross, int32_t* __restrict__ cidx, double* __restrict__ crec) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= F.N) return;
+  if (n >= N) return;
   if (!needs[n]) {
     cidx[n] = -1;
     return;
   }
   const int32_t r = scan[n];
   cidx[n] = r;
-  const DeviceForestView<D> V{F};
-  Qnnn<D> rec;
-  construct_neighbors_v<D>(V, (int32_t)n, rec);
-  cross_terms<D>(rec, crec + (int64_t)6 * r);
+  for (int i = 0; i < 6; ++i) crec[(int64_t)6 * r + i] = cross[(int64_t)6 * n + i];
 }
 
 // ---- mixed tables -------------------------------------------------------------------------------
@@ -129,9 +131,8 @@ template <int D>
 __global__ void __launch_bounds__(TPB) k_lvl_codes(const double* __restrict__ d, int64_t N, double ts0, double ts1, double ts2,
                                                    int8_t* __restrict__ code, int* __restrict__ base_min) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
   int best = 64;
-  for (int dir = 0; dir < 2 * D; ++dir) {
+  for (int dir = 0; dir < 2 * D && n < N; ++dir) {
     const double dv = d[(int64_t)dir * N + n];
     const int a = dir >> 1;
     const double size = a == 0 ? ts0 : (a == 1 ? ts1 : ts2);
@@ -150,7 +151,9 @@ __global__ void __launch_bounds__(TPB) k_lvl_codes(const double* __restrict__ d,
     }
     code[(int64_t)dir * N + n] = c;
   }
-  if (best < 64) atomicMin(base_min, best);
+  // one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0 && best < 64) atomicMin(base_min, best);
 }
 
 // regular: no wall, no correction, one face node with weight 1 and no third-order factor per
@@ -325,19 +328,25 @@ __global__ void __launch_bounds__(TPB) k_perm_keys(const uint8_t* __restrict__ i
                                                    uint64_t* __restrict__ keys, int32_t* __restrict__ vals,
                                                    unsigned long long* __restrict__ counts) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  uint64_t group, pos;
-  if (is_reg[n]) {
-    const bool uni = (meta2[n] >> 30) & 1u, inset = in_x[n] != 0;
-    group = uni ? (inset ? 1 : 0) : (inset ? 2 : 3);
-    pos = (uint64_t)n;
-  } else {
-    group = 4;
-    pos = (uint64_t)irr_rank[n];
+  uint64_t group = 5;  // none: past the end
+  if (n < N) {
+    uint64_t pos;
+    if (is_reg[n]) {
+      const bool uni = (meta2[n] >> 30) & 1u, inset = in_x[n] != 0;
+      group = uni ? (inset ? 1 : 0) : (inset ? 2 : 3);
+      pos = (uint64_t)n;
+    } else {
+      group = 4;
+      pos = (uint64_t)irr_rank[n];
+    }
+    keys[n] = (group << 40) | pos;
+    vals[n] = (int32_t)n;
   }
-  keys[n] = (group << 40) | pos;
-  vals[n] = (int32_t)n;
-  atomicAdd(counts + group, 1ull);
+  // group sizes: one atomic per warp and group
+  for (int g = 0; g < 5; ++g) {
+    const unsigned c = __popc(__ballot_sync(0xffffffffu, group == (uint64_t)g));
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(counts + g, (unsigned long long)c);
+  }
 }
 
 __global__ void __launch_bounds__(TPB) k_iperm(const int32_t* __restrict__ perm, int64_t N, int32_t* __restrict__ iperm) {
@@ -555,13 +564,36 @@ __global__ void __launch_bounds__(TPB) k_tag_leaves(const uint64_t* __restrict__
 
 }  // namespace
 
-// exclusive prefix sum of n int32 values (CUB), temp storage from a grow-only buffer
-static void exclusive_sum(const int32_t* in, int32_t* out, int64_t n, DevBuf<uint8_t>& temp, cudaStream_t s) {
+// One device allocation carved into the temporaries of a build (one allocator call instead of one per
+// temporary). Pieces start on 256-byte boundaries.
+struct Arena {
+  DevBuf<uint8_t> buf;
+  size_t off = 0;
+  template <typename T>
+  static size_t bytes(size_t n) {
+    return (n * sizeof(T) + 255) & ~(size_t)255;
+  }
+  void reserve(size_t total) {
+    buf.alloc(total + 256);
+    off = 0;
+  }
+  template <typename T>
+  T* take(size_t n) {
+    const size_t b = bytes<T>(n);
+    if (off + b > buf.n) throw std::logic_error("device flattener: scratch arena too small");
+    T* p = reinterpret_cast<T*>(buf.p + off);
+    off += b;
+    return p;
+  }
+};
+
+// exclusive prefix sum of n int32 values (CUB)
+static void exclusive_sum(const int32_t* in, int32_t* out, int64_t n, void* temp, size_t temp_bytes, cudaStream_t s) {
   if (n == 0) return;
   size_t bytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)n, s);
-  temp.ensure(bytes + 1);
-  cuda_check(cub::DeviceScan::ExclusiveSum(temp.p, bytes, in, out, (int)n, s), "exclusive scan");
+  if (bytes > temp_bytes) throw std::logic_error("device flattener: scan scratch too small");
+  cuda_check(cub::DeviceScan::ExclusiveSum(temp, bytes, in, out, (int)n, s), "exclusive scan");
 }
 
 // total of a 0/1 flag array given its exclusive scan
@@ -586,23 +618,28 @@ int64_t build_tables64_device(const DForest<D>& F, const Tab64Dev<D>& out, cudaS
   out.cidx->alloc((size_t)N);
   out.wall->alloc((size_t)N);
   out.smin->alloc((size_t)N);
-  DevBuf<int32_t> needs, scan;
-  DevBuf<int> failed;
-  DevBuf<uint8_t> temp;
-  needs.alloc((size_t)N + 1);
-  scan.alloc((size_t)N + 1);
-  failed.alloc(1);
-  cuda_check(cudaMemsetAsync(failed.p, 0, sizeof(int), s), "memset");
-  if (N) k_rows64<D><<<nblocks(N), TPB, 0, s>>>(F, out.nbr->p, out.w->p, out.nrm->p, out.d->p, out.q->p, out.wall->p, out.smin->p, needs.p,
-                                                failed.p);
+  size_t tb = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb, (const int32_t*)nullptr, (int32_t*)nullptr, (int)N, s);
+  tb += 1;
+  Arena A;
+  A.reserve(2 * Arena::bytes<int32_t>((size_t)N + 1) + Arena::bytes<double>((size_t)6 * N + 1) + Arena::bytes<int>(1) +
+            Arena::bytes<uint8_t>(tb));
+  int32_t* needs = A.take<int32_t>((size_t)N + 1);
+  int32_t* scan = A.take<int32_t>((size_t)N + 1);
+  double* cross = A.take<double>((size_t)6 * N + 1);
+  int* failed = A.take<int>(1);
+  void* temp = A.take<uint8_t>(tb);
+  cuda_check(cudaMemsetAsync(failed, 0, sizeof(int), s), "memset");
+  if (N) k_rows64<D><<<nblocks(N), TPB, 0, s>>>(F, out.nbr->p, out.w->p, out.nrm->p, out.d->p, out.q->p, out.wall->p, out.smin->p, needs,
+                                                cross, failed);
   cuda_check(cudaGetLastError(), "device flattener rows");
-  exclusive_sum(needs.p, scan.p, N, temp, s);
+  exclusive_sum(needs, scan, N, temp, tb, s);
   int nfail = 0;
-  cuda_check(cudaMemcpyAsync(&nfail, failed.p, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
-  const int64_t R = scan_total(needs.p, scan.p, N, s);
+  cuda_check(cudaMemcpyAsync(&nfail, failed, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+  const int64_t R = scan_total(needs, scan, N, s);
   if (nfail) throw std::runtime_error("node neighbours: incomplete stencil in a single-process forest");
   out.crec->alloc((size_t)6 * R + 6);
-  if (N) k_crec64<D><<<nblocks(N), TPB, 0, s>>>(F, needs.p, scan.p, out.cidx->p, out.crec->p);
+  if (N) k_crec64<<<nblocks(N), TPB, 0, s>>>(N, needs, scan, cross, out.cidx->p, out.crec->p);
   cuda_check(cudaGetLastError(), "device flattener corrections");
   cuda_check(cudaStreamSynchronize(s), "device flattener");
   return R;
@@ -614,90 +651,97 @@ void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDe
   constexpr int NS = 2 * D * H;
   constexpr int CW = cls_words<D>();
   const int64_t N = T.N;
-  DevBuf<uint8_t> temp, is_reg, in_x;
-  DevBuf<int8_t> code;
-  DevBuf<int> base_min;
-  DevBuf<uint32_t> icount, meta2n;
-  DevBuf<int32_t> irr_flag, irr_pos, slot, slot_sorted, irr_node, flag, excl, node_cls, irr_rank, vals;
-  DevBuf<uint64_t> hash, hash_sorted, keys, keys_sorted;
-  DevBuf<double> rec;
-  DevBuf<unsigned long long> counts;
-  code.alloc((size_t)2 * D * N + 1);
-  base_min.alloc(1);
-  is_reg.alloc((size_t)N + 1);
-  in_x.alloc((size_t)N + 1);
-  icount.alloc((size_t)N + 1);
-  meta2n.alloc((size_t)N + 1);
-  irr_flag.alloc((size_t)N + 1);
-  irr_pos.alloc((size_t)N + 1);
-  node_cls.alloc((size_t)N + 1);
-  irr_rank.alloc((size_t)N + 1);
-  counts.alloc(5);
+  // temporaries sized by N, carved from one allocation
+  size_t tb1 = 0, tsort = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb1, (const int32_t*)nullptr, (int32_t*)nullptr, (int)N, s);
+  cub::DeviceRadixSort::SortPairs(nullptr, tsort, (const uint64_t*)nullptr, (uint64_t*)nullptr, (const int32_t*)nullptr, (int32_t*)nullptr,
+                                  (int)N, 0, 43, s);
+  tb1 = std::max(tb1, tsort) + 1;
+  const size_t N1 = (size_t)N + 1;
+  Arena A;
+  A.reserve(Arena::bytes<int8_t>((size_t)2 * D * N + 1) + Arena::bytes<int>(1) + 2 * Arena::bytes<uint8_t>(N1) +
+            2 * Arena::bytes<uint32_t>(N1) + 5 * Arena::bytes<int32_t>(N1) + 2 * Arena::bytes<uint64_t>(N1) +
+            Arena::bytes<unsigned long long>(5) + Arena::bytes<uint8_t>(tb1));
+  int8_t* code = A.take<int8_t>((size_t)2 * D * N + 1);
+  int* base_min = A.take<int>(1);
+  uint8_t* is_reg = A.take<uint8_t>(N1);
+  uint8_t* in_x = A.take<uint8_t>(N1);
+  uint32_t* icount = A.take<uint32_t>(N1);
+  uint32_t* meta2n = A.take<uint32_t>(N1);
+  int32_t* irr_flag = A.take<int32_t>(N1);
+  int32_t* irr_pos = A.take<int32_t>(N1);
+  int32_t* node_cls = A.take<int32_t>(N1);
+  int32_t* irr_rank = A.take<int32_t>(N1);
+  int32_t* vals = A.take<int32_t>(N1);
+  uint64_t* keys = A.take<uint64_t>(N1);
+  uint64_t* keys_sorted = A.take<uint64_t>(N1);
+  unsigned long long* counts = A.take<unsigned long long>(5);
+  void* temp1 = A.take<uint8_t>(tb1);
   // base level
   int h_base = 64;
-  cuda_check(cudaMemcpyAsync(base_min.p, &h_base, sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
-  if (N) k_lvl_codes<D><<<nblocks(N), TPB, 0, s>>>(T.d, N, ts[0], ts[1], D == 3 ? ts[2] : 1.0, code.p, base_min.p);
-  cuda_check(cudaMemcpyAsync(&h_base, base_min.p, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaMemcpyAsync(base_min, &h_base, sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+  if (N) k_lvl_codes<D><<<nblocks(N), TPB, 0, s>>>(T.d, N, ts[0], ts[1], D == 3 ? ts[2] : 1.0, code, base_min);
+  cuda_check(cudaMemcpyAsync(&h_base, base_min, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
   cuda_check(cudaStreamSynchronize(s), "base level");
   const int base = h_base == 64 ? 0 : h_base;
   M.base = base;
   // classification
-  if (N) k_classify<D><<<nblocks(N), TPB, 0, s>>>(T, code.p, base, is_reg.p, icount.p, irr_flag.p);
-  exclusive_sum(irr_flag.p, irr_pos.p, N, temp, s);
-  const int64_t nI = scan_total(irr_flag.p, irr_pos.p, N, s);
+  if (N) k_classify<D><<<nblocks(N), TPB, 0, s>>>(T, code, base, is_reg, icount, irr_flag);
+  exclusive_sum(irr_flag, irr_pos, N, temp1, tb1, s);
+  const int64_t nI = scan_total(irr_flag, irr_pos, N, s);
   const int64_t nR = N - nI;
-  // geometry classes: records, grouped by hash (stable: node order inside a group), runs of equal records
-  rec.alloc((size_t)nI * CW + 1);
-  hash.alloc((size_t)nI + 1);
-  hash_sorted.alloc((size_t)nI + 1);
-  slot.alloc((size_t)nI + 1);
-  slot_sorted.alloc((size_t)nI + 1);
-  irr_node.alloc((size_t)nI + 1);
-  flag.alloc((size_t)nI + 1);
-  excl.alloc((size_t)nI + 1);
+  // geometry classes: records, grouped by hash (stable: node order inside a group), runs of equal records;
+  // temporaries sized by the irregular count, carved from a second allocation
+  size_t tb2 = 0, tcls = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb2, (const int32_t*)nullptr, (int32_t*)nullptr, (int)nI, s);
+  cub::DeviceRadixSort::SortPairs(nullptr, tcls, (const uint64_t*)nullptr, (uint64_t*)nullptr, (const int32_t*)nullptr, (int32_t*)nullptr,
+                                  (int)nI, 0, 64, s);
+  tb2 = std::max(tb2, tcls) + 1;
+  const size_t I1 = (size_t)nI + 1;
+  Arena B;
+  B.reserve(Arena::bytes<double>((size_t)nI * CW + 1) + 2 * Arena::bytes<uint64_t>(I1) + 5 * Arena::bytes<int32_t>(I1) +
+            Arena::bytes<uint8_t>(tb2));
+  double* rec = B.take<double>((size_t)nI * CW + 1);
+  uint64_t* hash = B.take<uint64_t>(I1);
+  uint64_t* hash_sorted = B.take<uint64_t>(I1);
+  int32_t* slot = B.take<int32_t>(I1);
+  int32_t* slot_sorted = B.take<int32_t>(I1);
+  int32_t* irr_node = B.take<int32_t>(I1);
+  int32_t* flag = B.take<int32_t>(I1);
+  int32_t* excl = B.take<int32_t>(I1);
+  void* temp2 = B.take<uint8_t>(tb2);
   int64_t ncls = 0;
   if (nI) {
-    k_records<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg.p, icount.p, irr_pos.p, rec.p, hash.p, slot.p, irr_node.p);
-    size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, hash.p, hash_sorted.p, slot.p, slot_sorted.p, (int)nI, 0, 64, s);
-    temp.ensure(bytes + 1);
-    cuda_check(cub::DeviceRadixSort::SortPairs(temp.p, bytes, hash.p, hash_sorted.p, slot.p, slot_sorted.p, (int)nI, 0, 64, s),
-               "class sort");
-    k_class_flags<D><<<nblocks(nI), TPB, 0, s>>>(rec.p, slot_sorted.p, nI, flag.p);
-    exclusive_sum(flag.p, excl.p, nI, temp, s);
-    ncls = scan_total(flag.p, excl.p, nI, s);
+    k_records<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg, icount, irr_pos, rec, hash, slot, irr_node);
+    cuda_check(cub::DeviceRadixSort::SortPairs(temp2, tcls, hash, hash_sorted, slot, slot_sorted, (int)nI, 0, 64, s), "class sort");
+    k_class_flags<D><<<nblocks(nI), TPB, 0, s>>>(rec, slot_sorted, nI, flag);
+    exclusive_sum(flag, excl, nI, temp2, tb2, s);
+    ncls = scan_total(flag, excl, nI, s);
   }
   M.cls32->alloc((size_t)ncls * CW + 1);
   DevBuf<double> cls64;
   cls64.alloc((size_t)ncls * CW + 1);
   if (nI)
-    k_class_write<D><<<nblocks(nI), TPB, 0, s>>>(rec.p, slot_sorted.p, irr_node.p, flag.p, excl.p, nI, cls64.p, M.cls32->p, node_cls.p,
-                                                 irr_rank.p);
+    k_class_write<D><<<nblocks(nI), TPB, 0, s>>>(rec, slot_sorted, irr_node, flag, excl, nI, cls64.p, M.cls32->p, node_cls, irr_rank);
   M.ncls = ncls;
   // regular nodes: second neighbours, uniform flag, extended set
-  cuda_check(cudaMemsetAsync(in_x.p, 0, (size_t)N + 1, s), "memset");
-  cuda_check(cudaMemsetAsync(meta2n.p, 0, ((size_t)N + 1) * sizeof(uint32_t), s), "memset");
-  cuda_check(cudaMemsetAsync(counts.p, 0, 5 * sizeof(unsigned long long), s), "memset");
+  cuda_check(cudaMemsetAsync(in_x, 0, N1, s), "memset");
+  cuda_check(cudaMemsetAsync(meta2n, 0, N1 * sizeof(uint32_t), s), "memset");
+  cuda_check(cudaMemsetAsync(counts, 0, 5 * sizeof(unsigned long long), s), "memset");
   if (N) {
-    k_regular_info<D><<<nblocks(N), TPB, 0, s>>>(T, code.p, base, is_reg.p, meta2n.p, in_x.p);
-    k_mark_irregular<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg.p, in_x.p);
+    k_regular_info<D><<<nblocks(N), TPB, 0, s>>>(T, code, base, is_reg, meta2n, in_x);
+    k_mark_irregular<D><<<nblocks(N), TPB, 0, s>>>(T, is_reg, in_x);
   }
   // device order
-  keys.alloc((size_t)N + 1);
-  keys_sorted.alloc((size_t)N + 1);
-  vals.alloc((size_t)N + 1);
   M.perm->alloc((size_t)N);
   M.iperm->alloc((size_t)N);
   if (N) {
-    k_perm_keys<<<nblocks(N), TPB, 0, s>>>(is_reg.p, meta2n.p, in_x.p, irr_rank.p, N, keys.p, vals.p, counts.p);
-    size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys.p, keys_sorted.p, vals.p, M.perm->p, (int)N, 0, 43, s);
-    temp.ensure(bytes + 1);
-    cuda_check(cub::DeviceRadixSort::SortPairs(temp.p, bytes, keys.p, keys_sorted.p, vals.p, M.perm->p, (int)N, 0, 43, s), "order sort");
+    k_perm_keys<<<nblocks(N), TPB, 0, s>>>(is_reg, meta2n, in_x, irr_rank, N, keys, vals, counts);
+    cuda_check(cub::DeviceRadixSort::SortPairs(temp1, tsort, keys, keys_sorted, vals, M.perm->p, (int)N, 0, 43, s), "order sort");
     k_iperm<<<nblocks(N), TPB, 0, s>>>(M.perm->p, N, M.iperm->p);
   }
   unsigned long long g[5] = {0, 0, 0, 0, 0};
-  cuda_check(cudaMemcpyAsync(g, counts.p, sizeof(g), cudaMemcpyDeviceToHost, s), "D2H");
+  cuda_check(cudaMemcpyAsync(g, counts, sizeof(g), cudaMemcpyDeviceToHost, s), "D2H");
   cuda_check(cudaStreamSynchronize(s), "group counts");
   if ((int64_t)(g[0] + g[1] + g[2] + g[3]) != nR || (int64_t)g[4] != nI) throw std::runtime_error("device flattener: group counts");
   M.nR = nR;
@@ -711,7 +755,7 @@ void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDe
   M.r_nbr2->alloc((size_t)2 * D * nR + 1);
   M.r_meta2->alloc((size_t)nR + 1);
   if (nR)
-    k_fill_regular<D><<<nblocks(nR), TPB, 0, s>>>(T, code.p, base, is_reg.p, meta2n.p, M.perm->p, M.iperm->p, nR, M.r_meta->p, M.r_nbr->p,
+    k_fill_regular<D><<<nblocks(nR), TPB, 0, s>>>(T, code, base, is_reg, meta2n, M.perm->p, M.iperm->p, nR, M.r_meta->p, M.r_nbr->p,
                                                   M.r_nbr2->p, M.r_meta2->p);
   // irregular group
   M.i_meta->alloc((size_t)nI + 1);
@@ -725,7 +769,7 @@ void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDe
   M.i_d64->alloc((size_t)2 * D * nI + 1);
   M.i_q64->alloc((size_t)2 * D * (D - 1) * nI + 1);
   DMixedOut O{M.i_meta->p, M.i_cls->p, M.i_nbr->p, M.i_wf->p, M.i_d->p, M.i_q->p, M.i_cidx->p, M.i_wf64->p, M.i_d64->p, M.i_q64->p};
-  if (nI) k_fill_irregular<D><<<nblocks(nI), TPB, 0, s>>>(T, icount.p, node_cls.p, M.perm->p, M.iperm->p, nR, O);
+  if (nI) k_fill_irregular<D><<<nblocks(nI), TPB, 0, s>>>(T, icount, node_cls, M.perm->p, M.iperm->p, nR, O);
   // correction matrices
   M.corr->alloc((size_t)D * D * R + 1);
   M.corr64->alloc((size_t)D * D * R + 1);
@@ -783,25 +827,25 @@ void build_nodes_device(Forest<D>& F, cudaStream_t s) {
   auto X = std::make_shared<ForestDevice<D>>();
   upload_leaves_and_brick(F, *X, s);
   const int64_t nl = X->nl, nc = nl * DD::CHILDREN;
-  DevBuf<uint64_t> corner, sorted;
-  DevBuf<uint8_t> temp;
-  DevBuf<int64_t> nsel;
-  corner.alloc((size_t)nc + 1);
-  sorted.alloc((size_t)nc + 1);
+  size_t b1 = 0, b2 = 0;
+  cub::DeviceRadixSort::SortKeys(nullptr, b1, (const uint64_t*)nullptr, (uint64_t*)nullptr, (int)nc, 0, 64, s);
+  cub::DeviceSelect::Unique(nullptr, b2, (const uint64_t*)nullptr, (uint64_t*)nullptr, (int64_t*)nullptr, (int)nc, s);
+  const size_t tb = std::max(b1, b2) + 1;
+  Arena A;
+  A.reserve(2 * Arena::bytes<uint64_t>((size_t)nc + 1) + Arena::bytes<int64_t>(1) + Arena::bytes<uint8_t>(tb));
+  uint64_t* corner = A.take<uint64_t>((size_t)nc + 1);
+  uint64_t* sorted = A.take<uint64_t>((size_t)nc + 1);
+  int64_t* nsel = A.take<int64_t>(1);
+  void* temp = A.take<uint8_t>(tb);
   X->node_key.alloc((size_t)nc + 1);
-  nsel.alloc(1);
   if (nc) {
     k_corner_keys<D><<<nblocks(nc), TPB, 0, s>>>(X->leaf_key.p, X->level.p, nl, F.brick.n[0], F.brick.n[1], F.brick.n[2], X->tree_ijk.p,
-                                                 X->ijk_to_tree.p, corner.p);
-    size_t b1 = 0, b2 = 0;
-    cub::DeviceRadixSort::SortKeys(nullptr, b1, corner.p, sorted.p, (int)nc, 0, 64, s);
-    cub::DeviceSelect::Unique(nullptr, b2, sorted.p, X->node_key.p, nsel.p, (int)nc, s);
-    temp.ensure(std::max(b1, b2) + 1);
-    cuda_check(cub::DeviceRadixSort::SortKeys(temp.p, b1, corner.p, sorted.p, (int)nc, 0, 64, s), "corner sort");
-    cuda_check(cub::DeviceSelect::Unique(temp.p, b2, sorted.p, X->node_key.p, nsel.p, (int)nc, s), "corner unique");
+                                                 X->ijk_to_tree.p, corner);
+    cuda_check(cub::DeviceRadixSort::SortKeys(temp, b1, corner, sorted, (int)nc, 0, 64, s), "corner sort");
+    cuda_check(cub::DeviceSelect::Unique(temp, b2, sorted, X->node_key.p, nsel, (int)nc, s), "corner unique");
   }
   int64_t nn = 0;
-  if (nc) cuda_check(cudaMemcpyAsync(&nn, nsel.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "D2H");
+  if (nc) cuda_check(cudaMemcpyAsync(&nn, nsel, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "D2H");
   cuda_check(cudaStreamSynchronize(s), "node count");
   if (nn >= (int64_t)INT32_MAX) throw std::runtime_error("too many nodes for 32-bit node indices");
   X->nn = nn;
@@ -809,7 +853,7 @@ void build_nodes_device(Forest<D>& F, cudaStream_t s) {
   X->node_x.alloc((size_t)nn * D + 1);
   X->local_nodes.alloc((size_t)nc + 1);
   if (nn) k_decode_nodes<D><<<nblocks(nn), TPB, 0, s>>>(X->node_key.p, nn, X->node_tree.p, X->node_x.p);
-  if (nc) k_local_nodes<<<nblocks(nc), TPB, 0, s>>>(corner.p, nc, X->node_key.p, nn, X->local_nodes.p);
+  if (nc) k_local_nodes<<<nblocks(nc), TPB, 0, s>>>(corner, nc, X->node_key.p, nn, X->local_nodes.p);
   cuda_check(cudaGetLastError(), "device node numbering");
   F.node_key.resize((size_t)nn);
   F.node_tree.resize((size_t)nn);
