@@ -426,12 +426,14 @@ def run_large(args):
     t0 = time.perf_counter()
     f = G.my_p4est_brick_new([1, 1, 1], [-1, -1, -1], [1, 1, 1])
     f.refine_levelset(shapes.spheres(centres, radii), lmin, lmax, lip=LIP)
-    f.build_nodes()
+    f.build_nodes(device=True)
+    torch.cuda.synchronize()
     t_grid = time.perf_counter() - t0
     phi0 = f.sample(shapes.spheres(centres, radii, scale=(0.1, centres[0])))
     N = f.num_nodes
     t0 = time.perf_counter()
-    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed", device_build=True)
+    torch.cuda.synchronize()
     t_tables = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
@@ -511,7 +513,8 @@ def run_large(args):
                             "mixed_node_steps_per_s": N * 20 / (adv_ms["mixed"] / 1e3),
                             "fp64_node_steps_per_s": N * 20 / (adv_ms["fp64"] / 1e3),
                             "band_linf_mixed_vs_fp64": adv_err, "dt": dt},
-        "autotuned_stage_config": cfg, "setup_s": {"grid": t_grid, "tables": t_tables},
+        "autotuned_stage_config": cfg,
+        "setup_s": {"grid": t_grid, "tables": t_tables, "note": "host refinement, node numbering and tables on the GPU"},
         "device_memory_used_gb": (lambda fr: (fr[1] - fr[0]) / 1e9)(torch.cuda.mem_get_info()),
     }
     print(json.dumps(out), flush=True)

@@ -812,10 +812,10 @@ ForestDevice<D>& forest_device(Forest<D>& F, cudaStream_t s) {
   auto X = std::make_shared<ForestDevice<D>>();
   upload_leaves_and_brick(F, *X, s);
   X->nn = (int64_t)F.num_nodes();
-  X->node_key.upload(F.node_key, s);
-  X->node_tree.upload(F.node_tree, s);
-  X->node_x.upload(F.node_x, s);
-  X->local_nodes.upload(F.local_nodes, s);
+  X->node_key.upload(F.nd->node_key, s);
+  X->node_tree.upload(F.nd->node_tree, s);
+  X->node_x.upload(F.nd->node_x, s);
+  X->local_nodes.upload(F.nd->local_nodes, s);
   cuda_check(cudaStreamSynchronize(s), "forest upload");
   F.device = X;
   return *X;
@@ -855,17 +855,19 @@ void build_nodes_device(Forest<D>& F, cudaStream_t s) {
   if (nn) k_decode_nodes<D><<<nblocks(nn), TPB, 0, s>>>(X->node_key.p, nn, X->node_tree.p, X->node_x.p);
   if (nc) k_local_nodes<<<nblocks(nc), TPB, 0, s>>>(corner, nc, X->node_key.p, nn, X->local_nodes.p);
   cuda_check(cudaGetLastError(), "device node numbering");
-  F.node_key.resize((size_t)nn);
-  F.node_tree.resize((size_t)nn);
-  F.node_x.resize((size_t)nn * D);
-  F.local_nodes.resize((size_t)nc);
+  auto H = std::make_shared<NodeArrays>();
+  H->node_key.resize((size_t)nn);
+  H->node_tree.resize((size_t)nn);
+  H->node_x.resize((size_t)nn * D);
+  H->local_nodes.resize((size_t)nc);
   if (nn) {
-    cuda_check(cudaMemcpyAsync(F.node_key.data(), X->node_key.p, (size_t)nn * 8, cudaMemcpyDeviceToHost, s), "D2H");
-    cuda_check(cudaMemcpyAsync(F.node_tree.data(), X->node_tree.p, (size_t)nn * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    cuda_check(cudaMemcpyAsync(F.node_x.data(), X->node_x.p, (size_t)nn * D * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(H->node_key.data(), X->node_key.p, (size_t)nn * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(H->node_tree.data(), X->node_tree.p, (size_t)nn * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(H->node_x.data(), X->node_x.p, (size_t)nn * D * 4, cudaMemcpyDeviceToHost, s), "D2H");
   }
-  if (nc) cuda_check(cudaMemcpyAsync(F.local_nodes.data(), X->local_nodes.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s), "D2H");
+  if (nc) cuda_check(cudaMemcpyAsync(H->local_nodes.data(), X->local_nodes.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s), "D2H");
   cuda_check(cudaStreamSynchronize(s), "node download");
+  F.nd = H;
   F.nodes_built = true;
   F.device = X;
 }

@@ -79,8 +79,7 @@ void Forest<D>::init(const int* n, const double* xyz_min, const double* xyz_max,
     leaves.push_back(q);
     leaf_key.push_back(((uint64_t)t) << tree_shift<D>());
   }
-  nodes_built = false;
-  device.reset();
+  drop_nodes();
 }
 
 template <int D>
@@ -114,8 +113,7 @@ void Forest<D>::refine(const uint8_t* tags) {
   }
   leaves.swap(out);
   leaf_key.swap(keys);
-  nodes_built = false;
-  device.reset();
+  drop_nodes();
 }
 
 template <int D>
@@ -161,53 +159,109 @@ void Forest<D>::coarsen(const uint8_t* tags) {
   }
   leaves.swap(out);
   leaf_key.swap(keys);
-  nodes_built = false;
-  device.reset();
+  drop_nodes();
 }
 
+// Exclusive prefix sum of cnt[0..n) into off[0..n], off[n] = total; OpenMP blocks of the range each
+// sum their part, then add the totals of the blocks before them.
+static void exclusive_scan_sizes(const uint8_t* cnt, size_t n, std::vector<size_t>& off) {
+  off.assign(n + 1, 0);
+#ifdef _OPENMP
+  const int nt = n > ((size_t)1 << 15) ? omp_get_max_threads() : 1;
+#else
+  const int nt = 1;
+#endif
+  std::vector<size_t> part((size_t)nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num();
+#else
+    const int t = 0;
+#endif
+    const size_t lo = n * (size_t)t / (size_t)nt, hi = n * (size_t)(t + 1) / (size_t)nt;
+    size_t sum = 0;
+    for (size_t i = lo; i < hi; ++i) sum += cnt[i];
+    part[(size_t)t + 1] = sum;
+#pragma omp barrier
+#pragma omp single
+    for (int k = 0; k < nt; ++k) part[(size_t)k + 1] += part[(size_t)k];
+    size_t run = part[(size_t)t];
+    for (size_t i = lo; i < hi; ++i) {
+      off[i] = run;
+      run += cnt[i];
+    }
+  }
+  off[n] = part[(size_t)nt];
+}
+
+// The sequential pass (coarsen every complete family tagged -1 in linear order, then refine the
+// surviving leaves tagged +1) in three parallel sweeps. Families cannot overlap in a linear forest
+// and a family can only start at its first child, so testing every leaf independently finds the same
+// families as the sequential scan; each leaf then emits 0 (inside a family), 1 or CHILDREN leaves at
+// an offset from a prefix sum, in the sequential output order.
 template <int D>
 bool Forest<D>::coarsen_then_refine(const int8_t* tag) {
+  constexpr int C = DD::CHILDREN;
   const size_t nl = leaves.size();
-  const bool had_nodes = nodes_built;
-  std::shared_ptr<void> had_device = device;
-  std::vector<uint8_t> ctag(nl);
-  for (size_t i = 0; i < nl; ++i) ctag[i] = tag[i] < 0;
-  std::vector<Quad> out;
-  std::vector<uint64_t> keys;
-  std::vector<uint8_t> rtag;
-  out.reserve(nl);
-  keys.reserve(nl);
-  rtag.reserve(nl);
-  bool changed = false;
-  size_t i = 0;
-  while (i < nl) {
-    const Quad& q = leaves[i];
-    if (family_at(i, ctag.data())) {
-      Quad p = q;
-      p.level = q.level - 1;
-      out.push_back(p);
-      keys.push_back(leaf_key[i]);
-      rtag.push_back(0);
-      changed = true;
-      i += DD::CHILDREN;
+  std::vector<uint8_t> ctag(nl), fam(nl), cnt(nl);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii) ctag[(size_t)ii] = tag[ii] < 0;
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii) fam[(size_t)ii] = family_at((size_t)ii, ctag.data()) ? 1 : 0;
+  int changed = 0;
+#pragma omp parallel for schedule(static) reduction(| : changed)
+  for (long long ii = 0; ii < (long long)nl; ++ii) {
+    const size_t i = (size_t)ii;
+    bool inside = false;
+    for (int c = 1; c < C && !inside; ++c) inside = i >= (size_t)c && fam[i - (size_t)c];
+    if (fam[i]) {
+      cnt[i] = 1;
+      changed = 1;
+    } else if (inside) {
+      cnt[i] = 0;
+    } else if (tag[i] > 0) {
+      if (leaves[i].level >= DD::QMAXLEVEL) changed |= 2;
+      cnt[i] = (uint8_t)C;
+      changed |= 1;
     } else {
-      out.push_back(q);
-      keys.push_back(leaf_key[i]);
-      rtag.push_back(tag[i] > 0 ? 1 : 0);
-      ++i;
+      cnt[i] = 1;
+    }
+  }
+  if (changed & 2) throw std::invalid_argument("refine: quadrant already at the maximum level");
+  if (!changed) return false;  // same leaves: the node numbering (and its device copy) still holds
+  std::vector<size_t> off;
+  exclusive_scan_sizes(cnt.data(), nl, off);
+  std::vector<Quad> out(off[nl]);
+  std::vector<uint64_t> keys(off[nl]);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nl; ++ii) {
+    const size_t i = (size_t)ii;
+    const size_t o = off[i];
+    const Quad& q = leaves[i];
+    if (cnt[i] == 0) continue;
+    if (fam[i]) {
+      Quad pq = q;
+      pq.level = q.level - 1;
+      out[o] = pq;
+      keys[o] = leaf_key[i];  // the parent starts where its first child does
+    } else if (cnt[i] == 1) {
+      out[o] = q;
+      keys[o] = leaf_key[i];
+    } else {
+      const int32_t h = quadrant_len(DD::MAXLEVEL, q.level + 1);
+      for (int c = 0; c < C; ++c) {
+        Quad ch = q;
+        ch.level = q.level + 1;
+        for (int a = 0; a < D; ++a) ch.x[a] = q.x[a] + (((c >> a) & 1) ? h : 0);
+        out[o + (size_t)c] = ch;
+        keys[o + (size_t)c] = (((uint64_t)ch.tree) << tree_shift<D>()) | morton<D>(ch.x);
+      }
     }
   }
   leaves.swap(out);
   leaf_key.swap(keys);
-  nodes_built = false;
-  device.reset();
-  for (uint8_t t : rtag) changed = changed || t;
-  if (!changed) {
-    nodes_built = had_nodes;  // same leaves: the node numbering (and its device copy) still holds
-    device = had_device;
-    return false;
-  }
-  refine(rtag.data());
+  drop_nodes();
   return true;
 }
 
@@ -227,7 +281,7 @@ void Forest<D>::tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double 
       continue;
     }
     double f[DD::CHILDREN];
-    for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[local_nodes[(size_t)ii * DD::CHILDREN + c]];
+    for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[nd->local_nodes[(size_t)ii * DD::CHILDREN + c]];
     const double* tmn = &brick.tmin[3 * qd.tree];
     const double* tmx = &brick.tmax[3 * qd.tree];
     const double dmin = (double)quadrant_len(DD::MAXLEVEL, qd.level) / (double)DD::ROOT_LEN;
@@ -288,8 +342,7 @@ void Forest<D>::set_leaves(size_t n, const int32_t* tree, const int32_t* level, 
   if (expect_tree != brick.num_trees || expect_key != 0) throw std::invalid_argument("set_leaves: the leaves do not cover every tree");
   leaves.swap(ls);
   leaf_key.swap(keys);
-  nodes_built = false;
-  device.reset();
+  drop_nodes();
 }
 
 template <int D>
@@ -374,6 +427,11 @@ void Forest<D>::build_nodes() {
 #pragma omp parallel for schedule(static)
   for (long long ii = 0; ii < (long long)nl; ++ii)
     for (int c = 0; c < DD::CHILDREN; ++c) corner_key[(size_t)ii * DD::CHILDREN + c] = canon(leaves[(size_t)ii], c);
+  auto A = std::make_shared<NodeArrays>();
+  std::vector<uint64_t>& node_key = A->node_key;
+  std::vector<int32_t>& node_tree = A->node_tree;
+  std::vector<int32_t>& node_x = A->node_x;
+  std::vector<int32_t>& local_nodes = A->local_nodes;
   node_key = corner_key;
   sort_u64(node_key);
   node_key.erase(std::unique(node_key.begin(), node_key.end()), node_key.end());
@@ -399,15 +457,16 @@ void Forest<D>::build_nodes() {
     auto it = std::lower_bound(node_key.begin(), node_key.end(), corner_key[(size_t)ii]);
     local_nodes[(size_t)ii] = (int32_t)(it - node_key.begin());
   }
+  nd = A;
   nodes_built = true;
   device.reset();
 }
 
 template <int D>
 void Forest<D>::node_xyz(int32_t n, double* xyz) const {
-  const int32_t t = node_tree[n];
+  const int32_t t = nd->node_tree[n];
   for (int a = 0; a < D; ++a) {
-    const int32_t v = node_x[(size_t)D * n + a];
+    const int32_t v = nd->node_x[(size_t)D * n + a];
     const double r = (v == DD::ROOT_LEN - 1) ? 1.0 : (double)v / (double)DD::ROOT_LEN;
     xyz[a] = (brick.tmax[3 * t + a] - brick.tmin[3 * t + a]) * r + brick.tmin[3 * t + a];
   }

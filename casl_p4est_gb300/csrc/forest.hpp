@@ -47,17 +47,23 @@ struct Quad {
   int32_t level;
 };
 
+// Node numbering of a forest. Built whole and never changed afterwards, so copies of a forest share
+// one instance (a forest copied before a regrid pays nothing for nodes that the regrid replaces).
+struct NodeArrays {
+  std::vector<int32_t> node_tree;    // owner tree
+  std::vector<int32_t> node_x;       // D per node, clamped logical coordinates in the owner tree
+  std::vector<uint64_t> node_key;
+  std::vector<int32_t> local_nodes;  // CHILDREN per leaf, corner c = xbit + 2 ybit + 4 zbit
+};
+
 template <int D>
 struct Forest {
   using DD = Dim<D>;
   Brick brick;
   std::vector<Quad> leaves;          // tree-major Morton order
   std::vector<uint64_t> leaf_key;    // (tree << D*MAXLEVEL) | morton(x)
-  // node numbering (valid once build_nodes() ran)
-  std::vector<int32_t> node_tree;    // owner tree
-  std::vector<int32_t> node_x;       // D per node, clamped logical coordinates in the owner tree
-  std::vector<uint64_t> node_key;
-  std::vector<int32_t> local_nodes;  // CHILDREN per leaf, corner c = xbit + 2 ybit + 4 zbit
+  // node numbering (valid once build_nodes() ran); replaced as a whole, shared by copies
+  std::shared_ptr<const NodeArrays> nd = std::make_shared<const NodeArrays>();
   bool nodes_built = false;
   // device copy of the leaves and nodes (ForestDevice, flatten.hpp), set by the device node numbering
   // or on first device use, dropped whenever the leaves or the nodes change
@@ -69,6 +75,12 @@ struct Forest {
   // Coarsening pass: each complete family of CHILDREN sibling leaves with all tags set is merged.
   void coarsen(const uint8_t* tags);
   void build_nodes();
+  // the leaves changed: the node numbering and the device copy no longer hold
+  void drop_nodes() {
+    nodes_built = false;
+    nd = std::make_shared<const NodeArrays>();
+    device.reset();
+  }
   // Replace the leaves with a caller-supplied complete linear forest (tree-major Morton order,
   // every tree covered exactly once); throws std::invalid_argument otherwise.
   void set_leaves(size_t n, const int32_t* tree, const int32_t* level, const int32_t* xyz);
@@ -83,7 +95,7 @@ struct Forest {
   void tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double band, const double* phi, int8_t* tag) const;
 
   size_t num_leaves() const { return leaves.size(); }
-  size_t num_nodes() const { return node_tree.size(); }
+  size_t num_nodes() const { return nd->node_tree.size(); }
 
   // Leaf containing the logical point x (0 <= x < ROOT_LEN) of tree `tree`; -1 if none.
   int32_t find_leaf(int32_t tree, const int32_t* x) const;
@@ -94,7 +106,7 @@ struct Forest {
   // Unclamped logical coordinates of a node (p4est_node_unclamp).
   void node_unclamped(int32_t n, int32_t* x) const {
     for (int a = 0; a < D; ++a) {
-      int32_t v = node_x[(size_t)D * n + a];
+      int32_t v = nd->node_x[(size_t)D * n + a];
       x[a] = (v == DD::ROOT_LEN - 1) ? DD::ROOT_LEN : v;
     }
   }

@@ -984,7 +984,7 @@ void LevelSet<D>::build_locator() {
     for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
     loc_key.upload(f.leaf_key, stream);
     loc_level.upload(lvl, stream);
-    loc_nodes.upload(f.local_nodes, stream);
+    loc_nodes.upload(f.nd->local_nodes, stream);
     loc_ijk.upload(f.brick.ijk_to_tree, stream);
     loc_tmin.upload(f.brick.tmin, stream);
     loc_tmax.upload(f.brick.tmax, stream);
