@@ -119,6 +119,8 @@ SIGNATURES = {
     "lsg_level_set_table_stats": (_I, [_P, C.POINTER(_I64)]),
     "lsg_level_set_kernel_times": (_I, [_P, _DP, C.POINTER(_I64), _I, _I]),
     "lsg_level_set_launch_count": (_I64, [_P]),
+    "lsg_device_cache_bytes": (_I64, []),
+    "lsg_device_cache_release": (_I, []),
 }
 
 KERNEL_KINDS = ["dd64", "prep64", "stage64", "advect64", "dd32", "prep_mixed", "stage32", "advect32", "convert", "copy", "interp"]

@@ -1182,4 +1182,10 @@ int64_t lsg_level_set_launch_count(const lsg_level_set* ls) {
   return ls->dim == 2 ? ls->l2->timer.launches : ls->l3->timer.launches;
 }
 
+int64_t lsg_device_cache_bytes(void) { return (int64_t)DeviceCache::get().cached_bytes(); }
+
+int lsg_device_cache_release(void) {
+  return guard([&] { DeviceCache::get().trim(); });
+}
+
 }  // extern "C"

@@ -380,6 +380,14 @@ int lsg_level_set_kernel_times(lsg_level_set* ls, double* ms, int64_t* counts, i
 /* number of kernel launches this object issued since the last kernel-times reset */
 int64_t lsg_level_set_launch_count(const lsg_level_set* ls);
 
+/* ---- device memory (no reference counterpart; PETSc owns the reference's Vec memory) ---------- */
+/* Device memory released by level sets, grids' device copies and temporaries is kept for reuse
+ * (handed out again only after a device synchronisation that follows its release).
+ * lsg_device_cache_bytes: bytes held that way now; lsg_device_cache_release: give them all back to
+ * the driver (synchronises the device). */
+int64_t lsg_device_cache_bytes(void);
+int lsg_device_cache_release(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,14 @@ def test_python_binding_covers_the_header():
     assert set(declared_symbols()) <= set(L.SIGNATURES)
 
 
+def test_device_cache_queries_need_no_device():
+    # nothing allocated yet in this process: nothing cached, and releasing nothing succeeds
+    assert G.device_cache_bytes() >= 0
+    if G.device_cache_bytes() == 0:
+        G.release_device_cache()
+        assert G.device_cache_bytes() == 0
+
+
 def test_bad_arguments_return_status_codes():
     lib = L.load()
     h = C.c_void_p()
