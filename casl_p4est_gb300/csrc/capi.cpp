@@ -55,6 +55,9 @@ int guard(Fn&& fn) {
   } catch (const CudaOutOfMemory& e) {
     g_last_error = e.what();
     return LSG_ENOMEM;
+  } catch (const DeviceTimeout& e) {
+    g_last_error = e.what();
+    return LSG_ETIMEOUT;
   } catch (const CudaError& e) {
     g_last_error = e.what();
     return LSG_EDEVICE;
@@ -1124,7 +1127,7 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config != nullptr, "null config");
     need(config[0] == 32 || config[0] == 64 || config[0] == 128 || config[0] == 256, "threads per block must be 32, 64, 128 or 256");
     need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
-    need(config[3] == 1 || config[3] == 2, "pipeline depth must be 1 or 2");
+    need(config[3] >= 1 && config[3] <= 3, "pipeline depth must be 1, 2 or 3");
     with_ls(ls, [&](auto& L) {
       L.cfg.tpb = config[0];
       L.cfg.uniform_blocks = config[1];

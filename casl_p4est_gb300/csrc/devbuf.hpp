@@ -19,6 +19,10 @@ struct CudaError : std::runtime_error {
 struct CudaOutOfMemory : CudaError {
   using CudaError::CudaError;
 };
+// a bounded device-side wait gave up (reported as LSG_ETIMEOUT)
+struct DeviceTimeout : CudaError {
+  using CudaError::CudaError;
+};
 
 inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));

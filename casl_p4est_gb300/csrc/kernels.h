@@ -24,7 +24,9 @@ struct StageCfg {
   int uniform_blocks = 0;
   int regular_blocks = 0;
   int tpb = 256;
-  int depth = 1;  // pipeline depth of the uniform kernel: nodes whose gathers are in flight per thread
+  // pipeline of the uniform kernel: 1 or 2 nodes whose gathers are in flight per thread, or 3: the
+  // node words bulk-copied into shared memory three tiles ahead (cp.async.bulk + mbarrier)
+  int depth = 1;
 };
 
 template <int D>
@@ -212,9 +214,12 @@ void launch_freeze32(const uint16_t* lim, int it, uint16_t* status, int64_t n, c
 // One RK stage of the mixed reinitialisation is split in three parts that write disjoint node ranges:
 // uniform regular nodes (no dependence on ddx), other regular nodes and irregular nodes (both read ddx).
 enum { STAGE_PART_UNIFORM = 0, STAGE_PART_REGULAR = 1, STAGE_PART_IRREGULAR = 2 };
+// err: device word that a bounded wait of the bulk-copy uniform kernel (cfg.depth 3) sets when it
+// gives up (the kernel then stops; the host reads the word after the call)
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
-                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg);
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg,
+                          int* err);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);

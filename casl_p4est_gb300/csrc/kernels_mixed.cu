@@ -624,6 +624,204 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uin
   }
 }
 
+// ---- uniform kernel with bulk-copied stencil words ------------------------------------------------
+// The same update, with the words each node streams from HBM (status, level code, the 4D face and
+// second-neighbour indices, its own value and the RK partner) moved into shared memory by bulk
+// asynchronous copies (cp.async.bulk, completion counted on an mbarrier) STAGES tiles ahead of the
+// tile being computed. The threads then issue only the gathers of the face values, so the table
+// stream no longer waits on gather latency and needs no registers to stay in flight.
+//
+// A CTA owns tiles blockIdx.x, blockIdx.x + gridDim.x, ... of blockDim.x nodes. Copies start on
+// 16-byte boundaries: a segment starting at element e0 is copied from e0 rounded down to 16 bytes
+// and read at the remainder. A tile is copied only when its node range ends at least 8 nodes before
+// the uniform group does, so every copied byte lies inside its array (a plane of the index tables
+// holds nR >= nU entries); the last tiles load directly from global memory. Every wait on an
+// mbarrier is bounded (about a second of clock cycles); a wait that runs out sets *err and the CTA
+// stops. NPT nodes per thread and tile: the launcher uses one (two measured slower on the 13.7M-node
+// flower grid: fewer, larger tiles leave less room for the concurrent irregular kernels).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// false once about 2^31 SM cycles (about a second) have passed without the phase completing
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > (1ll << 31)) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// segments of a tile: status (u16), level code word, 2D face-index planes, 2D second-neighbour
+// planes, phi_n, and the RK partner when averaging
+template <int D, bool AVG>
+struct UniBulk {
+  static constexpr int NSEG = 2 + 4 * D + 1 + (AVG ? 1 : 0);
+  // bytes of one segment's slot in a stage (tile + 8 elements, 16-byte multiple)
+  static __host__ __device__ uint32_t slot_bytes(int tile, int es) { return (uint32_t)(((tile + 8) * es + 15) & ~15); }
+  static __host__ __device__ uint32_t stage_bytes(int tile) { return slot_bytes(tile, 2) + (NSEG - 1) * slot_bytes(tile, 4); }
+  // global array, element size and first element of segment g for the tile starting at node m0
+  static __device__ __forceinline__ const char* seg(const DTab32<D>& T, const uint16_t* status, const float* phin, const float* avg_with,
+                                                     int g, int64_t m0, int& es, int64_t& e0) {
+    const int64_t nR = T.nR;
+    es = g == 0 ? 2 : 4;
+    if (g == 0) {
+      e0 = m0;
+      return (const char*)status;
+    }
+    if (g == 1) {
+      e0 = m0;
+      return (const char*)T.r_meta;
+    }
+    if (g < 2 + 2 * D) {
+      e0 = (int64_t)(g - 2) * nR + m0;
+      return (const char*)T.r_nbr;
+    }
+    if (g < 2 + 4 * D) {
+      e0 = (int64_t)(g - 2 - 2 * D) * nR + m0;
+      return (const char*)T.r_nbr2;
+    }
+    e0 = m0;
+    return g == 2 + 4 * D ? (const char*)phin : (const char*)avg_with;
+  }
+  static __device__ __forceinline__ uint32_t slot_offset(int tile, int g) { return g == 0 ? 0 : slot_bytes(tile, 2) + (g - 1) * slot_bytes(tile, 4); }
+};
+
+template <int D, bool AVG, int STAGES, int NPT>
+__global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, const uint16_t* __restrict__ status,
+                                                               const float* __restrict__ s_near, const float* __restrict__ phin,
+                                                               float* out, const float* avg_with, int* err) {
+  using B = UniBulk<D, AVG>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[STAGES];
+  const int tile = NPT * blockDim.x;  // NPT nodes per thread and tile
+  const int tid = threadIdx.x;
+  const int64_t nU = T.nU;
+  const int64_t ntiles = (nU + tile - 1) / tile;
+  const uint32_t sb = B::stage_bytes(tile);
+  // tile k of this CTA is copied when it ends at least 8 nodes before the uniform group does
+  auto tile_of = [&](int64_t k) { return (int64_t)blockIdx.x + k * (int64_t)gridDim.x; };
+  auto bulk_ok = [&](int64_t t) { return (t + 1) * (int64_t)tile + 8 <= nU; };
+  auto issue = [&](int64_t t, int s) {  // one thread: arm stage s and copy tile t into it
+    const int64_t m0 = t * (int64_t)tile;
+    uint32_t total = 0;
+    uint32_t bytes[B::NSEG];
+#pragma unroll
+    for (int g = 0; g < B::NSEG; ++g) {
+      int es;
+      int64_t e0;
+      B::seg(T, status, phin, avg_with, g, m0, es, e0);
+      const int ga = 16 / es;
+      const int off = (int)(e0 & (ga - 1));
+      bytes[g] = (uint32_t)(((off + tile + ga - 1) / ga) * ga * es);
+      total += bytes[g];
+    }
+    mbar_arrive_expect_tx(&full[s], total);
+#pragma unroll
+    for (int g = 0; g < B::NSEG; ++g) {
+      int es;
+      int64_t e0;
+      const char* base = B::seg(T, status, phin, avg_with, g, m0, es, e0);
+      const int ga = 16 / es;
+      const int64_t a0 = e0 & ~(int64_t)(ga - 1);
+      bulk_copy_g2s(smem + (size_t)s * sb + B::slot_offset(tile, g), base + a0 * es, bytes[g], &full[s]);
+    }
+  };
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int s = 0; s < STAGES; ++s)
+      if (tile_of(s) < ntiles && bulk_ok(tile_of(s))) issue(tile_of(s), s);
+  const int nR = (int)T.nR;
+  for (int64_t k = 0;; ++k) {
+    const int64_t t = tile_of(k);
+    if (t >= ntiles) break;
+    const int s = (int)(k % STAGES);
+    const int64_t m0 = t * (int64_t)tile;
+    UniIdx<D> I[NPT];
+    bool have[NPT];
+    if (bulk_ok(t)) {
+      if (!mbar_wait_bounded(&full[s], (uint32_t)((k / STAGES) & 1))) {
+        atomicOr(err, 1);
+        if (tid == 0)  // let the copies this CTA issued land (bounded) before it exits
+          for (int64_t kk = k; kk < k + STAGES; ++kk)
+            if (tile_of(kk) < ntiles && bulk_ok(tile_of(kk))) mbar_wait_bounded(&full[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
+        return;
+      }
+      const unsigned char* st = smem + (size_t)s * sb;
+      auto word = [&](int g, int li) -> uint32_t {
+        int es;
+        int64_t e0;
+        B::seg(T, status, phin, avg_with, g, m0, es, e0);
+        return reinterpret_cast<const uint32_t*>(st + B::slot_offset(tile, g))[(int)(e0 & 3) + li];
+      };
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+        const int li = tid + j * blockDim.x;
+        I[j].n = (int)(m0 + li);
+        I[j].st = reinterpret_cast<const uint16_t*>(st)[(int)(m0 & 7) + li];
+        I[j].code = word(1, li) & 15u;
+#pragma unroll
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          I[j].nb[dir] = (int32_t)word(2 + dir, li);
+          I[j].nb2[dir] = (int32_t)word(2 + 2 * D + dir, li);
+        }
+        I[j].f0 = __uint_as_float(word(2 + 4 * D, li));
+        I[j].avg = AVG ? __uint_as_float(word(3 + 4 * D, li)) : 0.0f;
+        have[j] = true;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+        const int64_t m = m0 + tid + j * blockDim.x;
+        have[j] = m < nU;
+        if (have[j]) uni_load<D, AVG>(T, nR, status, phin, avg_with, (int)m, I[j]);
+      }
+    }
+    UniVal<D> V[NPT];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+      if (have[j]) uni_gather<D>(I[j], phin, V[j]);
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+      if (have[j]) out[V[j].n] = uni_update<D, AVG>(T, s_near, V[j]);
+    __syncthreads();  // every thread is done with stage s
+    if (tid == 0) {
+      const int64_t tn = tile_of(k + STAGES);
+      if (tn < ntiles && bulk_ok(tn)) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the reads above come before the copy's writes
+        issue(tn, s);
+      }
+    }
+  }
+}
+
 template <int D, bool AVG>
 __global__ void __launch_bounds__(TPB) k_advect_stage32(DTab32<D> T, const float* __restrict__ phin, const float* __restrict__ ddq,
                                                         const float* __restrict__ ddm, const float* __restrict__ vn, float dt,
@@ -980,9 +1178,16 @@ static int persistent_blocks(const void* kernel) {
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 
+// the bulk copies read 16-byte aligned spans from the bases of these arrays
+template <int D>
+static bool uniform_bulk_ok(const DTab32<D>& T, const uint16_t* status, const float* phin, const float* avg_with) {
+  auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+  return al(status) && al(phin) && al(avg_with) && al(T.r_meta) && al(T.r_nbr) && al(T.r_nbr2);
+}
+
 template <int D, int OS, bool AVG>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
-                         float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg) {
+                         float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg, int* err) {
   static int gb_reg = 0, gb_uni = 0, gb_uni2 = 0;
   if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
   if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1>);
@@ -999,7 +1204,26 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
     k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(T.nR - uni_end)), tpb, 0, s>>>(
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
   }
-  if (part == STAGE_PART_UNIFORM && uni_end > 0) {
+  if (part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth == 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
+    using B = UniBulk<D, AVG>;
+    constexpr int STAGES = 3;
+    const uint32_t smem = STAGES * B::stage_bytes(tpb);
+    auto kern = k_reinit_uniform32_bulk<D, AVG, STAGES, 1>;
+    static int configured_tpb = 0, per_sm = 0;
+    if (configured_tpb != tpb) {
+      // a failure here makes the launch below fail, which the caller's cudaGetLastError reports
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
+      configured_tpb = tpb;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int full = sms * (per_sm > 0 ? per_sm : 1);
+    const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
+    const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
+    kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err);
+  } else if (part == STAGE_PART_UNIFORM && uni_end > 0) {
     const int full = (cfg.depth == 2 ? gb_uni2 : gb_uni) * scale;
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
     const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
@@ -1012,14 +1236,15 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
 
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
-                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg) {
+                          const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg,
+                          int* err) {
   if (T.N == 0) return;
   if (order_space > 1) {
-    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
-    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
+    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
+    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
   } else {
-    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
-    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg);
+    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
+    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
   }
 }
 
@@ -1052,7 +1277,7 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
                                          const float*, cudaStream_t);                                                           \
   template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t, int);                                  \
   template void launch_reinit_part32<D>(const DTab32<D>&, int, int, const uint16_t*, const float*, const float*, const float*,  \
-                                        float*, const float*, cudaStream_t, const StageCfg&);
+                                        float*, const float*, cudaStream_t, const StageCfg&, int*);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

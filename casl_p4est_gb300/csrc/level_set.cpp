@@ -347,6 +347,8 @@ void LevelSet<D>::set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int bas
   nR = nR_;
   nI = nI_;
   ncls = ncls_;
+  kerr.alloc(1);
+  cuda_check(cudaMemsetAsync(kerr.p, 0, sizeof(int), stream), "memset");
   T32.N = N;
   T32.nR = nR_;
   T32.nI = nI_;
@@ -377,6 +379,21 @@ void LevelSet<D>::set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int bas
   mixed_ready = true;
 }
 
+template <int D>
+void LevelSet<D>::check_device_waits() {
+  if (!kerr.p) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cuda_check(cudaStreamIsCapturing(stream, &cs), "cudaStreamIsCapturing");
+  if (cs != cudaStreamCaptureStatusNone) return;
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, kerr.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H");
+  cuda_check(cudaStreamSynchronize(stream), "device wait check");
+  if (h) {
+    cuda_check(cudaMemsetAsync(kerr.p, 0, sizeof(int), stream), "memset");
+    throw DeviceTimeout("reinitialize (mixed): a bounded wait for a bulk copy gave up; results of this call are incomplete");
+  }
+}
+
 // One RK stage of the mixed path on two streams: the side stream computes the extended second
 // derivatives and then the irregular nodes while the main stream runs the uniform regular nodes;
 // the remaining regular nodes follow once the extended second derivatives are ready.
@@ -397,11 +414,11 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
   cuda_check(cudaStreamWaitEvent(side_stream, ev_fork, 0), "cudaStreamWaitEvent");
   launch_dd_x32<D>(T32, phin, f_dd.p, side_stream, cfg.tpb);
   cuda_check(cudaEventRecord(ev_ddx, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, cfg);
+  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, cfg, kerr.p);
   cuda_check(cudaEventRecord(ev_join, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg);
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
   cuda_check(cudaStreamWaitEvent(stream, ev_ddx, 0), "cudaStreamWaitEvent");
-  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg);
+  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
   cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
   timer.end(stream);
   timer.launches += 3;  // four kernels per stage
@@ -435,6 +452,7 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   }
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
+  if (cfg.depth == 3) check_device_waits();
 }
 
 template <int D>
@@ -553,6 +571,7 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
   }
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream, iter_lim.p));
   cuda_check(cudaGetLastError(), "reinitialize (batch)");
+  if (cfg.depth == 3) check_device_waits();
 }
 
 // Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, pipeline
@@ -593,7 +612,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     StageCfg c;
     c.tpb = tpb;
     float c_ms = 1e30f;
-    for (int depth : {1, 2})
+    for (int depth : {1, 2, 3})
       for (int g : grids) {
         StageCfg t = c;
         t.depth = depth;
@@ -624,6 +643,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
   timer.enabled = timing;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  check_device_waits();
   drop_graph();  // launch shapes are baked into a captured graph
   cuda_check(cudaGetLastError(), "autotune");
 }

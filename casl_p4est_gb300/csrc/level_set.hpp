@@ -54,6 +54,7 @@ struct LevelSet {
   cudaStream_t side_stream = nullptr;  // second stream of the mixed stage (fork/join with events)
   cudaEvent_t ev_fork = nullptr, ev_ddx = nullptr, ev_join = nullptr;
   StageCfg cfg;                        // launch shape of the mixed stage kernels (see autotune)
+  DevBuf<int> kerr;                    // set by a device-side wait that gave up (bulk-copy uniform kernel)
   int64_t num_corrections = 0;
 
   // FP64 tables
@@ -218,6 +219,9 @@ struct LevelSet {
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
+  // throws DeviceTimeout if a bounded device-side wait gave up since the last check (synchronises the
+  // stream; skipped while the stream is being captured)
+  void check_device_waits();
   void build_locator();
   void build_gradient();
   const double* derivatives_of(int nf, const double* F, const double* Fdd, DevBuf<double>& store);

@@ -356,10 +356,12 @@ int lsg_batch_reinitialize(lsg_level_set* batch, double* phi, const int* iterati
 int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const int* iterations, int use_graph);
 /* Launch shape of the mixed stage kernels, four ints: config[0] threads per block (32..256),
  * config[1] grid of the persistent uniform-stencil kernel, config[2] grid of the persistent regular
- * kernel (0: one full wave), config[3] pipeline depth of the uniform kernel (1 or 2 nodes in flight
- * per thread). lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials`
- * iterations each, keeps the fastest and returns it in config (may be NULL). Results do not depend
- * on the shape. */
+ * kernel (0: one full wave), config[3] pipeline of the uniform kernel (1 or 2 nodes in flight per
+ * thread, or 3: the nodes' table words bulk-copied into shared memory three tiles ahead; a bounded
+ * wait of that kernel that gives up makes the call return LSG_ETIMEOUT).
+ * lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials` iterations
+ * each, keeps the fastest and returns it in config (may be NULL). Results do not depend on the
+ * shape. */
 int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int* config);
 int lsg_level_set_stage_config(const lsg_level_set* ls, int* config);
 int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config);

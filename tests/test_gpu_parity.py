@@ -173,12 +173,15 @@ def test_band_linf_device_matches_numpy():
     assert np.isnan(val)
 
 
-@pytest.mark.parametrize("shape", [(256, 0, 0, 1), (128, 912, 304, 2), (64, 152, 0, 2)])
-def test_mixed_result_independent_of_launch_shape(shape):
+@pytest.mark.parametrize("shape", [(256, 0, 0, 1), (128, 912, 304, 2), (64, 152, 0, 2), (256, 0, 0, 3), (256, 4, 0, 3),
+                                   (32, 2, 304, 3), (128, 608, 0, 3)])
+@pytest.mark.parametrize("grid", ["flower3d", "circle2d"])
+def test_mixed_result_independent_of_launch_shape(shape, grid):
     """The mixed stages are Jacobi updates: threads per block, persistent grids and the uniform kernel's
-    pipeline depth change no bit of the result."""
-    f = flower_3d(3, 6)
-    phi0 = phi0_flower_3d(f)
+    pipeline (depth 3: bulk-copied tiles; a grid of 2 or 4 CTAs makes every CTA cycle through its three
+    stages many times) change no bit of the result."""
+    f = flower_3d(3, 6) if grid == "flower3d" else circle_2d(3, 9)
+    phi0 = phi0_flower_3d(f) if grid == "flower3d" else phi0_circle_2d(f)
     ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
     ref = phi0.copy()
     ls.reinitialize_2nd_order(ref, 7)
