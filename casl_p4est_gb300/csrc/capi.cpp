@@ -466,9 +466,9 @@ int lsg_forest_nodes(const lsg_forest* f, int32_t* tree, int32_t* xyz) {
       using FT = std::decay_t<decltype(F)>;
       constexpr int D = FT::DD::CHILDREN == 4 ? 2 : 3;
       for (size_t n = 0; n < F.num_nodes(); ++n) {
-        if (tree) tree[n] = F.nd->node_tree[n];
+        if (tree) tree[n] = F.nd->host().node_tree[n];
         if (xyz)
-          for (int a = 0; a < 3; ++a) xyz[3 * n + a] = a < D ? F.nd->node_x[D * n + a] : 0;
+          for (int a = 0; a < 3; ++a) xyz[3 * n + a] = a < D ? F.nd->host().node_x[D * n + a] : 0;
       }
     });
   });
@@ -479,7 +479,7 @@ int lsg_forest_local_nodes(const lsg_forest* f, int32_t* out) {
     need(out != nullptr, "null output");
     with_forest(f, [&](auto& F) {
       need_nodes(F);
-      memcpy(out, F.nd->local_nodes.data(), F.nd->local_nodes.size() * sizeof(int32_t));
+      memcpy(out, F.nd->host().local_nodes.data(), F.nd->host().local_nodes.size() * sizeof(int32_t));
     });
   });
 }

@@ -812,10 +812,11 @@ ForestDevice<D>& forest_device(Forest<D>& F, cudaStream_t s) {
   auto X = std::make_shared<ForestDevice<D>>();
   upload_leaves_and_brick(F, *X, s);
   X->nn = (int64_t)F.num_nodes();
-  X->node_key.upload(F.nd->node_key, s);
-  X->node_tree.upload(F.nd->node_tree, s);
-  X->node_x.upload(F.nd->node_x, s);
-  X->local_nodes.upload(F.nd->local_nodes, s);
+  const NodeArrays& A = F.nd->host();
+  X->node_key.upload(A.node_key, s);
+  X->node_tree.upload(A.node_tree, s);
+  X->node_x.upload(A.node_x, s);
+  X->local_nodes.upload(A.local_nodes, s);
   cuda_check(cudaStreamSynchronize(s), "forest upload");
   F.device = X;
   return *X;
@@ -855,21 +856,55 @@ void build_nodes_device(Forest<D>& F, cudaStream_t s) {
   if (nn) k_decode_nodes<D><<<nblocks(nn), TPB, 0, s>>>(X->node_key.p, nn, X->node_tree.p, X->node_x.p);
   if (nc) k_local_nodes<<<nblocks(nc), TPB, 0, s>>>(corner, nc, X->node_key.p, nn, X->local_nodes.p);
   cuda_check(cudaGetLastError(), "device node numbering");
+  // the host copies of the arrays are made on first host use
   auto H = std::make_shared<NodeArrays>();
-  H->node_key.resize((size_t)nn);
-  H->node_tree.resize((size_t)nn);
-  H->node_x.resize((size_t)nn * D);
-  H->local_nodes.resize((size_t)nc);
-  if (nn) {
-    cuda_check(cudaMemcpyAsync(H->node_key.data(), X->node_key.p, (size_t)nn * 8, cudaMemcpyDeviceToHost, s), "D2H");
-    cuda_check(cudaMemcpyAsync(H->node_tree.data(), X->node_tree.p, (size_t)nn * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    cuda_check(cudaMemcpyAsync(H->node_x.data(), X->node_x.p, (size_t)nn * D * 4, cudaMemcpyDeviceToHost, s), "D2H");
-  }
-  if (nc) cuda_check(cudaMemcpyAsync(H->local_nodes.data(), X->local_nodes.p, (size_t)nc * 4, cudaMemcpyDeviceToHost, s), "D2H");
-  cuda_check(cudaStreamSynchronize(s), "node download");
+  H->count = (size_t)nn;
+  std::shared_ptr<const ForestDevice<D>> Xc = X;
+  H->fetch = [Xc, nn, nc](NodeArrays& A) {
+    A.node_key.resize((size_t)nn);
+    A.node_tree.resize((size_t)nn);
+    A.node_x.resize((size_t)nn * D);
+    A.local_nodes.resize((size_t)nc);
+    if (nn) {
+      cuda_check(cudaMemcpy(A.node_key.data(), Xc->node_key.p, (size_t)nn * 8, cudaMemcpyDeviceToHost), "D2H");
+      cuda_check(cudaMemcpy(A.node_tree.data(), Xc->node_tree.p, (size_t)nn * 4, cudaMemcpyDeviceToHost), "D2H");
+      cuda_check(cudaMemcpy(A.node_x.data(), Xc->node_x.p, (size_t)nn * D * 4, cudaMemcpyDeviceToHost), "D2H");
+    }
+    if (nc) cuda_check(cudaMemcpy(A.local_nodes.data(), Xc->local_nodes.p, (size_t)nc * 4, cudaMemcpyDeviceToHost), "D2H");
+  };
+  cuda_check(cudaStreamSynchronize(s), "device node numbering");
   F.nd = H;
   F.nodes_built = true;
   F.device = X;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TPB) k_coarse_table(const uint64_t* __restrict__ key, int64_t nl, int64_t ncells, int64_t ncoarse, int L0,
+                                                      int32_t* __restrict__ ctab) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > ncells) return;
+  if (i == ncells) {
+    ctab[i] = (int32_t)(nl - 1);
+    return;
+  }
+  const uint64_t t = (uint64_t)(i / ncoarse), c = (uint64_t)(i % ncoarse);
+  const uint64_t k = (t << tree_shift<D>()) | (c << (D * (Dim<D>::MAXLEVEL - L0)));
+  int64_t lo = 0, hi = nl - 1;  // the last leaf with key <= k, else 0
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (key[mid] <= k)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  ctab[i] = (int32_t)lo;
+}
+
+template <int D>
+void coarse_table_device(const uint64_t* leaf_key, int64_t nl, int nt, int L0, int32_t* ctab, cudaStream_t s) {
+  const int64_t ncoarse = int64_t(1) << (D * L0), ncells = (int64_t)nt * ncoarse;
+  k_coarse_table<D><<<nblocks(ncells + 1), TPB, 0, s>>>(leaf_key, nl, ncells, ncoarse, L0, ctab);
+  cuda_check(cudaGetLastError(), "coarse cell table");
 }
 
 template <int D>
@@ -898,6 +933,7 @@ bool refine_and_coarsen_device(Forest<D>& F, int min_lvl, int max_lvl, double li
   template void build_nodes_device<D>(Forest<D>&, cudaStream_t);                             \
   template ForestDevice<D>& forest_device<D>(Forest<D>&, cudaStream_t);                      \
   template void node_xyz_device<D>(Forest<D>&, double*, cudaStream_t);                       \
+  template void coarse_table_device<D>(const uint64_t*, int64_t, int, int, int32_t*, cudaStream_t); \
   template bool refine_and_coarsen_device<D>(Forest<D>&, int, int, double, double, const double*, cudaStream_t); \
   template int64_t build_tables64_device<D>(const DForest<D>&, const Tab64Dev<D>&, cudaStream_t); \
   template void build_mixed_device<D>(const DTab64<D>&, int64_t, const double*, MixedDev<D>&, cudaStream_t);

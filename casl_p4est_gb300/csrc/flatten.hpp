@@ -42,10 +42,15 @@ struct ForestDevice {
   DevBuf<double> tmin, tmax;
 };
 
-// Node numbering on the device (the same keys, order and corner map as Forest::build_nodes), copied
-// back into the forest's host arrays; the device copy stays attached to the forest.
+// Node numbering on the device (the same keys, order and corner map as Forest::build_nodes); the
+// device copy stays attached to the forest and the host arrays are copied down on first host use.
 template <int D>
 void build_nodes_device(Forest<D>& F, cudaStream_t s);
+// Coarse-cell table of point location: for each cell i of the uniform level L0 in each tree (ncoarse
+// cells per tree, nt trees), the last leaf whose key is <= the cell's first point (0 if none), and
+// ctab[nt * ncoarse] = nl - 1; from the sorted leaf keys on the device.
+template <int D>
+void coarse_table_device(const uint64_t* leaf_key, int64_t nl, int nt, int L0, int32_t* ctab, cudaStream_t s);
 // The forest's device copy, uploaded from the host arrays if the forest has none (nodes must be built).
 template <int D>
 ForestDevice<D>& forest_device(Forest<D>& F, cudaStream_t s);

@@ -269,6 +269,7 @@ template <int D>
 void Forest<D>::tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double band, const double* phi, int8_t* tag) const {
   if (!nodes_built) throw std::invalid_argument("refine_and_coarsen: the forest's nodes are not built");
   const size_t nl = leaves.size();
+  const std::vector<int32_t>& ln = nd->host().local_nodes;
 #pragma omp parallel for schedule(static)
   for (long long ii = 0; ii < (long long)nl; ++ii) {
     const Quad& qd = leaves[(size_t)ii];
@@ -281,7 +282,7 @@ void Forest<D>::tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double 
       continue;
     }
     double f[DD::CHILDREN];
-    for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[nd->local_nodes[(size_t)ii * DD::CHILDREN + c]];
+    for (int c = 0; c < DD::CHILDREN; ++c) f[c] = phi[ln[(size_t)ii * DD::CHILDREN + c]];
     const double* tmn = &brick.tmin[3 * qd.tree];
     const double* tmx = &brick.tmax[3 * qd.tree];
     const double dmin = (double)quadrant_len(DD::MAXLEVEL, qd.level) / (double)DD::ROOT_LEN;
@@ -457,6 +458,7 @@ void Forest<D>::build_nodes() {
     auto it = std::lower_bound(node_key.begin(), node_key.end(), corner_key[(size_t)ii]);
     local_nodes[(size_t)ii] = (int32_t)(it - node_key.begin());
   }
+  A->count = nn;
   nd = A;
   nodes_built = true;
   device.reset();
@@ -464,9 +466,10 @@ void Forest<D>::build_nodes() {
 
 template <int D>
 void Forest<D>::node_xyz(int32_t n, double* xyz) const {
-  const int32_t t = nd->node_tree[n];
+  const NodeArrays& A = nd->host();
+  const int32_t t = A.node_tree[n];
   for (int a = 0; a < D; ++a) {
-    const int32_t v = nd->node_x[(size_t)D * n + a];
+    const int32_t v = A.node_x[(size_t)D * n + a];
     const double r = (v == DD::ROOT_LEN - 1) ? 1.0 : (double)v / (double)DD::ROOT_LEN;
     xyz[a] = (brick.tmax[3 * t + a] - brick.tmin[3 * t + a]) * r + brick.tmin[3 * t + a];
   }

@@ -17,9 +17,11 @@
 #pragma once
 #include <stdint.h>
 
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
-#include <memory>
 #include <vector>
 
 #include "lsg_common.h"
@@ -49,11 +51,23 @@ struct Quad {
 
 // Node numbering of a forest. Built whole and never changed afterwards, so copies of a forest share
 // one instance (a forest copied before a regrid pays nothing for nodes that the regrid replaces).
+// A numbering made on the device stays there until host code first reads the arrays: host() copies
+// them down once (fetch), so a regrid loop that only feeds device kernels never downloads them.
 struct NodeArrays {
+  size_t count = 0;                  // number of nodes
   std::vector<int32_t> node_tree;    // owner tree
   std::vector<int32_t> node_x;       // D per node, clamped logical coordinates in the owner tree
   std::vector<uint64_t> node_key;
   std::vector<int32_t> local_nodes;  // CHILDREN per leaf, corner c = xbit + 2 ybit + 4 zbit
+  std::function<void(NodeArrays&)> fetch;  // fills the vectors from the device copy (device numbering)
+
+  const NodeArrays& host() const {
+    if (fetch) std::call_once(fetched_, [this] { fetch(const_cast<NodeArrays&>(*this)); });
+    return *this;
+  }
+
+ private:
+  mutable std::once_flag fetched_;
 };
 
 template <int D>
@@ -95,7 +109,7 @@ struct Forest {
   void tag_refine_coarsen(int min_lvl, int max_lvl, double lip, double band, const double* phi, int8_t* tag) const;
 
   size_t num_leaves() const { return leaves.size(); }
-  size_t num_nodes() const { return nd->node_tree.size(); }
+  size_t num_nodes() const { return nd->count; }
 
   // Leaf containing the logical point x (0 <= x < ROOT_LEN) of tree `tree`; -1 if none.
   int32_t find_leaf(int32_t tree, const int32_t* x) const;
@@ -106,7 +120,7 @@ struct Forest {
   // Unclamped logical coordinates of a node (p4est_node_unclamp).
   void node_unclamped(int32_t n, int32_t* x) const {
     for (int a = 0; a < D; ++a) {
-      int32_t v = nd->node_x[(size_t)D * n + a];
+      int32_t v = nd->host().node_x[(size_t)D * n + a];
       x[a] = (v == DD::ROOT_LEN - 1) ? DD::ROOT_LEN : v;
     }
   }

@@ -157,7 +157,7 @@ void vtk_write_all(const Forest<D>& F, const std::string& filename, bool write_t
     data_array(f, "Float64", "Position", 3, pos, binary);
     s = "      </Points>\n      <Cells>\n";
     f.write(s.data(), s.size());
-    std::vector<int32_t> conn(F.nd->local_nodes.begin(), F.nd->local_nodes.end()), offs(nc);
+    std::vector<int32_t> conn(F.nd->host().local_nodes.begin(), F.nd->host().local_nodes.end()), offs(nc);
     for (size_t c = 0; c < nc; ++c) offs[c] = (int32_t)(CH * (c + 1));
     std::vector<uint8_t> types(nc, (uint8_t)(D == 3 ? 11 : 8));  // VTK_VOXEL / VTK_PIXEL
     data_array(f, "Int32", "connectivity", 1, conn, binary);

@@ -979,17 +979,24 @@ void LevelSet<D>::build_locator() {
   int L0 = 0;
   while (L0 < DD::MAXLEVEL && ((int64_t)nt << (D * (L0 + 1))) <= 2 * nl) ++L0;
   const int64_t ncoarse = int64_t(1) << (D * L0);
-  std::vector<int32_t> ctab((size_t)(nt * ncoarse + 1));
-  // merge the coarse cells' first points (in key order) with the sorted leaf keys
-  int64_t j = 0;
-  for (int64_t i = 0; i < nt * ncoarse; ++i) {
-    const uint64_t t = (uint64_t)(i / ncoarse), c = (uint64_t)(i % ncoarse);
-    const uint64_t key = (t << tree_shift<D>()) | (c << (D * (DD::MAXLEVEL - L0)));
-    while (j + 1 < nl && f.leaf_key[(size_t)(j + 1)] <= key) ++j;
-    ctab[(size_t)i] = (int32_t)j;
+  if (fdev) {
+    // the coarse-cell table by binary searches over the device copy's leaf keys
+    const ForestDevice<D>& X = *static_cast<const ForestDevice<D>*>(fdev.get());
+    loc_ctab.alloc((size_t)(nt * ncoarse + 1));
+    coarse_table_device<D>(X.leaf_key.p, nl, nt, L0, loc_ctab.p, stream);
+  } else {
+    std::vector<int32_t> ctab((size_t)(nt * ncoarse + 1));
+    // merge the coarse cells' first points (in key order) with the sorted leaf keys
+    int64_t j = 0;
+    for (int64_t i = 0; i < nt * ncoarse; ++i) {
+      const uint64_t t = (uint64_t)(i / ncoarse), c = (uint64_t)(i % ncoarse);
+      const uint64_t key = (t << tree_shift<D>()) | (c << (D * (DD::MAXLEVEL - L0)));
+      while (j + 1 < nl && f.leaf_key[(size_t)(j + 1)] <= key) ++j;
+      ctab[(size_t)i] = (int32_t)j;
+    }
+    ctab[(size_t)(nt * ncoarse)] = (int32_t)(nl - 1);
+    loc_ctab.upload(ctab, stream);
   }
-  ctab[(size_t)(nt * ncoarse)] = (int32_t)(nl - 1);
-  loc_ctab.upload(ctab, stream);
   if (fdev) {
     // the forest's device copy already holds the leaves, corner nodes and brick
     const ForestDevice<D>& X = *static_cast<const ForestDevice<D>*>(fdev.get());
@@ -1004,7 +1011,7 @@ void LevelSet<D>::build_locator() {
     for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
     loc_key.upload(f.leaf_key, stream);
     loc_level.upload(lvl, stream);
-    loc_nodes.upload(f.nd->local_nodes, stream);
+    loc_nodes.upload(f.nd->host().local_nodes, stream);
     loc_ijk.upload(f.brick.ijk_to_tree, stream);
     loc_tmin.upload(f.brick.tmin, stream);
     loc_tmax.upload(f.brick.tmax, stream);

@@ -40,8 +40,9 @@ struct Qnnn {
 template <int D>
 struct HostForestView {
   const Forest<D>& F;
-  int32_t node_tree(int32_t n) const { return F.nd->node_tree[n]; }
-  int32_t node_x(int32_t n, int a) const { return F.nd->node_x[(size_t)D * n + a]; }
+  const NodeArrays& A = F.nd->host();
+  int32_t node_tree(int32_t n) const { return A.node_tree[n]; }
+  int32_t node_x(int32_t n, int a) const { return A.node_x[(size_t)D * n + a]; }
   void node_unclamped(int32_t n, int32_t* x) const { F.node_unclamped(n, x); }
   int nt(int a) const { return F.brick.n[a]; }
   int tree_ijk(int32_t t, int a) const { return F.brick.tree_ijk[3 * t + a]; }
@@ -52,7 +53,7 @@ struct HostForestView {
   int leaf_level(int32_t q) const { return F.leaves[q].level; }
   int32_t leaf_tree(int32_t q) const { return F.leaves[q].tree; }
   int32_t leaf_x(int32_t q, int a) const { return F.leaves[q].x[a]; }
-  int32_t local_node(int32_t q, int c) const { return F.nd->local_nodes[(size_t)Dim<D>::CHILDREN * q + c]; }
+  int32_t local_node(int32_t q, int c) const { return A.local_nodes[(size_t)Dim<D>::CHILDREN * q + c]; }
 };
 
 // find_neighbor_cell_of_node (src/my_p4est_hierarchy.cpp:569-600): perturb the unclamped node by one

@@ -104,7 +104,7 @@ void build_corner_neighbors(const Forest<D>& F, std::vector<int32_t>& out) {
       find_neighbor_cell_of_node<D>(F, n, c, quad, tree);
       cell[v] = quad;
     }
-    auto node = [&](int32_t quad, int v) { return F.nd->local_nodes[(size_t)quad * CH + v]; };
+    auto node = [&](int32_t quad, int v) { return F.nd->host().local_nodes[(size_t)quad * CH + v]; };
     auto pick = [&](int c1, int v1, int c2, int v2) -> int32_t {
       return cell[c1] >= 0 ? node(cell[c1], v1) : (cell[c2] >= 0 ? node(cell[c2], v2) : -1);
     };
