@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(TPB) k_node_xyz(const int32_t* __restrict__ no
 template <int D>
 static void upload_leaves_and_brick(const Forest<D>& F, ForestDevice<D>& X, cudaStream_t s) {
   X.nl = (int64_t)F.leaves.size();
-  X.leaf_key.upload(F.leaf_key, s);
+  X.leaf_key.upload(F.leaf_key.vec(), s);
   std::vector<int8_t> lvl((size_t)X.nl);
   for (int64_t q = 0; q < X.nl; ++q) lvl[(size_t)q] = (int8_t)F.leaves[(size_t)q].level;
   X.level.upload(lvl, s);

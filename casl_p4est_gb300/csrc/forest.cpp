@@ -69,16 +69,18 @@ void Forest<D>::init(const int* n, const double* xyz_min, const double* xyz_max,
   for (int a = 0; a < D; ++a)
     if (brick.periodic[a]) throw std::invalid_argument("periodic bricks are not supported by this build of the host forest");
   if (brick.num_trees > max_trees_for_keys<D>()) throw std::invalid_argument("too many trees for 64-bit node keys");
-  leaves.clear();
-  leaf_key.clear();
+  std::vector<Quad> roots;
+  std::vector<uint64_t> keys;
   for (int t = 0; t < brick.num_trees; ++t) {
     Quad q;
     q.x[0] = q.x[1] = q.x[2] = 0;
     q.tree = t;
     q.level = 0;
-    leaves.push_back(q);
-    leaf_key.push_back(((uint64_t)t) << tree_shift<D>());
+    roots.push_back(q);
+    keys.push_back(((uint64_t)t) << tree_shift<D>());
   }
+  leaves.replace(std::move(roots));
+  leaf_key.replace(std::move(keys));
   drop_nodes();
 }
 
@@ -111,8 +113,8 @@ void Forest<D>::refine(const uint8_t* tags) {
       keys[o + c] = (((uint64_t)ch.tree) << tree_shift<D>()) | morton<D>(ch.x);
     }
   }
-  leaves.swap(out);
-  leaf_key.swap(keys);
+  leaves.replace(std::move(out));
+  leaf_key.replace(std::move(keys));
   drop_nodes();
 }
 
@@ -157,8 +159,8 @@ void Forest<D>::coarsen(const uint8_t* tags) {
       ++i;
     }
   }
-  leaves.swap(out);
-  leaf_key.swap(keys);
+  leaves.replace(std::move(out));
+  leaf_key.replace(std::move(keys));
   drop_nodes();
 }
 
@@ -259,8 +261,8 @@ bool Forest<D>::coarsen_then_refine(const int8_t* tag) {
       }
     }
   }
-  leaves.swap(out);
-  leaf_key.swap(keys);
+  leaves.replace(std::move(out));
+  leaf_key.replace(std::move(keys));
   drop_nodes();
   return true;
 }
@@ -341,8 +343,8 @@ void Forest<D>::set_leaves(size_t n, const int32_t* tree, const int32_t* level, 
     keys[i] = (((uint64_t)q.tree) << tree_shift<D>()) | m;
   }
   if (expect_tree != brick.num_trees || expect_key != 0) throw std::invalid_argument("set_leaves: the leaves do not cover every tree");
-  leaves.swap(ls);
-  leaf_key.swap(keys);
+  leaves.replace(std::move(ls));
+  leaf_key.replace(std::move(keys));
   drop_nodes();
 }
 

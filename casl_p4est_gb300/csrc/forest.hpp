@@ -49,6 +49,24 @@ struct Quad {
   int32_t level;
 };
 
+// An array that is replaced whole and never edited in place, so copies of its owner share it.
+template <typename T>
+class SharedArray {
+ public:
+  SharedArray() : p_(std::make_shared<const std::vector<T>>()) {}
+  size_t size() const { return p_->size(); }
+  bool empty() const { return p_->empty(); }
+  const T& operator[](size_t i) const { return (*p_)[i]; }
+  const T* data() const { return p_->data(); }
+  typename std::vector<T>::const_iterator begin() const { return p_->begin(); }
+  typename std::vector<T>::const_iterator end() const { return p_->end(); }
+  const std::vector<T>& vec() const { return *p_; }
+  void replace(std::vector<T>&& v) { p_ = std::make_shared<const std::vector<T>>(std::move(v)); }
+
+ private:
+  std::shared_ptr<const std::vector<T>> p_;
+};
+
 // Node numbering of a forest. Built whole and never changed afterwards, so copies of a forest share
 // one instance (a forest copied before a regrid pays nothing for nodes that the regrid replaces).
 // A numbering made on the device stays there until host code first reads the arrays: host() copies
@@ -74,8 +92,8 @@ template <int D>
 struct Forest {
   using DD = Dim<D>;
   Brick brick;
-  std::vector<Quad> leaves;          // tree-major Morton order
-  std::vector<uint64_t> leaf_key;    // (tree << D*MAXLEVEL) | morton(x)
+  SharedArray<Quad> leaves;          // tree-major Morton order; replaced whole, shared by copies
+  SharedArray<uint64_t> leaf_key;    // (tree << D*MAXLEVEL) | morton(x)
   // node numbering (valid once build_nodes() ran); replaced as a whole, shared by copies
   std::shared_ptr<const NodeArrays> nd = std::make_shared<const NodeArrays>();
   bool nodes_built = false;

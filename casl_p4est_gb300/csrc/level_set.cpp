@@ -1009,7 +1009,7 @@ void LevelSet<D>::build_locator() {
   } else {
     std::vector<int8_t> lvl((size_t)nl);
     for (int64_t q = 0; q < nl; ++q) lvl[(size_t)q] = (int8_t)f.leaves[(size_t)q].level;
-    loc_key.upload(f.leaf_key, stream);
+    loc_key.upload(f.leaf_key.vec(), stream);
     loc_level.upload(lvl, stream);
     loc_nodes.upload(f.nd->host().local_nodes, stream);
     loc_ijk.upload(f.brick.ijk_to_tree, stream);
