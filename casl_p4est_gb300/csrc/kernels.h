@@ -17,6 +17,18 @@ enum : uint16_t {
   ST_CUT_SHIFT = 8,  // bit (8 + dir): the neighbour in direction dir is across the interface
 };
 
+// SM count of the device current at the first call (grids of persistent and grid-stride kernels)
+inline int device_sm_count() {
+  static int sms = 0;
+  if (sms <= 0) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 1;
+  }
+  return sms;
+}
+
 // Launch shape of the mixed stage kernels (chosen by the autotuner): grid of the persistent uniform
 // and regular kernels (0: one full wave at maximum occupancy), threads per block of every stage
 // kernel, and the pipeline depth of the uniform kernel.

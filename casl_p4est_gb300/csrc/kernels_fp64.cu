@@ -786,7 +786,7 @@ void launch_apply_mask(const double* mask, const int32_t* perm, uint16_t* status
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s) {
   cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
   if (n == 0) return;
-  const unsigned g = std::min<unsigned>(nblocks(n), 152u * 8u);
+  const unsigned g = std::min<unsigned>(nblocks(n), (unsigned)device_sm_count() * 8u);
   k_band_linf64<<<g, TPB, 0, s>>>(a, b, band, n, out3);
 }
 

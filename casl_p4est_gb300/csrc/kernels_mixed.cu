@@ -1133,7 +1133,7 @@ void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const dou
   k_gather64<<<nblocks(T.N), TPB, 0, s>>>(phi0, perm, phi0_dev, T.N);
   if (T.nI) k_dd0_irr<D><<<nblocks(T.nI), TPB, 0, s>>>(T, phi0_dev, dd0_irr);
   k_prep_classify<D><<<nblocks(T.N), TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, lim_lo, lim_hi, status, near_list, near_count);
-  k_prep_subcell<D><<<152 * 8, TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, order_space, near_list, near_count, status, s_near);
+  k_prep_subcell<D><<<(unsigned)device_sm_count() * 8u, TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, order_space, near_list, near_count, status, s_near);
 }
 
 template <int D>
@@ -1171,11 +1171,9 @@ void launch_freeze32(const uint16_t* lim, int it, uint16_t* status, int64_t n, c
 
 template <int D>
 static int persistent_blocks(const void* kernel) {
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
-  return sms * (per_sm > 0 ? per_sm : 1);
+  return device_sm_count() * (per_sm > 0 ? per_sm : 1);
 }
 
 // the bulk copies read 16-byte aligned spans from the bases of these arrays
@@ -1216,10 +1214,7 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
       configured_tpb = tpb;
     }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int full = sms * (per_sm > 0 ? per_sm : 1);
+    const int full = device_sm_count() * (per_sm > 0 ? per_sm : 1);
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
     const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
     kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err);

@@ -585,9 +585,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
   cudaEvent_t e0, e1;
   cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
   cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
-  int sms = 152, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sm_count();
   const bool timing = timer.enabled;
   timer.enabled = false;
   auto run = [&](const StageCfg& c) -> float {
