@@ -131,7 +131,6 @@ template <int D>
 void LevelSet<D>::init_stream() {
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   own_stream = true;
-  if (const char* ub = getenv("LSG_UNIFORM_BLOCKS")) cfg.uniform_blocks = atoi(ub);
 }
 
 template <int D>
