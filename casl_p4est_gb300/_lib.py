@@ -109,6 +109,7 @@ SIGNATURES = {
     "lsg_semi_lagrangian_advect_callback": (_I, [_P, _DP, _I64, _D, _P, _P, _DP, _DP, _I, _DP]),
     "lsg_band_linf_device": (_I, [_P, _P, _P, _D, _DP, C.POINTER(_I64)]),
     "lsg_batch_create": (_I, [_I, C.POINTER(_P), C.POINTER(_P)]),
+    "lsg_batch_create_ex": (_I, [_I, C.POINTER(_P), _I, C.POINTER(_P)]),
     "lsg_batch_count": (_I, [_P]),
     "lsg_batch_offsets": (_I, [_P, C.POINTER(_I64)]),
     "lsg_batch_reinitialize": (_I, [_P, _DP, _I32P, _I]),

@@ -1035,8 +1035,14 @@ int lsg_semi_lagrangian_advect_callback(lsg_level_set* ls, const double* xyz, in
 }
 
 int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set** out) {
+  return lsg_batch_create_ex(count, forests, 0, out);
+}
+
+int lsg_batch_create_ex(int count, const lsg_forest* const* forests, int flags, lsg_level_set** out) {
   return guard([&] {
     need(out != nullptr && forests != nullptr && count > 0, "batch: null arguments or no grids");
+    need((flags & ~LSG_BUILD_ON_DEVICE) == 0, "unknown batch flags");
+    const bool on_device = (flags & LSG_BUILD_ON_DEVICE) != 0;
     const int dim = forests[0] ? forests[0]->dim : 0;
     need(dim == 2 || dim == 3, "batch: null forest");
     for (int k = 0; k < count; ++k) need(forests[k] != nullptr && forests[k]->dim == dim, "batch: grids of one dimension required");
@@ -1046,11 +1052,11 @@ int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set*
       if (dim == 2) {
         std::vector<const Forest<2>*> parts;
         for (int k = 0; k < count; ++k) parts.push_back(forests[k]->f2);
-        ls->l2 = new LevelSet<2>(parts);
+        ls->l2 = new LevelSet<2>(parts, on_device);
       } else {
         std::vector<const Forest<3>*> parts;
         for (int k = 0; k < count; ++k) parts.push_back(forests[k]->f3);
-        ls->l3 = new LevelSet<3>(parts);
+        ls->l3 = new LevelSet<3>(parts, on_device);
       }
     } catch (...) {
       delete ls;

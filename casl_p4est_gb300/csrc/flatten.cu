@@ -878,6 +878,22 @@ void build_nodes_device(Forest<D>& F, cudaStream_t s) {
   F.device = X;
 }
 
+__global__ void __launch_bounds__(TPB) k_concat_index(const int32_t* __restrict__ src, int64_t n, int64_t total,
+                                                      int32_t* __restrict__ dst, int64_t Ndst, int64_t off, int32_t add) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total) return;
+  const int64_t p = e / n, i = e - p * n;
+  const int32_t v = src[e];
+  dst[p * Ndst + off + i] = v >= 0 ? v + add : v;
+}
+
+void concat_index_planes(const int32_t* src, int64_t n, int planes, int32_t* dst, int64_t Ndst, int64_t off, int32_t add,
+                         cudaStream_t s) {
+  const int64_t total = n * planes;
+  if (total) k_concat_index<<<nblocks(total), TPB, 0, s>>>(src, n, total, dst, Ndst, off, add);
+  cuda_check(cudaGetLastError(), "index concatenation");
+}
+
 template <int D>
 __global__ void __launch_bounds__(TPB) k_coarse_table(const uint64_t* __restrict__ key, int64_t nl, int64_t ncells, int64_t ncoarse, int L0,
                                                       int32_t* __restrict__ ctab) {

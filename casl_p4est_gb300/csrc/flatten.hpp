@@ -46,6 +46,10 @@ struct ForestDevice {
 // device copy stays attached to the forest and the host arrays are copied down on first host use.
 template <int D>
 void build_nodes_device(Forest<D>& F, cudaStream_t s);
+// Concatenation of index tables: dst[p * Ndst + off + i] = src[p * n + i] (+ add where src >= 0) for
+// every plane p < planes and i < n.
+void concat_index_planes(const int32_t* src, int64_t n, int planes, int32_t* dst, int64_t Ndst, int64_t off, int32_t add,
+                         cudaStream_t s);
 // Coarse-cell table of point location: for each cell i of the uniform level L0 in each tree (ncoarse
 // cells per tree, nt trees), the last leaf whose key is <= the cell's first point (0 if none), and
 // ctab[nt * ncoarse] = nl - 1; from the sorted leaf keys on the device.

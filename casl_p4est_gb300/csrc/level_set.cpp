@@ -1,6 +1,8 @@
 // Host drivers of the device level-set operator (see level_set.hpp).
 #include "level_set.hpp"
 
+#include <array>
+
 #include "flatten.hpp"
 
 #include <float.h>
@@ -133,8 +135,40 @@ void LevelSet<D>::init_stream() {
   own_stream = true;
 }
 
+// FP64 tables of one grid built on the device into `out` (the grid's device copy is made if absent);
+// returns the number of correction records
 template <int D>
-LevelSet<D>::LevelSet(const std::vector<const Forest<D>*>& parts) : F(nullptr) {
+static int64_t device_tables_of(const Forest<D>& f, const Tab64Dev<D>& out, cudaStream_t s) {
+  using DD = Dim<D>;
+  const ForestDevice<D>& X = forest_device(const_cast<Forest<D>&>(f), s);
+  const int64_t nl = (int64_t)f.leaves.size();
+  const int nt = f.brick.num_trees;
+  int L0 = 0;  // the point-location table's uniform level, as build_locator chooses it
+  while (L0 < DD::MAXLEVEL && ((int64_t)nt << (D * (L0 + 1))) <= 2 * nl) ++L0;
+  DevBuf<int32_t> ctab;
+  ctab.alloc((size_t)((int64_t)nt * (int64_t(1) << (D * L0)) + 1));
+  coarse_table_device<D>(X.leaf_key.p, nl, nt, L0, ctab.p, s);
+  DForest<D> DF{};
+  DF.nleaves = nl;
+  DF.N = (int64_t)f.num_nodes();
+  DF.key = X.leaf_key.p;
+  DF.level = X.level.p;
+  DF.local_nodes = X.local_nodes.p;
+  DF.ctab = ctab.p;
+  DF.L0 = L0;
+  DF.ncoarse = int64_t(1) << (D * L0);
+  for (int a = 0; a < 3; ++a) DF.n[a] = f.brick.n[a];
+  DF.ijk_to_tree = X.ijk_to_tree.p;
+  DF.tree_ijk = X.tree_ijk.p;
+  DF.tmin = X.tmin.p;
+  DF.tmax = X.tmax.p;
+  DF.node_tree = X.node_tree.p;
+  DF.node_x = X.node_x.p;
+  return build_tables64_device<D>(DF, out, s);  // synchronises s, so ctab may go
+}
+
+template <int D>
+LevelSet<D>::LevelSet(const std::vector<const Forest<D>*>& parts, bool device_build) : F(nullptr) {
   if (parts.empty()) throw std::invalid_argument("batch: no grids");
   std::vector<Tables64<D>> T(parts.size());
   std::vector<const Tables64<D>*> ptr(parts.size());
@@ -155,6 +189,73 @@ LevelSet<D>::LevelSet(const std::vector<const Forest<D>*>& parts) : F(nullptr) {
   }
   zdt = EPS * (D == 3 ? min3(tdim[0], tdim[1], tdim[2]) : min2(tdim[0], tdim[1]));
   part_offsets.assign(1, 0);
+  if (device_build) {
+    init_stream();
+    // every grid's tables, then the union: planes [slot][node] concatenated with node indices and
+    // correction-record indices offset by the parts before
+    std::vector<std::array<DevBuf<int32_t>, 2>> ib(parts.size());   // nbr, cidx
+    std::vector<std::array<DevBuf<double>, 6>> db(parts.size());    // w, nrm, d, q, crec, smin
+    std::vector<DevBuf<uint8_t>> wb(parts.size());
+    std::vector<int64_t> R(parts.size());
+    int64_t Rtot = 0;
+    for (size_t k = 0; k < parts.size(); ++k) {
+      const Tab64Dev<D> out{&ib[k][0], &db[k][0], &db[k][1], &db[k][2], &db[k][3], &ib[k][1], &db[k][4], &wb[k], &db[k][5]};
+      R[k] = device_tables_of<D>(*parts[k], out, stream);
+      part_offsets.push_back(part_offsets.back() + (int64_t)parts[k]->num_nodes());
+      Rtot += R[k];
+    }
+    N = part_offsets.back();
+    num_corrections = Rtot;
+    nbr.alloc((size_t)NS * N);
+    w.alloc((size_t)NS * N);
+    nrm.alloc((size_t)2 * D * N);
+    d.alloc((size_t)2 * D * N);
+    q.alloc((size_t)2 * D * (D - 1) * N);
+    cidx.alloc((size_t)N);
+    crec.alloc((size_t)6 * Rtot + 6);
+    wall.alloc((size_t)N);
+    smin.alloc((size_t)N);
+    int64_t roff = 0;
+    for (size_t k = 0; k < parts.size(); ++k) {
+      const int64_t o = part_offsets[k], nk = part_offsets[k + 1] - o;
+      auto planes = [&](void* dst, const void* src, size_t es, int np) {
+        if (nk)
+          cuda_check(cudaMemcpy2DAsync((char*)dst + o * es, (size_t)N * es, src, (size_t)nk * es, (size_t)nk * es, (size_t)np,
+                                       cudaMemcpyDeviceToDevice, stream),
+                     "batch table concatenation");
+      };
+      concat_index_planes(ib[k][0].p, nk, NS, nbr.p, N, o, (int32_t)o, stream);
+      concat_index_planes(ib[k][1].p, nk, 1, cidx.p, N, o, (int32_t)roff, stream);
+      planes(w.p, db[k][0].p, 8, NS);
+      planes(nrm.p, db[k][1].p, 8, 2 * D);
+      planes(d.p, db[k][2].p, 8, 2 * D);
+      planes(q.p, db[k][3].p, 8, 2 * D * (D - 1));
+      planes(smin.p, db[k][5].p, 8, 1);
+      planes(wall.p, wb[k].p, 1, 1);
+      if (R[k])
+        cuda_check(cudaMemcpyAsync(crec.p + 6 * roff, db[k][4].p, (size_t)6 * R[k] * sizeof(double), cudaMemcpyDeviceToDevice, stream),
+                   "batch correction records");
+      roff += R[k];
+    }
+    cuda_check(cudaStreamSynchronize(stream), "batch tables");  // the parts' buffers go back to the cache
+    T64.N = N;
+    T64.nbr = nbr.p;
+    T64.w = w.p;
+    T64.nrm = nrm.p;
+    T64.d = d.p;
+    T64.q = q.p;
+    T64.cidx = cidx.p;
+    T64.crec = crec.p;
+    T64.wall = wall.p;
+    device_flat = true;
+    MixedDev<D> M{&r_meta, &r_nbr, &r_nbr2, &r_meta2, &i_meta, &i_cls, &i_nbr, &i_wf, &i_d, &i_q, &i_cidx, &corr32, &cls32,
+                  &i_wf64, &i_d64, &i_q64, &corr64, &perm, &iperm};
+    build_mixed_device<D>(T64, num_corrections, ts, M, stream);
+    near_list.alloc((size_t)N);
+    near_count.alloc(1);
+    set_mixed_views(M.nR, M.nI, M.nU, M.base, M.x_first, M.nX, M.ncls, ts);
+    return;
+  }
 #pragma omp parallel for schedule(dynamic, 1)
   for (long long k = 0; k < (long long)parts.size(); ++k) build_tables64<D>(*parts[(size_t)k], T[(size_t)k]);
   for (size_t k = 0; k < parts.size(); ++k) {

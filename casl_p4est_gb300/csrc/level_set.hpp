@@ -120,7 +120,9 @@ struct LevelSet {
   explicit LevelSet(const Forest<D>& forest, bool with_mixed = true, bool device_build = false);
   // level set over the disjoint union of grids with equal tree sizes: tables concatenated in node
   // order (parts[k] occupies nodes part_offsets[k] .. part_offsets[k+1]-1)
-  LevelSet(const std::vector<const Forest<D>*>& parts);
+  // device_build: each grid's FP64 tables built on the GPU and concatenated there, then the union's
+  // mixed tables built on the GPU (same results as the host build)
+  LevelSet(const std::vector<const Forest<D>*>& parts, bool device_build = false);
   ~LevelSet();
   void set_stream(cudaStream_t s);
 

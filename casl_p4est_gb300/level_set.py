@@ -380,11 +380,13 @@ class my_p4est_level_set_batch_t:
     The grids' tables are concatenated on the device; reinitialize_2nd_order runs every stage kernel
     once over all grids, grid k for its own iteration count, the loop captured as a CUDA graph."""
 
-    def __init__(self, forests):
+    def __init__(self, forests, device_build: bool = False):
+        """device_build: build the grids' tables on the GPU (same results, no host table work)."""
         self.forests = list(forests)  # kept alive: the batch borrows them
         arr = (C.c_void_p * len(self.forests))(*[f.handle.value for f in self.forests])
         h = C.c_void_p()
-        L.check(L.load().lsg_batch_create(len(self.forests), C.cast(arr, C.POINTER(C.c_void_p)), C.byref(h)))
+        L.check(L.load().lsg_batch_create_ex(len(self.forests), C.cast(arr, C.POINTER(C.c_void_p)),
+                                             L.LSG_BUILD_ON_DEVICE if device_build else 0, C.byref(h)))
         self._h = h
         self.count = int(L.load().lsg_batch_count(h))
         off = np.zeros(self.count + 1, np.int64)

@@ -346,6 +346,9 @@ int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b
  * own node order) so every stage kernel covers all grids in one launch. The returned handle is a
  * level-set handle, destroyed with lsg_level_set_destroy; the forests must outlive it. */
 int lsg_batch_create(int count, const lsg_forest* const* forests, lsg_level_set** out);
+/* The same with flags. LSG_BUILD_ON_DEVICE: each grid's node-neighbour tables are built on the GPU
+ * and concatenated there, and the union's mixed tables are built on the GPU (same results). */
+int lsg_batch_create_ex(int count, const lsg_forest* const* forests, int flags, lsg_level_set** out);
 int lsg_batch_count(const lsg_level_set* batch);
 int lsg_batch_offsets(const lsg_level_set* batch, int64_t* offsets); /* count + 1 values */
 /* reinitialize_2nd_order of every grid, grid k for iterations[k] pseudo-time iterations (mixed

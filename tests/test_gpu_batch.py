@@ -97,3 +97,31 @@ def test_batch_rejects_mixed_tree_sizes():
     c.build_nodes()
     with pytest.raises(G.LsgInvalidArgument):
         G.my_p4est_level_set_batch_t([a, c])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_device_built_batch_equals_host_built(batch2d, dim):
+    """Tables built on the GPU (each grid's, concatenated there, then the union's mixed tables) give the
+    host-built batch's results bit for bit, with per-grid iteration counts; the grids' nodes are
+    numbered on the host for one half of them and on the device for the other."""
+    if dim == 2:
+        grids = batch2d[0]
+        forests = [g[0] for g in grids]
+        phis = [g[1] for g in grids]
+    else:
+        from grids import flower_3d, phi0_flower_3d
+        forests = [flower_3d(2, 5), flower_3d(3, 6), flower_3d(2, 4)]
+        phis = [phi0_flower_3d(f) for f in forests]
+    copies = [f.copy() for f in forests]
+    for k, f in enumerate(copies):
+        if k % 2:
+            f.build_nodes(device=True)
+    host = G.my_p4est_level_set_batch_t(forests)
+    dev = G.my_p4est_level_set_batch_t(copies, device_build=True)
+    assert np.array_equal(dev.offsets, host.offsets)
+    its = [int(i) for i in np.arange(len(forests)) % 4 + 3]
+    a = host.concat(phis)
+    b = dev.concat(phis)
+    host.reinitialize_2nd_order(a, its)
+    dev.reinitialize_2nd_order(b, its)
+    assert np.array_equal(a, b)
