@@ -905,6 +905,21 @@ __device__ __forceinline__ double rcp64(double x) {
   return fma(r, e, r);
 }
 
+// a * b < 0.0 with IEEE double semantics, decided from the bit patterns where that is exact: opposite
+// sign bits, both finite and normal, and exponents large enough that the product cannot round to
+// zero (|a b| >= 2^(ea+eb-2046) >= 2^-1074); every other case takes the FP64 product. GB300's FP64
+// rate makes the multiply and compare the cost of the near-interface test.
+__device__ __forceinline__ bool product_negative(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if ((ia ^ ib) >= 0) {
+    if (((ia >> 52) & 0x7ff) != 0x7ff && ((ib >> 52) & 0x7ff) != 0x7ff) return false;  // same signs, no NaN: a b >= 0
+    return a * b < 0.0;
+  }
+  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
+  if (ea > 0 && eb > 0 && ea < 0x7ff && eb < 0x7ff && ea + eb >= 972) return true;
+  return a * b < 0.0;
+}
+
 __device__ __forceinline__ double level_size64(double tsize, int base, uint32_t code) {
   return __longlong_as_double(__double_as_longlong(tsize) - ((long long)(base + (int)code) << 52));
 }
@@ -1014,7 +1029,7 @@ __global__ void __launch_bounds__(TPB) k_prep_classify(DTab32<D> T, const double
     } else {
       st = (p0 > 0.0) ? ST_POSITIVE : 0;
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) near = near || (p0 * quad_nb_m64<D>(T, n, dir, phi0, dd0_irr) < 0.0);
+      for (int dir = 0; dir < 2 * D; ++dir) near = near || product_negative(p0, quad_nb_m64<D>(T, n, dir, phi0, dd0_irr));
     }
     status[n] = st;
   }
@@ -1056,7 +1071,7 @@ __global__ void __launch_bounds__(TPB) k_prep_subcell(DTab32<D> T, const double*
 #pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
       const double fn = quad_nb_m64<D>(T, n, dir, phi0, dd0_irr);
-      if (!(p0 * fn < 0.0)) continue;
+      if (!product_negative(p0, fn)) continue;
       st |= (uint16_t)(1u << (ST_CUT_SHIFT + dir));
       const int axis = dir >> 1;
       double xx_nb = 0.0;
