@@ -561,8 +561,8 @@ def main():
     f, phi0 = build_grid(args.levels)
     N = f.num_nodes
     ngbd = G.my_p4est_node_neighbors_t(f)
-    ngbd.init_neighbors()
-    ls = G.my_p4est_level_set_t(ngbd, precision="mixed")
+    # node-neighbour tables built on the GPU (the same tables as the host build)
+    ls = G.my_p4est_level_set_t(ngbd, precision="mixed", device_build=True)
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
     stage_cfg = ls.autotune(phi0, trials=8)

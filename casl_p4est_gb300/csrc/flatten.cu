@@ -12,6 +12,10 @@
 // (-ffp-contract=off) does, so the FP64 tables are bit-identical to the host's.
 #include <cub/cub.cuh>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "flatten.hpp"
 #include "tables.hpp"
 
@@ -181,6 +185,25 @@ __global__ void __launch_bounds__(TPB) k_classify(DTab64<D> T, const int8_t* __r
   icount[n] = counts;
   is_reg[n] = regular ? 1 : 0;
   irr_flag[n] = regular ? 0 : 1;
+}
+
+// first position of every class in the hash-grouped order
+__global__ void __launch_bounds__(TPB) k_class_starts(const int32_t* __restrict__ flag, const int32_t* __restrict__ excl, int64_t nI,
+                                                      int32_t* __restrict__ start) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nI && flag[i]) start[excl[i]] = (int32_t)i;
+}
+
+// renumber the classes (new id and shift of each class's block of the irregular order)
+__global__ void __launch_bounds__(TPB) k_class_renumber(const int32_t* __restrict__ irr_node, int64_t nI, const int32_t* __restrict__ newid,
+                                                        const int32_t* __restrict__ shift, int32_t* __restrict__ node_cls,
+                                                        int32_t* __restrict__ irr_rank) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nI) return;
+  const int32_t n = irr_node[k];
+  const int32_t c = node_cls[n];
+  node_cls[n] = newid[c];
+  irr_rank[n] += shift[c];
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t h) {
@@ -723,6 +746,42 @@ void build_mixed_device(const DTab64<D>& T, int64_t R, const double* ts, MixedDe
   cls64.alloc((size_t)ncls * CW + 1);
   if (nI)
     k_class_write<D><<<nblocks(nI), TPB, 0, s>>>(rec, slot_sorted, irr_node, flag, excl, nI, cls64.p, M.cls32->p, node_cls, irr_rank);
+  // classes renumbered in the host build's order (records compared as bytes), which also orders the
+  // irregular group: each class's block of (class, node) positions moves as a whole
+  if (ncls > 1) {
+    std::vector<double> h64((size_t)ncls * CW);
+    std::vector<float> h32((size_t)ncls * CW);
+    std::vector<int32_t> start((size_t)ncls);
+    DevBuf<int32_t> dstart, dnew, dshift;
+    dstart.alloc((size_t)ncls);
+    k_class_starts<<<nblocks(nI), TPB, 0, s>>>(flag, excl, nI, dstart.p);
+    cuda_check(cudaGetLastError(), "class starts");
+    cuda_check(cudaMemcpyAsync(h64.data(), cls64.p, h64.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(h32.data(), M.cls32->p, h32.size() * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaMemcpyAsync(start.data(), dstart.p, start.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "class records");
+    std::vector<int32_t> order((size_t)ncls), newid((size_t)ncls), shift((size_t)ncls);
+    for (int64_t c = 0; c < ncls; ++c) order[(size_t)c] = (int32_t)c;
+    std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+      return memcmp(&h64[(size_t)a * CW], &h64[(size_t)b * CW], CW * sizeof(double)) < 0;
+    });
+    std::vector<float> n32(h32.size());
+    int64_t pos = 0;
+    for (int64_t p = 0; p < ncls; ++p) {
+      const int32_t c = order[(size_t)p];
+      const int64_t cnt = (c + 1 < ncls ? start[(size_t)c + 1] : nI) - start[(size_t)c];
+      newid[(size_t)c] = (int32_t)p;
+      shift[(size_t)c] = (int32_t)(pos - start[(size_t)c]);
+      pos += cnt;
+      memcpy(&n32[(size_t)p * CW], &h32[(size_t)c * CW], CW * sizeof(float));
+    }
+    dnew.upload(newid, s);
+    dshift.upload(shift, s);
+    cuda_check(cudaMemcpyAsync(M.cls32->p, n32.data(), n32.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    k_class_renumber<<<nblocks(nI), TPB, 0, s>>>(irr_node, nI, dnew.p, dshift.p, node_cls, irr_rank);
+    cuda_check(cudaGetLastError(), "class renumbering");
+    cuda_check(cudaStreamSynchronize(s), "class renumbering");  // the host vectors above go out of scope
+  }
   M.ncls = ncls;
   // regular nodes: second neighbours, uniform flag, extended set
   cuda_check(cudaMemsetAsync(in_x, 0, N1, s), "memset");
