@@ -17,8 +17,9 @@
 //   node interpolation      src/my_p4est_utils.cpp:367-576, src/my_p4est_interpolation_nodes.cpp:107-288,
 //                           src/my_p4est_hierarchy.cpp:264-567, src/my_p4est_utils.h:2177-2187
 //   semi-Lagrangian step    src/my_p4est_semi_lagrangian.cpp:148-223
-// Parity is pinned by analytic known answers and convergence orders (the reference has no value-level
-// golden vectors for this path and cannot be built here: p4est/PETSc/MPI are absent).
+// Pinned to the reference itself: oracle/_ref compiles the reference's own sources for these functions
+// (ref_harness.cpp, `make ref`), and tests/test_ref_pin.py checks this restatement against them bit for bit;
+// also pinned by analytic known answers and convergence orders.
 #include <float.h>
 #include <math.h>
 #include <stdint.h>

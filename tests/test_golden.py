@@ -1,7 +1,8 @@
-"""Regression fixtures (tests/golden, made by tests/golden/make_golden.py): the grid rebuilt leaf by leaf,
-the oracle's FP64 outputs reproduced bit for bit on the CPU, and the CUDA path's FP64 outputs equal to
-the same numbers on the GPU (no oracle at run time). Also the known answer of the quadratic interface
-root (src/casl_math.cpp:67-97): exact for a quadratic sampled at the cell ends."""
+"""Reference fixtures (tests/golden, made by tests/golden/make_golden.py from the reference's own code compiled
+from its sources): the grid rebuilt leaf by leaf, the restatement's FP64 outputs reproduced bit for bit on the
+CPU, and the CUDA path's FP64 outputs equal to the same numbers on the GPU (nothing from the reference tree
+or the oracle at run time). Also the known answer of the quadratic interface root (src/casl_math.cpp:67-97):
+exact for a quadratic sampled at the cell ends."""
 import glob
 import os
 
@@ -12,16 +13,21 @@ import casl_p4est_gb300 as G
 import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+FIXTURES = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz")) if "config1" not in p)
+CONFIG1 = os.path.join(HERE, "golden", "circle2d_L4-9_config1.npz")
+
+
+def grid_from(z, prefix=""):
+    dim = int(z["dim"])
+    f = G.my_p4est_brick_new(list(z["n_xyz"][:dim]), list(z["xyz_min"][:dim]), list(z["xyz_max"][:dim]))
+    f.set_leaves(z[prefix + "tree"], z[prefix + "level"], z[prefix + "lxyz"])
+    f.build_nodes()
+    return f
 
 
 def load(path):
     z = dict(np.load(path))
-    dim = int(z["dim"])
-    f = G.my_p4est_brick_new(list(z["n_xyz"][:dim]), list(z["xyz_min"][:dim]), list(z["xyz_max"][:dim]))
-    f.set_leaves(z["tree"], z["level"], z["lxyz"])
-    f.build_nodes()
-    return f, z
+    return grid_from(z), z
 
 
 @pytest.fixture(params=FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
@@ -30,7 +36,7 @@ def golden(request):
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 2
+    assert len(FIXTURES) >= 3 and os.path.exists(CONFIG1)
 
 
 def test_grid_rebuilds_from_leaves(golden):
@@ -47,9 +53,29 @@ def test_oracle_reproduces_fixtures(golden):
         p = phi0.copy()
         og.reinitialize(p, os_, ot, iterations=8)
         assert np.array_equal(p, z[key]), key
+    p = phi0.copy()
+    og.reinitialize(p, 2, 2, limit_high=0.3, limit_low=-0.2, iterations=8)
+    assert np.array_equal(p, z["reinit_22_limited"])
+    adv = z["reinit_22"].copy()
+    og.advect_in_normal_direction(z["vn"], adv, float(z["advect_dt"]))
+    assert np.array_equal(adv, z["advect"])
     for m in range(5):
         assert np.array_equal(og.interpolate(m, z["reinit_22"], z["points"]), z[f"interp_{m}"]), m
     assert np.array_equal(og.sl_advect(z["node_xyz"], 0.05, z["velocity"], z["reinit_22"]), z["sl"])
+
+
+def test_oracle_reproduces_configuration_1():
+    """2D, levels 4-9, 20 iterations of reinitialize_2nd_order: the reference's result and error."""
+    z = dict(np.load(CONFIG1))
+    f = grid_from(z)
+    og = O.OracleGrid.from_forest(f)
+    p = z["phi0"].copy()
+    og.reinitialize(p, 2, 2, iterations=20)
+    assert np.array_equal(p, z["reinit_20"])
+    x = z["node_xyz"]
+    band = np.abs(p) < 3 * float(z["dx_min"])
+    err = float(np.max(np.abs(p[band] - (np.sqrt(x[band, 0] ** 2 + x[band, 1] ** 2) - 0.5))))
+    assert err == float(z["band_error"]) and err < 1e-3 * float(z["dx_min"])
 
 
 @pytest.mark.parametrize("c", [(0.7, 0.3, -0.005), (-1.3, 0.2, 0.01), (0.0, 1.0, -0.0125), (40.0, 3.0, 0.01)])
@@ -85,10 +111,36 @@ def test_cuda_path_matches_fixtures(golden):
     assert np.array_equal(p, z["reinit_22_limited"])
     adv = z["reinit_22"].copy()
     dt = ls.advect_in_normal_direction(lambda xyz: 1.0 + 0.5 * np.sin(3 * xyz[:, 0]), adv.copy())
-    ls.advect_in_normal_direction(z["vn"], adv, 0.4 * dt)
+    assert 0.4 * dt == float(z["advect_dt"])
+    ls.advect_in_normal_direction(z["vn"], adv, float(z["advect_dt"]))
     assert np.array_equal(adv, z["advect"])
     interp = G.my_p4est_interpolation_nodes_t(ls)
     for m in range(5):
         assert np.array_equal(interp.interpolate_points(z["points"], z["reinit_22"], m), z[f"interp_{m}"]), m
     sl = G.my_p4est_semi_lagrangian_t(f, ls)
     assert np.array_equal(sl.advect_from_n_to_np1(0.05, z["velocity"], z["reinit_22"]), z["sl"])
+
+
+@pytest.mark.gpu
+def test_cuda_path_matches_configuration_1():
+    """The 2D configuration on the GPU: FP64 equal to the reference's numbers; mixed within 1e-4 dx_min of
+    them in |phi| < 3 dx_min; the error against r - 0.5 reported for both."""
+    z = dict(np.load(CONFIG1))
+    f = grid_from(z)
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    dmin = float(z["dx_min"])
+    p = z["phi0"].copy()
+    ls.reinitialize_2nd_order(p, 20, precision="fp64")
+    assert np.array_equal(p, z["reinit_20"])
+    m = z["phi0"].copy()
+    ls.reinitialize_2nd_order(m, 20, precision="mixed")
+    band = np.abs(p) < 3 * dmin
+    assert float(np.max(np.abs(m[band] - p[band]))) <= 1e-4 * dmin
+    x = z["node_xyz"]
+    exact = np.sqrt(x[:, 0] ** 2 + x[:, 1] ** 2) - 0.5
+    err64 = float(np.max(np.abs(p[band] - exact[band])))
+    err32 = float(np.max(np.abs(m[band] - exact[band])))
+    assert err64 == float(z["band_error"])
+    assert abs(err32 - err64) <= 1e-4 * dmin
+    print(f"configuration 1: {f.num_nodes} nodes, error |phi-(r-0.5)| in the band: FP64 {err64:.3e} ({err64 / dmin:.2e} dx_min), "
+          f"mixed {err32:.3e}")
