@@ -65,8 +65,8 @@ def build_grid(levels):
 
 def workload_config(args, N, world=1):
     return {"workload": f"3D flower octree [-1,1]^3 levels {args.levels[0]}-{args.levels[1]} (lip 2.4), "
-                        f"{N} nodes, reinitialize_2nd_order {args.iters} iterations, mixed FP32/FP64",
-            "nodes": N, "iterations": args.iters, "precision": "mixed",
+                        f"{N} nodes, reinitialize_2nd_order {args.iters} iterations",
+            "nodes": N, "iterations": args.iters,
             "l2": "working set > L2 (no flush needed)", "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
@@ -143,19 +143,21 @@ class ClockSampler:
 
 
 def cpu_reinit_sample(f, phi0, iters, nthreads):
-    """The oracle (CPU restatement of reinitialize_2nd_order) on the same grid: `iters` iterations."""
-    import casl_p4est_gb300 as G
+    """The oracle (CPU restatement of reinitialize_2nd_order, its grid and stencils from its own construction)
+    on the same grid: `iters` iterations. Returns (seconds, result)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    rec = G.my_p4est_node_neighbors_t(f).get_neighbors()
-    og = O.OracleGrid.from_records(3, rec, f.wall_mask(), [2.0, 2.0, 2.0])
+    og = O.OracleGrid.from_forest(f)
     phi = phi0.copy()
     t = time.perf_counter()
     og.reinitialize(phi, 2, 2, iterations=iters, nthreads=nthreads)
-    return time.perf_counter() - t, og, rec
+    return time.perf_counter() - t, phi
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference loops (the reference itself needs p4est, PETSc
+    and MPI), its grid and stencils from its own construction, on all host cores; every timed step is the
+    full workload (all nodes, args.iters iterations); warm-up steps are one iteration each."""
     if rank != 0:
         return
     f, phi0 = build_grid(args.levels)
@@ -163,29 +165,28 @@ def run_reference(args, rank, world):
     cores = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    import casl_p4est_gb300 as G
-    rec = G.my_p4est_node_neighbors_t(f).get_neighbors()
-    og = O.OracleGrid.from_records(3, rec, f.wall_mask(), [2.0, 2.0, 2.0])
-    sample_iters = 3
-    phi = phi0.copy()
+    og = O.OracleGrid.from_forest(f)
     for _ in range(args.warmup):
-        og.reinitialize(phi, 2, 2, iterations=sample_iters, nthreads=cores)
+        phi = phi0.copy()
+        og.reinitialize(phi, 2, 2, iterations=1, nthreads=cores)
     times = []
     for _ in range(args.steps):
         phi = phi0.copy()
         t = time.perf_counter()
-        og.reinitialize(phi, 2, 2, iterations=sample_iters, nthreads=cores)
+        og.reinitialize(phi, 2, 2, iterations=args.iters, nthreads=cores)
         times.append(time.perf_counter() - t)
     total = sum(times)
-    value = N * sample_iters * args.steps / total
+    value = N * args.iters * args.steps / total
     out = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "node-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(workload_config(args, N), sample=f"{sample_iters} iteration(s) of the full grid per step"),
+        "config": workload_config(args, N),
         "cpu_baseline": {"value": value, "unit": "node-iters/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample_iters} reinit iteration(s) x {N} nodes per step, {cores} threads, CPU restatement of "
-                                   "reinitialize_one_iteration/compute_derivatives (the reference needs p4est/PETSc/MPI)"},
+                         "sample": f"the full workload per timed step: reinitialize_2nd_order, {args.iters} iterations x {N} nodes, "
+                                   f"{cores} threads, FP64; CPU restatement of reinitialize_one_iteration/compute_derivatives "
+                                   "(oracle/, bit-identical to the reference's own code built from its sources); warm-up steps are "
+                                   "1 iteration each"},
         "e2e": {"value": value, "unit": "node-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -467,7 +468,8 @@ def run_large(args):
     mixed_d = phi_d.clone()
     ms_fp64 = timed(lambda: reinit("fp64"), 1)
     band_err, band_nodes = ls.band_linf(mixed_d, phi_d, 3 * dmin)
-    iface_err, _ = ls.band_linf(mixed_d, phi_d, dmin)
+    near_err, _ = ls.band_linf(mixed_d, phi_d, dmin)
+    iface_loc, iface_edges, iface_mismatch = ls.interface_location_error(mixed_d, phi_d)
     del mixed_d
     # normal advection, vn = 1, 20 steps from the reinitialised field
     vn = torch.ones_like(phi0_d)
@@ -507,7 +509,9 @@ def run_large(args):
                    "nodes": N, "leaves": f.num_leaves, "l2": "working set > L2 (no flush needed)"},
         "fp64": {"ms_per_step": ms_fp64, "value": N * iters / (ms_fp64 / 1e3)},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
-        "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
+        "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "band_linf_near_interface_vs_fp64": near_err,
+        "interface_location_err_vs_fp64": iface_loc, "interface_location_err_over_dx_min": iface_loc / dmin,
+        "interface_cut_edges": iface_edges, "interface_sign_mismatches": iface_mismatch,
         "band_nodes": band_nodes, "dx_min": dmin,
         "roofline_per_iteration": {"alg_bytes_per_node_iter": 284, "achieved_GBps": gbs, "peak": peak, "frac": gbs / peak,
                                    "peak_source": peak_kind},
@@ -582,7 +586,8 @@ def main():
     ref64_d = phi_d.clone()
     step("mixed")
     band_err, band_nodes = ls.band_linf(phi_d, ref64_d, 3 * dmin)
-    iface_err, _ = ls.band_linf(phi_d, ref64_d, dmin)
+    near_err, _ = ls.band_linf(phi_d, ref64_d, dmin)
+    iface_loc, iface_edges, iface_mismatch = ls.interface_location_error(phi_d, ref64_d)
     del ref64_d
 
     # warm-up and timed region (mixed)
@@ -654,9 +659,13 @@ def main():
     dom_ms = per_kernel[dom]["ms_per_launch"]
     achieved = alg[dom] * N / (dom_ms / 1e3) / 1e9
     tpn = profile_traffic_per_node(dom)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (tpn * N if tpn is not None else None), "kernel": "k_reinit_fused32 (second-derivative + stage sweeps)",
-                "peak_source": peak_kind, "alg_bytes_per_node": alg[dom]}
+    traffic = tpn * N if tpn is not None else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "kernel": "one mixed RK stage: k_dd_x32 then k_reinit_fused32 (side stream) alongside k_reinit_uniform32 then "
+                          "k_reinit_fused_reg32 (main stream); second-derivative and stage sweeps of every node",
+                "peak_source": peak_kind, "alg_bytes_per_node": alg[dom],
+                "dram_GBps": (traffic / (dom_ms / 1e3) / 1e9 if traffic is not None else None),
+                "dram_frac": (traffic / (dom_ms / 1e3) / 1e9 / peak if traffic is not None else None)}
     iter_bytes = 2 * (dd_sweep + stage_sweep) + 3 * 4  # 284 B per node-iteration
     roofline["per_iteration"] = {"alg_bytes_per_node_iter": iter_bytes, "achieved_GBps": iter_bytes * value / world / 1e9,
                                  "frac": iter_bytes * value / world / 1e9 / peak}
@@ -680,25 +689,37 @@ def main():
            "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8}
 
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        secs, _, _ = cpu_reinit_sample(f, phi0, CPU_SAMPLE_ITERS, cores)
+        secs, cpu_phi = cpu_reinit_sample(f, phi0, CPU_SAMPLE_ITERS, cores)
         cpu = {"value": N * CPU_SAMPLE_ITERS / secs, "unit": "node-iters/s", "cores": cores, "kind": "port",
                "sample": f"{CPU_SAMPLE_ITERS} reinitialize_2nd_order iterations of the same {N}-node grid on {cores} host threads "
-                         f"({secs:.1f} s; oracle/, CPU restatement of the reference loops)"}
+                         f"({secs:.1f} s; oracle/, CPU restatement of the reference loops, bit-identical to the reference's own "
+                         "code built from its sources)"}
+        # the FP64 GPU path on the full grid for the same iterations, against the oracle's result
+        gpu_phi = phi0.copy()
+        ls.reinitialize_2nd_order(gpu_phi, CPU_SAMPLE_ITERS, precision="fp64")
+        diff = float(np.max(np.abs(gpu_phi - cpu_phi)))
+        parity = {"fp64_equals_oracle": bool(np.array_equal(gpu_phi, cpu_phi)), "max_abs_diff": diff,
+                  "iterations": CPU_SAMPLE_ITERS, "nodes": N}
 
     if rank == 0:
         out = {
             "metric": METRIC,
             "value": value, "unit": "node-iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "data": "synthetic", "precision": "mixed: FP32 stencil/RK, FP64 subcell step and checks",
             "config": workload_config(args, N, world),
             "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
             "speedup_mixed_vs_fp64": value / value64,
-            "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "interface_err_vs_fp64": iface_err,
-            "band_nodes": band_nodes,
+            "band_linf_vs_fp64": band_err, "band_linf_over_dx_min": band_err / dmin, "band_nodes": band_nodes,
+            "band_linf_near_interface_vs_fp64": near_err,
+            "interface_location_err_vs_fp64": iface_loc, "interface_location_err_over_dx_min": iface_loc / dmin,
+            "interface_cut_edges": iface_edges, "interface_sign_mismatches": iface_mismatch,
             "dx_min": dmin,
+            "fp64_vs_oracle_full_grid": parity,
+            "fp64_vs_cpu_same_precision": (value64 / cpu["value"] if cpu else None),
             "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
             "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
             "autotuned_stage_config": stage_cfg, "mixed_tables": ls.table_stats(),

@@ -5,7 +5,7 @@ semi-Lagrangian node interpolation on quadtree/octree grids, as CUDA kernels for
 C ABI (include/lsgpu.h). The Python classes mirror the reference's C++ class API.
 """
 from . import shapes
-from ._lib import LSG_FP64, LSG_MIXED, LsgError, LsgInvalidArgument, load
+from ._lib import LSG_FP64, LSG_MIXED, LsgError, LsgInvalidArgument, LsgTimeout, load
 
 
 def device_cache_bytes() -> int:
@@ -27,7 +27,7 @@ from .save_load import (VecDump, VecLoad, my_p4est_load_forest_and_data, my_p4es
                         my_p4est_vtk_write_all)
 
 __all__ = [
-    "shapes", "load", "LsgError", "LsgInvalidArgument", "LSG_FP64", "LSG_MIXED", "Forest", "my_p4est_brick_new",
+    "shapes", "load", "LsgError", "LsgInvalidArgument", "LsgTimeout", "LSG_FP64", "LSG_MIXED", "Forest", "my_p4est_brick_new",
     "my_p4est_node_neighbors_t", "qnnn_dtype", "my_p4est_level_set_t", "DBL_MAX", "interpolation",
     "my_p4est_interpolation_nodes_t", "my_p4est_semi_lagrangian_t", "VortexVelocity", "my_p4est_level_set_batch_t",
     "save_load", "VecDump", "VecLoad", "my_p4est_save_forest_and_data", "my_p4est_load_forest_and_data",

@@ -107,6 +107,13 @@ SIGNATURES = {
     "lsg_semi_lagrangian_advect_cf": (_I, [_P, _DP, _I64, _D, _I, _DP, _I, _DP, _DP, _I, _DP]),
     "lsg_semi_lagrangian_advect_cf_device": (_I, [_P, _P, _I64, _D, _I, _DP, _I, _P, _P, _I, _P]),
     "lsg_semi_lagrangian_advect_callback": (_I, [_P, _DP, _I64, _D, _P, _P, _DP, _DP, _I, _DP]),
+    "lsg_semi_lagrangian_advect2": (_I, [_P, _P, _DP, _I64, _D, _D, _DP, _DP, _DP, _DP, _DP, _DP, _I, _I, _DP]),
+    "lsg_semi_lagrangian_advect2_device": (_I, [_P, _P, _P, _I64, _D, _D, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "lsg_level_set_set_wait_limit": (_I, [_P, C.c_longlong]),
+    "lsg_second_derivatives_range_device": (_I, [_P, _P, _P, _I64, _I64]),
+    "lsg_reinit_prep_range_device": (_I, [_P, _P, _P, _I, _D, _D, _I64, _I64]),
+    "lsg_reinit_stage_range_device": (_I, [_P, _I, _P, _P, _P, _P, _P, _I64, _I64]),
+    "lsg_interface_location_error_device": (_I, [_P, _P, _P, _DP, C.POINTER(_I64), C.POINTER(_I64)]),
     "lsg_band_linf_device": (_I, [_P, _P, _P, _D, _DP, C.POINTER(_I64)]),
     "lsg_batch_create": (_I, [_I, C.POINTER(_P), C.POINTER(_P)]),
     "lsg_batch_create_ex": (_I, [_I, C.POINTER(_P), _I, C.POINTER(_P)]),
@@ -137,6 +144,10 @@ class LsgInvalidArgument(LsgError, ValueError):
     pass
 
 
+class LsgTimeout(LsgError, TimeoutError):
+    """A bounded device-side wait gave up (LSG_ETIMEOUT); the call's results are incomplete."""
+
+
 _lib = None
 
 
@@ -161,6 +172,8 @@ def check(code: int) -> None:
     msg = load().lsg_last_error().decode(errors="replace")
     if code == LSG_EINVAL:
         raise LsgInvalidArgument(code, msg)
+    if code == LSG_ETIMEOUT:
+        raise LsgTimeout(code, msg)
     raise LsgError(code, msg)
 
 

@@ -26,13 +26,19 @@ struct lsg_forest {
   }
 };
 
+// A level set lives on the device that was current when it was created: every call on it runs there
+// (the caller's current device is restored afterwards), whatever device the caller has current.
 struct lsg_level_set {
   int dim = 2;
+  int device = 0;
   LevelSet<2>* l2 = nullptr;
   LevelSet<3>* l3 = nullptr;
   ~lsg_level_set() {
+    int prev = 0;
+    const bool switched = cudaGetDevice(&prev) == cudaSuccess && prev != device && cudaSetDevice(device) == cudaSuccess;
     delete l2;
     delete l3;
+    if (switched) cudaSetDevice(prev);
   }
 };
 
@@ -95,10 +101,24 @@ void with_forest(const lsg_forest* f, Fn&& fn) {
 template <typename Fn>
 void with_ls(lsg_level_set* ls, Fn&& fn) {
   need(ls != nullptr, "null level set");
+  DeviceGuard on(ls->device);
   if (ls->dim == 2)
     fn(*ls->l2);
   else
     fn(*ls->l3);
+}
+
+// the two level sets of a two-velocity step: same dimension, same device
+template <typename Fn>
+void with_ls_pair(lsg_level_set* n, lsg_level_set* nm1, Fn&& fn) {
+  need(n != nullptr && nm1 != nullptr, "null level set");
+  need(n->dim == nm1->dim, "the grids at n and n-1 must have the same dimension");
+  need(n->device == nm1->device, "the grids at n and n-1 must live on the same device");
+  DeviceGuard on(n->device);
+  if (n->dim == 2)
+    fn(*n->l2, *nm1->l2);
+  else
+    fn(*n->l3, *nm1->l3);
 }
 
 template <int D>
@@ -554,9 +574,11 @@ int lsg_level_set_create_ex(const lsg_forest* f, int flags, lsg_level_set** out)
     try {
       if (f->dim == 2) {
         need_nodes(*f->f2);
+        ls->device = current_device();
         ls->l2 = new LevelSet<2>(*f->f2, true, on_device);
       } else {
         need_nodes(*f->f3);
+        ls->device = current_device();
         ls->l3 = new LevelSet<3>(*f->f3, true, on_device);
       }
     } catch (...) {
@@ -975,6 +997,30 @@ int lsg_semi_lagrangian_advect_device(lsg_level_set* ls, const double* xyz, int6
   });
 }
 
+int lsg_semi_lagrangian_advect2(lsg_level_set* ls_n, lsg_level_set* ls_nm1, const double* xyz_np1, int64_t npts, double dt_nm1,
+                                double dt_n, const double* vnm1, const double* vnm1_dd, const double* vn, const double* vn_dd,
+                                const double* phi_n, const double* phi_dd, int velo_method, int phi_method, double* phi_np1) {
+  return guard([&] {
+    need(vnm1 != nullptr && vn != nullptr && phi_n != nullptr && phi_np1 != nullptr && (xyz_np1 != nullptr || npts == 0),
+         "null argument");
+    with_ls_pair(ls_n, ls_nm1, [&](auto& L, auto& M) {
+      L.sl_advect2_host(M, xyz_np1, npts, dt_nm1, dt_n, vnm1, vnm1_dd, vn, vn_dd, phi_n, phi_dd, velo_method, phi_method, phi_np1);
+    });
+  });
+}
+
+int lsg_semi_lagrangian_advect2_device(lsg_level_set* ls_n, lsg_level_set* ls_nm1, const double* xyz_np1, int64_t npts, double dt_nm1,
+                                       double dt_n, const double* vnm1, const double* vnm1_dd, const double* vn, const double* vn_dd,
+                                       const double* phi_n, const double* phi_dd, int velo_method, int phi_method, double* phi_np1) {
+  return guard([&] {
+    need(vnm1 != nullptr && vn != nullptr && phi_n != nullptr && phi_np1 != nullptr && (xyz_np1 != nullptr || npts == 0),
+         "null argument");
+    with_ls_pair(ls_n, ls_nm1, [&](auto& L, auto& M) {
+      L.sl_advect2(M, xyz_np1, npts, dt_nm1, dt_n, vnm1, vnm1_dd, vn, vn_dd, phi_n, phi_dd, velo_method, phi_method, phi_np1);
+    });
+  });
+}
+
 static double velocity_scale(int velocity, const double* params, int nparams) {
   need(velocity == LSG_VELOCITY_VORTEX, "unknown analytic velocity");
   return (params != nullptr && nparams > 0) ? params[0] : 1.0;
@@ -1048,6 +1094,7 @@ int lsg_batch_create_ex(int count, const lsg_forest* const* forests, int flags, 
     for (int k = 0; k < count; ++k) need(forests[k] != nullptr && forests[k]->dim == dim, "batch: grids of one dimension required");
     lsg_level_set* ls = new lsg_level_set();
     ls->dim = dim;
+    ls->device = current_device();
     try {
       if (dim == 2) {
         std::vector<const Forest<2>*> parts;
@@ -1144,6 +1191,37 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
   });
 }
 
+int lsg_second_derivatives_range_device(lsg_level_set* ls, const double* f_dev, double* f_dd_dev, int64_t first, int64_t count) {
+  return guard([&] {
+    need(f_dev != nullptr && f_dd_dev != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.fp64_dd_range(f_dev, f_dd_dev, first, count); });
+  });
+}
+
+int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, const double* phi0_dd_dev, int order_space, double limit_high,
+                                 double limit_low, int64_t first, int64_t count) {
+  return guard([&] {
+    need(phi0_dev != nullptr, "null phi_0");
+    with_ls(ls, [&](auto& L) { L.fp64_prep_range(phi0_dev, phi0_dd_dev, order_space, limit_high, limit_low, first, count); });
+  });
+}
+
+int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const double* phi0_dev, const double* phin_dev,
+                                  const double* phin_dd_dev, double* out_dev, const double* avg_with_dev, int64_t first, int64_t count) {
+  return guard([&] {
+    need(phi0_dev != nullptr && phin_dev != nullptr && out_dev != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { L.fp64_stage_range(order_space, phi0_dev, phin_dev, phin_dd_dev, out_dev, avg_with_dev, first, count); });
+  });
+}
+
+int lsg_interface_location_error_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double* out, int64_t* edges,
+                                        int64_t* mismatched) {
+  return guard([&] {
+    need(a_dev != nullptr && b_dev != nullptr && out != nullptr, "null argument");
+    with_ls(ls, [&](auto& L) { *out = L.interface_location_error(a_dev, b_dev, edges, mismatched); });
+  });
+}
+
 int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double band, double* out, int64_t* count) {
   return guard([&] {
     need(a_dev != nullptr && b_dev != nullptr && out != nullptr, "null argument");
@@ -1170,6 +1248,10 @@ int lsg_level_set_table_stats(lsg_level_set* ls, int64_t* out) {
 
 int lsg_level_set_enable_kernel_timing(lsg_level_set* ls, int on) {
   return guard([&] { with_ls(ls, [&](auto& L) { L.timer.enabled = on != 0; }); });
+}
+
+int lsg_level_set_set_wait_limit(lsg_level_set* ls, long long cycles) {
+  return guard([&] { with_ls(ls, [&](auto& L) { L.set_wait_limit(cycles); }); });
 }
 
 int lsg_level_set_kernel_times(lsg_level_set* ls, double* ms, int64_t* counts, int nkinds, int reset) {

@@ -28,11 +28,40 @@ inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Makes `dev` the current device for its lifetime and restores the caller's device afterwards.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    cuda_check(cudaGetDevice(&prev_), "cudaGetDevice");
+    if (dev != prev_) {
+      cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+      switched_ = true;
+    }
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = 0;
+  bool switched_ = false;
+};
+
+inline int current_device() {
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  return dev;
+}
+
 // Device memory cache behind every DevBuf. A released block is kept for reuse instead of going back
 // to the driver (cudaMalloc and cudaFree cost tens of microseconds each, and cudaFree waits for the
 // whole device); a level set built for every new grid otherwise pays that for each of its tables.
-// Reuse keeps cudaFree's guarantee: a block released since the last device synchronisation is handed
-// out again only after a cudaDeviceSynchronize, so no kernel still in flight can see it change owner.
+// Reuse keeps cudaFree's guarantee: a block released since its device's last synchronisation is handed
+// out again only after a cudaDeviceSynchronize of that device, so no kernel still in flight can see it
+// change owner. The synchronisation count is kept per device: synchronising one GPU says nothing about
+// the kernels in flight on another.
 // Blocks are grouped by size class (eight classes per power of two, at most 12.5% unused).
 class DeviceCache {
  public:
@@ -57,9 +86,9 @@ class DeviceCache {
         Block b = it->second.back();
         it->second.pop_back();
         cached_ -= cls;
-        if (b.epoch == epoch_) {
+        if (b.epoch == epoch_[dev]) {  // released since this device's last synchronisation
           cuda_check(cudaDeviceSynchronize(), "device synchronisation before reuse");
-          ++epoch_;
+          ++epoch_[dev];
         }
         return b.p;
       }
@@ -83,23 +112,41 @@ class DeviceCache {
     {
       std::lock_guard<std::mutex> g(mu_);
       if (cls <= kMaxBlock && cached_ + cls <= kMaxCached) {
-        free_[Key{dev, cls}].push_back(Block{p, epoch_});
+        free_[Key{dev, cls}].push_back(Block{p, epoch_[dev]});
         cached_ += cls;
         return;
       }
     }
-    cudaFree(p);
+    int cur = -1;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != dev) {
+      cudaSetDevice(dev);
+      cudaFree(p);
+      cudaSetDevice(cur);
+    } else {
+      cudaFree(p);
+    }
   }
-  // return every cached block to the driver
+  // return every cached block to the driver (each device synchronised before its blocks are freed)
   void trim() {
     std::lock_guard<std::mutex> g(mu_);
     if (cached_ == 0) return;
-    cudaDeviceSynchronize();
-    for (auto& kv : free_)
+    int cur = 0;
+    cudaGetDevice(&cur);
+    int synced = -1;
+    for (auto& kv : free_) {  // ordered by device
+      if (kv.second.empty()) continue;
+      const int dev = kv.first.dev;
+      if (dev != synced) {
+        cudaSetDevice(dev);
+        cudaDeviceSynchronize();
+        ++epoch_[dev];
+        synced = dev;
+      }
       for (const Block& b : kv.second) cudaFree(b.p);
+    }
+    cudaSetDevice(cur);
     free_.clear();
     cached_ = 0;
-    ++epoch_;
   }
   size_t cached_bytes() {
     std::lock_guard<std::mutex> g(mu_);
@@ -116,12 +163,12 @@ class DeviceCache {
   };
   struct Block {
     void* p;
-    uint64_t epoch;  // the synchronisation count at release
+    uint64_t epoch;  // its device's synchronisation count at release
   };
   std::mutex mu_;
   std::map<Key, std::vector<Block>> free_;
   size_t cached_ = 0;
-  uint64_t epoch_ = 0;
+  std::map<int, uint64_t> epoch_;  // synchronisations per device
 };
 
 template <typename T>

@@ -39,6 +39,9 @@ struct StageCfg {
   // pipeline of the uniform kernel: 1 or 2 nodes whose gathers are in flight per thread, or 3: the
   // node words bulk-copied into shared memory three tiles ahead (cp.async.bulk + mbarrier)
   int depth = 1;
+  // bound of the bulk kernel's waits for its copies, in SM clock cycles (0: about a second); a wait that
+  // runs out makes the call report LSG_ETIMEOUT
+  long long wait_cycles = 0;
 };
 
 template <int D>
@@ -113,15 +116,17 @@ struct DTab32 {
   const double* corr64;
 };
 
+// FP64 sweeps over the nodes [first, first + count) (count < 0: to the last node), by default all of them.
 template <int D>
-void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s);
+void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s, int64_t first = 0, int64_t count = -1);
 template <int D>
 void launch_reinit_prep64(const DTab64<D>& T, const double* phi0, const double* dd0, double zdt, double lim_lo, double lim_hi,
-                          int order_space, uint16_t* status, double* s_near, cudaStream_t s);
+                          int order_space, uint16_t* status, double* s_near, cudaStream_t s, int64_t first = 0, int64_t count = -1);
 // out = stage(phin); if avg_with != nullptr: out = 0.5*(avg_with + stage(phin)) (may alias avg_with).
 template <int D>
 void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* status, const double* s_near, const double* phi0,
-                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s);
+                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s,
+                           int64_t first = 0, int64_t count = -1);
 template <int D>
 void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double* ddq, const double* ddm, const double* vn, double dt,
                            double* out, const double* avg_with, cudaStream_t s);
@@ -171,6 +176,10 @@ void launch_ext_q(const DTab64<D>& T, const double* q, double* tmp, const double
 // nodes whose mask is 0 (mask in node order; perm maps status indices to nodes, or null) become ST_OUTSIDE
 void launch_apply_mask(const double* mask, const int32_t* perm, uint16_t* status, int64_t n, cudaStream_t s);
 void launch_band_linf64(const double* a, const double* b, double band, int64_t n, unsigned long long* out3, cudaStream_t s);
+// FP64 interface location along cut grid edges: out3 = {bits of max |t_a - t_b|, cut edges of b, edges where a
+// does not change sign}, t the linear zero crossing's distance from the edge's first node
+template <int D>
+void launch_iface_err64(const DTab64<D>& T, const double* a, const double* b, unsigned long long* out3, cudaStream_t s);
 // Node interpolation (kernels_interp.cu, FP64). Points: D doubles each. When shift is given, point p
 // is first moved to xyz[p] - coef*shift[:, p] and clipped into the domain (the semi-Lagrangian
 // backtrace). F: nf x N values, Fdd: nf x D x N second derivatives (ignored for linear), out: nf x np.
@@ -182,6 +191,11 @@ void launch_interp64(const DLoc<D>& L, int method, const double* xyz, int64_t np
 template <int D>
 void launch_sl_vortex64(const DLoc<D>& L, int method, const double* xyz, int64_t np, double dt, double vscale, const double* phi,
                         const double* phi_dd, double* out, cudaStream_t s);
+// Last round of the two-velocity semi-Lagrangian step: x_d = xyz - dt_n (ca vn_star - cb vnm1_star)
+// (D x np each), clipped, and phi interpolated there.
+template <int D>
+void launch_sl2_phi64(const DLoc<D>& L, int method, const double* xyz, int64_t np, const double* vn_star, const double* vnm1_star,
+                      double ca, double cb, double dt_n, const double* phi, const double* phi_dd, double* out, cudaStream_t s);
 // Leaf chosen by the point location for each point (clipped first).
 template <int D>
 void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* leaf, cudaStream_t s);

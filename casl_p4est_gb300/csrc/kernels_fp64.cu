@@ -24,9 +24,10 @@ using namespace st64;
 constexpr int TPB = 256;
 
 template <int D>
-__global__ void __launch_bounds__(TPB) k_dd64(DTab64<D> T, const double* __restrict__ f, double* __restrict__ dd) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= T.N) return;
+__global__ void __launch_bounds__(TPB) k_dd64(DTab64<D> T, const double* __restrict__ f, double* __restrict__ dd, int64_t first,
+                                              int64_t last) {
+  const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= last) return;
   double Dv[D];
   laplace64<D>(T, n, f, Dv);
 #pragma unroll
@@ -38,10 +39,11 @@ __global__ void __launch_bounds__(TPB) k_dd64(DTab64<D> T, const double* __restr
 template <int D>
 __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0,
                                                        double zdt, double lim_lo, double lim_hi, int order_space,
-                                                       uint16_t* __restrict__ status, double* __restrict__ s_near) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                       uint16_t* __restrict__ status, double* __restrict__ s_near, int64_t first,
+                                                       int64_t last) {
+  const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
-  if (n >= N) return;
+  if (n >= last) return;
   const double p0 = phi0[n];
   if (fabs(p0) < zdt) {
     status[n] = ST_ANCHORED;
@@ -93,10 +95,11 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
                                                         const double* __restrict__ phi0, const double* __restrict__ phin,
-                                                        const double* __restrict__ dd, double* out, const double* avg_with) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                        const double* __restrict__ dd, double* out, const double* avg_with,
+                                                        int64_t first, int64_t last) {
+  const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
-  if (n >= N) return;
+  if (n >= last) return;
   const uint16_t st = status[n];
   double r;
   if (st & ST_ANCHORED) {
@@ -704,6 +707,73 @@ __global__ void __launch_bounds__(TPB) k_band_linf64(const double* __restrict__ 
   }
 }
 
+// Interface location along cut grid edges, in FP64: every node n and direction whose stencil slot holds
+// a single node (a grid edge to a node at distance d) where the reference field b changes sign; the crossing
+// lies at t_b = d b_n / (b_n - b_nb) from n (the linear root along the edge). Where a changes sign on the same
+// edge, |t_a - t_b| enters the maximum; otherwise the edge counts as a sign mismatch. out: max bits, cut edges,
+// mismatched edges (each edge is seen from both ends). Same reduction as k_band_linf64.
+template <int D>
+__global__ void __launch_bounds__(TPB) k_iface_err64(DTab64<D> T, const double* __restrict__ a, const double* __restrict__ b,
+                                                     unsigned long long* __restrict__ out) {
+  constexpr int H = Dim<D>::HALF;
+  __shared__ double s_max[TPB / 32];
+  __shared__ unsigned long long s_cnt[TPB / 32], s_mis[TPB / 32];
+  const int64_t N = T.N;
+  double m = 0.0;
+  unsigned long long cnt = 0, mis = 0;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const double b0 = b[n], a0 = a[n];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int64_t base = (int64_t)(dir * H) * N + n;
+      bool single = true;
+#pragma unroll
+      for (int k = 1; k < H; ++k) single = single && T.nbr[base + k * N] < 0;
+      const int32_t nb = T.nbr[base];
+      if (!single || nb < 0 || nb == n) continue;
+      const double b1 = b[nb];
+      if (!(b0 * b1 < 0.0)) continue;
+      ++cnt;
+      const double a1 = a[nb];
+      if (!(a0 * a1 < 0.0)) {
+        ++mis;
+        continue;
+      }
+      const double d = T.d[(int64_t)dir * N + n];
+      const double tb = d * b0 / (b0 - b1), ta = d * a0 / (a0 - a1);
+      m = fmax(m, fabs(ta - tb));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    mis += __shfl_xor_sync(0xffffffffu, mis, o);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    s_max[w] = m;
+    s_cnt[w] = cnt;
+    s_mis[w] = mis;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    m = lane < nw ? s_max[lane] : 0.0;
+    cnt = lane < nw ? s_cnt[lane] : 0ull;
+    mis = lane < nw ? s_mis[lane] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      mis += __shfl_xor_sync(0xffffffffu, mis, o);
+    }
+    if (lane == 0) {
+      atomicMax(out, (unsigned long long)__double_as_longlong(m));
+      atomicAdd(out + 1, cnt);
+      atomicAdd(out + 2, mis);
+    }
+  }
+}
+
 inline unsigned nblocks(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 
 }  // namespace
@@ -791,33 +861,46 @@ void launch_band_linf64(const double* a, const double* b, double band, int64_t n
 }
 
 template <int D>
-void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s) {
+void launch_iface_err64(const DTab64<D>& T, const double* a, const double* b, unsigned long long* out3, cudaStream_t s) {
+  cudaMemsetAsync(out3, 0, 3 * sizeof(unsigned long long), s);
   if (T.N == 0) return;
-  k_dd64<D><<<nblocks(T.N), TPB, 0, s>>>(T, f, dd);
+  const unsigned g = std::min<unsigned>(nblocks(T.N), (unsigned)device_sm_count() * 8u);
+  k_iface_err64<D><<<g, TPB, 0, s>>>(T, a, b, out3);
+}
+
+// Each sweep covers the nodes [first, first + count) (count < 0: every node from first on).
+template <int D>
+void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s, int64_t first, int64_t count) {
+  const int64_t last = count < 0 ? T.N : first + count;
+  if (last <= first) return;
+  k_dd64<D><<<nblocks(last - first), TPB, 0, s>>>(T, f, dd, first, last);
 }
 
 template <int D>
 void launch_reinit_prep64(const DTab64<D>& T, const double* phi0, const double* dd0, double zdt, double lim_lo, double lim_hi,
-                          int order_space, uint16_t* status, double* s_near, cudaStream_t s) {
-  if (T.N == 0) return;
-  k_reinit_prep64<D><<<nblocks(T.N), TPB, 0, s>>>(T, phi0, dd0, zdt, lim_lo, lim_hi, order_space, status, s_near);
+                          int order_space, uint16_t* status, double* s_near, cudaStream_t s, int64_t first, int64_t count) {
+  const int64_t last = count < 0 ? T.N : first + count;
+  if (last <= first) return;
+  k_reinit_prep64<D><<<nblocks(last - first), TPB, 0, s>>>(T, phi0, dd0, zdt, lim_lo, lim_hi, order_space, status, s_near, first, last);
 }
 
 template <int D>
 void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* status, const double* s_near, const double* phi0,
-                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s) {
-  if (T.N == 0) return;
-  const unsigned g = nblocks(T.N);
+                           const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s, int64_t first,
+                           int64_t count) {
+  const int64_t last = count < 0 ? T.N : first + count;
+  if (last <= first) return;
+  const unsigned g = nblocks(last - first);
   if (order_space > 1) {
     if (avg_with)
-      k_reinit_stage64<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+      k_reinit_stage64<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with, first, last);
     else
-      k_reinit_stage64<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+      k_reinit_stage64<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with, first, last);
   } else {
     if (avg_with)
-      k_reinit_stage64<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+      k_reinit_stage64<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with, first, last);
     else
-      k_reinit_stage64<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with);
+      k_reinit_stage64<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phi0, phin, dd, out, avg_with, first, last);
   }
 }
 
@@ -844,11 +927,12 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
 }
 
 #define LSG_INST(D)                                                                                                          \
-  template void launch_dd64<D>(const DTab64<D>&, const double*, double*, cudaStream_t);                                      \
+  template void launch_dd64<D>(const DTab64<D>&, const double*, double*, cudaStream_t, int64_t, int64_t);                    \
+  template void launch_iface_err64<D>(const DTab64<D>&, const double*, const double*, unsigned long long*, cudaStream_t);     \
   template void launch_reinit_prep64<D>(const DTab64<D>&, const double*, const double*, double, double, double, int, uint16_t*, \
-                                        double*, cudaStream_t);                                                              \
+                                        double*, cudaStream_t, int64_t, int64_t);                                            \
   template void launch_reinit_stage64<D>(const DTab64<D>&, int, const uint16_t*, const double*, const double*, const double*, \
-                                         const double*, double*, const double*, cudaStream_t);                               \
+                                         const double*, double*, const double*, cudaStream_t, int64_t, int64_t);             \
   template void launch_advect_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, double,  \
                                          double*, const double*, cudaStream_t);                                              \
   template void launch_grad64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, int, cudaStream_t);      \

@@ -287,6 +287,27 @@ __global__ void __launch_bounds__(TPB) k_sl_vortex64(DLoc<D> L, const double* __
   interpolate_at<D, M>(L, xd, 1, phi, phi_dd, np, p, out);
 }
 
+// Last round of the two-velocity semi-Lagrangian step (src/my_p4est_semi_lagrangian.cpp:296-314): with
+// v_n(x*) and v_nm1(x*) from the previous rounds, v* = ca v_n(x*) - cb v_nm1(x*) (ca = 1 + dt_n/(2 dt_nm1),
+// cb = dt_n/(2 dt_nm1), formed by the caller in the reference's order), x_d = x - dt_n v* clipped into the
+// domain, and phi_n interpolated at x_d.
+template <int D, int M>
+__global__ void __launch_bounds__(TPB) k_sl2_phi64(DLoc<D> L, const double* __restrict__ xyz, int64_t np,
+                                                   const double* __restrict__ vn_star, const double* __restrict__ vnm1_star, double ca,
+                                                   double cb, double dt_n, const double* __restrict__ phi,
+                                                   const double* __restrict__ phi_dd, double* __restrict__ out) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  double x[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double vs = ca * vn_star[(int64_t)a * np + p] - cb * vnm1_star[(int64_t)a * np + p];
+    x[a] = xyz[p * D + a] - dt_n * vs;
+  }
+  clip_in_domain<D>(L, x);
+  interpolate_at<D, M>(L, x, 1, phi, phi_dd, np, p, out);
+}
+
 template <int D>
 __global__ void __launch_bounds__(TPB) k_locate64(DLoc<D> L, const double* __restrict__ xyz, int64_t np, int32_t* __restrict__ leaf) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -435,6 +456,20 @@ void launch_sl_vortex64(const DLoc<D>& L, int method, const double* xyz, int64_t
 }
 
 template <int D>
+void launch_sl2_phi64(const DLoc<D>& L, int method, const double* xyz, int64_t np, const double* vn_star, const double* vnm1_star,
+                      double ca, double cb, double dt_n, const double* phi, const double* phi_dd, double* out, cudaStream_t s) {
+  if (np == 0) return;
+  const int64_t g = nblocks(np);
+  switch (method) {
+    case 0: k_sl2_phi64<D, 0><<<g, TPB, 0, s>>>(L, xyz, np, vn_star, vnm1_star, ca, cb, dt_n, phi, phi_dd, out); break;
+    case 1: k_sl2_phi64<D, 1><<<g, TPB, 0, s>>>(L, xyz, np, vn_star, vnm1_star, ca, cb, dt_n, phi, phi_dd, out); break;
+    case 2: k_sl2_phi64<D, 2><<<g, TPB, 0, s>>>(L, xyz, np, vn_star, vnm1_star, ca, cb, dt_n, phi, phi_dd, out); break;
+    case 3: k_sl2_phi64<D, 3><<<g, TPB, 0, s>>>(L, xyz, np, vn_star, vnm1_star, ca, cb, dt_n, phi, phi_dd, out); break;
+    default: k_sl2_phi64<D, 4><<<g, TPB, 0, s>>>(L, xyz, np, vn_star, vnm1_star, ca, cb, dt_n, phi, phi_dd, out); break;
+  }
+}
+
+template <int D>
 void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* leaf, cudaStream_t s) {
   if (np == 0) return;
   k_locate64<D><<<nblocks(np), TPB, 0, s>>>(L, xyz, np, leaf);
@@ -446,6 +481,8 @@ void launch_locate64(const DLoc<D>& L, const double* xyz, int64_t np, int32_t* l
   template void launch_sl_vortex64<D>(const DLoc<D>&, int, const double*, int64_t, double, double, const double*, const double*, \
                                       double*, cudaStream_t);                                                                  \
   template void launch_locate64<D>(const DLoc<D>&, const double*, int64_t, int32_t*, cudaStream_t);                              \
+  template void launch_sl2_phi64<D>(const DLoc<D>&, int, const double*, int64_t, const double*, const double*, double, double,   \
+                                    double, const double*, const double*, double*, cudaStream_t);                               \
   template void launch_efi_init64<D>(const DTab64<D>&, const DLoc<D>&, int, const double*, const double*, const double*,        \
                                      const double*, const double*, const double*, double, double, double, double*, double*,     \
                                      double*, uint8_t*, cudaStream_t);

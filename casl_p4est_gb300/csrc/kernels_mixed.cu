@@ -636,8 +636,10 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uin
 // and read at the remainder. A tile is copied only when its node range ends at least 8 nodes before
 // the uniform group does, so every copied byte lies inside its array (a plane of the index tables
 // holds nR >= nU entries); the last tiles load directly from global memory. Every wait on an
-// mbarrier is bounded (about a second of clock cycles); a wait that runs out sets *err and the CTA
-// stops. NPT nodes per thread and tile: the launcher uses one (two measured slower on the 13.7M-node
+// mbarrier is bounded (wait_cycles SM clock cycles, about a second by default); the CTA then decides
+// together (__syncthreads_or, so no thread is left at a barrier the others skip) whether any thread gave
+// up, and if so sets *err, lets the copies it issued land (bounded by the full limit) and stops.
+// NPT nodes per thread and tile: the launcher uses one (two measured slower on the 13.7M-node
 // flower grid: fewer, larger tiles leave less room for the concurrent irregular kernels).
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -651,24 +653,27 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
       "r"(bytes)
       : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// non-blocking test of the phase (test_wait, unlike try_wait, never suspends the thread, so the bound
+// below is kept to the cycle)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(done)
       : "r"(smem_addr(bar)), "r"(parity)
       : "memory");
   return done != 0;
 }
-// false once about 2^31 SM cycles (about a second) have passed without the phase completing
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// false once `limit` SM cycles have passed without the phase completing
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1ll << 31)) return false;
+  while (!mbar_test_wait(bar, parity))
+    if (clock64() - t0 > limit) return false;
   return true;
 }
+constexpr long long kFullWaitCycles = 1ll << 31;  // about a second at the SM clock
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src),
                "r"(bytes), "r"(smem_addr(bar))
@@ -713,7 +718,7 @@ struct UniBulk {
 template <int D, bool AVG, int STAGES, int NPT>
 __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, const uint16_t* __restrict__ status,
                                                                const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                               float* out, const float* avg_with, int* err) {
+                                                               float* out, const float* avg_with, int* err, long long wait_cycles) {
   using B = UniBulk<D, AVG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[STAGES];
@@ -766,12 +771,16 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
     const int64_t m0 = t * (int64_t)tile;
     UniIdx<D> I[NPT];
     bool have[NPT];
-    if (bulk_ok(t)) {
-      if (!mbar_wait_bounded(&full[s], (uint32_t)((k / STAGES) & 1))) {
-        atomicOr(err, 1);
-        if (tid == 0)  // let the copies this CTA issued land (bounded) before it exits
+    if (bulk_ok(t)) {  // the same for every thread of the CTA
+      const bool landed = mbar_wait_bounded(&full[s], (uint32_t)((k / STAGES) & 1), wait_cycles);
+      if (__syncthreads_or(!landed)) {
+        if (tid == 0) {
+          atomicOr(err, 1);
+          // let the copies this CTA issued land (bounded by the full limit) before it exits
           for (int64_t kk = k; kk < k + STAGES; ++kk)
-            if (tile_of(kk) < ntiles && bulk_ok(tile_of(kk))) mbar_wait_bounded(&full[kk % STAGES], (uint32_t)((kk / STAGES) & 1));
+            if (tile_of(kk) < ntiles && bulk_ok(tile_of(kk)))
+              mbar_wait_bounded(&full[kk % STAGES], (uint32_t)((kk / STAGES) & 1), kFullWaitCycles);
+        }
         return;
       }
       const unsigned char* st = smem + (size_t)s * sb;
@@ -1232,7 +1241,7 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
     const int full = device_sm_count() * (per_sm > 0 ? per_sm : 1);
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
     const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
-    kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err);
+    kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err, cfg.wait_cycles > 0 ? cfg.wait_cycles : kFullWaitCycles);
   } else if (part == STAGE_PART_UNIFORM && uni_end > 0) {
     const int full = (cfg.depth == 2 ? gb_uni2 : gb_uni) * scale;
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;

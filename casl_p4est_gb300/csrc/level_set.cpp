@@ -388,6 +388,43 @@ void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo,
   cuda_check(cudaGetLastError(), "reinitialize (fp64)");
 }
 
+static void check_range(int64_t first, int64_t count, int64_t N) {
+  if (first < 0 || count < 0 || first > N || count > N - first) throw std::invalid_argument("node range outside the grid");
+}
+
+template <int D>
+void LevelSet<D>::fp64_dd_range(const double* f, double* dd, int64_t first, int64_t count) {
+  check_range(first, count, N);
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, f, dd, stream, first, count));
+  cuda_check(cudaGetLastError(), "second derivatives (node range)");
+}
+
+template <int D>
+void LevelSet<D>::fp64_prep_range(const double* phi0_, const double* dd0_, int os, double limit_high, double limit_low, int64_t first,
+                                  int64_t count) {
+  check_range(first, count, N);
+  if (os < 1 || os > 2) throw std::invalid_argument("reinitialize: the order in space must be 1 or 2");
+  if (!(limit_high > limit_low)) throw std::invalid_argument("reinitialize: limit_high must exceed limit_low");
+  if (os > 1 && !dd0_) throw std::invalid_argument("reinitialize: second order in space needs phi_0's second derivatives");
+  const double big = largest_dbl_smaller_than_dbl_max();
+  const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
+  const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
+  snear.ensure((size_t)2 * D * N);
+  status.ensure((size_t)N);
+  LSG_LAUNCH(K_PREP64, launch_reinit_prep64<D>(T64, phi0_, dd0_, zdt, lo, hi, os, status.p, snear.p, stream, first, count));
+  cuda_check(cudaGetLastError(), "reinitialize preparation (node range)");
+}
+
+template <int D>
+void LevelSet<D>::fp64_stage_range(int os, const double* phi0_, const double* phin, const double* dd, double* out, const double* avg_with,
+                                   int64_t first, int64_t count) {
+  check_range(first, count, N);
+  if (!status.p || status.n < (size_t)N) throw std::invalid_argument("reinitialize stage: run the preparation first");
+  if (os > 1 && !dd) throw std::invalid_argument("reinitialize stage: second order in space needs the second derivatives");
+  LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0_, phin, dd, out, avg_with, stream, first, count));
+  cuda_check(cudaGetLastError(), "reinitialize stage (node range)");
+}
+
 template <int D>
 void LevelSet<D>::build_mixed() {
   if (mixed_ready) return;
@@ -480,18 +517,26 @@ void LevelSet<D>::set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int bas
 }
 
 template <int D>
-void LevelSet<D>::check_device_waits() {
-  if (!kerr.p) return;
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cuda_check(cudaStreamIsCapturing(stream, &cs), "cudaStreamIsCapturing");
-  if (cs != cudaStreamCaptureStatusNone) return;
+bool LevelSet<D>::take_device_wait_flag() {
+  if (!kerr.p) return false;
   int h = 0;
   cuda_check(cudaMemcpyAsync(&h, kerr.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H");
   cuda_check(cudaStreamSynchronize(stream), "device wait check");
   if (h) {
     cuda_check(cudaMemsetAsync(kerr.p, 0, sizeof(int), stream), "memset");
-    throw DeviceTimeout("reinitialize (mixed): a bounded wait for a bulk copy gave up; results of this call are incomplete");
+    cuda_check(cudaStreamSynchronize(stream), "device wait check");
   }
+  return h != 0;
+}
+
+template <int D>
+void LevelSet<D>::check_device_waits() {
+  if (!kerr.p) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cuda_check(cudaStreamIsCapturing(stream, &cs), "cudaStreamIsCapturing");
+  if (cs != cudaStreamCaptureStatusNone) return;
+  if (take_device_wait_flag())
+    throw DeviceTimeout("reinitialize (mixed): a bounded wait for a bulk copy gave up; results of this call are incomplete");
 }
 
 // One RK stage of the mixed path on two streams: the side stream computes the extended second
@@ -701,14 +746,19 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
     float ms = 0;
     cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    // a candidate whose bounded waits gave up left CTAs early: it only looks fast, so drop it
+    if (c.depth == 3 && take_device_wait_flag()) return 1e30f;
     return ms;
   };
+  const long long wait_cycles = cfg.wait_cycles;
   StageCfg best;
+  best.wait_cycles = wait_cycles;
   float best_ms = 1e30f;
   const int grids[] = {0, 2, 3, 4, 6};
   for (int tpb : {256, 128}) {
     StageCfg c;
     c.tpb = tpb;
+    c.wait_cycles = wait_cycles;
     float c_ms = 1e30f;
     for (int depth : {1, 2, 3})
       for (int g : grids) {
@@ -817,6 +867,20 @@ double LevelSet<D>::band_linf(const double* a, const double* b, double band, int
   cuda_check(cudaStreamSynchronize(stream), "band check sync");
   if (count) *count = (int64_t)h[1];
   if (h[2]) return NAN;
+  double v;
+  memcpy(&v, &h[0], sizeof(v));
+  return v;
+}
+
+template <int D>
+double LevelSet<D>::interface_location_error(const double* a, const double* b, int64_t* edges, int64_t* mismatched) {
+  linf_buf.ensure(3);
+  LSG_LAUNCH(K_CONVERT, launch_iface_err64<D>(T64, a, b, linf_buf.p, stream));
+  unsigned long long h[3] = {0, 0, 0};
+  cuda_check(cudaMemcpyAsync(h, linf_buf.p, sizeof(h), cudaMemcpyDeviceToHost, stream), "interface check");
+  cuda_check(cudaStreamSynchronize(stream), "interface check sync");
+  if (edges) *edges = (int64_t)h[1];
+  if (mismatched) *mismatched = (int64_t)h[2];
   double v;
   memcpy(&v, &h[0], sizeof(v));
   return v;
@@ -1185,6 +1249,45 @@ void LevelSet<D>::sl_advect(const double* xyz, int64_t np, double dt, const doub
   cuda_check(cudaGetLastError(), "advect_from_n_to_np1");
 }
 
+// advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1)
+// (src/my_p4est_semi_lagrangian.cpp:225-319): v_n at the new nodes by quadratic interpolation (the
+// reference fixes that method for this round), then at x* = x - dt_n/2 v_n (clipped) v_n on this grid and
+// v_nm1 on grid n-1 with velo_method, and phi_n at x_d = x - dt_n v* with v* = (1 + dt_n/(2 dt_nm1)) v_n(x*) -
+// dt_n/(2 dt_nm1) v_nm1(x*). Four launches, all on this object's stream.
+template <int D>
+void LevelSet<D>::sl_advect2(LevelSet<D>& nm1, const double* xyz, int64_t np, double dt_nm1, double dt_n, const double* vnm1,
+                             const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd,
+                             int velo_method, int phi_method, double* phi_np1) {
+  check_method(velo_method);
+  check_method(phi_method);
+  if (np < 0) throw std::invalid_argument("advect_from_n_to_np1: negative number of points");
+  if (!(dt_nm1 > 0.0)) throw std::invalid_argument("advect_from_n_to_np1: dt_nm1 must be positive");
+  build_locator();
+  nm1.build_locator();
+  const double* vd = derivatives_of(D, vn, vn_dd, ws_fdd);  // the quadratic round needs them whatever velo_method is
+  const double* md = nullptr;
+  if (velo_method != 0) {
+    md = vnm1_dd;
+    if (!md) {  // as compute_derivatives does on grid n-1, on this stream
+      ws_fdd3.ensure((size_t)D * D * nm1.N);
+      for (int k = 0; k < D; ++k)
+        LSG_LAUNCH(K_DD64, launch_dd64<D>(nm1.T64, vnm1 + (size_t)k * nm1.N, ws_fdd3.p + (size_t)k * D * nm1.N, stream));
+      md = ws_fdd3.p;
+    }
+  }
+  const double* pd = phi_method == 0 ? nullptr : derivatives_of(1, phi, phi_dd, ws_fdd2);
+  ws_v1.ensure((size_t)D * np + 1);
+  ws_v2.ensure((size_t)D * np + 1);
+  ws_v3.ensure((size_t)D * np + 1);
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, 1, xyz, np, nullptr, 0.0, D, vn, vd, ws_v1.p, stream));
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(nm1.TL, velo_method, xyz, np, ws_v1.p, 0.5 * dt_n, D, vnm1, md, ws_v3.p, stream));
+  LSG_LAUNCH(K_INTERP, launch_interp64<D>(TL, velo_method, xyz, np, ws_v1.p, 0.5 * dt_n, D, vn, velo_method == 0 ? nullptr : vd,
+                                          ws_v2.p, stream));
+  const double ca = 1.0 + .5 * dt_n / dt_nm1, cb = 0.5 * dt_n / dt_nm1;
+  LSG_LAUNCH(K_INTERP, launch_sl2_phi64<D>(TL, phi_method, xyz, np, ws_v2.p, ws_v3.p, ca, cb, dt_n, phi, pd, phi_np1, stream));
+  cuda_check(cudaGetLastError(), "advect_from_n_to_np1 (two velocities)");
+}
+
 template <int D>
 void LevelSet<D>::sl_advect_vortex(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd,
                                    int phi_method, double* phi_np1) {
@@ -1253,6 +1356,39 @@ void LevelSet<D>::sl_advect_vortex_host(const double* xyz, int64_t np, double dt
   if (phi_dd) h2d(dpdd, phi_dd, npd, stream);
   sl_advect_vortex(ws_xyz.p, np, dt, vscale, ws_f.p, dpdd, phi_method, ws_out.p);
   if (np) cuda_check(cudaMemcpyAsync(phi_np1, ws_out.p, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
+  cuda_check(cudaStreamSynchronize(stream), "advect_from_n_to_np1 sync");
+}
+
+template <int D>
+void LevelSet<D>::sl_advect2_host(LevelSet<D>& nm1, const double* xyz, int64_t np, double dt_nm1, double dt_n, const double* vnm1,
+                                  const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd,
+                                  int velo_method, int phi_method, double* phi_np1) {
+  const size_t Nm = (size_t)nm1.N;
+  DevBuf<double> d_xyz, d_vn, d_vm, d_phi, d_vnd, d_vmd, d_pd, d_out;
+  d_xyz.alloc((size_t)D * np + 1);
+  d_vn.alloc((size_t)D * N);
+  d_vm.alloc((size_t)D * Nm + 1);
+  d_phi.alloc((size_t)N);
+  d_out.alloc((size_t)np + 1);
+  h2d(d_xyz.p, xyz, (size_t)D * np, stream);
+  h2d(d_vn.p, vn, (size_t)D * N, stream);
+  h2d(d_vm.p, vnm1, (size_t)D * Nm, stream);
+  h2d(d_phi.p, phi, (size_t)N, stream);
+  if (vn_dd) {
+    d_vnd.alloc((size_t)D * D * N);
+    h2d(d_vnd.p, vn_dd, (size_t)D * D * N, stream);
+  }
+  if (vnm1_dd) {
+    d_vmd.alloc((size_t)D * D * Nm + 1);
+    h2d(d_vmd.p, vnm1_dd, (size_t)D * D * Nm, stream);
+  }
+  if (phi_dd) {
+    d_pd.alloc((size_t)D * N);
+    h2d(d_pd.p, phi_dd, (size_t)D * N, stream);
+  }
+  sl_advect2(nm1, d_xyz.p, np, dt_nm1, dt_n, d_vm.p, vnm1_dd ? d_vmd.p : nullptr, d_vn.p, vn_dd ? d_vnd.p : nullptr, d_phi.p,
+             phi_dd ? d_pd.p : nullptr, velo_method, phi_method, d_out.p);
+  if (np) cuda_check(cudaMemcpyAsync(phi_np1, d_out.p, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, stream), "D2H");
   cuda_check(cudaStreamSynchronize(stream), "advect_from_n_to_np1 sync");
 }
 

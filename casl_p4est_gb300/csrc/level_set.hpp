@@ -96,7 +96,7 @@ struct LevelSet {
   // work vectors
   DevBuf<double> ws_phi, phi0, phi1, dd0, ddc, snear, ws_vn, ws_vn1, ws_dd, dt_dev;
   DevBuf<double> ws_gdd, ws_gdd2;
-  DevBuf<double> ws_xyz, ws_f, ws_fdd, ws_out, ws_v1, ws_v2, ws_fdd2;
+  DevBuf<double> ws_xyz, ws_f, ws_fdd, ws_out, ws_v1, ws_v2, ws_v3, ws_fdd2, ws_fdd3;
   DevBuf<unsigned long long> linf_buf;
   DevBuf<uint16_t> status;
   DevBuf<float> f_phi0, f_phi, f_phi1, f_dd, f_ddm, f_snear, f_vn;
@@ -139,6 +139,19 @@ struct LevelSet {
   // FP64 band check: max |a - b| over the nodes with |b| < band (device pointers, N values each);
   // NaN if a NaN was met; count: nodes in the band.
   double band_linf(const double* a, const double* b, double band, int64_t* count);
+  // interface location check: max over the grid edges cut by b of the distance between a's and b's linear
+  // zero crossings (device pointers, N values each); edges: edges cut by b, mismatched: of those, edges a
+  // does not cut.
+  double interface_location_error(const double* a, const double* b, int64_t* edges, int64_t* mismatched);
+
+  // The per-rank FP64 sweeps of a Morton-range split: each covers nodes [first, first + count) only and
+  // reads every other node's value from the full-length (device, node-order) arrays the caller keeps
+  // current with its halo exchange. prep: status and subcell distances from phi_0 (kept in this object)
+  // with the caller's phi_0 limits; stage: out = stage(phin) or 0.5 (avg_with + stage(phin)).
+  void fp64_dd_range(const double* f, double* dd, int64_t first, int64_t count);
+  void fp64_prep_range(const double* phi0, const double* dd0, int os, double limit_high, double limit_low, int64_t first, int64_t count);
+  void fp64_stage_range(int os, const double* phi0, const double* phin, const double* dd, double* out, const double* avg_with,
+                        int64_t first, int64_t count);
 
   // reinitialize() in FP64 with no allocation: the work vectors come from a static device array
   // (reinit_fp64_static) that holds grids up to LSG_NOALLOC_SCRATCH_BYTES of scratch.
@@ -188,6 +201,16 @@ struct LevelSet {
   // (component, axis, node) or null; phi_dd: D x N or null. Device pointers.
   void sl_advect(const double* xyz, int64_t np, double dt, const double* v, const double* vdd, const double* phi, const double* phi_dd,
                  int velo_method, int phi_method, double* phi_np1);
+  // advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1), the two-velocity
+  // second-order step: this object's grid is time n (vn: D x N, phi_n), nm1 the grid at n-1 (vnm1:
+  // D x N_nm1); xyz the np nodes of the grid at n+1. vn_dd / vnm1_dd: D x D x N of their grids (component,
+  // axis, node) or null; phi_dd: D x N or null. Device pointers, both level sets on the current device.
+  void sl_advect2(LevelSet<D>& nm1, const double* xyz, int64_t np, double dt_nm1, double dt_n, const double* vnm1,
+                  const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd, int velo_method,
+                  int phi_method, double* phi_np1);
+  void sl_advect2_host(LevelSet<D>& nm1, const double* xyz, int64_t np, double dt_nm1, double dt_n, const double* vnm1,
+                       const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd,
+                       int velo_method, int phi_method, double* phi_np1);
   // the CF overload with the single-vortex velocity scaled by vscale
   void sl_advect_vortex(const double* xyz, int64_t np, double dt, double vscale, const double* phi, const double* phi_dd, int phi_method,
                         double* phi_np1);
@@ -196,8 +219,11 @@ struct LevelSet {
   // count: phi on the device in union node order. With use_graph the iteration loop runs as one CUDA
   // graph (captured on the first call with these iteration counts, replayed afterwards).
   void reinitialize_batch(double* phi, const int* iterations, bool use_graph);
-  // Times candidate launch shapes of the mixed stage on phi (device, node order) and keeps the fastest.
+  // Times candidate launch shapes of the mixed stage on phi (device, node order) and keeps the fastest;
+  // a candidate whose bounded waits gave up is discarded.
   void autotune(const double* phi, int trials);
+  // bound of the bulk-copy stage kernel's waits in SM clock cycles (0: the default, about a second)
+  void set_wait_limit(long long cycles) { cfg.wait_cycles = cycles > 0 ? cycles : 0; }
   void drop_graph();  // forget a captured graph (after a launch-shape change)
 
   // host-buffer conveniences (copies inside)
@@ -224,6 +250,8 @@ struct LevelSet {
   // throws DeviceTimeout if a bounded device-side wait gave up since the last check (synchronises the
   // stream; skipped while the stream is being captured)
   void check_device_waits();
+  // reads and clears the flag a bounded device-side wait sets when it gives up (synchronises the stream)
+  bool take_device_wait_flag();
   void build_locator();
   void build_gradient();
   const double* derivatives_of(int nf, const double* F, const double* Fdd, DevBuf<double>& store);

@@ -6,14 +6,14 @@
 // the object's lifetime. This variant carves the same vectors out of g_reinit_scratch and runs the
 // same kernels in the same order, so its results are identical to the allocating path's.
 //
-// Set-up: the first call on a device (with that device current) takes the array's address with
-// cudaGetSymbolAddress, which also loads this file's device code; the address is cached per device
-// ordinal. Make that first call before any stream capture on the device.
+// Set-up: every call looks up the array's address on the level set's device (which the C ABI makes
+// current for the call) with cudaGetSymbolAddress and checks the result. The lookup is cheap once the
+// module is loaded and is never stale, even after the device's primary context was reset and made again.
+// The first call on a device also loads this file's device code: make it before any stream capture.
 // Nothing in the scratch must start at zero: every vector is written before it is read (status for
 // every node; subcell distances only for the nodes whose status says they are read).
 // There is one array per device: calls that overlap on the same device (other streams, other
 // threads, other level-set objects) race on it and must be serialised by the caller.
-#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -27,21 +27,11 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_reinit_scratch[LSG_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
-
+// the array's device address on the current device (host code cannot use the symbol itself)
 unsigned char* scratch_address() {
-  int dev = 0;
-  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) throw std::invalid_argument("static reinitialisation scratch: device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    cuda_check(cudaGetSymbolAddress(&p, g_reinit_scratch), "cudaGetSymbolAddress(static reinitialisation scratch)");
-    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-  }
-  return g_scratch_addr[dev];
+  void* p = nullptr;
+  cuda_check(cudaGetSymbolAddress(&p, g_reinit_scratch), "cudaGetSymbolAddress(static reinitialisation scratch)");
+  return static_cast<unsigned char*>(p);
 }
 
 constexpr size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }

@@ -1,8 +1,8 @@
 """Node interpolation and the semi-Lagrangian step on the GPU (FP64).
 
 Mirrors my_p4est_interpolation_nodes_t (src/my_p4est_interpolation_nodes.h:33-103, set_input /
-add_point / interpolate) and my_p4est_semi_lagrangian_t::advect_from_n_to_np1
-(src/my_p4est_semi_lagrangian.cpp:108-223). Arrays are numpy float64 in node order (host, copied
+add_point / interpolate) and my_p4est_semi_lagrangian_t::advect_from_n_to_np1 / update_p4est, with one
+velocity (src/my_p4est_semi_lagrangian.cpp:108-223, 321-529) and with two (:225-319, 779-939). Arrays are numpy float64 in node order (host, copied
 inside each call) or CUDA tensors (device-resident).
 """
 from __future__ import annotations
@@ -114,11 +114,13 @@ class my_p4est_semi_lagrangian_t:
     """advect_from_n_to_np1 from the grid at time n (ls_n) onto the nodes of the grid at n+1.
 
     splitting: (min_lvl, max_lvl, lip) of the grid's splitting criterion (the reference reads it from
-    p4est->user_pointer), used by update_p4est."""
+    p4est->user_pointer), used by update_p4est. ls_nm1: the grid at n-1 (the reference's ngbd_nm1), needed
+    by the two-velocity forms."""
 
-    def __init__(self, forest_np1, ls_n: my_p4est_level_set_t, splitting=None):
+    def __init__(self, forest_np1, ls_n: my_p4est_level_set_t, splitting=None, ls_nm1: my_p4est_level_set_t = None):
         self.forest_np1 = forest_np1
         self.ls_n = ls_n
+        self.ls_nm1 = ls_nm1
         self.splitting = splitting
         self.dim = ls_n.ngbd.dim
         self.velo_interpolation = quadratic_non_oscillatory_continuous_v2
@@ -134,7 +136,54 @@ class my_p4est_semi_lagrangian_t:
             raise ValueError("unknown interpolation_method")
         self.phi_interpolation = method
 
-    def advect_from_n_to_np1(self, dt, v, phi_n, vxx=None, phi_xx_n=None, xyz_np1=None):
+    def advect_from_n_to_np1(self, *args, **kw):
+        """advect_from_n_to_np1(dt, v, phi_n, vxx=None, phi_xx_n=None, xyz_np1=None), or the two-velocity
+        form advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vn, phi_n, vxx_nm1=None, vxx_n=None, phi_xx_n=None,
+        xyz_np1=None), told apart as the reference's overloads are, by the arguments: a number in second
+        place is dt_n."""
+        if len(args) >= 2 and isinstance(args[1], (int, float, np.floating)):
+            return self._advect2(*args, **kw)
+        return self._advect1(*args, **kw)
+
+    def _advect2(self, dt_nm1, dt_n, vnm1, vn, phi_n, vxx_nm1=None, vxx_n=None, phi_xx_n=None, xyz_np1=None):
+        """The two-velocity second-order step (src/my_p4est_semi_lagrangian.cpp:225-319): vn (dim, N_n) and
+        phi_n on ls_n's grid, vnm1 (dim, N_nm1) on ls_nm1's; vxx_* (dim, dim, N) and phi_xx_n (dim, N_n) may be
+        omitted (computed as the reference's update_p4est does). numpy arrays (copied in and out) or CUDA
+        tensors (device-resident; xyz_np1 then a (npts, dim) CUDA tensor, default forest_np1's nodes on the
+        device). Returns phi at the nodes of forest_np1."""
+        if self.ls_nm1 is None:
+            raise ValueError("the two-velocity step needs the grid at n-1 (ls_nm1)")
+        lib = L.load()
+        d = self.dim
+        Nn, Nm = self.ls_n.num_nodes, self.ls_nm1.num_nodes
+        if _is_device(phi_n):
+            import torch
+            xyz = xyz_np1 if xyz_np1 is not None else self.forest_np1.node_xyz_device()
+            npts = xyz.shape[0]
+            for name, a, n in (("vn", vn, d * Nn), ("vnm1", vnm1, d * Nm), ("phi_n", phi_n, Nn)):
+                if not _is_device(a) or a.dtype != torch.float64 or a.numel() != n or not a.is_contiguous():
+                    raise ValueError(f"{name} must be a contiguous float64 CUDA tensor of {n} values")
+            out = torch.empty(npts, dtype=torch.float64, device=phi_n.device)
+            L.check(lib.lsg_semi_lagrangian_advect2_device(self.ls_n.handle, self.ls_nm1.handle, _ptr(xyz), npts, float(dt_nm1),
+                                                           float(dt_n), _ptr(vnm1), _ptr(vxx_nm1), _ptr(vn), _ptr(vxx_n),
+                                                           _ptr(phi_n), _ptr(phi_xx_n), int(self.velo_interpolation),
+                                                           int(self.phi_interpolation), _ptr(out)))
+            return out
+        xyz = xyz_np1 if xyz_np1 is not None else self.forest_np1.node_xyz()
+        xyz = _f64(xyz, "xyz_np1").reshape(-1, d)
+        vn = _f64(vn, "vn", d * Nn)
+        vnm1 = _f64(vnm1, "vnm1", d * Nm)
+        phi_n = _f64(phi_n, "phi_n", Nn)
+        vxn = None if vxx_n is None else _f64(vxx_n, "vxx_n", d * d * Nn)
+        vxm = None if vxx_nm1 is None else _f64(vxx_nm1, "vxx_nm1", d * d * Nm)
+        pdd = None if phi_xx_n is None else _f64(phi_xx_n, "phi_xx_n", d * Nn)
+        out = np.empty(len(xyz), np.float64)
+        L.check(lib.lsg_semi_lagrangian_advect2(self.ls_n.handle, self.ls_nm1.handle, L.dptr(xyz), len(xyz), float(dt_nm1), float(dt_n),
+                                                L.dptr(vnm1), _ptr(vxm), L.dptr(vn), _ptr(vxn), L.dptr(phi_n), _ptr(pdd),
+                                                int(self.velo_interpolation), int(self.phi_interpolation), L.dptr(out)))
+        return out
+
+    def _advect1(self, dt, v, phi_n, vxx=None, phi_xx_n=None, xyz_np1=None):
         """v: (dim, N_n) node velocities, a VortexVelocity, or a callable velocity(xyz) -> (dim, npts)
         evaluated on the host at points xyz (npts, dim) (the CF overload). Returns phi at the nodes of
         forest_np1 (host arrays)."""
@@ -179,7 +228,70 @@ class my_p4est_semi_lagrangian_t:
                                                L.dptr(out)))
         return out
 
-    def update_p4est(self, v, dt, phi, phi_xx=None, vxx=None):
+    def update_p4est(self, *args, **kw):
+        """update_p4est(v, dt, phi, phi_xx=None, vxx=None), or the two-velocity form update_p4est(vnm1, vn,
+        dt_nm1, dt_n, phi, phi_xx=None, phi_add_refine=None) (a number in third place is dt_nm1)."""
+        if len(args) >= 3 and isinstance(args[2], (int, float, np.floating)):
+            return self._update_p4est2(*args, **kw)
+        return self._update_p4est1(*args, **kw)
+
+    def _update_p4est2(self, vnm1, vn, dt_nm1, dt_n, phi, phi_xx=None, phi_add_refine=None):
+        """update_p4est(vnm1, vn, dt_nm1, dt_n, phi, phi_xx, phi_add_refine) (src/my_p4est_semi_lagrangian.cpp:779-939):
+        the second derivatives of both velocities (and of phi unless given) once, then the two-velocity step
+        onto forest_np1 and splitting_criteria_tag_t::refine_and_coarsen from the advected values (or from
+        min(|phi_np1|, |phi_add_refine|), phi_add_refine on grid n interpolated linearly), until the grid
+        stops changing. numpy arrays or CUDA tensors. Returns phi at the nodes of the final forest_np1
+        (modified in place)."""
+        if self.splitting is None:
+            raise ValueError("update_p4est needs the splitting criterion (min_lvl, max_lvl, lip)")
+        if self.ls_nm1 is None:
+            raise ValueError("the two-velocity update_p4est needs the grid at n-1 (ls_nm1)")
+        min_lvl, max_lvl, lip = self.splitting
+        d = self.dim
+        dev = _is_device(phi)
+        if dev:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+            self.ls_n.set_stream(stream)
+            self.ls_nm1.set_stream(stream)
+            stack = lambda xs: torch.stack(xs)
+            vn = vn.contiguous()
+            vnm1 = vnm1.contiguous()
+            row = lambda a, k: a[k].contiguous()
+        else:
+            stack = np.stack
+            vn = _f64(vn, "vn", d * self.ls_n.num_nodes).reshape(d, -1)
+            vnm1 = _f64(vnm1, "vnm1", d * self.ls_nm1.num_nodes).reshape(d, -1)
+            phi = _f64(phi, "phi", self.ls_n.num_nodes)
+            row = lambda a, k: np.ascontiguousarray(a[k])
+        vxx_n = stack([self.ls_n.compute_derivatives(row(vn, k)) for k in range(d)])
+        vxx_nm1 = stack([self.ls_nm1.compute_derivatives(row(vnm1, k)) for k in range(d)])
+        if phi_xx is None:
+            phi_xx = self.ls_n.compute_derivatives(phi)
+        f = self.forest_np1
+        self.iterations = 0
+        while True:
+            xyz = f.node_xyz_device() if dev else f.node_xyz()
+            phi_np1 = self._advect2(dt_nm1, dt_n, vnm1, vn, phi, vxx_nm1=vxx_nm1, vxx_n=vxx_n, phi_xx_n=phi_xx, xyz_np1=xyz)
+            self.iterations += 1
+            eff = phi_np1
+            if phi_add_refine is not None:
+                add = my_p4est_interpolation_nodes_t(self.ls_n)
+                if dev:
+                    extra = torch.empty_like(phi_np1)
+                    add.interpolate_device(xyz, phi_add_refine, 1, linear, extra)
+                    eff = torch.minimum(extra.abs(), phi_np1.abs())
+                else:
+                    extra = add.interpolate_points(xyz, phi_add_refine, linear)
+                    eff = np.minimum(np.abs(extra), np.abs(phi_np1))
+            if not f.refine_and_coarsen(min_lvl, max_lvl, eff, lip=lip):
+                return phi_np1
+            if dev:
+                f.build_nodes(device=True)
+            else:
+                f.build_nodes()
+
+    def _update_p4est1(self, v, dt, phi, phi_xx=None, vxx=None):
         """update_p4est(v, dt, phi[, phi_xx]) (src/my_p4est_semi_lagrangian.cpp:321-392 for an analytic
         velocity, :394-529 for node velocities): advect phi onto forest_np1, regrid it with
         splitting_criteria_tag_t::refine_and_coarsen from the advected values, and repeat until the grid

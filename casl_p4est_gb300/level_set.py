@@ -325,6 +325,18 @@ class my_p4est_level_set_t:
                                               C.byref(out), C.byref(cnt)))
         return out.value, cnt.value
 
+    def interface_location_error(self, a, b):
+        """FP64 max distance between the zero crossings of a and b along the grid edges b cuts (CUDA tensors);
+        returns (value, cut edges, edges a does not cut)."""
+        if not (_is_device(a) and _is_device(b)):
+            raise TypeError("interface_location_error takes CUDA tensors")
+        out = C.c_double()
+        edges = C.c_int64()
+        mis = C.c_int64()
+        L.check(L.load().lsg_interface_location_error_device(self._h, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                                             C.byref(out), C.byref(edges), C.byref(mis)))
+        return out.value, edges.value, mis.value
+
     def table_stats(self):
         """Sizes of the mixed tables: nodes, regular, uniform, irregular, extended set, classes, corrections."""
         out = np.zeros(7, np.int64)
@@ -344,6 +356,11 @@ class my_p4est_level_set_t:
     @stage_config.setter
     def stage_config(self, cfg):
         _set_stage_config(self._h, cfg)
+
+    def set_wait_limit(self, cycles=0):
+        """Bound of the bulk-copy stage kernel's waits in SM clock cycles (0: the default, about a second).
+        A wait that runs out makes the call raise LsgTimeout; the next call starts clean."""
+        L.check(L.load().lsg_level_set_set_wait_limit(self._h, int(cycles)))
 
     def perturb_level_set_function(self, phi, epsilon):
         _host_f64(phi, self.num_nodes, "phi")

@@ -180,9 +180,11 @@ int lsg_reinitialize_with_mask_device(lsg_level_set* ls, double* phi_dev, const 
  * is handed out by another pool (cudaMalloc there fails or fragments it), a time loop that cannot
  * take the device-wide synchronisation of cudaFree, and programs with many level-set objects on
  * small grids, which would otherwise each keep their own work vectors.
- * The first call on a device (with that device current) takes the array's address with
- * cudaGetSymbolAddress; make it before any stream capture. Nothing in the array must start at
- * zero. Calls that overlap on one device race on the array: serialise them. */
+ * Every call runs on the level set's device and looks the array's address up there with
+ * cudaGetSymbolAddress; the first call on a device also loads the array's module, so make it before any
+ * stream capture. Nothing in the array must start at zero. All calls on one device share the array:
+ * calls that overlap there (other streams, threads or level-set objects) race on it, so the caller must
+ * serialise them. */
 #define LSG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int lsg_reinitialize_device_noalloc(lsg_level_set* ls, double* phi_dev, int order_space, int order_pseudotime,
                                     double limit_high, double limit_low, int iterations);
@@ -310,6 +312,21 @@ int lsg_semi_lagrangian_advect_device(lsg_level_set* ls, const double* xyz_np1_d
                                       const double* vdd_dev, const double* phi_n_dev, const double* phi_dd_dev, int velo_method,
                                       int phi_method, double* phi_np1_dev);
 
+/* the two-velocity second-order step my_p4est_semi_lagrangian_t::advect_from_n_to_np1(dt_nm1, dt_n, vnm1,
+ * vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1) (src/my_p4est_semi_lagrangian.cpp:225-319), the step
+ * update_p4est(Vec* vnm1, Vec* vn, dt_nm1, dt_n, phi, ...) (:779-939) repeats while it regrids: ls_n is the
+ * grid at time n (vn: dim x N_n, phi_n, phi_dd: dim x N_n or NULL, vn_dd: dim x dim x N_n or NULL), ls_nm1
+ * the grid at n-1 (vnm1: dim x N_nm1, vnm1_dd: dim x dim x N_nm1 or NULL), xyz_np1 the npts nodes of the grid
+ * at n+1. v_n is interpolated at the new nodes quadratically (as the reference does), x* = x - dt_n/2 v_n
+ * (clipped), v* = (1 + dt_n/(2 dt_nm1)) v_n(x*) - dt_n/(2 dt_nm1) v_nm1(x*), both with velo_method, and
+ * phi_np1 = phi_n(x - dt_n v*) (clipped) with phi_method. Both level sets must be on one device. */
+int lsg_semi_lagrangian_advect2(lsg_level_set* ls_n, lsg_level_set* ls_nm1, const double* xyz_np1, int64_t npts, double dt_nm1,
+                                double dt_n, const double* vnm1, const double* vnm1_dd, const double* vn, const double* vn_dd,
+                                const double* phi_n, const double* phi_dd, int velo_method, int phi_method, double* phi_np1);
+int lsg_semi_lagrangian_advect2_device(lsg_level_set* ls_n, lsg_level_set* ls_nm1, const double* xyz_np1, int64_t npts, double dt_nm1,
+                                       double dt_n, const double* vnm1, const double* vnm1_dd, const double* vn, const double* vn_dd,
+                                       const double* phi_n, const double* phi_dd, int velo_method, int phi_method, double* phi_np1);
+
 /* the CF overload advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1)
  * (src/my_p4est_semi_lagrangian.cpp:108-146) with an analytic velocity evaluated on the device:
  * velocity LSG_VELOCITY_VORTEX is the single vortex of examples/level_set_advection/main_2d.cpp:116-181
@@ -336,6 +353,31 @@ int lsg_semi_lagrangian_advect_callback(lsg_level_set* ls, const double* xyz_np1
  * pointers of N values; no counterpart in the reference, whose examples compute the same norm on the
  * host (examples/reinitialization/main_2d.cpp:254-262). */
 int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double band, double* out, int64_t* count);
+/* The per-rank FP64 sweeps of a Morton-range split of one grid: on one rank of an MPI run the reference
+ * sweeps its layer and local node lists (reinitialize_one_iteration(phi_np1, list_of_node_idx, ...),
+ * src/my_p4est_level_set.cpp:59-288; second_derivatives_central over the same lists,
+ * src/my_p4est_node_neighbors.cpp:1552-1627) between ghost updates (:376-401, :450-464). Each call covers the
+ * nodes [first, first + count) only and reads every other node from the full-length device arrays (node
+ * order), whose ghost values the caller keeps current with its own halo exchange.
+ * lsg_second_derivatives_range_device: f_dd (dim x N) at the range.
+ * lsg_reinit_prep_range_device: what the stages derive from phi_0 alone (status, subcell distances, kept in
+ * the level set) with the phi_0 limits of reinitialize_within_range_of_phi_0; phi0_dd as from
+ * lsg_second_derivatives_range_device (NULL for first order in space).
+ * lsg_reinit_stage_range_device: out = one stage of phin (phin_dd its second derivatives, NULL for first
+ * order), or 0.5 (avg_with + stage) when avg_with is given (the RK average; may alias out). */
+int lsg_second_derivatives_range_device(lsg_level_set* ls, const double* f_dev, double* f_dd_dev, int64_t first, int64_t count);
+int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, const double* phi0_dd_dev, int order_space, double limit_high,
+                                 double limit_low, int64_t first, int64_t count);
+int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const double* phi0_dev, const double* phin_dev,
+                                  const double* phin_dd_dev, double* out_dev, const double* avg_with_dev, int64_t first, int64_t count);
+
+/* The interface-location check that accompanies every mixed-precision result: over the grid edges (a node
+ * and a neighbour that its stencil reaches with one node) cut by the reference field b (e.g. the FP64
+ * result), the largest distance between the zero crossings of a and b along the edge, each the linear root
+ * d b_n / (b_n - b_nb) in FP64 on the device; *edges (may be NULL) counts the cut edges (both ends),
+ * *mismatched (may be NULL) those a does not cut. No counterpart in the reference. */
+int lsg_interface_location_error_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double* out, int64_t* edges,
+                                        int64_t* mismatched);
 
 /* ---- batched reinitialisation (mixed precision) --------------------------------------------- */
 
@@ -368,6 +410,11 @@ int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const i
 int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int* config);
 int lsg_level_set_stage_config(const lsg_level_set* ls, int* config);
 int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config);
+/* Bound of the bulk-copy stage kernel's waits for its own copies, in SM clock cycles (0 restores the
+ * default, about a second). A wait that runs out stops that kernel's blocks after their copies have landed
+ * and makes the call return LSG_ETIMEOUT; the next call starts clean. No counterpart in the reference
+ * (which has no device waits); a diagnostic for callers that must bound every device-side wait. */
+int lsg_level_set_set_wait_limit(lsg_level_set* ls, long long cycles);
 
 /* Sizes of the mixed tables (7 values): nodes, regular nodes, uniform-stencil nodes, irregular nodes,
  * regular nodes of the extended second-derivative set, geometry classes, cross-term corrections. */

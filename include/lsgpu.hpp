@@ -17,7 +17,8 @@
  *                                             cf, grad_phi, blocksize), set_interpolation_on_interface
  *                                                                      src/my_p4est_level_set.h:775-776, 843
  *   my_p4est_interpolation_nodes_t: set_input, add_point, interpolate  src/my_p4est_interpolation_nodes.h:33-103
- *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1, update_p4est     src/my_p4est_semi_lagrangian.h:83-196
+ *   my_p4est_semi_lagrangian_t::advect_from_n_to_np1, update_p4est (one and two velocities)
+ *                                                                      src/my_p4est_semi_lagrangian.h:83-196
  *
  * Vec: with LSGPU_WITH_PETSC defined before inclusion, PETSc's Vec (read through VecGetArray);
  * otherwise a minimal host vector with the same accessor names (VecGetArray / VecRestoreArray /
@@ -34,7 +35,10 @@
 
 #include <float.h>
 #include <limits.h>
+#include <math.h>
 
+#include <algorithm>
+#include <cmath>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -446,6 +450,9 @@ class my_p4est_semi_lagrangian_t {
   // with the splitting criterion of grid n+1 (the reference reads it from p4est->user_pointer)
   my_p4est_semi_lagrangian_t(lsg_forest* forest_np1, my_p4est_node_neighbors_t* ngbd_n, int min_lvl, int max_lvl, double lip)
       : forest_np1_(forest_np1), ngbd_n_(ngbd_n), min_lvl_(min_lvl), max_lvl_(max_lvl), lip_(lip) {}
+  // with the grid at n-1 as well (the reference's ngbd_nm1), for the two-velocity forms
+  my_p4est_semi_lagrangian_t(lsg_forest* forest_np1, my_p4est_node_neighbors_t* ngbd_n, my_p4est_node_neighbors_t* ngbd_nm1)
+      : forest_np1_(forest_np1), ngbd_n_(ngbd_n), ngbd_nm1_(ngbd_nm1) {}
   void set_splitting(int min_lvl, int max_lvl, double lip) {
     min_lvl_ = min_lvl;
     max_lvl_ = max_lvl;
@@ -456,7 +463,7 @@ class my_p4est_semi_lagrangian_t {
   // until it no longer changes; phi is then replaced by its values at the final nodes. Returns the number
   // of advection passes.
   // phi_xx: phi's second derivatives on grid n (computed when null); band: the splitting criterion's band.
-  // phi_add_refine (an extra refinement field) is not supported.
+  // phi_add_refine: an extra field of grid n whose |value| also drives the refinement.
   int update_p4est(Vec* v, double dt, Vec& phi, Vec* phi_xx = nullptr, Vec phi_add_refine = nullptr, const double& band = 0) {
     const int D = ngbd_n_->dim();
     const size_t N = (size_t)ngbd_n_->num_nodes();
@@ -471,6 +478,26 @@ class my_p4est_semi_lagrangian_t {
                                                               const std::vector<double>& pdd, std::vector<double>& out) {
       lsgpu::check(lsg_semi_lagrangian_advect(ngbd_n_->device(), xyz.data(), (int64_t)out.size(), dt, vv.data(), vdd.data(), pn.data(),
                                               pdd.data(), (int)velo_, (int)phi_, out.data()));
+    });
+  }
+  // update_p4est(vnm1, vn, dt_nm1, dt_n, phi, phi_xx, phi_add_refine) (src/my_p4est_semi_lagrangian.cpp:779-939):
+  // the two-velocity second-order step (vn[D] on grid n, vnm1[D] on grid n-1) repeated while forest_np1 is
+  // refined and coarsened from the advected values (or from min(|phi_np1|, |phi_add_refine|) with
+  // phi_add_refine on grid n interpolated linearly); phi then holds the values at the final nodes.
+  int update_p4est(Vec* vnm1, Vec* vn, double dt_nm1, double dt_n, Vec& phi, Vec* phi_xx = nullptr, Vec phi_add_refine = nullptr) {
+    if (!ngbd_nm1_) throw std::invalid_argument("update_p4est: the two-velocity form needs the grid at n-1 (ngbd_nm1)");
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes(), Nm = (size_t)ngbd_nm1_->num_nodes();
+    std::vector<double> vn_v = gather(vn, D, N), vm_v = gather(vnm1, D, Nm), vn_dd((size_t)D * D * N), vm_dd((size_t)D * D * Nm);
+    for (int a = 0; a < D; ++a) {
+      lsgpu::check(lsg_second_derivatives(ngbd_n_->device(), &vn_v[a * N], &vn_dd[(size_t)a * D * N]));
+      lsgpu::check(lsg_second_derivatives(ngbd_nm1_->device(), &vm_v[a * Nm], &vm_dd[(size_t)a * D * Nm]));
+    }
+    return regrid(dt_n, phi, phi_xx, phi_add_refine, 0.0, [&](const std::vector<double>& xyz, const std::vector<double>& pn,
+                                                              const std::vector<double>& pdd, std::vector<double>& out) {
+      lsgpu::check(lsg_semi_lagrangian_advect2(ngbd_n_->device(), ngbd_nm1_->device(), xyz.data(), (int64_t)out.size(), dt_nm1, dt_n,
+                                               vm_v.data(), vm_dd.data(), vn_v.data(), vn_dd.data(), pn.data(), pdd.data(), (int)velo_,
+                                               (int)phi_, out.data()));
     });
   }
   // update_p4est(const CF** v, dt, phi, phi_xx) (src/my_p4est_semi_lagrangian.cpp:321-392): v[D] function
@@ -531,6 +558,26 @@ class my_p4est_semi_lagrangian_t {
     lsgpu::check(lsg_semi_lagrangian_advect(ngbd_n_->device(), xyz.data(), np, dt, vv.data(), vdd.empty() ? nullptr : vdd.data(), p.p,
                                             pdd.empty() ? nullptr : pdd.data(), (int)velo_, (int)phi_, phi_np1));
   }
+  // advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1)
+  // (src/my_p4est_semi_lagrangian.cpp:225-319): vnm1[D] on grid n-1, vn[D] and phi_n on grid n; vxx_nm1,
+  // vxx_n ([D][D]) and phi_xx_n ([D]) may be null (computed); phi_np1 has one value per node of grid n+1.
+  void advect_from_n_to_np1(double dt_nm1, double dt_n, Vec* vnm1, Vec** vxx_nm1, Vec* vn, Vec** vxx_n, Vec phi_n, Vec* phi_xx_n,
+                            double* phi_np1) const {
+    if (!ngbd_nm1_) throw std::invalid_argument("advect_from_n_to_np1: the two-velocity form needs the grid at n-1 (ngbd_nm1)");
+    const int D = ngbd_n_->dim();
+    const size_t N = (size_t)ngbd_n_->num_nodes(), Nm = (size_t)ngbd_nm1_->num_nodes();
+    std::vector<double> vn_v = gather(vn, D, N), vm_v = gather(vnm1, D, Nm), vn_dd, vm_dd, pdd;
+    if (vxx_n) vn_dd = gather2(vxx_n, D, N);
+    if (vxx_nm1) vm_dd = gather2(vxx_nm1, D, Nm);
+    if (phi_xx_n) pdd = gather(phi_xx_n, D, N);
+    const int64_t np = lsg_forest_num_nodes(forest_np1_);
+    std::vector<double> xyz((size_t)np * D);
+    lsgpu::check(lsg_forest_node_xyz(forest_np1_, xyz.data()));
+    lsgpu::VecArray p(phi_n);
+    lsgpu::check(lsg_semi_lagrangian_advect2(ngbd_n_->device(), ngbd_nm1_->device(), xyz.data(), np, dt_nm1, dt_n, vm_v.data(),
+                                             vm_dd.empty() ? nullptr : vm_dd.data(), vn_v.data(), vn_dd.empty() ? nullptr : vn_dd.data(), p.p,
+                                             pdd.empty() ? nullptr : pdd.data(), (int)velo_, (int)phi_, phi_np1));
+  }
   // advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1): v[D] function objects of the
   // coordinates, evaluated on the host at the nodes of grid n+1 and at the midpoints.
   template <typename CF>
@@ -568,13 +615,32 @@ class my_p4est_semi_lagrangian_t {
   }
 
  private:
-  // advect phi onto forest_np1 with `advect`, refine/coarsen from the result, repeat until the grid
-  // settles; phi becomes the values at the final nodes
+  // D vectors of n values each, packed component after component
+  static std::vector<double> gather(Vec* v, int D, size_t n) {
+    std::vector<double> out((size_t)D * n);
+    for (int a = 0; a < D; ++a) {
+      lsgpu::VecArray x(v[a]);
+      for (size_t i = 0; i < n; ++i) out[a * n + i] = x.p[i];
+    }
+    return out;
+  }
+  // D x D vectors (component, derivative axis) of n values each
+  static std::vector<double> gather2(Vec** v, int D, size_t n) {
+    std::vector<double> out((size_t)D * D * n);
+    for (int c = 0; c < D; ++c)
+      for (int a = 0; a < D; ++a) {
+        lsgpu::VecArray x(v[c][a]);
+        for (size_t i = 0; i < n; ++i) out[((size_t)c * D + a) * n + i] = x.p[i];
+      }
+    return out;
+  }
+  // advect phi onto forest_np1 with `advect`, refine/coarsen from the result (or from
+  // min(|result|, |phi_add_refine|), phi_add_refine on grid n interpolated linearly at the new nodes),
+  // repeat until the grid settles; phi becomes the values at the final nodes
   template <typename Advect>
   int regrid(double dt, Vec& phi, Vec* phi_xx, Vec phi_add_refine, double band, Advect advect) {
     (void)dt;
     if (max_lvl_ < 0) throw std::invalid_argument("update_p4est: set the splitting criterion first");
-    if (phi_add_refine != nullptr) throw std::invalid_argument("update_p4est: phi_add_refine is not supported");
     const int D = ngbd_n_->dim();
     const size_t N = (size_t)ngbd_n_->num_nodes();
     std::vector<double> pn(N), pdd((size_t)D * N);
@@ -601,7 +667,16 @@ class my_p4est_semi_lagrangian_t {
       advect(xyz, pn, pdd, out);
       ++passes;
       int changed = 0;
-      lsgpu::check(lsg_forest_refine_and_coarsen(forest_np1_, min_lvl_, max_lvl_, lip_, band, out.data(), &changed));
+      const double* tag_from = out.data();
+      std::vector<double> eff;
+      if (phi_add_refine != nullptr) {
+        eff.resize((size_t)np);
+        lsgpu::VecArray add(phi_add_refine);
+        lsgpu::check(lsg_interpolate_nodes(ngbd_n_->device(), xyz.data(), np, add.p, 1, nullptr, (int)linear, eff.data()));
+        for (int64_t n = 0; n < np; ++n) eff[(size_t)n] = std::min(std::fabs(eff[(size_t)n]), std::fabs(out[(size_t)n]));
+        tag_from = eff.data();
+      }
+      lsgpu::check(lsg_forest_refine_and_coarsen(forest_np1_, min_lvl_, max_lvl_, lip_, band, tag_from, &changed));
       if (!changed) break;
       lsgpu::check(lsg_forest_build_nodes(forest_np1_));
     }
@@ -618,6 +693,7 @@ class my_p4est_semi_lagrangian_t {
 
   lsg_forest* forest_np1_;
   my_p4est_node_neighbors_t* ngbd_n_;
+  my_p4est_node_neighbors_t* ngbd_nm1_ = nullptr;
   int min_lvl_ = 0, max_lvl_ = -1;
   double lip_ = 1.2;
   interpolation_method velo_ = quadratic_non_oscillatory_continuous_v2;

@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <map>
+#include <parallel/algorithm>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -201,13 +202,17 @@ int32_t descend(const Grid<D>& g, int tree, const double* s) {
 }
 
 // ---- nodes -----------------------------------------------------------------------------------
+// Every leaf corner is a node owned by the lowest tree containing it, stored clamped inside that tree
+// (ROOT_LEN -> ROOT_LEN - 1); nodes are numbered in (owner tree, Morton index) order. The corner keys are
+// made in parallel, sorted and made unique, and each corner finds its node by binary search.
 template <int D>
 void build_nodes(Grid<D>& g) {
   typedef std::pair<int32_t, uint64_t> Key;
-  std::map<Key, int32_t> idx;
-  std::vector<Key> corner_keys(g.leaves.size() * Grid<D>::CH);
-  std::vector<std::pair<int32_t, std::vector<int64_t>>> node_data;
-  for (size_t q = 0; q < g.leaves.size(); ++q) {
+  const size_t nc = g.leaves.size() * Grid<D>::CH;
+  std::vector<Key> corner_keys(nc);
+#pragma omp parallel for schedule(static)
+  for (long long qq = 0; qq < (long long)g.leaves.size(); ++qq) {
+    const size_t q = (size_t)qq;
     const Leaf& L = g.leaves[q];
     const int64_t h = Grid<D>::ROOT_LEN >> L.level;
     for (int c = 0; c < Grid<D>::CH; ++c) {
@@ -237,33 +242,38 @@ void build_nodes(Grid<D>& g) {
               oijk[2] = k;
             }
           }
-      std::vector<int64_t> xl(D);
+      int64_t xl[3] = {0, 0, 0};
       for (int a = 0; a < D; ++a) {
         int64_t v = G[a] - (int64_t)oijk[a] * Grid<D>::ROOT_LEN;
         if (v == Grid<D>::ROOT_LEN) v = Grid<D>::ROOT_LEN - 1;
         xl[a] = v;
       }
-      const Key key(owner, interleave(xl.data(), D));
-      corner_keys[q * Grid<D>::CH + c] = key;
-      if (!idx.count(key)) {
-        idx[key] = 0;
-        node_data.push_back({owner, xl});
-      }
+      corner_keys[q * Grid<D>::CH + c] = Key(owner, interleave(xl, D));
     }
   }
   // (tree, Morton) order
-  int32_t k = 0;
-  for (auto& kv : idx) kv.second = k++;
-  g.node_tree.assign(idx.size(), 0);
-  g.node_x.assign(idx.size() * D, 0);
-  for (auto& nd : node_data) {
-    const Key key(nd.first, interleave(nd.second.data(), D));
-    const int32_t i = idx[key];
-    g.node_tree[i] = nd.first;
-    for (int a = 0; a < D; ++a) g.node_x[(size_t)i * D + a] = nd.second[a];
+  std::vector<Key> nodes(corner_keys);
+  __gnu_parallel::sort(nodes.begin(), nodes.end());
+  nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
+  const size_t N = nodes.size();
+  g.node_tree.assign(N, 0);
+  g.node_x.assign(N * D, 0);
+  const int bits = (D == 2 ? 30 : 19);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)N; ++ii) {
+    const size_t i = (size_t)ii;
+    g.node_tree[i] = nodes[i].first;
+    const uint64_t key = nodes[i].second;
+    for (int a = 0; a < D; ++a) {
+      int64_t v = 0;
+      for (int b = 0; b < bits; ++b) v |= (int64_t)((key >> (D * b + a)) & 1) << b;
+      g.node_x[i * D + a] = v;
+    }
   }
-  g.local_nodes.assign(g.leaves.size() * Grid<D>::CH, 0);
-  for (size_t i = 0; i < corner_keys.size(); ++i) g.local_nodes[i] = idx[corner_keys[i]];
+  g.local_nodes.assign(nc, 0);
+#pragma omp parallel for schedule(static)
+  for (long long ii = 0; ii < (long long)nc; ++ii)
+    g.local_nodes[(size_t)ii] = (int32_t)(std::lower_bound(nodes.begin(), nodes.end(), corner_keys[(size_t)ii]) - nodes.begin());
 }
 
 // ---- construct_neighbors ----------------------------------------------------------------------
@@ -594,7 +604,8 @@ struct Ctx {
 // reinitialize_one_iteration (src/my_p4est_level_set.cpp:59-288)
 template <int D>
 void reinitialize_one_iteration(const Ctx& cx, double* phi_np1, const double* phi_0, const double* phi_n, double limit_high_,
-                                double limit_low_, const double* phi_0_dd, const double* phi_n_dd, int nthreads) {
+                                double limit_low_, const double* phi_0_dd, const double* phi_n_dd, int nthreads, int64_t first = 0,
+                                int64_t count = -1) {
   const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
   const bool second_order = phi_0_dd != nullptr && phi_n_dd != nullptr;
   const double zdt = cx.zero_distance_threshold;
@@ -604,8 +615,9 @@ void reinitialize_one_iteration(const Ctx& cx, double* phi_np1, const double* ph
   const double low = (limit_low_ < -big ? -DBL_MAX : limit_low_ - MAX(zdt, ORA_EPS * fabs(limit_low_)));
   const double high = (limit_high_ > big ? DBL_MAX : limit_high_ + MAX(zdt, ORA_EPS * fabs(limit_high_)));
   const int64_t N = cx.N;
+  const int64_t end = count < 0 ? N : first + count;
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
-  for (long long k = 0; k < (long long)N; ++k) {
+  for (long long k = first; k < (long long)end; ++k) {
     const int64_t n = k;
     if (fabs(phi_0[n]) < zdt) {
       phi_np1[n] = 0.0;
@@ -699,11 +711,12 @@ void reinitialize_one_iteration(const Ctx& cx, double* phi_np1, const double* ph
 }
 
 template <int D>
-void compute_derivatives(const Ctx& cx, const double* f, double* fdd, int nthreads) {
+void compute_derivatives(const Ctx& cx, const double* f, double* fdd, int nthreads, int64_t first = 0, int64_t count = -1) {
   const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
   const int64_t N = cx.N;
+  const int64_t end = count < 0 ? N : first + count;
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
-  for (long long n = 0; n < (long long)N; ++n) {
+  for (long long n = first; n < (long long)end; ++n) {
     double f0, fnb[6], dd[3] = {0, 0, 0};
     laplace(Q[n], f, &f0, fnb, dd);
     for (int a = 0; a < D; ++a) fdd[(size_t)a * N + n] = dd[a];
@@ -1425,6 +1438,42 @@ void sl_advect(const Ctx& cx, int64_t np, const double* xyz, double dt, const do
   interpolate_points<D>(cx, phi_method, 1, phi, phi_dd, np, pts.data(), phi_np1, nthreads);
 }
 
+// advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1)
+// (src/my_p4est_semi_lagrangian.cpp:225-319): v_n at the new nodes (quadratic), v_n and v_nm1 at
+// x* = x - dt_n/2 v_n (clipped) with velo_method on grids n and n-1, phi_n at x_d = x - dt_n v* (clipped),
+// v* = (1 + .5 dt_n/dt_nm1) v_n(x*) - .5 dt_n/dt_nm1 v_nm1(x*).
+template <int D>
+void sl_advect2(const Ctx& cn, const Ctx& cm, int64_t np, const double* xyz, double dt_nm1, double dt_n, const double* vnm1,
+                const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd, int velo_method,
+                int phi_method, double* phi_np1, int nthreads) {
+  const Grid<D>& g = *static_cast<const Grid<D>*>(cn.grid);
+  std::vector<double> vs, ms, ps;
+  vn_dd = derivatives_of<D>(cn, D, vn, vn_dd, vs, nthreads);
+  vnm1_dd = (velo_method == ORA_LINEAR ? nullptr : derivatives_of<D>(cm, D, vnm1, vnm1_dd, ms, nthreads));
+  phi_dd = (phi_method == ORA_LINEAR ? nullptr : derivatives_of<D>(cn, 1, phi, phi_dd, ps, nthreads));
+  std::vector<double> vt_n((size_t)D * np), vt_nm1((size_t)D * np), pts((size_t)D * np);
+  interpolate_points<D>(cn, ORA_QUADRATIC, D, vn, vn_dd, np, xyz, vt_n.data(), nthreads);
+  for (int64_t n = 0; n < np; ++n) {
+    double x[3];
+    for (int a = 0; a < D; ++a) x[a] = xyz[n * D + a];
+    for (int a = 0; a < D; ++a) x[a] -= .5 * dt_n * vt_n[(size_t)a * np + n];
+    clip_in_domain(g, x);
+    for (int a = 0; a < D; ++a) pts[n * D + a] = x[a];
+  }
+  interpolate_points<D>(cm, velo_method, D, vnm1, vnm1_dd, np, pts.data(), vt_nm1.data(), nthreads);
+  interpolate_points<D>(cn, velo_method, D, vn, velo_method == ORA_LINEAR ? nullptr : vn_dd, np, pts.data(), vt_n.data(), nthreads);
+  for (int64_t n = 0; n < np; ++n) {
+    double v_star[3], x[3];
+    for (int a = 0; a < D; ++a)
+      v_star[a] = (1.0 + .5 * dt_n / dt_nm1) * vt_n[(size_t)a * np + n] - 0.5 * dt_n / dt_nm1 * vt_nm1[(size_t)a * np + n];
+    for (int a = 0; a < D; ++a) x[a] = xyz[n * D + a];
+    for (int a = 0; a < D; ++a) x[a] -= dt_n * v_star[a];
+    clip_in_domain(g, x);
+    for (int a = 0; a < D; ++a) pts[n * D + a] = x[a];
+  }
+  interpolate_points<D>(cn, phi_method, 1, phi, phi_dd, np, pts.data(), phi_np1, nthreads);
+}
+
 // advect_from_n_to_np1(dt, const CF** v, phi_n, phi_xx_n, phi_np1) (src/my_p4est_semi_lagrangian.cpp:108-146)
 // with the single-vortex velocity scaled by vscale.
 template <int D>
@@ -1645,7 +1694,8 @@ Ctx* build_from_leaves(const int* n_xyz, const double* lo, const double* hi, int
   g->qnnn.resize(N);
   g->wall.resize(N);
   int bad = 0;
-  for (int64_t i = 0; i < N; ++i) {
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : bad)
+  for (long long i = 0; i < (long long)N; ++i) {  // independent per node
     if (construct_neighbors(*g, (int32_t)i, g->qnnn[i])) ++bad;
     g->wall[i] = wall_of(*g, (int32_t)i);
   }
@@ -1852,6 +1902,45 @@ int ora_sl_advect(void* h, int64_t npts, const double* xyz, double dt, const dou
     if (!cx->grid) throw std::runtime_error("semi-Lagrangian step needs a grid built from leaves");
     if (cx->dim == 2) sl_advect<2>(*cx, npts, xyz, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
     else sl_advect<3>(*cx, npts, xyz, dt, v, vdd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
+  });
+}
+
+// One sweep over the nodes [first, first + count) only (the per-rank work of a Morton-range split):
+// compute_derivatives, and one reinitialize_one_iteration stage (phi_0_dd / phi_n_dd null: first order in
+// space). The limits are the caller's phi_0 range, widened as reinitialize_within_range_of_phi_0 does.
+int ora_compute_derivatives_range(void* h, const double* f, double* out, int64_t first, int64_t count, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (first < 0 || count < 0 || first + count > cx->N) throw std::runtime_error("node range out of bounds");
+    if (cx->dim == 2) compute_derivatives<2>(*cx, f, out, nthreads, first, count);
+    else compute_derivatives<3>(*cx, f, out, nthreads, first, count);
+  });
+}
+
+int ora_reinit_stage_range(void* h, double* phi_np1, const double* phi_0, const double* phi_n, double limit_high, double limit_low,
+                           const double* phi_0_dd, const double* phi_n_dd, int64_t first, int64_t count, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (first < 0 || count < 0 || first + count > cx->N) throw std::runtime_error("node range out of bounds");
+    if (cx->dim == 2)
+      reinitialize_one_iteration<2>(*cx, phi_np1, phi_0, phi_n, limit_high, limit_low, phi_0_dd, phi_n_dd, nthreads, first, count);
+    else
+      reinitialize_one_iteration<3>(*cx, phi_np1, phi_0, phi_n, limit_high, limit_low, phi_0_dd, phi_n_dd, nthreads, first, count);
+  });
+}
+
+int ora_sl_advect2(void* h_n, void* h_nm1, int64_t npts, const double* xyz, double dt_nm1, double dt_n, const double* vnm1,
+                   const double* vnm1_dd, const double* vn, const double* vn_dd, const double* phi, const double* phi_dd, int velo_method,
+                   int phi_method, double* phi_np1, int nthreads) {
+  return guard([&] {
+    Ctx* cn = static_cast<Ctx*>(h_n);
+    Ctx* cm = static_cast<Ctx*>(h_nm1);
+    if (!cn->grid || !cm->grid) throw std::runtime_error("semi-Lagrangian step needs grids built from leaves");
+    if (cn->dim != cm->dim) throw std::runtime_error("grids of one dimension required");
+    if (cn->dim == 2)
+      sl_advect2<2>(*cn, *cm, npts, xyz, dt_nm1, dt_n, vnm1, vnm1_dd, vn, vn_dd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
+    else
+      sl_advect2<3>(*cn, *cm, npts, xyz, dt_nm1, dt_n, vnm1, vnm1_dd, vn, vn_dd, phi, phi_dd, velo_method, phi_method, phi_np1, nthreads);
   });
 }
 

@@ -36,6 +36,9 @@ SIG = {
     "ora_locate": (_I, [_P, _I64, _DP, _P]),
     "ora_sl_advect": (_I, [_P, _I64, _DP, _D, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
     "ora_sl_advect_vortex": (_I, [_P, _I64, _DP, _D, _D, _DP, _DP, _I, _DP, _I]),
+    "ora_compute_derivatives_range": (_I, [_P, _DP, _DP, _I64, _I64, _I]),
+    "ora_reinit_stage_range": (_I, [_P, _DP, _DP, _DP, _D, _D, _DP, _DP, _I64, _I64, _I]),
+    "ora_sl_advect2": (_I, [_P, _P, _I64, _DP, _D, _D, _DP, _DP, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
     "ora_vortex": (_I, [_I, _I64, _DP, _D, _DP]),
     "ora_first_derivatives": (_I, [_P, _DP, _DP, _I]),
     "ora_compute_normals": (_I, [_P, _DP, _DP, _I]),
@@ -137,6 +140,20 @@ class OracleGrid:
         out = np.empty((self.dim, self.N), np.float64)
         _chk(load().ora_compute_derivatives(self._h, _dp(f), _dp(out), nthreads))
         return out
+
+    def compute_derivatives_range(self, f, out, first, count, nthreads=1):
+        """compute_derivatives over the nodes [first, first + count) only; out (D, N) updated there."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.dim * self.N
+        _chk(load().ora_compute_derivatives_range(self._h, _dp(np.ascontiguousarray(f, np.float64)), _dp(out), int(first), int(count),
+                                                  nthreads))
+
+    def reinit_stage_range(self, phi_np1, phi_0, phi_n, limit_high, limit_low, dd0, ddc, first, count, nthreads=1):
+        """One reinitialize_one_iteration stage over the nodes [first, first + count) only (dd0/ddc None: first
+        order in space); phi_np1 (N) updated there."""
+        assert phi_np1.dtype == np.float64 and phi_np1.flags.c_contiguous and phi_np1.size == self.N
+        f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        _chk(load().ora_reinit_stage_range(self._h, _dp(phi_np1), _dp(f(phi_0)), _dp(f(phi_n)), float(limit_high), float(limit_low),
+                                           _dp(f(dd0)), _dp(f(ddc)), int(first), int(count), nthreads))
 
     def reinitialize(self, phi, order_space=2, order_pseudotime=2, limit_high=np.finfo(np.float64).max,
                      limit_low=-np.finfo(np.float64).max, iterations=50, nthreads=1):
@@ -258,6 +275,18 @@ class OracleGrid:
         out = np.empty(len(pts), np.float64)
         _chk(load().ora_sl_advect(self._h, len(pts), _dp(pts), float(dt), _dp(v), _dp(vdd), _dp(phi), _dp(phi_dd), int(velo_method),
                                   int(phi_method), _dp(out), nthreads))
+        return out
+
+    def sl_advect2(self, grid_nm1, xyz_np1, dt_nm1, dt_n, vnm1, vn, phi, vnm1_dd=None, vn_dd=None, phi_dd=None, velo_method=4, phi_method=4,
+                   nthreads=1):
+        """Two-velocity second-order step: vn, phi on this grid (time n), vnm1 on grid_nm1, departure from the
+        points xyz_np1 (the new grid's nodes)."""
+        pts = np.ascontiguousarray(xyz_np1, np.float64).reshape(-1, self.dim)
+        f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        out = np.empty(len(pts), np.float64)
+        _chk(load().ora_sl_advect2(self._h, grid_nm1._h, len(pts), _dp(pts), float(dt_nm1), float(dt_n), _dp(f(vnm1)), _dp(f(vnm1_dd)),
+                                   _dp(f(vn)), _dp(f(vn_dd)), _dp(f(phi)), _dp(f(phi_dd)), int(velo_method), int(phi_method),
+                                   _dp(out), nthreads))
         return out
 
     def sl_advect_vortex(self, xyz_np1, dt, vscale, phi, phi_dd=None, phi_method=4, nthreads=1):

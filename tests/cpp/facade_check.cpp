@@ -139,6 +139,34 @@ int main() {
                                           np1_ref.data()));
   if (memcmp(np1.data(), np1_ref.data(), N * sizeof(double)) != 0) return fail("advect_from_n_to_np1");
 
+  // the two-velocity step (velocity n-1 a scaled copy on the same grid) against the C ABI
+  {
+    lsgpu_vec wx{std::vector<double>((size_t)N)}, wy{std::vector<double>((size_t)N)};
+    for (int64_t i = 0; i < N; ++i) {
+      wx.values[i] = 0.8 * vx.values[i] + 0.1;
+      wy.values[i] = 0.8 * vy.values[i];
+    }
+    Vec w[2] = {&wx, &wy};
+    my_p4est_semi_lagrangian_t sl2(f, &ngbd, &ngbd);
+    std::vector<double> np2((size_t)N), np2_ref((size_t)N), ww((size_t)2 * N);
+    sl2.advect_from_n_to_np1(0.04, 0.05, w, nullptr, v, nullptr, &phi, nullptr, np2.data());
+    memcpy(ww.data(), wx.values.data(), N * sizeof(double));
+    memcpy(ww.data() + N, wy.values.data(), N * sizeof(double));
+    lsgpu::check(lsg_semi_lagrangian_advect2(raw, raw, xyz.data(), N, 0.04, 0.05, ww.data(), nullptr, vv.data(), nullptr, phi.values.data(),
+                                             nullptr, LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2,
+                                             LSG_QUADRATIC_NON_OSCILLATORY_CONTINUOUS_V2, np2_ref.data()));
+    if (memcmp(np2.data(), np2_ref.data(), N * sizeof(double)) != 0) return fail("advect_from_n_to_np1 (two velocities)");
+    lsg_forest* fu = nullptr;
+    lsgpu::check(lsg_forest_copy(f, &fu));
+    my_p4est_semi_lagrangian_t up2(fu, &ngbd, &ngbd);
+    up2.set_splitting(3, 7, 2.4);
+    lsgpu_vec phi2{phi.values};
+    Vec p2 = &phi2;
+    if (up2.update_p4est(w, v, 0.04, 0.05, p2, nullptr, &phi) < 1 || phi2.values.size() != (size_t)lsg_forest_num_nodes(fu))
+      return fail("update_p4est (two velocities)");
+    lsg_forest_destroy(fu);
+  }
+
   // extension over the interface with given normals and a mask
   lsgpu_vec q{std::vector<double>((size_t)N)}, nx{std::vector<double>((size_t)N)}, ny{std::vector<double>((size_t)N)};
   for (int64_t i = 0; i < N; ++i) {

@@ -62,6 +62,12 @@ def test_oracle_reproduces_fixtures(golden):
     for m in range(5):
         assert np.array_equal(og.interpolate(m, z["reinit_22"], z["points"]), z[f"interp_{m}"]), m
     assert np.array_equal(og.sl_advect(z["node_xyz"], 0.05, z["velocity"], z["reinit_22"]), z["sl"])
+    if "vnm1" in z:
+        o_nm1 = O.OracleGrid.from_forest(grid_from(z, "nm1_"))
+        x_np1 = grid_from(z, "np1_").node_xyz()
+        for vm in (4, 1):
+            got = og.sl_advect2(o_nm1, x_np1, 0.04, 0.05, z["vnm1"], z["velocity"], z["reinit_22"], velo_method=vm, phi_method=vm)
+            assert np.array_equal(got, z[f"sl2_{vm}"]), vm
 
 
 def test_oracle_reproduces_configuration_1():
@@ -119,6 +125,15 @@ def test_cuda_path_matches_fixtures(golden):
         assert np.array_equal(interp.interpolate_points(z["points"], z["reinit_22"], m), z[f"interp_{m}"]), m
     sl = G.my_p4est_semi_lagrangian_t(f, ls)
     assert np.array_equal(sl.advect_from_n_to_np1(0.05, z["velocity"], z["reinit_22"]), z["sl"])
+    if "vnm1" in z:
+        f_nm1, f_np1 = grid_from(z, "nm1_"), grid_from(z, "np1_")
+        ls_nm1 = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f_nm1))
+        sl2 = G.my_p4est_semi_lagrangian_t(f_np1, ls, ls_nm1=ls_nm1)
+        for vm in (4, 1):
+            sl2.set_velo_interpolation(vm)
+            sl2.set_phi_interpolation(vm)
+            got = sl2.advect_from_n_to_np1(0.04, 0.05, z["vnm1"], z["velocity"], z["reinit_22"])
+            assert np.array_equal(got, z[f"sl2_{vm}"]), vm
 
 
 @pytest.mark.gpu

@@ -145,6 +145,42 @@ def test_semi_lagrangian_step_matches_reference(case):
     assert np.array_equal(og.sl_advect(x, 0.07, v, phi0), rg.sl_advect(0.07, v, vxx, phi0, dd))
 
 
+def _neighbour_grids(name):
+    """Two more grids on the same brick: the grid at n-1 and the new grid at n+1."""
+    if name.startswith("circle2d"):
+        return circle_2d(3, 6, center=(0.04, -0.03)), circle_2d(3, 7, center=(0.02, 0.01))
+    if name.startswith("flower3d"):
+        return flower_3d(3, 4), flower_3d(2, 5)
+    if name.startswith("brick2d"):
+        return brick_2d(1, 4), brick_2d(2, 5)
+    return brick_3d(1, 3), brick_3d(2, 4)
+
+
+@pytest.mark.parametrize("methods", [(4, 4), (1, 1), (0, 2)])
+def test_two_velocity_step_matches_reference(case, methods):
+    """advect_from_n_to_np1(dt_nm1, dt_n, vnm1, vxx_nm1, vn, vxx_n, phi_n, phi_xx_n, phi_np1)
+    (src/my_p4est_semi_lagrangian.cpp:225-319) across three different grids."""
+    f, phi0, rg, og = case
+    name = [g[0] for g in GRIDS if g[1] is f][0]
+    f_nm1, f_np1 = _neighbour_grids(name)
+    r_nm1, r_np1 = R.RefGrid.from_forest(f_nm1), R.RefGrid.from_forest(f_np1)
+    o_nm1 = O.OracleGrid.from_forest(f_nm1)
+    x, xm = f.node_xyz(), f_nm1.node_xyz()
+    vn = np.stack([-x[:, 1] + 0.1, x[:, 0]] + ([0.3 * x[:, 0]] if f.dim == 3 else []))
+    vm = np.stack([-0.9 * xm[:, 1], 1.1 * xm[:, 0] - 0.05] + ([0.2 * xm[:, 1]] if f.dim == 3 else []))
+    vxx_n = np.stack([og.compute_derivatives(vn[c]) for c in range(f.dim)])
+    vxx_m = np.stack([o_nm1.compute_derivatives(vm[c]) for c in range(f.dim)])
+    pdd = og.compute_derivatives(phi0)
+    vmth, pmth = methods
+    ref = r_np1.sl_advect2(rg, r_nm1, 0.04, 0.06, vm, vxx_m, vn, vxx_n, phi0, pdd, vmth, pmth)
+    got = og.sl_advect2(o_nm1, f_np1.node_xyz(), 0.04, 0.06, vm, vn, phi0, vnm1_dd=vxx_m, vn_dd=vxx_n, phi_dd=pdd, velo_method=vmth,
+                        phi_method=pmth)
+    assert np.array_equal(got, ref)
+    # second derivatives computed by the oracle itself when none are given
+    got = og.sl_advect2(o_nm1, f_np1.node_xyz(), 0.04, 0.06, vm, vn, phi0, velo_method=vmth, phi_method=pmth)
+    assert np.array_equal(got, ref)
+
+
 def test_casl_math_matches_reference():
     """interface_Location, interface_Location_With_Second_Order_Derivative (src/casl_math.cpp:55-97) and
     MINMOD (src/casl_math.h:80-88) on random and edge inputs: |f| < EPS at either end, |c2| < EPS, both

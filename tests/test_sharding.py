@@ -1,5 +1,9 @@
-"""Batch sharding across ranks (host logic): every grid on exactly one rank, loads balanced to within
-the largest grid, and the same assignment computed independently on world_size-2 gloo ranks."""
+"""Work split across ranks, host logic on CPU ranks (gloo).
+
+Batches: every grid on exactly one rank, loads balanced to within the largest grid, and the same assignment
+computed independently on world_size-2 ranks. One grid in Morton ranges: the ghost lists cover every stencil,
+and two ranks that sweep their ranges (with the oracle's node-range functions) and exchange ghosts after every
+sweep give the single-rank result bit for bit."""
 import os
 import socket
 
@@ -63,3 +67,147 @@ def test_gloo_world2_ranks_agree():
     assert res[1][1] == owners
     assert sorted(set(owners)) == [1, 2]  # every grid owned by rank 0 or rank 1, none by both
     assert sum(res[0][2]) == sum(sizes)
+
+
+# ---- one grid split into Morton ranges --------------------------------------------------------------
+from casl_p4est_gb300.sharding import MortonPartition, band_linf_sharded, reinit_schedule, reinitialize_sharded, run_schedule  # noqa: E402
+
+POISON = 1.0e30  # entries a rank neither owns nor receives: any read of them would spoil its results
+
+
+class OracleBackend:
+    """A rank's sweeps on the CPU with the oracle's node-range functions (test infrastructure only)."""
+
+    def __init__(self, og):
+        self.og = og
+        self.dim = og.dim
+        self.N = og.N
+
+    def dd(self, f, out, first, count):
+        self.og.compute_derivatives_range(f.numpy(), out.numpy(), first, count)
+
+    def prep(self, phi0, dd0, order_space, limit_high, limit_low, first, count):
+        self.dd0 = None if dd0 is None else dd0.numpy()
+        self.limits = (limit_high, limit_low)
+
+    def stage(self, order_space, phi0, phin, dd, out, avg_with, first, count):
+        hi, lo = self.limits
+        ddc = None if (order_space < 2 or dd is None) else dd.numpy()
+        dd0 = self.dd0 if order_space > 1 else None
+        if avg_with is None:
+            self.og.reinit_stage_range(out.numpy(), phi0.numpy(), phin.numpy(), hi, lo, dd0, ddc, first, count)
+        else:
+            tmp = np.empty(self.N)
+            self.og.reinit_stage_range(tmp, phi0.numpy(), phin.numpy(), hi, lo, dd0, ddc, first, count)
+            a = avg_with.numpy()
+            out.numpy()[first:first + count] = .5 * (a[first:first + count] + tmp[first:first + count])
+
+    def copy(self, src, dst, first, count):
+        dst[first:first + count] = src[first:first + count]
+
+
+def _grid(name):
+    import grids
+    import casl_p4est_gb300 as G
+    if name == "circle2d":
+        f = grids.circle_2d(3, 7)
+        return f, grids.phi0_circle_2d(f)
+    if name == "brick2d":
+        f = grids.brick_2d(1, 6)
+        return f, f.sample(G.shapes.sphere_scaled([0.3, 0.1], 0.6, 0.2, [0.5, 0.5]))
+    if name == "flower3d":
+        f = grids.flower_3d(3, 5)
+        return f, grids.phi0_flower_3d(f)
+    f = grids.brick_3d(1, 4)
+    return f, f.sample(G.shapes.sphere_scaled([0.7, 0.5, 0.9], 0.3, 0.1, [1, 0.5, 1]))
+
+
+def test_morton_partition_ghosts_cover_every_stencil():
+    import casl_p4est_gb300 as G
+    import oracle as O
+    f, _ = _grid("flower3d")
+    og = O.OracleGrid.from_forest(f)
+    rec = og.qnnn(G.qnnn_dtype(3))
+    for world in (1, 2, 3, 5):
+        part = MortonPartition(rec, world)
+        assert part.bounds[0] == 0 and part.bounds[-1] == og.N
+        nb = rec["nb"].reshape(og.N, -1)
+        for r in range(world):
+            b, e = part.bounds[r], part.bounds[r + 1]
+            need = set(np.unique(nb[b:e].ravel()).tolist()) - {-1}
+            have = set(range(b, e)) | set(part.ghosts[r].tolist())
+            assert need <= have
+            assert sorted(np.concatenate([v for v in part.recv[r].values()]).tolist() if part.recv[r] else []) == part.ghosts[r].tolist()
+            for s, idx in part.send[r].items():  # what r sends s is exactly what s expects from r
+                assert np.array_equal(idx, part.recv[s][r])
+                assert np.all((idx >= b) & (idx < e))
+        if world > 1:
+            assert max(len(g) for g in part.ghosts) < 0.25 * og.N  # a halo, not a copy of the grid
+
+
+def _split_worker(rank, world, port, name, orders, iters, limits, q):
+    import torch
+    import torch.distributed as dist
+    import casl_p4est_gb300 as G
+    import oracle as O
+    from casl_p4est_gb300.sharding import HaloExchange
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f, phi0 = _grid(name)
+        og = O.OracleGrid.from_forest(f)
+        part = MortonPartition(og.qnnn(G.qnnn_dtype(f.dim)), world)
+        first, count = part.range_of(rank)
+        phi = torch.full((og.N,), POISON, dtype=torch.float64)
+        phi[first:first + count] = torch.from_numpy(phi0[first:first + count])
+        hi, lo = limits
+        reinitialize_sharded(part, rank, phi, OracleBackend(og), HaloExchange(part, rank), iterations=iters, order_space=orders[0],
+                             order_pseudotime=orders[1], limit_high=hi, limit_low=lo)
+        sizes = [part.range_of(r)[1] for r in range(world)]
+        width = max(sizes)
+        mine = torch.zeros(width, dtype=torch.float64)
+        mine[:count] = phi[first:first + count]
+        pieces = [torch.empty(width, dtype=torch.float64) for _ in range(world)]
+        dist.all_gather(pieces, mine)
+        whole = torch.cat([pieces[r][:sizes[r]] for r in range(world)])
+        ref = torch.from_numpy(phi0.copy())
+        og.reinitialize(ref.numpy(), orders[0], orders[1], hi, lo, iterations=iters)
+        band = band_linf_sharded(part, rank, whole, ref, 0.1)
+        q.put((rank, bool(torch.equal(whole, ref)), float((whole - ref).abs().max()), band))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name,orders,limits", [("circle2d", (2, 2), (np.finfo(np.float64).max, -np.finfo(np.float64).max)),
+                                                ("brick2d", (1, 2), (0.3, -0.2)),
+                                                ("flower3d", (2, 2), (np.finfo(np.float64).max, -np.finfo(np.float64).max)),
+                                                ("brick3d", (2, 1), (0.25, -0.15))])
+def test_morton_split_on_gloo_world2_equals_one_rank(name, orders, limits):
+    """Two CPU ranks, each sweeping its Morton range with the oracle and exchanging the ghosts of phi and of the
+    second derivatives after every sweep: bit-identical to the single-rank result; the band check is one
+    all-reduce and equals zero."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_split_worker, args=(r, 2, port, name, orders, 6, limits, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, equal, diff, band in res:
+        assert equal, (rank, diff)
+        assert band == 0.0
+
+
+def test_schedule_matches_the_reference_sweeps():
+    ops = reinit_schedule(2, 2, 1)
+    kinds = [o[0] for o in ops]
+    # phi_0's derivatives and the preparation once, then per iteration dd, stage, dd, stage (+ average), each
+    # followed by its ghost update
+    assert kinds == ["dd", "exchange", "prep", "dd", "exchange", "stage", "exchange", "dd", "exchange", "stage", "exchange"]
+    assert ops[-2] == ("stage", "phi1", "phi", "phi")
+    assert [o[0] for o in reinit_schedule(1, 1, 2)] == ["prep", "stage", "exchange", "stage", "exchange"]
