@@ -1201,7 +1201,7 @@ int lsg_second_derivatives_range_device(lsg_level_set* ls, const double* f_dev, 
 int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, const double* phi0_dd_dev, int order_space, double limit_high,
                                  double limit_low, int64_t first, int64_t count) {
   return guard([&] {
-    need(phi0_dev != nullptr, "null phi_0");
+    need(phi0_dev != nullptr && phi0_dd_dev != nullptr, "null phi_0 or second derivatives");
     with_ls(ls, [&](auto& L) { L.fp64_prep_range(phi0_dev, phi0_dd_dev, order_space, limit_high, limit_low, first, count); });
   });
 }
@@ -1209,7 +1209,7 @@ int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, cons
 int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const double* phi0_dev, const double* phin_dev,
                                   const double* phin_dd_dev, double* out_dev, const double* avg_with_dev, int64_t first, int64_t count) {
   return guard([&] {
-    need(phi0_dev != nullptr && phin_dev != nullptr && out_dev != nullptr, "null argument");
+    need(phi0_dev != nullptr && phin_dev != nullptr && phin_dd_dev != nullptr && out_dev != nullptr, "null argument");
     with_ls(ls, [&](auto& L) { L.fp64_stage_range(order_space, phi0_dev, phin_dev, phin_dd_dev, out_dev, avg_with_dev, first, count); });
   });
 }

@@ -259,10 +259,29 @@ __device__ __forceinline__ float lin_cls(const DTab32<D>& T, const Cls<D>& C, ui
   return acc;
 }
 
+// the same with the first face node of the direction already loaded (j0); the remaining ones are read
+// only when the face holds more than one node
+template <int D>
+__device__ __forceinline__ float lin_cls_h(const DTab32<D>& T, const Cls<D>& C, uint32_t meta, int dir, int64_t i, int32_t j0,
+                                           const float* __restrict__ f) {
+  constexpr int H = Dim<D>::HALF;
+  const int c = face_count(meta, dir);
+  if (c == 1) return __ldg(f + j0);
+  const int64_t base = (int64_t)(dir * H) * T.nI + i;
+  float acc = fmaf(C.wf(dir, 0), __ldg(f + j0), 0.0f);
+#pragma unroll
+  for (int k = 1; k < H; ++k)
+    if (k < c) acc = fmaf(C.wf(dir, k), __ldg(f + __ldcs(T.i_nbr + base + k * T.nI)), acc);
+  return acc;
+}
+
 // second derivatives on the extended set: irregular nodes (laplace with the class coefficients and
-// the correction matrix) and the listed regular nodes (central differences)
+// the correction matrix) and the listed regular nodes (central differences). An irregular node issues
+// its class id, the first face node of every direction and its own value together, so the class record
+// and the gathers wait for one round trip instead of three.
 template <int D>
 __global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __restrict__ f, float* __restrict__ ddx) {
+  constexpr int H = Dim<D>::HALF;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   float Dv[D];
@@ -270,12 +289,17 @@ __global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __rest
   if (t < T.nI) {
     const int64_t i = t;
     n = T.nR + i;
-    const Cls<D> C = cls_of<D>(T, i);
-    const uint32_t meta = C.meta();
+    const uint32_t ci = __ldcs(T.i_cls + i);
+    int32_t j0[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) j0[dir] = __ldcs(T.i_nbr + (int64_t)(dir * H) * T.nI + i);
     const float f0 = __ldg(f + n);
+    const Cls<D> C{T.cls32 + (int64_t)ci * cls_words<D>()};
+    const uint32_t meta = C.meta();
 #pragma unroll
     for (int a = 0; a < D; ++a)
-      Dv[a] = central_dd(lin_cls<D>(T, C, meta, 2 * a + 1, i, f), f0, lin_cls<D>(T, C, meta, 2 * a, i, f), C.d(2 * a + 1), C.d(2 * a));
+      Dv[a] = central_dd(lin_cls_h<D>(T, C, meta, 2 * a + 1, i, j0[2 * a + 1], f), f0, lin_cls_h<D>(T, C, meta, 2 * a, i, j0[2 * a], f),
+                         C.d(2 * a + 1), C.d(2 * a));
     if (meta & (1u << 16)) {
       float o[D];
 #pragma unroll
@@ -305,6 +329,9 @@ __global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __rest
   for (int a = 0; a < D; ++a) ddx[(int64_t)a * N + n] = Dv[a];
 }
 
+// Irregular nodes [first, last) (first = nR). The loads that depend on nothing but the node (status,
+// class id, the first face node of every direction, its value and second derivatives) are issued together,
+// so the class record and the gathers wait for one round trip instead of three.
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                         const float* __restrict__ s_near, const float* __restrict__ phin,
@@ -314,62 +341,63 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
   const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= last) return;
+  const int64_t i = n - T.nR;
   const uint16_t st = __ldcs(status + n);
+  const uint32_t ci = __ldcs(T.i_cls + i);
+  int32_t j0[2 * D];
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) j0[dir] = __ldcs(T.i_nbr + (int64_t)(dir * H) * T.nI + i);
+  const float f0 = __ldg(phin + n);
+  float Dv[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd_irr + (int64_t)a * N + n);
   float r;
   if (st & ST_ANCHORED) {
     r = 0.0f;
   } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
-    r = phin[n];
+    r = f0;
   } else {
-    const float f0 = __ldg(phin + n);
-    float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
-    {
-      // irregular nodes only (regular ones run in k_reinit_fused_reg32)
-      const int64_t i = n - T.nR;
-      const Cls<D> C = cls_of<D>(T, i);
-      const uint32_t meta = C.meta();
+    float fnb[2 * D], s[2 * D], xxnb[2 * D];
+    const Cls<D> C{T.cls32 + (int64_t)ci * cls_words<D>()};
+    const uint32_t meta = C.meta();
+    const uint32_t wl = meta >> 24;
 #pragma unroll
-      for (int a = 0; a < D; ++a) Dv[a] = __ldg(dd_irr + (int64_t)a * N + n);
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int axis = dir >> 1;
+      const int c = face_count(meta, dir);
+      const int64_t base = (int64_t)(dir * H) * T.nI + i;
+      s[dir] = C.d(dir);
+      if (c == 1) {
+        fnb[dir] = __ldg(phin + j0[dir]);
+        if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd_irr + (int64_t)axis * N + j0[dir]);
+      } else {
+        float v = 0.0f, x = 0.0f;
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        const int axis = dir >> 1;
-        const int c = face_count(meta, dir);
-        const int64_t base = (int64_t)(dir * H) * T.nI + i;
-        s[dir] = C.d(dir);
-        if (c == 1) {
-          const int32_t j = __ldcs(T.i_nbr + base);
-          fnb[dir] = __ldg(phin + j);
-          if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd_irr + (int64_t)axis * N + j);
-        } else {
-          float v = 0.0f, x = 0.0f;
-#pragma unroll
-          for (int k = 0; k < H; ++k) {
-            if (k < c) {
-              const int32_t j = __ldcs(T.i_nbr + base + k * T.nI);
-              const float w = C.wf(dir, k);
-              v = fmaf(w, __ldg(phin + j), v);
-              if (ORDER_SPACE > 1) x = fmaf(w, __ldg(dd_irr + (int64_t)axis * N + j), x);
-            }
+        for (int k = 0; k < H; ++k) {
+          if (k < c) {
+            const int32_t j = k == 0 ? j0[dir] : __ldcs(T.i_nbr + base + k * T.nI);
+            const float w = C.wf(dir, k);
+            v = fmaf(w, __ldg(phin + j), v);
+            if (ORDER_SPACE > 1) x = fmaf(w, __ldg(dd_irr + (int64_t)axis * N + j), x);
           }
-#pragma unroll
-          for (int jj = 0; jj < D - 1; ++jj) v = fmaf(-C.q(dir, jj), Dv[tan_axis32(axis, jj)], v);
-          fnb[dir] = v;
-          xxnb[dir] = x;
         }
+#pragma unroll
+        for (int jj = 0; jj < D - 1; ++jj) v = fmaf(-C.q(dir, jj), Dv[tan_axis32(axis, jj)], v);
+        fnb[dir] = v;
+        xxnb[dir] = x;
       }
-      const uint32_t wl = meta >> 24;
+    }
 #pragma unroll
-      for (int a = 0; a < D; ++a) {
-        if (wl & (1u << (2 * a))) {
-          s[2 * a] = s[2 * a + 1];
-          fnb[2 * a] = fnb[2 * a + 1];
-          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
-        }
-        if (wl & (1u << (2 * a + 1))) {
-          s[2 * a + 1] = s[2 * a];
-          fnb[2 * a + 1] = fnb[2 * a];
-          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
-        }
+    for (int a = 0; a < D; ++a) {
+      if (wl & (1u << (2 * a))) {
+        s[2 * a] = s[2 * a + 1];
+        fnb[2 * a] = fnb[2 * a + 1];
+        Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
+      }
+      if (wl & (1u << (2 * a + 1))) {
+        s[2 * a + 1] = s[2 * a];
+        fnb[2 * a + 1] = fnb[2 * a];
+        Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
       }
     }
     if (st & ST_NEAR) {
@@ -378,18 +406,15 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         s[dir] = __ldg(s_near + (int64_t)dir * N + n);
         if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
       }
-      if (n >= T.nR) {
-        const uint32_t wl = cls_of<D>(T, n - T.nR).meta() >> 24;
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          if (wl & (1u << (2 * a))) {
-            s[2 * a] = s[2 * a + 1];
-            fnb[2 * a] = fnb[2 * a + 1];
-          }
-          if (wl & (1u << (2 * a + 1))) {
-            s[2 * a + 1] = s[2 * a];
-            fnb[2 * a + 1] = fnb[2 * a];
-          }
+      for (int a = 0; a < D; ++a) {
+        if (wl & (1u << (2 * a))) {
+          s[2 * a] = s[2 * a + 1];
+          fnb[2 * a] = fnb[2 * a + 1];
+        }
+        if (wl & (1u << (2 * a + 1))) {
+          s[2 * a + 1] = s[2 * a];
+          fnb[2 * a + 1] = fnb[2 * a];
         }
       }
     }

@@ -405,7 +405,8 @@ void LevelSet<D>::fp64_prep_range(const double* phi0_, const double* dd0_, int o
   check_range(first, count, N);
   if (os < 1 || os > 2) throw std::invalid_argument("reinitialize: the order in space must be 1 or 2");
   if (!(limit_high > limit_low)) throw std::invalid_argument("reinitialize: limit_high must exceed limit_low");
-  if (os > 1 && !dd0_) throw std::invalid_argument("reinitialize: second order in space needs phi_0's second derivatives");
+  // the quadratic neighbour values read the node's own second derivatives at every order
+  if (!phi0_ || !dd0_) throw std::invalid_argument("reinitialize preparation: phi_0 and its second derivatives are required");
   const double big = largest_dbl_smaller_than_dbl_max();
   const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
   const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
@@ -420,7 +421,7 @@ void LevelSet<D>::fp64_stage_range(int os, const double* phi0_, const double* ph
                                    int64_t first, int64_t count) {
   check_range(first, count, N);
   if (!status.p || status.n < (size_t)N) throw std::invalid_argument("reinitialize stage: run the preparation first");
-  if (os > 1 && !dd) throw std::invalid_argument("reinitialize stage: second order in space needs the second derivatives");
+  if (!phi0_ || !phin || !dd || !out) throw std::invalid_argument("reinitialize stage: phi_0, phi_n, its second derivatives and out are required");
   LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0_, phin, dd, out, avg_with, stream, first, count));
   cuda_check(cudaGetLastError(), "reinitialize stage (node range)");
 }

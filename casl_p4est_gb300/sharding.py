@@ -111,19 +111,24 @@ class HaloExchange:
 
 def reinit_schedule(order_space, order_pseudotime, iterations):
     """The sweeps and ghost updates of reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557)
-    for one rank: ("dd", src, dst), ("exchange", name, planes), ("prep",), ("stage", src, dst, avg_with)."""
+    for one rank: ("dd", src, dst), ("exchange", name, planes), ("prep",), ("stage", src, dst, avg_with).
+    The second derivatives are swept at every order: the quadratic neighbour values of a node
+    (ngbd_with_quadratic_interpolation) need its own; second order in space also reads them at the
+    neighbours, so only then are their ghosts updated."""
     ops = []
     second = order_space > 1
+    ops.append(("dd", "phi0", "dd0"))
     if second:
-        ops += [("dd", "phi0", "dd0"), ("exchange", "dd0", True)]
+        ops.append(("exchange", "dd0", True))
     ops.append(("prep",))
     for _ in range(iterations):
+        ops.append(("dd", "phi", "ddc"))
         if second:
-            ops += [("dd", "phi", "ddc"), ("exchange", "ddc", True)]
+            ops.append(("exchange", "ddc", True))
         if order_pseudotime > 1:
-            ops += [("stage", "phi", "phi1", None), ("exchange", "phi1", False)]
+            ops += [("stage", "phi", "phi1", None), ("exchange", "phi1", False), ("dd", "phi1", "ddc")]
             if second:
-                ops += [("dd", "phi1", "ddc"), ("exchange", "ddc", True)]
+                ops.append(("exchange", "ddc", True))
             ops += [("stage", "phi1", "phi", "phi"), ("exchange", "phi", False)]
         else:
             ops += [("stage", "phi", "phi", None), ("exchange", "phi", False)]
@@ -139,14 +144,14 @@ def run_schedule(ops, backend, arrays, first, count, exchange, dim, order_space,
         elif kind == "exchange":
             exchange(arrays[op[1]], dim if op[2] else 1)
         elif kind == "prep":
-            backend.prep(arrays["phi0"], arrays.get("dd0"), order_space, limit_high, limit_low, first, count)
+            backend.prep(arrays["phi0"], arrays["dd0"], order_space, limit_high, limit_low, first, count)
         else:
             src, dst, avg = op[1], op[2], op[3]
             if dst == src and avg is None:  # first order in pseudo-time: phi_n+1 replaces phi_n after the stage
-                backend.stage(order_space, arrays["phi0"], arrays[src], arrays.get("ddc"), arrays["phi1"], None, first, count)
+                backend.stage(order_space, arrays["phi0"], arrays[src], arrays["ddc"], arrays["phi1"], None, first, count)
                 backend.copy(arrays["phi1"], arrays[dst], first, count)
             else:
-                backend.stage(order_space, arrays["phi0"], arrays[src], arrays.get("ddc"), arrays[dst],
+                backend.stage(order_space, arrays["phi0"], arrays[src], arrays["ddc"], arrays[dst],
                               arrays[avg] if avg else None, first, count)
 
 
@@ -159,10 +164,9 @@ def reinitialize_sharded(part: MortonPartition, rank: int, phi, backend, exchang
     N = part.N
     dim = backend.dim
     exchange(phi, 1)
-    arrays = {"phi": phi, "phi0": phi.clone(), "phi1": torch.empty_like(phi)}
-    if order_space > 1:
-        arrays["dd0"] = torch.zeros(dim * N, dtype=phi.dtype, device=phi.device)
-        arrays["ddc"] = torch.zeros(dim * N, dtype=phi.dtype, device=phi.device)
+    arrays = {"phi": phi, "phi0": phi.clone(), "phi1": torch.empty_like(phi),
+              "dd0": torch.zeros(dim * N, dtype=phi.dtype, device=phi.device),
+              "ddc": torch.zeros(dim * N, dtype=phi.dtype, device=phi.device)}
     first, count = part.range_of(rank)
     run_schedule(reinit_schedule(order_space, order_pseudotime, iterations), backend, arrays, first, count, exchange, dim, order_space,
                  limit_high, limit_low)

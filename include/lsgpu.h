@@ -362,9 +362,12 @@ int lsg_band_linf_device(lsg_level_set* ls, const double* a_dev, const double* b
  * lsg_second_derivatives_range_device: f_dd (dim x N) at the range.
  * lsg_reinit_prep_range_device: what the stages derive from phi_0 alone (status, subcell distances, kept in
  * the level set) with the phi_0 limits of reinitialize_within_range_of_phi_0; phi0_dd as from
- * lsg_second_derivatives_range_device (NULL for first order in space).
- * lsg_reinit_stage_range_device: out = one stage of phin (phin_dd its second derivatives, NULL for first
- * order), or 0.5 (avg_with + stage) when avg_with is given (the RK average; may alias out). */
+ * lsg_second_derivatives_range_device.
+ * lsg_reinit_stage_range_device: out = one stage of phin (phin_dd its second derivatives), or
+ * 0.5 (avg_with + stage) when avg_with is given (the RK average; may alias out).
+ * The second derivatives are required at every order (the quadratic neighbour values of
+ * ngbd_with_quadratic_interpolation read the node's own); at second order in space the stages also read
+ * them at the neighbours, whose ghost values the caller must then update too. */
 int lsg_second_derivatives_range_device(lsg_level_set* ls, const double* f_dev, double* f_dd_dev, int64_t first, int64_t count);
 int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, const double* phi0_dd_dev, int order_space, double limit_high,
                                  double limit_low, int64_t first, int64_t count);

@@ -125,3 +125,34 @@ def test_device_built_batch_equals_host_built(batch2d, dim):
     host.reinitialize_2nd_order(a, its)
     dev.reinitialize_2nd_order(b, its)
     assert np.array_equal(a, b)
+
+
+def test_every_grid_of_a_batch_within_the_fp64_band_tolerance():
+    """Each grid of a batch (sizes from 4k to about 400k nodes, refined in a wide band as the batch workload
+    is) against its own FP64 reinitialisation: band L-infinity within 1e-4 dx_min in |phi| < 3 dx_min, and the
+    interface zero crossings along the cut grid edges within the same bound."""
+    import torch
+    rng = np.random.default_rng(17)
+    grids = []
+    for lmax in (6, 8, 9, 11):
+        items = [(rng.uniform(-0.6, 0.6), rng.uniform(-0.6, 0.6), rng.uniform(0.05, 0.4), rng.uniform(0.05, 0.4),
+                  rng.uniform(0, np.pi)) for _ in range(int(rng.integers(1, 9)))]
+        scale = (0.1, (rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5)), rng.uniform(0.5, 1.5))
+        f = G.my_p4est_brick_new([1, 1], [-1, -1], [1, 1])
+        f.refine_levelset(shapes.ellipses(items), 6, lmax, lip=14.4)
+        f.build_nodes()
+        grids.append((f, f.sample(shapes.ellipses(items, scale=scale)), lmax))
+    assert grids[-1][0].num_nodes > 200000
+    b = G.my_p4est_level_set_batch_t([g[0] for g in grids])
+    phi = b.concat([g[1] for g in grids])
+    b.reinitialize_2nd_order(phi, 30)
+    for k, (f, p0, lmax) in enumerate(grids):
+        ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+        ref = p0.copy()
+        ls.reinitialize_2nd_order(ref, 30, precision="fp64")
+        got = b.split(phi)[k]
+        dmin = 2.0 / (1 << lmax)
+        band = np.abs(ref) < 3 * dmin
+        assert float(np.max(np.abs(got[band] - ref[band]))) <= 1e-4 * dmin, k
+        loc, edges, mismatched = ls.interface_location_error(torch.from_numpy(got).cuda(), torch.from_numpy(ref).cuda())
+        assert edges > 0 and mismatched == 0 and loc <= 1e-4 * dmin, (k, loc, edges, mismatched)

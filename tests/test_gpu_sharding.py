@@ -35,10 +35,9 @@ def lockstep(part, backend, phi0, order_space, order_pseudotime, iterations, lim
         first, count = part.range_of(r)
         phi = torch.full((N,), POISON, dtype=torch.float64, device="cuda")
         phi[first:first + count] = phi0[first:first + count]
-        arrays = {"phi": phi, "phi1": torch.empty_like(phi)}
-        if order_space > 1:
-            arrays["dd0"] = torch.full((D * N,), POISON, dtype=torch.float64, device="cuda")
-            arrays["ddc"] = torch.full((D * N,), POISON, dtype=torch.float64, device="cuda")
+        arrays = {"phi": phi, "phi1": torch.empty_like(phi),
+                  "dd0": torch.full((D * N,), POISON, dtype=torch.float64, device="cuda"),
+                  "ddc": torch.full((D * N,), POISON, dtype=torch.float64, device="cuda")}
         ranks.append((first, count, arrays))
 
     def exchange_all(name, planes):
