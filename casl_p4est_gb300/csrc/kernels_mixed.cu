@@ -471,33 +471,26 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
       r = f0;
     } else {
-      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fn2[2 * D];
+      // one round of gathers: every face value and, per direction, the second neighbour's value or
+      // (when the face node has none recorded) the face node's second derivative along the axis
+      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fx[2 * D];
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
         fnb[dir] = __ldg(phin + nb[dir]);
-        if (ORDER_SPACE > 1 && (far >> 31)) fn2[dir] = __ldg(phin + nb2[dir]);
+        if (ORDER_SPACE > 1) fx[dir] = __ldg(nb2[dir] >= 0 ? phin + nb2[dir] : dd_irr + (int64_t)(dir >> 1) * T.N + nb[dir]);
         s[dir] = level_size(T.tsize[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
       }
 #pragma unroll
       for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
       if (ORDER_SPACE > 1) {
-        if (far >> 31) {
 #pragma unroll
-          for (int dir = 0; dir < 2 * D; ++dir) {
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          if (nb2[dir] >= 0) {
             const float dfar = level_size(T.tsize[dir >> 1], T.base, (far >> (4 * dir)) & 15u);
             // outer side of the face node: second neighbour; inner side: this node
-            xxnb[dir] = (dir & 1) ? central_dd(fn2[dir], fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], fn2[dir], s[dir], dfar);
-          }
-        } else {
-#pragma unroll
-          for (int dir = 0; dir < 2 * D; ++dir) {
-            if (nb2[dir] >= 0) {
-              const float dfar = level_size(T.tsize[dir >> 1], T.base, (far >> (4 * dir)) & 15u);
-              const float f2 = __ldg(phin + nb2[dir]);
-              xxnb[dir] = (dir & 1) ? central_dd(f2, fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], f2, s[dir], dfar);
-            } else {
-              xxnb[dir] = __ldg(dd_irr + (int64_t)(dir >> 1) * T.N + nb[dir]);
-            }
+            xxnb[dir] = (dir & 1) ? central_dd(fx[dir], fnb[dir], f0, dfar, s[dir]) : central_dd(f0, fnb[dir], fx[dir], s[dir], dfar);
+          } else {
+            xxnb[dir] = fx[dir];
           }
         }
       }
