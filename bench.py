@@ -44,8 +44,9 @@ def parse():
     p.add_argument("--iters", type=int, default=ITERS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--fp64-steps", type=int, default=2)
-    p.add_argument("--workload", default="reinit3d", choices=["reinit3d", "transport3d", "batch2d", "large3d"],
-                   help="reinit3d: the headline reinitialisation line; transport3d: the level-set transport run "
+    p.add_argument("--workload", default="reinit3d", choices=["reinit3d", "reinit2d", "transport3d", "batch2d", "large3d"],
+                   help="reinit3d: the headline reinitialisation line; reinit2d: the 2D quadtree configuration (FP64, 20 "
+                        "iterations, error against r - 0.5); transport3d: the level-set transport run "
                         "(semi-Lagrangian step + host regrid + 5 reinitialisation iterations per step; --steps time steps); "
                         "batch2d: 256 quadtrees reinitialised together (--steps timed batch calls)")
     p.add_argument("--batch", type=int, default=256, help="batch2d: number of quadtrees")
@@ -536,6 +537,85 @@ def run_large(args):
     print(json.dumps(out), flush=True)
 
 
+def run_reinit2d(args):
+    """The 2D configuration: quadtree on [-1,1]^2, levels 4-9, refined where |r - 0.5| <= 1.2 diag (lip 2.4);
+    phi0 = (r - 0.5)(0.1 + (x-0.2)^2 + (y-0.3)^2); reinitialize_2nd_order, 20 iterations, FP64. Error
+    max |phi - (r - 0.5)| over |phi| < 3 dx_min (and over |phi| < 3 diag_min, the example's band). The FP64
+    GPU path, the mixed path and the CPU restatement (all host cores and one core) on the same grid; the FP64
+    GPU result must equal the CPU result bit for bit."""
+    import torch
+    import casl_p4est_gb300 as G
+    from casl_p4est_gb300 import shapes
+    torch.cuda.set_device(0)
+    iters, lmin, lmax = 20, 4, 9
+    f = G.my_p4est_brick_new([1, 1], [-1, -1], [1, 1])
+    f.refine_levelset(shapes.sphere([0, 0], 0.5), lmin, lmax, lip=LIP)
+    f.build_nodes()
+    phi0 = f.sample(shapes.sphere_scaled([0, 0], 0.5, 0.1, [0.2, 0.3]))
+    N = f.num_nodes
+    x = f.node_xyz()
+    exact = np.sqrt(x[:, 0] ** 2 + x[:, 1] ** 2) - 0.5
+    _, dmin, diag = f.dxyz_min(lmax)
+    stream = torch.cuda.current_stream()
+    ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f))
+    ls.set_stream(stream.cuda_stream)
+    phi0_d = torch.from_numpy(phi0).cuda()
+    phi_d = torch.empty_like(phi0_d)
+
+    def gpu(prec, steps):
+        for _ in range(args.warmup):
+            phi_d.copy_(phi0_d)
+            ls.reinitialize_2nd_order(phi_d, iters, precision=prec)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(steps):
+            phi_d.copy_(phi0_d)
+            e0.record(stream)
+            ls.reinitialize_2nd_order(phi_d, iters, precision=prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / steps, phi_d.cpu().numpy()
+
+    ms64, p64 = gpu("fp64", args.steps)
+    ms32, p32 = gpu("mixed", args.steps)
+    cores = os.cpu_count() or 1
+    cpu = {}
+    for nt in (cores, 1):
+        reps = 5 if nt > 1 else 2
+        best = None
+        for _ in range(reps):
+            s, pc = cpu_reinit_sample(f, phi0, iters, nt)
+            best = s if best is None else min(best, s)
+        cpu[nt] = (best, pc)
+
+    def err(p, band):
+        m = np.abs(p) < band
+        return float(np.max(np.abs(p[m] - exact[m])))
+
+    band = np.abs(p64) < 3 * dmin
+    out = {
+        "metric": "reinit node-iters/s, 2D quadtree L4-9, 20 iterations (FP64 GPU vs CPU restatement) and error vs r-0.5",
+        "value": N * iters / (ms64 / 1e3), "unit": "node-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"2D quadtree [-1,1]^2 levels {lmin}-{lmax} (lip 2.4), {N} nodes, phi0 = (r-0.5)(0.1+(x-0.2)^2+(y-0.3)^2), "
+                               f"reinitialize_2nd_order {iters} iterations", "nodes": N, "iterations": iters,
+                   "l2": "working set inside L2 (a 2D grid of this size; no flush, each step restarts from phi0)"},
+        "fp64_gpu": {"ms": ms64, "value": N * iters / (ms64 / 1e3), "err_3dx_min": err(p64, 3 * dmin), "err_3diag_min": err(p64, 3 * diag)},
+        "mixed_gpu": {"ms": ms32, "value": N * iters / (ms32 / 1e3), "err_3dx_min": err(p32, 3 * dmin),
+                      "band_linf_vs_fp64_over_dx_min": float(np.max(np.abs(p32[band] - p64[band]))) / dmin},
+        "cpu_restatement": {str(nt): {"ms": 1e3 * s, "value": N * iters / s} for nt, (s, _) in cpu.items()},
+        "cpu_err_3dx_min": err(cpu[cores][1], 3 * dmin),
+        "fp64_gpu_equals_cpu": bool(np.array_equal(p64, cpu[cores][1]) and np.array_equal(p64, cpu[1][1])),
+        "dx_min": dmin, "diag_min": diag,
+        "cpu_baseline": {"value": N * iters / cpu[cores][0], "unit": "node-iters/s", "cores": cores, "kind": "port",
+                         "sample": f"the whole workload ({iters} iterations x {N} nodes), best of 5, oracle/ (CPU restatement of the reference loops)"},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -554,6 +634,10 @@ def main():
     if args.workload == "large3d":
         if rank == 0:
             run_large(args)
+        return
+    if args.workload == "reinit2d":
+        if rank == 0:
+            run_reinit2d(args)
         return
 
     import torch

@@ -1159,6 +1159,7 @@ int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int
         config[1] = L.cfg.uniform_blocks;
         config[2] = L.cfg.regular_blocks;
         config[3] = L.cfg.depth;
+        config[4] = L.cfg.halo;
       }
     });
   });
@@ -1172,6 +1173,7 @@ int lsg_level_set_stage_config(const lsg_level_set* ls, int* config) {
     config[1] = c.uniform_blocks;
     config[2] = c.regular_blocks;
     config[3] = c.depth;
+    config[4] = c.halo;
   });
 }
 
@@ -1180,12 +1182,14 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config != nullptr, "null config");
     need(config[0] == 32 || config[0] == 64 || config[0] == 128 || config[0] == 256, "threads per block must be 32, 64, 128 or 256");
     need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
-    need(config[3] >= 1 && config[3] <= 3, "pipeline depth must be 1, 2 or 3");
+    need(config[3] >= 1 && config[3] <= 4, "pipeline depth must be 1, 2, 3 or 4");
+    need(config[4] >= 0 && config[4] <= 4096 && config[4] % 4 == 0, "window halo must be a multiple of 4 in 0..4096");
     with_ls(ls, [&](auto& L) {
       L.cfg.tpb = config[0];
       L.cfg.uniform_blocks = config[1];
       L.cfg.regular_blocks = config[2];
       L.cfg.depth = config[3];
+      L.cfg.halo = config[4];
       L.drop_graph();
     });
   });

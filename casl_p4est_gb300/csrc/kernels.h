@@ -36,9 +36,12 @@ struct StageCfg {
   int uniform_blocks = 0;
   int regular_blocks = 0;
   int tpb = 256;
-  // pipeline of the uniform kernel: 1 or 2 nodes whose gathers are in flight per thread, or 3: the
-  // node words bulk-copied into shared memory three tiles ahead (cp.async.bulk + mbarrier)
+  // pipeline of the uniform kernel: 1 or 2 nodes whose gathers are in flight per thread, or 3 (4): the
+  // node words and a window of phi bulk-copied into shared memory two (three) tiles ahead
+  // (cp.async.bulk + mbarrier)
   int depth = 1;
+  // nodes on either side of a tile in the phi window of the bulk-copy kernel (a multiple of 4)
+  int halo = 512;
   // bound of the bulk kernel's waits for its copies, in SM clock cycles (0: about a second); a wait that
   // runs out makes the call report LSG_ETIMEOUT
   long long wait_cycles = 0;

@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
     double gp[D], gm[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      gp[a] = (fnb[2 * a + 1] - f0) / s[2 * a + 1];
-      gm[a] = (f0 - fnb[2 * a]) / s[2 * a];
+      gp[a] = qdiv(fnb[2 * a + 1] - f0, s[2 * a + 1]);
+      gm[a] = qdiv(f0 - fnb[2 * a], s[2 * a]);
     }
     if (ORDER_SPACE > 1) {
 #pragma unroll
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
     double dt = min2(s[0], s[1]);
     dt = min3(dt, s[2], s[3]);
     if (D == 3) dt = min3(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
-    dt /= (double)D;
+    dt = qdiv(dt, (double)D);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       if (sgn * gp[a] > 0.0) gp[a] = 0.0;
@@ -223,8 +223,8 @@ __global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const doubl
   double gp[D], gm[D];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    gp[a] = (fnb[2 * a + 1] - f0) / s[2 * a + 1];
-    gm[a] = (f0 - fnb[2 * a]) / s[2 * a];
+    gp[a] = qdiv(fnb[2 * a + 1] - f0, s[2 * a + 1]);
+    gm[a] = qdiv(f0 - fnb[2 * a], s[2 * a]);
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) {
@@ -272,7 +272,7 @@ __device__ __forceinline__ double grad_comp64(const DTab64<D>& T, const DGrad& G
   const double f0 = f[n];
   const double fm = lin64<D>(T, 2 * a, n, f), fp = lin64<D>(T, 2 * a + 1, n, f);
   const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
-  double g = ((fp - f0) * dm / dp + (f0 - fm) * dp / dm) / (dp + dm);
+  double g = qdiv(qdiv((fp - f0) * dm, dp) + qdiv((f0 - fm) * dp, dm), dp + dm);
   if (r >= 0) {
     const uint8_t mask = G.gmask[r];
 #pragma unroll
@@ -481,11 +481,11 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
       if (neg) {
         const double dx = T.d[n] + T.d[N + n], dy = T.d[2 * N + n] + T.d[3 * N + n];
         const int mm0 = D == 3 ? 8 : 0, pm0 = D == 3 ? 9 : 1, mp0 = D == 3 ? 10 : 2, pp0 = D == 3 ? 11 : 3;
-        Qxy = (q[nb[pp0]] + q[nb[mm0]] - q[nb[mp0]] - q[nb[pm0]]) / dx / dy;
+        Qxy = qdiv(qdiv(q[nb[pp0]] + q[nb[mm0]] - q[nb[mp0]] - q[nb[pm0]], dx), dy);
         if (D == 3) {
           const double dz = T.d[4 * N + n] + T.d[5 * N + n];
-          Qyz = (q[nb[7]] + q[nb[4]] - q[nb[6]] - q[nb[5]]) / dy / dz;
-          Qzx = (q[nb[3]] + q[nb[0]] - q[nb[1]] - q[nb[2]]) / dz / dx;
+          Qyz = qdiv(qdiv(q[nb[7]] + q[nb[4]] - q[nb[6]] - q[nb[5]], dy), dz);
+          Qzx = qdiv(qdiv(q[nb[3]] + q[nb[0]] - q[nb[1]] - q[nb[2]], dz), dx);
         }
         ok = true;
       }
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
   for (int a = 0; a < D; ++a) {
     const double fp = quad_nb64<D>(T, 2 * a + 1, n, q, Dq), fm = quad_nb64<D>(T, 2 * a, n, q, Dq);
     const double dp = T.d[(int64_t)(2 * a + 1) * N + n], dm = T.d[(int64_t)(2 * a) * N + n];
-    Qaa[a] = ((fp - q[n]) / dp + (fm - q[n]) / dm) * 2. / (dp + dm);
+    Qaa[a] = qdiv((qdiv(fp - q[n], dp) + qdiv(fm - q[n], dm)) * 2., dp + dm);
   }
   const double Qx = qx[n], Qy = qx[N + n];
   const double Nx = nrm[n], Ny = nrm[N + n];
@@ -538,8 +538,8 @@ __global__ void __launch_bounds__(TPB) k_ext_march(DTab64<D> T, const double* __
   double g[3];
 #pragma unroll
   for (int a = 0; a < D; ++a)
-    g[a] = nrm[(int64_t)a * N + n] > 0 ? (v[n] - lin64<D>(T, 2 * a, n, v)) / T.d[(int64_t)(2 * a) * N + n]
-                                        : (lin64<D>(T, 2 * a + 1, n, v) - v[n]) / T.d[(int64_t)(2 * a + 1) * N + n];
+    g[a] = nrm[(int64_t)a * N + n] > 0 ? qdiv(v[n] - lin64<D>(T, 2 * a, n, v), T.d[(int64_t)(2 * a) * N + n])
+                                        : qdiv(lin64<D>(T, 2 * a + 1, n, v) - v[n], T.d[(int64_t)(2 * a + 1) * N + n]);
   double s = nrm[n] * g[0] + nrm[N + n] * g[1];
   if (D == 3) s = s + nrm[2 * N + n] * g[2];
   tmp[n] = SRC ? v[n] - dt * (s - src[n]) : v[n] - dt * s;
@@ -557,8 +557,8 @@ __global__ void __launch_bounds__(TPB) k_ext_q(DTab64<D> T, const double* __rest
   double g[3];
 #pragma unroll
   for (int a = 0; a < D; ++a)
-    g[a] = nrm[(int64_t)a * N + n] > 0 ? (q[n] - lin64<D>(T, 2 * a, n, q)) / T.d[(int64_t)(2 * a) * N + n]
-                                        : (lin64<D>(T, 2 * a + 1, n, q) - q[n]) / T.d[(int64_t)(2 * a + 1) * N + n];
+    g[a] = nrm[(int64_t)a * N + n] > 0 ? qdiv(q[n] - lin64<D>(T, 2 * a, n, q), T.d[(int64_t)(2 * a) * N + n])
+                                        : qdiv(lin64<D>(T, 2 * a + 1, n, q) - q[n], T.d[(int64_t)(2 * a + 1) * N + n]);
   if (ORDER == 2) {
 #pragma unroll
     for (int a = 0; a < D; ++a) {
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(TPB) k_efi_stage64(DTab64<D> T, const double* 
     double dt = min2(s[0], s[1]);
     dt = min3(dt, s[2], s[3]);
     if (D == 3) dt = min3(dt, s[D == 3 ? 4 : 0], s[D == 3 ? 5 : 0]);
-    dt /= ((double)D);
+    dt = qdiv(dt, (double)D);
     const double gx = grad[n], gy = grad[N + n], gz = D == 3 ? grad[(D == 3 ? 2 : 0) * N + n] : 0.0;
     const double mag = D == 3 ? sqrt(gx * gx + gy * gy + gz * gz) : sqrt(gx * gx + gy * gy);
     const double sg = phi[n] < 0.0 ? -1.0 : +1.0;
@@ -644,8 +644,8 @@ __global__ void __launch_bounds__(TPB) k_efi_stage64(DTab64<D> T, const double* 
     double t[3];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      const double qm = (q0 - qn[2 * a]) / s[2 * a] + 0.5 * s[2 * a] * minmod(dm[a], d0[a]);
-      const double qp = (qn[2 * a + 1] - q0) / s[2 * a + 1] - 0.5 * s[2 * a + 1] * minmod(dp[a], d0[a]);
+      const double qm = qdiv(q0 - qn[2 * a], s[2 * a]) + 0.5 * s[2 * a] * minmod(dm[a], d0[a]);
+      const double qp = qdiv(qn[2 * a + 1] - q0, s[2 * a + 1]) - 0.5 * s[2 * a + 1] * minmod(dp[a], d0[a]);
       t[a] = nv[a] * (nv[a] > 0.0 ? qm : qp);
     }
     res = q0 - dt * (D == 3 ? (t[0] + t[1] + t[D == 3 ? 2 : 0]) : (t[0] + t[1]));

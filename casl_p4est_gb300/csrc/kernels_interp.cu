@@ -65,7 +65,7 @@ __device__ int32_t locate(const DLoc<D>& L, const double* xyz) {
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     double xs = xyz[a] - L.xyz_min[a];
-    xs /= L.tree_dim[a];
+    xs = st64::qdiv(xs, L.tree_dim[a]);
     xs = max2(qeps, min2(xs, L.n[a] - qeps));
     tr[a] = (int)floor(xs);
     c[a] = (xs - tr[a]) * ROOT;
@@ -111,14 +111,14 @@ __device__ __forceinline__ void local_weights(const DLoc<D>& L, int32_t q, const
   int32_t X[3] = {0, 0, 0};
   unmorton<D>(key & ((uint64_t(1) << tree_shift<D>()) - 1), X);
   const int lvl = __ldg(L.level + q);
-  const double qh = (double)(Dim<D>::ROOT_LEN >> lvl) / (double)Dim<D>::ROOT_LEN;
+  const double qh = st64::qdiv((double)(Dim<D>::ROOT_LEN >> lvl), (double)Dim<D>::ROOT_LEN);
   double d0[3], d1[3];
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     const double tmin = __ldg(L.tmin + 3 * tree + a), tmax = __ldg(L.tmax + 3 * tree + a);
-    const double qmin = (double)X[a] / (double)Dim<D>::ROOT_LEN;
-    double x = (xg[a] - tmin) / (tmax - tmin);
-    x = (x - qmin) / qh;
+    const double qmin = st64::qdiv((double)X[a], (double)Dim<D>::ROOT_LEN);
+    double x = st64::qdiv(xg[a] - tmin, tmax - tmin);
+    x = st64::qdiv(x - qmin, qh);
     d0[a] = 1.0 - x;
     d1[a] = x;
     const double h = (tmax - tmin) * qh;

@@ -642,23 +642,26 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uin
   }
 }
 
-// ---- uniform kernel with bulk-copied stencil words ------------------------------------------------
-// The same update, with the words each node streams from HBM (status, level code, the 4D face and
-// second-neighbour indices, its own value and the RK partner) moved into shared memory by bulk
-// asynchronous copies (cp.async.bulk, completion counted on an mbarrier) STAGES tiles ahead of the
-// tile being computed. The threads then issue only the gathers of the face values, so the table
-// stream no longer waits on gather latency and needs no registers to stay in flight.
+// ---- uniform kernel with bulk-copied stencil words and a staged window of phi ---------------------
+// The same update, with everything a tile of nodes reads moved into shared memory by bulk asynchronous
+// copies (cp.async.bulk, completion counted on an mbarrier) STAGES tiles ahead of the tile being
+// computed: the words each node streams from HBM (status, level code, the 4D face and second-neighbour
+// indices, the RK partner) and the window phi[m0 - halo, m0 + tile + halo) of the Morton-contiguous
+// tile [m0, m0 + tile). In Morton order most face and second neighbours of a tile's nodes lie in that
+// window (about 79% of the references with halo 512 on the 3D flower grids), so those values come from
+// shared memory; the rest are gathered from global memory. The node's own value is read from the
+// window too.
 //
 // A CTA owns tiles blockIdx.x, blockIdx.x + gridDim.x, ... of blockDim.x nodes. Copies start on
-// 16-byte boundaries: a segment starting at element e0 is copied from e0 rounded down to 16 bytes
-// and read at the remainder. A tile is copied only when its node range ends at least 8 nodes before
-// the uniform group does, so every copied byte lies inside its array (a plane of the index tables
-// holds nR >= nU entries); the last tiles load directly from global memory. Every wait on an
-// mbarrier is bounded (wait_cycles SM clock cycles, about a second by default); the CTA then decides
-// together (__syncthreads_or, so no thread is left at a barrier the others skip) whether any thread gave
-// up, and if so sets *err, lets the copies it issued land (bounded by the full limit) and stops.
-// NPT nodes per thread and tile: the launcher uses one (two measured slower on the 13.7M-node
-// flower grid: fewer, larger tiles leave less room for the concurrent irregular kernels).
+// 16-byte boundaries: a table segment starting at element e0 is copied from e0 rounded down to 16
+// bytes and read at the remainder; the window starts at a multiple of 4 elements and ends at most at
+// N rounded down to a multiple of 4. A tile is copied only when its node range ends at least 8 nodes
+// before the uniform group does, so every copied byte lies inside its array (a plane of the index
+// tables holds nR >= nU entries, phi holds N >= nU); the last tiles load directly from global memory.
+// Every wait on an mbarrier is bounded (wait_cycles SM clock cycles, about a second by default) and
+// suspends the thread between polls (try_wait) instead of spinning; the CTA then decides together
+// (__syncthreads_or, so no thread is left at a barrier the others skip) whether any thread gave up,
+// and if so sets *err, lets the copies it issued land (bounded by the full limit) and stops.
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -671,23 +674,23 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
       "r"(bytes)
       : "memory");
 }
-// non-blocking test of the phase (test_wait, unlike try_wait, never suspends the thread, so the bound
-// below is kept to the cycle)
-__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+// potentially blocking test of the phase: the thread may be suspended until the phase completes or a
+// hardware time limit passes, so a waiting warp takes no issue slots from the warps doing work
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(done)
       : "r"(smem_addr(bar)), "r"(parity)
       : "memory");
   return done != 0;
 }
-// false once `limit` SM cycles have passed without the phase completing
+// false once `limit` SM cycles have passed without the phase completing (checked after every poll)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
-  while (!mbar_test_wait(bar, parity))
+  while (!mbar_try_wait(bar, parity))
     if (clock64() - t0 > limit) return false;
   return true;
 }
@@ -698,17 +701,20 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                : "memory");
 }
 
-// segments of a tile: status (u16), level code word, 2D face-index planes, 2D second-neighbour
-// planes, phi_n, and the RK partner when averaging
+// table segments of a tile: status (u16), level code word, 2D face-index planes, 2D second-neighbour
+// planes, and the RK partner when averaging; then the phi window
 template <int D, bool AVG>
 struct UniBulk {
-  static constexpr int NSEG = 2 + 4 * D + 1 + (AVG ? 1 : 0);
+  static constexpr int NSEG = 2 + 4 * D + (AVG ? 1 : 0);
   // bytes of one segment's slot in a stage (tile + 8 elements, 16-byte multiple)
   static __host__ __device__ uint32_t slot_bytes(int tile, int es) { return (uint32_t)(((tile + 8) * es + 15) & ~15); }
-  static __host__ __device__ uint32_t stage_bytes(int tile) { return slot_bytes(tile, 2) + (NSEG - 1) * slot_bytes(tile, 4); }
+  static __host__ __device__ uint32_t table_bytes(int tile) { return slot_bytes(tile, 2) + (NSEG - 1) * slot_bytes(tile, 4); }
+  // the window holds at most tile + 2 halo + 4 values (halo a multiple of 4)
+  static __host__ __device__ uint32_t window_bytes(int tile, int halo) { return (uint32_t)((tile + 2 * halo + 8) * 4); }
+  static __host__ __device__ uint32_t stage_bytes(int tile, int halo) { return table_bytes(tile) + window_bytes(tile, halo); }
   // global array, element size and first element of segment g for the tile starting at node m0
-  static __device__ __forceinline__ const char* seg(const DTab32<D>& T, const uint16_t* status, const float* phin, const float* avg_with,
-                                                     int g, int64_t m0, int& es, int64_t& e0) {
+  static __device__ __forceinline__ const char* seg(const DTab32<D>& T, const uint16_t* status, const float* avg_with, int g, int64_t m0,
+                                                     int& es, int64_t& e0) {
     const int64_t nR = T.nR;
     es = g == 0 ? 2 : 4;
     if (g == 0) {
@@ -728,23 +734,36 @@ struct UniBulk {
       return (const char*)T.r_nbr2;
     }
     e0 = m0;
-    return g == 2 + 4 * D ? (const char*)phin : (const char*)avg_with;
+    return (const char*)avg_with;
   }
   static __device__ __forceinline__ uint32_t slot_offset(int tile, int g) { return g == 0 ? 0 : slot_bytes(tile, 2) + (g - 1) * slot_bytes(tile, 4); }
+  // window [w0, w0 + len) of the tile at m0: w0 = max(m0 - halo, 0) rounded down to a multiple of 4;
+  // the end m0 + tile + halo, at most nal (N rounded down to a multiple of 4), rounded up to a multiple of 4
+  static __device__ __forceinline__ void window(int64_t m0, int tile, int halo, int64_t nal, int64_t& w0, int& len) {
+    int64_t lo = m0 - halo;
+    if (lo < 0) lo = 0;
+    lo &= ~(int64_t)3;
+    int64_t hi = m0 + tile + halo;
+    if (hi > nal) hi = nal;
+    w0 = lo;
+    len = (int)(((hi + 3) & ~(int64_t)3) - lo);
+  }
 };
 
 template <int D, bool AVG, int STAGES, int NPT>
 __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, const uint16_t* __restrict__ status,
                                                                const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                               float* out, const float* avg_with, int* err, long long wait_cycles) {
+                                                               float* out, const float* avg_with, int* err, long long wait_cycles, int halo) {
   using B = UniBulk<D, AVG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[STAGES];
   const int tile = NPT * blockDim.x;  // NPT nodes per thread and tile
   const int tid = threadIdx.x;
   const int64_t nU = T.nU;
+  const int64_t nal = T.N & ~(int64_t)3;
   const int64_t ntiles = (nU + tile - 1) / tile;
-  const uint32_t sb = B::stage_bytes(tile);
+  const uint32_t sb = B::stage_bytes(tile, halo);
+  const uint32_t woff = B::table_bytes(tile);
   // tile k of this CTA is copied when it ends at least 8 nodes before the uniform group does
   auto tile_of = [&](int64_t k) { return (int64_t)blockIdx.x + k * (int64_t)gridDim.x; };
   auto bulk_ok = [&](int64_t t) { return (t + 1) * (int64_t)tile + 8 <= nU; };
@@ -756,22 +775,27 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
     for (int g = 0; g < B::NSEG; ++g) {
       int es;
       int64_t e0;
-      B::seg(T, status, phin, avg_with, g, m0, es, e0);
+      B::seg(T, status, avg_with, g, m0, es, e0);
       const int ga = 16 / es;
       const int off = (int)(e0 & (ga - 1));
       bytes[g] = (uint32_t)(((off + tile + ga - 1) / ga) * ga * es);
       total += bytes[g];
     }
+    int64_t w0;
+    int wlen;
+    B::window(m0, tile, halo, nal, w0, wlen);
+    total += (uint32_t)wlen * 4u;
     mbar_arrive_expect_tx(&full[s], total);
 #pragma unroll
     for (int g = 0; g < B::NSEG; ++g) {
       int es;
       int64_t e0;
-      const char* base = B::seg(T, status, phin, avg_with, g, m0, es, e0);
+      const char* base = B::seg(T, status, avg_with, g, m0, es, e0);
       const int ga = 16 / es;
       const int64_t a0 = e0 & ~(int64_t)(ga - 1);
       bulk_copy_g2s(smem + (size_t)s * sb + B::slot_offset(tile, g), base + a0 * es, bytes[g], &full[s]);
     }
+    bulk_copy_g2s(smem + (size_t)s * sb + woff, phin + w0, (uint32_t)wlen * 4u, &full[s]);
   };
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
@@ -789,6 +813,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
     const int64_t m0 = t * (int64_t)tile;
     UniIdx<D> I[NPT];
     bool have[NPT];
+    UniVal<D> V[NPT];
     if (bulk_ok(t)) {  // the same for every thread of the CTA
       const bool landed = mbar_wait_bounded(&full[s], (uint32_t)((k / STAGES) & 1), wait_cycles);
       if (__syncthreads_or(!landed)) {
@@ -802,25 +827,37 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
         return;
       }
       const unsigned char* st = smem + (size_t)s * sb;
+      const float* win = reinterpret_cast<const float*>(st + woff);
+      int64_t w0;
+      int wlen;
+      B::window(m0, tile, halo, nal, w0, wlen);
+      const int wbase = (int)w0;
       auto word = [&](int g, int li) -> uint32_t {
         int es;
         int64_t e0;
-        B::seg(T, status, phin, avg_with, g, m0, es, e0);
+        B::seg(T, status, avg_with, g, m0, es, e0);
         return reinterpret_cast<const uint32_t*>(st + B::slot_offset(tile, g))[(int)(e0 & 3) + li];
+      };
+      // a value from the window when the index falls inside it, else from global memory
+      auto value = [&](int j) -> float {
+        const unsigned r = (unsigned)(j - wbase);
+        return r < (unsigned)wlen ? win[r] : __ldg(phin + j);
       };
 #pragma unroll
       for (int j = 0; j < NPT; ++j) {
         const int li = tid + j * blockDim.x;
-        I[j].n = (int)(m0 + li);
-        I[j].st = reinterpret_cast<const uint16_t*>(st)[(int)(m0 & 7) + li];
-        I[j].code = word(1, li) & 15u;
+        const int m = (int)(m0 + li);
+        V[j].n = m;
+        V[j].st = reinterpret_cast<const uint16_t*>(st)[(int)(m0 & 7) + li];
+        V[j].code = word(1, li) & 15u;
+        V[j].f0 = win[m - wbase];
+        V[j].avg = AVG ? __uint_as_float(word(2 + 4 * D, li)) : 0.0f;
+        const bool active = !(V[j].st & (ST_ANCHORED | ST_OUTSIDE | ST_FROZEN));
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) {
-          I[j].nb[dir] = (int32_t)word(2 + dir, li);
-          I[j].nb2[dir] = (int32_t)word(2 + 2 * D + dir, li);
+          V[j].v[dir] = active ? value((int32_t)word(2 + dir, li)) : 0.0f;
+          V[j].v2[dir] = active ? value((int32_t)word(2 + 2 * D + dir, li)) : 0.0f;
         }
-        I[j].f0 = __uint_as_float(word(2 + 4 * D, li));
-        I[j].avg = AVG ? __uint_as_float(word(3 + 4 * D, li)) : 0.0f;
         have[j] = true;
       }
     } else {
@@ -830,11 +867,10 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
         have[j] = m < nU;
         if (have[j]) uni_load<D, AVG>(T, nR, status, phin, avg_with, (int)m, I[j]);
       }
-    }
-    UniVal<D> V[NPT];
 #pragma unroll
-    for (int j = 0; j < NPT; ++j)
-      if (have[j]) uni_gather<D>(I[j], phin, V[j]);
+      for (int j = 0; j < NPT; ++j)
+        if (have[j]) uni_gather<D>(I[j], phin, V[j]);
+    }
 #pragma unroll
     for (int j = 0; j < NPT; ++j)
       if (have[j]) out[V[j].n] = uni_update<D, AVG>(T, s_near, V[j]);
@@ -1225,6 +1261,30 @@ static bool uniform_bulk_ok(const DTab32<D>& T, const uint16_t* status, const fl
   return al(status) && al(phin) && al(avg_with) && al(T.r_meta) && al(T.r_nbr) && al(T.r_nbr2);
 }
 
+// the bulk-copy uniform kernel with STAGES tiles in flight: shared memory per CTA and the full-wave grid
+// are set up again whenever the tile or the halo changes
+template <int D, bool AVG, int STAGES>
+static void bulk_launch(const DTab32<D>& T, const uint16_t* status, const float* s_near, const float* phin, float* out,
+                        const float* avg_with, int* err, long long wait_cycles, int halo, int tpb, int blocks, unsigned max_grid,
+                        cudaStream_t s) {
+  using B = UniBulk<D, AVG>;
+  const uint32_t smem = STAGES * B::stage_bytes(tpb, halo);
+  auto kern = k_reinit_uniform32_bulk<D, AVG, STAGES, 1>;
+  static uint32_t configured_smem = 0;
+  static int configured_tpb = 0, per_sm = 0;
+  if (configured_smem != smem || configured_tpb != tpb) {
+    // a failure here makes the launch below fail, which the caller's cudaGetLastError reports
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
+    configured_smem = smem;
+    configured_tpb = tpb;
+  }
+  const int full = device_sm_count() * (per_sm > 0 ? per_sm : 1);
+  const int gb = blocks > 0 ? std::min(blocks, full) : full;
+  const unsigned g = std::min<unsigned>((unsigned)gb, max_grid);
+  kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err, wait_cycles, halo);
+}
+
 template <int D, int OS, bool AVG>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
                          float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg, int* err) {
@@ -1244,22 +1304,13 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
     k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(T.nR - uni_end)), tpb, 0, s>>>(
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
   }
-  if (part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth == 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
-    using B = UniBulk<D, AVG>;
-    constexpr int STAGES = 3;
-    const uint32_t smem = STAGES * B::stage_bytes(tpb);
-    auto kern = k_reinit_uniform32_bulk<D, AVG, STAGES, 1>;
-    static int configured_tpb = 0, per_sm = 0;
-    if (configured_tpb != tpb) {
-      // a failure here makes the launch below fail, which the caller's cudaGetLastError reports
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tpb, smem);
-      configured_tpb = tpb;
-    }
-    const int full = device_sm_count() * (per_sm > 0 ? per_sm : 1);
-    const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
-    const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
-    kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err, cfg.wait_cycles > 0 ? cfg.wait_cycles : kFullWaitCycles);
+  if (part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth >= 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
+    const int halo = cfg.halo >= 0 ? (cfg.halo & ~3) : 512;
+    const long long wc = cfg.wait_cycles > 0 ? cfg.wait_cycles : kFullWaitCycles;
+    if (cfg.depth == 4)
+      bulk_launch<D, AVG, 3>(T, status, s_near, phin, out, avg_with, err, wc, halo, tpb, cfg.uniform_blocks, grid_of(uni_end), s);
+    else
+      bulk_launch<D, AVG, 2>(T, status, s_near, phin, out, avg_with, err, wc, halo, tpb, cfg.uniform_blocks, grid_of(uni_end), s);
   } else if (part == STAGE_PART_UNIFORM && uni_end > 0) {
     const int full = (cfg.depth == 2 ? gb_uni2 : gb_uni) * scale;
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;

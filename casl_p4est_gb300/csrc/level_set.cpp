@@ -598,7 +598,7 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   }
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
-  if (cfg.depth == 3) check_device_waits();
+  if (cfg.depth >= 3) check_device_waits();
 }
 
 template <int D>
@@ -717,11 +717,12 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
   }
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream, iter_lim.p));
   cuda_check(cudaGetLastError(), "reinitialize (batch)");
-  if (cfg.depth == 3) check_device_waits();
+  if (cfg.depth >= 3) check_device_waits();
 }
 
 // Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, pipeline
-// depth and grid of the persistent uniform kernel, grid of the persistent regular kernel), timing
+// depth and grid of the persistent uniform kernel, the phi window of its bulk-copy form, grid of the
+// persistent regular kernel), timing
 // `trials` iterations per candidate with CUDA events on the object's stream.
 template <int D>
 void LevelSet<D>::autotune(const double* phi, int trials) {
@@ -748,7 +749,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     float ms = 0;
     cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
     // a candidate whose bounded waits gave up left CTAs early: it only looks fast, so drop it
-    if (c.depth == 3 && take_device_wait_flag()) return 1e30f;
+    if (c.depth >= 3 && take_device_wait_flag()) return 1e30f;
     return ms;
   };
   const long long wait_cycles = cfg.wait_cycles;
@@ -761,7 +762,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     c.tpb = tpb;
     c.wait_cycles = wait_cycles;
     float c_ms = 1e30f;
-    for (int depth : {1, 2, 3})
+    for (int depth : {1, 2, 3, 4})
       for (int g : grids) {
         StageCfg t = c;
         t.depth = depth;
@@ -771,6 +772,16 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
           c_ms = ms;
           c.depth = depth;
           c.uniform_blocks = t.uniform_blocks;
+        }
+      }
+    if (c.depth >= 3)  // the phi window of the bulk-copy kernel
+      for (int halo : {128, 256, 1024, 2048}) {
+        StageCfg t = c;
+        t.halo = halo;
+        const float ms = run(t);
+        if (ms < c_ms) {
+          c_ms = ms;
+          c.halo = halo;
         }
       }
     for (int g : grids) {

@@ -16,6 +16,19 @@ namespace st64 {
 
 __device__ __forceinline__ bool is_zero(double v) { return fabs(v) < EPS; }  // check_if_zero, .h:186
 
+// x / y, bit for bit. When y is a normal power of two whose reciprocal 1/y is normal too (octree cell
+// sizes and their sums of equal halves are, for power-of-two tree sizes), x * (1/y) is exactly the real
+// number x / y, and IEEE multiplication and division round that same number the same way (subnormal,
+// infinite and zero results included), so one multiplication replaces the division sequence; GB300
+// issues FP64 at 2 operations per SM cycle, where a division takes about ten. Any other y is divided.
+__device__ __forceinline__ double qdiv(double x, double y) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;  // biased exponent
+  if ((b & 0x000fffffffffffffull) == 0 && e - 1u < 2045u)  // mantissa zero, e in [1, 2045]: 1/y = 2^(1023 - (e - 1023))
+    return __dmul_rn(x, __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046u - e) << 52))));
+  return x / y;
+}
+
 template <int D>
 __device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f) {
   constexpr int H = Dim<D>::HALF;
@@ -27,7 +40,7 @@ __device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, 
     const int32_t ik = T.nbr[base + k * N];
     if (ik >= 0) acc = acc + f[ik] * T.w[base + k * N];
   }
-  return acc / T.nrm[(int64_t)dir * N + n];
+  return qdiv(acc, T.nrm[(int64_t)dir * N + n]);
 }
 
 // correct_naive_second_derivatives (src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298), all branches.
@@ -125,7 +138,7 @@ __device__ __forceinline__ void laplace64(const DTab64<D>& T, int64_t n, const d
     const double fm = lin64<D>(T, 2 * a, n, f);
     const double fp = lin64<D>(T, 2 * a + 1, n, f);
     const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
-    Dv[a] = ((fp - f0) / dp + (fm - f0) / dm) * 2. / (dp + dm);
+    Dv[a] = qdiv((qdiv(fp - f0, dp) + qdiv(fm - f0, dm)) * 2., dp + dm);
   }
   const int32_t ci = T.cidx[n];
   if (ci >= 0) correct64<D>(T.crec + (int64_t)6 * ci, Dv);

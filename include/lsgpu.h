@@ -402,11 +402,12 @@ int lsg_batch_offsets(const lsg_level_set* batch, int64_t* offsets); /* count + 
  * replayed afterwards (make that first call outside any stream capture). */
 int lsg_batch_reinitialize(lsg_level_set* batch, double* phi, const int* iterations, int use_graph);
 int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const int* iterations, int use_graph);
-/* Launch shape of the mixed stage kernels, four ints: config[0] threads per block (32..256),
+/* Launch shape of the mixed stage kernels, five ints: config[0] threads per block (32..256),
  * config[1] grid of the persistent uniform-stencil kernel, config[2] grid of the persistent regular
  * kernel (0: one full wave), config[3] pipeline of the uniform kernel (1 or 2 nodes in flight per
- * thread, or 3: the nodes' table words bulk-copied into shared memory three tiles ahead; a bounded
- * wait of that kernel that gives up makes the call return LSG_ETIMEOUT).
+ * thread, or 3 / 4: the nodes' table words and a window of phi bulk-copied into shared memory two /
+ * three tiles ahead; a bounded wait of that kernel that gives up makes the call return LSG_ETIMEOUT),
+ * config[4] nodes on either side of a tile in that window (a multiple of 4 in 0..4096).
  * lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials` iterations
  * each, keeps the fastest and returns it in config (may be NULL). Results do not depend on the
  * shape. */

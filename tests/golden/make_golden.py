@@ -1,7 +1,7 @@
 """Generate the fixtures in this folder from the reference itself (run from the repository root, where the
 reference tree is present):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]   (default: every fixture)
 
 Each fixture holds small grids leaf by leaf (tree, level, logical corner), so Forest.set_leaves rebuilds them
 exactly, the input fields, and the outputs of the reference's own code (oracle/_ref, compiled from the
@@ -30,7 +30,7 @@ import casl_p4est_gb300 as G  # noqa: E402
 import oracle as O  # noqa: E402
 import ref as R  # noqa: E402
 from casl_p4est_gb300 import shapes  # noqa: E402
-from grids import brick_2d, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d  # noqa: E402
+from grids import brick_2d, brick_3d_odd, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d  # noqa: E402
 
 DBL_MAX = np.finfo(np.float64).max
 
@@ -120,11 +120,29 @@ def make_config1():
     print("circle2d_L4-9_config1", f.num_nodes, "nodes, band error", err, "=", err / dmin, "dx_min")
 
 
+def fixtures():
+    def circle():
+        f2 = circle_2d(3, 6)
+        make("circle2d_L3-6", f2, phi0_circle_2d(f2), circle_2d(3, 5, center=(0.05, -0.03)), circle_2d(3, 6, center=(0.02, 0.01)))
+
+    def flower():
+        f3 = flower_3d(2, 4)
+        make("flower3d_L2-4", f3, phi0_flower_3d(f3), flower_3d(2, 3), flower_3d(2, 5))
+
+    def brick():
+        fb = brick_2d(1, 5)
+        make("brick2d_3x2_L1-5", fb, fb.sample(shapes.sphere_scaled([0.3, 0.1], 0.6, 0.1, [0.2, 0.3])))
+
+    def brick_odd():
+        # tree sizes 1/3 x 0.3 x 0.25: neighbour distances that are not powers of two
+        fo = brick_3d_odd(1, 4)
+        make("brick3d_odd_L1-4", fo, fo.sample(shapes.sphere_scaled([0.5, 0.15, 0.25], 0.1, 0.1, [0.3, 0.1, 0.2])))
+
+    return {"circle2d_L3-6": circle, "flower3d_L2-4": flower, "brick2d_3x2_L1-5": brick, "brick3d_odd_L1-4": brick_odd,
+            "circle2d_L4-9_config1": make_config1}
+
+
 if __name__ == "__main__":
-    f2 = circle_2d(3, 6)
-    make("circle2d_L3-6", f2, phi0_circle_2d(f2), circle_2d(3, 5, center=(0.05, -0.03)), circle_2d(3, 6, center=(0.02, 0.01)))
-    f3 = flower_3d(2, 4)
-    make("flower3d_L2-4", f3, phi0_flower_3d(f3), flower_3d(2, 3), flower_3d(2, 5))
-    fb = brick_2d(1, 5)
-    make("brick2d_3x2_L1-5", fb, fb.sample(shapes.sphere_scaled([0.3, 0.1], 0.6, 0.1, [0.2, 0.3])))
-    make_config1()
+    todo = fixtures()
+    for name in (sys.argv[1:] or list(todo)):
+        todo[name]()

@@ -43,6 +43,22 @@ def brick_3d(lmin=1, lmax=5):
     return f
 
 
+def brick_2d_odd(lmin=1, lmax=6):
+    """3 x 2 trees of size 1/3 x 0.35: no cell size or neighbour distance is a power of two."""
+    f = G.my_p4est_brick_new([3, 2], [0, 0], [1, 0.7])
+    f.refine_levelset(shapes.sphere([0.45, 0.35], 0.2), lmin, lmax, lip=1.2)
+    f.build_nodes()
+    return f
+
+
+def brick_3d_odd(lmin=1, lmax=5):
+    """3 x 1 x 2 trees of size 1/3 x 0.3 x 0.25: x and y spacings are not powers of two, z spacings are."""
+    f = G.my_p4est_brick_new([3, 1, 2], [0, 0, 0], [1, 0.3, 0.5])
+    f.refine_levelset(shapes.sphere([0.5, 0.15, 0.25], 0.1), lmin, lmax, lip=1.2)
+    f.build_nodes()
+    return f
+
+
 def band_error(phi, exact, band):
     m = np.abs(phi) < band
     return float(np.max(np.abs(phi[m] - exact[m]))) if m.any() else 0.0

@@ -12,7 +12,8 @@ import pytest
 import casl_p4est_gb300 as G
 import oracle as O
 
-from grids import (band_error, brick_2d, brick_3d, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d)
+from grids import (band_error, brick_2d, brick_2d_odd, brick_3d, brick_3d_odd, circle_2d, flower_3d, phi0_circle_2d,
+                   phi0_flower_3d)
 
 pytestmark = pytest.mark.gpu
 
@@ -21,6 +22,9 @@ GRIDS = {
     "brick2d": (lambda: brick_2d(1, 7), lambda f: f.sample(G.shapes.sphere_scaled([0.3, 0.1], 0.6, 0.2, [0.5, 0.5]))),
     "flower3d": (lambda: flower_3d(3, 6), phi0_flower_3d),
     "brick3d": (lambda: brick_3d(1, 5), lambda f: f.sample(G.shapes.sphere_scaled([0.7, 0.5, 0.9], 0.3, 0.1, [1, 0.5, 1]))),
+    # tree sizes that are not powers of two: the FP64 kernels divide instead of multiplying by exact reciprocals
+    "brick2d_odd": (lambda: brick_2d_odd(1, 7), lambda f: f.sample(G.shapes.sphere_scaled([0.45, 0.35], 0.2, 0.1, [0.3, 0.2]))),
+    "brick3d_odd": (lambda: brick_3d_odd(1, 5), lambda f: f.sample(G.shapes.sphere_scaled([0.5, 0.15, 0.25], 0.1, 0.1, [0.3, 0.1, 0.2]))),
 }
 
 
@@ -173,20 +177,24 @@ def test_band_linf_device_matches_numpy():
     assert np.isnan(val)
 
 
-@pytest.mark.parametrize("shape", [(256, 0, 0, 1), (128, 912, 304, 2), (64, 152, 0, 2), (256, 0, 0, 3), (256, 4, 0, 3),
-                                   (32, 2, 304, 3), (128, 608, 0, 3)])
+@pytest.mark.parametrize("shape", [(256, 0, 0, 1, 512), (128, 912, 304, 2, 512), (64, 152, 0, 2, 512), (256, 0, 0, 3, 512),
+                                   (256, 4, 0, 3, 0), (32, 2, 304, 3, 128), (128, 608, 0, 3, 2048), (256, 0, 0, 4, 512),
+                                   (256, 4, 0, 4, 1024), (64, 3, 0, 4, 4096), (128, 0, 304, 4, 4)])
 @pytest.mark.parametrize("grid", ["flower3d", "circle2d"])
 def test_mixed_result_independent_of_launch_shape(shape, grid):
-    """The mixed stages are Jacobi updates: threads per block, persistent grids and the uniform kernel's
-    pipeline (depth 3: bulk-copied tiles; a grid of 2 or 4 CTAs makes every CTA cycle through its three
-    stages many times) change no bit of the result."""
+    """The mixed stages are Jacobi updates: threads per block, persistent grids, the uniform kernel's
+    pipeline (depth 3 / 4: bulk-copied tiles two / three ahead; a grid of 2 to 4 CTAs makes every CTA cycle
+    through its stages many times) and the phi window around each tile (halo 0 to 4096 nodes) change no
+    bit of the result."""
     f = flower_3d(3, 6) if grid == "flower3d" else circle_2d(3, 9)
     phi0 = phi0_flower_3d(f) if grid == "flower3d" else phi0_circle_2d(f)
     ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
     ref = phi0.copy()
     ls.reinitialize_2nd_order(ref, 7)
-    tpb, ub, rb, depth = shape
-    ls.stage_config = {"threads_per_block": tpb, "uniform_blocks": ub, "regular_blocks": rb, "uniform_depth": depth}
+    tpb, ub, rb, depth, halo = shape
+    ls.stage_config = {"threads_per_block": tpb, "uniform_blocks": ub, "regular_blocks": rb, "uniform_depth": depth,
+                       "window_halo": halo}
+    assert ls.stage_config["window_halo"] == halo
     got = phi0.copy()
     ls.reinitialize_2nd_order(got, 7)
     assert np.array_equal(got, ref)

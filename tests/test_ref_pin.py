@@ -16,7 +16,7 @@ import casl_p4est_gb300 as G
 import oracle as O
 import ref as R
 from casl_p4est_gb300 import shapes
-from grids import brick_2d, brick_3d, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d
+from grids import brick_2d, brick_2d_odd, brick_3d, brick_3d_odd, circle_2d, flower_3d, phi0_circle_2d, phi0_flower_3d
 
 pytestmark = pytest.mark.skipif(not R.available(), reason="the reference tree is not present on this machine")
 
@@ -33,6 +33,11 @@ def _grids():
     out.append(("brick2d_3x2_L1-5", f, f.sample(shapes.sphere_scaled([0.3, 0.1], 0.6, 0.1, [0.2, 0.3]))))
     f = brick_3d(1, 4)
     out.append(("brick3d_2x1x2_L1-4", f, f.sample(shapes.sphere_scaled([0.7, 0.5, 0.9], 0.3, 0.1, [0.2, 0.3, 0.1]))))
+    # trees whose sizes are not powers of two (every division stays a division)
+    f = brick_2d_odd(1, 5)
+    out.append(("brick2d_odd_L1-5", f, f.sample(shapes.sphere_scaled([0.45, 0.35], 0.2, 0.1, [0.3, 0.2]))))
+    f = brick_3d_odd(1, 4)
+    out.append(("brick3d_odd_L1-4", f, f.sample(shapes.sphere_scaled([0.5, 0.15, 0.25], 0.1, 0.1, [0.3, 0.1, 0.2]))))
     return out
 
 
