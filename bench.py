@@ -51,7 +51,20 @@ def parse():
                         "batch2d: 256 quadtrees reinitialised together (--steps timed batch calls)")
     p.add_argument("--batch", type=int, default=256, help="batch2d: number of quadtrees")
     p.add_argument("--large-levels", type=int, nargs=2, default=[6, 11], help="large3d: min and max level")
-    return p.parse_args()
+    p.add_argument("--stage-config", default=None,
+                   help="reinit3d: fixed launch shape of the mixed stage instead of the autotuner's, as five integers "
+                        "threads_per_block,uniform_blocks,regular_blocks,uniform_depth,window_halo (e.g. 256,0,0,3,512)")
+    args = p.parse_args()
+    if args.fp64_steps < 1:
+        p.error("--fp64-steps must be at least 1")
+    return args
+
+
+def parse_stage_config(text):
+    v = [int(x) for x in text.split(",")]
+    if len(v) != 5:
+        raise SystemExit("--stage-config takes five integers")
+    return {"threads_per_block": v[0], "uniform_blocks": v[1], "regular_blocks": v[2], "uniform_depth": v[3], "window_halo": v[4]}
 
 
 def build_grid(levels):
@@ -663,7 +676,11 @@ def main():
     ls = G.my_p4est_level_set_t(ngbd, precision="mixed", device_build=True)
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
-    stage_cfg = ls.autotune(phi0, trials=8)
+    if args.stage_config:
+        ls.stage_config = parse_stage_config(args.stage_config)
+        stage_cfg = dict(ls.stage_config, fixed=True)
+    else:
+        stage_cfg = ls.autotune(phi0, trials=8)
     setup_s = time.perf_counter() - t0
     _, dmin, _ = f.dxyz_min(args.levels[1])
 
