@@ -61,9 +61,9 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
 #pragma unroll
   for (int dir = 0; dir < 2 * D; ++dir) {
     fn[dir] = quad_nb64<D>(T, dir, n, phi0, Dv);
-    near = near || (p0 * fn[dir] < 0.0);
+    near = near || product_negative(p0, fn[dir]);
   }
-  uint16_t st = (p0 > 0.0) ? ST_POSITIVE : 0;
+  uint16_t st = positive(p0) ? ST_POSITIVE : 0;
   if (near) {
     st |= ST_NEAR;
     double s[2 * D];
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
     for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.d[(int64_t)dir * N + n];
 #pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
-      if (!(p0 * fn[dir] < 0.0)) continue;
+      if (!product_negative(p0, fn[dir])) continue;
       st |= (uint16_t)(1u << (ST_CUT_SHIFT + dir));
       const int axis = dir >> 1;
       if (dir & 1) {
@@ -158,26 +158,29 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
     if (ORDER_SPACE > 1) {
 #pragma unroll
       for (int a = 0; a < D; ++a) {
-        const double xm = minmod(xxnb[2 * a], xx0[a]);
+        const double xm = minmod_x(xxnb[2 * a], xx0[a]);
         gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
-        const double xp = minmod(xxnb[2 * a + 1], xx0[a]);
+        const double xp = minmod_x(xxnb[2 * a + 1], xx0[a]);
         gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
       }
     }
-    const double sgn = (p0 > 0.0 ? 1.0 : -1.0);
-    double dt = min2(s[0], s[1]);
-    dt = min3(dt, s[2], s[3]);
-    if (D == 3) dt = min3(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
+    // sgn = (p0 > 0 ? 1 : -1): the prep step stored p0 > 0 as ST_POSITIVE; sgn * g is +-g exactly, so the
+    // upwind tests are sign tests of g
+    const bool pos = (st & ST_POSITIVE) != 0;
+    const double sgn = pos ? 1.0 : -1.0;
+    double dt = min2x(s[0], s[1]);
+    dt = min3x(dt, s[2], s[3]);
+    if (D == 3) dt = min3x(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
     dt = qdiv(dt, (double)D);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      if (sgn * gp[a] > 0.0) gp[a] = 0.0;
-      if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+      if (pos ? positive(gp[a]) : negative(gp[a])) gp[a] = 0.0;  // sgn * gp > 0
+      if (pos ? negative(gm[a]) : positive(gm[a])) gm[a] = 0.0;  // sgn * gm < 0
     }
-    double h = max2(gp[0] * gp[0], gm[0] * gm[0]) + max2(gp[1] * gp[1], gm[1] * gm[1]);
-    if (D == 3) h = h + max2(gp[2 % D] * gp[2 % D], gm[2 % D] * gm[2 % D]);
+    double h = max2x(gp[0] * gp[0], gm[0] * gm[0]) + max2x(gp[1] * gp[1], gm[1] * gm[1]);
+    if (D == 3) h = h + max2x(gp[2 % D] * gp[2 % D], gm[2 % D] * gm[2 % D]);
     r = f0 - dt * sgn * (sqrt(h) - 1.);
-    if (p0 * r < 0.0) r *= -1.0;
+    if (product_negative(p0, r)) r *= -1.0;
   }
   if (AVG) r = .5 * (avg_with[n] + r);
   out[n] = r;
@@ -228,17 +231,18 @@ __global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const doubl
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    const double xm = minmod(xxnb[2 * a], xx0[a]);
+    const double xm = minmod_x(xxnb[2 * a], xx0[a]);
     gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
-    const double xp = minmod(xxnb[2 * a + 1], xx0[a]);
+    const double xp = minmod_x(xxnb[2 * a + 1], xx0[a]);
     gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
   }
   const double v = vn[n];
-  const double sgn = (v > 0.0 ? +1.0 : -1.0);
+  // sgn = (v > 0 ? 1 : -1); sgn * g is +-g exactly, so the upwind tests are sign tests of g
+  const bool pos = positive(v);
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    if (sgn * gp[a] > 0.0) gp[a] = 0.0;
-    if (sgn * gm[a] < 0.0) gm[a] = 0.0;
+    if (pos ? positive(gp[a]) : negative(gp[a])) gp[a] = 0.0;  // sgn * gp > 0
+    if (pos ? negative(gm[a]) : positive(gm[a])) gm[a] = 0.0;  // sgn * gm < 0
   }
   double h = (gp[0] * gp[0] + gm[0] * gm[0]) + (gp[1] * gp[1] + gm[1] * gm[1]);
   if (D == 3) h = h + (gp[2 % D] * gp[2 % D] + gm[2 % D] * gm[2 % D]);

@@ -968,20 +968,7 @@ __device__ __forceinline__ double rcp64(double x) {
   return fma(r, e, r);
 }
 
-// a * b < 0.0 with IEEE double semantics, decided from the bit patterns where that is exact: opposite
-// sign bits, both finite and normal, and exponents large enough that the product cannot round to
-// zero (|a b| >= 2^(ea+eb-2046) >= 2^-1074); every other case takes the FP64 product. GB300's FP64
-// rate makes the multiply and compare the cost of the near-interface test.
-__device__ __forceinline__ bool product_negative(double a, double b) {
-  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-  if ((ia ^ ib) >= 0) {
-    if (((ia >> 52) & 0x7ff) != 0x7ff && ((ib >> 52) & 0x7ff) != 0x7ff) return false;  // same signs, no NaN: a b >= 0
-    return a * b < 0.0;
-  }
-  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
-  if (ea > 0 && eb > 0 && ea < 0x7ff && eb < 0x7ff && ea + eb >= 972) return true;
-  return a * b < 0.0;
-}
+using st64::product_negative;
 
 __device__ __forceinline__ double level_size64(double tsize, int base, uint32_t code) {
   return __longlong_as_double(__double_as_longlong(tsize) - ((long long)(base + (int)code) << 52));
@@ -1074,8 +1061,9 @@ __device__ __forceinline__ double quad_nb_m64(const DTab32<D>& T, int64_t n, int
   return v;
 }
 
-// pass 1 (every node): anchoring, limits, sign and the sign test against phi_0's quadratic
-// neighbours; interface-adjacent nodes are appended to a list.
+// pass 1 (every node): anchoring, limits, sign and the sign test against each of phi_0's quadratic
+// neighbours; the cut directions go into the status word and interface-adjacent nodes are appended to a
+// list.
 template <int D>
 __global__ void __launch_bounds__(TPB) k_prep_classify(DTab32<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0_irr,
                                                        double zdt, double lim_lo, double lim_hi, uint16_t* __restrict__ status,
@@ -1091,8 +1079,14 @@ __global__ void __launch_bounds__(TPB) k_prep_classify(DTab32<D> T, const double
       st = ST_OUTSIDE;
     } else {
       st = (p0 > 0.0) ? ST_POSITIVE : 0;
+      uint32_t cut = 0;
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) near = near || product_negative(p0, quad_nb_m64<D>(T, n, dir, phi0, dd0_irr));
+      for (int dir = 0; dir < 2 * D; ++dir)
+        if (product_negative(p0, quad_nb_m64<D>(T, n, dir, phi0, dd0_irr))) cut |= 1u << dir;
+      if (cut) {
+        near = true;
+        st |= (uint16_t)(ST_NEAR | (cut << ST_CUT_SHIFT));
+      }
     }
     status[n] = st;
   }
@@ -1107,73 +1101,108 @@ __global__ void __launch_bounds__(TPB) k_prep_classify(DTab32<D> T, const double
   }
 }
 
-// pass 2 (interface-adjacent nodes): subcell distances (src/my_p4est_level_set.cpp:133-211)
+// grid distance of node n (device order) in direction dir: its level's cell size, or the table distance
+template <int D>
+__device__ __forceinline__ double grid_distance64(const DTab32<D>& T, int64_t n, int dir) {
+  if (n < T.nR) return level_size64(T.tsize64[dir >> 1], T.base, (T.r_meta[n] >> (4 * dir)) & 15u);
+  return T.i_d64[(int64_t)dir * T.nI + (n - T.nR)];
+}
+
+// subcell distance of node n in the cut direction dir (src/my_p4est_level_set.cpp:133-211)
+template <int D>
+__device__ double subcell_distance64(const DTab32<D>& T, const double* __restrict__ phi0, const double* __restrict__ dd0_irr,
+                                     int order_space, int64_t n, int dir) {
+  constexpr int H = Dim<D>::HALF;
+  const int axis = dir >> 1;
+  const double p0 = phi0[n];
+  const double s = grid_distance64<D>(T, n, dir);
+  const double fn = quad_nb_m64<D>(T, n, dir, phi0, dd0_irr);
+  double xx0 = 0.0, xx_nb = 0.0;
+  if (order_space > 1) {
+    xx0 = dd_axis64<D>(T, n, axis, phi0, dd0_irr);
+    // f_<dir>_linear of phi_0's second derivative along axis
+    if (n < T.nR) {
+      xx_nb = dd_axis64<D>(T, T.r_nbr[(int64_t)dir * T.nR + n], axis, phi0, dd0_irr);
+    } else {
+      const int64_t i = n - T.nR;
+      const int c = face_count(T.i_meta[i], dir);
+      const int64_t base = (int64_t)(dir * H) * T.nI + i;
+      if (c == 1) {
+        xx_nb = dd_axis64<D>(T, T.i_nbr[base], axis, phi0, dd0_irr);
+      } else {
+        for (int kk = 0; kk < c; ++kk)
+          xx_nb = fma(T.i_wf64[base + kk * T.nI], dd_axis64<D>(T, T.i_nbr[base + kk * T.nI], axis, phi0, dd0_irr), xx_nb);
+      }
+    }
+  }
+  if (dir & 1)
+    return order_space > 1 ? st64::interface_location_2nd(0.0, s, p0, fn, xx0, xx_nb) : st64::interface_location(0.0, s, p0, fn);
+  return order_space > 1 ? -st64::interface_location_2nd(-s, 0.0, fn, p0, xx_nb, xx0) : -st64::interface_location(-s, 0.0, fn, p0);
+}
+
+// pass 2 (interface-adjacent nodes): subcell distances. A warp takes 32 listed nodes, writes the grid
+// distance of every direction that is not cut, and deals the warp's cut (node, direction) pairs out to
+// its lanes, so each lane computes only cut directions and only the second derivatives along their axis
+// (a node has one or two cut directions of its 2D).
 template <int D>
 __global__ void __launch_bounds__(TPB) k_prep_subcell(DTab32<D> T, const double* __restrict__ phi0, const double* __restrict__ dd0_irr,
                                                       double zdt, int order_space, const int32_t* __restrict__ near_list,
-                                                      const unsigned* __restrict__ near_count, uint16_t* __restrict__ status,
+                                                      const unsigned* __restrict__ near_count, const uint16_t* __restrict__ status,
                                                       float* __restrict__ s_near) {
-  constexpr int H = Dim<D>::HALF;
+  constexpr unsigned FULL = 0xffffffffu;
   const int64_t N = T.N;
   const unsigned cnt = *near_count;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
-    const int64_t n = near_list[k];
-    const double p0 = phi0[n];
-    double s[2 * D], Dv[D];
+  const int lane = threadIdx.x & 31;
+  const unsigned warp = (unsigned)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const unsigned nwarps = (unsigned)((gridDim.x * blockDim.x) >> 5);
+  for (unsigned base = warp * 32u; base < cnt; base += nwarps * 32u) {  // the same trip count for every lane of the warp
+    const unsigned k = base + (unsigned)lane;
+    const bool valid = k < cnt;
+    const int n = valid ? near_list[k] : 0;
+    const uint32_t cut = valid ? ((uint32_t)status[n] >> ST_CUT_SHIFT) & ((1u << (2 * D)) - 1u) : 0u;
+    if (valid) {
 #pragma unroll
-    for (int a = 0; a < D; ++a) Dv[a] = dd_axis64<D>(T, n, a, phi0, dd0_irr);
-    if (n < T.nR) {
-      const uint32_t codes = T.r_meta[n];
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = level_size64(T.tsize64[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
-    } else {
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.i_d64[(int64_t)dir * T.nI + (n - T.nR)];
+      for (int dir = 0; dir < 2 * D; ++dir)
+        if (!((cut >> dir) & 1u)) s_near[(int64_t)dir * N + n] = (float)max2(grid_distance64<D>(T, n, dir), zdt);
     }
-    uint16_t st = ((p0 > 0.0) ? ST_POSITIVE : 0) | ST_NEAR;
+    // inclusive prefix sum of the lanes' cut counts
+    const unsigned c = (unsigned)__popc(cut);
+    unsigned incl = c;
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) {
-      const double fn = quad_nb_m64<D>(T, n, dir, phi0, dd0_irr);
-      if (!product_negative(p0, fn)) continue;
-      st |= (uint16_t)(1u << (ST_CUT_SHIFT + dir));
-      const int axis = dir >> 1;
-      double xx_nb = 0.0;
-      if (order_space > 1) {
-        // f_<dir>_linear of phi_0's second derivative along axis
-        if (n < T.nR) {
-          xx_nb = dd_axis64<D>(T, T.r_nbr[(int64_t)dir * T.nR + n], axis, phi0, dd0_irr);
-        } else {
-          const int64_t i = n - T.nR;
-          const uint32_t meta = T.i_meta[i];
-          const int c = face_count(meta, dir);
-          const int64_t base = (int64_t)(dir * H) * T.nI + i;
-          if (c == 1) {
-            xx_nb = dd_axis64<D>(T, T.i_nbr[base], axis, phi0, dd0_irr);
-          } else {
-            for (int kk = 0; kk < c; ++kk)
-              xx_nb = fma(T.i_wf64[base + kk * T.nI], dd_axis64<D>(T, T.i_nbr[base + kk * T.nI], axis, phi0, dd0_irr), xx_nb);
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned v = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const unsigned total = __shfl_sync(FULL, incl, 31);
+    for (unsigned t0 = 0; t0 < total; t0 += 32u) {  // warp-uniform
+      const unsigned t = t0 + (unsigned)lane;
+      // owner: the lowest lane whose inclusive count exceeds t
+      int pos = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const unsigned v = __shfl_sync(FULL, incl, pos + step - 1);
+        if (v <= t) pos += step;
+      }
+      const unsigned o_incl = __shfl_sync(FULL, incl, pos);
+      const uint32_t o_cut = __shfl_sync(FULL, cut, pos);
+      const int o_n = __shfl_sync(FULL, n, pos);
+      if (t < total) {
+        // the j-th cut direction of the owner, j counted from its first item
+        int j = (int)(t - (o_incl - (unsigned)__popc(o_cut)));
+        int dir = 0;
+#pragma unroll
+        for (int d = 0; d < 2 * D; ++d)
+          if ((o_cut >> d) & 1u) {
+            if (j == 0) dir = d;
+            --j;
           }
-        }
-      }
-      if (dir & 1) {
-        if (order_space > 1)
-          s[dir] = st64::interface_location_2nd(0.0, s[dir], p0, fn, Dv[axis], xx_nb);
-        else
-          s[dir] = st64::interface_location(0.0, s[dir], p0, fn);
-      } else {
-        if (order_space > 1)
-          s[dir] = -st64::interface_location_2nd(-s[dir], 0.0, fn, p0, xx_nb, Dv[axis]);
-        else
-          s[dir] = -st64::interface_location(-s[dir], 0.0, fn, p0);
+        const double sd = subcell_distance64<D>(T, phi0, dd0_irr, order_space, o_n, dir);
+        s_near[(int64_t)dir * N + o_n] = (float)max2(sd, zdt);
       }
     }
-#pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) s_near[(int64_t)dir * N + n] = (float)max2(s[dir], zdt);
-    status[n] = st;
   }
 }
 
-// conversions between node order (FP64, caller's arrays) and device order (FP32)
 __global__ void k_gather_f32(const double* __restrict__ src, const int32_t* __restrict__ perm, float* __restrict__ dst, int64_t n,
                              int64_t src_stride, int64_t dst_stride, int blocks) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -14,7 +14,55 @@
 namespace lsg {
 namespace st64 {
 
-__device__ __forceinline__ bool is_zero(double v) { return fabs(v) < EPS; }  // check_if_zero, .h:186
+// Comparisons of doubles decided on their bit patterns where that gives the IEEE answer for every input (other
+// inputs take the FP64 comparison). GB300 issues FP64 instructions, compares included, at 2 per SM cycle and
+// integer ones at 64, so these keep the FP64 pipe for arithmetic.
+constexpr unsigned long long kMag = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
+__device__ __forceinline__ unsigned long long bits_of(double v) { return (unsigned long long)__double_as_longlong(v); }
+// +0 .. +inf (no sign bit, not NaN): for these the integer order of the bit patterns is the numeric order
+__device__ __forceinline__ bool nonneg_num(unsigned long long b) { return b <= kInf; }
+__device__ __forceinline__ bool is_zero(double v) { return (bits_of(v) & kMag) < bits_of(EPS); }  // fabs(v) < EPS, check_if_zero .h:186
+__device__ __forceinline__ bool nonzero(double v) { return (bits_of(v) << 1) != 0; }             // v != 0.0 (NaN included)
+__device__ __forceinline__ bool positive(double v) { return bits_of(v) - 1ull < kInf; }          // v > 0.0
+__device__ __forceinline__ bool negative(double v) {                                              // v < 0.0
+  const unsigned long long b = bits_of(v);
+  return (b >> 63) && (b & kMag) - 1ull < kInf;
+}
+// max2 (src/casl_math.h: b < a ? a : b) and min2 / min3 (a < b ? ...), the same result for every input
+__device__ __forceinline__ bool less64(double a, double b) {
+  const unsigned long long ia = bits_of(a), ib = bits_of(b);
+  if (nonneg_num(ia) && nonneg_num(ib)) return ia < ib;
+  return a < b;
+}
+__device__ __forceinline__ double max2x(double a, double b) { return less64(b, a) ? a : b; }
+__device__ __forceinline__ double min2x(double a, double b) { return less64(a, b) ? a : b; }
+__device__ __forceinline__ double min3x(double a, double b, double c) { return less64(a, b) ? min2x(a, c) : min2x(b, c); }
+// MINMOD (src/casl_math.h:80-88: a b <= 0 ? 0 : (|a| < |b| ? a : b)). Both finite with opposite signs: the
+// product is <= 0. Same signs, both normal and ea + eb >= 972: |a b| >= 2^(ea+eb-2046) >= 2^-1074, so the
+// product is > 0 and the magnitudes order as their bit patterns. Anything else is decided in FP64.
+__device__ __forceinline__ double minmod_x(double a, double b) {
+  const unsigned long long ia = bits_of(a), ib = bits_of(b);
+  const unsigned ea = (unsigned)(ia >> 52) & 0x7ffu, eb = (unsigned)(ib >> 52) & 0x7ffu;
+  if (ea != 0x7ffu && eb != 0x7ffu) {
+    if ((ia ^ ib) >> 63) return 0.0;
+    if (ea > 0 && eb > 0 && ea + eb >= 972u) return (ia & kMag) < (ib & kMag) ? a : b;
+  }
+  return minmod(a, b);
+}
+// a * b < 0.0 with IEEE double semantics, decided from the bit patterns where that is exact: opposite
+// sign bits, both finite and normal, and exponents large enough that the product cannot round to
+// zero (|a b| >= 2^(ea+eb-2046) >= 2^-1074); same signs without NaN give a b >= 0; every other case takes
+// the FP64 product.
+__device__ __forceinline__ bool product_negative(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if ((ia ^ ib) >= 0) {
+    if (((ia >> 52) & 0x7ff) != 0x7ff && ((ib >> 52) & 0x7ff) != 0x7ff) return false;  // same signs, no NaN: a b >= 0
+    return a * b < 0.0;
+  }
+  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
+  if (ea > 0 && eb > 0 && ea < 0x7ff && eb < 0x7ff && ea + eb >= 972) return true;
+  return a * b < 0.0;
+}
 
 // x / y, bit for bit. When y is a normal power of two whose reciprocal 1/y is normal too (octree cell
 // sizes and their sums of equal halves are, for power-of-two tree sizes), x * (1/y) is exactly the real
@@ -157,10 +205,10 @@ __device__ __forceinline__ double quad_nb64(const DTab64<D>& T, int dir, int64_t
   const int axis = dir >> 1;
   if (D == 2) {
     const double q0 = T.q[(int64_t)dir * N + n];
-    if (q0 != 0.0) v = v - q0 * Dv[tan_axis(axis, 0)];
+    if (nonzero(q0)) v = v - q0 * Dv[tan_axis(axis, 0)];
   } else {
     const double q0 = T.q[(int64_t)(2 * dir) * N + n], q1 = T.q[(int64_t)(2 * dir + 1) * N + n];
-    if (q0 != 0.0 || q1 != 0.0) v = v - (q0 * Dv[tan_axis(axis, 0)] + q1 * Dv[tan_axis(axis, 1 % (D - 1))]);
+    if (nonzero(q0) || nonzero(q1)) v = v - (q0 * Dv[tan_axis(axis, 0)] + q1 * Dv[tan_axis(axis, 1 % (D - 1))]);
   }
   return v;
 }
@@ -175,8 +223,8 @@ __device__ inline double interface_location_2nd(double a, double b, double fa, d
   const double fxx = minmod(fxxa, fxxb);
   const double h = b - a;
   const double c2 = 0.5 * fxx;
-  const double c1 = (fb - fa) / h;
-  const double c0 = 0.5 * (fb + fa) - h * h / 8 * fxx;
+  const double c1 = qdiv(fb - fa, h);
+  const double c0 = 0.5 * (fb + fa) - qdiv(h * h, 8.0) * fxx;
   double x;
   if (fabs(c2) < EPS)
     x = -c0 / c1;
