@@ -52,8 +52,9 @@ def parse():
     p.add_argument("--batch", type=int, default=256, help="batch2d: number of quadtrees")
     p.add_argument("--large-levels", type=int, nargs=2, default=[6, 11], help="large3d: min and max level")
     p.add_argument("--stage-config", default=None,
-                   help="reinit3d: fixed launch shape of the mixed stage instead of the autotuner's, as five integers "
-                        "threads_per_block,uniform_blocks,regular_blocks,uniform_depth,window_halo (e.g. 256,0,0,3,512)")
+                   help="reinit3d, large3d: fixed launch shape of the mixed stage instead of the autotuner's, as five to seven "
+                        "integers threads_per_block,uniform_blocks,regular_blocks,uniform_depth,window_halo[,streams[,priority]] "
+                        "(e.g. 256,0,0,3,512 or 256,912,304,1,512,1)")
     args = p.parse_args()
     if args.fp64_steps < 1:
         p.error("--fp64-steps must be at least 1")
@@ -62,9 +63,10 @@ def parse():
 
 def parse_stage_config(text):
     v = [int(x) for x in text.split(",")]
-    if len(v) != 5:
-        raise SystemExit("--stage-config takes five integers")
-    return {"threads_per_block": v[0], "uniform_blocks": v[1], "regular_blocks": v[2], "uniform_depth": v[3], "window_halo": v[4]}
+    if len(v) not in (5, 6, 7):
+        raise SystemExit("--stage-config takes five to seven integers")
+    return {"threads_per_block": v[0], "uniform_blocks": v[1], "regular_blocks": v[2], "uniform_depth": v[3], "window_halo": v[4],
+            "streams": v[5] if len(v) > 5 else 2, "priority": v[6] if len(v) > 6 else 2}
 
 
 def build_grid(levels):
@@ -465,7 +467,11 @@ def run_large(args):
     stream = torch.cuda.current_stream()
     ls.set_stream(stream.cuda_stream)
     _, dmin, _ = f.dxyz_min(lmax)
-    cfg = ls.autotune(phi0, trials=2)
+    if args.stage_config:
+        ls.stage_config = parse_stage_config(args.stage_config)
+        cfg = dict(ls.stage_config, fixed=True)
+    else:
+        cfg = ls.autotune(phi0, trials=2)
     phi0_d = torch.from_numpy(phi0).cuda()
     del phi0
     phi_d = torch.empty_like(phi0_d)

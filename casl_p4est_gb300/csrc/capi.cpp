@@ -1160,6 +1160,8 @@ int lsg_level_set_autotune(lsg_level_set* ls, const double* phi, int trials, int
         config[2] = L.cfg.regular_blocks;
         config[3] = L.cfg.depth;
         config[4] = L.cfg.halo;
+        config[5] = L.cfg.streams;
+        config[6] = L.cfg.priority;
       }
     });
   });
@@ -1174,6 +1176,8 @@ int lsg_level_set_stage_config(const lsg_level_set* ls, int* config) {
     config[2] = c.regular_blocks;
     config[3] = c.depth;
     config[4] = c.halo;
+    config[5] = c.streams;
+    config[6] = c.priority;
   });
 }
 
@@ -1184,12 +1188,16 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
     need(config[3] >= 1 && config[3] <= 4, "pipeline depth must be 1, 2, 3 or 4");
     need(config[4] >= 0 && config[4] <= 4096 && config[4] % 4 == 0, "window halo must be a multiple of 4 in 0..4096");
+    need(config[5] == 1 || config[5] == 2, "streams must be 1 or 2");
+    need(config[6] >= 0 && config[6] <= 2, "priority must be 0, 1 or 2");
     with_ls(ls, [&](auto& L) {
       L.cfg.tpb = config[0];
       L.cfg.uniform_blocks = config[1];
       L.cfg.regular_blocks = config[2];
       L.cfg.depth = config[3];
       L.cfg.halo = config[4];
+      L.cfg.streams = config[5];
+      L.cfg.priority = config[6];
       L.drop_graph();
     });
   });

@@ -42,6 +42,17 @@ struct StageCfg {
   int depth = 1;
   // nodes on either side of a tile in the phi window of the bulk-copy kernel (a multiple of 4)
   int halo = 512;
+  // 2: the second derivatives and the irregular nodes on a side stream while the main stream runs the
+  // uniform nodes; 1: the four stage kernels one after another on the object's stream (on grids far larger
+  // than L2 the concurrent kernels evict each other's gathered lines)
+  int streams = 2;
+  // with two streams, which kernels the block scheduler prefers: 0 both streams at the default priority,
+  // 1 the side stream (second derivatives, irregular nodes) at the highest priority, 2 the uniform and
+  // other regular nodes on an internal stream at the highest priority. With 2 the persistent uniform
+  // kernel's blocks are resident from the start and the side stream's short blocks fill the rest; with
+  // equal priorities the side stream's many blocks can take the SMs first and the stage ran 15% slower
+  // on most calls (13.7M and 122M-node grids)
+  int priority = 2;
   // bound of the bulk kernel's waits for its copies, in SM clock cycles (0: about a second); a wait that
   // runs out makes the call report LSG_ETIMEOUT
   long long wait_cycles = 0;

@@ -305,10 +305,15 @@ LevelSet<D>::~LevelSet() {
   drop_graph();
   if (side_stream) {
     cudaStreamSynchronize(side_stream);
+    cudaStreamSynchronize(side_hi);
+    cudaStreamSynchronize(main_hi);
     cudaStreamDestroy(side_stream);
+    cudaStreamDestroy(side_hi);
+    cudaStreamDestroy(main_hi);
     cudaEventDestroy(ev_fork);
     cudaEventDestroy(ev_ddx);
     cudaEventDestroy(ev_join);
+    cudaEventDestroy(ev_main);
   }
   if (own_stream && stream) cudaStreamDestroy(stream);
   if (capture_stream) cudaStreamDestroy(capture_stream);
@@ -542,29 +547,52 @@ void LevelSet<D>::check_device_waits() {
 
 // One RK stage of the mixed path on two streams: the side stream computes the extended second
 // derivatives and then the irregular nodes while the main stream runs the uniform regular nodes;
-// the remaining regular nodes follow once the extended second derivatives are ready.
+// the remaining regular nodes follow once the extended second derivatives are ready. With one stream
+// (cfg.streams 1) the four kernels run one after another.
 template <int D>
 void LevelSet<D>::ensure_side_stream() {
   if (side_stream) return;
+  int least = 0, greatest = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
   cuda_check(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaStreamCreateWithPriority(&side_hi, cudaStreamNonBlocking, greatest), "cudaStreamCreateWithPriority");
+  cuda_check(cudaStreamCreateWithPriority(&main_hi, cudaStreamNonBlocking, greatest), "cudaStreamCreateWithPriority");
   cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_ddx, cudaEventDisableTiming), "cudaEventCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming), "cudaEventCreate");
 }
 
 template <int D>
 void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with) {
+  if (cfg.streams == 1) {
+    timer.begin(K_STAGE32, stream);
+    launch_dd_x32<D>(T32, phin, f_dd.p, stream, cfg.tpb);
+    launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
+    launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
+    launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
+    timer.end(stream);
+    timer.launches += 3;  // four kernels per stage
+    return;
+  }
   ensure_side_stream();
+  const cudaStream_t side = cfg.priority == 1 ? side_hi : side_stream;
+  const cudaStream_t main = cfg.priority == 2 ? main_hi : stream;
   timer.begin(K_STAGE32, stream);
   cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
-  cuda_check(cudaStreamWaitEvent(side_stream, ev_fork, 0), "cudaStreamWaitEvent");
-  launch_dd_x32<D>(T32, phin, f_dd.p, side_stream, cfg.tpb);
-  cuda_check(cudaEventRecord(ev_ddx, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side_stream, cfg, kerr.p);
-  cuda_check(cudaEventRecord(ev_join, side_stream), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
-  cuda_check(cudaStreamWaitEvent(stream, ev_ddx, 0), "cudaStreamWaitEvent");
-  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
+  cuda_check(cudaStreamWaitEvent(side, ev_fork, 0), "cudaStreamWaitEvent");
+  if (main != stream) cuda_check(cudaStreamWaitEvent(main, ev_fork, 0), "cudaStreamWaitEvent");
+  launch_dd_x32<D>(T32, phin, f_dd.p, side, cfg.tpb);
+  cuda_check(cudaEventRecord(ev_ddx, side), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side, cfg, kerr.p);
+  cuda_check(cudaEventRecord(ev_join, side), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, main, cfg, kerr.p);
+  cuda_check(cudaStreamWaitEvent(main, ev_ddx, 0), "cudaStreamWaitEvent");
+  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, main, cfg, kerr.p);
+  if (main != stream) {
+    cuda_check(cudaEventRecord(ev_main, main), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(stream, ev_main, 0), "cudaStreamWaitEvent");
+  }
   cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
   timer.end(stream);
   timer.launches += 3;  // four kernels per stage
@@ -722,7 +750,7 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
 
 // Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, pipeline
 // depth and grid of the persistent uniform kernel, the phi window of its bulk-copy form, grid of the
-// persistent regular kernel), timing
+// persistent regular kernel, one or two streams and their priorities), timing
 // `trials` iterations per candidate with CUDA events on the object's stream.
 template <int D>
 void LevelSet<D>::autotune(const double* phi, int trials) {
@@ -735,22 +763,27 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
   const int sms = device_sm_count();
   const bool timing = timer.enabled;
   timer.enabled = false;
+  // a candidate's time: the median of three timings of `trials` iterations (how the two streams' blocks
+  // share the SMs can differ from one run to the next, so a single timing can catch a lucky run)
   auto run = [&](const StageCfg& c) -> float {
     cfg = c;
     mixed_stage(2, f_phi.p, f_phi1.p, nullptr);  // warm-up
     mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
-    cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
-    for (int t = 0; t < trials; ++t) {
-      mixed_stage(2, f_phi.p, f_phi1.p, nullptr);
-      mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
+    float rep[3];
+    for (int k = 0; k < 3; ++k) {
+      cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
+      for (int t = 0; t < trials; ++t) {
+        mixed_stage(2, f_phi.p, f_phi1.p, nullptr);
+        mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
+      }
+      cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
+      cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+      cuda_check(cudaEventElapsedTime(&rep[k], e0, e1), "cudaEventElapsedTime");
     }
-    cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
-    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-    float ms = 0;
-    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
     // a candidate whose bounded waits gave up left CTAs early: it only looks fast, so drop it
     if (c.depth >= 3 && take_device_wait_flag()) return 1e30f;
-    return ms;
+    std::sort(rep, rep + 3);
+    return rep[1];
   };
   const long long wait_cycles = cfg.wait_cycles;
   StageCfg best;
@@ -794,6 +827,25 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
         c.regular_blocks = t.regular_blocks;
       }
     }
+    {  // the four kernels on one stream
+      StageCfg t = c;
+      t.streams = 1;
+      const float ms = run(t);
+      if (ms < c_ms) {
+        c_ms = ms;
+        c.streams = 1;
+      }
+    }
+    if (c.streams == 2)  // stream priorities (the candidates above ran with the default, 2)
+      for (int pr : {0, 1}) {
+        StageCfg t = c;
+        t.priority = pr;
+        const float ms = run(t);
+        if (ms < c_ms) {
+          c_ms = ms;
+          c.priority = pr;
+        }
+      }
     if (c_ms < best_ms) {
       best_ms = c_ms;
       best = c;

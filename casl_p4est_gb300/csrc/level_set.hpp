@@ -52,7 +52,8 @@ struct LevelSet {
   bool own_stream = false;
   KernelTimer timer;
   cudaStream_t side_stream = nullptr;  // second stream of the mixed stage (fork/join with events)
-  cudaEvent_t ev_fork = nullptr, ev_ddx = nullptr, ev_join = nullptr;
+  cudaStream_t side_hi = nullptr, main_hi = nullptr;  // the same at the highest stream priority (cfg.priority 1, 2)
+  cudaEvent_t ev_fork = nullptr, ev_ddx = nullptr, ev_join = nullptr, ev_main = nullptr;
   StageCfg cfg;                        // launch shape of the mixed stage kernels (see autotune)
   DevBuf<int> kerr;                    // set by a device-side wait that gave up (bulk-copy uniform kernel)
   int64_t num_corrections = 0;

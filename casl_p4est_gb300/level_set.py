@@ -369,25 +369,26 @@ class my_p4est_level_set_t:
 
 def _cfg_dict(cfg):
     return {"threads_per_block": int(cfg[0]), "uniform_blocks": int(cfg[1]), "regular_blocks": int(cfg[2]),
-            "uniform_depth": int(cfg[3]), "window_halo": int(cfg[4])}
+            "uniform_depth": int(cfg[3]), "window_halo": int(cfg[4]), "streams": int(cfg[5]),
+            "priority": int(cfg[6])}
 
 
 def _autotune(handle, phi, trials):
     phi = np.ascontiguousarray(phi, np.float64)
-    cfg = np.zeros(5, np.int32)
+    cfg = np.zeros(7, np.int32)
     L.check(L.load().lsg_level_set_autotune(handle, L.dptr(phi), int(trials), L.i32ptr(cfg)))
     return _cfg_dict(cfg)
 
 
 def _stage_config(handle):
-    cfg = np.zeros(5, np.int32)
+    cfg = np.zeros(7, np.int32)
     L.check(L.load().lsg_level_set_stage_config(handle, L.i32ptr(cfg)))
     return _cfg_dict(cfg)
 
 
 def _set_stage_config(handle, cfg):
     arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"], cfg.get("uniform_depth", 1),
-                    cfg.get("window_halo", 512)], np.int32)
+                    cfg.get("window_halo", 512), cfg.get("streams", 2), cfg.get("priority", 2)], np.int32)
     L.check(L.load().lsg_level_set_set_stage_config(handle, L.i32ptr(arr)))
 
 

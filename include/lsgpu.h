@@ -402,12 +402,15 @@ int lsg_batch_offsets(const lsg_level_set* batch, int64_t* offsets); /* count + 
  * replayed afterwards (make that first call outside any stream capture). */
 int lsg_batch_reinitialize(lsg_level_set* batch, double* phi, const int* iterations, int use_graph);
 int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const int* iterations, int use_graph);
-/* Launch shape of the mixed stage kernels, five ints: config[0] threads per block (32..256),
+/* Launch shape of the mixed stage kernels, seven ints: config[0] threads per block (32..256),
  * config[1] grid of the persistent uniform-stencil kernel, config[2] grid of the persistent regular
  * kernel (0: one full wave), config[3] pipeline of the uniform kernel (1 or 2 nodes in flight per
  * thread, or 3 / 4: the nodes' table words and a window of phi bulk-copied into shared memory two /
  * three tiles ahead; a bounded wait of that kernel that gives up makes the call return LSG_ETIMEOUT),
- * config[4] nodes on either side of a tile in that window (a multiple of 4 in 0..4096).
+ * config[4] nodes on either side of a tile in that window (a multiple of 4 in 0..4096), config[5] streams
+ * of a stage (2: second derivatives and irregular nodes beside the uniform nodes; 1: the four kernels one
+ * after another), config[6] with two streams the one the block scheduler prefers (0: neither, 1: the second
+ * derivatives and irregular nodes, 2: the uniform and other regular nodes).
  * lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials` iterations
  * each, keeps the fastest and returns it in config (may be NULL). Results do not depend on the
  * shape. */

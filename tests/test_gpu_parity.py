@@ -177,24 +177,28 @@ def test_band_linf_device_matches_numpy():
     assert np.isnan(val)
 
 
-@pytest.mark.parametrize("shape", [(256, 0, 0, 1, 512), (128, 912, 304, 2, 512), (64, 152, 0, 2, 512), (256, 0, 0, 3, 512),
-                                   (256, 4, 0, 3, 0), (32, 2, 304, 3, 128), (128, 608, 0, 3, 2048), (256, 0, 0, 4, 512),
-                                   (256, 4, 0, 4, 1024), (64, 3, 0, 4, 4096), (128, 0, 304, 4, 4)])
+@pytest.mark.parametrize("shape", [(256, 0, 0, 1, 512, 2), (128, 912, 304, 2, 512, 2), (64, 152, 0, 2, 512, 2), (256, 0, 0, 3, 512, 2),
+                                   (256, 4, 0, 3, 0, 2), (32, 2, 304, 3, 128, 2), (128, 608, 0, 3, 2048, 2), (256, 0, 0, 4, 512, 2),
+                                   (256, 4, 0, 4, 1024, 2), (64, 3, 0, 4, 4096, 2), (128, 0, 304, 4, 4, 2), (256, 0, 0, 1, 512, 1),
+                                   (128, 912, 304, 2, 512, 1), (256, 4, 0, 3, 256, 1), (128, 1216, 608, 1, 512, 2, 1),
+                                   (256, 0, 0, 3, 512, 2, 0), (128, 1216, 608, 1, 512, 2, 0)])
 @pytest.mark.parametrize("grid", ["flower3d", "circle2d"])
 def test_mixed_result_independent_of_launch_shape(shape, grid):
     """The mixed stages are Jacobi updates: threads per block, persistent grids, the uniform kernel's
     pipeline (depth 3 / 4: bulk-copied tiles two / three ahead; a grid of 2 to 4 CTAs makes every CTA cycle
-    through its stages many times) and the phi window around each tile (halo 0 to 4096 nodes) change no
-    bit of the result."""
+    through its stages many times), the phi window around each tile (halo 0 to 4096 nodes), one or two
+    streams per stage and their priorities change no bit of the result."""
     f = flower_3d(3, 6) if grid == "flower3d" else circle_2d(3, 9)
     phi0 = phi0_flower_3d(f) if grid == "flower3d" else phi0_circle_2d(f)
     ls = G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed")
     ref = phi0.copy()
     ls.reinitialize_2nd_order(ref, 7)
-    tpb, ub, rb, depth, halo = shape
+    tpb, ub, rb, depth, halo, streams = shape[:6]
+    priority = shape[6] if len(shape) > 6 else 2
     ls.stage_config = {"threads_per_block": tpb, "uniform_blocks": ub, "regular_blocks": rb, "uniform_depth": depth,
-                       "window_halo": halo}
-    assert ls.stage_config["window_halo"] == halo
+                       "window_halo": halo, "streams": streams, "priority": priority}
+    assert ls.stage_config["window_halo"] == halo and ls.stage_config["streams"] == streams
+    assert ls.stage_config["priority"] == priority
     got = phi0.copy()
     ls.reinitialize_2nd_order(got, 7)
     assert np.array_equal(got, ref)
