@@ -1189,7 +1189,7 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config[3] >= 1 && config[3] <= 4, "pipeline depth must be 1, 2, 3 or 4");
     need(config[4] >= 0 && config[4] <= 4096 && config[4] % 4 == 0, "window halo must be a multiple of 4 in 0..4096");
     need(config[5] == 1 || config[5] == 2, "streams must be 1 or 2");
-    need(config[6] >= 0 && config[6] <= 2, "priority must be 0, 1 or 2");
+    need(config[6] >= 0 && config[6] <= 4, "priority must be 0 .. 4");
     with_ls(ls, [&](auto& L) {
       L.cfg.tpb = config[0];
       L.cfg.uniform_blocks = config[1];

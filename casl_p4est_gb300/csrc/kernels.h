@@ -46,12 +46,13 @@ struct StageCfg {
   // uniform nodes; 1: the four stage kernels one after another on the object's stream (on grids far larger
   // than L2 the concurrent kernels evict each other's gathered lines)
   int streams = 2;
-  // with two streams, which kernels the block scheduler prefers: 0 both streams at the default priority,
-  // 1 the side stream (second derivatives, irregular nodes) at the highest priority, 2 the uniform and
-  // other regular nodes on an internal stream at the highest priority. With 2 the persistent uniform
-  // kernel's blocks are resident from the start and the side stream's short blocks fill the rest; with
-  // equal priorities the side stream's many blocks can take the SMs first and the stage ran 15% slower
-  // on most calls (13.7M and 122M-node grids)
+  // with two streams, how the kernels pair up and which chain the block scheduler prefers. Chain A runs the
+  // second derivatives, chain B the uniform nodes; then A runs the irregular and B the other regular nodes
+  // (0 both at the default priority, 1 A at the highest, 2 B at the highest), or A the other regular and B
+  // the irregular nodes (3 A at the highest, 4 B at the highest). With 2 the persistent uniform kernel's
+  // blocks are resident from the start and the short blocks of chain A fill the rest; with equal priorities
+  // A's many blocks can take the SMs first and the stage ran 15% slower on most calls (13.7M and 122M-node
+  // grids)
   int priority = 2;
   // bound of the bulk kernel's waits for its copies, in SM clock cycles (0: about a second); a wait that
   // runs out makes the call report LSG_ETIMEOUT

@@ -576,21 +576,26 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
     return;
   }
   ensure_side_stream();
-  const cudaStream_t side = cfg.priority == 1 ? side_hi : side_stream;
-  const cudaStream_t main = cfg.priority == 2 ? main_hi : stream;
+  // two chains: A = second derivatives then one of the two kernels that need them, B = the uniform nodes then
+  // the other one (which waits for A's second derivatives)
+  const bool swap = cfg.priority >= 3;  // A ends with the other regular nodes, B with the irregular ones
+  const cudaStream_t a = (cfg.priority == 1 || cfg.priority == 3) ? side_hi : side_stream;
+  const cudaStream_t b = (cfg.priority == 2 || cfg.priority == 4) ? main_hi : stream;
   timer.begin(K_STAGE32, stream);
   cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
-  cuda_check(cudaStreamWaitEvent(side, ev_fork, 0), "cudaStreamWaitEvent");
-  if (main != stream) cuda_check(cudaStreamWaitEvent(main, ev_fork, 0), "cudaStreamWaitEvent");
-  launch_dd_x32<D>(T32, phin, f_dd.p, side, cfg.tpb);
-  cuda_check(cudaEventRecord(ev_ddx, side), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, side, cfg, kerr.p);
-  cuda_check(cudaEventRecord(ev_join, side), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, main, cfg, kerr.p);
-  cuda_check(cudaStreamWaitEvent(main, ev_ddx, 0), "cudaStreamWaitEvent");
-  launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, main, cfg, kerr.p);
-  if (main != stream) {
-    cuda_check(cudaEventRecord(ev_main, main), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(a, ev_fork, 0), "cudaStreamWaitEvent");
+  if (b != stream) cuda_check(cudaStreamWaitEvent(b, ev_fork, 0), "cudaStreamWaitEvent");
+  launch_dd_x32<D>(T32, phin, f_dd.p, a, cfg.tpb);
+  cuda_check(cudaEventRecord(ev_ddx, a), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, swap ? STAGE_PART_REGULAR : STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, a,
+                          cfg, kerr.p);
+  cuda_check(cudaEventRecord(ev_join, a), "cudaEventRecord");
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b, cfg, kerr.p);
+  cuda_check(cudaStreamWaitEvent(b, ev_ddx, 0), "cudaStreamWaitEvent");
+  launch_reinit_part32<D>(T32, swap ? STAGE_PART_IRREGULAR : STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b,
+                          cfg, kerr.p);
+  if (b != stream) {
+    cuda_check(cudaEventRecord(ev_main, b), "cudaEventRecord");
     cuda_check(cudaStreamWaitEvent(stream, ev_main, 0), "cudaStreamWaitEvent");
   }
   cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
@@ -750,7 +755,7 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
 
 // Autotuner: coordinate search over the launch shape of the mixed stage (threads per block, pipeline
 // depth and grid of the persistent uniform kernel, the phi window of its bulk-copy form, grid of the
-// persistent regular kernel, one or two streams and their priorities), timing
+// persistent regular kernel, one or two streams), timing
 // `trials` iterations per candidate with CUDA events on the object's stream.
 template <int D>
 void LevelSet<D>::autotune(const double* phi, int trials) {
@@ -836,16 +841,9 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
         c.streams = 1;
       }
     }
-    if (c.streams == 2)  // stream priorities (the candidates above ran with the default, 2)
-      for (int pr : {0, 1}) {
-        StageCfg t = c;
-        t.priority = pr;
-        const float ms = run(t);
-        if (ms < c_ms) {
-          c_ms = ms;
-          c.priority = pr;
-        }
-      }
+    // The stream priority stays at its default (2): in whole 50-iteration calls it was the fastest setting on
+    // both grids measured and the only one whose calls all took the same time, while in short trials the
+    // other settings sometimes timed faster than they run.
     if (c_ms < best_ms) {
       best_ms = c_ms;
       best = c;

@@ -409,8 +409,10 @@ int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const i
  * three tiles ahead; a bounded wait of that kernel that gives up makes the call return LSG_ETIMEOUT),
  * config[4] nodes on either side of a tile in that window (a multiple of 4 in 0..4096), config[5] streams
  * of a stage (2: second derivatives and irregular nodes beside the uniform nodes; 1: the four kernels one
- * after another), config[6] with two streams the one the block scheduler prefers (0: neither, 1: the second
- * derivatives and irregular nodes, 2: the uniform and other regular nodes).
+ * after another), config[6] with two streams their pairing and the one the block scheduler prefers (0:
+ * second derivatives then irregular nodes beside uniform then other regular nodes, neither preferred; 1: the
+ * first chain preferred; 2: the second; 3 and 4: the same with the irregular and other regular nodes
+ * swapped between the chains, the first / second chain preferred).
  * lsg_level_set_autotune times candidate shapes on phi (host, node order) for `trials` iterations
  * each, keeps the fastest and returns it in config (may be NULL). Results do not depend on the
  * shape. */

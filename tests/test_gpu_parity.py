@@ -181,7 +181,8 @@ def test_band_linf_device_matches_numpy():
                                    (256, 4, 0, 3, 0, 2), (32, 2, 304, 3, 128, 2), (128, 608, 0, 3, 2048, 2), (256, 0, 0, 4, 512, 2),
                                    (256, 4, 0, 4, 1024, 2), (64, 3, 0, 4, 4096, 2), (128, 0, 304, 4, 4, 2), (256, 0, 0, 1, 512, 1),
                                    (128, 912, 304, 2, 512, 1), (256, 4, 0, 3, 256, 1), (128, 1216, 608, 1, 512, 2, 1),
-                                   (256, 0, 0, 3, 512, 2, 0), (128, 1216, 608, 1, 512, 2, 0)])
+                                   (256, 0, 0, 3, 512, 2, 0), (128, 1216, 608, 1, 512, 2, 0), (128, 912, 0, 1, 512, 2, 3),
+                                   (256, 0, 304, 2, 512, 2, 4), (64, 3, 0, 4, 256, 2, 3)])
 @pytest.mark.parametrize("grid", ["flower3d", "circle2d"])
 def test_mixed_result_independent_of_launch_shape(shape, grid):
     """The mixed stages are Jacobi updates: threads per block, persistent grids, the uniform kernel's
