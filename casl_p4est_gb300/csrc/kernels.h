@@ -134,6 +134,21 @@ struct DTab32 {
 // FP64 sweeps over the nodes [first, first + count) (count < 0: to the last node), by default all of them.
 template <int D>
 void launch_dd64(const DTab64<D>& T, const double* f, double* dd, cudaStream_t s, int64_t first = 0, int64_t count = -1);
+// The FP64 tables in stencil-pattern order (face-node counts, correction, walls; node order within a pattern):
+// perm (sorted index -> node), iperm and the permuted arrays (neighbour indices renumbered). keys, keys_out
+// and idx hold N entries each; temp holds sort64_temp_bytes(N) bytes.
+struct Tab64Out {
+  int32_t* nbr;
+  double *w, *nrm, *d, *q;
+  int32_t* cidx;
+  uint8_t* wall;
+};
+size_t sort64_temp_bytes(int64_t n);
+template <int D>
+cudaError_t launch_sort_tab64(const DTab64<D>& T, uint32_t* keys, uint32_t* keys_out, int32_t* idx, void* temp, size_t temp_bytes,
+                              int32_t* perm, int32_t* iperm, const Tab64Out& out, cudaStream_t s);
+void launch_gather_perm64(const double* src, const int32_t* perm, double* dst, int64_t n, cudaStream_t s);   // dst[i] = src[perm[i]]
+void launch_scatter_perm64(const double* src, const int32_t* perm, double* dst, int64_t n, cudaStream_t s);  // dst[perm[i]] = src[i]
 template <int D>
 void launch_reinit_prep64(const DTab64<D>& T, const double* phi0, const double* dd0, double zdt, double lim_lo, double lim_hi,
                           int order_space, uint16_t* status, double* s_near, cudaStream_t s, int64_t first = 0, int64_t count = -1);

@@ -12,6 +12,8 @@
 //   CFL of the CF overload                     src/my_p4est_level_set.cpp:745-783
 #include <algorithm>
 
+#include <cub/cub.cuh>
+
 #include "kernels.h"
 #include "stencil64.cuh"
 #include "tables.hpp"
@@ -932,7 +934,101 @@ void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_
   k_min_cfl<<<nblocks(n), TPB, 0, s>>>(smin, vn, n, (unsigned long long*)dt_out_dev);
 }
 
+// ---- FP64 tables in stencil-pattern order ---------------------------------------------------------------
+// The FP64 sweeps run one thread per node; in the reference's node order a warp mixes nodes with one face node
+// per direction and hanging ones (two or four, a division by a non-power-of-two d_m + d_p, a correction), and
+// GB300's FP64 pipe pays every divergent branch for the whole warp. Sorting the nodes by their stencil pattern
+// (face-node counts, correction, walls; node order within a pattern) gives warps one path. The tables are
+// copied in that order with neighbour indices renumbered; the per-node arithmetic is unchanged, so results
+// are bit for bit those of the node-ordered sweeps.
+namespace {
+template <int D>
+__global__ void k_pattern_key64(DTab64<D> T, uint32_t* __restrict__ key, int32_t* __restrict__ idx) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= T.N) return;
+  uint32_t k = 0;
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    int cnt = 0;
+#pragma unroll
+    for (int j = 0; j < H; ++j) cnt += T.nbr[(int64_t)(dir * H + j) * T.N + n] >= 0 ? 1 : 0;
+    k |= (uint32_t)(cnt > 0 ? cnt - 1 : 0) << (2 * dir);
+  }
+  if (T.cidx[n] >= 0) k |= 1u << 12;
+  k |= (uint32_t)T.wall[n] << 13;
+  key[n] = k;
+  idx[n] = (int32_t)n;
+}
+__global__ void k_inverse_perm(const int32_t* __restrict__ perm, int32_t* __restrict__ iperm, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) iperm[perm[i]] = (int32_t)i;
+}
+template <int D>
+__global__ void k_permute_tab64(DTab64<D> T, const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm, int32_t* __restrict__ nbr,
+                                double* __restrict__ w, double* __restrict__ nrm, double* __restrict__ d, double* __restrict__ q,
+                                int32_t* __restrict__ cidx, uint8_t* __restrict__ wall) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = T.N;
+  if (i >= N) return;
+  const int64_t n = perm[i];
+#pragma unroll
+  for (int sl = 0; sl < 2 * D * H; ++sl) {
+    const int32_t nb = T.nbr[(int64_t)sl * N + n];
+    nbr[(int64_t)sl * N + i] = nb >= 0 ? iperm[nb] : -1;
+    w[(int64_t)sl * N + i] = T.w[(int64_t)sl * N + n];
+  }
+#pragma unroll
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    nrm[(int64_t)dir * N + i] = T.nrm[(int64_t)dir * N + n];
+    d[(int64_t)dir * N + i] = T.d[(int64_t)dir * N + n];
+  }
+#pragma unroll
+  for (int j = 0; j < 2 * D * (D - 1); ++j) q[(int64_t)j * N + i] = T.q[(int64_t)j * N + n];
+  cidx[i] = T.cidx[n];
+  wall[i] = T.wall[n];
+}
+__global__ void k_gather_perm64(const double* __restrict__ src, const int32_t* __restrict__ perm, double* __restrict__ dst, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[perm[i]];
+}
+__global__ void k_scatter_perm64(const double* __restrict__ src, const int32_t* __restrict__ perm, double* __restrict__ dst, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[perm[i]] = src[i];
+}
+}  // namespace
+
+size_t sort64_temp_bytes(int64_t n) {
+  size_t bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int32_t*)nullptr, (int32_t*)nullptr,
+                                  (int)n, 0, 19);
+  return bytes;
+}
+
+template <int D>
+cudaError_t launch_sort_tab64(const DTab64<D>& T, uint32_t* keys, uint32_t* keys_out, int32_t* idx, void* temp, size_t temp_bytes,
+                              int32_t* perm, int32_t* iperm, const Tab64Out& out, cudaStream_t s) {
+  const int64_t N = T.N;
+  if (N == 0) return cudaSuccess;
+  k_pattern_key64<D><<<nblocks(N), TPB, 0, s>>>(T, keys, idx);
+  const cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, perm, (int)N, 0, 19, s);
+  if (e != cudaSuccess) return e;
+  k_inverse_perm<<<nblocks(N), TPB, 0, s>>>(perm, iperm, N);
+  k_permute_tab64<D><<<nblocks(N), TPB, 0, s>>>(T, perm, iperm, out.nbr, out.w, out.nrm, out.d, out.q, out.cidx, out.wall);
+  return cudaGetLastError();
+}
+
+void launch_gather_perm64(const double* src, const int32_t* perm, double* dst, int64_t n, cudaStream_t s) {
+  if (n) k_gather_perm64<<<nblocks(n), TPB, 0, s>>>(src, perm, dst, n);
+}
+void launch_scatter_perm64(const double* src, const int32_t* perm, double* dst, int64_t n, cudaStream_t s) {
+  if (n) k_scatter_perm64<<<nblocks(n), TPB, 0, s>>>(src, perm, dst, n);
+}
+
 #define LSG_INST(D)                                                                                                          \
+  template cudaError_t launch_sort_tab64<D>(const DTab64<D>&, uint32_t*, uint32_t*, int32_t*, void*, size_t, int32_t*, int32_t*, \
+                                            const Tab64Out&, cudaStream_t);                                                  \
   template void launch_dd64<D>(const DTab64<D>&, const double*, double*, cudaStream_t, int64_t, int64_t);                    \
   template void launch_iface_err64<D>(const DTab64<D>&, const double*, const double*, unsigned long long*, cudaStream_t);     \
   template void launch_reinit_prep64<D>(const DTab64<D>&, const double*, const double*, double, double, double, int, uint16_t*, \

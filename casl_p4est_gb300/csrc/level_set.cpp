@@ -369,27 +369,84 @@ void LevelSet<D>::reinitialize_fp64_noalloc(double* phi, int os, int ot, double 
 // reinitialize_within_range_of_phi_0 (src/my_p4est_level_set.cpp:290-557) on one device:
 // the ghost updates of a single process are no-ops and the layer/local split merges into one launch.
 template <int D>
-void LevelSet<D>::reinit_fp64(double* phi, int os, int ot, double hi, double lo, int iters, const double* mask) {
+bool LevelSet<D>::ensure_sorted64() {
+  if (sorted64_ready) return true;
+  if (sorted64_failed || N == 0) return false;
+  constexpr int NS = 2 * D * Dim<D>::HALF;
+  try {
+    s_perm.alloc(N);
+    s_iperm.alloc(N);
+    s_nbr.alloc((size_t)NS * N);
+    s_w.alloc((size_t)NS * N);
+    s_nrm.alloc((size_t)2 * D * N);
+    s_d.alloc((size_t)2 * D * N);
+    s_q.alloc((size_t)2 * D * (D - 1) * N);
+    s_cidx.alloc(N);
+    s_wall.alloc(N);
+    DevBuf<uint32_t> keys, keys_out;
+    DevBuf<int32_t> idx;
+    DevBuf<unsigned char> temp;
+    keys.alloc(N);
+    keys_out.alloc(N);
+    idx.alloc(N);
+    const size_t tb = sort64_temp_bytes(N);
+    temp.alloc(tb > 0 ? tb : 1);
+    const Tab64Out out{s_nbr.p, s_w.p, s_nrm.p, s_d.p, s_q.p, s_cidx.p, s_wall.p};
+    cuda_check(launch_sort_tab64<D>(T64, keys.p, keys_out.p, idx.p, temp.p, tb, s_perm.p, s_iperm.p, out, stream), "pattern sort");
+  } catch (const CudaOutOfMemory&) {
+    for (DevBuf<int32_t>* b : {&s_perm, &s_iperm, &s_nbr, &s_cidx}) b->release();
+    for (DevBuf<double>* b : {&s_w, &s_nrm, &s_d, &s_q}) b->release();
+    s_wall.release();
+    sorted64_failed = true;
+    return false;
+  }
+  T64s = T64;
+  T64s.nbr = s_nbr.p;
+  T64s.w = s_w.p;
+  T64s.nrm = s_nrm.p;
+  T64s.d = s_d.p;
+  T64s.q = s_q.p;
+  T64s.cidx = s_cidx.p;
+  T64s.wall = s_wall.p;
+  sorted64_ready = true;
+  return true;
+}
+
+// The FP64 reinitialisation: phi_0's second derivatives and the phi_0-only preparation once, then per
+// iteration the second-derivative and stage sweeps of each RK stage. The sweeps run on the tables in
+// stencil-pattern order (phi gathered into that order first and scattered back at the end) when those
+// could be built, else on the node-ordered tables; the results are the same bits either way.
+template <int D>
+void LevelSet<D>::reinit_fp64(double* phi_user, int os, int ot, double hi, double lo, int iters, const double* mask) {
   phi0.alloc(N);
   phi1.alloc(N);
   dd0.alloc((size_t)D * N);
   ddc.alloc((size_t)D * N);
   snear.alloc((size_t)2 * D * N);
   status.alloc(N);
+  const bool sorted = ensure_sorted64();
+  const DTab64<D>& T = sorted ? T64s : T64;
+  double* phi = phi_user;
+  if (sorted) {
+    s_phi.alloc(N);
+    phi = s_phi.p;
+    launch_gather_perm64(phi_user, s_perm.p, phi, N, stream);
+  }
   cuda_check(cudaMemcpyAsync(phi0.p, phi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_0");
-  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi0.p, dd0.p, stream));
-  LSG_LAUNCH(K_PREP64, launch_reinit_prep64<D>(T64, phi0.p, dd0.p, zdt, lo, hi, os, status.p, snear.p, stream));
-  if (mask) LSG_LAUNCH(K_PREP64, launch_apply_mask(mask, nullptr, status.p, N, stream));
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T, phi0.p, dd0.p, stream));
+  LSG_LAUNCH(K_PREP64, launch_reinit_prep64<D>(T, phi0.p, dd0.p, zdt, lo, hi, os, status.p, snear.p, stream));
+  if (mask) LSG_LAUNCH(K_PREP64, launch_apply_mask(mask, sorted ? s_perm.p : nullptr, status.p, N, stream));
   for (int it = 0; it < iters; ++it) {
-    LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, ddc.p, stream));
-    LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0.p, phi, ddc.p, phi1.p, nullptr, stream));
+    LSG_LAUNCH(K_DD64, launch_dd64<D>(T, phi, ddc.p, stream));
+    LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T, os, status.p, snear.p, phi0.p, phi, ddc.p, phi1.p, nullptr, stream));
     if (ot > 1) {
-      LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi1.p, ddc.p, stream));
-      LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T64, os, status.p, snear.p, phi0.p, phi1.p, ddc.p, phi, phi, stream));
+      LSG_LAUNCH(K_DD64, launch_dd64<D>(T, phi1.p, ddc.p, stream));
+      LSG_LAUNCH(K_STAGE64, launch_reinit_stage64<D>(T, os, status.p, snear.p, phi0.p, phi1.p, ddc.p, phi, phi, stream));
     } else {
       cuda_check(cudaMemcpyAsync(phi, phi1.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_np1");
     }
   }
+  if (sorted) launch_scatter_perm64(phi, s_perm.p, phi_user, N, stream);
   cuda_check(cudaGetLastError(), "reinitialize (fp64)");
 }
 

@@ -63,6 +63,14 @@ struct LevelSet {
   DevBuf<double> w, nrm, d, q, crec, smin;
   DevBuf<uint8_t> wall;
   DTab64<D> T64{};
+  // the FP64 tables in stencil-pattern order (launch_sort_tab64), built on the first FP64 reinitialisation;
+  // if device memory runs out the reinitialisation keeps the node-ordered tables
+  bool sorted64_ready = false, sorted64_failed = false;
+  DevBuf<int32_t> s_perm, s_iperm, s_nbr, s_cidx;
+  DevBuf<double> s_w, s_nrm, s_d, s_q, s_phi;
+  DevBuf<uint8_t> s_wall;
+  DTab64<D> T64s{};
+  bool ensure_sorted64();
   // mixed tables (built on first mixed call)
   bool mixed_ready = false;
   DevBuf<uint32_t> r_meta, i_meta, r_meta2, i_cls;
