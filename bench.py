@@ -259,8 +259,8 @@ def run_transport(args):
     f0.build_nodes()
     dmin = 1.0 / (1 << lmax)
     dt = dmin
-    results = {}
-    for prec in ("mixed", "fp64"):
+
+    def gpu_loop(prec, steps):
         f = f0.copy()
         phi_h = f.sample(sphere)
         vol0 = negative_volume(f, phi_h)
@@ -272,7 +272,7 @@ def run_transport(args):
         regrid_iters = 0
         torch.cuda.synchronize()
         t_all = time.perf_counter()
-        for step in range(args.steps):
+        for step in range(steps):
             t0 = time.perf_counter()
             sl = G.my_p4est_semi_lagrangian_t(f.copy(), ls, splitting=(lmin, lmax, 1.2))
             phi = sl.update_p4est(G.VortexVelocity(math.cos(math.pi * (t + 0.5 * dt) / T)), dt, phi)  # device fields
@@ -292,9 +292,36 @@ def run_transport(args):
             t += dt
         wall = time.perf_counter() - t_all
         phi = phi.cpu().numpy()
-        results[prec] = {"forest": f, "phi": phi, "ls": ls, "vol0": vol0, "vol": negative_volume(f, phi), "wall_s": wall,
-                         "times_s": times, "nodes_mean": float(np.mean(nodes)), "nodes_last": nodes[-1],
-                         "regrid_iterations": regrid_iters, "t_final": t}
+        return {"forest": f, "phi": phi, "ls": ls, "vol0": vol0, "vol": negative_volume(f, phi), "wall_s": wall,
+                "times_s": times, "nodes_mean": float(np.mean(nodes)), "nodes_last": nodes[-1],
+                "regrid_iterations": regrid_iters, "t_final": t}
+
+    def cpu_loop(steps, nthreads):
+        """The same steps on the host: the CPU restatement of the semi-Lagrangian step and of the
+        reinitialisation (oracle/) on all host cores, the regrid and node numbering by the host forest code,
+        the node-neighbour construction by the restatement."""
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        f = f0.copy()
+        phi = f.sample(sphere)
+        og = O.OracleGrid.from_forest(f)
+        t = 0.0
+        t_all = time.perf_counter()
+        for step in range(steps):
+            scale = math.cos(math.pi * (t + 0.5 * dt) / T)
+            g = f.copy()
+            while True:
+                new = og.sl_advect_vortex(g.node_xyz(), dt, scale, phi, nthreads=nthreads)
+                if not g.refine_and_coarsen(lmin, lmax, new, lip=1.2):
+                    break
+                g.build_nodes()
+            f, phi = g, new
+            og = O.OracleGrid.from_forest(f)
+            og.reinitialize(phi, 2, 2, iterations=5, nthreads=nthreads)
+            t += dt
+        return f, phi, time.perf_counter() - t_all
+
+    results = {prec: gpu_loop(prec, args.steps) for prec in ("mixed", "fp64")}
     m, d = results["mixed"], results["fp64"]
     # FP64 result on the mixed run's final nodes (quadratic node interpolation), compared in the band
     interp = G.my_p4est_interpolation_nodes_t(d["ls"])
@@ -319,6 +346,21 @@ def run_transport(args):
         "same_final_grid": bool(m["forest"].num_leaves == d["forest"].num_leaves
                                 and np.array_equal(m["forest"].leaves()[2], d["forest"].leaves()[2])),
     }
+    # CPU baseline: a bounded sample of the same steps on the host cores, and the FP64 GPU path over the same
+    # steps for comparison (the GPU evaluates the vortex velocity with its own sin/cos, so the two agree to
+    # rounding, not bit for bit)
+    k = min(args.steps, 10)
+    cores = os.cpu_count() or 1
+    f_cpu, phi_cpu, cpu_s = cpu_loop(k, cores)
+    ref = results["fp64"] if k == args.steps else gpu_loop("fp64", k)
+    same_grid = bool(f_cpu.num_leaves == ref["forest"].num_leaves and np.array_equal(f_cpu.leaves()[2], ref["forest"].leaves()[2]))
+    out["cpu_baseline"] = {"value": 1e3 * cpu_s / k, "unit": "ms/step", "cores": cores, "kind": "port",
+                           "sample": f"the first {k} steps of the same run on the host: the CPU restatement (oracle/) of the "
+                                     "semi-Lagrangian step, the node-neighbour construction and 5 reinitialisation iterations on "
+                                     f"{cores} threads, the regrid and node numbering by the host forest code"}
+    out["cpu_vs_gpu_fp64"] = {"steps": k, "same_grid": same_grid,
+                              "max_abs_diff": float(np.max(np.abs(phi_cpu - ref["phi"]))) if same_grid else None,
+                              "gpu_fp64_ms_per_step": 1e3 * ref["wall_s"] / k}
     print(json.dumps(out), flush=True)
 
 
