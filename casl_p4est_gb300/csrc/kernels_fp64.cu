@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
     double dt = min2x(s[0], s[1]);
     dt = min3x(dt, s[2], s[3]);
     if (D == 3) dt = min3x(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
-    dt = qdiv(dt, (double)D);
+    dt = D == 3 ? div3(dt) : qdiv(dt, (double)D);
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       if (pos ? positive(gp[a]) : negative(gp[a])) gp[a] = 0.0;  // sgn * gp > 0

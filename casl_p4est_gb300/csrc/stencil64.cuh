@@ -77,6 +77,16 @@ __device__ __forceinline__ double qdiv(double x, double y) {
   return x / y;
 }
 
+// x / 3 (the local pseudo-time step min(s) / P4EST_DIM of a 3D node), bit for bit. When x = +-2^k with x and
+// x/3 in the normal range, RN(x/3) = x * RN(1/3): scaling by a power of two commutes with rounding, so one
+// multiplication by the double nearest 1/3 (0x3FD5555555555555) replaces the division; any other x is divided.
+__device__ __forceinline__ double div3(double x) {
+  const unsigned long long b = bits_of(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if ((b & 0x000fffffffffffffull) == 0 && e > 2u && e < 2047u) return __dmul_rn(x, __longlong_as_double(0x3FD5555555555555ll));
+  return x / 3.0;
+}
+
 template <int D>
 __device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f) {
   constexpr int H = Dim<D>::HALF;
