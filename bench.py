@@ -463,7 +463,7 @@ def run_batch(args):
         mismatched += mis
     node_iters = N * iters
     out = {
-        "metric": "batched reinit node-iters/s (256 quadtrees, one CUDA graph)", "value": node_iters / (ms_graph / 1e3),
+        "metric": f"batched reinit node-iters/s ({b.count} quadtrees, one CUDA graph)", "value": node_iters / (ms_graph / 1e3),
         "unit": "node-iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_graph,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{b.count} quadtrees on [-1,1]^2, max level U{{6..11}}, union of 1-8 random ellipses, refined where "
