@@ -821,7 +821,7 @@ def main():
     traffic = tpn * N if tpn is not None else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "kernel": "one mixed RK stage: k_dd_x32 then k_reinit_fused32 (side stream) alongside k_reinit_uniform32 then "
-                          "k_reinit_fused_reg32 (main stream); second-derivative and stage sweeps of every node",
+                          "k_reinit_fused_reg32 (higher-priority stream); second-derivative and stage sweeps of every node",
                 "peak_source": peak_kind, "alg_bytes_per_node": alg[dom],
                 "dram_GBps": (traffic / (dom_ms / 1e3) / 1e9 if traffic is not None else None),
                 "dram_frac": (traffic / (dom_ms / 1e3) / 1e9 / peak if traffic is not None else None)}
