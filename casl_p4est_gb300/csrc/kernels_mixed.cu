@@ -687,12 +687,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-// false once `limit` SM cycles have passed without the phase completing (checked after every poll)
+// non-blocking test of the phase
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// false once `limit` SM cycles have passed without the phase completing: a non-blocking test first, then
+// suspending polls, the clock checked before each of them
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
+  if (mbar_test_wait(bar, parity)) return true;
+  for (;;) {
     if (clock64() - t0 > limit) return false;
-  return true;
+    if (mbar_try_wait(bar, parity)) return true;
+  }
 }
 constexpr long long kFullWaitCycles = 1ll << 31;  // about a second at the SM clock
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

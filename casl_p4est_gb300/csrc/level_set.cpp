@@ -623,6 +623,7 @@ void LevelSet<D>::ensure_side_stream() {
 template <int D>
 void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with) {
   if (cfg.streams == 1) {
+    mixed_join();
     timer.begin(K_STAGE32, stream);
     launch_dd_x32<D>(T32, phin, f_dd.p, stream, cfg.tpb);
     launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
@@ -638,10 +639,18 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
   const bool swap = cfg.priority >= 3;  // A ends with the other regular nodes, B with the irregular ones
   const cudaStream_t a = (cfg.priority == 1 || cfg.priority == 3) ? side_hi : side_stream;
   const cudaStream_t b = (cfg.priority == 2 || cfg.priority == 4) ? main_hi : stream;
+  if (chains_open && (timer.enabled || join_each_stage || a != chain_a || b != chain_b)) mixed_join();
   timer.begin(K_STAGE32, stream);
-  cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
-  cuda_check(cudaStreamWaitEvent(a, ev_fork, 0), "cudaStreamWaitEvent");
-  if (b != stream) cuda_check(cudaStreamWaitEvent(b, ev_fork, 0), "cudaStreamWaitEvent");
+  if (!chains_open) {
+    cuda_check(cudaEventRecord(ev_fork, stream), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(a, ev_fork, 0), "cudaStreamWaitEvent");
+    if (b != stream) cuda_check(cudaStreamWaitEvent(b, ev_fork, 0), "cudaStreamWaitEvent");
+  } else {
+    // the previous stage's other chain: every kernel of that stage has finished reading and writing before
+    // this stage's kernels start (chain order covers the rest)
+    cuda_check(cudaStreamWaitEvent(a, ev_main, 0), "cudaStreamWaitEvent");
+    cuda_check(cudaStreamWaitEvent(b, ev_join, 0), "cudaStreamWaitEvent");
+  }
   launch_dd_x32<D>(T32, phin, f_dd.p, a, cfg.tpb);
   cuda_check(cudaEventRecord(ev_ddx, a), "cudaEventRecord");
   launch_reinit_part32<D>(T32, swap ? STAGE_PART_REGULAR : STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, a,
@@ -651,13 +660,26 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
   cuda_check(cudaStreamWaitEvent(b, ev_ddx, 0), "cudaStreamWaitEvent");
   launch_reinit_part32<D>(T32, swap ? STAGE_PART_IRREGULAR : STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b,
                           cfg, kerr.p);
-  if (b != stream) {
-    cuda_check(cudaEventRecord(ev_main, b), "cudaEventRecord");
-    cuda_check(cudaStreamWaitEvent(stream, ev_main, 0), "cudaStreamWaitEvent");
-  }
-  cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
+  cuda_check(cudaEventRecord(ev_main, b), "cudaEventRecord");
+  chains_open = true;
+  chain_a = a;
+  chain_b = b;
+  // with the per-stage timer the caller's stream joins every stage (the timing brackets one stage), and so it
+  // does in a captured graph (a graph of per-stage forks and joins replayed faster than one of open chains:
+  // 18.7 against 19.5 ms on the 256-grid batch); otherwise the chains stay open into the next stage and
+  // mixed_join() closes them after the last one (34.6 against 34.8 ms on the 13.7M-node grid)
+  if (timer.enabled || join_each_stage) mixed_join();
   timer.end(stream);
   timer.launches += 3;  // four kernels per stage
+}
+
+// the caller's stream waits for both chains of the last mixed stage
+template <int D>
+void LevelSet<D>::mixed_join() {
+  if (!chains_open) return;
+  if (chain_b != stream) cuda_check(cudaStreamWaitEvent(stream, ev_main, 0), "cudaStreamWaitEvent");
+  cuda_check(cudaStreamWaitEvent(stream, ev_join, 0), "cudaStreamWaitEvent");
+  chains_open = false;
 }
 
 // Mixed precision: phi_n and all per-iteration work in FP32 (device node order); the phi_0-only
@@ -686,6 +708,7 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
       std::swap(f_phi.p, f_phi1.p);
     }
   }
+  mixed_join();
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
   if (cfg.depth >= 3) check_device_waits();
@@ -706,12 +729,14 @@ template <int D>
 void LevelSet<D>::mixed_loop(int os, int iters, const std::vector<int>& freeze_at) {
   for (int it = 0; it < iters; ++it) {
     if (std::binary_search(freeze_at.begin(), freeze_at.end(), it)) {
+      mixed_join();
       timer.launches += 1;
       launch_freeze32(iter_lim.p, it, status.p, N, stream);
     }
     mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
     mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
   }
+  mixed_join();
 }
 
 // phi_0-only preparation of a batched call (reinitialize_2nd_order: limits +-DBL_MAX, second order).
@@ -775,9 +800,12 @@ void LevelSet<D>::reinitialize_batch(double* phi, const int* iterations, bool us
       stream = capture_stream;
       cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
+        join_each_stage = true;
         try {
           mixed_loop(2, max_it, freeze_at);
+          join_each_stage = false;
         } catch (...) {
+          join_each_stage = false;
           cudaGraph_t g = nullptr;
           cudaStreamEndCapture(stream, &g);
           if (g) cudaGraphDestroy(g);
@@ -831,6 +859,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
     cfg = c;
     mixed_stage(2, f_phi.p, f_phi1.p, nullptr);  // warm-up
     mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
+    mixed_join();
     float rep[3];
     for (int k = 0; k < 3; ++k) {
       cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
@@ -838,6 +867,7 @@ void LevelSet<D>::autotune(const double* phi, int trials) {
         mixed_stage(2, f_phi.p, f_phi1.p, nullptr);
         mixed_stage(2, f_phi1.p, f_phi.p, f_phi.p);
       }
+      mixed_join();
       cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
       cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
       cuda_check(cudaEventElapsedTime(&rep[k], e0, e1), "cudaEventElapsedTime");

@@ -256,6 +256,11 @@ struct LevelSet {
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
+  void mixed_join();
+  // the two chains of the last mixed stage are still open (not yet joined into the caller's stream)
+  bool chains_open = false;
+  bool join_each_stage = false;  // set while a graph is captured
+  cudaStream_t chain_a = nullptr, chain_b = nullptr;
   // throws DeviceTimeout if a bounded device-side wait gave up since the last check (synchronises the
   // stream; skipped while the stream is being captured)
   void check_device_waits();
