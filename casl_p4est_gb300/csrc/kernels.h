@@ -271,11 +271,13 @@ void launch_freeze32(const uint16_t* lim, int it, uint16_t* status, int64_t n, c
 // uniform regular nodes (no dependence on ddx), other regular nodes and irregular nodes (both read ddx).
 enum { STAGE_PART_UNIFORM = 0, STAGE_PART_REGULAR = 1, STAGE_PART_IRREGULAR = 2 };
 // err: device word that a bounded wait of the bulk-copy uniform kernel (cfg.depth 3) sets when it
-// gives up (the kernel then stops; the host reads the word after the call)
+// gives up (the kernel then stops; the host reads the word after the call). With adv_vn the same kernels
+// run a stage of advect_in_normal_direction instead (normal velocity adv_vn, device order; time step
+// adv_dt; every node updated, upwinding by the sign of vn; status and s_near unused).
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
                           const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg,
-                          int* err);
+                          int* err, const float* adv_vn = nullptr, float adv_dt = 0.0f);
 template <int D>
 void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* ddq, const float* ddm, const float* vn, float dt,
                            float* out, const float* avg_with, cudaStream_t s);

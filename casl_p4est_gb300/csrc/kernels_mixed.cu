@@ -129,6 +129,26 @@ __device__ __forceinline__ float reinit_update(float f0, const float* fnb, const
   return r;
 }
 
+// advect_in_normal_direction_one_iteration's update after the neighbour values (src/my_p4est_level_set.cpp:559-654):
+// one-sided slopes with the minmod terms, upwinding by the sign of vn, phi - dt vn sqrt(sum gp^2 + gm^2)
+template <int D>
+__device__ __forceinline__ float advect_update(float f0, const float* fnb, const float* s, const float* xx0, const float* xxnb, float v,
+                                               float dt) {
+  const float sgn = v > 0.0f ? 1.0f : -1.0f;
+  float h = 0.0f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    float gp = __fdividef(fnb[2 * a + 1] - f0, s[2 * a + 1]);
+    float gm = __fdividef(f0 - fnb[2 * a], s[2 * a]);
+    gm = fmaf(0.5f * s[2 * a], minmodf(xxnb[2 * a], xx0[a]), gm);
+    gp = fmaf(-0.5f * s[2 * a + 1], minmodf(xxnb[2 * a + 1], xx0[a]), gp);
+    if (sgn * gp > 0.0f) gp = 0.0f;
+    if (sgn * gm < 0.0f) gm = 0.0f;
+    h += gp * gp + gm * gm;
+  }
+  return f0 - dt * v * sqrtf(h);
+}
+
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                         const float* __restrict__ s_near, const float* __restrict__ phin,
@@ -332,17 +352,18 @@ __global__ void __launch_bounds__(TPB) k_dd_x32(DTab32<D> T, const float* __rest
 // Irregular nodes [first, last) (first = nR). The loads that depend on nothing but the node (status,
 // class id, the first face node of every direction, its value and second derivatives) are issued together,
 // so the class record and the gathers wait for one round trip instead of three.
-template <int D, int ORDER_SPACE, bool AVG>
+template <int D, int ORDER_SPACE, bool AVG, bool ADV>
 __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                         const float* __restrict__ s_near, const float* __restrict__ phin,
                                                         const float* __restrict__ dd_irr, float* out, const float* avg_with,
-                                                        int64_t first, int64_t last) {
+                                                        int64_t first, int64_t last, const float* __restrict__ vn, float adv_dt) {
   constexpr int H = Dim<D>::HALF;
   const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
   if (n >= last) return;
   const int64_t i = n - T.nR;
-  const uint16_t st = __ldcs(status + n);
+  const uint16_t st = ADV ? (uint16_t)0 : __ldcs(status + n);
+  const float v = ADV ? __ldcs(vn + n) : 0.0f;
   const uint32_t ci = __ldcs(T.i_cls + i);
   int32_t j0[2 * D];
 #pragma unroll
@@ -400,7 +421,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
       }
     }
-    if (st & ST_NEAR) {
+    if (!ADV && (st & ST_NEAR)) {
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
         s[dir] = __ldg(s_near + (int64_t)dir * N + n);
@@ -418,7 +439,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         }
       }
     }
-    r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+    r = ADV ? advect_update<D>(f0, fnb, s, Dv, xxnb, v, adv_dt) : reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
   }
   if (AVG) r = 0.5f * (avg_with[n] + r);
   out[n] = r;
@@ -429,20 +450,21 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
 // and value. A face node's second derivative along its axis is a central difference of
 // (second neighbour, face node, this node) when the second neighbour is recorded; otherwise it is
 // read from the extended second-derivative set (k_dd_x32).
-template <int D, int ORDER_SPACE, bool AVG>
+template <int D, int ORDER_SPACE, bool AVG, bool ADV>
 __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                             const float* __restrict__ s_near, const float* __restrict__ phin,
                                                             const float* __restrict__ dd_irr, float* out, const float* avg_with,
-                                                            int first, int last) {
+                                                            int first, int last, const float* __restrict__ vn, float adv_dt) {
   const int nR = (int)T.nR;
   const int stride = gridDim.x * blockDim.x;
   int n = first + blockIdx.x * blockDim.x + threadIdx.x;
   uint16_t p_st = 0;
   uint32_t p_codes = 0, p_far = 0;
   int32_t p_nb[2 * D], p_nb2[2 * D];
-  float p_f0 = 0.0f, p_avg = 0.0f;
+  float p_f0 = 0.0f, p_avg = 0.0f, p_vn = 0.0f;
   auto prefetch = [&](int m) {
-    p_st = __ldcs(status + m);
+    p_st = ADV ? (uint16_t)0 : __ldcs(status + m);
+    if (ADV) p_vn = __ldcs(vn + m);
     p_codes = __ldcs(T.r_meta + m);
     p_far = __ldcs(T.r_meta2 + m);
 #pragma unroll
@@ -463,7 +485,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
       nb[dir] = p_nb[dir];
       nb2[dir] = p_nb2[dir];
     }
-    const float f0 = p_f0, avg = p_avg;
+    const float f0 = p_f0, avg = p_avg, v = p_vn;
     if (n + stride < last) prefetch(n + stride);
     float r;
     if (st & ST_ANCHORED) {
@@ -494,14 +516,14 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
           }
         }
       }
-      if (st & ST_NEAR) {
+      if (!ADV && (st & ST_NEAR)) {
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) {
           s[dir] = __ldg(s_near + (int64_t)dir * T.N + n);
           if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
         }
       }
-      r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+      r = ADV ? advect_update<D>(f0, fnb, s, Dv, xxnb, v, adv_dt) : reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
     }
     if (AVG) r = 0.5f * (avg + r);
     out[n] = r;
@@ -519,7 +541,7 @@ struct UniIdx {  // a node's own words and stencil indices
   int n;
   uint16_t st;
   uint32_t code;
-  float f0, avg;
+  float f0, avg, vn;
   int32_t nb[2 * D], nb2[2 * D];
 };
 template <int D>
@@ -527,15 +549,17 @@ struct UniVal {  // the same node with its face and second-neighbour values gath
   int n;
   uint16_t st;
   uint32_t code;
-  float f0, avg;
+  float f0, avg, vn;
   float v[2 * D], v2[2 * D];
 };
 
-template <int D, bool AVG>
+// ADV: the normal-advection stage (every node updated, upwinding by vn) instead of the reinitialisation stage
+template <int D, bool AVG, bool ADV>
 __device__ __forceinline__ void uni_load(const DTab32<D>& T, int nR, const uint16_t* __restrict__ status, const float* __restrict__ phin,
-                                         const float* avg_with, int m, UniIdx<D>& I) {
+                                         const float* avg_with, const float* __restrict__ vn, int m, UniIdx<D>& I) {
   I.n = m;
-  I.st = __ldcs(status + m);
+  I.st = ADV ? (uint16_t)0 : __ldcs(status + m);
+  I.vn = ADV ? __ldcs(vn + m) : 0.0f;
   I.code = __ldcs(T.r_meta + m) & 15u;
 #pragma unroll
   for (int dir = 0; dir < 2 * D; ++dir) {
@@ -553,6 +577,7 @@ __device__ __forceinline__ void uni_gather(const UniIdx<D>& I, const float* __re
   V.code = I.code;
   V.f0 = I.f0;
   V.avg = I.avg;
+  V.vn = I.vn;
   const bool active = !(I.st & (ST_ANCHORED | ST_OUTSIDE | ST_FROZEN));
 #pragma unroll
   for (int dir = 0; dir < 2 * D; ++dir) {
@@ -561,8 +586,8 @@ __device__ __forceinline__ void uni_gather(const UniIdx<D>& I, const float* __re
   }
 }
 
-template <int D, bool AVG>
-__device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __restrict__ s_near, const UniVal<D>& V) {
+template <int D, bool AVG, bool ADV>
+__device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __restrict__ s_near, const UniVal<D>& V, float adv_dt) {
   const uint16_t st = V.st;
   const float f0 = V.f0;
   float r;
@@ -572,8 +597,8 @@ __device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __r
     r = f0;
   } else {
     const int lvl = T.base + (int)V.code;
-    const bool near = (st & ST_NEAR) != 0;
-    const float sgn = (st & ST_POSITIVE) ? 1.0f : -1.0f;
+    const bool near = !ADV && (st & ST_NEAR) != 0;
+    const float sgn = ADV ? (V.vn > 0.0f ? 1.0f : -1.0f) : ((st & ST_POSITIVE) ? 1.0f : -1.0f);
     float smin = 3.0e38f, hsum = 0.0f;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
@@ -600,43 +625,47 @@ __device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __r
       }
       if (sgn * gp > 0.0f) gp = 0.0f;
       if (sgn * gm < 0.0f) gm = 0.0f;
-      hsum += fmaxf(gp * gp, gm * gm);
+      hsum += ADV ? gp * gp + gm * gm : fmaxf(gp * gp, gm * gm);
     }
-    r = f0 - smin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
-    if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
+    if (ADV) {
+      r = f0 - adv_dt * V.vn * sqrtf(hsum);
+    } else {
+      r = f0 - smin * (1.0f / D) * sgn * (sqrtf(hsum) - 1.0f);
+      if ((st & ST_POSITIVE) ? (r < 0.0f) : (r > 0.0f)) r = -r;
+    }
   }
   if (AVG) r = 0.5f * (V.avg + r);
   return r;
 }
 
-template <int D, bool AVG, int DEPTH>
+template <int D, bool AVG, int DEPTH, bool ADV>
 __global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                           const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                          float* out, const float* avg_with) {
+                                                          float* out, const float* avg_with, const float* __restrict__ vn, float adv_dt) {
   const int nR = (int)T.nR, nU = (int)T.nU;
   const int stride = gridDim.x * blockDim.x;
   int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nU) return;
   UniIdx<D> I;
-  uni_load<D, AVG>(T, nR, status, phin, avg_with, n, I);
+  uni_load<D, AVG, ADV>(T, nR, status, phin, avg_with, vn, n, I);
   if (DEPTH == 1) {
     for (; n < nU; n += stride) {
       UniVal<D> V;
       uni_gather<D>(I, phin, V);
-      if (n + stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + stride, I);
-      out[V.n] = uni_update<D, AVG>(T, s_near, V);
+      if (n + stride < nU) uni_load<D, AVG, ADV>(T, nR, status, phin, avg_with, vn, n + stride, I);
+      out[V.n] = uni_update<D, AVG, ADV>(T, s_near, V, adv_dt);
     }
   } else {
     UniVal<D> V;
     uni_gather<D>(I, phin, V);
-    if (n + stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + stride, I);
+    if (n + stride < nU) uni_load<D, AVG, ADV>(T, nR, status, phin, avg_with, vn, n + stride, I);
     for (; n < nU; n += stride) {
       // gathers of the next node and index loads of the one after are issued before this node's update
       UniVal<D> Vn;
       const bool more = n + stride < nU;
       if (more) uni_gather<D>(I, phin, Vn);
-      if (n + 2 * stride < nU) uni_load<D, AVG>(T, nR, status, phin, avg_with, n + 2 * stride, I);
-      out[V.n] = uni_update<D, AVG>(T, s_near, V);
+      if (n + 2 * stride < nU) uni_load<D, AVG, ADV>(T, nR, status, phin, avg_with, vn, n + 2 * stride, I);
+      out[V.n] = uni_update<D, AVG, ADV>(T, s_near, V, adv_dt);
       if (more) V = Vn;
     }
   }
@@ -867,6 +896,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
         V[j].code = word(1, li) & 15u;
         V[j].f0 = win[m - wbase];
         V[j].avg = AVG ? __uint_as_float(word(2 + 4 * D, li)) : 0.0f;
+        V[j].vn = 0.0f;
         const bool active = !(V[j].st & (ST_ANCHORED | ST_OUTSIDE | ST_FROZEN));
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) {
@@ -880,7 +910,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
       for (int j = 0; j < NPT; ++j) {
         const int64_t m = m0 + tid + j * blockDim.x;
         have[j] = m < nU;
-        if (have[j]) uni_load<D, AVG>(T, nR, status, phin, avg_with, (int)m, I[j]);
+        if (have[j]) uni_load<D, AVG, false>(T, nR, status, phin, avg_with, nullptr, (int)m, I[j]);
       }
 #pragma unroll
       for (int j = 0; j < NPT; ++j)
@@ -888,7 +918,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_uniform32_bulk(DTab32<D> T, cons
     }
 #pragma unroll
     for (int j = 0; j < NPT; ++j)
-      if (have[j]) out[V[j].n] = uni_update<D, AVG>(T, s_near, V[j]);
+      if (have[j]) out[V[j].n] = uni_update<D, AVG, false>(T, s_near, V[j], 0.0f);
     __syncthreads();  // every thread is done with stage s
     if (tid == 0) {
       const int64_t tn = tile_of(k + STAGES);
@@ -1329,26 +1359,27 @@ static void bulk_launch(const DTab32<D>& T, const uint16_t* status, const float*
   kern<<<g, tpb, smem, s>>>(T, status, s_near, phin, out, avg_with, err, wait_cycles, halo);
 }
 
-template <int D, int OS, bool AVG>
+template <int D, int OS, bool AVG, bool ADV>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
-                         float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg, int* err) {
+                         float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg, int* err, const float* vn, float adv_dt) {
   static int gb_reg = 0, gb_uni = 0, gb_uni2 = 0;
-  if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG>);
-  if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1>);
-  if (!gb_uni2) gb_uni2 = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 2>);
+  if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG, ADV>);
+  if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1, ADV>);
+  if (!gb_uni2) gb_uni2 = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 2, ADV>);
   const int tpb = (cfg.tpb > 0 && cfg.tpb <= TPB) ? cfg.tpb : TPB;
   // a persistent grid sized for TPB-thread blocks keeps the same thread count with smaller blocks
   const int scale = TPB / tpb;
   auto grid_of = [&](int64_t n) { return (unsigned)((n + tpb - 1) / tpb); };
   const int64_t uni_end = (OS > 1) ? T.nU : 0;  // the uniform kernel is second order in space only
   if (part == STAGE_PART_IRREGULAR && T.nI)
-    k_reinit_fused32<D, OS, AVG><<<grid_of(T.nI), tpb, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N);
+    k_reinit_fused32<D, OS, AVG, ADV><<<grid_of(T.nI), tpb, 0, s>>>(T, status, s_near, phin, ddx, out, avg_with, T.nR, T.N, vn, adv_dt);
   if (part == STAGE_PART_REGULAR && T.nR > uni_end) {
     const int gb = cfg.regular_blocks > 0 ? std::min(cfg.regular_blocks, gb_reg * scale) : gb_reg * scale;
-    k_reinit_fused_reg32<D, OS, AVG><<<(unsigned)std::min<int64_t>(gb, grid_of(T.nR - uni_end)), tpb, 0, s>>>(
-        T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR);
+    k_reinit_fused_reg32<D, OS, AVG, ADV><<<(unsigned)std::min<int64_t>(gb, grid_of(T.nR - uni_end)), tpb, 0, s>>>(
+        T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR, vn, adv_dt);
   }
-  if (part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth >= 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
+  // the bulk-copy uniform kernel serves the reinitialisation only; the advection stage uses the register pipeline
+  if (!ADV && part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth >= 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
     const int halo = cfg.halo >= 0 ? (cfg.halo & ~3) : 512;
     const long long wc = cfg.wait_cycles > 0 ? cfg.wait_cycles : kFullWaitCycles;
     if (cfg.depth == 4)
@@ -1360,23 +1391,26 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
     const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
     if (cfg.depth == 2)
-      k_reinit_uniform32<D, AVG, 2><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
+      k_reinit_uniform32<D, AVG, 2, ADV><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with, vn, adv_dt);
     else
-      k_reinit_uniform32<D, AVG, 1><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with);
+      k_reinit_uniform32<D, AVG, 1, ADV><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with, vn, adv_dt);
   }
 }
 
 template <int D>
 void launch_reinit_part32(const DTab32<D>& T, int part, int order_space, const uint16_t* status, const float* s_near,
                           const float* phin, const float* ddx, float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg,
-                          int* err) {
+                          int* err, const float* adv_vn, float adv_dt) {
   if (T.N == 0) return;
-  if (order_space > 1) {
-    if (avg_with) fused_launch<D, 2, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
-    else fused_launch<D, 2, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
+  if (adv_vn) {  // the normal-advection stage: second order in space, every node updated
+    if (avg_with) fused_launch<D, 2, true, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, adv_vn, adv_dt);
+    else fused_launch<D, 2, false, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, adv_vn, adv_dt);
+  } else if (order_space > 1) {
+    if (avg_with) fused_launch<D, 2, true, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, nullptr, 0.0f);
+    else fused_launch<D, 2, false, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, nullptr, 0.0f);
   } else {
-    if (avg_with) fused_launch<D, 1, true>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
-    else fused_launch<D, 1, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err);
+    if (avg_with) fused_launch<D, 1, true, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, nullptr, 0.0f);
+    else fused_launch<D, 1, false, false>(T, part, status, s_near, phin, ddx, out, avg_with, s, cfg, err, nullptr, 0.0f);
   }
 }
 
@@ -1409,7 +1443,7 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
                                          const float*, cudaStream_t);                                                           \
   template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t, int);                                  \
   template void launch_reinit_part32<D>(const DTab32<D>&, int, int, const uint16_t*, const float*, const float*, const float*,  \
-                                        float*, const float*, cudaStream_t, const StageCfg&, int*);
+                                        float*, const float*, cudaStream_t, const StageCfg&, int*, const float*, float);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST

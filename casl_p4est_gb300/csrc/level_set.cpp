@@ -621,14 +621,14 @@ void LevelSet<D>::ensure_side_stream() {
 }
 
 template <int D>
-void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with) {
+void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float* avg_with, const float* adv_vn, float adv_dt) {
   if (cfg.streams == 1) {
     mixed_join();
     timer.begin(K_STAGE32, stream);
     launch_dd_x32<D>(T32, phin, f_dd.p, stream, cfg.tpb);
-    launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
-    launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
-    launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p);
+    launch_reinit_part32<D>(T32, STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p, adv_vn, adv_dt);
+    launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p, adv_vn, adv_dt);
+    launch_reinit_part32<D>(T32, STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, stream, cfg, kerr.p, adv_vn, adv_dt);
     timer.end(stream);
     timer.launches += 3;  // four kernels per stage
     return;
@@ -654,12 +654,12 @@ void LevelSet<D>::mixed_stage(int os, const float* phin, float* out, const float
   launch_dd_x32<D>(T32, phin, f_dd.p, a, cfg.tpb);
   cuda_check(cudaEventRecord(ev_ddx, a), "cudaEventRecord");
   launch_reinit_part32<D>(T32, swap ? STAGE_PART_REGULAR : STAGE_PART_IRREGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, a,
-                          cfg, kerr.p);
+                          cfg, kerr.p, adv_vn, adv_dt);
   cuda_check(cudaEventRecord(ev_join, a), "cudaEventRecord");
-  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b, cfg, kerr.p);
+  launch_reinit_part32<D>(T32, STAGE_PART_UNIFORM, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b, cfg, kerr.p, adv_vn, adv_dt);
   cuda_check(cudaStreamWaitEvent(b, ev_ddx, 0), "cudaStreamWaitEvent");
   launch_reinit_part32<D>(T32, swap ? STAGE_PART_IRREGULAR : STAGE_PART_REGULAR, os, status.p, f_snear.p, phin, f_dd.p, out, avg_with, b,
-                          cfg, kerr.p);
+                          cfg, kerr.p, adv_vn, adv_dt);
   cuda_check(cudaEventRecord(ev_main, b), "cudaEventRecord");
   chains_open = true;
   chain_a = a;
@@ -981,6 +981,19 @@ void LevelSet<D>::advect_mixed(const double* vn, const double* vn_np1, double* p
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi0.p, N, 0, 0, 1, stream));
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(vn, perm.p, f_vn.p, N, 0, 0, 1, stream));
   if (vn_np1) LSG_LAUNCH(K_CONVERT, launch_gather_f32(vn_np1, perm.p, f_vn.p + N, N, 0, 0, 1, stream));
+  if (!phi_dd) {
+    // both RK stages on the reinitialisation's stage kernels (second derivatives rebuilt from second
+    // neighbours, the extended set by k_dd_x32, the two-stream schedule); with caller-given second derivatives
+    // (used in the minmod terms of the first stage and overwritten) the separate sweeps below run instead
+    status.ensure(N);  // the kernels' arguments; the advection stage reads neither
+    f_snear.ensure(1);
+    mixed_stage(2, f_phi0.p, f_phi.p, nullptr, f_vn.p, (float)dt);
+    mixed_stage(2, f_phi.p, f_phi1.p, f_phi0.p, vn_np1 ? f_vn.p + N : f_vn.p, (float)dt);
+    mixed_join();
+    LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi1.p, perm.p, nullptr, phi, N, 0, 0, 1, stream));
+    cuda_check(cudaGetLastError(), "advect_in_normal_direction (mixed)");
+    return;
+  }
   LSG_LAUNCH(K_DD32, launch_dd32<D>(T32, f_phi0.p, f_dd.p, stream));
   const float* ddm = f_dd.p;
   if (phi_dd) {

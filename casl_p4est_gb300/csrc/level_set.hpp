@@ -255,7 +255,8 @@ struct LevelSet {
   void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
-  void mixed_stage(int os, const float* phin, float* out, const float* avg_with);
+  // one RK stage on the mixed tables: the reinitialisation, or with adv_vn the normal advection
+  void mixed_stage(int os, const float* phin, float* out, const float* avg_with, const float* adv_vn = nullptr, float adv_dt = 0.0f);
   void mixed_join();
   // the two chains of the last mixed stage are still open (not yet joined into the caller's stream)
   bool chains_open = false;

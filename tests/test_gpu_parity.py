@@ -123,6 +123,45 @@ def test_mixed_advect_close_to_fp64(case):
     assert band_error(b, a, 3 * dmin) <= 1e-4 * dmin
 
 
+def test_mixed_advect_two_velocities_both_signs(case):
+    """The mixed normal advection runs on the reinitialisation's stage kernels (upwinding by the sign of vn):
+    speeds of both signs and a second velocity for the second RK stage, several steps, against the FP64 path."""
+    name, f, ls, og, phi0 = case
+    xyz = f.node_xyz()
+    vn = 0.8 * np.sin(4 * xyz[:, 0] + 1.0) * np.cos(3 * xyz[:, 1])
+    vn1 = vn + 0.3 * np.cos(2 * xyz[:, 0])
+    dt = 0.5 * og.advect_cfl_dt(np.maximum(np.abs(vn), np.abs(vn1)))
+    a = phi0.copy()
+    b = phi0.copy()
+    for _ in range(3):
+        ls.advect_in_normal_direction(vn, a, dt, vn_np1=vn1, precision="fp64")
+        ls.advect_in_normal_direction(vn, b, dt, vn_np1=vn1, precision="mixed")
+    lvl = f.leaves()[1].max()
+    _, dmin, _ = f.dxyz_min(int(lvl))
+    assert band_error(b, a, 3 * dmin) <= 1e-4 * dmin, (name, band_error(b, a, 3 * dmin) / dmin)
+
+
+def test_mixed_advect_launch_shapes_agree(case):
+    """The advection stage gives the same bits for every launch shape and stream schedule (Jacobi update)."""
+    name, f, ls, og, phi0 = case
+    xyz = f.node_xyz()
+    vn = 1.0 - 0.7 * np.cos(2 * xyz[:, 1])
+    dt = 0.5 * og.advect_cfl_dt(vn)
+    cfg = ls.stage_config
+    out = []
+    try:
+        for shape in ({"threads_per_block": 256, "uniform_blocks": 0, "regular_blocks": 0, "uniform_depth": 1, "streams": 2, "priority": 2},
+                      {"threads_per_block": 64, "uniform_blocks": 152, "regular_blocks": 304, "uniform_depth": 2, "streams": 1},
+                      {"threads_per_block": 128, "uniform_blocks": 0, "regular_blocks": 0, "uniform_depth": 3, "streams": 2, "priority": 0}):
+            ls.stage_config = shape
+            p = phi0.copy()
+            ls.advect_in_normal_direction(vn, p, dt, precision="mixed")
+            out.append(p)
+    finally:
+        ls.stage_config = cfg
+    assert all(np.array_equal(out[0], o) for o in out[1:])
+
+
 def test_device_resident_matches_host(case):
     torch = pytest.importorskip("torch")
     name, f, ls, og, phi0 = case
