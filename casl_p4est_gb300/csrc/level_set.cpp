@@ -687,6 +687,7 @@ void LevelSet<D>::mixed_join() {
 template <int D>
 void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters, const double* mask) {
   if (iters == 0) return;  // phi unchanged, as with no iteration in FP64
+  mixed_join();  // chains left open by a call that stopped on an error
   build_mixed();
   f_phi.alloc(N);
   f_phi1.alloc(N);
@@ -742,6 +743,7 @@ void LevelSet<D>::mixed_loop(int os, int iters, const std::vector<int>& freeze_a
 // phi_0-only preparation of a batched call (reinitialize_2nd_order: limits +-DBL_MAX, second order).
 template <int D>
 void LevelSet<D>::prep_batch(const double* phi) {
+  mixed_join();  // chains left open by a call that stopped on an error
   build_mixed();
   f_phi.alloc(N);
   f_phi1.alloc(N);
@@ -972,6 +974,7 @@ void LevelSet<D>::advect_normal(const double* vn, const double* vn_np1, double* 
 
 template <int D>
 void LevelSet<D>::advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd) {
+  mixed_join();  // chains left open by a call that stopped on an error
   build_mixed();
   f_phi.alloc(N);
   f_phi0.alloc(N);
