@@ -258,9 +258,6 @@ template <int D>
 void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const double* phi0, double zdt, double lim_lo, double lim_hi,
                               int order_space, double* phi0_dev, double* dd0_irr, uint16_t* status, float* s_near, int32_t* near_list,
                               unsigned* near_count, cudaStream_t s);
-template <int D>
-void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
-                           const float* dd, float* out, const float* avg_with, cudaStream_t s);
 // fused stage: second derivatives of face nodes rebuilt from recorded second neighbours, or read from
 // ddx (D x N, written by launch_dd_x32 for the same phi on the extended set)
 template <int D>

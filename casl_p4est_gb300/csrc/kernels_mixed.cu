@@ -149,99 +149,6 @@ __device__ __forceinline__ float advect_update(float f0, const float* fnb, const
   return f0 - dt * v * sqrtf(h);
 }
 
-template <int D, int ORDER_SPACE, bool AVG>
-__global__ void __launch_bounds__(TPB) k_reinit_stage32(DTab32<D> T, const uint16_t* __restrict__ status,
-                                                        const float* __restrict__ s_near, const float* __restrict__ phin,
-                                                        const float* __restrict__ dd, float* out, const float* avg_with) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t N = T.N;
-  if (n >= N) return;
-  const uint16_t st = __ldcs(status + n);
-  float r;
-  if (st & ST_ANCHORED) {
-    r = 0.0f;
-  } else if (st & (ST_OUTSIDE | ST_FROZEN)) {
-    r = phin[n];
-  } else {
-    const float f0 = __ldg(phin + n);
-    float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D];
-    // second derivatives at the node are recomputed from the gathered neighbours (same arithmetic
-    // as k_dd32) rather than re-read
-    if (n < T.nR) {
-      const Reg<D> R{__ldcs(T.r_meta + n)};
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        const int32_t nb = __ldcs(T.r_nbr + (int64_t)dir * T.nR + n);
-        fnb[dir] = __ldg(phin + nb);
-        if (ORDER_SPACE > 1) xxnb[dir] = __ldg(dd + (int64_t)(dir >> 1) * N + nb);
-        s[dir] = R.d(T, dir);
-      }
-#pragma unroll
-      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
-    } else {
-      const int64_t i = n - T.nR;
-      const uint32_t meta = __ldg(T.i_meta + i);
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        fnb[dir] = lin_irr<D>(T, meta, dir, i, phin);
-        if (ORDER_SPACE > 1) xxnb[dir] = lin_irr<D>(T, meta, dir, i, dd + (int64_t)(dir >> 1) * N);
-        s[dir] = __ldg(T.i_d + (int64_t)dir * T.nI + i);
-      }
-#pragma unroll
-      for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
-      correct_irr<D>(T, meta, i, Dv);
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        if (face_count(meta, dir) > 1) {
-#pragma unroll
-          for (int j = 0; j < D - 1; ++j)
-            fnb[dir] = fmaf(-__ldg(T.i_q + (int64_t)(dir * (D - 1) + j) * T.nI + i), Dv[tan_axis32(dir >> 1, j)], fnb[dir]);
-        }
-      }
-      const uint32_t wl = meta >> 24;
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        if (wl & (1u << (2 * a))) {
-          s[2 * a] = s[2 * a + 1];
-          fnb[2 * a] = fnb[2 * a + 1];
-          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
-        }
-        if (wl & (1u << (2 * a + 1))) {
-          s[2 * a + 1] = s[2 * a];
-          fnb[2 * a + 1] = fnb[2 * a];
-          Dv[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0f;
-        }
-      }
-    }
-    if (st & ST_NEAR) {
-      // the subcell distances replace s everywhere (clamped), cut neighbours are set to 0; a wall
-      // direction mirrors the clamped value of its opposite direction (wall step comes after)
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        s[dir] = __ldg(s_near + (int64_t)dir * N + n);
-        if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
-      }
-      if (n >= T.nR) {
-        const uint32_t wl = __ldg(T.i_meta + (n - T.nR)) >> 24;
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          if (wl & (1u << (2 * a))) {
-            s[2 * a] = s[2 * a + 1];
-            fnb[2 * a] = fnb[2 * a + 1];
-          }
-          if (wl & (1u << (2 * a + 1))) {
-            s[2 * a + 1] = s[2 * a];
-            fnb[2 * a + 1] = fnb[2 * a];
-          }
-        }
-      }
-    }
-    r = reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
-  }
-  if (AVG) r = 0.5f * (avg_with[n] + r);
-  out[n] = r;
-}
-
 // ---- fused reinitialisation stage ----------------------------------------------------------------
 // One stage of reinitialize_one_iteration per node without a separate second-derivative sweep: the
 // second derivatives of the face nodes along their axis are recomputed from phi here (regular face
@@ -1288,23 +1195,6 @@ void launch_reinit_prep_mixed(const DTab32<D>& T, const int32_t* perm, const dou
   k_prep_subcell<D><<<(unsigned)device_sm_count() * 8u, TPB, 0, s>>>(T, phi0_dev, dd0_irr, zdt, order_space, near_list, near_count, status, s_near);
 }
 
-template <int D>
-void launch_reinit_stage32(const DTab32<D>& T, int order_space, const uint16_t* status, const float* s_near, const float* phin,
-                           const float* dd, float* out, const float* avg_with, cudaStream_t s) {
-  if (T.N == 0) return;
-  const unsigned g = nblocks(T.N);
-  if (order_space > 1) {
-    if (avg_with)
-      k_reinit_stage32<D, 2, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd, out, avg_with);
-    else
-      k_reinit_stage32<D, 2, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd, out, avg_with);
-  } else {
-    if (avg_with)
-      k_reinit_stage32<D, 1, true><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd, out, avg_with);
-    else
-      k_reinit_stage32<D, 1, false><<<g, TPB, 0, s>>>(T, status, s_near, phin, dd, out, avg_with);
-  }
-}
 
 template <int D>
 void launch_dd_x32(const DTab32<D>& T, const float* f, float* ddx, cudaStream_t s, int tpb) {
@@ -1437,8 +1327,6 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
   template void launch_dd32<D>(const DTab32<D>&, const float*, float*, cudaStream_t);                                           \
   template void launch_reinit_prep_mixed<D>(const DTab32<D>&, const int32_t*, const double*, double, double, double, int,       \
                                             double*, double*, uint16_t*, float*, int32_t*, unsigned*, cudaStream_t);            \
-  template void launch_reinit_stage32<D>(const DTab32<D>&, int, const uint16_t*, const float*, const float*, const float*,      \
-                                         float*, const float*, cudaStream_t);                                                   \
   template void launch_advect_stage32<D>(const DTab32<D>&, const float*, const float*, const float*, const float*, float, float*, \
                                          const float*, cudaStream_t);                                                           \
   template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t, int);                                  \
