@@ -372,6 +372,10 @@ template <int D>
 bool LevelSet<D>::ensure_sorted64() {
   if (sorted64_ready) return true;
   if (sorted64_failed || N == 0) return false;
+  // LSGPU_FP64_NODE_ORDER=1 keeps the FP64 sweeps on the node-ordered tables (the layout they fall back to when
+  // the sorted copy does not fit), so that path can be exercised without running out of memory
+  const char* node_order = std::getenv("LSGPU_FP64_NODE_ORDER");
+  if (node_order && node_order[0] == '1') return false;
   constexpr int NS = 2 * D * Dim<D>::HALF;
   try {
     s_perm.alloc(N);
@@ -958,17 +962,49 @@ void LevelSet<D>::advect_normal(const double* vn, const double* vn_np1, double* 
   phi0.alloc(N);
   phi1.alloc(N);
   ddc.alloc((size_t)D * N);
+  // the sweeps run on the tables in stencil-pattern order when those exist (phi, the velocities and the given
+  // second derivatives gathered into that order, phi and the derivatives scattered back), else on the
+  // node-ordered tables; the same bits either way
+  const bool sorted = ensure_sorted64();
+  const DTab64<D>& T = sorted ? T64s : T64;
+  double* phi_u = phi;
+  double* dd_u = phi_dd;
+  if (sorted) {
+    // own buffers: the host entry point passes its staging buffers (ws_vn, ws_dd) in
+    s_phi.alloc(N);
+    s_vn.alloc(N);
+    launch_gather_perm64(phi_u, s_perm.p, s_phi.p, N, stream);
+    launch_gather_perm64(vn, s_perm.p, s_vn.p, N, stream);
+    phi = s_phi.p;
+    vn = s_vn.p;
+    if (vn_np1) {
+      s_vn1.alloc(N);
+      launch_gather_perm64(vn_np1, s_perm.p, s_vn1.p, N, stream);
+      vn_np1 = s_vn1.p;
+    }
+    if (phi_dd) {
+      s_dd.alloc((size_t)D * N);
+      for (int a = 0; a < D; ++a) launch_gather_perm64(dd_u + (int64_t)a * N, s_perm.p, s_dd.p + (int64_t)a * N, N, stream);
+      phi_dd = s_dd.p;
+    }
+  }
   // stage 1: the quadratic neighbours use laplace(phi) (computed inline by the reference); the
   // minmod terms use the given second derivatives, or the same laplace(phi) when none are given.
-  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, ddc.p, stream));
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T, phi, ddc.p, stream));
   const double* ddm = phi_dd ? phi_dd : ddc.p;
   cuda_check(cudaMemcpyAsync(phi0.p, phi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi_n");
-  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T64, phi0.p, ddc.p, ddm, vn, dt, phi, nullptr, stream));
+  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T, phi0.p, ddc.p, ddm, vn, dt, phi, nullptr, stream));
   // stage 2 with the derivatives of the intermediate phi (written to the caller's arrays if given)
   double* dd2 = phi_dd ? phi_dd : ddc.p;
-  LSG_LAUNCH(K_DD64, launch_dd64<D>(T64, phi, dd2, stream));
-  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T64, phi, dd2, dd2, vn_np1 ? vn_np1 : vn, dt, phi1.p, phi0.p, stream));
-  cuda_check(cudaMemcpyAsync(phi, phi1.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi");
+  LSG_LAUNCH(K_DD64, launch_dd64<D>(T, phi, dd2, stream));
+  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T, phi, dd2, dd2, vn_np1 ? vn_np1 : vn, dt, phi1.p, phi0.p, stream));
+  if (sorted) {
+    launch_scatter_perm64(phi1.p, s_perm.p, phi_u, N, stream);
+    if (dd_u)
+      for (int a = 0; a < D; ++a) launch_scatter_perm64(phi_dd + (int64_t)a * N, s_perm.p, dd_u + (int64_t)a * N, N, stream);
+  } else {
+    cuda_check(cudaMemcpyAsync(phi, phi1.p, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy phi");
+  }
   cuda_check(cudaGetLastError(), "advect_in_normal_direction");
 }
 

@@ -96,6 +96,32 @@ def test_advect_fp64_bitwise(case):
     assert np.array_equal(dd_a, dd_b)
 
 
+def test_fp64_node_order_fallback_bitwise(case, monkeypatch):
+    """The FP64 sweeps on the node-ordered tables (their layout when the copy sorted by stencil pattern does not
+    fit in memory) give the same bits as the sorted ones and the oracle."""
+    name, f, ls, og, phi0 = case
+    monkeypatch.setenv("LSGPU_FP64_NODE_ORDER", "1")
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    ngbd.init_neighbors()
+    ls_node = G.my_p4est_level_set_t(ngbd)
+    a = phi0.copy()
+    b = phi0.copy()
+    ls_node.reinitialize_2nd_order(a, 4, precision="fp64")
+    og.reinitialize(b, 2, 2, iterations=4)
+    assert np.array_equal(a, b)
+    xyz = f.node_xyz()
+    vn = 1.0 + 0.5 * np.sin(3 * xyz[:, 0]) * np.cos(2 * xyz[:, 1])
+    dt = og.advect_cfl_dt(vn)
+    dd_a = ls_node.compute_derivatives(phi0)
+    dd_b = dd_a.copy()
+    a = phi0.copy()
+    b = phi0.copy()
+    ls_node.advect_in_normal_direction(vn, a, dt, phi_xx=dd_a, vn_np1=0.5 * vn, precision="fp64")
+    og.advect_in_normal_direction(vn, b, dt, vn_np1=0.5 * vn, phi_dd=dd_b)
+    assert np.array_equal(a, b)
+    assert np.array_equal(dd_a, dd_b)
+
+
 def test_mixed_band_error_vs_fp64(case):
     name, f, ls, og, phi0 = case
     a = phi0.copy()
