@@ -110,7 +110,8 @@ def profile_traffic_per_node(kernel):
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+              "clocks.mem,clocks.max.mem,temperature.gpu")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
@@ -139,7 +140,7 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.t.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, reasons, mem, mmax, temp = [], [], set(), [], [], []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -153,9 +154,41 @@ class ClockSampler:
             for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
+            try:
+                mem.append(float(parts[9]))
+                mmax.append(float(parts[10]))
+                temp.append(float(parts[11]))
+            except (IndexError, ValueError):
+                pass
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+        if mem:
+            out.update(mem_mhz=statistics.median(mem), mem_max_mhz=max(mmax), temp_c=max(temp))
+        return out
+
+
+def box_copy_bandwidth(stream):
+    """Device-to-device copy bandwidth of this GPU (1 GiB, read + written bytes per second), beside the pool's
+    measured peak: GPUs of the same kind differ by several percent, and so do the memory-bound kernels on them."""
+    import torch
+    n = 1 << 28
+    x = torch.empty(n, dtype=torch.float32, device="cuda")
+    y = torch.empty_like(x)
+    x.fill_(1.0)
+    for _ in range(3):
+        y.copy_(x)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(10):
+        y.copy_(x)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gbs = 10 * 2 * x.numel() * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del x, y
+    return gbs
 
 
 def cpu_reinit_sample(f, phi0, iters, nthreads):
@@ -828,6 +861,8 @@ def main():
     iter_bytes = 2 * (dd_sweep + stage_sweep) + 3 * 4  # 284 B per node-iteration
     roofline["per_iteration"] = {"alg_bytes_per_node_iter": iter_bytes, "achieved_GBps": iter_bytes * value / world / 1e9,
                                  "frac": iter_bytes * value / world / 1e9 / peak}
+    box_bw = box_copy_bandwidth(stream)
+    roofline["frac_of_box_copy"] = achieved / box_bw
 
     # end to end through the public host API: pinned host phi, H2D + reinit + D2H per step
     host = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
@@ -880,7 +915,7 @@ def main():
             "fp64_vs_oracle_full_grid": parity,
             "fp64_vs_cpu_same_precision": (value64 / cpu["value"] if cpu else None),
             "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
-            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "setup_s": setup_s,
+            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "box_copy_GBps": box_bw, "setup_s": setup_s,
             "autotuned_stage_config": stage_cfg, "mixed_tables": ls.table_stats(),
         }
         print(json.dumps(out), flush=True)

@@ -1186,7 +1186,7 @@ int lsg_level_set_set_stage_config(lsg_level_set* ls, const int* config) {
     need(config != nullptr, "null config");
     need(config[0] == 32 || config[0] == 64 || config[0] == 128 || config[0] == 256, "threads per block must be 32, 64, 128 or 256");
     need(config[1] >= 0 && config[2] >= 0, "grid sizes must be >= 0 (0: one full wave)");
-    need(config[3] >= 1 && config[3] <= 4, "pipeline depth must be 1, 2, 3 or 4");
+    need(config[3] >= 1 && config[3] <= 5, "uniform kernel variant (pipeline depth) must be 1 to 5");
     need(config[4] >= 0 && config[4] <= 4096 && config[4] % 4 == 0, "window halo must be a multiple of 4 in 0..4096");
     need(config[5] == 1 || config[5] == 2, "streams must be 1 or 2");
     need(config[6] >= 0 && config[6] <= 4, "priority must be 0 .. 4");

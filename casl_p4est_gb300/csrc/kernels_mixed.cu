@@ -545,8 +545,10 @@ __device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __r
   return r;
 }
 
-template <int D, bool AVG, int DEPTH, bool ADV>
-__global__ void __launch_bounds__(TPB) k_reinit_uniform32(DTab32<D> T, const uint16_t* __restrict__ status,
+// MINB > 1 caps the registers so that MINB blocks of TPB threads fit on an SM (6: 40 registers, a few of the
+// node's words spill to L1): more of the uniform kernel's warps stay resident beside the side stream's kernels.
+template <int D, bool AVG, int DEPTH, bool ADV, int MINB = 1>
+__global__ void __launch_bounds__(TPB, MINB) k_reinit_uniform32(DTab32<D> T, const uint16_t* __restrict__ status,
                                                           const float* __restrict__ s_near, const float* __restrict__ phin,
                                                           float* out, const float* avg_with, const float* __restrict__ vn, float adv_dt) {
   const int nR = (int)T.nR, nU = (int)T.nU;
@@ -1252,10 +1254,11 @@ static void bulk_launch(const DTab32<D>& T, const uint16_t* status, const float*
 template <int D, int OS, bool AVG, bool ADV>
 static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, const float* s_near, const float* phin, const float* ddx,
                          float* out, const float* avg_with, cudaStream_t s, const StageCfg& cfg, int* err, const float* vn, float adv_dt) {
-  static int gb_reg = 0, gb_uni = 0, gb_uni2 = 0;
+  static int gb_reg = 0, gb_uni = 0, gb_uni2 = 0, gb_uni5 = 0;
   if (!gb_reg) gb_reg = persistent_blocks<D>((const void*)k_reinit_fused_reg32<D, OS, AVG, ADV>);
   if (!gb_uni) gb_uni = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1, ADV>);
   if (!gb_uni2) gb_uni2 = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 2, ADV>);
+  if (!gb_uni5) gb_uni5 = persistent_blocks<D>((const void*)k_reinit_uniform32<D, AVG, 1, ADV, 6>);
   const int tpb = (cfg.tpb > 0 && cfg.tpb <= TPB) ? cfg.tpb : TPB;
   // a persistent grid sized for TPB-thread blocks keeps the same thread count with smaller blocks
   const int scale = TPB / tpb;
@@ -1269,7 +1272,8 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
         T, status, s_near, phin, ddx, out, avg_with, (int)uni_end, (int)T.nR, vn, adv_dt);
   }
   // the bulk-copy uniform kernel serves the reinitialisation only; the advection stage uses the register pipeline
-  if (!ADV && part == STAGE_PART_UNIFORM && uni_end > 0 && cfg.depth >= 3 && uniform_bulk_ok(T, status, phin, avg_with) && err) {
+  if (!ADV && part == STAGE_PART_UNIFORM && uni_end > 0 && (cfg.depth == 3 || cfg.depth == 4) && uniform_bulk_ok(T, status, phin, avg_with) &&
+      err) {
     const int halo = cfg.halo >= 0 ? (cfg.halo & ~3) : 512;
     const long long wc = cfg.wait_cycles > 0 ? cfg.wait_cycles : kFullWaitCycles;
     if (cfg.depth == 4)
@@ -1277,11 +1281,13 @@ static void fused_launch(const DTab32<D>& T, int part, const uint16_t* status, c
     else
       bulk_launch<D, AVG, 2>(T, status, s_near, phin, out, avg_with, err, wc, halo, tpb, cfg.uniform_blocks, grid_of(uni_end), s);
   } else if (part == STAGE_PART_UNIFORM && uni_end > 0) {
-    const int full = (cfg.depth == 2 ? gb_uni2 : gb_uni) * scale;
+    const int full = (cfg.depth == 2 ? gb_uni2 : cfg.depth == 5 ? gb_uni5 : gb_uni) * scale;
     const int gb = cfg.uniform_blocks > 0 ? std::min(cfg.uniform_blocks, full) : full;
     const unsigned g = (unsigned)std::min<int64_t>(gb, grid_of(uni_end));
     if (cfg.depth == 2)
       k_reinit_uniform32<D, AVG, 2, ADV><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with, vn, adv_dt);
+    else if (cfg.depth == 5)
+      k_reinit_uniform32<D, AVG, 1, ADV, 6><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with, vn, adv_dt);
     else
       k_reinit_uniform32<D, AVG, 1, ADV><<<g, tpb, 0, s>>>(T, status, s_near, phin, out, avg_with, vn, adv_dt);
   }

@@ -178,7 +178,8 @@ def test_mixed_advect_launch_shapes_agree(case):
     try:
         for shape in ({"threads_per_block": 256, "uniform_blocks": 0, "regular_blocks": 0, "uniform_depth": 1, "streams": 2, "priority": 2},
                       {"threads_per_block": 64, "uniform_blocks": 152, "regular_blocks": 304, "uniform_depth": 2, "streams": 1},
-                      {"threads_per_block": 128, "uniform_blocks": 0, "regular_blocks": 0, "uniform_depth": 3, "streams": 2, "priority": 0}):
+                      {"threads_per_block": 128, "uniform_blocks": 0, "regular_blocks": 0, "uniform_depth": 3, "streams": 2, "priority": 0},
+                      {"threads_per_block": 128, "uniform_blocks": 1216, "regular_blocks": 0, "uniform_depth": 5, "streams": 2}):
             ls.stage_config = shape
             p = phi0.copy()
             ls.advect_in_normal_direction(vn, p, dt, precision="mixed")
@@ -247,12 +248,13 @@ def test_band_linf_device_matches_numpy():
                                    (256, 4, 0, 4, 1024, 2), (64, 3, 0, 4, 4096, 2), (128, 0, 304, 4, 4, 2), (256, 0, 0, 1, 512, 1),
                                    (128, 912, 304, 2, 512, 1), (256, 4, 0, 3, 256, 1), (128, 1216, 608, 1, 512, 2, 1),
                                    (256, 0, 0, 3, 512, 2, 0), (128, 1216, 608, 1, 512, 2, 0), (128, 912, 0, 1, 512, 2, 3),
-                                   (256, 0, 304, 2, 512, 2, 4), (64, 3, 0, 4, 256, 2, 3)])
+                                   (256, 0, 304, 2, 512, 2, 4), (64, 3, 0, 4, 256, 2, 3), (128, 1216, 0, 5, 512, 2),
+                                   (256, 0, 0, 5, 512, 1), (64, 152, 304, 5, 512, 2, 0)])
 @pytest.mark.parametrize("grid", ["flower3d", "circle2d"])
 def test_mixed_result_independent_of_launch_shape(shape, grid):
     """The mixed stages are Jacobi updates: threads per block, persistent grids, the uniform kernel's
     pipeline (depth 3 / 4: bulk-copied tiles two / three ahead; a grid of 2 to 4 CTAs makes every CTA cycle
-    through its stages many times), the phi window around each tile (halo 0 to 4096 nodes), one or two
+    through its stages many times; depth 5: registers capped), the phi window around each tile (halo 0 to 4096 nodes), one or two
     streams per stage and their priorities change no bit of the result."""
     f = flower_3d(3, 6) if grid == "flower3d" else circle_2d(3, 9)
     phi0 = phi0_flower_3d(f) if grid == "flower3d" else phi0_circle_2d(f)
