@@ -510,6 +510,7 @@ def run_batch(args):
         "one_call_per_grid_equals_batched": same,
         "band_linf_vs_fp64_over_dx_min": dmin_err, "interface_location_err_over_dx_min": iface_err,
         "interface_sign_mismatches": mismatched, "accuracy_checked_grids": b.count, "setup_s": setup_s,
+        "box_copy_GBps": box_copy_bandwidth(stream),
     }
     print(json.dumps(out), flush=True)
 
@@ -624,7 +625,7 @@ def run_large(args):
                             "mixed_node_steps_per_s": N * 20 / (adv_ms["mixed"] / 1e3),
                             "fp64_node_steps_per_s": N * 20 / (adv_ms["fp64"] / 1e3),
                             "band_linf_mixed_vs_fp64": adv_err, "dt": dt},
-        "autotuned_stage_config": cfg,
+        "autotuned_stage_config": cfg, "box_copy_GBps": box_copy_bandwidth(stream),
         "setup_s": {"grid": t_grid, "tables": t_tables, "note": "host refinement, node numbering and tables on the GPU"},
         "device_memory_used_gb": (lambda fr: (fr[1] - fr[0]) / 1e9)(torch.cuda.mem_get_info()),
     }

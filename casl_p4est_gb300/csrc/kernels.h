@@ -39,8 +39,8 @@ struct StageCfg {
   // pipeline of the uniform kernel: 1 or 2 nodes whose gathers are in flight per thread, or 3 (4): the
   // node words and a window of phi bulk-copied into shared memory two (three) tiles ahead
   // (cp.async.bulk + mbarrier), or 5: as 1 with the registers capped at 40 so that more of its warps stay
-  // resident beside the side stream's kernels
-  int depth = 1;
+  // resident beside the side stream's kernels (the default: 5-6% faster stages than 1 on the 13.7M-node grid)
+  int depth = 5;
   // nodes on either side of a tile in the phi window of the bulk-copy kernel (a multiple of 4)
   int halo = 512;
   // 2: the second derivatives and the irregular nodes on a side stream while the main stream runs the

@@ -387,7 +387,7 @@ def _stage_config(handle):
 
 
 def _set_stage_config(handle, cfg):
-    arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"], cfg.get("uniform_depth", 1),
+    arr = np.array([cfg["threads_per_block"], cfg["uniform_blocks"], cfg["regular_blocks"], cfg.get("uniform_depth", 5),
                     cfg.get("window_halo", 512), cfg.get("streams", 2), cfg.get("priority", 2)], np.int32)
     L.check(L.load().lsg_level_set_set_stage_config(handle, L.i32ptr(arr)))
 

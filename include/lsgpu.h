@@ -406,8 +406,8 @@ int lsg_batch_reinitialize_device(lsg_level_set* batch, double* phi_dev, const i
  * config[1] grid of the persistent uniform-stencil kernel, config[2] grid of the persistent regular
  * kernel (0: one full wave), config[3] pipeline of the uniform kernel (1 or 2 nodes in flight per
  * thread, or 3 / 4: the nodes' table words and a window of phi bulk-copied into shared memory two /
- * three tiles ahead; a bounded wait of that kernel that gives up makes the call return LSG_ETIMEOUT; or 5:
- * as 1 with the kernel's registers capped so that more of its threads stay resident),
+ * three tiles ahead; a bounded wait of that kernel that gives up makes the call return LSG_ETIMEOUT; or 5,
+ * the default: as 1 with the kernel's registers capped so that more of its threads stay resident),
  * config[4] nodes on either side of a tile in that window (a multiple of 4 in 0..4096), config[5] streams
  * of a stage (2: second derivatives and irregular nodes beside the uniform nodes; 1: the four kernels one
  * after another), config[6] with two streams their pairing and the one the block scheduler prefers (0:
