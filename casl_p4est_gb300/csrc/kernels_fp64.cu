@@ -161,15 +161,14 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
 #pragma unroll
       for (int a = 0; a < D; ++a) {
         const double xm = minmod_x(xxnb[2 * a], xx0[a]);
-        gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
+        gm[a] = gm[a] + scale2(s[2 * a], -1) * xm;
         const double xp = minmod_x(xxnb[2 * a + 1], xx0[a]);
-        gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
+        gp[a] = gp[a] - scale2(s[2 * a + 1], -1) * xp;
       }
     }
     // sgn = (p0 > 0 ? 1 : -1): the prep step stored p0 > 0 as ST_POSITIVE; sgn * g is +-g exactly, so the
     // upwind tests are sign tests of g
     const bool pos = (st & ST_POSITIVE) != 0;
-    const double sgn = pos ? 1.0 : -1.0;
     double dt = min2x(s[0], s[1]);
     dt = min3x(dt, s[2], s[3]);
     if (D == 3) dt = min3x(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
@@ -181,10 +180,10 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
     }
     double h = max2x(gp[0] * gp[0], gm[0] * gm[0]) + max2x(gp[1] * gp[1], gm[1] * gm[1]);
     if (D == 3) h = h + max2x(gp[2 % D] * gp[2 % D], gm[2 % D] * gm[2 % D]);
-    r = f0 - dt * sgn * (sqrt(h) - 1.);
-    if (product_negative(p0, r)) r *= -1.0;
+    r = f0 - times_sign(dt, pos) * (sqrt(h) - 1.);
+    if (product_negative(p0, r)) r = neg1(r);
   }
-  if (AVG) r = .5 * (avg_with[n] + r);
+  if (AVG) r = scale2(avg_with[n] + r, -1);
   out[n] = r;
 }
 
@@ -234,9 +233,9 @@ __global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const doubl
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     const double xm = minmod_x(xxnb[2 * a], xx0[a]);
-    gm[a] = gm[a] + 0.5 * s[2 * a] * xm;
+    gm[a] = gm[a] + scale2(s[2 * a], -1) * xm;
     const double xp = minmod_x(xxnb[2 * a + 1], xx0[a]);
-    gp[a] = gp[a] - 0.5 * s[2 * a + 1] * xp;
+    gp[a] = gp[a] - scale2(s[2 * a + 1], -1) * xp;
   }
   const double v = vn[n];
   // sgn = (v > 0 ? 1 : -1); sgn * g is +-g exactly, so the upwind tests are sign tests of g
@@ -249,7 +248,7 @@ __global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const doubl
   double h = (gp[0] * gp[0] + gm[0] * gm[0]) + (gp[1] * gp[1] + gm[1] * gm[1]);
   if (D == 3) h = h + (gp[2 % D] * gp[2 % D] + gm[2 % D] * gm[2 % D]);
   double r = f0 - dt * v * (sqrt(h));
-  if (AVG) r = 0.5 * (avg_with[n] + r);
+  if (AVG) r = scale2(avg_with[n] + r, -1);
   out[n] = r;
 }
 
@@ -466,10 +465,10 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
   bool ok = false;
   if (stencil_negative_flag<D>(T, n, bqn)) {
     ok = true;
-    Qxy = .5 * (grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 0, r) + grad_comp64<D>(T, G, n, qx, qxdd, 1, r));
+    Qxy = scale2(grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 0, r) + grad_comp64<D>(T, G, n, qx, qxdd, 1, r), -1);
     if (D == 3) {
-      Qyz = .5 * (grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 1, r) + grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 2, r));
-      Qzx = .5 * (grad_comp64<D>(T, G, n, qx, qxdd, 2, r) + grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 0, r));
+      Qyz = scale2(grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 1, r) + grad_comp64<D>(T, G, n, qx + N, qxdd + DN, 2, r), -1);
+      Qzx = scale2(grad_comp64<D>(T, G, n, qx, qxdd, 2, r) + grad_comp64<D>(T, G, n, qx + 2 * N, qxdd + 2 * DN, 0, r), -1);
     }
   } else {
     constexpr int K = D == 3 ? 12 : 4;
@@ -512,7 +511,7 @@ __global__ void __launch_bounds__(TPB) k_ext_init2(DTab64<D> T, DGrad G, const d
   for (int a = 0; a < D; ++a) {
     const double fp = quad_nb64<D>(T, 2 * a + 1, n, q, Dq), fm = quad_nb64<D>(T, 2 * a, n, q, Dq);
     const double dp = T.d[(int64_t)(2 * a + 1) * N + n], dm = T.d[(int64_t)(2 * a) * N + n];
-    Qaa[a] = qdiv((qdiv(fp - q[n], dp) + qdiv(fm - q[n], dm)) * 2., dp + dm);
+    Qaa[a] = qdiv(scale2(qdiv(fp - q[n], dp) + qdiv(fm - q[n], dm), 1), dp + dm);
   }
   const double Qx = qx[n], Qy = qx[N + n];
   const double Nx = nrm[n], Ny = nrm[N + n];
@@ -574,9 +573,9 @@ __global__ void __launch_bounds__(TPB) k_ext_q(DTab64<D> T, const double* __rest
       qm = c * qm < 0 ? 0 : (fabs(c) < fabs(qm) ? c : qm);
       qp = c * qp < 0 ? 0 : (fabs(c) < fabs(qp) ? c : qp);
       if (nrm[(int64_t)a * N + n] < 0)
-        g[a] -= .5 * T.d[(int64_t)(2 * a + 1) * N + n] * qp;
+        g[a] -= scale2(T.d[(int64_t)(2 * a + 1) * N + n], -1) * qp;
       else
-        g[a] += .5 * T.d[(int64_t)(2 * a) * N + n] * qm;
+        g[a] += scale2(T.d[(int64_t)(2 * a) * N + n], -1) * qm;
     }
   }
   double s = nrm[n] * g[0] + nrm[N + n] * g[1];
@@ -650,14 +649,14 @@ __global__ void __launch_bounds__(TPB) k_efi_stage64(DTab64<D> T, const double* 
     double t[3];
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      const double qm = qdiv(q0 - qn[2 * a], s[2 * a]) + 0.5 * s[2 * a] * minmod(dm[a], d0[a]);
-      const double qp = qdiv(qn[2 * a + 1] - q0, s[2 * a + 1]) - 0.5 * s[2 * a + 1] * minmod(dp[a], d0[a]);
+      const double qm = qdiv(q0 - qn[2 * a], s[2 * a]) + scale2(s[2 * a], -1) * minmod(dm[a], d0[a]);
+      const double qp = qdiv(qn[2 * a + 1] - q0, s[2 * a + 1]) - scale2(s[2 * a + 1], -1) * minmod(dp[a], d0[a]);
       t[a] = nv[a] * (nv[a] > 0.0 ? qm : qp);
     }
     res = q0 - dt * (D == 3 ? (t[0] + t[1] + t[D == 3 ? 2 : 0]) : (t[0] + t[1]));
   }
   if (AVG)
-    out[n] = .5 * (out[n] + res);
+    out[n] = scale2(out[n] + res, -1);
   else
     out[n] = res;
 }

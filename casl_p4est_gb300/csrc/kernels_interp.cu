@@ -191,9 +191,9 @@ __device__ __forceinline__ double interpolate_local(const double* lw, const doub
     for (int j = 0; j < CH; ++j) r += f[j] * lw[j];
   }
   if (D == 3)
-    r -= 0.5 * (sdw[0] * dd[0] + sdw[1] * dd[1] + sdw[2] * dd[2]);
+    r -= st64::scale2(sdw[0] * dd[0] + sdw[1] * dd[1] + sdw[2] * dd[2], -1);
   else
-    r -= 0.5 * (sdw[0] * dd[0] + sdw[1] * dd[1]);
+    r -= st64::scale2(sdw[0] * dd[0] + sdw[1] * dd[1], -1);
   return r;
 }
 
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(TPB) k_sl_vortex64(DLoc<D> L, const double* __
   for (int a = 0; a < D; ++a) x[a] = xyz[p * D + a];
   vortex<D>(x, vscale, v);
 #pragma unroll
-  for (int a = 0; a < D; ++a) xs[a] = x[a] - 0.5 * dt * v[a];
+  for (int a = 0; a < D; ++a) xs[a] = x[a] - st64::scale2(dt, -1) * v[a];
   clip_in_domain<D>(L, xs);
   vortex<D>(xs, vscale, v);
 #pragma unroll

@@ -69,12 +69,42 @@ __device__ __forceinline__ bool product_negative(double a, double b) {
 // number x / y, and IEEE multiplication and division round that same number the same way (subnormal,
 // infinite and zero results included), so one multiplication replaces the division sequence; GB300
 // issues FP64 at 2 operations per SM cycle, where a division takes about ten. Any other y is divided.
+// When x and the quotient are normal numbers the quotient is exact, and it is x's bit pattern with the exponent
+// field moved by e - 1023 and the sign bit of y added: integer work, no FP64 instruction at all.
 __device__ __forceinline__ double qdiv(double x, double y) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(y);
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;  // biased exponent
-  if ((b & 0x000fffffffffffffull) == 0 && e - 1u < 2045u)  // mantissa zero, e in [1, 2045]: 1/y = 2^(1023 - (e - 1023))
+  if ((b & 0x000fffffffffffffull) == 0 && e - 1u < 2045u) {  // mantissa zero, e in [1, 2045]: 1/y = 2^(1023 - (e - 1023))
+    const unsigned long long bx = bits_of(x) ^ (b & 0x8000000000000000ull);
+    const int ex = (int)((bx >> 52) & 0x7ffu), r = ex + 1023 - (int)e;
+    if (ex >= 1 && ex <= 2046 && r >= 1 && r <= 2046)
+      return __longlong_as_double((long long)(bx - ((unsigned long long)e << 52) + (1023ull << 52)));
     return __dmul_rn(x, __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046u - e) << 52))));
+  }
   return x / y;
+}
+
+// x * 2^k (k in [-1022, 1023]), bit for bit: when x and the product are normal the product is exact and is x with
+// k added to its exponent field (integer work); zeros, subnormals, infinities, NaN and products outside the normal
+// range take the FP64 multiplication by 2^k. scale2(x, -1) is 0.5 * x and scale2(x, 1) is x * 2.
+__device__ __forceinline__ double scale2(double x, int k) {
+  const unsigned long long b = bits_of(x);
+  const int e = (int)((b >> 52) & 0x7ffu), r = e + k;
+  if (e >= 1 && e <= 2046 && r >= 1 && r <= 2046) return __longlong_as_double((long long)(b + ((unsigned long long)(long long)k << 52)));
+  return __dmul_rn(x, __longlong_as_double((long long)(1023 + k) << 52));
+}
+
+// x * -1.0 bit for bit: the sign bit flipped; a NaN is multiplied
+__device__ __forceinline__ double neg1(double x) {
+  const unsigned long long b = bits_of(x);
+  if ((b & kMag) > kInf) return __dmul_rn(x, -1.0);
+  return __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
+}
+// x * (pos ? 1.0 : -1.0) bit for bit
+__device__ __forceinline__ double times_sign(double x, bool pos) {
+  const unsigned long long b = bits_of(x);
+  if ((b & kMag) > kInf) return __dmul_rn(x, pos ? 1.0 : -1.0);
+  return pos ? x : __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
 }
 
 // x / 3 (the local pseudo-time step min(s) / P4EST_DIM of a 3D node), bit for bit. When x = +-2^k with x and
@@ -87,18 +117,38 @@ __device__ __forceinline__ double div3(double x) {
   return x / 3.0;
 }
 
+// (f w) / nrm with one face node and nrm == w == 2^k, bit for bit: it is f itself whenever f w is a normal
+// number (then f w and the division by 2^k are exact). The test is integer work on the bit patterns; a face
+// node that coincides with the neighbour position (every regular direction on power-of-two trees) then costs
+// no FP64 operation. Any other case takes the reference's arithmetic.
+__device__ __forceinline__ bool unit_weight_exact(double f, double w, double nrm) {
+  const unsigned long long bw = bits_of(w), bf = bits_of(f);
+  const int ew = (int)(bw >> 52);  // w > 0: no sign bit
+  const int ef = (int)((bf >> 52) & 0x7ffu);
+  const int e = ef + ew - 1023;  // biased exponent of f w
+  return bw == bits_of(nrm) && (bw & 0x000fffffffffffffull) == 0 && ew >= 1 && ew <= 2045 && ef >= 1 && ef <= 2046 && e >= 1 &&
+         e <= 2046;
+}
+
 template <int D>
 __device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f) {
   constexpr int H = Dim<D>::HALF;
   const int64_t N = T.N;
   const int64_t base = (int64_t)(dir * H) * N + n;
-  double acc = f[T.nbr[base]] * T.w[base];
+  const double f0 = f[T.nbr[base]], w0 = T.w[base], nrm = T.nrm[(int64_t)dir * N + n];
+  int32_t ik[H];
+  bool single = true;
 #pragma unroll
   for (int k = 1; k < H; ++k) {
-    const int32_t ik = T.nbr[base + k * N];
-    if (ik >= 0) acc = acc + f[ik] * T.w[base + k * N];
+    ik[k] = T.nbr[base + k * N];
+    single = single && ik[k] < 0;
   }
-  return qdiv(acc, T.nrm[(int64_t)dir * N + n]);
+  if (single && unit_weight_exact(f0, w0, nrm)) return f0;
+  double acc = f0 * w0;
+#pragma unroll
+  for (int k = 1; k < H; ++k)
+    if (ik[k] >= 0) acc = acc + f[ik[k]] * T.w[base + k * N];
+  return qdiv(acc, nrm);
 }
 
 // correct_naive_second_derivatives (src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298), all branches.
@@ -196,7 +246,7 @@ __device__ __forceinline__ void laplace64(const DTab64<D>& T, int64_t n, const d
     const double fm = lin64<D>(T, 2 * a, n, f);
     const double fp = lin64<D>(T, 2 * a + 1, n, f);
     const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
-    Dv[a] = qdiv((qdiv(fp - f0, dp) + qdiv(fm - f0, dm)) * 2., dp + dm);
+    Dv[a] = qdiv(scale2(qdiv(fp - f0, dp) + qdiv(fm - f0, dm), 1), dp + dm);
   }
   const int32_t ci = T.cidx[n];
   if (ci >= 0) correct64<D>(T.crec + (int64_t)6 * ci, Dv);
@@ -224,7 +274,7 @@ __device__ __forceinline__ double quad_nb64(const DTab64<D>& T, int dir, int64_t
 }
 
 __device__ __forceinline__ double interface_location(double a, double b, double fa, double fb) {
-  return 0.5 * (a + b + (a - b) * (fa + fb) / (fb - fa));
+  return scale2(a + b + (a - b) * (fa + fb) / (fb - fa), -1);
 }
 
 __device__ inline double interface_location_2nd(double a, double b, double fa, double fb, double fxxa, double fxxb) {
@@ -232,19 +282,19 @@ __device__ inline double interface_location_2nd(double a, double b, double fa, d
   if (fabs(fb) < EPS) return b - EPS;
   const double fxx = minmod(fxxa, fxxb);
   const double h = b - a;
-  const double c2 = 0.5 * fxx;
+  const double c2 = scale2(fxx, -1);
   const double c1 = qdiv(fb - fa, h);
-  const double c0 = 0.5 * (fb + fa) - qdiv(h * h, 8.0) * fxx;
+  const double c0 = scale2(fb + fa, -1) - qdiv(h * h, 8.0) * fxx;
   double x;
   if (fabs(c2) < EPS)
     x = -c0 / c1;
   else {
     if (fb < 0)
-      x = (-2 * c0) / (c1 - sqrt(c1 * c1 - 4 * c2 * c0));
+      x = neg1(scale2(c0, 1)) / (c1 - sqrt(c1 * c1 - scale2(c2, 2) * c0));
     else
-      x = (-2 * c0) / (c1 + sqrt(c1 * c1 - 4 * c2 * c0));
+      x = neg1(scale2(c0, 1)) / (c1 + sqrt(c1 * c1 - scale2(c2, 2) * c0));
   }
-  return x + 0.5 * (a + b);
+  return x + scale2(a + b, -1);
 }
 
 
