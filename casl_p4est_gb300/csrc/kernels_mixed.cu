@@ -913,6 +913,11 @@ __global__ void __launch_bounds__(TPB) k_advect_stage32(DTab32<D> T, const float
 // Accurate FP64 arithmetic without the reference's division order: reciprocals by Newton iteration,
 // normalised weights and correction matrices precomputed in FP64.
 __device__ __forceinline__ double rcp64(double x) {
+  // a power of two (the product of uniform cell sizes) has an exact reciprocal: its exponent negated
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+  if ((b & 0x000fffffffffffffull) == 0 && ex - 1u < 2045u)
+    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046u - ex) << 52)));
   const double ax = fabs(x);
   if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
   double r = (double)__frcp_rn((float)x);
@@ -929,7 +934,7 @@ __device__ __forceinline__ double level_size64(double tsize, int base, uint32_t 
 }
 
 __device__ __forceinline__ double central_dd64(double fp, double f0, double fm, double dp, double dm) {
-  return 2.0 * fma(fp - f0, dm, (fm - f0) * dp) * rcp64(dp * dm * (dp + dm));
+  return st64::scale2(fma(fp - f0, dm, (fm - f0) * dp), 1) * rcp64(dp * dm * (dp + dm));
 }
 
 template <int D>
