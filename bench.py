@@ -168,6 +168,20 @@ class ClockSampler:
         return out
 
 
+def gpu_info(gpu_index):
+    """Read-only description of the GPU (which board, its ECC, power-limit and application-clock settings), so that
+    lines from different GPUs of the same kind can be told apart."""
+    fields = ["name", "uuid", "pci.bus_id", "vbios_version", "driver_version", "ecc.mode.current", "power.limit",
+              "clocks.applications.graphics", "clocks.applications.memory", "compute_mode", "mig.mode.current"]
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + ",".join(fields), "--format=csv,noheader"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=20).stdout.strip()
+        vals = [v.strip() for v in out.splitlines()[0].split(",")]
+        return dict(zip(fields, vals)) if len(vals) == len(fields) else None
+    except Exception:
+        return None
+
+
 def box_copy_bandwidth(stream):
     """Device-to-device copy bandwidth of this GPU (1 GiB, read + written bytes per second), beside the pool's
     measured peak: GPUs of the same kind differ by several percent, and so do the memory-bound kernels on them."""
@@ -916,7 +930,8 @@ def main():
             "fp64_vs_oracle_full_grid": parity,
             "fp64_vs_cpu_same_precision": (value64 / cpu["value"] if cpu else None),
             "roofline": roofline, "kernels": per_kernel, "kernels_fp64": per_kernel_fp64,
-            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "box_copy_GBps": box_bw, "setup_s": setup_s,
+            "e2e": e2e, "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clk, "box_copy_GBps": box_bw,
+            "gpu": gpu_info(local), "setup_s": setup_s,
             "autotuned_stage_config": stage_cfg, "mixed_tables": ls.table_stats(),
         }
         print(json.dumps(out), flush=True)
