@@ -19,6 +19,13 @@ namespace st64 {
 // integer ones at 64, so these keep the FP64 pipe for arithmetic.
 constexpr unsigned long long kMag = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
 __device__ __forceinline__ unsigned long long bits_of(double v) { return (unsigned long long)__double_as_longlong(v); }
+// The FP64 fallbacks of the helpers below are functions that are never inlined: inlined, the compiler may evaluate
+// a fallback on every lane and select its result (if-conversion), which puts its FP64 instructions on the pipe for
+// inputs that never need them. A call is taken only by the lanes whose inputs need it.
+static __device__ __noinline__ bool less_fp64(double a, double b) { return a < b; }
+static __device__ __noinline__ bool product_negative_fp64(double a, double b) { return a * b < 0.0; }
+static __device__ __noinline__ double mul_fp64(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __noinline__ double minmod_fp64(double a, double b) { return minmod(a, b); }
 // +0 .. +inf (no sign bit, not NaN): for these the integer order of the bit patterns is the numeric order
 __device__ __forceinline__ bool nonneg_num(unsigned long long b) { return b <= kInf; }
 __device__ __forceinline__ bool is_zero(double v) { return (bits_of(v) & kMag) < bits_of(EPS); }  // fabs(v) < EPS, check_if_zero .h:186
@@ -32,7 +39,7 @@ __device__ __forceinline__ bool negative(double v) {                            
 __device__ __forceinline__ bool less64(double a, double b) {
   const unsigned long long ia = bits_of(a), ib = bits_of(b);
   if (nonneg_num(ia) && nonneg_num(ib)) return ia < ib;
-  return a < b;
+  return less_fp64(a, b);
 }
 __device__ __forceinline__ double max2x(double a, double b) { return less64(b, a) ? a : b; }
 __device__ __forceinline__ double min2x(double a, double b) { return less64(a, b) ? a : b; }
@@ -47,7 +54,7 @@ __device__ __forceinline__ double minmod_x(double a, double b) {
     if ((ia ^ ib) >> 63) return 0.0;
     if (ea > 0 && eb > 0 && ea + eb >= 972u) return (ia & kMag) < (ib & kMag) ? a : b;
   }
-  return minmod(a, b);
+  return minmod_fp64(a, b);
 }
 // a * b < 0.0 with IEEE double semantics, decided from the bit patterns where that is exact: opposite
 // sign bits, both finite and normal, and exponents large enough that the product cannot round to
@@ -57,11 +64,11 @@ __device__ __forceinline__ bool product_negative(double a, double b) {
   const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
   if ((ia ^ ib) >= 0) {
     if (((ia >> 52) & 0x7ff) != 0x7ff && ((ib >> 52) & 0x7ff) != 0x7ff) return false;  // same signs, no NaN: a b >= 0
-    return a * b < 0.0;
+    return product_negative_fp64(a, b);
   }
   const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
   if (ea > 0 && eb > 0 && ea < 0x7ff && eb < 0x7ff && ea + eb >= 972) return true;
-  return a * b < 0.0;
+  return product_negative_fp64(a, b);
 }
 
 // x / y, bit for bit. When y is a normal power of two whose reciprocal 1/y is normal too (octree cell
@@ -79,7 +86,7 @@ __device__ __forceinline__ double qdiv(double x, double y) {
     const int ex = (int)((bx >> 52) & 0x7ffu), r = ex + 1023 - (int)e;
     if (ex >= 1 && ex <= 2046 && r >= 1 && r <= 2046)
       return __longlong_as_double((long long)(bx - ((unsigned long long)e << 52) + (1023ull << 52)));
-    return __dmul_rn(x, __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046u - e) << 52))));
+    return mul_fp64(x, __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046u - e) << 52))));
   }
   return x / y;
 }
@@ -91,19 +98,19 @@ __device__ __forceinline__ double scale2(double x, int k) {
   const unsigned long long b = bits_of(x);
   const int e = (int)((b >> 52) & 0x7ffu), r = e + k;
   if (e >= 1 && e <= 2046 && r >= 1 && r <= 2046) return __longlong_as_double((long long)(b + ((unsigned long long)(long long)k << 52)));
-  return __dmul_rn(x, __longlong_as_double((long long)(1023 + k) << 52));
+  return mul_fp64(x, __longlong_as_double((long long)(1023 + k) << 52));
 }
 
 // x * -1.0 bit for bit: the sign bit flipped; a NaN is multiplied
 __device__ __forceinline__ double neg1(double x) {
   const unsigned long long b = bits_of(x);
-  if ((b & kMag) > kInf) return __dmul_rn(x, -1.0);
+  if ((b & kMag) > kInf) return mul_fp64(x, -1.0);
   return __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
 }
 // x * (pos ? 1.0 : -1.0) bit for bit
 __device__ __forceinline__ double times_sign(double x, bool pos) {
   const unsigned long long b = bits_of(x);
-  if ((b & kMag) > kInf) return __dmul_rn(x, pos ? 1.0 : -1.0);
+  if ((b & kMag) > kInf) return mul_fp64(x, pos ? 1.0 : -1.0);
   return pos ? x : __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
 }
 
