@@ -15,6 +15,13 @@ of phi, point to point between the ranks that share ghosts (torch.distributed is
 tensors, gloo for host tensors), and the band check is one all-reduce of a double. Every rank holds
 full-length arrays and the full node tables (each sweep launches over its own range only), so a rank's
 memory does not shrink with the rank count; the work and the bytes each rank streams do.
+
+Interpolation at arbitrary points (the semi-Lagrangian step): leaves are split into Morton ranges too, and a point
+is interpolated by the rank that owns the leaf containing it, as my_p4est_interpolation_t forwards remote points
+to their owners and returns the values (src/my_p4est_interpolation.cpp:341-467): per rank pair one message with
+the point count, one with the points and one with the values. The owner reads the field and its second
+derivatives at its leaves' corner nodes only, so it needs its node range plus the corner ghosts that
+LeafPartition lists, filled by the same HaloExchange.
 """
 from __future__ import annotations
 
@@ -74,6 +81,127 @@ class MortonPartition:
     def halo_bytes(self, rank, planes=1, itemsize=8):
         """Bytes rank receives in one exchange of `planes` node-sampled planes."""
         return int(sum(len(v) for v in self.recv[rank].values())) * planes * itemsize
+
+
+class LeafPartition:
+    """Contiguous leaf ranges of equal size (leaves in tree-major Morton order, as p4est partitions quadrants)
+    and, per rank, the corner nodes of its leaves that lie outside its node range (node_bounds, the node
+    partition's ranges): ghosts[r], recv[r][s] = send[s][r] (the attributes HaloExchange reads, with N).
+
+    local_nodes: (leaves, 2^dim) corner node indices per leaf (Forest.local_nodes)."""
+
+    def __init__(self, local_nodes, node_bounds, world):
+        if world < 1 or len(node_bounds) != world + 1:
+            raise ValueError("need world >= 1 and world + 1 node bounds")
+        ln = np.asarray(local_nodes)
+        nl = len(ln)
+        ln = ln.reshape(nl, -1)
+        self.world = world
+        self.N = int(node_bounds[-1])
+        self.node_bounds = [int(b) for b in node_bounds]
+        self.bounds = [(nl * r) // world for r in range(world + 1)]
+        self.ghosts, self.recv = [], []
+        for r in range(world):
+            b, e = self.node_bounds[r], self.node_bounds[r + 1]
+            corners = np.unique(ln[self.bounds[r]:self.bounds[r + 1]].ravel())
+            g = corners[(corners < b) | (corners >= e)]
+            self.ghosts.append(g)
+            owner = np.searchsorted(self.node_bounds, g, side="right") - 1
+            self.recv.append({s: g[owner == s] for s in range(world) if s != r and np.any(owner == s)})
+        self.send = [{r: self.recv[r][s] for r in range(world) if s in self.recv[r]} for s in range(world)]
+
+    def owner_of_leaves(self, leaf):
+        """Rank owning each leaf index (a torch tensor or a numpy array of leaf indices)."""
+        if isinstance(leaf, np.ndarray):
+            return np.searchsorted(self.bounds, leaf, side="right") - 1
+        import torch
+        b = torch.as_tensor(self.bounds, dtype=torch.int64, device=leaf.device)
+        return torch.searchsorted(b, leaf.to(torch.int64), right=True) - 1
+
+
+def _exchange_sized(world, rank, outgoing, make_inbox):
+    """One batch of point-to-point messages: outgoing[peer] is sent to peer, and inbox[peer] = make_inbox(peer)
+    (or None: nothing expected) is filled by peer. Empty messages are not sent."""
+    import torch.distributed as dist
+    ops, inbox = [], {}
+    for peer in range(world):
+        if peer == rank:
+            continue
+        t = outgoing.get(peer)
+        if t is not None and t.numel() > 0:
+            ops.append(dist.P2POp(dist.isend, t.contiguous(), peer))
+        buf = make_inbox(peer)
+        if buf is not None and buf.numel() > 0:
+            inbox[peer] = buf
+            ops.append(dist.P2POp(dist.irecv, buf, peer))
+    if ops:
+        for req in dist.batch_isend_irecv(ops):
+            req.wait()
+    return inbox
+
+
+def interpolate_sharded(lpart: LeafPartition, rank: int, xyz, backend, method, F, Fdd=None):
+    """my_p4est_interpolation_nodes_t::interpolate on one rank of a Morton split (src/my_p4est_interpolation.cpp:
+    341-467, the query/reply exchange; the evaluation at a point is the single-process one, so the values are
+    the same bits as on one rank). xyz: (n, dim) float64 tensor of this rank's points; F: (nf, N) field tensor
+    and Fdd: (nf, dim, N) second derivatives (None for the linear method), valid at this rank's node range and
+    at lpart's ghosts; backend: locate(xyz) -> leaf indices, interpolate(method, F, Fdd, xyz) -> (nf, n).
+    Returns (nf, n)."""
+    import torch
+    world = lpart.world
+    dim = xyz.shape[1]
+    nf = F.shape[0]
+    owner = lpart.owner_of_leaves(backend.locate(xyz))
+    sel = {p: torch.nonzero(owner == p).flatten() for p in range(world)}
+    # the number of points each peer forwards here (the reduce-scatter of the reference's senders count)
+    counts_out = {p: torch.tensor([len(sel[p])], dtype=torch.int64) for p in range(world) if p != rank}
+    counts_in = _exchange_sized(world, rank, counts_out, lambda p: torch.zeros(1, dtype=torch.int64))
+    n_in = {p: int(counts_in[p].item()) for p in counts_in}
+    # queries: the points themselves
+    pts_in = _exchange_sized(world, rank, {p: xyz[sel[p]].to(torch.float64) for p in counts_out},
+                             lambda p: torch.empty((n_in[p], dim), dtype=torch.float64, device=xyz.device) if n_in[p] else None)
+    # every point this rank owns, its own first, then each peer's in rank order
+    peers = [p for p in range(world) if p != rank and n_in.get(p, 0) > 0]
+    mine = xyz[sel[rank]]
+    local_pts = torch.cat([mine] + [pts_in[p] for p in peers]) if peers else mine
+    vals = backend.interpolate(method, F, Fdd, local_pts) if len(local_pts) else torch.empty((nf, 0), dtype=torch.float64,
+                                                                                              device=xyz.device)
+    out = torch.empty((nf, len(xyz)), dtype=torch.float64, device=xyz.device)
+    out[:, sel[rank]] = vals[:, :len(mine)]
+    # replies: the values of the forwarded points, back to their ranks
+    replies, at = {}, len(mine)
+    for p in peers:
+        replies[p] = vals[:, at:at + n_in[p]].contiguous()
+        at += n_in[p]
+    got = _exchange_sized(world, rank, replies,
+                          lambda p: torch.empty((nf, len(sel[p])), dtype=torch.float64, device=xyz.device) if len(sel[p]) else None)
+    for p, v in got.items():
+        out[:, sel[p]] = v
+    return out
+
+
+def clip_in_domain(xyz, xyz_min, xyz_max):
+    """clip_in_domain (src/my_p4est_utils.h:2177-2187), non-periodic: coordinates outside the domain are clamped."""
+    import torch
+    lo = torch.as_tensor(xyz_min, dtype=xyz.dtype, device=xyz.device)
+    hi = torch.as_tensor(xyz_max, dtype=xyz.dtype, device=xyz.device)
+    out = (xyz < lo) | (xyz > hi)
+    return torch.where(out, torch.maximum(lo, torch.minimum(hi, xyz)), xyz)
+
+
+def sl_advect_sharded(lpart: LeafPartition, rank: int, xyz_np1, dt, v, vdd, phi, phi_dd, backend, xyz_min, xyz_max,
+                      velo_method=4, phi_method=4):
+    """my_p4est_semi_lagrangian_t::advect_from_n_to_np1(dt, v, vxx, phi_n, phi_xx_n, phi_np1) for this rank's new
+    nodes xyz_np1 (n, dim) (src/my_p4est_semi_lagrangian.cpp:148-223): v at the new nodes, the midpoint
+    x* = x - dt/2 v (clipped), v at x*, the departure point x_d = x - dt v(x*) (clipped), phi_n at x_d; every
+    interpolation through interpolate_sharded. v: (dim, N), vdd: (dim, dim, N), phi: (N,), phi_dd: (dim, N),
+    valid at this rank's nodes and lpart's ghosts. Returns phi_np1 at xyz_np1."""
+    vt = interpolate_sharded(lpart, rank, xyz_np1, backend, velo_method, v, vdd)
+    xs = clip_in_domain(xyz_np1 - (0.5 * dt) * vt.T, xyz_min, xyz_max)
+    vt = interpolate_sharded(lpart, rank, xs, backend, velo_method, v, vdd)
+    xd = clip_in_domain(xyz_np1 - dt * vt.T, xyz_min, xyz_max)
+    return interpolate_sharded(lpart, rank, xd, backend, phi_method, phi.reshape(1, -1),
+                               None if phi_dd is None else phi_dd.reshape(1, *phi_dd.shape))[0]
 
 
 class HaloExchange:
@@ -216,3 +344,43 @@ class ShardBackend:
 
     def copy(self, src, dst, first, count):
         dst[first:first + count] = src[first:first + count]
+
+
+class ShardInterpBackend:
+    """A rank's point location and node interpolation on its GPU (lsg_locate_points_device,
+    lsg_interpolate_nodes_device). The second derivatives are required for the quadratic methods: computed
+    from F inside the call they would read nodes this rank neither owns nor receives."""
+
+    def __init__(self, ls):
+        import torch
+        from . import _lib as L
+        self.L = L
+        self.ls = ls
+        self.dim = ls.ngbd.dim
+        ls.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    @staticmethod
+    def _p(t):
+        import ctypes as C
+        return None if t is None else C.c_void_p(t.data_ptr())
+
+    def locate(self, xyz):
+        import torch
+        x = xyz.contiguous()
+        leaf = torch.empty(len(x), dtype=torch.int32, device=x.device)
+        if len(x):
+            self.L.check(self.L.load().lsg_locate_points_device(self.ls.handle, self._p(x), len(x), self._p(leaf)))
+        return leaf.to(torch.int64)
+
+    def interpolate(self, method, F, Fdd, xyz):
+        import torch
+        if method != 0 and Fdd is None:
+            raise ValueError("the quadratic methods need the second derivatives (Fdd) in a split run")
+        x = xyz.contiguous()
+        F = F.contiguous()
+        out = torch.empty((F.shape[0], len(x)), dtype=torch.float64, device=x.device)
+        if len(x):
+            self.L.check(self.L.load().lsg_interpolate_nodes_device(self.ls.handle, self._p(x), len(x), self._p(F), int(F.shape[0]),
+                                                                    self._p(None if method == 0 else Fdd.contiguous()), int(method),
+                                                                    self._p(out)))
+        return out

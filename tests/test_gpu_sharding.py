@@ -76,3 +76,53 @@ def test_morton_split_equals_one_rank(name, world):
         ls.reinitialize_within_range_of_phi_0(ref, os_, ot, hi, lo, 7)
         got = lockstep(part, ShardBackend(ls), torch.from_numpy(phi0).cuda(), os_, ot, 7, hi, lo)
         assert np.array_equal(got, ref), (name, world, os_, ot, np.max(np.abs(got - ref)))
+
+
+@pytest.mark.parametrize("name", ["circle2d", "flower3d", "brick3d"])
+def test_forwarded_interpolation_lockstep_equals_one_rank(name):
+    """Interpolation across a Morton split of the leaves on the GPU (ShardInterpBackend), ranks emulated in one
+    process: every rank locates its points, each point is interpolated by the rank owning its leaf from that
+    rank's own copies of the fields (its node range plus the corner ghosts of its leaves, POISON elsewhere),
+    and the values equal the single-rank interpolation bit for bit. The message exchange itself
+    (interpolate_sharded over torch.distributed) is covered on CPU ranks in test_sharding.py."""
+    import torch
+    from casl_p4est_gb300.interpolation import my_p4est_interpolation_nodes_t
+    from casl_p4est_gb300.sharding import LeafPartition, ShardInterpBackend
+    build, phi0_of = GRIDS[name]
+    f = build()
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    ls = G.my_p4est_level_set_t(ngbd)
+    N, d, W = f.num_nodes, f.dim, 3
+    phi = phi0_of(f)
+    xyz = f.node_xyz()
+    v0 = np.sin(3 * xyz[:, 1]) * np.cos(2 * xyz[:, 0])
+    F = np.stack([phi, v0])
+    Fdd = np.stack([ls.compute_derivatives(phi), ls.compute_derivatives(v0)]).reshape(2, d, N)
+    rng = np.random.default_rng(5)
+    lo, hi = np.array(f.xyz_min[:d]), np.array(f.xyz_max[:d])
+    pts = lo - 0.02 + (hi - lo + 0.04) * rng.random((4000, d))
+    pts[:500] = xyz[rng.integers(0, N, 500)]
+    nb = [(N * r) // W for r in range(W + 1)]
+    lp = LeafPartition(f.local_nodes(), nb, W)
+    be = ShardInterpBackend(ls)
+    interp = my_p4est_interpolation_nodes_t(ls)
+    for method in (0, 2, 4):
+        ref = interp.interpolate_points(pts, F, method, None if method == 0 else Fdd)
+        copies = []
+        for r in range(W):
+            keep = np.zeros(N, bool)
+            keep[nb[r]:nb[r + 1]] = True
+            keep[lp.ghosts[r]] = True
+            Fr = np.where(keep, F, 1e30)
+            Fddr = np.where(keep, Fdd, 1e30)
+            copies.append((torch.from_numpy(Fr).cuda(), torch.from_numpy(np.ascontiguousarray(Fddr)).cuda()))
+        P = torch.from_numpy(pts).cuda()
+        owner = lp.owner_of_leaves(be.locate(P))
+        got = torch.empty((2, len(pts)), dtype=torch.float64, device="cuda")
+        for r in range(W):
+            sel = torch.nonzero(owner == r).flatten()
+            if len(sel):
+                got[:, sel] = be.interpolate(method, copies[r][0], None if method == 0 else copies[r][1], P[sel])
+        torch.cuda.synchronize()
+        assert np.array_equal(got.cpu().numpy(), ref), (name, method)
+        assert len(torch.unique(owner)) == W

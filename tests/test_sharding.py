@@ -213,3 +213,133 @@ def test_schedule_matches_the_reference_sweeps():
     # first order in space: the node's own second derivatives are still swept (the quadratic neighbour
     # values read them) but their ghosts are not exchanged
     assert [o[0] for o in reinit_schedule(1, 1, 2)] == ["dd", "prep", "dd", "stage", "exchange", "dd", "stage", "exchange"]
+
+
+# ---- interpolation at arbitrary points across a Morton split --------------------------------------
+from casl_p4est_gb300.sharding import LeafPartition, interpolate_sharded, sl_advect_sharded  # noqa: E402
+
+
+class OracleInterp:
+    """A rank's point location and interpolation on the CPU with the oracle (test infrastructure only)."""
+
+    def __init__(self, og):
+        self.og = og
+
+    def locate(self, xyz):
+        import torch
+        return torch.from_numpy(self.og.locate(xyz.numpy()).astype(np.int64))
+
+    def interpolate(self, method, F, Fdd, xyz):
+        import torch
+        if method != 0 and Fdd is None:
+            raise ValueError("second derivatives required")
+        out = self.og.interpolate(method, F.numpy(), xyz.numpy(), None if Fdd is None else Fdd.numpy())
+        return torch.from_numpy(np.ascontiguousarray(out).reshape(F.shape[0], -1))
+
+
+def _fields(f, og):
+    xyz = f.node_xyz()
+    d = f.dim
+    phi = np.sqrt(((xyz - 0.1) ** 2).sum(1)) - 0.45
+    v = np.stack([np.sin(3 * xyz[:, (a + 1) % d]) * (1.0 + 0.3 * a) for a in range(d)])
+    vdd = np.stack([og.compute_derivatives(v[a]) for a in range(d)])
+    return phi, og.compute_derivatives(phi), v, vdd
+
+
+def _query_points(f, n, seed):
+    rng = np.random.default_rng(seed)
+    lo, hi = np.array(f.xyz_min[:f.dim]), np.array(f.xyz_max[:f.dim])
+    pts = lo + (hi - lo) * rng.random((n, f.dim))
+    pts[: n // 8] = f.node_xyz()[rng.integers(0, f.num_nodes, n // 8)]  # points on nodes, faces and edges
+    pts[n // 8: n // 4] = lo - 0.05 + (hi - lo + 0.1) * rng.random((n // 4 - n // 8, f.dim))  # some outside: clipped
+    return pts
+
+
+def _interp_worker(rank, world, port, name, q):
+    import torch
+    import torch.distributed as dist
+    import casl_p4est_gb300 as G
+    import oracle as O
+    from casl_p4est_gb300.sharding import HaloExchange
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f, _ = _grid(name)
+        og = O.OracleGrid.from_forest(f)
+        N, d = og.N, f.dim
+        npart = MortonPartition(og.qnnn(G.qnnn_dtype(d)), world)
+        lpart = LeafPartition(f.local_nodes(), npart.bounds, world)
+        b, e = npart.bounds[rank], npart.bounds[rank + 1]
+        phi, phi_dd, v, vdd = _fields(f, og)
+
+        def mine(a):  # this rank's copy: its node range, POISON elsewhere until the exchange fills its ghosts
+            t = torch.full(a.shape, POISON, dtype=torch.float64)
+            t[..., b:e] = torch.from_numpy(np.ascontiguousarray(a[..., b:e]))
+            return t
+        F = mine(np.stack([phi, v[0]]))
+        Fdd = mine(np.stack([phi_dd, vdd[0]]))
+        V, Vdd, P, Pdd = mine(v), mine(vdd), mine(phi), mine(phi_dd)
+        ex = HaloExchange(lpart, rank)
+        for t, planes in ((F, 2), (Fdd, 2 * d), (V, d), (Vdd, d * d), (P, 1), (Pdd, d)):
+            ex(t.view(-1), planes)
+        # every rank asks for its own share of the query points
+        pts_all = _query_points(f, 3000, 11)
+        share = np.array_split(np.arange(len(pts_all)), world)[rank]
+        pts = torch.from_numpy(pts_all[share])
+        res = {}
+        for method in (0, 2, 4):
+            got = interpolate_sharded(lpart, rank, pts, OracleInterp(og), method, F, None if method == 0 else Fdd)
+            ref = og.interpolate(method, np.stack([phi, v[0]]), pts_all[share], None if method == 0 else np.stack([phi_dd, vdd[0]]))
+            res[method] = bool(np.array_equal(got.numpy(), ref))
+        # the semi-Lagrangian step for this rank's nodes of the same grid (the grid at n+1 equal to the grid at n)
+        xyz = torch.from_numpy(f.node_xyz()[b:e])
+        dt = 0.7 * float(f.dxyz_min()[1])
+        got = sl_advect_sharded(lpart, rank, xyz, dt, V, Vdd, P, Pdd, OracleInterp(og), f.xyz_min[:d], f.xyz_max[:d])
+        ref = og.sl_advect(f.node_xyz()[b:e], dt, v, phi, vdd=vdd, phi_dd=phi_dd)
+        res["sl"] = bool(np.array_equal(got.numpy(), ref))
+        res["forwarded"] = int(sum(len(x) for x in lpart.recv[rank].values()))
+        q.put((rank, res))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name,world", [("circle2d", 2), ("flower3d", 2), ("brick3d", 3)])
+def test_forwarded_interpolation_on_gloo_equals_one_rank(name, world):
+    """Points located in another rank's leaves are forwarded to it and the values sent back (the query/reply
+    exchange of my_p4est_interpolation_t): linear, quadratic non-oscillatory and continuous-v2 interpolation and
+    the semi-Lagrangian step on CPU ranks give the single-rank results bit for bit; each rank's copies of the
+    fields hold only its node range and the corner ghosts of its leaves."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_interp_worker, args=(r, world, port, name, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, r in res:
+        assert r[0] and r[2] and r[4] and r["sl"], (rank, r)
+        assert r["forwarded"] > 0
+
+
+def test_leaf_partition_ghosts_cover_every_leaf_corner():
+    import oracle as O
+    f, _ = _grid("flower3d")
+    og = O.OracleGrid.from_forest(f)
+    ln = f.local_nodes()
+    for world in (1, 2, 5):
+        nb = [(og.N * r) // world for r in range(world + 1)]
+        lp = LeafPartition(ln, nb, world)
+        assert lp.bounds[0] == 0 and lp.bounds[-1] == len(ln)
+        for r in range(world):
+            need = set(np.unique(ln[lp.bounds[r]:lp.bounds[r + 1]]).tolist())
+            have = set(range(nb[r], nb[r + 1])) | set(lp.ghosts[r].tolist())
+            assert need <= have
+            for s, idx in lp.send[r].items():
+                assert np.array_equal(idx, lp.recv[s][r])
+        owners = lp.owner_of_leaves(np.arange(len(ln)))
+        assert np.all(np.diff(owners) >= 0) and owners[0] == 0 and owners[-1] == world - 1
