@@ -468,10 +468,20 @@ __device__ __forceinline__ void uni_load(const DTab32<D>& T, int nR, const uint1
   I.st = ADV ? (uint16_t)0 : __ldcs(status + m);
   I.vn = ADV ? __ldcs(vn + m) : 0.0f;
   I.code = __ldcs(T.r_meta + m) & 15u;
+  // the 4D stencil indices with D vector loads from the node-major copy
+  int32_t w[4 * D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const int4 q = __ldcs(T.u_pack + (int64_t)D * m + k);
+    w[4 * k] = q.x;
+    w[4 * k + 1] = q.y;
+    w[4 * k + 2] = q.z;
+    w[4 * k + 3] = q.w;
+  }
 #pragma unroll
   for (int dir = 0; dir < 2 * D; ++dir) {
-    I.nb[dir] = __ldcs(T.r_nbr + dir * nR + m);
-    I.nb2[dir] = __ldcs(T.r_nbr2 + dir * nR + m);
+    I.nb[dir] = w[dir];
+    I.nb2[dir] = w[2 * D + dir];
   }
   I.f0 = __ldg(phin + m);
   I.avg = AVG ? __ldcs(avg_with + m) : 0.0f;
@@ -1325,6 +1335,23 @@ void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* d
     k_advect_stage32<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with);
 }
 
+template <int D>
+__global__ void k_pack_uniform32(DTab32<D> T, int4* __restrict__ out) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= T.nU) return;
+  int32_t w[4 * D];
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    w[dir] = T.r_nbr[dir * T.nR + m];
+    w[2 * D + dir] = T.r_nbr2[dir * T.nR + m];
+  }
+  for (int k = 0; k < D; ++k) out[(int64_t)D * m + k] = make_int4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+}
+
+template <int D>
+void launch_pack_uniform32(const DTab32<D>& T, int4* out, cudaStream_t s) {
+  if (T.nU > 0) k_pack_uniform32<D><<<nblocks(T.nU), TPB, 0, s>>>(T, out);
+}
+
 void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64_t n, int64_t src_stride, int64_t dst_stride,
                        int blocks, cudaStream_t s) {
   if (n) k_gather_f32<<<nblocks(n), TPB, 0, s>>>(src, perm, dst, n, src_stride, dst_stride, blocks);
@@ -1342,7 +1369,8 @@ void launch_scatter_f64(const float* src, const int32_t* perm, const uint16_t* s
                                          const float*, cudaStream_t);                                                           \
   template void launch_dd_x32<D>(const DTab32<D>&, const float*, float*, cudaStream_t, int);                                  \
   template void launch_reinit_part32<D>(const DTab32<D>&, int, int, const uint16_t*, const float*, const float*, const float*,  \
-                                        float*, const float*, cudaStream_t, const StageCfg&, int*, const float*, float);
+                                        float*, const float*, cudaStream_t, const StageCfg&, int*, const float*, float);        \
+  template void launch_pack_uniform32<D>(const DTab32<D>&, int4*, cudaStream_t);
 LSG_INST(2)
 LSG_INST(3)
 #undef LSG_INST
