@@ -110,8 +110,8 @@ struct DTab32 {
   float tsize[3];        // tree size per axis
   float inv_tsize[3];
   int64_t nU;            // regular nodes [0, nU) have uniform stencils
-  // the uniform nodes' face and second-neighbour indices node by node (D int4 per node: the 2D face indices,
-  // then the 2D second neighbours), so the uniform kernel loads them with D vector loads
+  // the regular nodes' face and second-neighbour indices node by node (D int4 per node: the 2D face indices,
+  // then the 2D second neighbours), so the uniform and regular stage kernels load them with D vector loads
   const int4* u_pack;
   const uint32_t* r_meta;
   const int32_t* r_nbr;  // 2D x nR
@@ -284,7 +284,7 @@ void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* d
                            float* out, const float* avg_with, cudaStream_t s);
 // node order (FP64) <-> device order (FP32): dst[b*dst_stride + i] = src[b*src_stride + perm[i]] and the
 // reverse scatter (skipping nodes whose status marks them outside the reinitialisation limits)
-// fills T.u_pack's layout (D int4 per uniform node) from the r_nbr / r_nbr2 planes
+// fills T.u_pack's layout (D int4 per regular node) from the r_nbr / r_nbr2 planes
 template <int D>
 void launch_pack_uniform32(const DTab32<D>& T, int4* out, cudaStream_t s);
 void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64_t n, int64_t src_stride, int64_t dst_stride,

@@ -374,10 +374,20 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     if (ADV) p_vn = __ldcs(vn + m);
     p_codes = __ldcs(T.r_meta + m);
     p_far = __ldcs(T.r_meta2 + m);
+    // the 4D stencil indices with D vector loads from the node-major copy
+    int32_t w[4 * D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const int4 q = __ldcs(T.u_pack + (int64_t)D * m + k);
+      w[4 * k] = q.x;
+      w[4 * k + 1] = q.y;
+      w[4 * k + 2] = q.z;
+      w[4 * k + 3] = q.w;
+    }
 #pragma unroll
     for (int dir = 0; dir < 2 * D; ++dir) {
-      p_nb[dir] = __ldcs(T.r_nbr + dir * nR + m);
-      if (ORDER_SPACE > 1) p_nb2[dir] = __ldcs(T.r_nbr2 + dir * nR + m);
+      p_nb[dir] = w[dir];
+      p_nb2[dir] = w[2 * D + dir];
     }
     p_f0 = __ldg(phin + m);
     if (AVG) p_avg = __ldcs(avg_with + m);
@@ -1338,7 +1348,7 @@ void launch_advect_stage32(const DTab32<D>& T, const float* phin, const float* d
 template <int D>
 __global__ void k_pack_uniform32(DTab32<D> T, int4* __restrict__ out) {
   const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= T.nU) return;
+  if (m >= T.nR) return;
   int32_t w[4 * D];
   for (int dir = 0; dir < 2 * D; ++dir) {
     w[dir] = T.r_nbr[dir * T.nR + m];
@@ -1349,7 +1359,7 @@ __global__ void k_pack_uniform32(DTab32<D> T, int4* __restrict__ out) {
 
 template <int D>
 void launch_pack_uniform32(const DTab32<D>& T, int4* out, cudaStream_t s) {
-  if (T.nU > 0) k_pack_uniform32<D><<<nblocks(T.nU), TPB, 0, s>>>(T, out);
+  if (T.nR > 0) k_pack_uniform32<D><<<nblocks(T.nR), TPB, 0, s>>>(T, out);
 }
 
 void launch_gather_f32(const double* src, const int32_t* perm, float* dst, int64_t n, int64_t src_stride, int64_t dst_stride,

@@ -580,10 +580,10 @@ void LevelSet<D>::set_mixed_views(int64_t nR_, int64_t nI_, int64_t nU_, int bas
   T32.i_d64 = i_d64.p;
   T32.i_q64 = i_q64.p;
   T32.corr64 = corr64.p;
-  // the uniform kernel's node-major copy of its stencil indices (D int4 per node, 16-byte aligned)
+  // the stage kernels' node-major copy of the regular nodes' stencil indices (D int4 per node, 16-byte aligned)
   T32.u_pack = nullptr;
-  if (nU_ > 0) {
-    u_pack.alloc((size_t)D * nU_);
+  if (nR_ > 0) {
+    u_pack.alloc((size_t)D * nR_);
     launch_pack_uniform32<D>(T32, u_pack.p, stream);
     cuda_check(cudaGetLastError(), "pack uniform indices");
     T32.u_pack = u_pack.p;

@@ -75,7 +75,7 @@ struct LevelSet {
   bool mixed_ready = false;
   DevBuf<uint32_t> r_meta, i_meta, r_meta2, i_cls;
   DevBuf<int32_t> r_nbr, r_nbr2, i_nbr, i_cidx, perm, iperm, near_list;
-  DevBuf<int4> u_pack;  // the uniform nodes' stencil indices node by node (DTab32::u_pack)
+  DevBuf<int4> u_pack;  // the regular nodes' stencil indices node by node (DTab32::u_pack)
   DevBuf<unsigned> near_count;
   DevBuf<float> i_wf, i_d, i_q, corr32, cls32;
   DevBuf<double> i_wf64, i_d64, i_q64, corr64;
