@@ -537,19 +537,21 @@ __device__ __forceinline__ float uni_update(const DTab32<D>& T, const float* __r
       const float xx0 = (fp + fm - 2.0f * f0) * ih2;
       const float mm = minmodf((f0 + fmm - 2.0f * fm) * ih2, xx0);
       const float mp = minmodf((fpp + f0 - 2.0f * fp) * ih2, xx0);
-      float gm, gp;
-      if (!near) {
-        gm = fmaf(0.5f * h, mm, (f0 - fm) * ih);
-        gp = fmaf(-0.5f * h, mp, (fp - f0) * ih);
-        smin = fminf(smin, h);
-      } else {
-        const float sm = __ldg(s_near + (int64_t)(2 * a) * T.N + V.n), sp = __ldg(s_near + (int64_t)(2 * a + 1) * T.N + V.n);
+      // one expression for both cases: away from the interface the distances are h and their reciprocal ih;
+      // an interface-adjacent node takes its subcell distances and the reciprocals of those, and a cut
+      // direction's neighbour value is the interface's zero
+      float sm = h, sp = h, im = ih, ip = ih;
+      if (near) {
+        sm = __ldg(s_near + (int64_t)(2 * a) * T.N + V.n);
+        sp = __ldg(s_near + (int64_t)(2 * a + 1) * T.N + V.n);
+        im = __fdividef(1.0f, sm);
+        ip = __fdividef(1.0f, sp);
         if (st & (1u << (ST_CUT_SHIFT + 2 * a))) fm = 0.0f;
         if (st & (1u << (ST_CUT_SHIFT + 2 * a + 1))) fp = 0.0f;
-        gm = fmaf(0.5f * sm, mm, __fdividef(f0 - fm, sm));
-        gp = fmaf(-0.5f * sp, mp, __fdividef(fp - f0, sp));
-        smin = fminf(smin, fminf(sm, sp));
       }
+      float gm = fmaf(0.5f * sm, mm, (f0 - fm) * im);
+      float gp = fmaf(-0.5f * sp, mp, (fp - f0) * ip);
+      smin = fminf(smin, fminf(sm, sp));
       if (sgn * gp > 0.0f) gp = 0.0f;
       if (sgn * gm < 0.0f) gm = 0.0f;
       hsum += ADV ? gp * gp + gm * gm : fmaxf(gp * gp, gm * gm);
