@@ -28,6 +28,10 @@ __device__ __forceinline__ int face_count(uint32_t meta, int dir) { return (int)
 __device__ __forceinline__ float level_size(float tsize, int base, uint32_t code) {
   return __int_as_float(__float_as_int(tsize) - ((base + (int)code) << 23));
 }
+// its reciprocal, exact: the reciprocal tree size with the exponent raised by the level
+__device__ __forceinline__ float level_inv(float inv_tsize, int base, uint32_t code) {
+  return __int_as_float(__float_as_int(inv_tsize) + ((base + (int)code) << 23));
+}
 
 template <int D>
 struct Reg {  // regular-node view
@@ -105,7 +109,8 @@ __global__ void __launch_bounds__(TPB) k_dd32(DTab32<D> T, const float* __restri
 
 // Godunov update shared by both groups (reinitialize_one_iteration after the neighbour values).
 template <int D, int ORDER_SPACE>
-__device__ __forceinline__ float reinit_update(float f0, const float* fnb, const float* s, const float* xx0, const float* xxnb, bool pos) {
+__device__ __forceinline__ float reinit_update(float f0, const float* fnb, const float* s, const float* is, const float* xx0,
+                                             const float* xxnb, bool pos) {
   const float sgn = pos ? 1.0f : -1.0f;
   float dt = fminf(s[0], s[1]);
 #pragma unroll
@@ -114,8 +119,8 @@ __device__ __forceinline__ float reinit_update(float f0, const float* fnb, const
   float h = 0.0f;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    float gp = __fdividef(fnb[2 * a + 1] - f0, s[2 * a + 1]);
-    float gm = __fdividef(f0 - fnb[2 * a], s[2 * a]);
+    float gp = (fnb[2 * a + 1] - f0) * is[2 * a + 1];
+    float gm = (f0 - fnb[2 * a]) * is[2 * a];
     if (ORDER_SPACE > 1) {
       gm = fmaf(0.5f * s[2 * a], minmodf(xxnb[2 * a], xx0[a]), gm);
       gp = fmaf(-0.5f * s[2 * a + 1], minmodf(xxnb[2 * a + 1], xx0[a]), gp);
@@ -132,14 +137,14 @@ __device__ __forceinline__ float reinit_update(float f0, const float* fnb, const
 // advect_in_normal_direction_one_iteration's update after the neighbour values (src/my_p4est_level_set.cpp:559-654):
 // one-sided slopes with the minmod terms, upwinding by the sign of vn, phi - dt vn sqrt(sum gp^2 + gm^2)
 template <int D>
-__device__ __forceinline__ float advect_update(float f0, const float* fnb, const float* s, const float* xx0, const float* xxnb, float v,
-                                               float dt) {
+__device__ __forceinline__ float advect_update(float f0, const float* fnb, const float* s, const float* is, const float* xx0,
+                                               const float* xxnb, float v, float dt) {
   const float sgn = v > 0.0f ? 1.0f : -1.0f;
   float h = 0.0f;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    float gp = __fdividef(fnb[2 * a + 1] - f0, s[2 * a + 1]);
-    float gm = __fdividef(f0 - fnb[2 * a], s[2 * a]);
+    float gp = (fnb[2 * a + 1] - f0) * is[2 * a + 1];
+    float gm = (f0 - fnb[2 * a]) * is[2 * a];
     gm = fmaf(0.5f * s[2 * a], minmodf(xxnb[2 * a], xx0[a]), gm);
     gp = fmaf(-0.5f * s[2 * a + 1], minmodf(xxnb[2 * a + 1], xx0[a]), gp);
     if (sgn * gp > 0.0f) gp = 0.0f;
@@ -346,7 +351,11 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused32(DTab32<D> T, const uint1
         }
       }
     }
-    r = ADV ? advect_update<D>(f0, fnb, s, Dv, xxnb, v, adv_dt) : reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+    float is[2 * D];
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) is[dir] = __fdividef(1.0f, s[dir]);
+    r = ADV ? advect_update<D>(f0, fnb, s, is, Dv, xxnb, v, adv_dt)
+              : reinit_update<D, ORDER_SPACE>(f0, fnb, s, is, Dv, xxnb, (st & ST_POSITIVE) != 0);
   }
   if (AVG) r = 0.5f * (avg_with[n] + r);
   out[n] = r;
@@ -412,12 +421,13 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
     } else {
       // one round of gathers: every face value and, per direction, the second neighbour's value or
       // (when the face node has none recorded) the face node's second derivative along the axis
-      float Dv[D], fnb[2 * D], s[2 * D], xxnb[2 * D], fx[2 * D];
+      float Dv[D], fnb[2 * D], s[2 * D], is[2 * D], xxnb[2 * D], fx[2 * D];
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
         fnb[dir] = __ldg(phin + nb[dir]);
         if (ORDER_SPACE > 1) fx[dir] = __ldg(nb2[dir] >= 0 ? phin + nb2[dir] : dd_irr + (int64_t)(dir >> 1) * T.N + nb[dir]);
         s[dir] = level_size(T.tsize[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
+        is[dir] = level_inv(T.inv_tsize[dir >> 1], T.base, (codes >> (4 * dir)) & 15u);
       }
 #pragma unroll
       for (int a = 0; a < D; ++a) Dv[a] = central_dd(fnb[2 * a + 1], f0, fnb[2 * a], s[2 * a + 1], s[2 * a]);
@@ -437,10 +447,12 @@ __global__ void __launch_bounds__(TPB) k_reinit_fused_reg32(DTab32<D> T, const u
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) {
           s[dir] = __ldg(s_near + (int64_t)dir * T.N + n);
+          is[dir] = __fdividef(1.0f, s[dir]);
           if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0f;
         }
       }
-      r = ADV ? advect_update<D>(f0, fnb, s, Dv, xxnb, v, adv_dt) : reinit_update<D, ORDER_SPACE>(f0, fnb, s, Dv, xxnb, (st & ST_POSITIVE) != 0);
+      r = ADV ? advect_update<D>(f0, fnb, s, is, Dv, xxnb, v, adv_dt)
+              : reinit_update<D, ORDER_SPACE>(f0, fnb, s, is, Dv, xxnb, (st & ST_POSITIVE) != 0);
     }
     if (AVG) r = 0.5f * (avg + r);
     out[n] = r;
