@@ -71,6 +71,10 @@ struct DTab64 {
   const int32_t* cidx;  // N
   const double* crec;   // 6 x R
   const uint8_t* wall;  // N
+  // per node (tables in stencil-pattern order only, else null): bits 2dir..2dir+1 face-node count - 1, bit 12 a
+  // correction record, bits 13.. the wall bits, bit 20 + dir a single face node whose weight equals the norm and
+  // is a power of two in [2^-400, 2^400], bit 26 + dir no tangential correction (both factors zero)
+  const uint32_t* word = nullptr;
 };
 
 // First-derivative correction records (build_gradient_tables): record index per node (-1: none),
@@ -148,6 +152,9 @@ struct Tab64Out {
   uint8_t* wall;
 };
 size_t sort64_temp_bytes(int64_t n);
+// fills DTab64::word for tables in stencil-pattern order
+template <int D>
+void launch_node_word64(const DTab64<D>& T, uint32_t* word, cudaStream_t s);
 template <int D>
 cudaError_t launch_sort_tab64(const DTab64<D>& T, uint32_t* keys, uint32_t* keys_out, int32_t* idx, void* temp, size_t temp_bytes,
                               int32_t* perm, int32_t* iperm, const Tab64Out& out, cudaStream_t s);

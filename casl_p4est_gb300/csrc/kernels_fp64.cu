@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
 #pragma unroll
     for (int a = 0; a < D; ++a) Dv[a] = dd[(int64_t)a * N + n];
     double fnb[2 * D], s[2 * D], xx0[D], xxnb[2 * D];
+    const NodeWord nw = node_word<D>(T, n);
 #pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dv);
+    for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dv, nw);
     if (st & ST_NEAR) {
 #pragma unroll
       for (int dir = 0; dir < 2 * D; ++dir) {
@@ -133,8 +134,8 @@ __global__ void __launch_bounds__(TPB, 2) k_reinit_stage64(DTab64<D> T, const ui
 #pragma unroll
       for (int a = 0; a < D; ++a) {
         xx0[a] = Dv[a];
-        xxnb[2 * a] = lin64<D>(T, 2 * a, n, dd + (int64_t)a * N);
-        xxnb[2 * a + 1] = lin64<D>(T, 2 * a + 1, n, dd + (int64_t)a * N);
+        xxnb[2 * a] = lin64w<D>(T, 2 * a, n, dd + (int64_t)a * N, nw);
+        xxnb[2 * a + 1] = lin64w<D>(T, 2 * a + 1, n, dd + (int64_t)a * N, nw);
       }
     }
     const uint8_t wl = T.wall[n];
@@ -199,16 +200,17 @@ __global__ void __launch_bounds__(TPB) k_advect_stage64(DTab64<D> T, const doubl
 #pragma unroll
   for (int a = 0; a < D; ++a) Dq[a] = ddq[(int64_t)a * N + n];
   double fnb[2 * D], s[2 * D], xx0[D], xxnb[2 * D];
+  const NodeWord nw = node_word<D>(T, n);
 #pragma unroll
   for (int dir = 0; dir < 2 * D; ++dir) {
-    fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dq);
+    fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dq, nw);
     s[dir] = T.d[(int64_t)dir * N + n];
   }
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     xx0[a] = ddm[(int64_t)a * N + n];
-    xxnb[2 * a] = lin64<D>(T, 2 * a, n, ddm + (int64_t)a * N);
-    xxnb[2 * a + 1] = lin64<D>(T, 2 * a + 1, n, ddm + (int64_t)a * N);
+    xxnb[2 * a] = lin64w<D>(T, 2 * a, n, ddm + (int64_t)a * N, nw);
+    xxnb[2 * a + 1] = lin64w<D>(T, 2 * a + 1, n, ddm + (int64_t)a * N, nw);
   }
   const uint8_t wl = T.wall[n];
 #pragma unroll
@@ -959,6 +961,36 @@ __global__ void k_pattern_key64(DTab64<D> T, uint32_t* __restrict__ key, int32_t
   key[n] = k;
   idx[n] = (int32_t)n;
 }
+// the pattern word of every node of tables in stencil-pattern order (DTab64::word)
+template <int D>
+__global__ void k_node_word64(DTab64<D> T, uint32_t* __restrict__ word) {
+  constexpr int H = Dim<D>::HALF;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= T.N) return;
+  const int64_t N = T.N;
+  uint32_t k = 0;
+  for (int dir = 0; dir < 2 * D; ++dir) {
+    int cnt = 0;
+    for (int j = 0; j < H; ++j) cnt += T.nbr[(int64_t)(dir * H + j) * N + n] >= 0 ? 1 : 0;
+    k |= (uint32_t)(cnt > 0 ? cnt - 1 : 0) << (2 * dir);
+    bool single = T.nbr[(int64_t)(dir * H) * N + n] >= 0;
+    for (int j = 1; j < H; ++j) single = single && T.nbr[(int64_t)(dir * H + j) * N + n] < 0;
+    if (single) {
+      const unsigned long long bw = bits_of(T.w[(int64_t)(dir * H) * N + n]);
+      const int ew = (int)(bw >> 52);  // a positive weight: no sign bit
+      if (bw == bits_of(T.nrm[(int64_t)dir * N + n]) && (bw & 0x000fffffffffffffull) == 0 && ew >= 623 && ew <= 1423)
+        k |= 1u << (20 + dir);
+    }
+    bool nocorr;
+    if (D == 2) nocorr = !nonzero(T.q[(int64_t)dir * N + n]);
+    else nocorr = !nonzero(T.q[(int64_t)(2 * dir) * N + n]) && !nonzero(T.q[(int64_t)(2 * dir + 1) * N + n]);
+    if (nocorr) k |= 1u << (26 + dir);
+  }
+  if (T.cidx[n] >= 0) k |= 1u << 12;
+  k |= (uint32_t)T.wall[n] << 13;
+  word[n] = k;
+}
+
 __global__ void k_inverse_perm(const int32_t* __restrict__ perm, int32_t* __restrict__ iperm, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) iperm[perm[i]] = (int32_t)i;
@@ -1018,6 +1050,11 @@ cudaError_t launch_sort_tab64(const DTab64<D>& T, uint32_t* keys, uint32_t* keys
   return cudaGetLastError();
 }
 
+template <int D>
+void launch_node_word64(const DTab64<D>& T, uint32_t* word, cudaStream_t s) {
+  if (T.N) k_node_word64<D><<<nblocks(T.N), TPB, 0, s>>>(T, word);
+}
+
 void launch_gather_perm64(const double* src, const int32_t* perm, double* dst, int64_t n, cudaStream_t s) {
   if (n) k_gather_perm64<<<nblocks(n), TPB, 0, s>>>(src, perm, dst, n);
 }
@@ -1026,6 +1063,7 @@ void launch_scatter_perm64(const double* src, const int32_t* perm, double* dst, 
 }
 
 #define LSG_INST(D)                                                                                                          \
+  template void launch_node_word64<D>(const DTab64<D>&, uint32_t*, cudaStream_t);                                             \
   template cudaError_t launch_sort_tab64<D>(const DTab64<D>&, uint32_t*, uint32_t*, int32_t*, void*, size_t, int32_t*, int32_t*, \
                                             const Tab64Out&, cudaStream_t);                                                  \
   template void launch_dd64<D>(const DTab64<D>&, const double*, double*, cudaStream_t, int64_t, int64_t);                    \

@@ -412,6 +412,16 @@ bool LevelSet<D>::ensure_sorted64() {
   T64s.q = s_q.p;
   T64s.cidx = s_cidx.p;
   T64s.wall = s_wall.p;
+  T64s.word = nullptr;
+  // the per-node pattern word; without the memory for it the sweeps read the full stencil of every face
+  try {
+    s_word.alloc(N);
+    launch_node_word64<D>(T64s, s_word.p, stream);
+    cuda_check(cudaGetLastError(), "node pattern words");
+    T64s.word = s_word.p;
+  } catch (const CudaOutOfMemory&) {
+    s_word.release();
+  }
   sorted64_ready = true;
   return true;
 }

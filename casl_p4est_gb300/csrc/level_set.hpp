@@ -68,6 +68,7 @@ struct LevelSet {
   bool sorted64_ready = false, sorted64_failed = false;
   DevBuf<int32_t> s_perm, s_iperm, s_nbr, s_cidx;
   DevBuf<double> s_w, s_nrm, s_d, s_q, s_phi, s_vn, s_vn1, s_dd;  // s_vn..s_dd: advection inputs in pattern order
+  DevBuf<uint32_t> s_word;  // per-node pattern word of the sorted tables (DTab64::word)
   DevBuf<uint8_t> s_wall;
   DTab64<D> T64s{};
   bool ensure_sorted64();

@@ -158,6 +158,30 @@ __device__ __forceinline__ double lin64(const DTab64<D>& T, int dir, int64_t n, 
   return qdiv(acc, nrm);
 }
 
+// The node's pattern word (DTab64::word) when the tables carry one: which faces have one face node of unit
+// weight and which need no tangential correction, so those faces load one index and one value instead of the
+// H indices, the weight, the norm and the two correction factors.
+struct NodeWord {
+  uint32_t w;
+  bool known;
+};
+template <int D>
+__device__ __forceinline__ NodeWord node_word(const DTab64<D>& T, int64_t n) {
+  return NodeWord{T.word ? __ldg(T.word + n) : 0u, T.word != nullptr};
+}
+// lin64 with the pattern word: a single face node of unit weight gives its value itself when that value's exponent
+// keeps f w normal for every weight in [2^-400, 2^400] (|f| in [2^-622, 2^622]); anything else takes lin64
+template <int D>
+__device__ __forceinline__ double lin64w(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f, NodeWord nw) {
+  constexpr int H = Dim<D>::HALF;
+  if (nw.known && ((nw.w >> (2 * dir)) & 3u) == 0 && ((nw.w >> (20 + dir)) & 1u)) {
+    const double f0 = f[T.nbr[(int64_t)(dir * H) * T.N + n]];
+    const int ef = (int)((bits_of(f0) >> 52) & 0x7ffu);
+    if (ef >= 401 && ef <= 1645) return f0;
+  }
+  return lin64<D>(T, dir, n, f);
+}
+
 // correct_naive_second_derivatives (src/my_p4est_quad_neighbor_nodes_of_node.cpp:44-298), all branches.
 template <int D>
 __device__ void correct64(const double* __restrict__ m, double* Dv) {
@@ -248,13 +272,15 @@ template <int D>
 __device__ __forceinline__ void laplace64(const DTab64<D>& T, int64_t n, const double* __restrict__ f, double* Dv) {
   const int64_t N = T.N;
   const double f0 = f[n];
+  const NodeWord nw = node_word<D>(T, n);
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    const double fm = lin64<D>(T, 2 * a, n, f);
-    const double fp = lin64<D>(T, 2 * a + 1, n, f);
+    const double fm = lin64w<D>(T, 2 * a, n, f, nw);
+    const double fp = lin64w<D>(T, 2 * a + 1, n, f, nw);
     const double dm = T.d[(int64_t)(2 * a) * N + n], dp = T.d[(int64_t)(2 * a + 1) * N + n];
     Dv[a] = qdiv(scale2(qdiv(fp - f0, dp) + qdiv(fm - f0, dm), 1), dp + dm);
   }
+  if (nw.known && !((nw.w >> 12) & 1u)) return;  // no correction record
   const int32_t ci = T.cidx[n];
   if (ci >= 0) correct64<D>(T.crec + (int64_t)6 * ci, Dv);
 }
@@ -266,9 +292,11 @@ __device__ __forceinline__ int tan_axis(int axis, int j) {
 
 // ngbd_with_quadratic_interpolation: f_dir -= (0.5 d_m0 d_p0 f_t1t1 [+ 0.5 d_0m d_0p f_t2t2]).
 template <int D>
-__device__ __forceinline__ double quad_nb64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f, const double* Dv) {
+__device__ __forceinline__ double quad_nb64(const DTab64<D>& T, int dir, int64_t n, const double* __restrict__ f, const double* Dv,
+                                           NodeWord nw = NodeWord{0u, false}) {
   const int64_t N = T.N;
-  double v = lin64<D>(T, dir, n, f);
+  double v = lin64w<D>(T, dir, n, f, nw);
+  if (nw.known && ((nw.w >> (26 + dir)) & 1u)) return v;  // both correction factors zero
   const int axis = dir >> 1;
   if (D == 2) {
     const double q0 = T.q[(int64_t)dir * N + n];
