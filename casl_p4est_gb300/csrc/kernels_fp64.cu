@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
 // Two blocks per SM (at most 128 registers, a few bytes spilled): with one block of 146 registers the
 // FP64 pipe waited on MUFU and division sequences with only 8 warps to switch between.
 template <int D, int ORDER_SPACE, bool AVG>
-__global__ void __launch_bounds__(TPB, 4) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
+__global__ void __launch_bounds__(TPB, 5) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
                                                         const double* __restrict__ phi0, const double* __restrict__ phin,
                                                         const double* __restrict__ dd, double* out, const double* avg_with,
                                                         int64_t first, int64_t last) {
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(TPB, 4) k_reinit_stage64(DTab64<D> T, const ui
 }
 
 template <int D, bool AVG>
-__global__ void __launch_bounds__(TPB, 3) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
+__global__ void __launch_bounds__(TPB, 4) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
                                                         const double* __restrict__ ddm, const double* __restrict__ vn, double dt,
                                                         double* out, const double* avg_with) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
