@@ -153,9 +153,10 @@ def interpolate_sharded(lpart: LeafPartition, rank: int, xyz, backend, method, F
     nf = F.shape[0]
     owner = lpart.owner_of_leaves(backend.locate(xyz))
     sel = {p: torch.nonzero(owner == p).flatten() for p in range(world)}
-    # the number of points each peer forwards here (the reduce-scatter of the reference's senders count)
-    counts_out = {p: torch.tensor([len(sel[p])], dtype=torch.int64) for p in range(world) if p != rank}
-    counts_in = _exchange_sized(world, rank, counts_out, lambda p: torch.zeros(1, dtype=torch.int64))
+    # the number of points each peer forwards here (the reduce-scatter of the reference's senders count); on the
+    # points' device, as NCCL wants CUDA tensors
+    counts_out = {p: torch.tensor([len(sel[p])], dtype=torch.int64, device=xyz.device) for p in range(world) if p != rank}
+    counts_in = _exchange_sized(world, rank, counts_out, lambda p: torch.zeros(1, dtype=torch.int64, device=xyz.device))
     n_in = {p: int(counts_in[p].item()) for p in counts_in}
     # queries: the points themselves
     pts_in = _exchange_sized(world, rank, {p: xyz[sel[p]].to(torch.float64) for p in counts_out},
