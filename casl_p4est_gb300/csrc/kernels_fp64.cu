@@ -94,13 +94,14 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
   status[n] = st;
 }
 
-// Five blocks per SM (at most 48 registers; about 300 bytes of a thread's state spill to L1): once the pattern word
-// and the exponent arithmetic had taken most of the FP64 work off the pipe, the kernel waited on its loads, and more
-// resident warps hide them better (per launch on 13.7M nodes: 2 blocks 3.46 ms, 3 blocks 2.75, 4 blocks 2.33,
-// 5 blocks 2.20, 6 blocks 2.21). The second-derivative sweep runs at six (40 registers) and the advection stage at
-// five for the same reason.
+// Six blocks per SM (at most 40 registers; a few hundred bytes of a thread's state spill to L1): once the pattern
+// word and the exponent arithmetic had taken most of the FP64 work off the pipe, the kernel waited on its loads, and
+// more resident warps hide them better (per launch on 13.7M nodes, all axes at once: 2 blocks 3.46 ms, 3 blocks
+// 2.75, 4 blocks 2.33, 5 blocks 2.20, 6 blocks 2.21; one axis at a time, fewer values live: 5 blocks 2.18, 6 blocks
+// 2.16). The second-derivative sweep runs at six blocks (40 registers) and the advection stage at five for the same
+// reason.
 template <int D, int ORDER_SPACE, bool AVG>
-__global__ void __launch_bounds__(TPB, 5) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
+__global__ void __launch_bounds__(TPB, 6) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
                                                         const double* __restrict__ phi0, const double* __restrict__ phin,
                                                         const double* __restrict__ dd, double* out, const double* avg_with,
                                                         int64_t first, int64_t last) {
@@ -119,71 +120,59 @@ __global__ void __launch_bounds__(TPB, 5) k_reinit_stage64(DTab64<D> T, const ui
     double Dv[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) Dv[a] = dd[(int64_t)a * N + n];
-    double fnb[2 * D], s[2 * D], xx0[D], xxnb[2 * D];
     const NodeWord nw = node_word<D>(T, n);
-#pragma unroll
-    for (int dir = 0; dir < 2 * D; ++dir) fnb[dir] = quad_nb64<D>(T, dir, n, phin, Dv, nw);
-    if (st & ST_NEAR) {
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        s[dir] = s_near[(int64_t)dir * N + n];
-        if (st & (1u << (ST_CUT_SHIFT + dir))) fnb[dir] = 0.0;
-      }
-    } else {
-#pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) s[dir] = T.d[(int64_t)dir * N + n];
-    }
-    if (ORDER_SPACE > 1) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        xx0[a] = Dv[a];
-        xxnb[2 * a] = lin64w<D>(T, 2 * a, n, dd + (int64_t)a * N, nw);
-        xxnb[2 * a + 1] = lin64w<D>(T, 2 * a + 1, n, dd + (int64_t)a * N, nw);
-      }
-    }
+    const bool near = (st & ST_NEAR) != 0;
     const uint8_t wl = T.wall[n];
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      if (wl & (1u << (2 * a))) {
-        s[2 * a] = s[2 * a + 1];
-        fnb[2 * a] = fnb[2 * a + 1];
-        if (ORDER_SPACE > 1) xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
-      }
-      if (wl & (1u << (2 * a + 1))) {
-        s[2 * a + 1] = s[2 * a];
-        fnb[2 * a + 1] = fnb[2 * a];
-        if (ORDER_SPACE > 1) xx0[a] = xxnb[2 * a] = xxnb[2 * a + 1] = 0.0;
-      }
-    }
-    double gp[D], gm[D];
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      gp[a] = qdiv(fnb[2 * a + 1] - f0, s[2 * a + 1]);
-      gm[a] = qdiv(f0 - fnb[2 * a], s[2 * a]);
-    }
-    if (ORDER_SPACE > 1) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        const double xm = minmod_x(xxnb[2 * a], xx0[a]);
-        gm[a] = gm[a] + scale2(s[2 * a], -1) * xm;
-        const double xp = minmod_x(xxnb[2 * a + 1], xx0[a]);
-        gp[a] = gp[a] - scale2(s[2 * a + 1], -1) * xp;
-      }
-    }
     // sgn = (p0 > 0 ? 1 : -1): the prep step stored p0 > 0 as ST_POSITIVE; sgn * g is +-g exactly, so the
     // upwind tests are sign tests of g
     const bool pos = (st & ST_POSITIVE) != 0;
-    double dt = min2x(s[0], s[1]);
-    dt = min3x(dt, s[2], s[3]);
-    if (D == 3) dt = min3x(dt, s[4 % (2 * D)], s[5 % (2 * D)]);
-    dt = D == 3 ? div3(dt) : qdiv(dt, (double)D);
+    // one axis at a time (the same operations on the same values as all axes at once, and the sum and the
+    // minimum accumulated in the same order), so that only one axis's values are live
+    double h = 0.0, dt = 0.0;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      if (pos ? positive(gp[a]) : negative(gp[a])) gp[a] = 0.0;  // sgn * gp > 0
-      if (pos ? negative(gm[a]) : positive(gm[a])) gm[a] = 0.0;  // sgn * gm < 0
+      double fm = quad_nb64<D>(T, 2 * a, n, phin, Dv, nw), fp = quad_nb64<D>(T, 2 * a + 1, n, phin, Dv, nw);
+      double sm, sp;
+      if (near) {
+        sm = s_near[(int64_t)(2 * a) * N + n];
+        sp = s_near[(int64_t)(2 * a + 1) * N + n];
+        if (st & (1u << (ST_CUT_SHIFT + 2 * a))) fm = 0.0;
+        if (st & (1u << (ST_CUT_SHIFT + 2 * a + 1))) fp = 0.0;
+      } else {
+        sm = T.d[(int64_t)(2 * a) * N + n];
+        sp = T.d[(int64_t)(2 * a + 1) * N + n];
+      }
+      double x0 = 0.0, xm_nb = 0.0, xp_nb = 0.0;
+      if (ORDER_SPACE > 1) {
+        x0 = Dv[a];
+        xm_nb = lin64w<D>(T, 2 * a, n, dd + (int64_t)a * N, nw);
+        xp_nb = lin64w<D>(T, 2 * a + 1, n, dd + (int64_t)a * N, nw);
+      }
+      if (wl & (1u << (2 * a))) {
+        sm = sp;
+        fm = fp;
+        x0 = xm_nb = xp_nb = 0.0;
+      }
+      if (wl & (1u << (2 * a + 1))) {
+        sp = sm;
+        fp = fm;
+        x0 = xm_nb = xp_nb = 0.0;
+      }
+      double gp = qdiv(fp - f0, sp);
+      double gm = qdiv(f0 - fm, sm);
+      if (ORDER_SPACE > 1) {
+        const double xm = minmod_x(xm_nb, x0);
+        gm = gm + scale2(sm, -1) * xm;
+        const double xp = minmod_x(xp_nb, x0);
+        gp = gp - scale2(sp, -1) * xp;
+      }
+      dt = a == 0 ? min2x(sm, sp) : min3x(dt, sm, sp);
+      if (pos ? positive(gp) : negative(gp)) gp = 0.0;  // sgn * gp > 0
+      if (pos ? negative(gm) : positive(gm)) gm = 0.0;  // sgn * gm < 0
+      const double ha = max2x(gp * gp, gm * gm);
+      h = a == 0 ? ha : h + ha;
     }
-    double h = max2x(gp[0] * gp[0], gm[0] * gm[0]) + max2x(gp[1] * gp[1], gm[1] * gm[1]);
-    if (D == 3) h = h + max2x(gp[2 % D] * gp[2 % D], gm[2 % D] * gm[2 % D]);
+    dt = D == 3 ? div3(dt) : qdiv(dt, (double)D);
     r = f0 - times_sign(dt, pos) * (sqrt(h) - 1.);
     if (product_negative(p0, r)) r = neg1(r);
   }
