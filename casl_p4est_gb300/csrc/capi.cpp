@@ -1226,6 +1226,16 @@ int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const doub
   });
 }
 
+int lsg_advect_stage_range_device(lsg_level_set* ls, const double* phin_dev, const double* phin_dd_dev, const double* minmod_dd_dev,
+                                  const double* vn_dev, double dt, double* out_dev, const double* avg_with_dev, int64_t first,
+                                  int64_t count) {
+  return guard([&] {
+    need(phin_dev != nullptr && phin_dd_dev != nullptr && minmod_dd_dev != nullptr && vn_dev != nullptr && out_dev != nullptr,
+         "null argument");
+    with_ls(ls, [&](auto& L) { L.fp64_advect_stage_range(phin_dev, phin_dd_dev, minmod_dd_dev, vn_dev, dt, out_dev, avg_with_dev, first, count); });
+  });
+}
+
 int lsg_interface_location_error_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double* out, int64_t* edges,
                                         int64_t* mismatched) {
   return guard([&] {

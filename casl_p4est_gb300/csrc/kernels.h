@@ -168,9 +168,10 @@ template <int D>
 void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* status, const double* s_near, const double* phi0,
                            const double* phin, const double* dd, double* out, const double* avg_with, cudaStream_t s,
                            int64_t first = 0, int64_t count = -1);
+// over the nodes [first, first + count) (count < 0: to the last node), by default all of them
 template <int D>
 void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double* ddq, const double* ddm, const double* vn, double dt,
-                           double* out, const double* avg_with, cudaStream_t s);
+                           double* out, const double* avg_with, cudaStream_t s, int64_t first = 0, int64_t count = -1);
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s);
 void launch_min_cfl(const double* smin, const double* vn, int64_t n, double* dt_out_dev, cudaStream_t s);
 // First derivatives (FP64, the reference's expression order). fdd: second derivatives of f (D x N,

@@ -183,10 +183,10 @@ __global__ void __launch_bounds__(TPB, 6) k_reinit_stage64(DTab64<D> T, const ui
 template <int D, bool AVG>
 __global__ void __launch_bounds__(TPB, 5) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
                                                         const double* __restrict__ ddm, const double* __restrict__ vn, double dt,
-                                                        double* out, const double* avg_with) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                        double* out, const double* avg_with, int64_t first, int64_t last) {
+  const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t N = T.N;
-  if (n >= N) return;
+  if (n >= last) return;
   const double f0 = phin[n];
   double Dq[D];
 #pragma unroll
@@ -907,12 +907,13 @@ void launch_reinit_stage64(const DTab64<D>& T, int order_space, const uint16_t* 
 
 template <int D>
 void launch_advect_stage64(const DTab64<D>& T, const double* phin, const double* ddq, const double* ddm, const double* vn, double dt,
-                           double* out, const double* avg_with, cudaStream_t s) {
-  if (T.N == 0) return;
+                           double* out, const double* avg_with, cudaStream_t s, int64_t first, int64_t count) {
+  const int64_t last = count < 0 ? T.N : first + count;
+  if (last <= first) return;
   if (avg_with)
-    k_advect_stage64<D, true><<<nblocks(T.N), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with);
+    k_advect_stage64<D, true><<<nblocks(last - first), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with, first, last);
   else
-    k_advect_stage64<D, false><<<nblocks(T.N), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with);
+    k_advect_stage64<D, false><<<nblocks(last - first), TPB, 0, s>>>(T, phin, ddq, ddm, vn, dt, out, avg_with, first, last);
 }
 
 void launch_copy64(const double* src, double* dst, int64_t n, cudaStream_t s) {
@@ -1065,7 +1066,7 @@ void launch_scatter_perm64(const double* src, const int32_t* perm, double* dst, 
   template void launch_reinit_stage64<D>(const DTab64<D>&, int, const uint16_t*, const double*, const double*, const double*, \
                                          const double*, double*, const double*, cudaStream_t, int64_t, int64_t);             \
   template void launch_advect_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, double,  \
-                                         double*, const double*, cudaStream_t);                                              \
+                                         double*, const double*, cudaStream_t, int64_t, int64_t);                                              \
   template void launch_grad64<D>(const DTab64<D>&, const DGrad&, const double*, const double*, double*, int, cudaStream_t);      \
   template void launch_efi_stage64<D>(const DTab64<D>&, const double*, const double*, const double*, const double*, const double*,  \
                                       const double*, const double*, const uint8_t*, double, bool, double*, cudaStream_t);          \

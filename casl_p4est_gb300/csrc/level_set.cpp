@@ -502,6 +502,18 @@ void LevelSet<D>::fp64_stage_range(int os, const double* phi0_, const double* ph
   cuda_check(cudaGetLastError(), "reinitialize stage (node range)");
 }
 
+// one advect_in_normal_direction_one_iteration sweep over the nodes [first, first + count), node-ordered tables
+// (the per-rank sweep of a Morton-range split): ddq the second derivatives of phin (its quadratic neighbour values),
+// ddm those of the minmod terms, out = phin - dt vn |grad|, averaged with avg_with when given
+template <int D>
+void LevelSet<D>::fp64_advect_stage_range(const double* phin, const double* ddq, const double* ddm, const double* vn, double dt, double* out,
+                                          const double* avg_with, int64_t first, int64_t count) {
+  check_range(first, count, N);
+  if (!phin || !ddq || !ddm || !vn || !out) throw std::invalid_argument("advection stage: phi_n, both second derivatives, vn and out are required");
+  LSG_LAUNCH(K_ADVECT64, launch_advect_stage64<D>(T64, phin, ddq, ddm, vn, dt, out, avg_with, stream, first, count));
+  cuda_check(cudaGetLastError(), "advection stage (node range)");
+}
+
 template <int D>
 void LevelSet<D>::build_mixed() {
   if (mixed_ready) return;

@@ -160,6 +160,8 @@ struct LevelSet {
   // current with its halo exchange. prep: status and subcell distances from phi_0 (kept in this object)
   // with the caller's phi_0 limits; stage: out = stage(phin) or 0.5 (avg_with + stage(phin)).
   void fp64_dd_range(const double* f, double* dd, int64_t first, int64_t count);
+  void fp64_advect_stage_range(const double* phin, const double* ddq, const double* ddm, const double* vn, double dt, double* out,
+                               const double* avg_with, int64_t first, int64_t count);
   void fp64_prep_range(const double* phi0, const double* dd0, int os, double limit_high, double limit_low, int64_t first, int64_t count);
   void fp64_stage_range(int os, const double* phi0, const double* phin, const double* dd, double* out, const double* avg_with,
                         int64_t first, int64_t count);

@@ -302,6 +302,56 @@ def reinitialize_sharded(part: MortonPartition, rank: int, phi, backend, exchang
     return phi
 
 
+def advect_schedule(given_dd):
+    """The sweeps and ghost updates of advect_in_normal_direction (src/my_p4est_level_set.cpp:656-725) for one rank:
+    second derivatives of phi_n (its quadratic neighbour values read the node's own; the minmod terms read the
+    caller's second derivatives when given, else these, at the neighbours too), the first stage into phi, the
+    second derivatives of that, the second stage averaged with phi_n. Ops: ("dd", src, dst), ("exchange", name,
+    planes), ("clone", src, dst), ("astage", phin, ddq, ddm, velocity, avg_with, out), ("copy", src, dst)."""
+    ddm = "phi_dd" if given_dd else "ddq"
+    dd2 = "phi_dd" if given_dd else "ddq"
+    return [("dd", "phi", "ddq"), ("exchange", ddm, True), ("clone", "phi", "phi_n"),
+            ("astage", "phi_n", "ddq", ddm, "vn", None, "phi"), ("exchange", "phi", False),
+            ("dd", "phi", dd2), ("exchange", dd2, True),
+            ("astage", "phi", dd2, dd2, "vn1", "phi_n", "tmp"), ("copy", "tmp", "phi"), ("exchange", "phi", False)]
+
+
+def run_advect_schedule(ops, backend, arrays, first, count, exchange, dim, dt):
+    """Run a rank's advection schedule: backend sweeps over [first, first + count), exchange(arr, planes) for ghosts."""
+    for op in ops:
+        kind = op[0]
+        if kind == "dd":
+            backend.dd(arrays[op[1]], arrays[op[2]], first, count)
+        elif kind == "exchange":
+            exchange(arrays[op[1]], dim if op[2] else 1)
+        elif kind == "clone":
+            arrays[op[2]] = arrays[op[1]].clone()
+        elif kind == "copy":
+            backend.copy(arrays[op[1]], arrays[op[2]], first, count)
+        else:
+            _, phin, ddq, ddm, vel, avg, out = op
+            backend.advect_stage(arrays[phin], arrays[ddq], arrays[ddm], arrays[vel], dt, arrays[out], arrays[avg] if avg else None,
+                                 first, count)
+
+
+def advect_normal_sharded(part: MortonPartition, rank: int, phi, vn, dt, backend, exchange, vn_np1=None, phi_dd=None):
+    """advect_in_normal_direction(vn[, vn_np1], phi, dt[, phi_dd]) on one rank of a Morton-range split. phi: a
+    full-length float64 tensor whose owned entries hold this rank's values; vn (and vn_np1) valid at the owned
+    range; phi_dd, when given, a (dim * N) tensor that ends holding the second derivatives of the intermediate phi
+    (as the reference overwrites its caller's arrays). Updates phi in place at the owned range and its ghosts."""
+    import torch
+    N = part.N
+    dim = backend.dim
+    exchange(phi, 1)
+    arrays = {"phi": phi, "vn": vn, "vn1": vn_np1 if vn_np1 is not None else vn, "tmp": torch.empty_like(phi),
+              "ddq": torch.zeros(dim * N, dtype=phi.dtype, device=phi.device)}
+    if phi_dd is not None:
+        arrays["phi_dd"] = phi_dd
+    first, count = part.range_of(rank)
+    run_advect_schedule(advect_schedule(phi_dd is not None), backend, arrays, first, count, exchange, dim, dt)
+    return phi
+
+
 def band_linf_sharded(part: MortonPartition, rank: int, a, b, band):
     """max |a - b| over the owned nodes with |b| < band, reduced over the ranks with one all-reduce(max)."""
     import torch
@@ -345,6 +395,10 @@ class ShardBackend:
 
     def copy(self, src, dst, first, count):
         dst[first:first + count] = src[first:first + count]
+
+    def advect_stage(self, phin, ddq, ddm, vn, dt, out, avg_with, first, count):
+        self.L.check(self.L.load().lsg_advect_stage_range_device(self.ls.handle, self._p(phin), self._p(ddq), self._p(ddm), self._p(vn),
+                                                                 float(dt), self._p(out), self._p(avg_with), first, count))
 
 
 class ShardInterpBackend:

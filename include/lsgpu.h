@@ -373,6 +373,14 @@ int lsg_reinit_prep_range_device(lsg_level_set* ls, const double* phi0_dev, cons
                                  double limit_low, int64_t first, int64_t count);
 int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const double* phi0_dev, const double* phin_dev,
                                   const double* phin_dd_dev, double* out_dev, const double* avg_with_dev, int64_t first, int64_t count);
+/* One advect_in_normal_direction_one_iteration sweep (src/my_p4est_level_set.cpp:559-654) over the nodes
+ * [first, first + count) of a rank's Morton range: out = phin - dt vn |grad phin| with the quadratic neighbour
+ * values from phin_dd (phin's second derivatives) and the minmod terms from minmod_dd (the caller's second
+ * derivatives, or phin_dd), or 0.5 (avg_with + that) when avg_with is given (the RK average; may alias out).
+ * Reads the ghosts of phin and minmod_dd. */
+int lsg_advect_stage_range_device(lsg_level_set* ls, const double* phin_dev, const double* phin_dd_dev, const double* minmod_dd_dev,
+                                  const double* vn_dev, double dt, double* out_dev, const double* avg_with_dev, int64_t first,
+                                  int64_t count);
 
 /* The interface-location check that accompanies every mixed-precision result: over the grid edges (a node
  * and a neighbour that its stencil reaches with one node) cut by the reference field b (e.g. the FP64

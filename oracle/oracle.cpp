@@ -761,11 +761,12 @@ void reinitialize(const Ctx& cx, double* phi, int order_space, int order_pseudot
 // advect_in_normal_direction_one_iteration (src/my_p4est_level_set.cpp:559-654)
 template <int D>
 void advect_one_iteration(const Ctx& cx, const double* vn, double dt, const double* dd, const double* phi_n, double* phi_np1,
-                          int nthreads) {
+                          int nthreads, int64_t first = 0, int64_t count = -1) {
   const Qnnn<D>* Q = static_cast<const Qnnn<D>*>(cx.qnnn);
   const int64_t N = cx.N;
+  const int64_t end = count < 0 ? N : first + count;
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
-  for (long long k = 0; k < (long long)N; ++k) {
+  for (long long k = first; k < (long long)end; ++k) {
     const int64_t n = k;
     const Qnnn<D>& q = Q[n];
     double pn_000, pn_nb[6];
@@ -1914,6 +1915,18 @@ int ora_compute_derivatives_range(void* h, const double* f, double* out, int64_t
     if (first < 0 || count < 0 || first + count > cx->N) throw std::runtime_error("node range out of bounds");
     if (cx->dim == 2) compute_derivatives<2>(*cx, f, out, nthreads, first, count);
     else compute_derivatives<3>(*cx, f, out, nthreads, first, count);
+  });
+}
+
+// One advect_in_normal_direction_one_iteration sweep over the nodes [first, first + count) only (the per-rank work of
+// a Morton-range split): phi_np1 = phi_n - dt vn |grad phi_n| there, dd the minmod terms' second derivatives.
+int ora_advect_stage_range(void* h, const double* vn, double dt, const double* dd, const double* phi_n, double* phi_np1, int64_t first,
+                           int64_t count, int nthreads) {
+  return guard([&] {
+    Ctx* cx = static_cast<Ctx*>(h);
+    if (first < 0 || count < 0 || first + count > cx->N) throw std::runtime_error("node range out of bounds");
+    if (cx->dim == 2) advect_one_iteration<2>(*cx, vn, dt, dd, phi_n, phi_np1, nthreads, first, count);
+    else advect_one_iteration<3>(*cx, vn, dt, dd, phi_n, phi_np1, nthreads, first, count);
   });
 }
 

@@ -38,6 +38,7 @@ SIG = {
     "ora_sl_advect_vortex": (_I, [_P, _I64, _DP, _D, _D, _DP, _DP, _I, _DP, _I]),
     "ora_compute_derivatives_range": (_I, [_P, _DP, _DP, _I64, _I64, _I]),
     "ora_reinit_stage_range": (_I, [_P, _DP, _DP, _DP, _D, _D, _DP, _DP, _I64, _I64, _I]),
+    "ora_advect_stage_range": (_I, [_P, _DP, _D, _DP, _DP, _DP, _I64, _I64, _I]),
     "ora_sl_advect2": (_I, [_P, _P, _I64, _DP, _D, _D, _DP, _DP, _DP, _DP, _DP, _DP, _I, _I, _DP, _I]),
     "ora_vortex": (_I, [_I, _I64, _DP, _D, _DP]),
     "ora_first_derivatives": (_I, [_P, _DP, _DP, _I]),
@@ -171,6 +172,13 @@ class OracleGrid:
 
     def advect_in_normal_direction(self, vn, phi, dt, vn_np1=None, phi_dd=None, nthreads=1):
         _chk(load().ora_advect_in_normal_direction(self._h, _dp(vn), _dp(vn_np1), _dp(phi), dt, _dp(phi_dd), nthreads))
+
+    def advect_stage_range(self, vn, dt, dd, phi_n, phi_np1, first, count, nthreads=1):
+        """One normal-advection sweep over the nodes [first, first + count); phi_np1 (N,) updated there."""
+        assert phi_np1.dtype == np.float64 and phi_np1.flags.c_contiguous and phi_np1.size == self.N
+        _chk(load().ora_advect_stage_range(self._h, _dp(np.ascontiguousarray(vn, np.float64)), float(dt),
+                                           _dp(np.ascontiguousarray(dd, np.float64)), _dp(np.ascontiguousarray(phi_n, np.float64)),
+                                           _dp(phi_np1), int(first), int(count), nthreads))
 
     def advect_cfl_dt(self, vn):
         out = C.c_double()

@@ -126,3 +126,65 @@ def test_forwarded_interpolation_lockstep_equals_one_rank(name):
         torch.cuda.synchronize()
         assert np.array_equal(got.cpu().numpy(), ref), (name, method)
         assert len(torch.unique(owner)) == W
+
+
+@pytest.mark.parametrize("name", sorted(GRIDS))
+@pytest.mark.parametrize("world", [1, 3])
+def test_advection_split_lockstep_equals_one_rank(name, world):
+    """advect_in_normal_direction over Morton ranges on the GPU (ShardBackend's node-range sweeps, lsg_advect_stage_
+    range_device), the ranks in lockstep in one process with their ghosts copied between sweeps: the same bits as the
+    single-GPU FP64 advection, with and without the caller's second derivatives and a second velocity."""
+    import torch
+    from casl_p4est_gb300.sharding import advect_schedule, run_advect_schedule
+    build, phi0_of = GRIDS[name]
+    f = build()
+    phi0 = phi0_of(f)
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    ls = G.my_p4est_level_set_t(ngbd)
+    part = MortonPartition(ngbd.get_neighbors(), world)
+    N, D = part.N, f.dim
+    xyz = f.node_xyz()
+    vn = 0.8 * np.sin(4 * xyz[:, 0] + 1.0) * np.cos(3 * xyz[:, 1])
+    vn1 = vn + 0.3 * np.cos(2 * xyz[:, 0])
+    backend = ShardBackend(ls)
+    for given_dd, two in ((False, False), (True, True)):
+        dt = 0.3 * float(f.dxyz_min()[1]) / float(np.max(np.maximum(np.abs(vn), np.abs(vn1))))
+        dd0 = ls.compute_derivatives(phi0).reshape(D, N)
+        ref = phi0.copy()
+        ref_dd = dd0.copy()
+        ls.advect_in_normal_direction(vn, ref, dt, phi_xx=ref_dd if given_dd else None, vn_np1=vn1 if two else None, precision="fp64")
+        ranks = []
+        for r in range(world):
+            first, count = part.range_of(r)
+
+            def mine(a):
+                t = torch.full(a.shape, POISON, dtype=torch.float64)
+                t[..., first:first + count] = torch.from_numpy(np.ascontiguousarray(a[..., first:first + count]))
+                return t.cuda().reshape(-1) if a.ndim > 1 else t.cuda()
+            arrays = {"phi": mine(phi0), "vn": mine(vn), "vn1": mine(vn1 if two else vn),
+                      "tmp": torch.empty(N, dtype=torch.float64, device="cuda"),
+                      "ddq": torch.full((D * N,), POISON, dtype=torch.float64, device="cuda")}
+            if given_dd:
+                arrays["phi_dd"] = mine(dd0)
+            ranks.append((first, count, arrays))
+
+        def exchange_all(name_, planes):
+            for r in range(world):
+                dst = ranks[r][2][name_].view(planes, N)
+                for s, idx in part.recv[r].items():
+                    i = torch.as_tensor(idx, dtype=torch.int64, device="cuda")
+                    dst[:, i] = ranks[s][2][name_].view(planes, N)[:, i]
+
+        exchange_all("phi", 1)
+        for op in advect_schedule(given_dd):
+            if op[0] == "exchange":
+                exchange_all(op[1], D if op[2] else 1)
+                continue
+            for first, count, arrays in ranks:
+                run_advect_schedule([op], backend, arrays, first, count, None, D, dt)
+        torch.cuda.synchronize()
+        got = torch.cat([arrays["phi"][first:first + count] for first, count, arrays in ranks]).cpu().numpy()
+        assert np.array_equal(got, ref), (name, world, given_dd, np.max(np.abs(got - ref)))
+        if given_dd:
+            got_dd = torch.cat([arrays["phi_dd"].view(D, N)[:, first:first + count] for first, count, arrays in ranks], dim=1).cpu().numpy()
+            assert np.array_equal(got_dd, ref_dd), (name, world)

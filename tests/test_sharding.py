@@ -105,6 +105,16 @@ class OracleBackend:
     def copy(self, src, dst, first, count):
         dst[first:first + count] = src[first:first + count]
 
+    def advect_stage(self, phin, ddq, ddm, vn, dt, out, avg_with, first, count):
+        # the oracle computes the quadratic neighbour values inline (ddq is what the GPU sweep reads for them)
+        if avg_with is None:
+            self.og.advect_stage_range(vn.numpy(), dt, ddm.numpy(), phin.numpy(), out.numpy(), first, count)
+        else:
+            tmp = np.empty(self.N)
+            self.og.advect_stage_range(vn.numpy(), dt, ddm.numpy(), phin.numpy(), tmp, first, count)
+            a = avg_with.numpy()
+            out.numpy()[first:first + count] = .5 * (a[first:first + count] + tmp[first:first + count])
+
 
 def _grid(name):
     import grids
@@ -343,3 +353,73 @@ def test_leaf_partition_ghosts_cover_every_leaf_corner():
                 assert np.array_equal(idx, lp.recv[s][r])
         owners = lp.owner_of_leaves(np.arange(len(ln)))
         assert np.all(np.diff(owners) >= 0) and owners[0] == 0 and owners[-1] == world - 1
+
+
+# ---- normal advection across a Morton split ---------------------------------------------------------
+from casl_p4est_gb300.sharding import advect_normal_sharded  # noqa: E402
+
+
+def _advect_worker(rank, world, port, name, given_dd, two_velocities, q):
+    import torch
+    import torch.distributed as dist
+    import casl_p4est_gb300 as G
+    import oracle as O
+    from casl_p4est_gb300.sharding import HaloExchange
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f, phi0 = _grid(name)
+        og = O.OracleGrid.from_forest(f)
+        N, d = og.N, f.dim
+        part = MortonPartition(og.qnnn(G.qnnn_dtype(d)), world)
+        first, count = part.range_of(rank)
+        xyz = f.node_xyz()
+        vn = 0.8 * np.sin(4 * xyz[:, 0] + 1.0) * np.cos(3 * xyz[:, 1])
+        vn1 = vn + 0.3 * np.cos(2 * xyz[:, 0]) if two_velocities else None
+        dt = 0.5 * og.advect_cfl_dt(np.abs(vn) if vn1 is None else np.maximum(np.abs(vn), np.abs(vn1)))
+        dd0 = og.compute_derivatives(phi0)
+
+        def mine(a):
+            t = torch.full(a.shape, POISON, dtype=torch.float64)
+            t[..., first:first + count] = torch.from_numpy(np.ascontiguousarray(a[..., first:first + count]))
+            return t
+        phi = mine(phi0)
+        pdd = mine(dd0).reshape(-1) if given_dd else None
+        advect_normal_sharded(part, rank, phi, mine(vn), dt, OracleBackend(og), HaloExchange(part, rank),
+                              vn_np1=None if vn1 is None else mine(vn1), phi_dd=pdd)
+        ref = phi0.copy()
+        ref_dd = dd0.copy()
+        og.advect_in_normal_direction(vn, ref, dt, vn_np1=vn1, phi_dd=ref_dd if given_dd else None)
+        ok = bool(np.array_equal(phi.numpy()[first:first + count], ref[first:first + count]))
+        if given_dd:
+            ok = ok and bool(np.array_equal(pdd.view(d, N).numpy()[:, first:first + count], ref_dd[:, first:first + count]))
+        q.put((rank, ok, float(np.max(np.abs(phi.numpy()[first:first + count] - ref[first:first + count])))))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name,given_dd,two", [("circle2d", False, False), ("flower3d", True, True), ("brick3d", False, True),
+                                               ("brick2d", True, False)])
+def test_advection_split_on_gloo_world2_equals_one_rank(name, given_dd, two):
+    """advect_in_normal_direction split into Morton ranges on two CPU ranks (the oracle's node-range sweeps, ghosts of
+    phi and of the second derivatives exchanged after every sweep): the owned values, and the caller's second
+    derivatives when given, equal the single-rank result bit for bit."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_advect_worker, args=(r, 2, port, name, given_dd, two, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ok, diff in res:
+        assert ok, (rank, diff)
+
+
+def test_advect_schedule_follows_the_reference():
+    kinds = [o[0] for o in __import__("casl_p4est_gb300.sharding", fromlist=["advect_schedule"]).advect_schedule(False)]
+    assert kinds == ["dd", "exchange", "clone", "astage", "exchange", "dd", "exchange", "astage", "copy", "exchange"]
