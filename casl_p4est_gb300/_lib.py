@@ -114,6 +114,11 @@ SIGNATURES = {
     "lsg_reinit_prep_range_device": (_I, [_P, _P, _P, _I, _D, _D, _I64, _I64]),
     "lsg_reinit_stage_range_device": (_I, [_P, _I, _P, _P, _P, _P, _P, _I64, _I64]),
     "lsg_advect_stage_range_device": (_I, [_P, _P, _P, _P, _P, _D, _P, _P, _I64, _I64]),
+    "lsg_mixed_split_begin_device": (_I, [_P, _P, _P, _I, _D, _D]),
+    "lsg_mixed_split_stage_device": (_I, [_P, _I, _I]),
+    "lsg_mixed_split_field_device": (_I, [_P, _I, C.POINTER(C.c_void_p)]),
+    "lsg_mixed_split_slots_device": (_I, [_P, _P]),
+    "lsg_mixed_split_end_device": (_I, [_P, _P]),
     "lsg_interface_location_error_device": (_I, [_P, _P, _P, _DP, C.POINTER(_I64), C.POINTER(_I64)]),
     "lsg_band_linf_device": (_I, [_P, _P, _P, _D, _DP, C.POINTER(_I64)]),
     "lsg_batch_create": (_I, [_I, C.POINTER(_P), C.POINTER(_P)]),

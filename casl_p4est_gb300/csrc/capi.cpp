@@ -1236,6 +1236,50 @@ int lsg_advect_stage_range_device(lsg_level_set* ls, const double* phin_dev, con
   });
 }
 
+int lsg_mixed_split_begin_device(lsg_level_set* ls, const double* phi_dev, const double* mask_dev, int order_space, double limit_high,
+                                 double limit_low) {
+  return guard([&] {
+    need(phi_dev != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) { L.mixed_split_begin(phi_dev, order_space, limit_high, limit_low, mask_dev); });
+  });
+}
+
+int lsg_mixed_split_stage_device(lsg_level_set* ls, int order_space, int stage) {
+  return guard([&] {
+    need(order_space == 1 || order_space == 2, "the order in space is 1 or 2");
+    need(stage == 0 || stage == 1, "stage is 0 or 1");
+    with_ls(ls, [&](auto& L) { L.mixed_step(order_space, stage); });
+  });
+}
+
+int lsg_mixed_split_field_device(lsg_level_set* ls, int which, float** field_dev) {
+  return guard([&] {
+    need(field_dev != nullptr && (which == 0 || which == 1), "which is 0 or 1, field_dev not null");
+    with_ls(ls, [&](auto& L) {
+      float* p = L.mixed_field(which);
+      if (!p) throw StateError("mixed split: call lsg_mixed_split_begin_device first");
+      *field_dev = p;
+    });
+  });
+}
+
+int lsg_mixed_split_slots_device(lsg_level_set* ls, int32_t* slots_dev) {
+  return guard([&] {
+    need(slots_dev != nullptr, "null output");
+    with_ls(ls, [&](auto& L) { L.mixed_slots(slots_dev); });
+  });
+}
+
+int lsg_mixed_split_end_device(lsg_level_set* ls, double* phi_dev) {
+  return guard([&] {
+    need(phi_dev != nullptr, "null phi");
+    with_ls(ls, [&](auto& L) {
+      if (!L.mixed_field(0)) throw StateError("mixed split: call lsg_mixed_split_begin_device first");
+      L.mixed_end(phi_dev);
+    });
+  });
+}
+
 int lsg_interface_location_error_device(lsg_level_set* ls, const double* a_dev, const double* b_dev, double* out, int64_t* edges,
                                         int64_t* mismatched) {
   return guard([&] {

@@ -721,6 +721,31 @@ void LevelSet<D>::mixed_join() {
 template <int D>
 void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo, int iters, const double* mask) {
   if (iters == 0) return;  // phi unchanged, as with no iteration in FP64
+  mixed_begin(phi, os, hi, lo, mask);
+  for (int it = 0; it < iters; ++it) {
+    mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
+    if (ot > 1) {
+      mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
+    } else {
+      std::swap(f_phi.p, f_phi1.p);
+    }
+  }
+  mixed_end(phi);
+}
+
+template <int D>
+void LevelSet<D>::mixed_split_begin(const double* phi, int os, double limit_high, double limit_low, const double* mask) {
+  if (os < 1 || os > 2) throw std::invalid_argument("mixed preparation: the order in space is 1 or 2");
+  if (!(limit_high > limit_low)) throw std::invalid_argument("mixed preparation: limit_high must exceed limit_low");
+  const double big = largest_dbl_smaller_than_dbl_max();
+  const double lo = (limit_low < -big ? -DBL_MAX : limit_low - max2(zdt, EPS * fabs(limit_low)));
+  const double hi = (limit_high > big ? DBL_MAX : limit_high + max2(zdt, EPS * fabs(limit_high)));
+  mixed_begin(phi, os, hi, lo, mask);
+}
+
+// The phi_0-only FP64 step of the mixed path and phi_n in FP32 device order (hi, lo: the widened limits).
+template <int D>
+void LevelSet<D>::mixed_begin(const double* phi, int os, double hi, double lo, const double* mask) {
   mixed_join();  // chains left open by a call that stopped on an error
   build_mixed();
   f_phi.alloc(N);
@@ -735,18 +760,33 @@ void LevelSet<D>::reinit_mixed(double* phi, int os, int ot, double hi, double lo
   timer.launches += 3;  // the FP64 subcell step is four kernels
   if (mask) LSG_LAUNCH(K_PREP_MIXED, launch_apply_mask(mask, perm.p, status.p, N, stream));
   LSG_LAUNCH(K_CONVERT, launch_gather_f32(phi, perm.p, f_phi.p, N, 0, 0, 1, stream));
-  for (int it = 0; it < iters; ++it) {
-    mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
-    if (ot > 1) {
-      mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
-    } else {
-      std::swap(f_phi.p, f_phi1.p);
-    }
-  }
+}
+
+// phi (FP64, node order) from the FP32 phi_n of the last stage; ends the chains
+template <int D>
+void LevelSet<D>::mixed_end(double* phi) {
   mixed_join();
   LSG_LAUNCH(K_CONVERT, launch_scatter_f64(f_phi.p, perm.p, status.p, phi, N, 0, 0, 1, stream));
   cuda_check(cudaGetLastError(), "reinitialize (mixed)");
   if (cfg.depth == 3 || cfg.depth == 4) check_device_waits();
+}
+
+// One RK stage of the mixed path for a caller that updates ghosts between stages (a rank of a Morton split):
+// stage 0 phi_n -> phi_1, stage 1 phi_1 -> phi_n averaged with phi_n; the object's stream has the stage's kernels
+// behind it on return (both chains joined), so a ghost update issued on that stream follows them.
+template <int D>
+void LevelSet<D>::mixed_step(int os, int stage) {
+  if (!f_phi.p || !f_phi1.p || !status.p) throw std::invalid_argument("mixed stage: call the mixed preparation first");
+  if (stage == 0) mixed_stage(os, f_phi.p, f_phi1.p, nullptr);
+  else mixed_stage(os, f_phi1.p, f_phi.p, f_phi.p);
+  mixed_join();
+  cuda_check(cudaGetLastError(), "mixed stage");
+}
+
+template <int D>
+void LevelSet<D>::mixed_slots(int32_t* out_dev) {
+  build_mixed();
+  cuda_check(cudaMemcpyAsync(out_dev, iperm.p, (size_t)N * sizeof(int32_t), cudaMemcpyDeviceToDevice, stream), "copy node slots");
 }
 
 template <int D>

@@ -160,6 +160,14 @@ struct LevelSet {
   // current with its halo exchange. prep: status and subcell distances from phi_0 (kept in this object)
   // with the caller's phi_0 limits; stage: out = stage(phin) or 0.5 (avg_with + stage(phin)).
   void fp64_dd_range(const double* f, double* dd, int64_t first, int64_t count);
+  // a rank's mixed reinitialisation with ghost updates between its stages (Morton split): the phi_0-only step
+  // (limits as reinitialize_within_range_of_phi_0 takes them; mask == 0 leaves a node out of the updates), one RK
+  // stage, the FP32 phi_n (0) or phi_1 (1) in device slot order, the slot of every node, and phi back in FP64
+  void mixed_split_begin(const double* phi, int os, double limit_high, double limit_low, const double* mask);
+  void mixed_step(int os, int stage);
+  float* mixed_field(int which) { return which == 0 ? f_phi.p : f_phi1.p; }
+  void mixed_slots(int32_t* out_dev);
+  void mixed_end(double* phi);
   void fp64_advect_stage_range(const double* phin, const double* ddq, const double* ddm, const double* vn, double dt, double* out,
                                const double* avg_with, int64_t first, int64_t count);
   void fp64_prep_range(const double* phi0, const double* dd0, int os, double limit_high, double limit_low, int64_t first, int64_t count);
@@ -258,6 +266,7 @@ struct LevelSet {
   void init_stream();
   void reinit_fp64(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
   void reinit_mixed(double* phi, int os, int ot, double lim_hi, double lim_lo, int iters, const double* mask = nullptr);
+  void mixed_begin(const double* phi, int os, double lim_hi, double lim_lo, const double* mask);
   void advect_mixed(const double* vn, const double* vn_np1, double* phi, double dt, double* phi_dd);
   // one RK stage on the mixed tables: the reinitialisation, or with adv_vn the normal advection
   void mixed_stage(int os, const float* phin, float* out, const float* avg_with, const float* adv_vn = nullptr, float adv_dt = 0.0f);

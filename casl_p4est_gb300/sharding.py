@@ -53,12 +53,13 @@ class MortonPartition:
     """Contiguous node ranges of equal size and the ghost lists of every rank.
 
     records: the node-neighbour records (qnnn_dtype, node order) of the whole grid; the stencil of a node is
-    the set of nodes its record names. ghosts[r]: the nodes outside rank r's range that its stencils reach;
-    recv[r][s] = send[s][r]: those of them rank s owns (sorted)."""
+    the set of nodes its record names. ghosts[r]: the nodes outside rank r's range that its stencils reach
+    (rings=2: also the nodes the stencils of those reach, which the mixed path reads: second neighbours and the
+    stencils of the neighbours' second derivatives); recv[r][s] = send[s][r]: those of them rank s owns (sorted)."""
 
-    def __init__(self, records, world):
-        if world < 1:
-            raise ValueError("world must be >= 1")
+    def __init__(self, records, world, rings=1):
+        if world < 1 or rings not in (1, 2):
+            raise ValueError("world must be >= 1 and rings 1 or 2")
         N = len(records)
         self.N = N
         self.world = world
@@ -69,6 +70,9 @@ class MortonPartition:
             b, e = self.bounds[r], self.bounds[r + 1]
             ref = np.unique(nb[b:e].ravel())
             ref = ref[ref >= 0]
+            if rings == 2:
+                ref = np.unique(np.concatenate([ref, nb[ref].ravel()]))
+                ref = ref[ref >= 0]
             g = ref[(ref < b) | (ref >= e)]
             self.ghosts.append(g)
             owner = np.searchsorted(self.bounds, g, side="right") - 1
@@ -210,14 +214,17 @@ class HaloExchange:
     go to peer, the values at recv[rank][peer] come from peer. Arrays are 1-D tensors of planes * N values
     (host tensors with gloo, CUDA tensors with NCCL)."""
 
-    def __init__(self, part: MortonPartition, rank: int, device=None):
+    def __init__(self, part: MortonPartition, rank: int, device=None, slots=None):
+        """slots: the slot of every node when the arrays are in another order (the mixed path's device order)."""
         import torch
         self.part = part
         self.rank = rank
         self.N = part.N
         dev = device if device is not None else "cpu"
-        self.send_idx = {p: torch.as_tensor(v, dtype=torch.int64, device=dev) for p, v in part.send[rank].items()}
-        self.recv_idx = {p: torch.as_tensor(v, dtype=torch.int64, device=dev) for p, v in part.recv[rank].items()}
+        s = None if slots is None else np.asarray(slots.cpu() if hasattr(slots, "cpu") else slots)
+        remap = (lambda v: v) if s is None else (lambda v: s[v])
+        self.send_idx = {p: torch.as_tensor(remap(v), dtype=torch.int64, device=dev) for p, v in part.send[rank].items()}
+        self.recv_idx = {p: torch.as_tensor(remap(v), dtype=torch.int64, device=dev) for p, v in part.recv[rank].items()}
 
     def __call__(self, arr, planes=1):
         import torch
@@ -439,3 +446,69 @@ class ShardInterpBackend:
                                                                     self._p(None if method == 0 else Fdd.contiguous()), int(method),
                                                                     self._p(out)))
         return out
+
+
+class ShardMixedBackend:
+    """A rank's mixed-precision reinitialisation on its GPU, stage by stage (lsg_mixed_split_*_device): the level
+    set keeps every node and leaves the ones the rank does not own out of the updates (mask 0)."""
+
+    def __init__(self, ls):
+        import torch
+        from . import _lib as L
+        self.L = L
+        self.ls = ls
+        self.N = ls.num_nodes
+        ls.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    def begin(self, phi, mask, order_space, limit_high, limit_low):
+        import ctypes as C
+        self.L.check(self.L.load().lsg_mixed_split_begin_device(self.ls.handle, C.c_void_p(phi.data_ptr()), C.c_void_p(mask.data_ptr()),
+                                                                int(order_space), float(limit_high), float(limit_low)))
+
+    def stage(self, order_space, stage):
+        self.L.check(self.L.load().lsg_mixed_split_stage_device(self.ls.handle, int(order_space), int(stage)))
+
+    def field(self, which):
+        """The FP32 phi_n (0) or phi_1 (1) of the level set, N values in slot order, as a tensor over its memory."""
+        import ctypes as C
+        import torch
+        p = C.c_void_p()
+        self.L.check(self.L.load().lsg_mixed_split_field_device(self.ls.handle, int(which), C.byref(p)))
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (self.N,), "typestr": "<f4", "data": (p.value, False), "version": 3}
+        return torch.as_tensor(_View(), device="cuda")
+
+    def slots(self):
+        import ctypes as C
+        import torch
+        out = torch.empty(self.N, dtype=torch.int32, device="cuda")
+        self.L.check(self.L.load().lsg_mixed_split_slots_device(self.ls.handle, C.c_void_p(out.data_ptr())))
+        return out
+
+    def end(self, phi):
+        import ctypes as C
+        self.L.check(self.L.load().lsg_mixed_split_end_device(self.ls.handle, C.c_void_p(phi.data_ptr())))
+
+
+def reinitialize_mixed_sharded(part: MortonPartition, rank: int, phi, backend, exchange, exchange32, iterations=50, order_space=2,
+                               limit_high=np.finfo(np.float64).max, limit_low=-np.finfo(np.float64).max):
+    """The mixed-precision reinitialize_within_range_of_phi_0 (second order in pseudo-time) on one rank of a Morton
+    split with two rings of ghosts (MortonPartition(..., rings=2)): phi's ghosts are updated once (exchange, node
+    order), the rank's level set prepares every node and leaves the ones it does not own out of the updates, and
+    after every stage the FP32 field's ghosts are updated (exchange32, slot order: HaloExchange(..., slots=)).
+    Updates phi (full-length float64 CUDA tensor) at the owned range."""
+    import torch
+    first, count = part.range_of(rank)
+    exchange(phi, 1)
+    mask = torch.zeros_like(phi)
+    mask[first:first + count] = 1.0
+    backend.begin(phi, mask, order_space, limit_high, limit_low)
+    f0, f1 = backend.field(0), backend.field(1)
+    for _ in range(iterations):
+        backend.stage(order_space, 0)
+        exchange32(f1, 1)
+        backend.stage(order_space, 1)
+        exchange32(f0, 1)
+    backend.end(phi)
+    return phi

@@ -381,6 +381,23 @@ int lsg_reinit_stage_range_device(lsg_level_set* ls, int order_space, const doub
 int lsg_advect_stage_range_device(lsg_level_set* ls, const double* phin_dev, const double* phin_dd_dev, const double* minmod_dd_dev,
                                   const double* vn_dev, double dt, double* out_dev, const double* avg_with_dev, int64_t first,
                                   int64_t count);
+/* The mixed-precision reinitialisation of one rank of a Morton split, stage by stage, so that the caller updates
+ * ghosts between stages (the mixed tables order nodes by stencil type, so a rank keeps every node and leaves the
+ * ones it does not own out of the updates):
+ * lsg_mixed_split_begin_device: the phi_0-only FP64 step and phi_n in FP32 (phi_dev: N values, node order, valid
+ * at the owned nodes and two rings of ghosts; mask_dev: N values, 0 leaves a node out of the updates, e.g. every
+ * node the rank does not own; limits as lsg_reinitialize takes them);
+ * lsg_mixed_split_stage_device: one RK stage, second order in time (stage 0: phi_n -> phi_1; stage 1: phi_1 ->
+ * phi_n averaged with phi_n), all of it ordered before later work on the level set's stream;
+ * lsg_mixed_split_field_device: the device address of the FP32 phi_n (which 0) or phi_1 (1), N values in slot
+ * order, for the ghost update; lsg_mixed_split_slots_device: slot of every node (N int32, device);
+ * lsg_mixed_split_end_device: phi (FP64, node order) from the last phi_n. */
+int lsg_mixed_split_begin_device(lsg_level_set* ls, const double* phi_dev, const double* mask_dev, int order_space, double limit_high,
+                                 double limit_low);
+int lsg_mixed_split_stage_device(lsg_level_set* ls, int order_space, int stage);
+int lsg_mixed_split_field_device(lsg_level_set* ls, int which, float** field_dev);
+int lsg_mixed_split_slots_device(lsg_level_set* ls, int32_t* slots_dev);
+int lsg_mixed_split_end_device(lsg_level_set* ls, double* phi_dev);
 
 /* The interface-location check that accompanies every mixed-precision result: over the grid edges (a node
  * and a neighbour that its stencil reaches with one node) cut by the reference field b (e.g. the FP64

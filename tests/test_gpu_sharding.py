@@ -188,3 +188,57 @@ def test_advection_split_lockstep_equals_one_rank(name, world):
         if given_dd:
             got_dd = torch.cat([arrays["phi_dd"].view(D, N)[:, first:first + count] for first, count, arrays in ranks], dim=1).cpu().numpy()
             assert np.array_equal(got_dd, ref_dd), (name, world)
+
+
+@pytest.mark.parametrize("name", sorted(GRIDS))
+@pytest.mark.parametrize("world", [1, 3])
+def test_mixed_split_lockstep_equals_one_rank(name, world):
+    """The mixed-precision reinitialisation over Morton ranges (two rings of ghosts; ShardMixedBackend: each rank's
+    level set prepares every node, leaves the ones it does not own out of the updates, and runs stage by stage), the
+    ranks in lockstep in one process with the FP32 field's ghosts copied after every stage: the owned values equal
+    the single-GPU mixed result bit for bit."""
+    import torch
+    from casl_p4est_gb300.sharding import ShardMixedBackend
+    build, phi0_of = GRIDS[name]
+    f = build()
+    phi0 = phi0_of(f)
+    ngbd = G.my_p4est_node_neighbors_t(f)
+    part = MortonPartition(ngbd.get_neighbors(), world, rings=2)
+    N = part.N
+    iters = 6
+    ref = phi0.copy()
+    G.my_p4est_level_set_t(ngbd, precision="mixed").reinitialize_2nd_order(ref, iters)
+    backends, phis = [], []
+    for r in range(world):
+        first, count = part.range_of(r)
+        keep = np.zeros(N, bool)
+        keep[first:first + count] = True
+        keep[part.ghosts[r]] = True
+        phi = torch.from_numpy(np.where(keep, phi0, POISON)).cuda()
+        mask = torch.zeros(N, dtype=torch.float64, device="cuda")
+        mask[first:first + count] = 1.0
+        b = ShardMixedBackend(G.my_p4est_level_set_t(G.my_p4est_node_neighbors_t(f), precision="mixed"))
+        b.begin(phi, mask, 2, np.finfo(np.float64).max, -np.finfo(np.float64).max)
+        backends.append(b)
+        phis.append(phi)
+    fields = [(b.field(0), b.field(1)) for b in backends]
+    slots = backends[0].slots().long().cpu().numpy()
+
+    def exchange_all(which):
+        for r in range(world):
+            for s, idx in part.recv[r].items():
+                sl = torch.as_tensor(slots[idx], dtype=torch.int64, device="cuda")
+                fields[r][which][sl] = fields[s][which][sl]
+
+    for _ in range(iters):
+        for b in backends:
+            b.stage(2, 0)
+        exchange_all(1)
+        for b in backends:
+            b.stage(2, 1)
+        exchange_all(0)
+    for b, phi in zip(backends, phis):
+        b.end(phi)
+    torch.cuda.synchronize()
+    got = np.concatenate([phis[r].cpu().numpy()[part.bounds[r]:part.bounds[r + 1]] for r in range(world)])
+    assert np.array_equal(got, ref), (name, world, np.max(np.abs(got - ref)))

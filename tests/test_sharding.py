@@ -423,3 +423,25 @@ def test_advection_split_on_gloo_world2_equals_one_rank(name, given_dd, two):
 def test_advect_schedule_follows_the_reference():
     kinds = [o[0] for o in __import__("casl_p4est_gb300.sharding", fromlist=["advect_schedule"]).advect_schedule(False)]
     assert kinds == ["dd", "exchange", "clone", "astage", "exchange", "dd", "exchange", "astage", "copy", "exchange"]
+
+
+def test_two_ring_partition_covers_second_neighbours():
+    import casl_p4est_gb300 as G
+    import oracle as O
+    f, _ = _grid("flower3d")
+    og = O.OracleGrid.from_forest(f)
+    rec = og.qnnn(G.qnnn_dtype(3))
+    nb = rec["nb"].reshape(og.N, -1)
+    for world in (2, 3):
+        p1 = MortonPartition(rec, world)
+        p2 = MortonPartition(rec, world, rings=2)
+        for r in range(world):
+            b, e = p2.bounds[r], p2.bounds[r + 1]
+            ring1 = np.unique(nb[b:e].ravel())
+            ring1 = ring1[ring1 >= 0]
+            ring2 = np.unique(nb[ring1].ravel())
+            need = set(ring2[ring2 >= 0].tolist()) - set(range(b, e))
+            assert need == set(p2.ghosts[r].tolist())
+            assert set(p1.ghosts[r].tolist()) <= set(p2.ghosts[r].tolist())
+            for s, idx in p2.send[r].items():
+                assert np.array_equal(idx, p2.recv[s][r])
