@@ -26,7 +26,7 @@ using namespace st64;
 constexpr int TPB = 256;
 
 template <int D>
-__global__ void __launch_bounds__(TPB, 6) k_dd64(DTab64<D> T, const double* __restrict__ f, double* __restrict__ dd, int64_t first,
+__global__ void __launch_bounds__(TPB, 8) k_dd64(DTab64<D> T, const double* __restrict__ f, double* __restrict__ dd, int64_t first,
                                               int64_t last) {
   const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= last) return;
@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(TPB) k_reinit_prep64(DTab64<D> T, const double
 // word and the exponent arithmetic had taken most of the FP64 work off the pipe, the kernel waited on its loads, and
 // more resident warps hide them better (per launch on 13.7M nodes, all axes at once: 2 blocks 3.46 ms, 3 blocks
 // 2.75, 4 blocks 2.33, 5 blocks 2.20, 6 blocks 2.21; one axis at a time, fewer values live: 5 blocks 2.18, 6 blocks
-// 2.16). The second-derivative sweep runs at six blocks (40 registers) and the advection stage at five for the same
-// reason.
+// 2.16). The second-derivative sweep runs at eight blocks (32 registers: 0.79 ms at five, 0.71 at six, 0.67 at
+// eight) and the advection stage at six (20 steps on 122M nodes: 866 ms at five, 848 at six) for the same reason.
 template <int D, int ORDER_SPACE, bool AVG>
 __global__ void __launch_bounds__(TPB, 6) k_reinit_stage64(DTab64<D> T, const uint16_t* __restrict__ status, const double* __restrict__ s_near,
                                                         const double* __restrict__ phi0, const double* __restrict__ phin,
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(TPB, 6) k_reinit_stage64(DTab64<D> T, const ui
 }
 
 template <int D, bool AVG>
-__global__ void __launch_bounds__(TPB, 5) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
+__global__ void __launch_bounds__(TPB, 6) k_advect_stage64(DTab64<D> T, const double* __restrict__ phin, const double* __restrict__ ddq,
                                                         const double* __restrict__ ddm, const double* __restrict__ vn, double dt,
                                                         double* out, const double* avg_with, int64_t first, int64_t last) {
   const int64_t n = first + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
