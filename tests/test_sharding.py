@@ -445,3 +445,48 @@ def test_two_ring_partition_covers_second_neighbours():
             assert set(p1.ghosts[r].tolist()) <= set(p2.ghosts[r].tolist())
             for s, idx in p2.send[r].items():
                 assert np.array_equal(idx, p2.recv[s][r])
+
+
+def _slots_worker(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    import casl_p4est_gb300 as G
+    import oracle as O
+    from casl_p4est_gb300.sharding import HaloExchange
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f, _ = _grid("flower3d")
+        og = O.OracleGrid.from_forest(f)
+        part = MortonPartition(og.qnnn(G.qnnn_dtype(3)), world, rings=2)
+        N = part.N
+        slots = np.random.default_rng(9).permutation(N).astype(np.int32)  # node -> slot, the same on every rank
+        truth = np.arange(N, dtype=np.float32) * 0.5 + 1.0  # a value per node
+        first, count = part.range_of(rank)
+        arr = torch.full((N,), -7.0, dtype=torch.float32)  # slot order; only this rank's nodes known
+        owned = np.arange(first, first + count)
+        arr[torch.as_tensor(slots[owned], dtype=torch.int64)] = torch.from_numpy(truth[owned])
+        HaloExchange(part, rank, slots=slots)(arr, 1)
+        g = part.ghosts[rank]
+        ok = bool(np.array_equal(arr.numpy()[slots[g]], truth[g])) and bool(np.array_equal(arr.numpy()[slots[owned]], truth[owned]))
+        q.put((rank, ok))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_slot_ordered_ghost_exchange_on_gloo_world2():
+    """The mixed split's ghost update runs on arrays in the level set's slot order (HaloExchange(..., slots=)): on two
+    CPU ranks every ghost slot receives its owner's value and no owned slot changes."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_slots_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert all(ok for _, ok in res), res
