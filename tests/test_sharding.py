@@ -490,3 +490,52 @@ def test_slot_ordered_ghost_exchange_on_gloo_world2():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert all(ok for _, ok in res), res
+
+
+def _empty_share_worker(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    import casl_p4est_gb300 as G
+    import oracle as O
+    from casl_p4est_gb300.sharding import HaloExchange
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        f, _ = _grid("circle2d")
+        og = O.OracleGrid.from_forest(f)
+        npart = MortonPartition(og.qnnn(G.qnnn_dtype(2)), world)
+        lpart = LeafPartition(f.local_nodes(), npart.bounds, world)
+        b, e = npart.bounds[rank], npart.bounds[rank + 1]
+        phi, phi_dd, _, _ = _fields(f, og)
+        F = torch.full((1, og.N), POISON, dtype=torch.float64)
+        F[0, b:e] = torch.from_numpy(phi[b:e])
+        Fdd = torch.full((1, 2, og.N), POISON, dtype=torch.float64)
+        Fdd[0, :, b:e] = torch.from_numpy(phi_dd[:, b:e])
+        ex = HaloExchange(lpart, rank)
+        ex(F.view(-1), 1)
+        ex(Fdd.view(-1), 2)
+        pts_all = _query_points(f, 500, 3)
+        mine = pts_all if rank == 0 else pts_all[:0]  # rank 1 asks for nothing but serves rank 0's remote points
+        got = interpolate_sharded(lpart, rank, torch.from_numpy(mine), OracleInterp(og), 4, F, Fdd)
+        ref = og.interpolate(4, phi.reshape(1, -1), mine, phi_dd.reshape(1, 2, -1)) if len(mine) else np.empty((1, 0))
+        q.put((rank, tuple(got.shape), bool(np.array_equal(got.numpy(), ref))))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_forwarded_interpolation_with_a_rank_asking_nothing():
+    """A rank with no points of its own still answers the points forwarded to it, and gets a (nf, 0) result."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_empty_share_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res[0][1] == (1, 500) and res[0][2], res
+    assert res[1][1] == (1, 0) and res[1][2], res
